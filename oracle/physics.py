@@ -1,0 +1,68 @@
+"""Excitation, extinction cross section, its adjoint gradient and Mie theory.
+FP64 restatement / published methods (test infrastructure only).
+
+* PlaneWavePointWise: src/src_vie/src_fields/src_excitations/PlaneWavePointWise.m:7-19.
+* C_ext: absent from the reference (README.md:35 lists far-field routines as a
+  to-do); Draine & Flatau, JOSA A 11 (1994) 1491, eq. (8):
+  C_ext = 4 pi k / |E0|^2 sum_j Im(E_inc,j^* . p_j), with p_j = dV * P_j because the
+  reference's unknown is the dipole moment per unit volume (main_DDA.m:75,139-140).
+* Gradient: adjoint method on A(eps) P = E_inc with A = diag(1/alpha_LDR(eps)) - dV*G;
+  A is complex symmetric, so the adjoint system is A^T lam = conj(E_inc).
+* Mie: Bohren & Huffman (1983) BHMIE series for the extinction efficiency.
+"""
+import numpy as np
+
+from .operators import alpha_ldr, dalpha_inv_deps
+
+
+def PlaneWavePointWise(Eo, kvec, r):
+    """Einc(L,M,N,3) = Eo * exp(i k.r), PlaneWavePointWise.m:7-19."""
+    r = np.asarray(r, dtype=float)
+    kr = kvec[0] * r[..., 0] + kvec[1] * r[..., 1] + kvec[2] * r[..., 2]
+    e = np.exp(1j * kr)
+    return np.stack([Eo[0] * e, Eo[1] * e, Eo[2] * e], axis=-1)
+
+
+def cext_dda(P, Einc, ko, dV, Eo):
+    """Extinction cross section from the polarisation P (3*nnz, idx3 order) and
+    the incident field at the same entries."""
+    return 4.0 * np.pi * ko * dV * np.sum(np.imag(np.conj(Einc) * P)) / np.sum(np.abs(np.asarray(Eo)) ** 2)
+
+
+def cext_grad_dda(P, lam, eps_vox, ko, d, kvec, Eo):
+    """dC_ext/dRe(eps) and dC_ext/dIm(eps) per voxel, given the forward solution P
+    and the adjoint solution lam of A^T lam = conj(E_inc) (both 3*nnz, idx3 order)."""
+    nnz = len(eps_vox)
+    dV = d ** 3
+    c = 4.0 * np.pi * ko * dV / np.sum(np.abs(np.asarray(Eo)) ** 2)
+    lp = (lam * P).reshape(3, nnz).sum(axis=0)
+    g = dalpha_inv_deps(eps_vox, ko, d, kvec, Eo) * lp
+    return -c * np.imag(g), -c * np.real(g)
+
+
+def mie_qext(x, m, nstop=None):
+    """Extinction efficiency of a homogeneous sphere, size parameter x, relative
+    index m (BHMIE recurrences, Bohren & Huffman 1983, appendix A)."""
+    m = complex(m)
+    if nstop is None:
+        nstop = int(np.ceil(x + 4.05 * x ** (1.0 / 3.0) + 2.0))
+    y = m * x
+    nmx = int(max(nstop, abs(y)) + 15)
+    D = np.zeros(nmx + 1, dtype=complex)
+    for n in range(nmx, 0, -1):
+        D[n - 1] = n / y - 1.0 / (D[n] + n / y)
+    psi0, psi1 = np.cos(x), np.sin(x)
+    chi0, chi1 = -np.sin(x), np.cos(x)
+    xi1 = complex(psi1, -chi1)
+    q = 0.0
+    for n in range(1, nstop + 1):
+        psi = (2.0 * n - 1.0) * psi1 / x - psi0
+        chi = (2.0 * n - 1.0) * chi1 / x - chi0
+        xi = complex(psi, -chi)
+        an = ((D[n] / m + n / x) * psi - psi1) / ((D[n] / m + n / x) * xi - xi1)
+        bn = ((D[n] * m + n / x) * psi - psi1) / ((D[n] * m + n / x) * xi - xi1)
+        q += (2.0 * n + 1.0) * (an.real + bn.real)
+        psi0, psi1 = psi1, psi
+        chi0, chi1 = chi1, chi
+        xi1 = complex(psi1, -chi1)
+    return 2.0 / x ** 2 * q

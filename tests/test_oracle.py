@@ -1,0 +1,238 @@
+"""The FP64 oracle against independent mathematics (CPU only)."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from oracle.mvp import MVP_plain_transpose
+from voxscatter_gb300 import workloads as W
+from voxscatter_gb300.geometry import geometry
+
+
+def _grid_from_vox(L, M, N, idx, vals):
+    g = np.zeros(L * M * N, dtype=complex)
+    g[idx] = vals
+    return g.reshape((L, M, N), order="F")
+
+
+def _setup(p, nearby="off"):
+    fN, Toep, alpha = O.getOPERATOR_DDA(p["r"], p["ko"], p["refInd"], p["kvec"], p["Eo"], nearby)
+    L, M, N = p["L"], p["M"], p["N"]
+    nD = L * M * N
+    idx = p["idx"]
+    idx3 = np.concatenate([idx, nD + idx, 2 * nD + idx])
+    chi = _grid_from_vox(L, M, N, idx, 1.0)
+    dV = p["d"] ** 3
+    return fN, Toep, alpha, idx3, chi, dV
+
+
+@pytest.mark.parametrize("m", [1.31, 1.31 + 0.05j])
+def test_mvp_matches_dense_direct_sum(m):
+    p = W.small_hex(m=m)
+    fN, Toep, alpha, idx3, chi, dV = _setup(p)
+    L, M, N = p["L"], p["M"], p["N"]
+    A = O.dense_dda_matrix(p["r"], p["idx"], p["ko"], 1 / alpha, dV)
+    A2 = O.dense_from_toeplitz(Toep, p["idx"], 1 / alpha, dV)
+    assert np.abs(A - A2).max() <= 1e-12 * np.abs(A).max()
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=len(idx3)) + 1j * rng.normal(size=len(idx3))
+    y = O.MVP(x, fN, np.ones((L, M, N)), dV * chi, 1 / alpha, "notransp", idx3)
+    yd = A @ x
+    assert np.linalg.norm(y - yd) <= 1e-12 * np.linalg.norm(yd)
+    # reference 'transp' branch is the conjugate transpose for real Gram
+    yt = O.MVP(x, fN, np.ones((L, M, N)), dV * chi, 2.5, "transp", idx3)
+    A_real_gram = O.dense_dda_matrix(p["r"], p["idx"], p["ko"], 2.5, dV)
+    assert np.linalg.norm(yt - A_real_gram.conj().T @ x) <= 1e-12 * np.linalg.norm(yt)
+    # plain transpose of a general (varying-Mc) operator
+    mc = dV * (1 + 0.3 * rng.normal(size=(L, M, N)))
+    ytt = MVP_plain_transpose(x, fN, np.ones((L, M, N)), mc, 1 / alpha, idx3)
+    Amc = O.dense_dda_matrix(p["r"], p["idx"], p["ko"], 1 / alpha, mc)
+    assert np.linalg.norm(ytt - Amc.T @ x) <= 1e-12 * np.linalg.norm(ytt)
+
+
+def test_dda_tensor_symmetry_and_zero_planes():
+    p = W.small_hex()
+    _, Toep, _, _, _, _ = _setup(p)
+    # odd components vanish exactly on their zero-offset planes (used by the
+    # sign bookkeeping of the circulant levels)
+    assert np.all(Toep[0, :, :, 1] == 0) and np.all(Toep[0, :, :, 2] == 0)
+    assert np.all(Toep[:, 0, :, 1] == 0) and np.all(Toep[:, 0, :, 4] == 0)
+    assert np.all(Toep[:, :, 0, 2] == 0) and np.all(Toep[:, :, 0, 4] == 0)
+    assert np.all(Toep[0, 0, 0] == 0)
+
+
+def test_alpha_ldr_limits():
+    # kd -> 0 gives Clausius-Mossotti
+    a = O.alpha_ldr(1.5, 1e-6, 1e-3, [0, 0, 1], [1, 0, 0])
+    assert abs(a - 3 / (4 * math.pi) * (2.25 - 1) / (2.25 + 2)) < 1e-12
+    eps = 2.0 + 0.1j
+    h = 1e-6
+    f = lambda e: 1 / O.alpha_ldr(e, 2.0, 0.1, [0, 0, 1], [1, 0, 0], is_eps=True)
+    fd = (f(eps + h) - f(eps - h)) / (2 * h)
+    assert abs(fd - O.dalpha_inv_deps(eps, 2.0, 0.1, [0, 0, 1], [1, 0, 0])) < 1e-6
+
+
+def _wrapped_average(T, n, axis_block):
+    """Frobenius-optimal circulant of each n x n Toeplitz sub-block."""
+    out = np.zeros_like(T)
+    i = np.arange(n)
+    for k in range(n):
+        mask = ((i[:, None] - i[None, :]) % n) == k
+        avg = T[..., mask].mean(axis=-1)
+        out[..., mask] = avg[..., None]
+    return out
+
+
+def test_circ_levels_match_dense_chan_approximation():
+    p = W.small_hex(m=1.4, nper=3, diameter=1.5)
+    fN, Toep, alpha, idx3, chi, dV = _setup(p)
+    L, M, N = p["L"], p["M"], p["N"]
+    allvox = np.arange(L * M * N)
+    A = O.dense_from_toeplitz(Toep, allvox, 0.0, -1.0)  # = +G on the full grid
+    n3 = 3 * L * M * N
+    # index (x, y, z, c) with x fastest
+    T = A.reshape(3, N, M, L, 3, N, M, L)  # [c,z,y,x, c',z',y',x']
+    T = T.transpose(1, 2, 0, 5, 6, 4, 3, 7)  # [z,y,c,z',y',c',x,x']
+    T1 = _wrapped_average(T, L, None)
+    F = np.fft.fft(np.eye(L))
+    # block for x-frequency i: F T1 F^-1 is diagonal in (x,x')
+    D1 = np.einsum("ia,...ab,bj->...ij", F, T1, np.linalg.inv(F))
+    lev1 = np.diagonal(D1, axis1=-2, axis2=-1)  # [z,y,c,z',y',c',i]
+    lev1 = lev1.transpose(6, 0, 2, 3, 5, 1, 4)  # [i,z,c,z',c',y,y']
+    T2 = _wrapped_average(lev1, M, None)
+    Fm = np.fft.fft(np.eye(M))
+    D2 = np.einsum("ja,...ab,bk->...jk", Fm, T2, np.linalg.inv(Fm))
+    lev2 = np.diagonal(D2, axis1=-2, axis2=-1)  # [i,z,c,z',c',j]
+    blocks_math = lev2.transpose(0, 5, 2, 1, 4, 3).reshape(L, M, 3 * N, 3 * N)  # (c,z) z fastest
+    _, circL = O.circ_1_level(Toep, L, M, N, 0, "off")
+    _, blocks = O.circ_2_level(circL, L, M, N)
+    assert np.abs(blocks - blocks_math).max() <= 1e-10 * np.abs(blocks_math).max()
+
+
+def test_prec_inverts_its_circulant():
+    p = W.small_hex(m=1.4, nper=3, diameter=1.5)
+    fN, Toep, alpha, idx3, chi, dV = _setup(p)
+    L, M, N = p["L"], p["M"], p["N"]
+    _, circL = O.circ_1_level(Toep, L, M, N, 0, "off")
+    _, blocks = O.circ_2_level(circL, L, M, N)
+    inv = O.invert_blocks(blocks, 1 / alpha, dV)
+    # forward 2-level circulant operator applied through FFTs
+    fwd = np.linalg.inv(inv)
+    allidx = np.arange(3 * L * M * N)
+    rng = np.random.default_rng(2)
+    x = rng.normal(size=allidx.size) + 1j * rng.normal(size=allidx.size)
+    y = O.mvp_circ_2_level(fwd, x, L, M, N, allidx)
+    z = O.mvp_circ_2_level(inv, y, L, M, N, allidx)
+    assert np.linalg.norm(z - x) <= 1e-11 * np.linalg.norm(x)
+
+
+def test_circ_1_level_blocks_and_chan_apply():
+    p = W.small_hex(m=1.4, nper=3, diameter=1.5)
+    fN, Toep, alpha, idx3, chi, dV = _setup(p)
+    L, M, N = p["L"], p["M"], p["N"]
+    circ, circL = O.circ_1_level(Toep, L, M, N, 0, "on")
+    assert circ.shape == (L, 3 * M * N, 3 * M * N)
+    inv = np.linalg.inv((1 / alpha) * np.eye(3 * M * N)[None] - dV * circ)
+    allidx = np.arange(3 * L * M * N)
+    x = np.random.default_rng(3).normal(size=allidx.size) + 0j
+    y = O.chan_mvp_idx(inv, x, L, M, N, allidx)
+    z = O.chan_mvp_idx(np.linalg.inv(inv), y, L, M, N, allidx)
+    assert np.linalg.norm(z - x) <= 1e-10 * np.linalg.norm(x)
+
+
+@pytest.mark.parametrize("solver", ["bicgstab", "gmres", "pgmres"])
+@pytest.mark.parametrize("prec", [False, True])
+def test_krylov_solves(solver, prec):
+    p = W.small_hex(m=1.31 + 0.05j)
+    fN, Toep, alpha, idx3, chi, dV = _setup(p)
+    L, M, N = p["L"], p["M"], p["N"]
+    A = lambda v: O.MVP(v, fN, np.ones((L, M, N)), dV * chi, 1 / alpha, "notransp", idx3)
+    Einc = O.PlaneWavePointWise(p["Eo"], p["kvec"], p["r"])
+    b = Einc.ravel(order="F")[idx3]
+    Pm = None
+    if prec:
+        _, circL = O.circ_1_level(Toep, L, M, N, 0, "off")
+        _, blocks = O.circ_2_level(circL, L, M, N)
+        inv = O.invert_blocks(blocks, 1 / alpha, dV)
+        Pm = lambda v: O.mvp_circ_2_level(inv, v, L, M, N, idx3)
+    tol = 1e-8
+    if solver == "bicgstab":
+        x, flag, relres, it, resvec = O.bicgstab(A, b, tol, 500, Pm)
+        assert len(resvec) == int(round(2 * it)) + 1
+    elif solver == "gmres":
+        x, flag, relres, it, resvec = O.gmres(A, b, 200, tol, 1, Pm)
+    else:
+        x, flag, relres, it, resvec = O.pgmres(A, b, 200, tol, 2, Pm)
+    Ad = O.dense_dda_matrix(p["r"], p["idx"], p["ko"], 1 / alpha, dV)
+    xd = np.linalg.solve(Ad, b)
+    assert flag == 0
+    assert np.linalg.norm(x - xd) <= 1e-6 * np.linalg.norm(xd)
+
+
+def test_mie_known_answer():
+    # Bohren & Huffman BHMIE sample case: radius 0.525, wavelength 0.6328, m=1.55
+    x = 2 * math.pi * 0.525 / 0.6328
+    assert abs(O.mie_qext(x, 1.55) - 3.10543) < 2e-5
+
+
+def test_dda_sphere_cext_vs_mie():
+    m = 1.31 + 0.01j
+    sizeParam = 2.0
+    r, idx, res, _, lam_ext, _ = geometry("sphere", m, sizeParam, 14)
+    L, M, N, _ = r.shape
+    ko = 2 * math.pi / lam_ext
+    kvec = np.array([0, 0, ko]); Eo = np.array([1.0, 0, 0])
+    fN, Toep, alpha = O.getOPERATOR_DDA(r, ko, m, kvec, Eo, "off")
+    nD = L * M * N
+    idx3 = np.concatenate([idx, nD + idx, 2 * nD + idx])
+    chi = _grid_from_vox(L, M, N, idx, 1.0)
+    dV = res ** 3
+    A = lambda v: O.MVP(v, fN, np.ones((L, M, N)), dV * chi, 1 / alpha, "notransp", idx3)
+    b = O.PlaneWavePointWise(Eo, kvec, r).ravel(order="F")[idx3]
+    P, flag, *_ = O.bicgstab(A, b, 1e-8, 1000)
+    assert flag == 0
+    cext = O.cext_dda(P, b, ko, dV, Eo)
+    a_eff = (3 * len(idx) * dV / (4 * math.pi)) ** (1 / 3)
+    q = cext / (math.pi * a_eff ** 2)
+    qmie = O.mie_qext(ko * a_eff, m)
+    assert abs(q - qmie) / qmie < 0.05
+
+
+def test_cext_gradient_central_differences():
+    p = W.config4(L=5, M=4, N=3)
+    L, M, N = p["L"], p["M"], p["N"]
+    d, ko = p["d"], p["ko"]
+    idx = p["idx"]
+    nD = L * M * N
+    idx3 = np.concatenate([idx, nD + idx, 2 * nD + idx])
+    Toep = O.green_toeplitz(p["r"], ko)
+    fN = O.fft_operator(O.circulant_nop_const(Toep))
+    dV = d ** 3
+    b = O.PlaneWavePointWise(p["Eo"], p["kvec"], p["r"]).ravel(order="F")[idx3]
+
+    def solve(eps, rhs, transpose=False):
+        ainv = 1 / O.alpha_ldr(eps, ko, d, p["kvec"], p["Eo"], is_eps=True)
+        G = _grid_from_vox(L, M, N, idx, ainv)
+        if transpose:
+            A = lambda v: MVP_plain_transpose(v, fN, np.ones((L, M, N)), dV, G, idx3)
+        else:
+            A = lambda v: O.MVP(v, fN, np.ones((L, M, N)), dV, G, "notransp", idx3)
+        x, flag, *_ = O.bicgstab(A, rhs, 1e-13, 2000)
+        assert flag == 0
+        return x
+
+    eps = p["eps"]
+    P = solve(eps, b)
+    lam = solve(eps, np.conj(b), transpose=True)
+    gre, gim = O.cext_grad_dda(P, lam, eps, ko, d, p["kvec"], p["Eo"])
+    h = 1e-6
+    rng = np.random.default_rng(0)
+    for j in rng.choice(len(idx), 6, replace=False):
+        for step, g in ((h, gre), (1j * h, gim)):
+            ep = eps.copy(); ep[j] += step
+            em = eps.copy(); em[j] -= step
+            cp = O.cext_dda(solve(ep, b), b, ko, dV, p["Eo"])
+            cm = O.cext_dda(solve(em, b), b, ko, dV, p["Eo"])
+            fd = (cp - cm) / (2 * h)
+            assert abs(fd - g[j]) <= 1e-5 * max(abs(g).max(), 1e-30)
