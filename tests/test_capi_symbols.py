@@ -1,0 +1,45 @@
+"""The C-ABI library builds, loads without a GPU and exports every function
+declared in include/voxscatter.h (no compute calls)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    txt = open(os.path.join(ROOT, "include", "voxscatter.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(vs_[A-Za-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from voxscatter_gb300 import build, _lib
+    build.build()
+    return _lib.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = _declared()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_binding_covers_header(lib):
+    from voxscatter_gb300 import _lib
+    assert set(_declared()) == set(_lib.SIGNATURES)
+
+
+def test_no_gpu_fails_loudly(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    from voxscatter_gb300 import _lib
+    h = ctypes.c_void_p()
+    st = lib.vs_ctx_create(0, ctypes.byref(h))
+    assert st != _lib.VS_OK
+    assert lib.vs_last_error(None)

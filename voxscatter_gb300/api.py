@@ -1,0 +1,177 @@
+"""Host-side mirror of the reference's MATLAB interface on libvoxscatter.
+
+Function names, argument order and meaning follow the reference:
+  getOPERATOR_DDA  src/src_vie/src_operators/getOPERATOR_DDA.m:1-2
+  MVP / mv_AN_const src/src_vie/src_mvp/MVP.m:1
+Indices are 0-based (MATLAB idx - 1).  The long-lived objects (Context,
+Operator) are the handle-based fast path; the MATLAB-named functions build
+them per call, as the reference's handles re-pass fN on every call.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+class Context:
+    """A CUDA device + stream owned by libvoxscatter."""
+
+    def __init__(self, device=0):
+        self._lib = L.load()
+        h = C.c_void_p()
+        L.check(self._lib.vs_ctx_create(int(device), C.byref(h)))
+        self.h = h
+        self.device = device
+
+    def synchronize(self):
+        L.check(self._lib.vs_ctx_synchronize(self.h), self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.vs_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _offsets(r):
+    r = np.asarray(r, dtype=float)
+    ox = np.ascontiguousarray(r[:, 0, 0, 0] - r[0, 0, 0, 0])
+    oy = np.ascontiguousarray(r[0, :, 0, 1] - r[0, 0, 0, 1])
+    oz = np.ascontiguousarray(r[0, 0, :, 2] - r[0, 0, 0, 2])
+    return ox, oy, oz
+
+
+def green_dda(r, ko, nearby_quad="off", ctx=None):
+    """Toep (L,M,N,6) on the device in FP64 (getOPERATOR_DDA.m:29-119)."""
+    ctx = ctx or default_context()
+    Lx, My, Nz = np.asarray(r).shape[:3]
+    ox, oy, oz = _offsets(r)
+    out = np.zeros(Lx * My * Nz * 6, dtype=np.complex128)
+    L.check(ctx._lib.vs_green_dda(ctx.h, Lx, My, Nz, L.dptr(ox), L.dptr(oy), L.dptr(oz), float(ko),
+                                  1 if nearby_quad == "on" else 0, L.dptr(out)), ctx.h)
+    return out.reshape((Lx, My, Nz, 6), order="F")
+
+
+def alpha_ldr(m, ko, d, kvec, Eo, is_eps=False):
+    """alpha_LDR (getOPERATOR_DDA.m:7-26), elementwise over m (or eps)."""
+    lib = L.load()
+    arr = np.atleast_1d(np.asarray(m, dtype=np.complex128)).ravel()
+    arr = np.ascontiguousarray(arr)
+    out = np.zeros_like(arr)
+    kv = np.ascontiguousarray(np.asarray(kvec, dtype=float))
+    e0 = np.ascontiguousarray(np.asarray(Eo, dtype=float))
+    L.check(lib.vs_alpha_ldr(L.dptr(arr), arr.size, 1 if is_eps else 0, float(ko), float(d), L.dptr(kv),
+                             L.dptr(e0), L.dptr(out)))
+    return out[0] if np.ndim(m) == 0 else out.reshape(np.shape(m))
+
+
+def circulant_fft(Toep, P=None, Q=None, R=None, ctx=None):
+    """fN = fft_operator(circulant_nop_const(Toep)) for (P,Q,R) = (2L,2M,2N) by default."""
+    ctx = ctx or default_context()
+    Lx, My, Nz = Toep.shape[:3]
+    P = P or 2 * Lx; Q = Q or 2 * My; R = R or 2 * Nz
+    t = L.cplx_flat(Toep)
+    out = np.zeros(P * Q * R * 6, dtype=np.complex128)
+    L.check(ctx._lib.vs_circulant_fft(ctx.h, Lx, My, Nz, L.dptr(t), P, Q, R, L.dptr(out)), ctx.h)
+    return out.reshape((P, Q, R, 6), order="F")
+
+
+def getOPERATOR_DDA(r, ko, refInd, kvec, Eo, nearby_quad="off", ctx=None):
+    """[op_out, Toep, alpha_LDR] = getOPERATOR_DDA(r, ko, refInd, kvec, Eo, nearby_quad)."""
+    r = np.asarray(r, dtype=float)
+    dx = r[1, 0, 0, 0] - r[0, 0, 0, 0]
+    Toep = green_dda(r, ko, nearby_quad, ctx)
+    fN = circulant_fft(Toep, ctx=ctx)
+    return fN, Toep, alpha_ldr(refInd, ko, dx, kvec, Eo)
+
+
+_TRANSP = {"notransp": L.VS_NOTRANSP, "transp": L.VS_CONJTRANSP, "plain_transp": L.VS_TRANSP}
+
+
+class Operator:
+    """Handle on a device operator A x = Gram.*Mr.*x - Mc.*N(x) on idx3."""
+
+    def __init__(self, L_, M_, N_, idx3, Mr=1.0, Mc=1.0, Gram=1.0, toep=None, fN=None, PQR=(0, 0, 0), ctx=None):
+        self.ctx = ctx or default_context()
+        lib = self.ctx._lib
+        keep = []
+        idx = np.ascontiguousarray(np.asarray(idx3, dtype=np.int64).ravel())
+        keep.append(idx)
+        dMr, dMc, dG = L.make_diag(Mr, keep), L.make_diag(Mc, keep), L.make_diag(Gram, keep)
+        h = C.c_void_p()
+        if fN is not None:
+            P, Q, R = fN.shape[:3]
+            f = L.cplx_flat(fN)
+            L.check(lib.vs_op_create_fN(self.ctx.h, L_, M_, N_, L.dptr(f), P, Q, R,
+                                        idx.ctypes.data_as(L._pi64), idx.size, dMr, dMc, dG, C.byref(h)), self.ctx.h)
+        else:
+            t = L.cplx_flat(toep)
+            L.check(lib.vs_op_create(self.ctx.h, L_, M_, N_, L.dptr(t), int(PQR[0]), int(PQR[1]), int(PQR[2]),
+                                     idx.ctypes.data_as(L._pi64), idx.size, dMr, dMc, dG, C.byref(h)), self.ctx.h)
+        self.h = h
+        self.n3 = idx.size
+        lmn = (C.c_int64 * 3)(); pqr = (C.c_int64 * 3)()
+        L.check(lib.vs_op_info(h, lmn, pqr, None))
+        self.LMN = tuple(lmn); self.PQR = tuple(pqr)
+
+    def apply(self, x, transp_flag="notransp", precision="c64"):
+        x = np.ascontiguousarray(np.asarray(x, dtype=np.complex128))
+        nrhs = x.size // self.n3
+        assert nrhs * self.n3 == x.size
+        y = np.empty_like(x)
+        L.check(self.ctx._lib.vs_op_apply(self.h, L.dptr(x), L.dptr(y), nrhs, _TRANSP[transp_flag],
+                                          L.VS_C64 if precision == "c64" else L.VS_C128), self.ctx.h)
+        return y
+
+    def apply_device(self, x, y, transp_flag="notransp"):
+        """x, y: CUDA torch tensors (complex64 or complex128), n3*nrhs elements."""
+        import torch
+        prec = L.VS_C64 if x.dtype == torch.complex64 else L.VS_C128
+        torch.cuda.synchronize()
+        L.check(self.ctx._lib.vs_op_apply_device(self.h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
+                                                 x.numel() // self.n3, _TRANSP[transp_flag], prec), self.ctx.h)
+        self.ctx.synchronize()
+        return y
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx._lib.vs_op_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def MVP(JIn0, fN, Mr, Mc, Gram, transp_flag, idx, GPU_flag=1, precision="c128", ctx=None):
+    """JOut = MVP(JIn0, fN, Mr, Mc, Gram, transp_flag, idx, GPU_flag) (MVP.m:1).
+    The device pipeline runs in ``precision`` ('c128' matches the reference's
+    FP64; 'c64' is the mixed-precision inner kernel)."""
+    Mr = np.asarray(Mr)
+    L_, M_, N_ = Mr.shape
+    op = Operator(L_, M_, N_, idx, Mr, Mc, Gram, fN=np.asarray(fN), ctx=ctx)
+    try:
+        return op.apply(JIn0, transp_flag, precision)
+    finally:
+        op.close()
+
+
+mv_AN_const = MVP

@@ -1,0 +1,79 @@
+// Shared device/host helpers for libvoxscatter: complex arithmetic on
+// float2/double2, status codes and launch checks.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cmath>
+#include <cstdio>
+#include <string>
+#include <stdexcept>
+#include "../../include/voxscatter.h"
+
+namespace vs {
+
+template <typename T> struct Cplx;
+template <> struct Cplx<float> { using type = float2; };
+template <> struct Cplx<double> { using type = double2; };
+template <typename T> using cplx_t = typename Cplx<T>::type;
+
+template <typename C> __host__ __device__ __forceinline__ C mk(double re, double im) {
+  C c; c.x = (decltype(c.x))re; c.y = (decltype(c.y))im; return c;
+}
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__host__ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+// a*conj(b)
+__host__ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+__host__ __device__ __forceinline__ double2 cmulc(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, a.y * b.y), fma(a.y, b.x, -a.x * b.y));
+}
+__host__ __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__host__ __device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+// a + b*c
+__host__ __device__ __forceinline__ float2 cfma(float2 b, float2 c, float2 a) {
+  return make_float2(fmaf(b.x, c.x, fmaf(-b.y, c.y, a.x)), fmaf(b.x, c.y, fmaf(b.y, c.x, a.y)));
+}
+__host__ __device__ __forceinline__ double2 cfma(double2 b, double2 c, double2 a) {
+  return make_double2(fma(b.x, c.x, fma(-b.y, c.y, a.x)), fma(b.x, c.y, fma(b.y, c.x, a.y)));
+}
+template <typename C> __host__ __device__ __forceinline__ C czero() { C c; c.x = 0; c.y = 0; return c; }
+template <typename D, typename S> __host__ __device__ __forceinline__ D ccast(S s) {
+  D d; d.x = (decltype(d.x))s.x; d.y = (decltype(d.y))s.y; return d;
+}
+
+// Error carried from a failing CUDA call or argument check to the C ABI.
+struct Error : std::runtime_error {
+  int status;
+  Error(int st, const std::string& m) : std::runtime_error(m), status(st) {}
+};
+
+#define VS_CUDA(call)                                                                 \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess) {                                                          \
+      throw ::vs::Error(e_ == cudaErrorMemoryAllocation ? VS_ERR_OOM : VS_ERR_CUDA,   \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));          \
+    }                                                                                 \
+  } while (0)
+
+#define VS_LAUNCH_CHECK() VS_CUDA(cudaGetLastError())
+
+#define VS_REQUIRE(cond, msg)                                    \
+  do {                                                           \
+    if (!(cond)) throw ::vs::Error(VS_ERR_ARG, msg);             \
+  } while (0)
+
+inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+}  // namespace vs

@@ -1,0 +1,317 @@
+// Mixed-radix Stockham FFT over lines held in shared memory.
+//
+// One CTA transforms a batch of lines cooperatively.  Element p of line b lives
+// at buf[b*ls + p*es]; `lines_fast` selects the butterfly-to-thread mapping so
+// that consecutive threads touch consecutive shared-memory words (lines
+// contiguous along x: lines_fast=false, es=1; lines strided across an x-tile:
+// lines_fast=true, ls=1).  Each radix-R stage reads R points at stride n/R,
+// twiddles them by w_n^(r*k*n/(Ns*R)) (k = j mod Ns), does an R-point DFT and
+// writes them at (j-k)*R + k + q*Ns, ping-ponging between two buffers (the
+// autosort form of Stockham; output in natural order, no bit reversal).
+// Radices 2,3,4,5,8 have closed-form butterflies, 7/11/13 use the twiddle
+// table at compile-time size, any other prime up to FFT_MAX_GENERIC_RADIX uses
+// a runtime O(R^2) DFT.  Forward = exp(-2 pi i/n) (MATLAB fft), inverse =
+// exp(+2 pi i/n) without the 1/n factor (folded elsewhere).
+#pragma once
+#include "vs_common.cuh"
+#include <vector>
+#include <cmath>
+
+namespace vs {
+
+constexpr int FFT_MAX_STAGES = 16;
+constexpr int FFT_MAX_GENERIC_RADIX = 128;
+
+struct FftPlan {
+  int n = 1;
+  int nstages = 0;
+  int radix[FFT_MAX_STAGES] = {};
+};
+
+inline FftPlan make_fft_plan(int n) {
+  FftPlan p;
+  p.n = n;
+  int m = n;
+  const int pref[] = {8, 4, 2, 3, 5, 7, 11, 13};
+  for (int r : pref) {
+    while (m % r == 0) {
+      VS_REQUIRE(p.nstages < FFT_MAX_STAGES, "FFT length has too many factors");
+      p.radix[p.nstages++] = r;
+      m /= r;
+    }
+  }
+  for (int f = 17; m > 1; f += 2) {
+    while (m % f == 0) {
+      VS_REQUIRE(f <= FFT_MAX_GENERIC_RADIX,
+                 "FFT length " + std::to_string(n) + " has a prime factor above 128");
+      VS_REQUIRE(p.nstages < FFT_MAX_STAGES, "FFT length has too many factors");
+      p.radix[p.nstages++] = f;
+      m /= f;
+    }
+  }
+  return p;
+}
+
+// exp(-2 pi i t / n), t = 0..n-1, in double (reduced to the first octant so the
+// table is accurate to the last bit of a double).
+inline std::vector<double> twiddle_table(int n) {
+  std::vector<double> t(2 * (size_t)n);
+  for (int k = 0; k < n; ++k) {
+    // angle = 2*pi*k/n ; use symmetric reduction via integer arithmetic
+    long long num = (long long)k * 8;  // in units of (2*pi/8)/n
+    double c, s;
+    long long q = num / n;  // octant index 0..7
+    double rem = (double)(num - q * n) / (double)n;  // fraction within the octant
+    double a = rem * (M_PI / 4);
+    double ca = std::cos(a), sa = std::sin(a);
+    double cb = std::cos(M_PI / 4 - a), sb = std::sin(M_PI / 4 - a);
+    switch (q) {
+      case 0: c = ca; s = sa; break;
+      case 1: c = sb; s = cb; break;
+      case 2: c = -sa; s = ca; break;
+      case 3: c = -cb; s = sb; break;
+      case 4: c = -ca; s = -sa; break;
+      case 5: c = -sb; s = -cb; break;
+      case 6: c = sa; s = -ca; break;
+      default: c = cb; s = -sb; break;
+    }
+    t[2 * k] = c;
+    t[2 * k + 1] = -s;
+  }
+  return t;
+}
+
+// Smallest m >= n whose prime factors are all in {2,3,5,7}.
+inline int smooth_size(int n) {
+  for (int m = n > 1 ? n : 1;; ++m) {
+    int r = m;
+    for (int f : {2, 3, 5, 7})
+      while (r % f == 0) r /= f;
+    if (r == 1) return m;
+  }
+}
+
+#if defined(__CUDACC__) || defined(VS_FFT_HOST_EMULATION)
+
+template <bool INV, typename C>
+__device__ __forceinline__ C twid(const C* __restrict__ tw, int idx) {
+  C w = __ldg(tw + idx);
+  if (INV) w.y = -w.y;
+  return w;
+}
+
+// multiply by -i (forward) or +i (inverse) as the sign of the 4-point DFT needs
+template <bool INV, typename C>
+__device__ __forceinline__ C rot90(C a) {
+  C r;
+  if (INV) { r.x = -a.y; r.y = a.x; }
+  else { r.x = a.y; r.y = -a.x; }
+  return r;
+}
+
+template <int R, bool INV, typename C>
+struct Butterfly;
+
+template <bool INV, typename C>
+struct Butterfly<2, INV, C> {
+  __device__ __forceinline__ static void run(C* v, const C*, int) {
+    C a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  }
+};
+
+template <bool INV, typename C>
+struct Butterfly<4, INV, C> {
+  __device__ __forceinline__ static void run(C* v, const C*, int) {
+    C s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+    C s13 = cadd(v[1], v[3]), d13 = rot90<INV>(csub(v[1], v[3]));
+    v[0] = cadd(s02, s13);
+    v[2] = csub(s02, s13);
+    v[1] = cadd(d02, d13);
+    v[3] = csub(d02, d13);
+  }
+};
+
+template <bool INV, typename C>
+struct Butterfly<8, INV, C> {
+  __device__ __forceinline__ static void run(C* v, const C* tw, int n) {
+    using T = decltype(v[0].x);
+    const T h = (T)0.70710678118654752440;
+    C u[4], w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      u[k] = cadd(v[k], v[k + 4]);
+      w[k] = csub(v[k], v[k + 4]);
+    }
+    // w[k] *= exp(-+ 2 pi i k / 8)
+    {
+      C a = w[1];
+      // forward: (1 - i)/sqrt2 ; inverse: (1 + i)/sqrt2
+      if (INV) { w[1].x = (a.x - a.y) * h; w[1].y = (a.x + a.y) * h; }
+      else { w[1].x = (a.x + a.y) * h; w[1].y = (a.y - a.x) * h; }
+      w[2] = rot90<INV>(w[2]);
+      C b = w[3];
+      // forward: (-1 - i)/sqrt2 ; inverse: (-1 + i)/sqrt2
+      if (INV) { w[3].x = (-b.x - b.y) * h; w[3].y = (b.x - b.y) * h; }
+      else { w[3].x = (b.y - b.x) * h; w[3].y = (-b.x - b.y) * h; }
+    }
+    Butterfly<4, INV, C>::run(u, tw, n);
+    Butterfly<4, INV, C>::run(w, tw, n);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      v[2 * q] = u[q];
+      v[2 * q + 1] = w[q];
+    }
+  }
+};
+
+template <bool INV, typename C>
+struct Butterfly<3, INV, C> {
+  __device__ __forceinline__ static void run(C* v, const C*, int) {
+    using T = decltype(v[0].x);
+    const T s3 = INV ? (T)0.86602540378443864676 : (T)-0.86602540378443864676;
+    C t1 = cadd(v[1], v[2]);
+    C t2 = make_c(v[0].x - (T)0.5 * t1.x, v[0].y - (T)0.5 * t1.y);
+    C d = csub(v[1], v[2]);
+    // i*s3*d
+    C t3 = make_c(-s3 * d.y, s3 * d.x);
+    v[0] = cadd(v[0], t1);
+    v[1] = cadd(t2, t3);
+    v[2] = csub(t2, t3);
+  }
+  __device__ __forceinline__ static C make_c(decltype(C().x) a, decltype(C().x) b) { C c; c.x = a; c.y = b; return c; }
+};
+
+template <bool INV, typename C>
+struct Butterfly<5, INV, C> {
+  __device__ __forceinline__ static void run(C* v, const C*, int) {
+    using T = decltype(v[0].x);
+    const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;
+    const T sg = INV ? (T)1 : (T)-1;
+    const T s1 = sg * (T)0.95105651629515357212, s2 = sg * (T)0.58778525229247312917;
+    C b1 = cadd(v[1], v[4]), b2 = cadd(v[2], v[3]);
+    C d1 = csub(v[1], v[4]), d2 = csub(v[2], v[3]);
+    C a0 = v[0];
+    C r1, r2, i1, i2;
+    r1.x = a0.x + c1 * b1.x + c2 * b2.x; r1.y = a0.y + c1 * b1.y + c2 * b2.y;
+    r2.x = a0.x + c2 * b1.x + c1 * b2.x; r2.y = a0.y + c2 * b1.y + c1 * b2.y;
+    // i*(s1 d1 + s2 d2) and i*(s2 d1 - s1 d2)
+    T e1x = s1 * d1.x + s2 * d2.x, e1y = s1 * d1.y + s2 * d2.y;
+    T e2x = s2 * d1.x - s1 * d2.x, e2y = s2 * d1.y - s1 * d2.y;
+    i1.x = -e1y; i1.y = e1x;
+    i2.x = -e2y; i2.y = e2x;
+    v[0] = cadd(a0, cadd(b1, b2));
+    v[1] = cadd(r1, i1);
+    v[4] = csub(r1, i1);
+    v[2] = cadd(r2, i2);
+    v[3] = csub(r2, i2);
+  }
+};
+
+// Compile-time-size DFT for the remaining small primes, roots read from the
+// length-n twiddle table: w_R^k = tw[k*n/R].
+template <int R, bool INV, typename C>
+struct Butterfly {
+  __device__ __forceinline__ static void run(C* v, const C* tw, int n) {
+    C y[R];
+    const int st = n / R;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      C acc = v[0];
+#pragma unroll
+      for (int r = 1; r < R; ++r) acc = cfma(v[r], twid<INV>(tw, ((r * q) % R) * st), acc);
+      y[q] = acc;
+    }
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = y[q];
+  }
+};
+
+template <int R, bool INV, typename C>
+__device__ __forceinline__ void fft_stage(const C* __restrict__ src, C* __restrict__ dst, int n, int Ns, int nlines,
+                                          int ls, int es, bool lines_fast, const C* __restrict__ tw) {
+  const int m = n / R;
+  const int total = nlines * m;
+  const int step = n / (Ns * R);
+  for (int u = threadIdx.x; u < total; u += blockDim.x) {
+    int line, j;
+    if (lines_fast) { line = u % nlines; j = u / nlines; }
+    else { line = u / m; j = u - line * m; }
+    const C* s = src + line * ls;
+    C* d = dst + line * ls;
+    const int k = j % Ns;
+    C v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = s[(j + r * m) * es];
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], twid<INV>(tw, r * k * step));
+    }
+    Butterfly<R, INV, C>::run(v, tw, n);
+    const int base = (j - k) * R + k;
+#pragma unroll
+    for (int q = 0; q < R; ++q) d[(base + q * Ns) * es] = v[q];
+  }
+}
+
+template <bool INV, typename C>
+__device__ __noinline__ void fft_stage_generic(const C* __restrict__ src, C* __restrict__ dst, int n, int R, int Ns,
+                                               int nlines, int ls, int es, bool lines_fast,
+                                               const C* __restrict__ tw) {
+  const int m = n / R;
+  const int total = nlines * m;
+  const int step = n / (Ns * R);
+  const int st = n / R;
+  C v[FFT_MAX_GENERIC_RADIX];
+  for (int u = threadIdx.x; u < total; u += blockDim.x) {
+    int line, j;
+    if (lines_fast) { line = u % nlines; j = u / nlines; }
+    else { line = u / m; j = u - line * m; }
+    const C* s = src + line * ls;
+    C* d = dst + line * ls;
+    const int k = j % Ns;
+    for (int r = 0; r < R; ++r) {
+      C a = s[(j + r * m) * es];
+      v[r] = (r > 0 && Ns > 1) ? cmul(a, twid<INV>(tw, r * k * step)) : a;
+    }
+    const int base = (j - k) * R + k;
+    for (int q = 0; q < R; ++q) {
+      C acc = v[0];
+      for (int r = 1; r < R; ++r) acc = cfma(v[r], twid<INV>(tw, ((r * q) % R) * st), acc);
+      d[(base + q * Ns) * es] = acc;
+    }
+  }
+}
+
+// Transforms `nlines` lines held in `a` (scratch `b` of the same shape).
+// Caller syncs before the call; the function ends with a __syncthreads() and
+// returns the buffer that holds the result.
+template <bool INV, typename C>
+__device__ C* fft_lines(C* a, C* b, const FftPlan& pl, int nlines, int ls, int es, bool lines_fast,
+                        const C* __restrict__ tw) {
+  const int n = pl.n;
+  int Ns = 1;
+  for (int s = 0; s < pl.nstages; ++s) {
+    const int R = pl.radix[s];
+    switch (R) {
+      case 2: fft_stage<2, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
+      case 3: fft_stage<3, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
+      case 4: fft_stage<4, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
+      case 5: fft_stage<5, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
+      case 7: fft_stage<7, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
+      case 8: fft_stage<8, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
+      case 11: fft_stage<11, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
+      case 13: fft_stage<13, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
+      default: fft_stage_generic<INV>(a, b, n, R, Ns, nlines, ls, es, lines_fast, tw); break;
+    }
+    __syncthreads();
+    C* t = a; a = b; b = t;
+    Ns *= R;
+  }
+  return a;
+}
+
+#endif  // __CUDACC__ || VS_FFT_HOST_EMULATION
+
+}  // namespace vs

@@ -1,0 +1,106 @@
+// Internal objects behind the C-ABI handles.
+#pragma once
+#include "vs_common.cuh"
+#include "vs_fft.cuh"
+#include <memory>
+#include <vector>
+#include <string>
+
+namespace vs {
+
+// Owned device allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  void alloc(size_t n) {
+    if (n <= bytes && p) return;
+    release();
+    if (n == 0) return;
+    VS_CUDA(cudaMalloc(&p, n));
+    bytes = n;
+  }
+  template <typename X> X* as() const { return reinterpret_cast<X*>(p); }
+};
+
+// One FFT axis: plan plus forward twiddle tables in both precisions.
+struct FftAxis {
+  FftPlan plan;
+  DevBuf tw32, tw64;
+  void init(int n, cudaStream_t st);
+  template <typename T> const cplx_t<T>* tw() const;
+};
+template <> inline const float2* FftAxis::tw<float>() const { return tw32.as<float2>(); }
+template <> inline const double2* FftAxis::tw<double>() const { return tw64.as<double2>(); }
+
+}  // namespace vs
+
+struct vs_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  vs::DevBuf stage;  // host<->device staging for the host-buffer entry points
+};
+
+// Diagonal coefficients of an operator at the n3 unknown positions.
+struct VsDiagDev {
+  bool arr = false;
+  double2 s = {0, 0};
+  vs::DevBuf v32, v64;
+  template <typename T> const vs::cplx_t<T>* ptr() const;
+};
+template <> inline const float2* VsDiagDev::ptr<float>() const { return arr ? v32.as<float2>() : nullptr; }
+template <> inline const double2* VsDiagDev::ptr<double>() const { return arr ? v64.as<double2>() : nullptr; }
+
+struct vs_op {
+  vs_ctx* ctx = nullptr;
+  int L = 0, M = 0, N = 0, P = 0, Q = 0, R = 0;
+  int64_t V = 0, n3 = 0;
+  vs::DevBuf map3;      // int32[3V]: unknown position of each grid entry, -1 if absent
+  vs::DevBuf pos2grid;  // int32[n3]: grid entry of each unknown
+  VsDiagDev d1, d1c, d2;  // Gram.*Mr, Gram.*conj(Mr), Mc at the unknowns
+  vs::DevBuf G32, G64;  // spectrum of the embedded tensor / (P*Q*R), 6 x P*Q*R
+  vs::DevBuf toep64;    // first-octant Toeplitz tensor, L*M*N*6 (double2)
+  vs::FftAxis ax[3];
+  vs::DevBuf t1, t2;    // pipeline intermediates
+  vs::DevBuf xin, yout; // device staging for host-buffer applies
+};
+
+namespace vs {
+
+// Launchers (vs_matvec.cu)
+template <typename T>
+void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
+            cudaStream_t st);
+void ensure_scratch(vs_op& op, int nrhs, size_t elem_bytes);
+
+// Generic batched FFT passes (vs_matvec.cu)
+template <typename T, bool INV>
+void fft_axis0(cplx_t<T>* data, int n, int64_t nlines, const FftAxis& ax, cudaStream_t st);
+template <typename T, bool INV>
+void fft_strided(cplx_t<T>* data, int xext, int n, int64_t row_stride, int na, int64_t stride_a, int nb,
+                 int64_t stride_b, const FftAxis& ax, cudaStream_t st);
+
+// Green tensor and embedding (vs_green.cu)
+void green_dda_device(int L, int M, int N, const double* ox, const double* oy, const double* oz, double ko,
+                      int near_quad, double2* toep, cudaStream_t st);
+void embed_fft_device(int L, int M, int N, const double2* toep, int P, int Q, int R, double2* out,
+                      FftAxis* ax, cudaStream_t st);
+void toep_from_fN_device(int L, int M, int N, int P, int Q, int R, double2* fN_inplace, double2* toep,
+                         FftAxis* ax, cudaStream_t st);
+void finalize_spectrum(const double2* fN, int64_t total, double scale, double2* g64, float2* g32,
+                       cudaStream_t st);
+
+// Elementwise helpers (vs_matvec.cu)
+void c128_to_c64(const double2* in, float2* out, int64_t n, cudaStream_t st);
+void c64_to_c128(const float2* in, double2* out, int64_t n, cudaStream_t st);
+
+}  // namespace vs

@@ -1,0 +1,440 @@
+// Fused FFT matvec of the DDA / JVIE operator (replaces src/src_vie/src_mvp/MVP.m:39-145).
+//
+// Pipeline for y = D1.*x - D2.*crop(IFFT(G ⊙ FFT(pad(x)))) on unknowns idx3:
+//   pass XF : gather x through map3 into (L,M,N,3) lines along x, zero-pad to P,
+//             forward FFT along x                          -> T1 (P, M, N, 3)
+//   pass YF : forward FFT along y (M -> Q) on x-tiles      -> T2 (P, Q, N, 3)
+//   pass Z  : forward FFT along z (N -> R), 6-component symmetric tensor
+//             multiply (MVP.m:108-123 pairing), inverse FFT along z, crop to N,
+//             in place in T2
+//   pass YI : inverse FFT along y, crop to M               -> T1
+//   pass XI : inverse FFT along x, crop to L, diagonal term and scatter to y
+// G holds the spectrum already divided by P*Q*R, so no pass rescales.
+// All passes are templated on the real type (float: c64 pipeline, double: c128)
+// and take an optional device flag `skip` so that a graph of Krylov steps can
+// turn itself into no-ops after convergence.
+#include "vs_internal.h"
+
+namespace vs {
+
+constexpr int kThreads = 256;
+constexpr size_t kSmemBudget = 100 * 1024;
+
+void FftAxis::init(int n, cudaStream_t st) {
+  plan = make_fft_plan(n);
+  std::vector<double> t = twiddle_table(n);
+  std::vector<float> tf(t.size());
+  for (size_t i = 0; i < t.size(); ++i) tf[i] = (float)t[i];
+  tw64.alloc(t.size() * sizeof(double));
+  tw32.alloc(tf.size() * sizeof(float));
+  VS_CUDA(cudaMemcpyAsync(tw64.p, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  VS_CUDA(cudaMemcpyAsync(tw32.p, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+  VS_CUDA(cudaStreamSynchronize(st));
+}
+
+template <typename C>
+struct DiagArg {
+  const C* v;
+  C s;
+  __device__ __forceinline__ C at(int pos) const { return v ? v[pos] : s; }
+};
+
+template <typename T>
+struct PipeArgs {
+  using C = cplx_t<T>;
+  int L, M, N, P, Q, R;
+  int64_t V, n3;
+  const int* map3;
+  const C* x;
+  C* y;
+  DiagArg<C> d1, d1c, d2;
+  C* t1;
+  C* t2;
+  const C* G;
+  const C* twP;
+  const C* twQ;
+  const C* twR;
+  FftPlan pP, pQ, pR;
+  int lpb;  // lines per block in the x passes
+  int tx;   // x-tile width of the y and z passes
+  const int* skip;
+};
+
+// ---- pass XF: gather + forward FFT along x ------------------------------
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kThreads) k_xf(PipeArgs<T> a) {
+  using C = cplx_t<T>;
+  if (a.skip && *a.skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* s0 = reinterpret_cast<C*>(smem_raw);
+  C* s1 = s0 + a.lpb * a.P;
+  const int rhs = blockIdx.y;
+  const C* x = a.x + (int64_t)rhs * a.n3;
+  C* t1 = a.t1 + (int64_t)rhs * a.P * a.M * a.N * 3;
+  const int nlines = a.M * a.N * 3;
+  const int line0 = blockIdx.x * a.lpb;
+  const int MN = a.M * a.N;
+  const int tot = a.lpb * a.P;
+  for (int u = threadIdx.x; u < tot; u += blockDim.x) {
+    const int l = u / a.P;
+    const int i = u - l * a.P;
+    const int line = line0 + l;
+    C v = czero<C>();
+    if (line < nlines && i < a.L) {
+      const int c = line / MN;
+      const int jk = line - c * MN;
+      const int pos = __ldg(a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L + i);
+      if (pos >= 0) {
+        v = x[pos];
+        if (MODE == VS_TRANSP) v = cmul(a.d2.at(pos), v);
+        if (MODE == VS_CONJTRANSP) v = cmul(a.d2.at(pos), cconj(v));
+      }
+    }
+    s0[u] = v;
+  }
+  __syncthreads();
+  C* res = fft_lines<false>(s0, s1, a.pP, a.lpb, a.P, 1, false, a.twP);
+  for (int u = threadIdx.x; u < tot; u += blockDim.x) {
+    const int l = u / a.P;
+    if (line0 + l < nlines) t1[(int64_t)line0 * a.P + u] = res[u];
+  }
+}
+
+// ---- pass XI: inverse FFT along x + diagonal + scatter ------------------
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kThreads) k_xi(PipeArgs<T> a) {
+  using C = cplx_t<T>;
+  if (a.skip && *a.skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* s0 = reinterpret_cast<C*>(smem_raw);
+  C* s1 = s0 + a.lpb * a.P;
+  const int rhs = blockIdx.y;
+  const C* x = a.x + (int64_t)rhs * a.n3;
+  C* y = a.y + (int64_t)rhs * a.n3;
+  const C* t1 = a.t1 + (int64_t)rhs * a.P * a.M * a.N * 3;
+  const int nlines = a.M * a.N * 3;
+  const int line0 = blockIdx.x * a.lpb;
+  const int MN = a.M * a.N;
+  const int tot = a.lpb * a.P;
+  for (int u = threadIdx.x; u < tot; u += blockDim.x) {
+    const int l = u / a.P;
+    s0[u] = (line0 + l < nlines) ? t1[(int64_t)line0 * a.P + u] : czero<C>();
+  }
+  __syncthreads();
+  C* res = fft_lines<true>(s0, s1, a.pP, a.lpb, a.P, 1, false, a.twP);
+  const int totL = a.lpb * a.L;
+  for (int u = threadIdx.x; u < totL; u += blockDim.x) {
+    const int l = u / a.L;
+    const int i = u - l * a.L;
+    const int line = line0 + l;
+    if (line >= nlines) continue;
+    const int c = line / MN;
+    const int jk = line - c * MN;
+    const int pos = __ldg(a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L + i);
+    if (pos < 0) continue;
+    const C conv = res[l * a.P + i];
+    const C xv = x[pos];
+    C out;
+    if (MODE == VS_NOTRANSP) out = csub(cmul(a.d1.at(pos), xv), cmul(a.d2.at(pos), conv));
+    else if (MODE == VS_TRANSP) out = csub(cmul(a.d1.at(pos), xv), conv);
+    else out = csub(cmul(a.d1c.at(pos), xv), cconj(conv));
+    y[pos] = out;
+  }
+}
+
+// ---- strided-axis pass (y of the pipeline; y and z of the setup FFTs) ----
+// Lines run along a strided axis; a CTA owns an x-tile of `tx` columns of one
+// plane.  Element (x, row) of plane (pa, pb) of the source is at
+//   src + pa*s_a + pb*s_b + row*s_row + x      (same form for the destination).
+// Rows [0, n_in) are loaded (zero pad up to n), rows [0, n_out) are stored.
+template <typename T>
+struct StridedArgs {
+  using C = cplx_t<T>;
+  const C* src;
+  C* dst;
+  int xext, n_in, n_out, tx, na;
+  int64_t s_row, s_a, s_b, s_rhs;
+  int64_t d_row, d_a, d_b, d_rhs;
+  FftPlan plan;
+  const C* tw;
+  const int* skip;
+};
+
+template <typename T, bool INV>
+__global__ void __launch_bounds__(kThreads) k_strided(StridedArgs<T> a) {
+  using C = cplx_t<T>;
+  if (a.skip && *a.skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = a.plan.n;
+  C* s0 = reinterpret_cast<C*>(smem_raw);
+  C* s1 = s0 + n * a.tx;
+  const int x0 = blockIdx.x * a.tx;
+  const int pa = blockIdx.y % a.na;
+  const int pb = blockIdx.y / a.na;
+  const C* src = a.src + pa * a.s_a + pb * a.s_b + (int64_t)blockIdx.z * a.s_rhs;
+  C* dst = a.dst + pa * a.d_a + pb * a.d_b + (int64_t)blockIdx.z * a.d_rhs;
+  const int tot = n * a.tx;
+  for (int u = threadIdx.x; u < tot; u += blockDim.x) {
+    const int row = u / a.tx;
+    const int xl = u - row * a.tx;
+    const int x = x0 + xl;
+    s0[u] = (row < a.n_in && x < a.xext) ? src[row * a.s_row + x] : czero<C>();
+  }
+  __syncthreads();
+  C* res = fft_lines<INV>(s0, s1, a.plan, a.tx, 1, a.tx, true, a.tw);
+  const int totO = a.n_out * a.tx;
+  for (int u = threadIdx.x; u < totO; u += blockDim.x) {
+    const int row = u / a.tx;
+    const int xl = u - row * a.tx;
+    const int x = x0 + xl;
+    if (x < a.xext) dst[row * a.d_row + x] = res[u];
+  }
+}
+
+// ---- pass Z: FFT_z ⊗ tensor multiply ⊗ IFFT_z, in place in T2 -----------
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_z(PipeArgs<T> a) {
+  using C = cplx_t<T>;
+  if (a.skip && *a.skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int R = a.R, tx = a.tx, w = 3 * tx;
+  C* s0 = reinterpret_cast<C*>(smem_raw);
+  C* s1 = s0 + R * w;
+  const int x0 = blockIdx.x * tx;
+  const int ky = blockIdx.y;
+  const int64_t PQ = (int64_t)a.P * a.Q;
+  C* t2 = a.t2 + (int64_t)blockIdx.z * PQ * a.N * 3;
+  const int tot = R * w;
+  for (int u = threadIdx.x; u < tot; u += blockDim.x) {
+    const int z = u / w;
+    const int rem = u - z * w;
+    const int c = rem / tx;
+    const int xl = rem - c * tx;
+    const int x = x0 + xl;
+    s0[u] = (z < a.N && x < a.P) ? t2[x + a.P * (ky + (int64_t)a.Q * (z + (int64_t)a.N * c))] : czero<C>();
+  }
+  __syncthreads();
+  C* res = fft_lines<false>(s0, s1, a.pR, w, 1, w, true, a.twR);
+  const int64_t PQR = PQ * R;
+  const int totm = R * tx;
+  for (int u = threadIdx.x; u < totm; u += blockDim.x) {
+    const int kz = u / tx;
+    const int xl = u - kz * tx;
+    const int x = x0 + xl;
+    if (x >= a.P) continue;
+    const int64_t gi = x + a.P * (ky + (int64_t)a.Q * kz);
+    const C g0 = __ldg(a.G + gi), g1 = __ldg(a.G + PQR + gi), g2 = __ldg(a.G + 2 * PQR + gi);
+    const C g3 = __ldg(a.G + 3 * PQR + gi), g4 = __ldg(a.G + 4 * PQR + gi), g5 = __ldg(a.G + 5 * PQR + gi);
+    C* p = res + kz * w + xl;
+    const C v0 = p[0], v1 = p[tx], v2 = p[2 * tx];
+    p[0] = cmul(g0, v0); p[0] = cfma(g1, v1, p[0]); p[0] = cfma(g2, v2, p[0]);
+    C o1 = cmul(g1, v0); o1 = cfma(g3, v1, o1); o1 = cfma(g4, v2, o1);
+    C o2 = cmul(g2, v0); o2 = cfma(g4, v1, o2); o2 = cfma(g5, v2, o2);
+    p[tx] = o1;
+    p[2 * tx] = o2;
+  }
+  __syncthreads();
+  C* other = (res == s0) ? s1 : s0;
+  C* out = fft_lines<true>(res, other, a.pR, w, 1, w, true, a.twR);
+  const int toto = a.N * w;
+  for (int u = threadIdx.x; u < toto; u += blockDim.x) {
+    const int z = u / w;
+    const int rem = u - z * w;
+    const int c = rem / tx;
+    const int xl = rem - c * tx;
+    const int x = x0 + xl;
+    if (x < a.P) t2[x + a.P * (ky + (int64_t)a.Q * (z + (int64_t)a.N * c))] = out[u];
+  }
+}
+
+static int pick_tile(int n, size_t csize, int width_mult) {
+  int tx = 32;
+  while (tx > 1 && 2ull * n * tx * width_mult * csize > kSmemBudget) tx >>= 1;
+  return tx;
+}
+
+template <typename K>
+static void set_smem(K kernel, size_t bytes) {
+  if (bytes > 227 * 1024)
+    throw Error(VS_ERR_UNSUPPORTED, "FFT tile needs " + std::to_string(bytes) + " bytes of shared memory (> 227 KB)");
+  if (bytes > 48 * 1024) VS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
+void ensure_scratch(vs_op& op, int nrhs, size_t elem_bytes) {
+  const size_t t1 = (size_t)op.P * op.M * op.N * 3 * elem_bytes * nrhs;
+  const size_t t2 = (size_t)op.P * op.Q * op.N * 3 * elem_bytes * nrhs;
+  op.t1.alloc(t1);
+  op.t2.alloc(t2);
+}
+
+template <typename T>
+static void launch_x(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaStream_t st) {
+  const int nlines = a.M * a.N * 3;
+  dim3 grid(ceil_div(nlines, a.lpb), nrhs);
+  const size_t smem = 2ull * a.lpb * a.P * sizeof(cplx_t<T>);
+#define VS_X(KER, MD)                              \
+  {                                                \
+    auto k = KER<T, MD>;                           \
+    set_smem(k, smem);                             \
+    k<<<grid, kThreads, smem, st>>>(a);            \
+  }
+  if (!inverse) {
+    if (mode == VS_NOTRANSP) VS_X(k_xf, VS_NOTRANSP)
+    else if (mode == VS_TRANSP) VS_X(k_xf, VS_TRANSP)
+    else VS_X(k_xf, VS_CONJTRANSP)
+  } else {
+    if (mode == VS_NOTRANSP) VS_X(k_xi, VS_NOTRANSP)
+    else if (mode == VS_TRANSP) VS_X(k_xi, VS_TRANSP)
+    else VS_X(k_xi, VS_CONJTRANSP)
+  }
+#undef VS_X
+  VS_LAUNCH_CHECK();
+}
+
+template <typename T, bool INV>
+static void launch_strided(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st) {
+  dim3 grid(ceil_div(a.xext, a.tx), nplanes, nrhs);
+  const size_t smem = 2ull * a.plan.n * a.tx * sizeof(cplx_t<T>);
+  auto k = k_strided<T, INV>;
+  set_smem(k, smem);
+  k<<<grid, kThreads, smem, st>>>(a);
+  VS_LAUNCH_CHECK();
+}
+
+template <typename T>
+static StridedArgs<T> y_pass_args(const vs_op& op, const PipeArgs<T>& a, bool inverse) {
+  StridedArgs<T> s;
+  const int64_t pm = (int64_t)op.P * op.M, pq = (int64_t)op.P * op.Q;
+  s.src = inverse ? a.t2 : a.t1;
+  s.dst = inverse ? a.t1 : a.t2;
+  s.xext = op.P;
+  s.n_in = inverse ? op.Q : op.M;
+  s.n_out = inverse ? op.M : op.Q;
+  s.tx = pick_tile(op.Q, sizeof(cplx_t<T>), 1);
+  s.na = op.N * 3;
+  s.s_row = op.P; s.d_row = op.P;
+  s.s_a = inverse ? pq : pm; s.d_a = inverse ? pm : pq;
+  s.s_b = 0; s.d_b = 0;
+  s.s_rhs = s.s_a * op.N * 3; s.d_rhs = s.d_a * op.N * 3;
+  s.plan = op.ax[1].plan;
+  s.tw = a.twQ;
+  s.skip = a.skip;
+  return s;
+}
+
+template <typename T>
+void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
+            cudaStream_t st) {
+  using C = cplx_t<T>;
+  VS_REQUIRE(mode >= VS_NOTRANSP && mode <= VS_CONJTRANSP, "mode must be VS_NOTRANSP, VS_TRANSP or VS_CONJTRANSP");
+  PipeArgs<T> a;
+  a.L = op.L; a.M = op.M; a.N = op.N; a.P = op.P; a.Q = op.Q; a.R = op.R;
+  a.V = op.V; a.n3 = op.n3;
+  a.map3 = op.map3.as<int>();
+  a.x = x; a.y = y;
+  a.d1 = {op.d1.ptr<T>(), mk<C>(op.d1.s.x, op.d1.s.y)};
+  a.d1c = {op.d1c.ptr<T>(), mk<C>(op.d1c.s.x, op.d1c.s.y)};
+  a.d2 = {op.d2.ptr<T>(), mk<C>(op.d2.s.x, op.d2.s.y)};
+  a.t1 = op.t1.as<C>();
+  a.t2 = op.t2.as<C>();
+  a.G = std::is_same<T, float>::value ? (const C*)op.G32.p : (const C*)op.G64.p;
+  a.twP = op.ax[0].tw<T>(); a.twQ = op.ax[1].tw<T>(); a.twR = op.ax[2].tw<T>();
+  a.pP = op.ax[0].plan; a.pQ = op.ax[1].plan; a.pR = op.ax[2].plan;
+  a.lpb = std::max(1, 2048 / op.P);
+  a.tx = pick_tile(op.R, sizeof(C), 3);
+  a.skip = skip;
+  launch_x<T>(a, false, mode, nrhs, st);
+  launch_strided<T, false>(y_pass_args<T>(op, a, false), op.N * 3, nrhs, st);
+  {
+    dim3 grid(ceil_div(op.P, a.tx), op.Q, nrhs);
+    const size_t smem = 2ull * op.R * 3 * a.tx * sizeof(C);
+    auto k = k_z<T>;
+    set_smem(k, smem);
+    k<<<grid, kThreads, smem, st>>>(a);
+    VS_LAUNCH_CHECK();
+  }
+  launch_strided<T, true>(y_pass_args<T>(op, a, true), op.N * 3, nrhs, st);
+  launch_x<T>(a, true, mode, nrhs, st);
+}
+
+template void matvec<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t);
+template void matvec<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t);
+
+// ---- generic batched FFTs (operator setup, preconditioner) --------------
+template <typename T, bool INV>
+__global__ void __launch_bounds__(kThreads) k_axis0(cplx_t<T>* data, int n, int64_t nlines, int lpb, FftPlan plan,
+                                                    const cplx_t<T>* tw) {
+  using C = cplx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* s0 = reinterpret_cast<C*>(smem_raw);
+  C* s1 = s0 + lpb * n;
+  const int64_t line0 = (int64_t)blockIdx.x * lpb;
+  const int tot = lpb * n;
+  C* base = data + line0 * n;
+  for (int u = threadIdx.x; u < tot; u += blockDim.x)
+    s0[u] = (line0 + u / n < nlines) ? base[u] : czero<C>();
+  __syncthreads();
+  C* res = fft_lines<INV>(s0, s1, plan, lpb, n, 1, false, tw);
+  for (int u = threadIdx.x; u < tot; u += blockDim.x)
+    if (line0 + u / n < nlines) base[u] = res[u];
+}
+
+template <typename T, bool INV>
+void fft_axis0(cplx_t<T>* data, int n, int64_t nlines, const FftAxis& ax, cudaStream_t st) {
+  const int lpb = std::max(1, 2048 / n);
+  const size_t smem = 2ull * lpb * n * sizeof(cplx_t<T>);
+  auto k = k_axis0<T, INV>;
+  set_smem(k, smem);
+  k<<<ceil_div(nlines, lpb), kThreads, smem, st>>>(data, n, nlines, lpb, ax.plan, ax.tw<T>());
+  VS_LAUNCH_CHECK();
+}
+
+template <typename T, bool INV>
+void fft_strided(cplx_t<T>* data, int xext, int n, int64_t row_stride, int na, int64_t stride_a, int nb,
+                 int64_t stride_b, const FftAxis& ax, cudaStream_t st) {
+  StridedArgs<T> s;
+  s.src = data; s.dst = data;
+  s.xext = xext; s.n_in = n; s.n_out = n;
+  s.tx = pick_tile(n, sizeof(cplx_t<T>), 1);
+  s.na = na;
+  s.s_row = s.d_row = row_stride;
+  s.s_a = s.d_a = stride_a;
+  s.s_b = s.d_b = stride_b;
+  s.s_rhs = s.d_rhs = 0;
+  s.plan = ax.plan;
+  s.tw = ax.tw<T>();
+  s.skip = nullptr;
+  launch_strided<T, INV>(s, na * nb, 1, st);
+}
+
+template void fft_axis0<double, false>(double2*, int, int64_t, const FftAxis&, cudaStream_t);
+template void fft_axis0<double, true>(double2*, int, int64_t, const FftAxis&, cudaStream_t);
+template void fft_axis0<float, false>(float2*, int, int64_t, const FftAxis&, cudaStream_t);
+template void fft_axis0<float, true>(float2*, int, int64_t, const FftAxis&, cudaStream_t);
+template void fft_strided<double, false>(double2*, int, int, int64_t, int, int64_t, int, int64_t, const FftAxis&, cudaStream_t);
+template void fft_strided<double, true>(double2*, int, int, int64_t, int, int64_t, int, int64_t, const FftAxis&, cudaStream_t);
+template void fft_strided<float, false>(float2*, int, int, int64_t, int, int64_t, int, int64_t, const FftAxis&, cudaStream_t);
+template void fft_strided<float, true>(float2*, int, int, int64_t, int, int64_t, int, int64_t, const FftAxis&, cudaStream_t);
+
+// ---- precision conversions ----------------------------------------------
+__global__ void k_c128_to_c64(const double2* __restrict__ in, float2* __restrict__ out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = make_float2((float)in[i].x, (float)in[i].y);
+}
+__global__ void k_c64_to_c128(const float2* __restrict__ in, double2* __restrict__ out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = make_double2(in[i].x, in[i].y);
+}
+static int grid_for(int64_t n) { return (int)std::min<int64_t>(ceil_div(n, kThreads), 152 * 16); }
+void c128_to_c64(const double2* in, float2* out, int64_t n, cudaStream_t st) {
+  if (n <= 0) return;
+  k_c128_to_c64<<<grid_for(n), kThreads, 0, st>>>(in, out, n);
+  VS_LAUNCH_CHECK();
+}
+void c64_to_c128(const float2* in, double2* out, int64_t n, cudaStream_t st) {
+  if (n <= 0) return;
+  k_c64_to_c128<<<grid_for(n), kThreads, 0, st>>>(in, out, n);
+  VS_LAUNCH_CHECK();
+}
+
+}  // namespace vs
