@@ -126,6 +126,94 @@ int vs_op_apply(vs_op* op, const double* x, double* y, int64_t nrhs, int mode, i
  * double2 for VS_C128), enqueued on the context's stream, no synchronisation. */
 int vs_op_apply_device(vs_op* op, const void* x, void* y, int64_t nrhs, int mode, int precision);
 
+/* ---- 2-level circulant preconditioner ------------------------------- */
+
+typedef struct vs_prec vs_prec;
+
+/* Bit mask of the precisions a preconditioner is built for. */
+enum vs_prec_mask { VS_BUILD_C64 = 1, VS_BUILD_C128 = 2 };
+
+/* circ_1_level (on_off = 'off') followed by circ_2_level on the device, FP64:
+ * src/src_preconditioning/circ_1_level.m:1-93 and circ_2_level.m:1-155.
+ *   toep: L*M*N*6 complex.  Outputs (any may be NULL):
+ *   circL_out: circ_L_opToep, L*M*N*6;  circM_out: circ_M_opToep, L*M*N*6;
+ *   blocks_out: the cell circ{i,j} as L*M blocks (block index i + L*j), each
+ *   3N x 3N column-major. */
+int vs_circ_levels(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* toep, double* circL_out,
+                   double* circM_out, double* blocks_out);
+
+/* Preconditioner inv(shift*I - diag(d)*C_ij) for every (x,y) frequency of the
+ * 2-level circulant approximation of op's Toeplitz tensor:
+ * main_DDA.m:98-116 (shift = 1/alpha_LDR, d = dV) and
+ * scatteringHumanHead.m:132-184 (shift = Gram, d = face3_2, a 3N vector).
+ *   shift: 1 complex; d: nd complex with nd = 1 or 3N;
+ *   precisions: VS_BUILD_C64 | VS_BUILD_C128 (inversions in FP32 / FP64).
+ * Returns VS_ERR_ARG if a block is singular.  The preconditioner copies op's
+ * unknown indices and does not reference op afterwards. */
+int vs_prec_create(vs_op* op, const double* shift, const double* d, int64_t nd, int precisions, vs_prec** out);
+
+/* Preconditioner from caller-supplied inverse blocks (the inv_blocks cell of
+ * mvp_circ_2_level.m:2): L*M blocks (index i + L*j), each 3N x 3N column-major
+ * complex; idx3: n3 0-based unknown indices into the (L,M,N,3) grid. */
+int vs_prec_create_blocks(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* inv_blocks,
+                          const int64_t* idx3, int64_t n3, int precisions, vs_prec** out);
+
+int vs_prec_destroy(vs_prec* prec);
+
+/* y = M^-1 x (mvp_circ_2_level.m:1-23) for nrhs right-hand sides, host
+ * buffers, complex double; precision VS_C64 or VS_C128 (must have been built). */
+int vs_prec_apply(vs_prec* prec, const double* x, double* y, int64_t nrhs, int precision);
+
+/* Same on device buffers of the precision's type, enqueued, no synchronisation. */
+int vs_prec_apply_device(vs_prec* prec, const void* x, void* y, int64_t nrhs, int precision);
+
+/* Copy out the inverse blocks of one precision as complex double, in the
+ * layout of vs_prec_create_blocks. */
+int vs_prec_get_blocks(vs_prec* prec, int precision, double* out);
+
+/* ---- Krylov solve ---------------------------------------------------- */
+
+enum vs_solve_method { VS_BICGSTAB = 0 };
+enum vs_solve_precision {
+  VS_SOLVE_MIXED = 0, /* c64 inner solve on the c64 pipeline inside FP64 iterative refinement */
+  VS_SOLVE_FP64 = 1   /* the same Krylov method on the c128 pipeline throughout               */
+};
+
+typedef struct vs_solve_opts {
+  int method;          /* VS_BICGSTAB                                                        */
+  int precision;       /* VS_SOLVE_MIXED or VS_SOLVE_FP64                                    */
+  double tol;          /* stop when ||b - A x|| <= tol ||b|| (FP64 true residual for MIXED)  */
+  int maxit;           /* maximum (inner) iterations in total                                */
+  double inner_tol;    /* MIXED: relative tolerance of each inner solve, 0 = automatic       */
+  int max_refine;      /* MIXED: maximum refinement steps                                    */
+  int iters_per_graph; /* iterations captured per CUDA graph launch (host polls in between)  */
+  double* resvec;      /* optional: relative residual norms at every half step               */
+  int64_t resvec_cap;  /* capacity of resvec                                                 */
+} vs_solve_opts;
+
+typedef struct vs_solve_info {
+  int flag;        /* 0 converged, 1 maxit reached, 4 breakdown, 5 non-finite (MATLAB flags) */
+  double relres;   /* final ||b - A x|| / ||b||, computed in FP64 on the c128 pipeline       */
+  double iter;     /* iterations (BiCGSTAB counts half steps as 0.5); inner total for MIXED  */
+  int refinements; /* MIXED: refinement steps taken                                          */
+  int64_t n_resvec;
+  double time_ms;  /* wall time of the call                                                  */
+} vs_solve_info;
+
+/* Fill opts with defaults: BiCGSTAB, MIXED, tol 1e-6, maxit 2000, automatic
+ * inner tolerance, 10 refinements, 4 iterations per graph, no resvec. */
+void vs_solve_opts_default(vs_solve_opts* opts);
+
+/* Solve A x = b with the (optional, may be NULL) preconditioner, right
+ * preconditioned as MATLAB's bicgstab(A, b, tol, maxit, M1) at
+ * main_DDA.m:82,120-121.  b: n3 complex (host); x: in = initial guess,
+ * out = solution.  Non-convergence is not an error: it is reported in
+ * info->flag, as MATLAB does. */
+int vs_solve(vs_op* op, vs_prec* prec, const double* b, double* x, const vs_solve_opts* opts, vs_solve_info* info);
+
+/* Same with b and x in device memory (double2, n3 each). */
+int vs_solve_device(vs_op* op, vs_prec* prec, const void* b, void* x, const vs_solve_opts* opts, vs_solve_info* info);
+
 #ifdef __cplusplus
 }
 #endif

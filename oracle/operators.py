@@ -78,8 +78,7 @@ def green_toeplitz(r, ko, nearby_quad="off"):
     (getOPERATOR_DDA.m:35-79)."""
     r = np.asarray(r, dtype=float)
     L, M, N, _ = r.shape
-    dx = r[1, 0, 0, 0] - r[0, 0, 0, 0] if L > 1 else (
-        r[0, 1, 0, 1] - r[0, 0, 0, 1] if M > 1 else r[0, 0, 1, 2] - r[0, 0, 0, 2])
+    dx = r[1, 0, 0, 0] - r[0, 0, 0, 0] if L > 1 else 0.0
     R0 = r[0, 0, 0, :]
     Roff = r - R0
     Toep = _dda_tensor(Roff, ko)

@@ -1,0 +1,103 @@
+"""GPU Krylov solves (BiCGSTAB, mixed c64 + FP64 refinement and plain FP64)
+against dense FP64 direct solves of the oracle operator.  Every solution is
+also re-checked with the oracle's FP64 MVP: ||b - A x||/||b|| <= tol."""
+import numpy as np
+import pytest
+
+import oracle as O
+from voxscatter_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def api():
+    from voxscatter_gb300 import build
+    build.build()
+    from voxscatter_gb300 import api as A
+    return A
+
+
+def _system(p):
+    L, M, N = p["L"], p["M"], p["N"]
+    nD = L * M * N
+    idx = p["idx"]
+    idx3 = np.concatenate([idx, nD + idx, 2 * nD + idx])
+    Toep = O.green_toeplitz(p["r"], p["ko"])
+    alpha = O.alpha_ldr(p["refInd"], p["ko"], p["d"], p["kvec"], p["Eo"])
+    dV = p["d"] ** 3
+    chi = np.zeros(nD); chi[idx] = 1
+    chi = chi.reshape((L, M, N), order="F")
+    fN = O.fft_operator(O.circulant_nop_const(Toep))
+    b = O.PlaneWavePointWise(p["Eo"], p["kvec"], p["r"]).ravel(order="F")[idx3]
+    Aor = lambda v: O.MVP(v, fN, np.ones((L, M, N)), dV * chi, 1 / alpha, "notransp", idx3)
+    return L, M, N, idx3, Toep, alpha, dV, b, Aor
+
+
+@pytest.mark.parametrize("precision,tol", [("mixed", 1e-6), ("fp64", 1e-10)])
+@pytest.mark.parametrize("use_prec", [False, True])
+def test_bicgstab_small(api, precision, tol, use_prec):
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, Toep, alpha, dV, b, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV) if use_prec else None
+    x, flag, relres, it, resvec = api.bicgstab(op, b, tol, 500, pr, precision=precision)
+    assert flag == 0, (flag, relres, it)
+    true_rel = np.linalg.norm(b - Aor(x)) / np.linalg.norm(b)
+    assert true_rel <= tol * 1.01
+    assert abs(true_rel - relres) <= 0.05 * max(true_rel, relres) + 1e-15
+    Ad = O.dense_dda_matrix(p["r"], p["idx"], p["ko"], 1 / alpha, dV)
+    xd = np.linalg.solve(Ad, b)
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 100 * tol
+    assert len(resvec) >= 2 and resvec[0] > 0
+    if precision == "fp64":
+        assert len(resvec) == int(round(2 * it)) + 1
+
+
+def test_bicgstab_iteration_count_matches_oracle(api):
+    """FP64 device BiCGSTAB follows the oracle's recurrences: same iteration count."""
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, Toep, alpha, dV, b, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
+    _, circL = O.circ_1_level(Toep, L, M, N, 0, "off")
+    _, blk = O.circ_2_level(circL, L, M, N)
+    inv = O.invert_blocks(blk, 1 / alpha, dV)
+    Pm = lambda v: O.mvp_circ_2_level(inv, v, L, M, N, idx3)
+    xo, fo, ro, ito, rvo = O.bicgstab(Aor, b, 1e-8, 500, Pm)
+    x, flag, relres, it, rv = api.bicgstab(op, b, 1e-8, 500, pr, precision="fp64")
+    assert flag == fo == 0
+    assert it == ito
+    n = min(len(rv), len(rvo))
+    assert np.allclose(rv[:n], rvo[:n], rtol=1e-6, atol=1e-12 * rvo[0])
+
+
+def test_bicgstab_flags(api):
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, Toep, alpha, dV, b, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    x, flag, relres, it, rv = api.bicgstab(op, b, 1e-12, 2, None, precision="fp64")
+    assert flag == 1 and it <= 2
+    from voxscatter_gb300 import _lib
+    bad = b.copy(); bad[3] = np.nan
+    with pytest.raises(_lib.VoxScatterError) as e:
+        api.bicgstab(op, bad, 1e-6, 10, None)
+    assert e.value.status == _lib.VS_ERR_NONFINITE
+    x, flag, relres, it, rv = api.bicgstab(op, np.zeros_like(b), 1e-6, 10, None)
+    assert flag == 0 and np.all(x == 0)
+
+
+def test_config1_mixed_and_fp64_agree(api):
+    """Hex plate 27x23x7 with the 2-level preconditioner, tol 1e-6 (the
+    reference's CPU configuration uses 1e-5): mixed and FP64 solutions agree with
+    the dense solve."""
+    p = W.config1()
+    L, M, N, idx3, Toep, alpha, dV, b, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
+    xm, im, rvm = api.solve(op, b, pr, tol=1e-6, precision="mixed")
+    xf, iff, rvf = api.solve(op, b, pr, tol=1e-6, precision="fp64")
+    assert im["flag"] == 0 and iff["flag"] == 0
+    for x in (xm, xf):
+        assert np.linalg.norm(b - Aor(x)) / np.linalg.norm(b) <= 1e-6 * 1.01
+    assert np.linalg.norm(xm - xf) / np.linalg.norm(xf) < 1e-4

@@ -43,7 +43,35 @@ SIGNATURES = {
     "vs_op_info": (C.c_int, [_vp, _pi64, _pi64, _pi64]),
     "vs_op_apply": (C.c_int, [_vp, _pd, _pd, _i64, C.c_int, C.c_int]),
     "vs_op_apply_device": (C.c_int, [_vp, _vp, _vp, _i64, C.c_int, C.c_int]),
+    "vs_circ_levels": (C.c_int, [_vp, _i64, _i64, _i64, _pd, _pd, _pd, _pd]),
+    "vs_prec_create": (C.c_int, [_vp, _pd, _pd, _i64, C.c_int, C.POINTER(_vp)]),
+    "vs_prec_create_blocks": (C.c_int, [_vp, _i64, _i64, _i64, _pd, _pi64, _i64, C.c_int, C.POINTER(_vp)]),
+    "vs_prec_destroy": (C.c_int, [_vp]),
+    "vs_prec_apply": (C.c_int, [_vp, _pd, _pd, _i64, C.c_int]),
+    "vs_prec_apply_device": (C.c_int, [_vp, _vp, _vp, _i64, C.c_int]),
+    "vs_prec_get_blocks": (C.c_int, [_vp, C.c_int, _pd]),
 }
+VS_BUILD_C64, VS_BUILD_C128 = 1, 2
+VS_BICGSTAB = 0
+VS_SOLVE_MIXED, VS_SOLVE_FP64 = 0, 1
+
+
+class vs_solve_opts(C.Structure):
+    _fields_ = [("method", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("maxit", C.c_int),
+                ("inner_tol", C.c_double), ("max_refine", C.c_int), ("iters_per_graph", C.c_int),
+                ("resvec", _pd), ("resvec_cap", _i64)]
+
+
+class vs_solve_info(C.Structure):
+    _fields_ = [("flag", C.c_int), ("relres", C.c_double), ("iter", C.c_double), ("refinements", C.c_int),
+                ("n_resvec", _i64), ("time_ms", C.c_double)]
+
+
+SIGNATURES.update({
+    "vs_solve_opts_default": (None, [C.POINTER(vs_solve_opts)]),
+    "vs_solve": (C.c_int, [_vp, _vp, _pd, _pd, C.POINTER(vs_solve_opts), C.POINTER(vs_solve_info)]),
+    "vs_solve_device": (C.c_int, [_vp, _vp, _vp, _vp, C.POINTER(vs_solve_opts), C.POINTER(vs_solve_info)]),
+})
 
 _lib = None
 

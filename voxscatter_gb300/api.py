@@ -1,8 +1,12 @@
 """Host-side mirror of the reference's MATLAB interface on libvoxscatter.
 
 Function names, argument order and meaning follow the reference:
-  getOPERATOR_DDA  src/src_vie/src_operators/getOPERATOR_DDA.m:1-2
+  getOPERATOR_DDA   src/src_vie/src_operators/getOPERATOR_DDA.m:1-2
   MVP / mv_AN_const src/src_vie/src_mvp/MVP.m:1
+  circ_1_level      src/src_preconditioning/circ_1_level.m:1
+  circ_2_level      src/src_preconditioning/circ_2_level.m:1
+  mvp_circ_2_level  src/src_preconditioning/mvp_circ_2_level.m:2
+  bicgstab          MATLAB bicgstab as called at main_DDA.m:82,120-121
 Indices are 0-based (MATLAB idx - 1).  The long-lived objects (Context,
 Operator) are the handle-based fast path; the MATLAB-named functions build
 them per call, as the reference's handles re-pass fN on every call.
@@ -175,3 +179,146 @@ def MVP(JIn0, fN, Mr, Mc, Gram, transp_flag, idx, GPU_flag=1, precision="c128", 
 
 
 mv_AN_const = MVP
+
+
+def _precisions(precisions):
+    m = 0
+    for p in precisions:
+        m |= L.VS_BUILD_C64 if p == "c64" else L.VS_BUILD_C128
+    return m
+
+
+def circ_levels(opToeplitz, Lx, My, Nz, want_blocks=True, ctx=None):
+    """(circ_L_opToep, circ_M_opToep, blocks[L,M,3N,3N]) computed on the device."""
+    ctx = ctx or default_context()
+    t = L.cplx_flat(opToeplitz)
+    V = Lx * My * Nz
+    c1 = np.zeros(6 * V, dtype=np.complex128)
+    c2 = np.zeros(6 * V, dtype=np.complex128)
+    n = 3 * Nz
+    blk = np.zeros(Lx * My * n * n, dtype=np.complex128) if want_blocks else None
+    L.check(ctx._lib.vs_circ_levels(ctx.h, Lx, My, Nz, L.dptr(t), L.dptr(c1), L.dptr(c2),
+                                    L.dptr(blk) if want_blocks else None), ctx.h)
+    shp = (Lx, My, Nz, 6)
+    blocks = None
+    if want_blocks:
+        # block b = i + L*j, each column-major n x n  ->  [i, j, p, q]
+        blocks = blk.reshape(My, Lx, n, n).transpose(1, 0, 3, 2)
+    return c1.reshape(shp, order="F"), c2.reshape(shp, order="F"), blocks
+
+
+def circ_1_level(opToeplitz, Lx, My, Nz, parallel_prec=0, on_off="off", ctx=None):
+    """[circ, circ_L_opToep] = circ_1_level(...) with on_off = 'off' (circ_1_level.m:1-93)."""
+    if on_off != "off":
+        raise NotImplementedError("dense 1-level blocks (on_off='on') are not built on the device")
+    c1, _, _ = circ_levels(opToeplitz, Lx, My, Nz, want_blocks=False, ctx=ctx)
+    return None, c1
+
+
+def circ_2_level(circ_L_opToep, Lx, My, Nz, opToeplitz=None, ctx=None):
+    """[circ_M_opToep, circ] = circ_2_level(circ_L_opToep, L, M, N).
+
+    The device pipeline starts from the Toeplitz tensor (both levels in one
+    call); pass it as ``opToeplitz``.  ``circ`` is returned as an
+    (L, M, 3N, 3N) array (the reference's cell{L,M})."""
+    if opToeplitz is None:
+        raise ValueError("the device path needs the Toeplitz tensor (opToeplitz=...)")
+    _, c2, blocks = circ_levels(opToeplitz, Lx, My, Nz, want_blocks=True, ctx=ctx)
+    return c2, blocks
+
+
+class Preconditioner:
+    """Handle on a device 2-level circulant preconditioner (y = M^-1 x)."""
+
+    def __init__(self, op=None, shift=None, d=None, inv_blocks=None, LMN=None, idx3=None,
+                 precisions=("c64", "c128"), ctx=None):
+        h = C.c_void_p()
+        mask = _precisions(precisions)
+        if op is not None:
+            self.ctx = op.ctx
+            sh = np.array([complex(shift)], dtype=np.complex128)
+            dd = np.ascontiguousarray(np.atleast_1d(np.asarray(d, dtype=np.complex128)).ravel())
+            L.check(self.ctx._lib.vs_prec_create(op.h, L.dptr(sh), L.dptr(dd), dd.size, mask, C.byref(h)), self.ctx.h)
+            self.n3 = op.n3
+        else:
+            self.ctx = ctx or default_context()
+            Lx, My, Nz = LMN
+            n = 3 * Nz
+            # [i, j, p, q] -> block i + L*j, column-major
+            flat = np.ascontiguousarray(np.asarray(inv_blocks, dtype=np.complex128).transpose(1, 0, 3, 2).ravel())
+            idx = np.ascontiguousarray(np.asarray(idx3, dtype=np.int64).ravel())
+            L.check(self.ctx._lib.vs_prec_create_blocks(self.ctx.h, Lx, My, Nz, L.dptr(flat),
+                                                        idx.ctypes.data_as(L._pi64), idx.size, mask, C.byref(h)),
+                    self.ctx.h)
+            self.n3 = idx.size
+        self.h = h
+
+    def apply(self, x, precision="c64"):
+        x = np.ascontiguousarray(np.asarray(x, dtype=np.complex128))
+        nrhs = x.size // self.n3
+        y = np.empty_like(x)
+        L.check(self.ctx._lib.vs_prec_apply(self.h, L.dptr(x), L.dptr(y), nrhs,
+                                            L.VS_C64 if precision == "c64" else L.VS_C128), self.ctx.h)
+        return y
+
+    def blocks(self, Lx, My, Nz, precision="c128"):
+        n = 3 * Nz
+        out = np.zeros(Lx * My * n * n, dtype=np.complex128)
+        L.check(self.ctx._lib.vs_prec_get_blocks(self.h, L.VS_C64 if precision == "c64" else L.VS_C128,
+                                                 L.dptr(out)), self.ctx.h)
+        return out.reshape(My, Lx, n, n).transpose(1, 0, 3, 2)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx._lib.vs_prec_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mvp_circ_2_level(inv_blocks, JIn, Lx, My, Nz, idx, precision="c128", ctx=None):
+    """mvp = mvp_circ_2_level(inv_blocks, JIn, L, M, N, idx) with inv_blocks as an
+    (L, M, 3N, 3N) array."""
+    pr = Preconditioner(inv_blocks=inv_blocks, LMN=(Lx, My, Nz), idx3=idx,
+                        precisions=(precision,), ctx=ctx)
+    try:
+        return pr.apply(JIn, precision)
+    finally:
+        pr.close()
+
+
+def solve(op, b, prec=None, tol=1e-6, maxit=2000, precision="mixed", x0=None, inner_tol=0.0, max_refine=10,
+          iters_per_graph=4, want_resvec=True):
+    """Device Krylov solve; returns (x, info dict, resvec)."""
+    lib = op.ctx._lib
+    b = np.ascontiguousarray(np.asarray(b, dtype=np.complex128).ravel())
+    x = np.zeros_like(b) if x0 is None else np.ascontiguousarray(np.asarray(x0, dtype=np.complex128).ravel()).copy()
+    o = L.vs_solve_opts()
+    lib.vs_solve_opts_default(C.byref(o))
+    o.precision = L.VS_SOLVE_MIXED if precision == "mixed" else L.VS_SOLVE_FP64
+    o.tol = float(tol); o.maxit = int(maxit); o.inner_tol = float(inner_tol); o.max_refine = int(max_refine)
+    o.iters_per_graph = int(iters_per_graph)
+    rv = np.zeros(4 * int(maxit) + 64 if want_resvec else 1)
+    if want_resvec:
+        o.resvec = L.dptr(rv); o.resvec_cap = rv.size
+    info = L.vs_solve_info()
+    L.check(lib.vs_solve(op.h, prec.h if prec is not None else None, L.dptr(b), L.dptr(x), C.byref(o),
+                         C.byref(info)), op.ctx.h)
+    d = dict(flag=info.flag, relres=info.relres, iter=info.iter, refinements=info.refinements,
+             time_ms=info.time_ms)
+    return x, d, rv[:info.n_resvec].copy()
+
+
+def bicgstab(A, b, tol=1e-6, maxit=20, M1=None, M2=None, x0=None, precision="mixed"):
+    """[x, flag, relres, iter, resvec] = bicgstab(A, b, tol, maxit, M1, M2, x0)
+    with A an Operator and M1 a Preconditioner (M2 must be None).  resvec holds
+    absolute residual norms at every half step, like MATLAB's."""
+    if M2 is not None:
+        raise NotImplementedError("a second preconditioner factor is not supported")
+    x, info, rv = solve(A, b, prec=M1, tol=tol, maxit=maxit, precision=precision, x0=x0)
+    nb = np.linalg.norm(np.asarray(b))
+    return x, info["flag"], info["relres"], info["iter"], rv * nb

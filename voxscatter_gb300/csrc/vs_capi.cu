@@ -2,6 +2,8 @@
 // arguments, runs on the context's stream and converts exceptions into a
 // status code plus a message readable through vs_last_error().
 #include "vs_internal.h"
+#include "vs_krylov.h"
+#include <chrono>
 #include <complex>
 #include <cstring>
 #include <cmath>
@@ -122,6 +124,50 @@ void spectrum_from_full(vs_op* op, const double2* full) {
   op->G32.alloc(6 * PQR * sizeof(float2));
   vs::finalize_spectrum(full, 6 * PQR, 1.0 / (double)PQR, op->G64.as<double2>(), op->G32.as<float2>(),
                         op->ctx->stream);
+}
+
+// Column-major caller blocks -> row-major device blocks (scaled), and back.
+__global__ void k_blocks_in(const double2* __restrict__ in, int64_t nblk, int n, double scale, double2* o64,
+                            float2* o32) {
+  const int64_t tot = nblk * n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / ((int64_t)n * n);
+    const int64_t r = e - b * n * n;
+    const int p = (int)(r / n), q = (int)(r - (int64_t)p * n);  // row-major destination (p, q)
+    const double2 a = in[b * n * n + (int64_t)q * n + p];      // column-major source
+    const double2 v = make_double2(a.x * scale, a.y * scale);
+    if (o64) o64[e] = v;
+    if (o32) o32[e] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+__global__ void k_blocks_out(const double2* __restrict__ i64, const float2* __restrict__ i32, int64_t nblk, int n,
+                             double scale, double2* __restrict__ out) {
+  const int64_t tot = nblk * n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / ((int64_t)n * n);
+    const int64_t r = e - b * n * n;
+    const int q = (int)(r / n), p = (int)(r - (int64_t)q * n);  // column-major destination (p, q)
+    const int64_t src = b * n * n + (int64_t)p * n + q;
+    const double2 a = i64 ? i64[src] : make_double2(i32[src].x, i32[src].y);
+    out[e] = make_double2(a.x * scale, a.y * scale);
+  }
+}
+
+void prec_common_impl(vs_prec* pr, int precisions) {
+  VS_REQUIRE(precisions >= 1 && precisions <= 3, "precisions must be VS_BUILD_C64 and/or VS_BUILD_C128");
+  cudaStream_t st = pr->ctx->stream;
+  pr->axL.init(pr->L, st);
+  pr->axM.init(pr->M, st);
+  pr->t.alloc((size_t)pr->L * pr->M * pr->N * 3 * sizeof(double2));
+  pr->nrhs_cap = 1;
+}
+
+void prec_scratch_impl(vs_prec* pr, int64_t nrhs) {
+  if (nrhs > pr->nrhs_cap) {
+    pr->t.alloc((size_t)pr->L * pr->M * pr->N * 3 * sizeof(double2) * nrhs);
+    pr->nrhs_cap = (int)nrhs;
+  }
 }
 
 }  // namespace
@@ -367,6 +413,285 @@ int vs_op_apply(vs_op* op, const double* x, double* y, int64_t nrhs, int mode, i
       VS_CUDA(cudaMemcpyAsync(y, op->yout.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
       VS_CUDA(cudaStreamSynchronize(st));
     }
+  });
+}
+
+// ---- preconditioner ---------------------------------------------------
+
+int vs_circ_levels(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* toep, double* circL_out,
+                   double* circM_out, double* blocks_out) {
+  if (!ctx) return VS_ERR_ARG;
+  return guarded(ctx, [&] {
+    check_grid(L, M, N);
+    VS_REQUIRE(toep, "toep is NULL");
+    cudaStream_t st = ctx->stream;
+    const int64_t V = L * M * N;
+    vs::DevBuf dt, l1, l2, blk, status;
+    dt.alloc(6 * V * sizeof(double2));
+    l1.alloc(6 * V * sizeof(double2));
+    l2.alloc(6 * V * sizeof(double2));
+    VS_CUDA(cudaMemcpyAsync(dt.p, toep, 6 * V * sizeof(double2), cudaMemcpyHostToDevice, st));
+    vs::FftAxis axL, axM;
+    axL.init((int)L, st);
+    axM.init((int)M, st);
+    vs::circ_levels_device((int)L, (int)M, (int)N, dt.as<double2>(), l1.as<double2>(), l2.as<double2>(), axL, axM, st);
+    if (circL_out) VS_CUDA(cudaMemcpyAsync(circL_out, l1.p, 6 * V * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    if (circM_out) {
+      VS_CUDA(cudaMemcpyAsync(circM_out, l2.p, 6 * V * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    }
+    if (blocks_out) {
+      const int64_t n = 3 * N;
+      blk.alloc(L * M * n * n * sizeof(double2));
+      status.alloc(sizeof(int));
+      VS_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), st));
+      vs::assemble_invert<double>(l2.as<double2>(), (int)L, (int)M, (int)N, make_double2(0, 0), nullptr,
+                                  make_double2(-1, 0), false, true, 1.0, blk.as<double2>(), status.as<int>(), st);
+      VS_CUDA(cudaMemcpyAsync(blocks_out, blk.p, L * M * n * n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    }
+    VS_CUDA(cudaStreamSynchronize(st));
+    if (circM_out) {  // circ_2_level.m:44 stores -CC3 for the xz component
+      double* c3 = circM_out + 2 * 2 * V;
+      for (int64_t e = 0; e < 2 * V; ++e) c3[e] = -c3[e];
+    }
+  });
+}
+
+
+int vs_prec_create(vs_op* op, const double* shift, const double* d, int64_t nd, int precisions, vs_prec** out) {
+  if (!op) return VS_ERR_ARG;
+  vs_prec* pr = nullptr;
+  int s = guarded(op->ctx, [&] {
+    VS_REQUIRE(shift && d && out, "NULL argument");
+    VS_REQUIRE(nd == 1 || nd == 3 * (int64_t)op->N, "d must have 1 or 3N entries");
+    pr = new vs_prec();
+    pr->ctx = op->ctx;
+    pr->L = op->L; pr->M = op->M; pr->N = op->N;
+    pr->V = op->V; pr->n3 = op->n3;
+    cudaStream_t st = op->ctx->stream;
+    pr->map3.alloc(3 * op->V * sizeof(int));
+    VS_CUDA(cudaMemcpyAsync(pr->map3.p, op->map3.p, 3 * op->V * sizeof(int), cudaMemcpyDeviceToDevice, st));
+    prec_common_impl(pr, precisions);
+    const int64_t V = op->V, n = 3 * op->N, LM = (int64_t)op->L * op->M;
+    vs::DevBuf l1, l2, dv, status;
+    l1.alloc(6 * V * sizeof(double2));
+    l2.alloc(6 * V * sizeof(double2));
+    status.alloc(sizeof(int));
+    VS_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), st));
+    vs::circ_levels_device(op->L, op->M, op->N, op->toep64.as<double2>(), l1.as<double2>(), l2.as<double2>(), pr->axL,
+                           pr->axM, st);
+    const double2 sh = make_double2(shift[0], shift[1]);
+    double2 ds = make_double2(d[0], d[1]);
+    const double2* dptr = nullptr;
+    if (nd > 1) {
+      dv.alloc(nd * sizeof(double2));
+      VS_CUDA(cudaMemcpyAsync(dv.p, d, nd * sizeof(double2), cudaMemcpyHostToDevice, st));
+      dptr = dv.as<double2>();
+    }
+    const double scale = 1.0 / (double)LM;
+    if (precisions & VS_BUILD_C64) {
+      pr->inv32.alloc(LM * n * n * sizeof(float2));
+      vs::assemble_invert<float>(l2.as<double2>(), op->L, op->M, op->N, sh, dptr, ds, true, false, scale,
+                                 pr->inv32.as<float2>(), status.as<int>(), st);
+    }
+    if (precisions & VS_BUILD_C128) {
+      pr->inv64.alloc(LM * n * n * sizeof(double2));
+      vs::assemble_invert<double>(l2.as<double2>(), op->L, op->M, op->N, sh, dptr, ds, true, false, scale,
+                                  pr->inv64.as<double2>(), status.as<int>(), st);
+    }
+    int hs = 0;
+    VS_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+    VS_REQUIRE(hs == 0, "a preconditioner block is singular or its inverse is not finite");
+    *out = pr;
+  });
+  if (s != VS_OK) delete pr;
+  return s;
+}
+
+int vs_prec_create_blocks(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* inv_blocks,
+                          const int64_t* idx3, int64_t n3, int precisions, vs_prec** out) {
+  if (!ctx) return VS_ERR_ARG;
+  vs_prec* pr = nullptr;
+  int s = guarded(ctx, [&] {
+    check_grid(L, M, N);
+    VS_REQUIRE(inv_blocks && idx3 && out, "NULL argument");
+    pr = new vs_prec();
+    pr->ctx = ctx;
+    pr->L = (int)L; pr->M = (int)M; pr->N = (int)N;
+    pr->V = L * M * N;
+    cudaStream_t st = ctx->stream;
+    const int64_t V = pr->V;
+    VS_REQUIRE(n3 >= 1 && n3 <= 3 * V, "n3 must be in [1, 3*L*M*N]");
+    std::vector<int> map3(3 * V, -1);
+    for (int64_t e = 0; e < n3; ++e) {
+      const int64_t g = idx3[e];
+      VS_REQUIRE(g >= 0 && g < 3 * V, "idx3 entry out of range [0, 3*L*M*N)");
+      VS_REQUIRE(map3[g] < 0, "idx3 has a repeated entry");
+      map3[g] = (int)e;
+    }
+    pr->n3 = n3;
+    pr->map3.alloc(3 * V * sizeof(int));
+    VS_CUDA(cudaMemcpyAsync(pr->map3.p, map3.data(), 3 * V * sizeof(int), cudaMemcpyHostToDevice, st));
+    prec_common_impl(pr, precisions);
+    const int64_t n = 3 * N, LM = L * M;
+    vs::DevBuf raw;
+    raw.alloc(LM * n * n * sizeof(double2));
+    VS_CUDA(cudaMemcpyAsync(raw.p, inv_blocks, LM * n * n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    if (precisions & VS_BUILD_C64) pr->inv32.alloc(LM * n * n * sizeof(float2));
+    if (precisions & VS_BUILD_C128) pr->inv64.alloc(LM * n * n * sizeof(double2));
+    const int64_t tot = LM * n * n;
+    k_blocks_in<<<(int)std::min<int64_t>(vs::ceil_div(tot, 256), 152 * 32), 256, 0, st>>>(
+        raw.as<double2>(), LM, (int)n, 1.0 / (double)LM, (precisions & VS_BUILD_C128) ? pr->inv64.as<double2>() : nullptr,
+        (precisions & VS_BUILD_C64) ? pr->inv32.as<float2>() : nullptr);
+    VS_LAUNCH_CHECK();
+    VS_CUDA(cudaStreamSynchronize(st));
+    *out = pr;
+  });
+  if (s != VS_OK) delete pr;
+  return s;
+}
+
+int vs_prec_destroy(vs_prec* prec) {
+  if (!prec) return VS_OK;
+  int s = guarded(prec->ctx, [&] { VS_CUDA(cudaStreamSynchronize(prec->ctx->stream)); });
+  delete prec;
+  return s;
+}
+
+
+int vs_prec_apply_device(vs_prec* prec, const void* x, void* y, int64_t nrhs, int precision) {
+  if (!prec) return VS_ERR_ARG;
+  return guarded(prec->ctx, [&] {
+    VS_REQUIRE(x && y, "NULL argument");
+    VS_REQUIRE(nrhs >= 1 && nrhs <= 65535, "nrhs must be in [1, 65535]");
+    VS_REQUIRE(precision == VS_C64 || precision == VS_C128, "bad precision");
+    prec_scratch_impl(prec, nrhs);
+    cudaStream_t st = prec->ctx->stream;
+    if (precision == VS_C64) vs::prec_apply<float>(*prec, (const float2*)x, (float2*)y, (int)nrhs, nullptr, st);
+    else vs::prec_apply<double>(*prec, (const double2*)x, (double2*)y, (int)nrhs, nullptr, st);
+  });
+}
+
+int vs_prec_apply(vs_prec* prec, const double* x, double* y, int64_t nrhs, int precision) {
+  if (!prec) return VS_ERR_ARG;
+  return guarded(prec->ctx, [&] {
+    VS_REQUIRE(x && y, "NULL argument");
+    VS_REQUIRE(nrhs >= 1 && nrhs <= 65535, "nrhs must be in [1, 65535]");
+    VS_REQUIRE(precision == VS_C64 || precision == VS_C128, "bad precision");
+    prec_scratch_impl(prec, nrhs);
+    cudaStream_t st = prec->ctx->stream;
+    const int64_t n = prec->n3 * nrhs;
+    prec->xin.alloc(n * sizeof(double2));
+    prec->yout.alloc(n * sizeof(double2));
+    VS_CUDA(cudaMemcpyAsync(prec->xin.p, x, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    if (precision == VS_C64) {
+      vs::DevBuf x32, y32;
+      x32.alloc(n * sizeof(float2));
+      y32.alloc(n * sizeof(float2));
+      vs::c128_to_c64(prec->xin.as<double2>(), x32.as<float2>(), n, st);
+      vs::prec_apply<float>(*prec, x32.as<float2>(), y32.as<float2>(), (int)nrhs, nullptr, st);
+      vs::c64_to_c128(y32.as<float2>(), prec->yout.as<double2>(), n, st);
+      VS_CUDA(cudaMemcpyAsync(y, prec->yout.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+      VS_CUDA(cudaStreamSynchronize(st));
+    } else {
+      vs::prec_apply<double>(*prec, prec->xin.as<double2>(), prec->yout.as<double2>(), (int)nrhs, nullptr, st);
+      VS_CUDA(cudaMemcpyAsync(y, prec->yout.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+      VS_CUDA(cudaStreamSynchronize(st));
+    }
+  });
+}
+
+int vs_prec_get_blocks(vs_prec* prec, int precision, double* out) {
+  if (!prec) return VS_ERR_ARG;
+  return guarded(prec->ctx, [&] {
+    VS_REQUIRE(out, "NULL argument");
+    VS_REQUIRE((precision == VS_C64 && prec->inv32.p) || (precision == VS_C128 && prec->inv64.p),
+               "preconditioner not built in that precision");
+    cudaStream_t st = prec->ctx->stream;
+    const int64_t n = 3 * prec->N, LM = (int64_t)prec->L * prec->M;
+    vs::DevBuf o;
+    o.alloc(LM * n * n * sizeof(double2));
+    k_blocks_out<<<(int)std::min<int64_t>(vs::ceil_div(LM * n * n, 256), 152 * 32), 256, 0, st>>>(
+        precision == VS_C128 ? prec->inv64.as<double2>() : nullptr,
+        precision == VS_C64 ? prec->inv32.as<float2>() : nullptr, LM, (int)n, (double)LM, o.as<double2>());
+    VS_LAUNCH_CHECK();
+    VS_CUDA(cudaMemcpyAsync(out, o.p, LM * n * n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+// ---- solve --------------------------------------------------------------
+
+void vs_solve_opts_default(vs_solve_opts* o) {
+  if (!o) return;
+  o->method = VS_BICGSTAB;
+  o->precision = VS_SOLVE_MIXED;
+  o->tol = 1e-6;
+  o->maxit = 2000;
+  o->inner_tol = 0;
+  o->max_refine = 10;
+  o->iters_per_graph = 4;
+  o->resvec = nullptr;
+  o->resvec_cap = 0;
+}
+
+static void solve_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, const vs_solve_opts* o,
+                       vs_solve_info* info) {
+  VS_REQUIRE(o && info, "NULL argument");
+  VS_REQUIRE(o->method == VS_BICGSTAB, "unsupported method");
+  VS_REQUIRE(o->precision == VS_SOLVE_MIXED || o->precision == VS_SOLVE_FP64, "bad precision");
+  VS_REQUIRE(o->tol > 0 && o->maxit >= 0 && o->iters_per_graph >= 1 && o->iters_per_graph <= 64, "bad options");
+  VS_REQUIRE(!prec || (prec->L == op->L && prec->M == op->M && prec->N == op->N && prec->n3 == op->n3),
+             "preconditioner does not match the operator");
+  VS_REQUIRE(!prec || (o->precision == VS_SOLVE_MIXED ? prec->inv32.p != nullptr : prec->inv64.p != nullptr),
+             "preconditioner not built in the precision this solve needs");
+  vs::SolveParams prm;
+  prm.mode = o->precision;
+  prm.tol = o->tol;
+  prm.maxit = o->maxit;
+  prm.inner_tol = o->inner_tol;
+  prm.max_refine = o->max_refine;
+  prm.per_graph = o->iters_per_graph;
+  prm.resvec_cap = (int)std::min<int64_t>(o->resvec ? o->resvec_cap : 0, 1 << 30);
+  prm.resvec_host = o->resvec;
+  if (prec) {
+    const int64_t need = (int64_t)prec->L * prec->M * prec->N * 3 * sizeof(double2);
+    if ((int64_t)prec->t.bytes < need) prec->t.alloc(need);
+  }
+  vs::SolveResult r;
+  vs::solve_bicgstab(*op, prec, b, x, prm, r, op->ctx->stream);
+  info->flag = r.flag;
+  info->relres = r.relres;
+  info->iter = r.iter;
+  info->refinements = r.refinements;
+  info->n_resvec = r.n_resvec;
+}
+
+int vs_solve_device(vs_op* op, vs_prec* prec, const void* b, void* x, const vs_solve_opts* opts, vs_solve_info* info) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(b && x, "NULL argument");
+    const auto t0 = std::chrono::steady_clock::now();
+    solve_impl(op, prec, (const double2*)b, (double2*)x, opts, info);
+    info->time_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  });
+}
+
+int vs_solve(vs_op* op, vs_prec* prec, const double* b, double* x, const vs_solve_opts* opts, vs_solve_info* info) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(b && x, "NULL argument");
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t st = op->ctx->stream;
+    const int64_t n = op->n3;
+    op->xin.alloc(n * sizeof(double2));
+    op->yout.alloc(n * sizeof(double2));
+    VS_CUDA(cudaMemcpyAsync(op->xin.p, b, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemcpyAsync(op->yout.p, x, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    solve_impl(op, prec, op->xin.as<double2>(), op->yout.as<double2>(), opts, info);
+    VS_CUDA(cudaMemcpyAsync(x, op->yout.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+    info->time_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   });
 }
 

@@ -76,4 +76,23 @@ struct Error : std::runtime_error {
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
+// Raise a kernel's dynamic shared-memory limit once (not per launch, so that
+// launches captured into CUDA graphs issue no attribute calls).
+inline void set_kernel_smem(const void* kernel, size_t bytes) {
+  if (bytes > 227 * 1024)
+    throw Error(VS_ERR_UNSUPPORTED, "kernel tile needs " + std::to_string(bytes) + " bytes of shared memory (> 227 KB)");
+  if (bytes <= 48 * 1024) return;
+  struct Entry { const void* k; int dev; size_t bytes; };
+  static thread_local Entry cache[64];
+  static thread_local int ncache = 0;
+  int dev = 0;
+  VS_CUDA(cudaGetDevice(&dev));
+  for (int i = 0; i < ncache; ++i)
+    if (cache[i].k == kernel && cache[i].dev == dev && cache[i].bytes >= bytes) return;
+  VS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  for (int i = 0; i < ncache; ++i)
+    if (cache[i].k == kernel && cache[i].dev == dev) { cache[i].bytes = bytes; return; }
+  if (ncache < 64) cache[ncache++] = Entry{kernel, dev, bytes};
+}
+
 }  // namespace vs

@@ -41,6 +41,14 @@ struct FftAxis {
 template <> inline const float2* FftAxis::tw<float>() const { return tw32.as<float2>(); }
 template <> inline const double2* FftAxis::tw<double>() const { return tw64.as<double2>(); }
 
+// Work vectors and device scalars of the Krylov solvers (vs_krylov.cu).
+struct KrylovWork {
+  DevBuf r, rt, p, v_, s, t, ph, sh, x;  // in the inner solver's precision
+  DevBuf r64, y64;                       // FP64 residual / matvec output
+  DevBuf partials, state, scal, resvec;
+  template <typename T> void ensure(int64_t n);
+};
+
 }  // namespace vs
 
 struct vs_ctx {
@@ -72,6 +80,20 @@ struct vs_op {
   vs::FftAxis ax[3];
   vs::DevBuf t1, t2;    // pipeline intermediates
   vs::DevBuf xin, yout; // device staging for host-buffer applies
+  vs::KrylovWork kw;    // solver state for vs_solve on this operator
+};
+
+// 2-level circulant preconditioner: inverse blocks per (x,y) frequency.
+struct vs_prec {
+  vs_ctx* ctx = nullptr;
+  int L = 0, M = 0, N = 0;
+  int64_t V = 0, n3 = 0;
+  vs::DevBuf map3;          // int32[3V] unknown position of each grid entry (-1: absent)
+  vs::DevBuf inv32, inv64;  // L*M blocks of (3N)^2, row-major, scaled by 1/(L*M)
+  vs::FftAxis axL, axM;
+  vs::DevBuf t;             // apply scratch (L,M,N,3) per right-hand side
+  vs::DevBuf xin, yout;
+  int nrhs_cap = 0;
 };
 
 namespace vs {
@@ -98,6 +120,15 @@ void toep_from_fN_device(int L, int M, int N, int P, int Q, int R, double2* fN_i
                          FftAxis* ax, cudaStream_t st);
 void finalize_spectrum(const double2* fN, int64_t total, double scale, double2* g64, float2* g32,
                        cudaStream_t st);
+
+// Preconditioner (vs_precond.cu)
+void circ_levels_device(int L, int M, int N, const double2* toep, double2* lev1, double2* lev2, const FftAxis& axL,
+                        const FftAxis& axM, cudaStream_t st);
+template <typename T>
+void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, const double2* dvec, double2 dscal,
+                     bool invert, bool colmajor, double scale, cplx_t<T>* out, int* status, cudaStream_t st);
+template <typename T>
+void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip, cudaStream_t st);
 
 // Elementwise helpers (vs_matvec.cu)
 void c128_to_c64(const double2* in, float2* out, int64_t n, cudaStream_t st);

@@ -1,0 +1,583 @@
+// Krylov solvers on the device.
+//
+// BiCGSTAB (van der Vorst 1992, preconditioned form of Barrett et al. 1994)
+// with MATLAB bicgstab's conventions (main_DDA.m:82,120): the preconditioner
+// applies M^-1, convergence is tested on the recurrence residual at every half
+// step, iter may be a half integer, resvec holds ||r|| at every half step.
+// All scalars (rho, alpha, omega, norms) live in device memory and are formed
+// by deterministic two-level reductions (per-CTA partials summed in a fixed
+// order by the last CTA to finish) with FP64 accumulation, so one iteration is
+// a fixed launch sequence that is captured once in a CUDA graph; a device
+// `skip` flag turns every launch into a no-op once the iteration has converged
+// or broken down, and the host polls the state once per graph launch.
+//
+// Mixed precision: the inner solve runs on the c64 pipeline; an outer loop
+// forms the true residual r = b - A x with the c128 pipeline and compensated
+// (Ogita-Rump-Oishi Dot2) FP64 norms, solves A d = r/||r|| in c64 and updates
+// x += ||r|| d in FP64 until ||r||/||b|| <= tol.
+#include "vs_krylov.h"
+
+#include <chrono>
+#include <cmath>
+#include <vector>
+
+namespace vs {
+
+constexpr int kRedThreads = 256;
+constexpr int kRedBlocks = 2 * 152;
+
+// FP64 double-double accumulation (TwoSum / TwoProd by fma) for the c128 path.
+struct DD {
+  double hi, lo;
+};
+__device__ __forceinline__ DD dd_add(DD a, double b) {
+  const double s = a.hi + b;
+  const double bb = s - a.hi;
+  const double err = (a.hi - (s - bb)) + (b - bb);
+  return DD{s, a.lo + err};
+}
+__device__ __forceinline__ DD dd_add(DD a, DD b) {
+  DD r = dd_add(a, b.hi);
+  r.lo += b.lo;
+  return r;
+}
+__device__ __forceinline__ DD dd_fma(DD a, double x, double y) {
+  const double p = x * y;
+  const double e = fma(x, y, -p);
+  DD r = dd_add(a, p);
+  r.lo += e;
+  return r;
+}
+
+// Accumulators: float inputs accumulate exactly-rounded products in double.
+template <typename T>
+struct Acc {
+  double re = 0, im = 0;
+  __device__ __forceinline__ void dot(cplx_t<T> u, cplx_t<T> v) {  // += conj(u) v
+    re = fma((double)u.x, (double)v.x, re);
+    re = fma((double)u.y, (double)v.y, re);
+    im = fma((double)u.x, (double)v.y, im);
+    im = fma(-(double)u.y, (double)v.x, im);
+  }
+  __device__ __forceinline__ void norm2(cplx_t<T> u) {
+    re = fma((double)u.x, (double)u.x, re);
+    re = fma((double)u.y, (double)u.y, re);
+  }
+  __device__ __forceinline__ double2 value() const { return make_double2(re, im); }
+};
+template <>
+struct Acc<double> {
+  DD re{0, 0}, im{0, 0};
+  __device__ __forceinline__ void dot(double2 u, double2 v) {
+    re = dd_fma(re, u.x, v.x);
+    re = dd_fma(re, u.y, v.y);
+    im = dd_fma(im, u.x, v.y);
+    im = dd_fma(im, -u.y, v.x);
+  }
+  __device__ __forceinline__ void norm2(double2 u) {
+    re = dd_fma(re, u.x, u.x);
+    re = dd_fma(re, u.y, u.y);
+  }
+  __device__ __forceinline__ double2 value() const { return make_double2(re.hi + re.lo, im.hi + im.lo); }
+};
+
+// Block reduction of NV doubles; returns true in the last CTA to finish, with
+// the grid totals in `tot` (all threads of that CTA).  Partials are summed in
+// CTA order, so the result does not depend on scheduling.
+template <int NV>
+__device__ bool grid_reduce(double (&v)[NV], double* __restrict__ partials, unsigned* __restrict__ counter,
+                            double (&tot)[NV]) {
+  __shared__ double sm[NV][kRedThreads / 32];
+  __shared__ bool s_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = v[k];
+#pragma unroll
+    for (int off = 16; off; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    if (lane == 0) sm[k][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double x = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) x += sm[k][w];
+      partials[blockIdx.x * NV + k] = x;
+    }
+    __threadfence();
+    const unsigned t = atomicAdd(counter, 1u);
+    s_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = 0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) x += ((volatile double*)partials)[b * NV + k];
+#pragma unroll
+    for (int off = 16; off; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    if (lane == 0) sm[k][warp] = x;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) x += sm[k][w];
+    tot[k] = x;
+  }
+  if (threadIdx.x == 0) *counter = 0;
+  return true;
+}
+
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  const double d = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+__device__ __forceinline__ bool cz(double2 a) { return a.x == 0.0 && a.y == 0.0; }
+__device__ __forceinline__ bool cfinite(double2 a) { return isfinite(a.x) && isfinite(a.y); }
+
+#define GRID_LOOP(i, n) for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+// rho = rt^H r ; beta = (rho/rho_prev)(alpha/omega)
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_bicg_rho(const cplx_t<T>* rt, const cplx_t<T>* r, int64_t n, KState* s) {
+  if (s->skip) return;
+  Acc<T> a;
+  GRID_LOOP(i, n) a.dot(rt[i], r[i]);
+  double v[2] = {a.value().x, a.value().y}, t[2];
+  if (grid_reduce<2>(v, s->partials, &s->counter, t) && threadIdx.x == 0) {
+    const double2 rho = make_double2(t[0], t[1]);
+    if (cz(rho) || !cfinite(rho)) {
+      s->flag = cfinite(rho) ? 4 : 5;
+      s->skip = 1;
+      return;
+    }
+    if (s->iter2 > 0) s->beta = cmul(cdiv(rho, s->rho_prev), cdiv(s->alpha, s->omega));
+    s->rho = rho;
+  }
+}
+
+// p = r (first iteration) or r + beta (p - omega v)
+template <typename T>
+__global__ void k_bicg_p(cplx_t<T>* p, const cplx_t<T>* r, const cplx_t<T>* v, int64_t n, const KState* s) {
+  using C = cplx_t<T>;
+  if (s->skip) return;
+  if (s->iter2 == 0) {
+    GRID_LOOP(i, n) p[i] = r[i];
+    return;
+  }
+  const C beta = ccast<C>(s->beta), om = ccast<C>(s->omega);
+  GRID_LOOP(i, n) p[i] = cfma(beta, csub(p[i], cmul(om, v[i])), r[i]);
+}
+
+// alpha = rho / (rt^H v)
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_bicg_alpha(const cplx_t<T>* rt, const cplx_t<T>* v, int64_t n, KState* s) {
+  if (s->skip) return;
+  Acc<T> a;
+  GRID_LOOP(i, n) a.dot(rt[i], v[i]);
+  double w[2] = {a.value().x, a.value().y}, t[2];
+  if (grid_reduce<2>(w, s->partials, &s->counter, t) && threadIdx.x == 0) {
+    const double2 d = make_double2(t[0], t[1]);
+    if (cz(d) || !cfinite(d)) {
+      s->flag = cfinite(d) ? 4 : 5;
+      s->skip = 1;
+      return;
+    }
+    s->alpha = cdiv(s->rho, d);
+  }
+}
+
+// s = r - alpha v ; ||s|| ; half-step convergence test
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_bicg_s(cplx_t<T>* sv, const cplx_t<T>* r, const cplx_t<T>* v, int64_t n, KState* s) {
+  using C = cplx_t<T>;
+  if (s->skip) return;
+  const C al = ccast<C>(s->alpha);
+  Acc<T> a;
+  GRID_LOOP(i, n) {
+    const C x = csub(r[i], cmul(al, v[i]));
+    sv[i] = x;
+    a.norm2(x);
+  }
+  double w[1] = {a.value().x}, t[1];
+  if (grid_reduce<1>(w, s->partials, &s->counter, t) && threadIdx.x == 0) {
+    const double res = sqrt(t[0]);
+    const int k = s->iter2 + 1;
+    if (k < s->resvec_cap) s->resvec[k] = res * s->res_scale;
+    s->nres = k + 1;
+    s->res = res;
+    if (!isfinite(res)) {
+      s->flag = 5;
+      s->skip = 1;
+    } else if (res <= s->tol_abs) {
+      s->half_pending = 1;
+      s->flag = 0;
+      s->iter2 = k;
+      s->skip = 1;
+    }
+  }
+}
+
+// x += alpha ph when the half step converged (runs regardless of skip).
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_bicg_xhalf(cplx_t<T>* x, const cplx_t<T>* ph, int64_t n, KState* s) {
+  using C = cplx_t<T>;
+  __shared__ int s_go;
+  __shared__ bool s_last;
+  if (threadIdx.x == 0) s_go = s->half_pending;
+  __syncthreads();
+  if (!s_go) return;
+  const C al = ccast<C>(s->alpha);
+  GRID_LOOP(i, n) x[i] = cfma(al, ph[i], x[i]);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned t = atomicAdd(&s->counter, 1u);
+    s_last = (t == gridDim.x - 1);
+    if (s_last) {
+      s->half_pending = 0;
+      s->counter = 0;
+    }
+  }
+}
+
+// omega = (t^H s)/(t^H t)
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_bicg_omega(const cplx_t<T>* t, const cplx_t<T>* sv, int64_t n, KState* s) {
+  if (s->skip) return;
+  Acc<T> a, b;
+  GRID_LOOP(i, n) {
+    a.dot(t[i], sv[i]);
+    b.norm2(t[i]);
+  }
+  double w[3] = {a.value().x, a.value().y, b.value().x}, tt[3];
+  if (grid_reduce<3>(w, s->partials, &s->counter, tt) && threadIdx.x == 0) {
+    const double2 ts = make_double2(tt[0], tt[1]);
+    const double t2 = tt[2];
+    if (!(t2 > 0) || !cfinite(ts)) {
+      s->flag = (t2 == 0) ? 4 : 5;
+      s->skip = 1;
+      return;
+    }
+    const double2 om = make_double2(ts.x / t2, ts.y / t2);
+    if (cz(om)) {
+      s->flag = 4;
+      s->skip = 1;
+      return;
+    }
+    s->omega = om;
+  }
+}
+
+// x += alpha ph + omega sh ; r = s - omega t ; ||r|| ; full-step test
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* x, cplx_t<T>* r, const cplx_t<T>* ph, const cplx_t<T>* sh,
+                                                        const cplx_t<T>* sv, const cplx_t<T>* t, int64_t n, KState* s) {
+  using C = cplx_t<T>;
+  if (s->skip) return;
+  const C al = ccast<C>(s->alpha), om = ccast<C>(s->omega);
+  Acc<T> a;
+  GRID_LOOP(i, n) {
+    x[i] = cfma(om, sh[i], cfma(al, ph[i], x[i]));
+    const C ri = csub(sv[i], cmul(om, t[i]));
+    r[i] = ri;
+    a.norm2(ri);
+  }
+  double w[1] = {a.value().x}, tt[1];
+  if (grid_reduce<1>(w, s->partials, &s->counter, tt) && threadIdx.x == 0) {
+    const double res = sqrt(tt[0]);
+    const int k = s->iter2 + 2;
+    if (k < s->resvec_cap) s->resvec[k] = res * s->res_scale;
+    s->nres = k + 1;
+    s->iter2 = k;
+    s->res = res;
+    s->rho_prev = s->rho;
+    if (!isfinite(res)) {
+      s->flag = 5;
+      s->skip = 1;
+    } else if (res <= s->tol_abs) {
+      s->flag = 0;
+      s->skip = 1;
+    } else if (k >= 2 * s->maxit) {
+      s->flag = 1;
+      s->skip = 1;
+    }
+  }
+}
+
+// ||u||^2 into s->aux (and u^H v optional) -- used for the initial residual.
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_norm(const cplx_t<T>* u, int64_t n, KState* s, double* out) {
+  Acc<T> a;
+  GRID_LOOP(i, n) a.norm2(u[i]);
+  double w[1] = {a.value().x}, t[1];
+  if (grid_reduce<1>(w, s->partials, &s->counter, t) && threadIdx.x == 0) *out = sqrt(t[0]);
+}
+
+template <typename T>
+__global__ void k_copy(cplx_t<T>* dst, const cplx_t<T>* src, int64_t n) {
+  GRID_LOOP(i, n) dst[i] = src[i];
+}
+template <typename T>
+__global__ void k_zero(cplx_t<T>* dst, int64_t n) {
+  GRID_LOOP(i, n) dst[i] = czero<cplx_t<T>>();
+}
+
+// r64 = b - y64 and its compensated norm
+__global__ void __launch_bounds__(kRedThreads) k_resid64(const double2* b, const double2* y, double2* r, int64_t n, KState* s,
+                                                        double* out) {
+  Acc<double> a;
+  GRID_LOOP(i, n) {
+    const double2 v = csub(b[i], y[i]);
+    r[i] = v;
+    a.norm2(v);
+  }
+  double w[1] = {a.value().x}, t[1];
+  if (grid_reduce<1>(w, s->partials, &s->counter, t) && threadIdx.x == 0) *out = sqrt(t[0]);
+}
+
+// r32 = r64 * sc
+__global__ void k_scale_down(const double2* r, float2* o, int64_t n, double sc) {
+  GRID_LOOP(i, n) o[i] = make_float2((float)(r[i].x * sc), (float)(r[i].y * sc));
+}
+// x64 += sc * d32
+__global__ void k_update64(double2* x, const float2* d, int64_t n, double sc) {
+  GRID_LOOP(i, n) {
+    x[i].x = fma(sc, (double)d[i].x, x[i].x);
+    x[i].y = fma(sc, (double)d[i].y, x[i].y);
+  }
+}
+
+static int vec_grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), kRedBlocks)); }
+
+// ---- host driver ---------------------------------------------------------
+
+template <typename T>
+void KrylovWork::ensure(int64_t n) {
+  using C = cplx_t<T>;
+  const size_t b = n * sizeof(C);
+  DevBuf* v[] = {&r, &rt, &p, &v_, &s, &t, &ph, &sh, &x};
+  for (DevBuf* d : v) d->alloc(b);
+}
+
+static void upload_state(KState* d, const KState& h, cudaStream_t st) {
+  VS_CUDA(cudaMemcpyAsync(d, &h, sizeof(KState), cudaMemcpyHostToDevice, st));
+}
+
+// One BiCGSTAB iteration (two half steps) as a fixed launch sequence.
+template <typename T>
+static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KState* s, int64_t n, cudaStream_t st) {
+  using C = cplx_t<T>;
+  C* r = w.r.as<C>();
+  C* rt = w.rt.as<C>();
+  C* p = w.p.as<C>();
+  C* v = w.v_.as<C>();
+  C* sv = w.s.as<C>();
+  C* t = w.t.as<C>();
+  C* ph = w.ph.as<C>();
+  C* sh = w.sh.as<C>();
+  C* x = w.x.as<C>();
+  const int g = vec_grid(n);
+  const int* skip = &s->skip;
+  k_bicg_rho<T><<<g, kRedThreads, 0, st>>>(rt, r, n, s);
+  k_bicg_p<T><<<g, 256, 0, st>>>(p, r, v, n, s);
+  if (pr) prec_apply<T>(*pr, p, ph, 1, skip, st);
+  else k_copy<T><<<g, 256, 0, st>>>(ph, p, n);
+  matvec<T>(op, ph, v, 1, VS_NOTRANSP, skip, st);
+  k_bicg_alpha<T><<<g, kRedThreads, 0, st>>>(rt, v, n, s);
+  k_bicg_s<T><<<g, kRedThreads, 0, st>>>(sv, r, v, n, s);
+  k_bicg_xhalf<T><<<g, kRedThreads, 0, st>>>(x, ph, n, s);
+  if (pr) prec_apply<T>(*pr, sv, sh, 1, skip, st);
+  else k_copy<T><<<g, 256, 0, st>>>(sh, sv, n);
+  matvec<T>(op, sh, t, 1, VS_NOTRANSP, skip, st);
+  k_bicg_omega<T><<<g, kRedThreads, 0, st>>>(t, sv, n, s);
+  k_bicg_xr<T><<<g, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, n, s);
+  VS_LAUNCH_CHECK();
+}
+
+// Runs BiCGSTAB on w.x (initial guess already there) for A x = w.r0-based
+// system: the caller has put the initial residual in w.r.  Returns the final
+// state.  Iterations are launched as a CUDA graph of `per_graph` iterations.
+template <typename T>
+static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t n, double bnorm, double tol,
+                            int maxit, double res_scale, double* resvec_dev, int resvec_cap, int per_graph,
+                            cudaStream_t st) {
+  using C = cplx_t<T>;
+  KState h{};
+  h.tol_abs = tol * bnorm;
+  h.maxit = maxit;
+  h.res_scale = res_scale;
+  h.resvec = resvec_dev;
+  h.resvec_cap = resvec_cap;
+  h.partials = w.partials.as<double>();
+  h.flag = 1;
+  KState* s = w.state.as<KState>();
+  // r0 norm
+  upload_state(s, h, st);
+  const int g = vec_grid(n);
+  k_copy<T><<<g, 256, 0, st>>>(w.rt.as<C>(), w.r.as<C>(), n);
+  k_norm<T><<<g, kRedThreads, 0, st>>>(w.r.as<C>(), n, s, w.scal.as<double>());
+  double r0 = 0;
+  VS_CUDA(cudaMemcpyAsync(&r0, w.scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+  VS_CUDA(cudaStreamSynchronize(st));
+  if (resvec_dev && resvec_cap > 0) {
+    const double v0 = r0 * res_scale;
+    VS_CUDA(cudaMemcpyAsync(resvec_dev, &v0, sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  h.res = r0;
+  h.nres = 1;
+  if (!(r0 > h.tol_abs) || maxit <= 0) {
+    h.flag = (r0 <= h.tol_abs) ? 0 : 1;
+    return h;
+  }
+  // One launch sequence with skip set, outside capture: every kernel returns at
+  // once, but first-use attribute calls happen here rather than in the capture.
+  {
+    KState idle = h;
+    idle.skip = 1;
+    upload_state(s, idle, st);
+    bicg_iteration<T>(op, pr, w, s, n, st);
+  }
+  upload_state(s, h, st);
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  VS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  try {
+    for (int k = 0; k < per_graph; ++k) bicg_iteration<T>(op, pr, w, s, n, st);
+  } catch (...) {
+    cudaStreamEndCapture(st, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    throw;
+  }
+  VS_CUDA(cudaStreamEndCapture(st, &graph));
+  VS_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  KState cur{};
+  const int max_launch = (maxit + per_graph - 1) / per_graph + 1;
+  for (int it = 0; it < max_launch; ++it) {
+    VS_CUDA(cudaGraphLaunch(exec, st));
+    VS_CUDA(cudaMemcpyAsync(&cur, s, sizeof(KState), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+    if (cur.skip) break;
+  }
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  if (!cur.skip) cur.flag = 1;
+  return cur;
+}
+
+static double norm64(KrylovWork& w, const double2* u, int64_t n, cudaStream_t st) {
+  KState* s = w.state.as<KState>();
+  k_norm<double><<<vec_grid(n), kRedThreads, 0, st>>>(u, n, s, w.scal.as<double>());
+  VS_LAUNCH_CHECK();
+  double h = 0;
+  VS_CUDA(cudaMemcpyAsync(&h, w.scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+  VS_CUDA(cudaStreamSynchronize(st));
+  return h;
+}
+
+// r64 = b - A x64 (c128 pipeline); returns ||r64||.
+static double residual64(const vs_op& op, KrylovWork& w, const double2* b, const double2* x, double2* r, int64_t n,
+                         cudaStream_t st) {
+  KState* s = w.state.as<KState>();
+  double2* y = w.y64.as<double2>();
+  matvec<double>(op, x, y, 1, VS_NOTRANSP, nullptr, st);
+  k_resid64<<<vec_grid(n), kRedThreads, 0, st>>>(b, y, r, n, s, w.scal.as<double>());
+  VS_LAUNCH_CHECK();
+  double h = 0;
+  VS_CUDA(cudaMemcpyAsync(&h, w.scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+  VS_CUDA(cudaStreamSynchronize(st));
+  return h;
+}
+
+void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
+                    cudaStream_t st) {
+  const int64_t n = op.n3;
+  KrylovWork& w = op.kw;
+  w.partials.alloc(kRedBlocks * 4 * sizeof(double));
+  w.state.alloc(sizeof(KState));
+  w.scal.alloc(4 * sizeof(double));
+  VS_CUDA(cudaMemsetAsync(w.partials.p, 0, kRedBlocks * 4 * sizeof(double), st));
+  KState zero{};
+  zero.partials = w.partials.as<double>();  // every reduction needs its partial-sum buffer
+  upload_state(w.state.as<KState>(), zero, st);
+  const int cap = prm.resvec_cap;
+  w.resvec.alloc(std::max(1, cap) * sizeof(double));
+  double* rv = cap > 0 ? w.resvec.as<double>() : nullptr;
+  ensure_scratch(op, 1, sizeof(double2));
+  const double bnorm = norm64(w, b, n, st);
+  if (!std::isfinite(bnorm)) throw Error(VS_ERR_NONFINITE, "right-hand side has NaN or Inf entries");
+  out = SolveResult{};
+  if (bnorm == 0) {
+    VS_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double2), st));
+    VS_CUDA(cudaStreamSynchronize(st));
+    out.flag = 0;
+    return;
+  }
+  if (prm.mode == VS_SOLVE_FP64) {
+    w.ensure<double>(n);
+    w.y64.alloc(n * sizeof(double2));
+    // x0 -> w.x ; r = b - A x0
+    k_copy<double><<<vec_grid(n), 256, 0, st>>>(w.x.as<double2>(), x, n);
+    residual64(op, w, b, x, w.r.as<double2>(), n, st);
+    KState fs = bicgstab_core<double>(op, pr, w, n, bnorm, prm.tol, prm.maxit, 1.0 / bnorm, rv, cap, prm.per_graph, st);
+    k_copy<double><<<vec_grid(n), 256, 0, st>>>(x, w.x.as<double2>(), n);
+    VS_LAUNCH_CHECK();
+    out.flag = fs.flag;
+    out.iter = fs.iter2 * 0.5;
+    out.inner_iters = fs.iter2 * 0.5;
+    out.n_resvec = std::min<int64_t>(fs.nres, cap);
+    const double rn = residual64(op, w, b, x, w.r.as<double2>(), n, st);
+    out.relres = rn / bnorm;
+    if (out.flag == 0 && out.relres > prm.tol) out.flag = 1;
+  } else {
+    // mixed: c64 inner BiCGSTAB inside FP64 refinement
+    w.ensure<float>(n);
+    w.y64.alloc(n * sizeof(double2));
+    w.r64.alloc(n * sizeof(double2));
+    double2* r64 = w.r64.as<double2>();
+    double rn = residual64(op, w, b, x, r64, n, st);
+    int inner_total2 = 0;
+    int64_t nres = 0;
+    int flag = 1;
+    int refine = 0;
+    for (; refine <= prm.max_refine; ++refine) {
+      if (rn <= prm.tol * bnorm) {
+        flag = 0;
+        break;
+      }
+      if (refine == prm.max_refine || inner_total2 >= 2 * prm.maxit) break;
+      double itol = prm.inner_tol > 0 ? prm.inner_tol : std::max(0.5 * prm.tol * bnorm / rn, prm.inner_floor);
+      itol = std::min(itol, 0.5);
+      k_scale_down<<<vec_grid(n), 256, 0, st>>>(r64, w.r.as<float2>(), n, 1.0 / rn);
+      k_zero<float><<<vec_grid(n), 256, 0, st>>>(w.x.as<float2>(), n);
+      VS_LAUNCH_CHECK();
+      double* rvk = (rv && nres < cap) ? rv + nres : nullptr;
+      const int capk = rv ? (int)(cap - nres) : 0;
+      KState fs = bicgstab_core<float>(op, pr, w, n, 1.0, itol, prm.maxit - inner_total2 / 2, rn / bnorm, rvk, capk,
+                                       prm.per_graph, st);
+      inner_total2 += fs.iter2;
+      nres += std::min<int64_t>(fs.nres, capk);
+      if (fs.flag >= 4 && fs.iter2 == 0) {
+        flag = fs.flag;
+        break;
+      }
+      k_update64<<<vec_grid(n), 256, 0, st>>>(x, w.x.as<float2>(), n, rn);
+      VS_LAUNCH_CHECK();
+      rn = residual64(op, w, b, x, r64, n, st);
+    }
+    out.flag = (rn <= prm.tol * bnorm) ? 0 : (flag >= 4 ? flag : 1);
+    out.relres = rn / bnorm;
+    out.iter = inner_total2 * 0.5;
+    out.inner_iters = inner_total2 * 0.5;
+    out.refinements = refine;
+    out.n_resvec = nres;
+  }
+  if (cap > 0 && prm.resvec_host && out.n_resvec > 0)
+    VS_CUDA(cudaMemcpyAsync(prm.resvec_host, rv, out.n_resvec * sizeof(double), cudaMemcpyDeviceToHost, st));
+  VS_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace vs

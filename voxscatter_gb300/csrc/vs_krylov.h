@@ -1,0 +1,40 @@
+// Device Krylov state and solver entry (vs_krylov.cu).
+#pragma once
+#include "vs_internal.h"
+
+namespace vs {
+
+
+// Scalars of one Krylov iteration, resident in device memory.
+struct KState {
+  double2 rho, rho_prev, alpha, omega, beta;
+  double tol_abs, res, res_scale;
+  double* partials;
+  double* resvec;
+  unsigned counter;
+  int skip, flag, half_pending, iter2, maxit, nres, resvec_cap;
+};
+
+struct SolveParams {
+  int mode = 0;  // 0 mixed, 1 fp64
+  double tol = 1e-6;
+  int maxit = 2000;
+  double inner_tol = 0;  // 0: automatic
+  double inner_floor = 1e-6;
+  int max_refine = 10;
+  int per_graph = 4;
+  int resvec_cap = 0;
+  double* resvec_host = nullptr;
+};
+
+struct SolveResult {
+  int flag = 1;
+  double relres = 0, iter = 0, inner_iters = 0;
+  int refinements = 0;
+  int64_t n_resvec = 0;
+};
+
+void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
+                    cudaStream_t st);
+
+}  // namespace vs

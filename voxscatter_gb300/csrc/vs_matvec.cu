@@ -13,7 +13,7 @@
 // All passes are templated on the real type (float: c64 pipeline, double: c128)
 // and take an optional device flag `skip` so that a graph of Krylov steps can
 // turn itself into no-ops after convergence.
-#include "vs_internal.h"
+#include "vs_pipeline.cuh"
 
 namespace vs {
 
@@ -31,34 +31,6 @@ void FftAxis::init(int n, cudaStream_t st) {
   VS_CUDA(cudaMemcpyAsync(tw32.p, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice, st));
   VS_CUDA(cudaStreamSynchronize(st));
 }
-
-template <typename C>
-struct DiagArg {
-  const C* v;
-  C s;
-  __device__ __forceinline__ C at(int pos) const { return v ? v[pos] : s; }
-};
-
-template <typename T>
-struct PipeArgs {
-  using C = cplx_t<T>;
-  int L, M, N, P, Q, R;
-  int64_t V, n3;
-  const int* map3;
-  const C* x;
-  C* y;
-  DiagArg<C> d1, d1c, d2;
-  C* t1;
-  C* t2;
-  const C* G;
-  const C* twP;
-  const C* twQ;
-  const C* twR;
-  FftPlan pP, pQ, pR;
-  int lpb;  // lines per block in the x passes
-  int tx;   // x-tile width of the y and z passes
-  const int* skip;
-};
 
 // ---- pass XF: gather + forward FFT along x ------------------------------
 template <typename T, int MODE>
@@ -133,32 +105,15 @@ __global__ void __launch_bounds__(kThreads) k_xi(PipeArgs<T> a) {
     const int pos = __ldg(a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L + i);
     if (pos < 0) continue;
     const C conv = res[l * a.P + i];
-    const C xv = x[pos];
+    const C xv = (MODE == MODE_PLAIN) ? conv : x[pos];
     C out;
     if (MODE == VS_NOTRANSP) out = csub(cmul(a.d1.at(pos), xv), cmul(a.d2.at(pos), conv));
     else if (MODE == VS_TRANSP) out = csub(cmul(a.d1.at(pos), xv), conv);
-    else out = csub(cmul(a.d1c.at(pos), xv), cconj(conv));
+    else if (MODE == VS_CONJTRANSP) out = csub(cmul(a.d1c.at(pos), xv), cconj(conv));
+    else out = conv;
     y[pos] = out;
   }
 }
-
-// ---- strided-axis pass (y of the pipeline; y and z of the setup FFTs) ----
-// Lines run along a strided axis; a CTA owns an x-tile of `tx` columns of one
-// plane.  Element (x, row) of plane (pa, pb) of the source is at
-//   src + pa*s_a + pb*s_b + row*s_row + x      (same form for the destination).
-// Rows [0, n_in) are loaded (zero pad up to n), rows [0, n_out) are stored.
-template <typename T>
-struct StridedArgs {
-  using C = cplx_t<T>;
-  const C* src;
-  C* dst;
-  int xext, n_in, n_out, tx, na;
-  int64_t s_row, s_a, s_b, s_rhs;
-  int64_t d_row, d_a, d_b, d_rhs;
-  FftPlan plan;
-  const C* tw;
-  const int* skip;
-};
 
 template <typename T, bool INV>
 __global__ void __launch_bounds__(kThreads) k_strided(StridedArgs<T> a) {
@@ -255,9 +210,7 @@ static int pick_tile(int n, size_t csize, int width_mult) {
 
 template <typename K>
 static void set_smem(K kernel, size_t bytes) {
-  if (bytes > 227 * 1024)
-    throw Error(VS_ERR_UNSUPPORTED, "FFT tile needs " + std::to_string(bytes) + " bytes of shared memory (> 227 KB)");
-  if (bytes > 48 * 1024) VS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  set_kernel_smem((const void*)kernel, bytes);
 }
 
 void ensure_scratch(vs_op& op, int nrhs, size_t elem_bytes) {
@@ -268,7 +221,7 @@ void ensure_scratch(vs_op& op, int nrhs, size_t elem_bytes) {
 }
 
 template <typename T>
-static void launch_x(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaStream_t st) {
+void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaStream_t st) {
   const int nlines = a.M * a.N * 3;
   dim3 grid(ceil_div(nlines, a.lpb), nrhs);
   const size_t smem = 2ull * a.lpb * a.P * sizeof(cplx_t<T>);
@@ -281,18 +234,20 @@ static void launch_x(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cud
   if (!inverse) {
     if (mode == VS_NOTRANSP) VS_X(k_xf, VS_NOTRANSP)
     else if (mode == VS_TRANSP) VS_X(k_xf, VS_TRANSP)
-    else VS_X(k_xf, VS_CONJTRANSP)
+    else if (mode == VS_CONJTRANSP) VS_X(k_xf, VS_CONJTRANSP)
+    else VS_X(k_xf, MODE_PLAIN)
   } else {
     if (mode == VS_NOTRANSP) VS_X(k_xi, VS_NOTRANSP)
     else if (mode == VS_TRANSP) VS_X(k_xi, VS_TRANSP)
-    else VS_X(k_xi, VS_CONJTRANSP)
+    else if (mode == VS_CONJTRANSP) VS_X(k_xi, VS_CONJTRANSP)
+    else VS_X(k_xi, MODE_PLAIN)
   }
 #undef VS_X
   VS_LAUNCH_CHECK();
 }
 
 template <typename T, bool INV>
-static void launch_strided(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st) {
+void launch_strided_pass(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st) {
   dim3 grid(ceil_div(a.xext, a.tx), nplanes, nrhs);
   const size_t smem = 2ull * a.plan.n * a.tx * sizeof(cplx_t<T>);
   auto k = k_strided<T, INV>;
@@ -343,8 +298,8 @@ void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mod
   a.lpb = std::max(1, 2048 / op.P);
   a.tx = pick_tile(op.R, sizeof(C), 3);
   a.skip = skip;
-  launch_x<T>(a, false, mode, nrhs, st);
-  launch_strided<T, false>(y_pass_args<T>(op, a, false), op.N * 3, nrhs, st);
+  launch_x_pass<T>(a, false, mode, nrhs, st);
+  launch_strided_pass<T, false>(y_pass_args<T>(op, a, false), op.N * 3, nrhs, st);
   {
     dim3 grid(ceil_div(op.P, a.tx), op.Q, nrhs);
     const size_t smem = 2ull * op.R * 3 * a.tx * sizeof(C);
@@ -353,9 +308,16 @@ void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mod
     k<<<grid, kThreads, smem, st>>>(a);
     VS_LAUNCH_CHECK();
   }
-  launch_strided<T, true>(y_pass_args<T>(op, a, true), op.N * 3, nrhs, st);
-  launch_x<T>(a, true, mode, nrhs, st);
+  launch_strided_pass<T, true>(y_pass_args<T>(op, a, true), op.N * 3, nrhs, st);
+  launch_x_pass<T>(a, true, mode, nrhs, st);
 }
+
+template void launch_x_pass<float>(const PipeArgs<float>&, bool, int, int, cudaStream_t);
+template void launch_x_pass<double>(const PipeArgs<double>&, bool, int, int, cudaStream_t);
+template void launch_strided_pass<float, false>(const StridedArgs<float>&, int, int, cudaStream_t);
+template void launch_strided_pass<float, true>(const StridedArgs<float>&, int, int, cudaStream_t);
+template void launch_strided_pass<double, false>(const StridedArgs<double>&, int, int, cudaStream_t);
+template void launch_strided_pass<double, true>(const StridedArgs<double>&, int, int, cudaStream_t);
 
 template void matvec<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t);
 template void matvec<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t);
@@ -404,7 +366,7 @@ void fft_strided(cplx_t<T>* data, int xext, int n, int64_t row_stride, int na, i
   s.plan = ax.plan;
   s.tw = ax.tw<T>();
   s.skip = nullptr;
-  launch_strided<T, INV>(s, na * nb, 1, st);
+  launch_strided_pass<T, INV>(s, na * nb, 1, st);
 }
 
 template void fft_axis0<double, false>(double2*, int, int64_t, const FftAxis&, cudaStream_t);

@@ -1,0 +1,62 @@
+// Argument blocks of the FFT passes shared by the matvec and the circulant
+// preconditioner (kernels live in vs_matvec.cu).
+#pragma once
+#include "vs_internal.h"
+
+namespace vs {
+
+// Extra X-pass mode beyond vs_mode: plain gather / plain scatter (no diagonal).
+constexpr int MODE_PLAIN = 3;
+
+template <typename C>
+struct DiagArg {
+  const C* v;
+  C s;
+  __device__ __forceinline__ C at(int pos) const { return v ? v[pos] : s; }
+};
+
+template <typename T>
+struct PipeArgs {
+  using C = cplx_t<T>;
+  int L, M, N, P, Q, R;
+  int64_t V, n3;
+  const int* map3;
+  const C* x;
+  C* y;
+  DiagArg<C> d1, d1c, d2;
+  C* t1;
+  C* t2;
+  const C* G;
+  const C* twP;
+  const C* twQ;
+  const C* twR;
+  FftPlan pP, pQ, pR;
+  int lpb;  // lines per block in the x passes
+  int tx;   // x-tile width of the y and z passes
+  const int* skip;
+};
+
+// ---- strided-axis pass (y of the pipeline; y and z of the setup FFTs) ----
+// Lines run along a strided axis; a CTA owns an x-tile of `tx` columns of one
+// plane.  Element (x, row) of plane (pa, pb) of the source is at
+//   src + pa*s_a + pb*s_b + row*s_row + x      (same form for the destination).
+// Rows [0, n_in) are loaded (zero pad up to n), rows [0, n_out) are stored.
+template <typename T>
+struct StridedArgs {
+  using C = cplx_t<T>;
+  const C* src;
+  C* dst;
+  int xext, n_in, n_out, tx, na;
+  int64_t s_row, s_a, s_b, s_rhs;
+  int64_t d_row, d_a, d_b, d_rhs;
+  FftPlan plan;
+  const C* tw;
+  const int* skip;
+};
+
+template <typename T>
+void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaStream_t st);
+template <typename T, bool INV>
+void launch_strided_pass(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st);
+
+}  // namespace vs

@@ -1,0 +1,297 @@
+// Chan-Olkin 2-level circulant preconditioner on the device.
+//
+// Build (FP64 up to the inversion):
+//   level 1: T. Chan optimal-circulant average along x + FFT_x   (circ_1_level.m:5-90)
+//   level 2: the same along y + FFT_y                              (circ_2_level.m:5-80)
+//   blocks : per (i,j) the 3N x 3N matrix of N x N Toeplitz pieces  (circ_2_level.m:82-154)
+//            shifted as shift*I - diag(d)*C                        (main_DDA.m:109,
+//                                                                   scatteringHumanHead.m:181)
+//            and inverted by Gauss-Jordan with partial pivoting in shared memory,
+//            in FP32 (mixed path) and/or FP64.
+// Apply (mvp_circ_2_level.m:4-22): gather + FFT_x, FFT_y, block GEMV, IFFT_y,
+// IFFT_x + scatter.  The 1/(L*M) of the two inverse FFTs is folded into the
+// stored inverse blocks.
+#include "vs_pipeline.cuh"
+
+namespace vs {
+
+// sign of the (n+1-i)/n term per component, circ_1_level.m:14,29,42,55,69,84
+__constant__ int c_s1[6] = {+1, -1, -1, +1, +1, +1};
+// same for circ_2_level.m:14,27,38,51,63,76
+__constant__ int c_s2[6] = {+1, -1, +1, +1, -1, +1};
+
+__global__ void k_chan_x(const double2* __restrict__ A, double2* __restrict__ out, int L, int M, int N) {
+  const int64_t V = (int64_t)L * M * N;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 6 * V; e += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(e / V);
+    const int i = (int)((e - c * V) % L);
+    double2 r;
+    if (i == 0) {
+      r = A[e];
+    } else {
+      const double w1 = c_s1[c] * (double)(L - i) / L, w2 = (double)i / L;
+      const double2 a = A[e], b = A[e - i + (L - i)];
+      r = make_double2(w1 * a.x + w2 * b.x, w1 * a.y + w2 * b.y);
+    }
+    out[e] = r;
+  }
+}
+
+__global__ void k_chan_y(const double2* __restrict__ A, double2* __restrict__ out, int L, int M, int N) {
+  const int64_t V = (int64_t)L * M * N;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 6 * V; e += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(e / V);
+    const int j = (int)(((e - c * V) / L) % M);
+    double2 r;
+    if (j == 0) {
+      r = A[e];
+    } else {
+      const double w1 = c_s2[c] * (double)(M - j) / M, w2 = (double)j / M;
+      const double2 a = A[e], b = A[e + (int64_t)(M - 2 * j) * L];
+      r = make_double2(w1 * a.x + w2 * b.x, w1 * a.y + w2 * b.y);
+    }
+    out[e] = r;
+  }
+}
+
+void circ_levels_device(int L, int M, int N, const double2* toep, double2* lev1, double2* lev2, const FftAxis& axL,
+                        const FftAxis& axM, cudaStream_t st) {
+  const int64_t V = (int64_t)L * M * N;
+  const int blocks = (int)std::min<int64_t>(ceil_div(6 * V, 256), 152 * 32);
+  k_chan_x<<<blocks, 256, 0, st>>>(toep, lev1, L, M, N);
+  VS_LAUNCH_CHECK();
+  fft_axis0<double, false>(lev1, L, (int64_t)M * N * 6, axL, st);
+  k_chan_y<<<blocks, 256, 0, st>>>(lev1, lev2, L, M, N);
+  VS_LAUNCH_CHECK();
+  fft_strided<double, false>(lev2, L, M, L, N * 6, (int64_t)L * M, 1, 0, axM, st);
+}
+
+__device__ __forceinline__ int comp_pair(int a, int b) {
+  const int t[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+  return t[a][b];
+}
+
+__host__ __device__ __forceinline__ float2 crecip(float2 a) {
+  const float d = a.x * a.x + a.y * a.y;
+  return make_float2(a.x / d, -a.y / d);
+}
+__host__ __device__ __forceinline__ double2 crecip(double2 a) {
+  const double d = a.x * a.x + a.y * a.y;
+  return make_double2(a.x / d, -a.y / d);
+}
+
+// One CTA per block (i, j) = (blockIdx.x, blockIdx.y).  With invert = false
+// the assembled matrix is stored as is (used to return circ_2_level's blocks).
+template <typename T>
+__global__ void __launch_bounds__(256) k_assemble_invert(const double2* __restrict__ lev2, int L, int M, int N,
+                                                         double2 shift, const double2* __restrict__ dvec,
+                                                         double2 dscal, int invert, int colmajor, double scale,
+                                                         cplx_t<T>* __restrict__ out, int* __restrict__ status) {
+  using C = cplx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = 3 * N;
+  C* A = reinterpret_cast<C*>(smem_raw);
+  C* colk = A + n * n;
+  int* perm = reinterpret_cast<int*>(colk + n);
+  __shared__ int s_piv;
+  __shared__ T s_pmag;
+  const int i = blockIdx.x, j = blockIdx.y;
+  for (int u = threadIdx.x; u < n * n; u += blockDim.x) {
+    const int p = u / n, q = u - p * n;
+    const int a = p / N, zp = p - a * N, b = q / N, zq = q - b * N;
+    const int c = comp_pair(a, b);
+    const bool negcol = (a == 2) != (b == 2);
+    int dz = zp - zq;
+    double sg = 1.0;
+    if (dz < 0) dz = -dz;
+    else if (negcol && dz > 0) sg = -1.0;
+    const double2 v = lev2[i + (int64_t)L * (j + (int64_t)M * (dz + (int64_t)N * c))];
+    const double2 dd = dvec ? dvec[p] : dscal;
+    double2 e = cmul(dd, v);
+    e.x *= -sg;
+    e.y *= -sg;
+    if (p == q) { e.x += shift.x; e.y += shift.y; }
+    A[u] = ccast<C>(e);
+  }
+  __syncthreads();
+  if (invert) {
+    for (int k = 0; k < n; ++k) {
+      if (threadIdx.x < 32) {
+        T best = -1;
+        int bi = k;
+        for (int r = k + threadIdx.x; r < n; r += 32) {
+          const C a = A[r * n + k];
+          const T m = a.x * a.x + a.y * a.y;
+          if (m > best) { best = m; bi = r; }
+        }
+        for (int off = 16; off; off >>= 1) {
+          const T ob = __shfl_xor_sync(0xffffffffu, best, off);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+          if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (threadIdx.x == 0) {
+          s_piv = bi;
+          s_pmag = best;
+          perm[k] = bi;
+        }
+      }
+      __syncthreads();
+      const int p = s_piv;
+      if (threadIdx.x == 0 && !(s_pmag > 0)) atomicOr(status, 1);
+      if (p != k) {
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+          const C t = A[k * n + q];
+          A[k * n + q] = A[p * n + q];
+          A[p * n + q] = t;
+        }
+      }
+      __syncthreads();
+      for (int r = threadIdx.x; r < n; r += blockDim.x) colk[r] = A[r * n + k];
+      __syncthreads();
+      const C rinv = crecip(colk[k]);
+      for (int q = threadIdx.x; q < n; q += blockDim.x) A[k * n + q] = (q == k) ? rinv : cmul(A[k * n + q], rinv);
+      __syncthreads();
+      for (int u = threadIdx.x; u < n * n; u += blockDim.x) {
+        const int r = u / n;
+        if (r == k) continue;
+        const int q = u - r * n;
+        const C base = (q == k) ? czero<C>() : A[u];
+        A[u] = csub(base, cmul(colk[r], A[k * n + q]));
+      }
+      __syncthreads();
+    }
+    for (int k = n - 1; k >= 0; --k) {
+      const int p = perm[k];
+      if (p != k) {
+        for (int r = threadIdx.x; r < n; r += blockDim.x) {
+          const C t = A[r * n + k];
+          A[r * n + k] = A[r * n + p];
+          A[r * n + p] = t;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  C* o = out + ((int64_t)i + (int64_t)L * j) * n * n;
+  for (int u = threadIdx.x; u < n * n; u += blockDim.x) {
+    const int p = u / n, q = u - p * n;
+    const C a = A[u];
+    if (!(isfinite(a.x) && isfinite(a.y))) atomicOr(status, 2);
+    o[colmajor ? q * n + p : u] = cscale(a, (T)scale);
+  }
+}
+
+size_t assemble_smem(int N, size_t csize) {
+  const int n = 3 * N;
+  return (size_t)n * n * csize + n * csize + n * sizeof(int) + 16;
+}
+
+template <typename T>
+void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, const double2* dvec, double2 dscal,
+                     bool invert, bool colmajor, double scale, cplx_t<T>* out, int* status, cudaStream_t st) {
+  const size_t smem = assemble_smem(N, sizeof(cplx_t<T>));
+  if (smem > 227 * 1024)
+    throw Error(VS_ERR_UNSUPPORTED, "3N x 3N block of " + std::to_string(3 * N) + " does not fit in shared memory");
+  auto k = k_assemble_invert<T>;
+  set_kernel_smem((const void*)k, smem);
+  k<<<dim3(L, M), 256, smem, st>>>(lev2, L, M, N, shift, dvec, dscal, invert ? 1 : 0, colmajor ? 1 : 0, scale, out,
+                                   status);
+  VS_LAUNCH_CHECK();
+}
+template void assemble_invert<float>(const double2*, int, int, int, double2, const double2*, double2, bool, bool,
+                                     double, float2*, int*, cudaStream_t);
+template void assemble_invert<double>(const double2*, int, int, int, double2, const double2*, double2, bool, bool,
+                                      double, double2*, int*, cudaStream_t);
+
+// ---- apply: block GEMV on the (x,y)-frequency planes --------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_block_gemv(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ inv, int L,
+                                                    int M, int N, int ti, int64_t rhs_stride, const int* skip) {
+  using C = cplx_t<T>;
+  if (skip && *skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = 3 * N;
+  C* v = reinterpret_cast<C*>(smem_raw);
+  C* o = v + ti * n;
+  const int i0 = blockIdx.x * ti, j = blockIdx.y;
+  C* tt = t + (int64_t)blockIdx.z * rhs_stride;
+  const int64_t LM = (int64_t)L * M;
+  for (int u = threadIdx.x; u < ti * n; u += blockDim.x) {
+    const int s = u / ti, il = u - s * ti;
+    const int i = i0 + il;
+    // s = comp*N + z  ->  grid entry (i, j, z, comp)
+    v[il * n + s] = (i < L) ? tt[i + (int64_t)L * j + LM * s] : czero<C>();
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int rr = warp; rr < ti * n; rr += nw) {
+    const int il = rr / n, r = rr - il * n;
+    const int i = i0 + il;
+    if (i >= L) continue;
+    const C* row = inv + (((int64_t)i + (int64_t)L * j) * n + r) * n;
+    C acc = czero<C>();
+    for (int s = lane; s < n; s += 32) acc = cfma(__ldg(row + s), v[il * n + s], acc);
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, off);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, off);
+    }
+    if (lane == 0) o[il * n + r] = acc;
+  }
+  __syncthreads();
+  for (int u = threadIdx.x; u < ti * n; u += blockDim.x) {
+    const int s = u / ti, il = u - s * ti;
+    const int i = i0 + il;
+    if (i < L) tt[i + (int64_t)L * j + LM * s] = o[il * n + s];
+  }
+}
+
+template <typename T>
+void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip, cudaStream_t st) {
+  using C = cplx_t<T>;
+  const int L = pr.L, M = pr.M, N = pr.N;
+  const C* inv = std::is_same<T, float>::value ? (const C*)pr.inv32.p : (const C*)pr.inv64.p;
+  VS_REQUIRE(inv != nullptr, "preconditioner was not built in this precision");
+  C* t = (C*)pr.t.p;
+  PipeArgs<T> a{};
+  a.L = L; a.M = M; a.N = N; a.P = L; a.Q = M; a.R = N;
+  a.V = pr.V; a.n3 = pr.n3;
+  a.map3 = pr.map3.as<int>();
+  a.x = x; a.y = y;
+  a.t1 = t; a.t2 = t;
+  a.twP = pr.axL.tw<T>();
+  a.pP = pr.axL.plan;
+  a.lpb = std::max(1, 2048 / L);
+  a.skip = skip;
+  launch_x_pass<T>(a, false, MODE_PLAIN, nrhs, st);
+  StridedArgs<T> s{};
+  s.src = t; s.dst = t;
+  s.xext = L; s.n_in = M; s.n_out = M;
+  int tx = 32;
+  while (tx > 1 && 2ull * M * tx * sizeof(C) > 100 * 1024) tx >>= 1;
+  s.tx = tx;
+  s.na = 3 * N;
+  s.s_row = s.d_row = L;
+  s.s_a = s.d_a = (int64_t)L * M;
+  s.s_b = s.d_b = 0;
+  s.s_rhs = s.d_rhs = (int64_t)L * M * N * 3;
+  s.plan = pr.axM.plan;
+  s.tw = pr.axM.tw<T>();
+  s.skip = skip;
+  launch_strided_pass<T, false>(s, 3 * N, nrhs, st);
+  {
+    const int ti = std::min(L, 8);
+    const int n = 3 * N;
+    const size_t smem = 2ull * ti * n * sizeof(C);
+    auto k = k_block_gemv<T>;
+    set_kernel_smem((const void*)k, smem);
+    k<<<dim3(ceil_div(L, ti), M, nrhs), 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
+    VS_LAUNCH_CHECK();
+  }
+  launch_strided_pass<T, true>(s, 3 * N, nrhs, st);
+  launch_x_pass<T>(a, true, MODE_PLAIN, nrhs, st);
+}
+template void prec_apply<float>(const vs_prec&, const float2*, float2*, int, const int*, cudaStream_t);
+template void prec_apply<double>(const vs_prec&, const double2*, double2*, int, const int*, cudaStream_t);
+
+}  // namespace vs
