@@ -1,0 +1,381 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 VoxScatter hot path.
+
+One step = one complete solve of the hexagonal-plate DDA problem (diameter
+8 lambda, thickness 2 lambda, m = 1.31+0.01i, grid 105x91x26, 558,714 unknowns)
+to ||b - A x|| / ||b|| <= 1e-6 (true residual, FP64) with right-preconditioned
+BiCGSTAB and the 2-level circulant preconditioner; mixed precision: the c64
+matvec/preconditioner pipeline inside FP64 iterative refinement.  The same
+solve with the c128 pipeline throughout is timed beside it.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  --impl reference times the FP64 NumPy/SciPy
+restatement of the reference algorithm on the host cores.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solve time to 1e-6 relative residual (BiCGSTAB + 2-level circulant preconditioner)"
+TOL = 1e-6
+
+
+def _env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def _workload():
+    from voxscatter_gb300 import workloads as W
+    p = W.config2()
+    return p
+
+
+def _config_dict(p, PQR=None):
+    L, M, N = p["L"], p["M"], p["N"]
+    d = {"workload": f"hex plate D=8 lambda, t=2 lambda, m=1.31+0.01i, grid {L}x{M}x{N}, "
+                     f"{len(p['idx'])} dipoles, {3 * len(p['idx'])} unknowns, +z incidence, x-pol",
+         "tol": TOL, "solver": "BiCGSTAB, right 2-level circulant preconditioner",
+         "l2": "inputs larger than L2 (c64 Green spectrum ~103 MB + preconditioner blocks ~465 MB read per iteration)"}
+    if PQR:
+        d["fft_grid"] = "x".join(str(v) for v in PQR)
+    return d
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        if not self.lines:
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1])); mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _pass_bytes(p, PQR, n3, e=8):
+    """Algorithmic DRAM bytes of each launch of the c64 pipelines (one rhs)."""
+    L, M, N = p["L"], p["M"], p["N"]
+    P, Q, R = PQR
+    V = L * M * N
+    i4 = 4
+    mv = [n3 * e + 3 * V * i4 + 3 * P * M * N * e,
+          3 * P * M * N * e + 3 * P * Q * N * e,
+          2 * 3 * P * Q * N * e + 6 * P * Q * R * e,
+          3 * P * Q * N * e + 3 * P * M * N * e,
+          3 * P * M * N * e + 3 * V * i4 + 2 * n3 * e]
+    n = 3 * N
+    pc = [n3 * e + 3 * V * i4 + 3 * V * e,
+          2 * 3 * V * e,
+          L * M * n * n * e + 2 * 3 * V * e,
+          2 * 3 * V * e,
+          3 * V * e + 3 * V * i4 + n3 * e]
+    pinned = e * (9 * V + 1.5 * V + 12 * P * M * N + 12 * P * Q * N) + 6 * P * Q * R * e
+    return mv, pc, pinned
+
+
+def _traffic_from_profiles(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for ln in open(path):
+        f = ln.split()
+        if len(f) >= 2 and f[0] == kernel:
+            try:
+                return float(f[1])
+            except ValueError:
+                return None
+    return None
+
+
+def _cpu_oracle_setup(p, workers):
+    import oracle as O
+    from oracle import _fft
+    _fft.set_workers(workers)
+    L, M, N = p["L"], p["M"], p["N"]
+    nD = L * M * N
+    idx = p["idx"]
+    idx3 = np.concatenate([idx, nD + idx, 2 * nD + idx])
+    Toep = O.green_toeplitz(p["r"], p["ko"])
+    alpha = O.alpha_ldr(p["refInd"], p["ko"], p["d"], p["kvec"], p["Eo"])
+    dV = p["d"] ** 3
+    fN = O.fft_operator(O.circulant_nop_const(Toep))
+    _, c1 = O.circ_1_level(Toep, L, M, N)
+    _, blk = O.circ_2_level(c1, L, M, N)
+    inv = O.invert_blocks(blk, 1 / alpha, dV)
+    del blk
+    chi = np.zeros(nD); chi[idx] = 1
+    chi = chi.reshape((L, M, N), order="F")
+    ones = np.ones((L, M, N))
+    b = O.PlaneWavePointWise(p["Eo"], p["kvec"], p["r"]).ravel(order="F")[idx3]
+    A = lambda v: O.MVP(v, fN, ones, dV * chi, 1 / alpha, "notransp", idx3)
+    Pm = lambda v: O.mvp_circ_2_level(inv, v, L, M, N, idx3)
+    return A, Pm, b
+
+
+def _cpu_iteration_seconds(A, Pm, b, iters):
+    import oracle as O
+    t0 = time.perf_counter()
+    _, flag, relres, it, _ = O.bicgstab(A, b, 1e-30, iters, Pm)
+    return (time.perf_counter() - t0) / max(it, 1)
+
+
+def run_reference(args):
+    rank = _env_int("RANK", 0)
+    if rank != 0:
+        return 0
+    p = _workload()
+    workers = os.cpu_count() or 1
+    A, Pm, b = _cpu_oracle_setup(p, workers)
+    import oracle as O
+    # iterations the FP64 reference algorithm needs (one untimed full solve)
+    x, flag, relres, it_needed, _ = O.bicgstab(A, b, TOL, 2000, Pm)
+    sample_iters = 2
+    for _ in range(args.warmup):
+        _cpu_iteration_seconds(A, Pm, b, sample_iters)
+    per = [_cpu_iteration_seconds(A, Pm, b, sample_iters) for _ in range(args.steps)]
+    per_it = float(np.median(per))
+    value_ms = per_it * it_needed * 1e3
+    sample = (f"{sample_iters} BiCGSTAB iterations per step of the FP64 NumPy/SciPy restatement "
+              f"(scipy.fft workers={workers}); solve = median s/iteration x {it_needed} iterations "
+              f"(full untimed reference solve: flag {flag}, relres {relres:.2e})")
+    line = {"impl": "reference", "metric": METRIC, "value": value_ms, "unit": "ms", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_it * sample_iters * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic (seeded reference-rule geometry)", "config": _config_dict(p),
+            "iterations": it_needed,
+            "cpu_baseline": {"value": value_ms, "unit": "ms", "cores": workers, "kind": "port", "sample": sample},
+            "e2e": {"value": value_ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    rank = _env_int("RANK", 0)
+    world = _env_int("WORLD_SIZE", 1)
+    local = _env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from voxscatter_gb300 import api
+    ctx = api.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr())
+
+    p = _workload()
+    L, M, N = p["L"], p["M"], p["N"]
+    nD = L * M * N
+    idx = p["idx"]
+    idx3 = np.concatenate([idx, nD + idx, 2 * nD + idx])
+    dV = p["d"] ** 3
+    t0 = time.perf_counter()
+    Toep = api.green_dda(p["r"], p["ko"], ctx=ctx)
+    alpha = api.alpha_ldr(p["refInd"], p["ko"], p["d"], p["kvec"], p["Eo"])
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep, ctx=ctx)
+    prec = api.Preconditioner(op, shift=1 / alpha, d=dV, precisions=("c64", "c128"))
+    ctx.synchronize()
+    setup_ms = (time.perf_counter() - t0) * 1e3
+    n3 = op.n3
+    bh = np.exp(1j * (p["kvec"][0] * p["r"][..., 0] + p["kvec"][1] * p["r"][..., 1] + p["kvec"][2] * p["r"][..., 2]))
+    b_host = np.zeros(3 * nD, dtype=np.complex128)
+    for c in range(3):
+        b_host[c * nD:(c + 1) * nD] = p["Eo"][c] * bh.ravel(order="F")
+    b_host = b_host[idx3]
+    b_dev = torch.from_numpy(b_host).cuda()
+    x_dev = torch.zeros_like(b_dev)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ctx.synchronize()
+
+    def timed(precision, steps):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        infos = []
+        barrier()
+        ev0.record(stream)
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                x_dev.zero_()
+            infos.append(api.solve_device(op, b_dev.data_ptr(), x_dev.data_ptr(), prec, tol=TOL,
+                                          precision=precision))
+        ev1.record(stream)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1) / steps
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, infos
+
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            x_dev.zero_()
+        api.solve_device(op, b_dev.data_ptr(), x_dev.data_ptr(), prec, tol=TOL, precision="mixed")
+    with ClockSampler(local) as clk:
+        ms_mixed, infos = timed("mixed", args.steps)
+    launches = int(np.mean([i["launches"] for i in infos]))
+    last = infos[-1]
+    ok = all(i["flag"] == 0 and i["relres"] <= TOL for i in infos)
+
+    # plain FP64 GPU path (same kernels in c128), fewer steps
+    api.solve_device(op, b_dev.data_ptr(), x_dev.data_ptr(), prec, tol=TOL, precision="fp64")
+    ms_fp64, infos64 = timed("fp64", max(1, min(args.steps, 3)))
+
+    # end to end through the host-buffer C API with pinned host memory
+    b_pin = torch.from_numpy(b_host).pin_memory()
+    x_pin = torch.zeros_like(b_pin).pin_memory()
+    e2e = []
+    for k in range(args.warmup + args.steps):
+        x_pin.zero_()
+        barrier()
+        t1 = time.perf_counter()
+        api.solve_host_ptr(op, b_pin.data_ptr(), x_pin.data_ptr(), prec, tol=TOL, precision="mixed")
+        if k >= args.warmup:
+            e2e.append((time.perf_counter() - t1) * 1e3)
+    e2e_ms = float(np.mean(e2e))
+
+    # per-launch timing of the pipeline passes (c64) for the roofline
+    xs = torch.randn(n3, dtype=torch.complex64, device="cuda")
+    ys = torch.empty_like(xs)
+    torch.cuda.synchronize()
+    mv_ms = op.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", 50)
+    pc_ms = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", 50)
+    mv_bytes, pc_bytes, pinned = _pass_bytes(p, op.PQR, n3)
+    names_mv = ["k_xf", "k_strided_fwd", "k_z", "k_strided_inv", "k_xi"]
+    names_pc = ["prec_k_xf", "prec_k_strided_fwd", "k_block_gemv", "prec_k_strided_inv", "prec_k_xi"]
+    allk = [(names_mv[i], mv_ms[i], mv_bytes[i]) for i in range(5)] + \
+           [(names_pc[i], pc_ms[i], pc_bytes[i]) for i in range(5)]
+    dom = max(allk, key=lambda t: t[1])
+    peak, peak_kind = _peaks()
+    achieved = dom[2] / (dom[1] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind,
+            "bytes_per_launch": dom[2], "ms_per_launch": dom[1],
+            "traffic": _traffic_from_profiles(dom[0])}
+    mv_total = sum(mv_ms)
+    matvec = {"ms": mv_total, "pinned_model_bytes": pinned, "GBps_pinned_model": pinned / (mv_total * 1e-3) / 1e9,
+              "GBps_own_passes": sum(mv_bytes) / (mv_total * 1e-3) / 1e9, "passes_ms": mv_ms,
+              "prec_apply_ms": sum(pc_ms), "prec_passes_ms": pc_ms,
+              "prec_GBps": sum(pc_bytes) / (sum(pc_ms) * 1e-3) / 1e9}
+
+    line = {"metric": METRIC, "value": ms_mixed, "unit": "ms", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64 (FP64 refinement, dots, norms)",
+            "data": "synthetic (seeded reference-rule geometry, plane-wave RHS)",
+            "config": dict(_config_dict(p, op.PQR), parallelism=f"replicas x{world}"),
+            "converged": ok, "relres": last["relres"], "iterations": last["iter"],
+            "refinements": last["refinements"],
+            "fp64_solve_ms": ms_fp64, "fp64_iterations": infos64[-1]["iter"],
+            "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed, "setup_ms": setup_ms,
+            "roofline": roof, "matvec": matvec,
+            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(b_pin.numel() * 16 * 2),
+                    "d2h_bytes_per_step": int(x_pin.numel() * 16)},
+            "gpu_launches": launches * args.steps, "clocks": clk.summary()}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        workers = os.cpu_count() or 1
+        A, Pm, b = _cpu_oracle_setup(p, workers)
+        sample_iters = 3
+        per_it = _cpu_iteration_seconds(A, Pm, b, sample_iters)
+        it_needed = infos64[-1]["iter"]
+        line["cpu_baseline"] = {
+            "value": per_it * it_needed * 1e3, "unit": "ms", "cores": workers, "kind": "port",
+            "sample": f"{sample_iters} BiCGSTAB iterations of the FP64 NumPy/SciPy restatement "
+                      f"(scipy.fft workers={workers}) x {it_needed} iterations (the FP64 iteration count, "
+                      f"which the oracle reproduces)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -198,6 +198,7 @@ typedef struct vs_solve_info {
   int refinements; /* MIXED: refinement steps taken                                          */
   int64_t n_resvec;
   double time_ms;  /* wall time of the call                                                  */
+  int64_t kernel_launches; /* kernels this call launched (each node of a graph launch counts) */
 } vs_solve_info;
 
 /* Fill opts with defaults: BiCGSTAB, MIXED, tol 1e-6, maxit 2000, automatic
@@ -213,6 +214,17 @@ int vs_solve(vs_op* op, vs_prec* prec, const double* b, double* x, const vs_solv
 
 /* Same with b and x in device memory (double2, n3 each). */
 int vs_solve_device(vs_op* op, vs_prec* prec, const void* b, void* x, const vs_solve_opts* opts, vs_solve_info* info);
+
+/* ---- diagnostics ----------------------------------------------------- */
+
+/* Time each of the 5 launches of one apply (matvec: X-forward gather, Y
+ * forward, Z FFT x tensor x inverse, Y inverse, X inverse + diagonal; the
+ * preconditioner: X-forward gather, Y forward, block GEMV, Y inverse, X
+ * inverse) with CUDA events on the context's stream, averaged over nrep
+ * back-to-back applies of nrhs right-hand sides.  ms_out receives 5 floats
+ * (milliseconds per launch).  Device buffers x, y of the precision's type. */
+int vs_op_time_passes(vs_op* op, const void* x, void* y, int64_t nrhs, int precision, int nrep, float* ms_out);
+int vs_prec_time_passes(vs_prec* prec, const void* x, void* y, int64_t nrhs, int precision, int nrep, float* ms_out);
 
 #ifdef __cplusplus
 }

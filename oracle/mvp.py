@@ -5,6 +5,8 @@ Follows src/src_vie/src_mvp/MVP.m:38-145 (identical to mv_AN_const.m).
 """
 import numpy as np
 
+from . import _fft as _F
+
 from .operators import COMP_PAIRS, _dda_tensor
 
 # Output component a accumulates fN component PAIR[a][b] times input b (MVP.m:108-123)
@@ -39,16 +41,16 @@ def MVP(JIn0, fN, Mr, Mc, Gram, transp_flag, idx, GPU_flag=0):
     JOut = np.zeros((L, M, N, 3), dtype=complex)
     if transp_flag == "transp":  # MVP.m:65-99
         Mcc = np.conj(Mc)
-        fJ = [np.fft.fftn(np.conj(Mcc * JIn[..., b]), s=(P, Q, R), axes=(0, 1, 2)) for b in range(3)]
+        fJ = [_F.fftn(np.conj(Mcc * JIn[..., b]), s=(P, Q, R), axes=(0, 1, 2)) for b in range(3)]
         for a in range(3):
             acc = sum(fN[..., PAIR[a][b]] * fJ[b] for b in range(3))
-            J = np.fft.ifftn(acc)
+            J = _F.ifftn(acc, axes=(0, 1, 2))
             JOut[..., a] = Gram * np.conj(Mr) * JIn[..., a] - np.conj(J[:L, :M, :N])
     elif transp_flag == "notransp":  # MVP.m:101-133
-        fJ = [np.fft.fftn(JIn[..., b], s=(P, Q, R), axes=(0, 1, 2)) for b in range(3)]
+        fJ = [_F.fftn(JIn[..., b], s=(P, Q, R), axes=(0, 1, 2)) for b in range(3)]
         for a in range(3):
             acc = sum(fN[..., PAIR[a][b]] * fJ[b] for b in range(3))
-            J = np.fft.ifftn(acc)
+            J = _F.ifftn(acc, axes=(0, 1, 2))
             JOut[..., a] = Gram * Mr * JIn[..., a] - Mc * J[:L, :M, :N]
     else:
         raise ValueError("transp_flag must be 'transp' or 'notransp'")
@@ -71,10 +73,10 @@ def MVP_plain_transpose(JIn0, fN, Mr, Mc, Gram, idx):
     JInf[np.asarray(idx)] = np.asarray(JIn0, dtype=complex).ravel()
     JIn = JInf.reshape((L, M, N, 3), order="F")
     JOut = np.zeros((L, M, N, 3), dtype=complex)
-    fJ = [np.fft.fftn(Mc * JIn[..., b], s=(P, Q, R), axes=(0, 1, 2)) for b in range(3)]
+    fJ = [_F.fftn(Mc * JIn[..., b], s=(P, Q, R), axes=(0, 1, 2)) for b in range(3)]
     for a in range(3):
         acc = sum(fN[..., PAIR[a][b]] * fJ[b] for b in range(3))
-        J = np.fft.ifftn(acc)
+        J = _F.ifftn(acc, axes=(0, 1, 2))
         JOut[..., a] = Gram * Mr * JIn[..., a] - J[:L, :M, :N]
     return JOut.ravel(order="F")[np.asarray(idx)]
 

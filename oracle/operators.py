@@ -6,6 +6,8 @@ circulant_nop_const.m:1-40, gperiodic_coeff_nop.m:1-33, fft_operator.m:1-8.
 """
 import numpy as np
 
+from . import _fft as _F
+
 # Lattice-dispersion-relation coefficients, getOPERATOR_DDA.m:7-9
 B1 = -1.8915316
 B2 = 0.1648469
@@ -136,7 +138,7 @@ def circulant_nop_const(G):
 
 def fft_operator(A):
     """3-D FFT of each component, fft_operator.m:1-8."""
-    return np.fft.fftn(A, axes=(0, 1, 2))
+    return _F.fftn(A, axes=(0, 1, 2))
 
 
 def getOPERATOR_DDA(r, ko, refInd, kvec, Eo, nearby_quad="off"):

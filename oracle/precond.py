@@ -12,6 +12,8 @@ stores -CC3 while the block uses CC3).
 """
 import numpy as np
 
+from . import _fft as _F
+
 # sign applied to the (L+1-i)/L term in circ_1_level.m:14,29,42,55,69,84
 _S1 = [+1, -1, -1, +1, +1, +1]
 # sign applied to the (M+1-i)/M term in circ_2_level.m:14,27,38,51,63,76
@@ -38,7 +40,7 @@ def circ_1_level(opToeplitz, L, M, N, parallel_prec=0, on_off="off"):
     T = np.asarray(opToeplitz, dtype=complex)
     out = np.zeros((L, M, N, 6), dtype=complex)
     for c in range(6):
-        out[..., c] = np.fft.fft(_chan_average(T[..., c], _S1[c]), axis=0)
+        out[..., c] = _F.fft(_chan_average(T[..., c], _S1[c]), axis=0)
     circ = circ_1_level_blocks(out, L, M, N) if on_off != "off" else None
     return circ, out
 
@@ -90,7 +92,7 @@ def circ_2_level(circ_L_opToep, L, M, N):
     C = np.asarray(circ_L_opToep, dtype=complex)
     lev2 = np.zeros((L, M, N, 6), dtype=complex)
     for c in range(6):
-        lev2[..., c] = np.fft.fft(_chan_average(np.moveaxis(C[..., c], 1, 0), _S2[c]), axis=0).swapaxes(0, 1)
+        lev2[..., c] = _F.fft(_chan_average(np.moveaxis(C[..., c], 1, 0), _S2[c]), axis=0).swapaxes(0, 1)
     circ_M = lev2 * np.array(_STORE2)[None, None, None, :]
     blocks = np.zeros((L, M, 3 * N, 3 * N), dtype=complex)
     for i in range(L):
@@ -126,11 +128,11 @@ def mvp_circ_2_level(inv_blocks, JIn, L, M, N, idx):
     V = np.zeros(3 * L * M * N, dtype=complex)
     V[np.asarray(idx)] = np.asarray(JIn, dtype=complex).ravel()
     V = V.reshape((L, M, N, 3), order="F")
-    V = np.fft.fft(np.fft.fft(V, axis=0), axis=1)
+    V = _F.fft(_F.fft(V, axis=0), axis=1)
     vec = V.transpose(0, 1, 3, 2).reshape(L, M, 3 * N)  # index comp*N + z
     out = np.einsum("ijab,ijb->ija", inv_blocks, vec)
     V = out.reshape(L, M, 3, N).transpose(0, 1, 3, 2)
-    V = np.fft.ifft(np.fft.ifft(V, axis=1), axis=0)
+    V = _F.ifft(_F.ifft(V, axis=1), axis=0)
     return V.ravel(order="F")[np.asarray(idx)]
 
 
@@ -138,7 +140,7 @@ def chan_mvp_idx(inv_blocks, JIn, L, M, N, idx):
     """1-level apply, chan_mvp_idx.m:1-17; ``inv_blocks`` is (L, 3MN, 3MN)."""
     V = np.zeros(3 * L * M * N, dtype=complex)
     V[np.asarray(idx)] = np.asarray(JIn, dtype=complex).ravel()
-    temp = np.fft.fft(V.reshape((L, 3 * M * N), order="F"), axis=0)
+    temp = _F.fft(V.reshape((L, 3 * M * N), order="F"), axis=0)
     temp = np.einsum("iab,ib->ia", inv_blocks, temp)
-    temp = np.fft.ifft(temp, axis=0)
+    temp = _F.ifft(temp, axis=0)
     return temp.ravel(order="F")[np.asarray(idx)]

@@ -64,10 +64,12 @@ class vs_solve_opts(C.Structure):
 
 class vs_solve_info(C.Structure):
     _fields_ = [("flag", C.c_int), ("relres", C.c_double), ("iter", C.c_double), ("refinements", C.c_int),
-                ("n_resvec", _i64), ("time_ms", C.c_double)]
+                ("n_resvec", _i64), ("time_ms", C.c_double), ("kernel_launches", _i64)]
 
 
 SIGNATURES.update({
+    "vs_op_time_passes": (C.c_int, [_vp, _vp, _vp, _i64, C.c_int, C.c_int, C.POINTER(C.c_float)]),
+    "vs_prec_time_passes": (C.c_int, [_vp, _vp, _vp, _i64, C.c_int, C.c_int, C.POINTER(C.c_float)]),
     "vs_solve_opts_default": (None, [C.POINTER(vs_solve_opts)]),
     "vs_solve": (C.c_int, [_vp, _vp, _pd, _pd, C.POINTER(vs_solve_opts), C.POINTER(vs_solve_info)]),
     "vs_solve_device": (C.c_int, [_vp, _vp, _vp, _vp, C.POINTER(vs_solve_opts), C.POINTER(vs_solve_info)]),

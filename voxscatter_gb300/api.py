@@ -31,6 +31,12 @@ class Context:
     def synchronize(self):
         L.check(self._lib.vs_ctx_synchronize(self.h), self.h)
 
+    def stream_ptr(self):
+        """The context's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+        ptr = C.c_void_p()
+        L.check(self._lib.vs_ctx_stream(self.h, C.byref(ptr)), self.h)
+        return ptr.value or 0
+
     def close(self):
         if getattr(self, "h", None):
             self._lib.vs_ctx_destroy(self.h)
@@ -153,6 +159,13 @@ class Operator:
         self.ctx.synchronize()
         return y
 
+    def time_passes(self, x_ptr, y_ptr, nrhs=1, precision="c64", nrep=20):
+        """Per-launch milliseconds of the 5 pipeline passes (CUDA events)."""
+        out = (C.c_float * 5)()
+        L.check(self.ctx._lib.vs_op_time_passes(self.h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), nrhs,
+                                                L.VS_C64 if precision == "c64" else L.VS_C128, nrep, out), self.ctx.h)
+        return list(out)
+
     def close(self):
         if getattr(self, "h", None):
             self.ctx._lib.vs_op_destroy(self.h)
@@ -261,6 +274,13 @@ class Preconditioner:
                                             L.VS_C64 if precision == "c64" else L.VS_C128), self.ctx.h)
         return y
 
+    def time_passes(self, x_ptr, y_ptr, nrhs=1, precision="c64", nrep=20):
+        out = (C.c_float * 5)()
+        L.check(self.ctx._lib.vs_prec_time_passes(self.h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), nrhs,
+                                                  L.VS_C64 if precision == "c64" else L.VS_C128, nrep, out),
+                self.ctx.h)
+        return list(out)
+
     def blocks(self, Lx, My, Nz, precision="c128"):
         n = 3 * Nz
         out = np.zeros(Lx * My * n * n, dtype=np.complex128)
@@ -309,8 +329,38 @@ def solve(op, b, prec=None, tol=1e-6, maxit=2000, precision="mixed", x0=None, in
     L.check(lib.vs_solve(op.h, prec.h if prec is not None else None, L.dptr(b), L.dptr(x), C.byref(o),
                          C.byref(info)), op.ctx.h)
     d = dict(flag=info.flag, relres=info.relres, iter=info.iter, refinements=info.refinements,
-             time_ms=info.time_ms)
+             time_ms=info.time_ms, launches=info.kernel_launches)
     return x, d, rv[:info.n_resvec].copy()
+
+
+def solve_device(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="mixed", inner_tol=0.0,
+                 max_refine=10, iters_per_graph=4):
+    """vs_solve_device on device buffers (double2, n3 each); returns the info dict."""
+    lib = op.ctx._lib
+    o = L.vs_solve_opts()
+    lib.vs_solve_opts_default(C.byref(o))
+    o.precision = L.VS_SOLVE_MIXED if precision == "mixed" else L.VS_SOLVE_FP64
+    o.tol = float(tol); o.maxit = int(maxit); o.inner_tol = float(inner_tol); o.max_refine = int(max_refine)
+    o.iters_per_graph = int(iters_per_graph)
+    info = L.vs_solve_info()
+    L.check(lib.vs_solve_device(op.h, prec.h if prec is not None else None, C.c_void_p(b_ptr), C.c_void_p(x_ptr),
+                                C.byref(o), C.byref(info)), op.ctx.h)
+    return dict(flag=info.flag, relres=info.relres, iter=info.iter, refinements=info.refinements,
+                time_ms=info.time_ms, launches=info.kernel_launches)
+
+
+def solve_host_ptr(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="mixed", iters_per_graph=4):
+    """vs_solve on host buffers given as raw pointers (e.g. pinned torch tensors)."""
+    lib = op.ctx._lib
+    o = L.vs_solve_opts()
+    lib.vs_solve_opts_default(C.byref(o))
+    o.precision = L.VS_SOLVE_MIXED if precision == "mixed" else L.VS_SOLVE_FP64
+    o.tol = float(tol); o.maxit = int(maxit); o.iters_per_graph = int(iters_per_graph)
+    info = L.vs_solve_info()
+    L.check(lib.vs_solve(op.h, prec.h if prec is not None else None, C.cast(C.c_void_p(b_ptr), L._pd),
+                         C.cast(C.c_void_p(x_ptr), L._pd), C.byref(o), C.byref(info)), op.ctx.h)
+    return dict(flag=info.flag, relres=info.relres, iter=info.iter, refinements=info.refinements,
+                time_ms=info.time_ms, launches=info.kernel_launches)
 
 
 def bicgstab(A, b, tol=1e-6, maxit=20, M1=None, M2=None, x0=None, precision="mixed"):

@@ -170,6 +170,33 @@ void prec_scratch_impl(vs_prec* pr, int64_t nrhs) {
   }
 }
 
+template <typename F>
+void time_passes(cudaStream_t st, int nrep, float* ms_out, F&& launch) {
+  cudaEvent_t ev[6];
+  for (auto& e : ev) VS_CUDA(cudaEventCreate(&e));
+  float acc[5] = {0, 0, 0, 0, 0};
+  try {
+    for (int r = 0; r < nrep; ++r) {
+      VS_CUDA(cudaEventRecord(ev[0], st));
+      for (int p = 0; p < 5; ++p) {
+        launch(p);
+        VS_CUDA(cudaEventRecord(ev[p + 1], st));
+      }
+      VS_CUDA(cudaEventSynchronize(ev[5]));
+      for (int p = 0; p < 5; ++p) {
+        float ms = 0;
+        VS_CUDA(cudaEventElapsedTime(&ms, ev[p], ev[p + 1]));
+        acc[p] += ms;
+      }
+    }
+  } catch (...) {
+    for (auto& e : ev) cudaEventDestroy(e);
+    throw;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  for (int p = 0; p < 5; ++p) ms_out[p] = acc[p] / nrep;
+}
+
 }  // namespace
 
 extern "C" {
@@ -665,6 +692,7 @@ static void solve_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, c
   info->iter = r.iter;
   info->refinements = r.refinements;
   info->n_resvec = r.n_resvec;
+  info->kernel_launches = r.launches;
 }
 
 int vs_solve_device(vs_op* op, vs_prec* prec, const void* b, void* x, const vs_solve_opts* opts, vs_solve_info* info) {
@@ -692,6 +720,47 @@ int vs_solve(vs_op* op, vs_prec* prec, const double* b, double* x, const vs_solv
     VS_CUDA(cudaMemcpyAsync(x, op->yout.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
     info->time_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  });
+}
+
+// ---- diagnostics ----------------------------------------------------------
+
+int vs_op_time_passes(vs_op* op, const void* x, void* y, int64_t nrhs, int precision, int nrep, float* ms_out) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(x && y && ms_out && nrep >= 1, "bad argument");
+    VS_REQUIRE(nrhs >= 1 && nrhs <= 65535, "nrhs must be in [1, 65535]");
+    cudaStream_t st = op->ctx->stream;
+    if (precision == VS_C64) {
+      vs::ensure_scratch(*op, (int)nrhs, sizeof(float2));
+      time_passes(st, nrep, ms_out, [&](int p) {
+        vs::matvec_pass<float>(*op, (const float2*)x, (float2*)y, (int)nrhs, VS_NOTRANSP, nullptr, st, p);
+      });
+    } else {
+      vs::ensure_scratch(*op, (int)nrhs, sizeof(double2));
+      time_passes(st, nrep, ms_out, [&](int p) {
+        vs::matvec_pass<double>(*op, (const double2*)x, (double2*)y, (int)nrhs, VS_NOTRANSP, nullptr, st, p);
+      });
+    }
+  });
+}
+
+int vs_prec_time_passes(vs_prec* prec, const void* x, void* y, int64_t nrhs, int precision, int nrep,
+                        float* ms_out) {
+  if (!prec) return VS_ERR_ARG;
+  return guarded(prec->ctx, [&] {
+    VS_REQUIRE(x && y && ms_out && nrep >= 1, "bad argument");
+    VS_REQUIRE(nrhs >= 1 && nrhs <= 65535, "nrhs must be in [1, 65535]");
+    prec_scratch_impl(prec, nrhs);
+    cudaStream_t st = prec->ctx->stream;
+    if (precision == VS_C64)
+      time_passes(st, nrep, ms_out, [&](int p) {
+        vs::prec_apply_pass<float>(*prec, (const float2*)x, (float2*)y, (int)nrhs, nullptr, st, p);
+      });
+    else
+      time_passes(st, nrep, ms_out, [&](int p) {
+        vs::prec_apply_pass<double>(*prec, (const double2*)x, (double2*)y, (int)nrhs, nullptr, st, p);
+      });
   });
 }
 

@@ -100,6 +100,9 @@ namespace vs {
 
 // Launchers (vs_matvec.cu)
 template <typename T>
+void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
+                 cudaStream_t st, int pass);
+template <typename T>
 void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
             cudaStream_t st);
 void ensure_scratch(vs_op& op, int nrhs, size_t elem_bytes);
@@ -127,6 +130,9 @@ void circ_levels_device(int L, int M, int N, const double2* toep, double2* lev1,
 template <typename T>
 void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, const double2* dvec, double2 dscal,
                      bool invert, bool colmajor, double scale, cplx_t<T>* out, int* status, cudaStream_t st);
+template <typename T>
+void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
+                     cudaStream_t st, int pass);
 template <typename T>
 void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip, cudaStream_t st);
 

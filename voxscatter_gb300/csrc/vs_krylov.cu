@@ -398,13 +398,17 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
   VS_LAUNCH_CHECK();
 }
 
+// Kernels in one bicg_iteration: 7 solver kernels, 2 matvecs of 5 passes, and
+// 2 preconditioner applies of 5 passes (or 2 copies without preconditioner).
+static int kernels_per_iteration(const vs_prec* pr) { return 7 + 10 + (pr ? 10 : 2); }
+
 // Runs BiCGSTAB on w.x (initial guess already there) for A x = w.r0-based
 // system: the caller has put the initial residual in w.r.  Returns the final
 // state.  Iterations are launched as a CUDA graph of `per_graph` iterations.
 template <typename T>
 static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t n, double bnorm, double tol,
                             int maxit, double res_scale, double* resvec_dev, int resvec_cap, int per_graph,
-                            cudaStream_t st) {
+                            cudaStream_t st, int64_t* launches) {
   using C = cplx_t<T>;
   KState h{};
   h.tol_abs = tol * bnorm;
@@ -420,6 +424,7 @@ static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, i
   const int g = vec_grid(n);
   k_copy<T><<<g, 256, 0, st>>>(w.rt.as<C>(), w.r.as<C>(), n);
   k_norm<T><<<g, kRedThreads, 0, st>>>(w.r.as<C>(), n, s, w.scal.as<double>());
+  *launches += 2;
   double r0 = 0;
   VS_CUDA(cudaMemcpyAsync(&r0, w.scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
   VS_CUDA(cudaStreamSynchronize(st));
@@ -440,6 +445,7 @@ static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, i
     idle.skip = 1;
     upload_state(s, idle, st);
     bicg_iteration<T>(op, pr, w, s, n, st);
+    *launches += kernels_per_iteration(pr);
   }
   upload_state(s, h, st);
   cudaGraph_t graph = nullptr;
@@ -458,6 +464,7 @@ static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, i
   const int max_launch = (maxit + per_graph - 1) / per_graph + 1;
   for (int it = 0; it < max_launch; ++it) {
     VS_CUDA(cudaGraphLaunch(exec, st));
+    *launches += (int64_t)per_graph * kernels_per_iteration(pr);
     VS_CUDA(cudaMemcpyAsync(&cur, s, sizeof(KState), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
     if (cur.skip) break;
@@ -468,7 +475,8 @@ static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, i
   return cur;
 }
 
-static double norm64(KrylovWork& w, const double2* u, int64_t n, cudaStream_t st) {
+static double norm64(KrylovWork& w, const double2* u, int64_t n, cudaStream_t st, int64_t* launches) {
+  *launches += 1;
   KState* s = w.state.as<KState>();
   k_norm<double><<<vec_grid(n), kRedThreads, 0, st>>>(u, n, s, w.scal.as<double>());
   VS_LAUNCH_CHECK();
@@ -480,7 +488,8 @@ static double norm64(KrylovWork& w, const double2* u, int64_t n, cudaStream_t st
 
 // r64 = b - A x64 (c128 pipeline); returns ||r64||.
 static double residual64(const vs_op& op, KrylovWork& w, const double2* b, const double2* x, double2* r, int64_t n,
-                         cudaStream_t st) {
+                         cudaStream_t st, int64_t* launches) {
+  *launches += 6;
   KState* s = w.state.as<KState>();
   double2* y = w.y64.as<double2>();
   matvec<double>(op, x, y, 1, VS_NOTRANSP, nullptr, st);
@@ -507,7 +516,8 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
   w.resvec.alloc(std::max(1, cap) * sizeof(double));
   double* rv = cap > 0 ? w.resvec.as<double>() : nullptr;
   ensure_scratch(op, 1, sizeof(double2));
-  const double bnorm = norm64(w, b, n, st);
+  int64_t launches = 0;
+  const double bnorm = norm64(w, b, n, st, &launches);
   if (!std::isfinite(bnorm)) throw Error(VS_ERR_NONFINITE, "right-hand side has NaN or Inf entries");
   out = SolveResult{};
   if (bnorm == 0) {
@@ -521,15 +531,17 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
     w.y64.alloc(n * sizeof(double2));
     // x0 -> w.x ; r = b - A x0
     k_copy<double><<<vec_grid(n), 256, 0, st>>>(w.x.as<double2>(), x, n);
-    residual64(op, w, b, x, w.r.as<double2>(), n, st);
-    KState fs = bicgstab_core<double>(op, pr, w, n, bnorm, prm.tol, prm.maxit, 1.0 / bnorm, rv, cap, prm.per_graph, st);
+    residual64(op, w, b, x, w.r.as<double2>(), n, st, &launches);
+    launches += 1;
+    KState fs = bicgstab_core<double>(op, pr, w, n, bnorm, prm.tol, prm.maxit, 1.0 / bnorm, rv, cap, prm.per_graph, st, &launches);
+    launches += 1;
     k_copy<double><<<vec_grid(n), 256, 0, st>>>(x, w.x.as<double2>(), n);
     VS_LAUNCH_CHECK();
     out.flag = fs.flag;
     out.iter = fs.iter2 * 0.5;
     out.inner_iters = fs.iter2 * 0.5;
     out.n_resvec = std::min<int64_t>(fs.nres, cap);
-    const double rn = residual64(op, w, b, x, w.r.as<double2>(), n, st);
+    const double rn = residual64(op, w, b, x, w.r.as<double2>(), n, st, &launches);
     out.relres = rn / bnorm;
     if (out.flag == 0 && out.relres > prm.tol) out.flag = 1;
   } else {
@@ -538,7 +550,7 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
     w.y64.alloc(n * sizeof(double2));
     w.r64.alloc(n * sizeof(double2));
     double2* r64 = w.r64.as<double2>();
-    double rn = residual64(op, w, b, x, r64, n, st);
+    double rn = residual64(op, w, b, x, r64, n, st, &launches);
     int inner_total2 = 0;
     int64_t nres = 0;
     int flag = 1;
@@ -557,7 +569,8 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
       double* rvk = (rv && nres < cap) ? rv + nres : nullptr;
       const int capk = rv ? (int)(cap - nres) : 0;
       KState fs = bicgstab_core<float>(op, pr, w, n, 1.0, itol, prm.maxit - inner_total2 / 2, rn / bnorm, rvk, capk,
-                                       prm.per_graph, st);
+                                       prm.per_graph, st, &launches);
+      launches += 2;
       inner_total2 += fs.iter2;
       nres += std::min<int64_t>(fs.nres, capk);
       if (fs.flag >= 4 && fs.iter2 == 0) {
@@ -566,7 +579,8 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
       }
       k_update64<<<vec_grid(n), 256, 0, st>>>(x, w.x.as<float2>(), n, rn);
       VS_LAUNCH_CHECK();
-      rn = residual64(op, w, b, x, r64, n, st);
+      launches += 1;
+      rn = residual64(op, w, b, x, r64, n, st, &launches);
     }
     out.flag = (rn <= prm.tol * bnorm) ? 0 : (flag >= 4 ? flag : 1);
     out.relres = rn / bnorm;
@@ -575,6 +589,7 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
     out.refinements = refine;
     out.n_resvec = nres;
   }
+  out.launches = launches;
   if (cap > 0 && prm.resvec_host && out.n_resvec > 0)
     VS_CUDA(cudaMemcpyAsync(prm.resvec_host, rv, out.n_resvec * sizeof(double), cudaMemcpyDeviceToHost, st));
   VS_CUDA(cudaStreamSynchronize(st));

@@ -32,6 +32,7 @@ struct SolveResult {
   double relres = 0, iter = 0, inner_iters = 0;
   int refinements = 0;
   int64_t n_resvec = 0;
+  int64_t launches = 0;  // kernels launched by the solve (graph nodes count per graph launch)
 };
 
 void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,

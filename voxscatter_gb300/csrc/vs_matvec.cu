@@ -278,11 +278,9 @@ static StridedArgs<T> y_pass_args(const vs_op& op, const PipeArgs<T>& a, bool in
 }
 
 template <typename T>
-void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
-            cudaStream_t st) {
+static PipeArgs<T> pipe_args(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, const int* skip) {
   using C = cplx_t<T>;
-  VS_REQUIRE(mode >= VS_NOTRANSP && mode <= VS_CONJTRANSP, "mode must be VS_NOTRANSP, VS_TRANSP or VS_CONJTRANSP");
-  PipeArgs<T> a;
+  PipeArgs<T> a{};
   a.L = op.L; a.M = op.M; a.N = op.N; a.P = op.P; a.Q = op.Q; a.R = op.R;
   a.V = op.V; a.n3 = op.n3;
   a.map3 = op.map3.as<int>();
@@ -298,18 +296,36 @@ void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mod
   a.lpb = std::max(1, 2048 / op.P);
   a.tx = pick_tile(op.R, sizeof(C), 3);
   a.skip = skip;
-  launch_x_pass<T>(a, false, mode, nrhs, st);
-  launch_strided_pass<T, false>(y_pass_args<T>(op, a, false), op.N * 3, nrhs, st);
-  {
-    dim3 grid(ceil_div(op.P, a.tx), op.Q, nrhs);
-    const size_t smem = 2ull * op.R * 3 * a.tx * sizeof(C);
-    auto k = k_z<T>;
-    set_smem(k, smem);
-    k<<<grid, kThreads, smem, st>>>(a);
-    VS_LAUNCH_CHECK();
+  return a;
+}
+
+template <typename T>
+void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
+                 cudaStream_t st, int pass) {
+  using C = cplx_t<T>;
+  VS_REQUIRE(mode >= VS_NOTRANSP && mode <= VS_CONJTRANSP, "mode must be VS_NOTRANSP, VS_TRANSP or VS_CONJTRANSP");
+  const PipeArgs<T> a = pipe_args<T>(op, x, y, skip);
+  switch (pass) {
+    case 0: launch_x_pass<T>(a, false, mode, nrhs, st); break;
+    case 1: launch_strided_pass<T, false>(y_pass_args<T>(op, a, false), op.N * 3, nrhs, st); break;
+    case 2: {
+      dim3 grid(ceil_div(op.P, a.tx), op.Q, nrhs);
+      const size_t smem = 2ull * op.R * 3 * a.tx * sizeof(C);
+      auto k = k_z<T>;
+      set_smem(k, smem);
+      k<<<grid, kThreads, smem, st>>>(a);
+      VS_LAUNCH_CHECK();
+      break;
+    }
+    case 3: launch_strided_pass<T, true>(y_pass_args<T>(op, a, true), op.N * 3, nrhs, st); break;
+    default: launch_x_pass<T>(a, true, mode, nrhs, st); break;
   }
-  launch_strided_pass<T, true>(y_pass_args<T>(op, a, true), op.N * 3, nrhs, st);
-  launch_x_pass<T>(a, true, mode, nrhs, st);
+}
+
+template <typename T>
+void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
+            cudaStream_t st) {
+  for (int pass = 0; pass < 5; ++pass) matvec_pass<T>(op, x, y, nrhs, mode, skip, st, pass);
 }
 
 template void launch_x_pass<float>(const PipeArgs<float>&, bool, int, int, cudaStream_t);
@@ -319,6 +335,8 @@ template void launch_strided_pass<float, true>(const StridedArgs<float>&, int, i
 template void launch_strided_pass<double, false>(const StridedArgs<double>&, int, int, cudaStream_t);
 template void launch_strided_pass<double, true>(const StridedArgs<double>&, int, int, cudaStream_t);
 
+template void matvec_pass<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t, int);
+template void matvec_pass<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t, int);
 template void matvec<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t);
 template void matvec<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t);
 

@@ -247,7 +247,8 @@ __global__ void __launch_bounds__(256) k_block_gemv(cplx_t<T>* __restrict__ t, c
 }
 
 template <typename T>
-void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip, cudaStream_t st) {
+void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
+                     cudaStream_t st, int pass) {
   using C = cplx_t<T>;
   const int L = pr.L, M = pr.M, N = pr.N;
   const C* inv = std::is_same<T, float>::value ? (const C*)pr.inv32.p : (const C*)pr.inv64.p;
@@ -263,7 +264,6 @@ void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, c
   a.pP = pr.axL.plan;
   a.lpb = std::max(1, 2048 / L);
   a.skip = skip;
-  launch_x_pass<T>(a, false, MODE_PLAIN, nrhs, st);
   StridedArgs<T> s{};
   s.src = t; s.dst = t;
   s.xext = L; s.n_in = M; s.n_out = M;
@@ -278,19 +278,30 @@ void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, c
   s.plan = pr.axM.plan;
   s.tw = pr.axM.tw<T>();
   s.skip = skip;
-  launch_strided_pass<T, false>(s, 3 * N, nrhs, st);
-  {
-    const int ti = std::min(L, 8);
-    const int n = 3 * N;
-    const size_t smem = 2ull * ti * n * sizeof(C);
-    auto k = k_block_gemv<T>;
-    set_kernel_smem((const void*)k, smem);
-    k<<<dim3(ceil_div(L, ti), M, nrhs), 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
-    VS_LAUNCH_CHECK();
+  switch (pass) {
+    case 0: launch_x_pass<T>(a, false, MODE_PLAIN, nrhs, st); break;
+    case 1: launch_strided_pass<T, false>(s, 3 * N, nrhs, st); break;
+    case 2: {
+      const int ti = std::min(L, 8);
+      const int n = 3 * N;
+      const size_t smem = 2ull * ti * n * sizeof(C);
+      auto k = k_block_gemv<T>;
+      set_kernel_smem((const void*)k, smem);
+      k<<<dim3(ceil_div(L, ti), M, nrhs), 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
+      VS_LAUNCH_CHECK();
+      break;
+    }
+    case 3: launch_strided_pass<T, true>(s, 3 * N, nrhs, st); break;
+    default: launch_x_pass<T>(a, true, MODE_PLAIN, nrhs, st); break;
   }
-  launch_strided_pass<T, true>(s, 3 * N, nrhs, st);
-  launch_x_pass<T>(a, true, MODE_PLAIN, nrhs, st);
 }
+
+template <typename T>
+void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip, cudaStream_t st) {
+  for (int pass = 0; pass < 5; ++pass) prec_apply_pass<T>(pr, x, y, nrhs, skip, st, pass);
+}
+template void prec_apply_pass<float>(const vs_prec&, const float2*, float2*, int, const int*, cudaStream_t, int);
+template void prec_apply_pass<double>(const vs_prec&, const double2*, double2*, int, const int*, cudaStream_t, int);
 template void prec_apply<float>(const vs_prec&, const float2*, float2*, int, const int*, cudaStream_t);
 template void prec_apply<double>(const vs_prec&, const double2*, double2*, int, const int*, cudaStream_t);
 
