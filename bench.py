@@ -364,6 +364,31 @@ def run_ours(args):
     return 0
 
 
+def run_passes(args):
+    """Setup + per-pass timing only (c64 and c128 matvec, c64 preconditioner)."""
+    import torch
+    from voxscatter_gb300 import api
+    ctx = api.Context(0)
+    p = _workload()
+    L, M, N = p["L"], p["M"], p["N"]
+    nD = L * M * N
+    idx = p["idx"]
+    idx3 = np.concatenate([idx, nD + idx, 2 * nD + idx])
+    dV = p["d"] ** 3
+    Toep = api.green_dda(p["r"], p["ko"], ctx=ctx)
+    alpha = api.alpha_ldr(p["refInd"], p["ko"], p["d"], p["kvec"], p["Eo"])
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep, ctx=ctx)
+    prec = api.Preconditioner(op, shift=1 / alpha, d=dV, precisions=("c64",))
+    xs = torch.randn(op.n3, dtype=torch.complex64, device="cuda")
+    ys = torch.empty_like(xs)
+    torch.cuda.synchronize()
+    out = {"fft_grid": op.PQR,
+           "matvec_c64_ms": op.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", args.steps),
+           "prec_c64_ms": prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", args.steps)}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -371,7 +396,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="solve", choices=["solve", "passes"],
+                    help="passes: only build the operator/preconditioner and time each pipeline launch "
+                         "(a short command for ncu captures)")
     args = ap.parse_args()
+    if args.mode == "passes":
+        return run_passes(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

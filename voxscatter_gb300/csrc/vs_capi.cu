@@ -126,30 +126,20 @@ void spectrum_from_full(vs_op* op, const double2* full) {
                         op->ctx->stream);
 }
 
-// Column-major caller blocks -> row-major device blocks (scaled), and back.
-__global__ void k_blocks_in(const double2* __restrict__ in, int64_t nblk, int n, double scale, double2* o64,
+// Caller blocks <-> device blocks (both column-major; device copies carry the 1/(L*M) of the inverse FFTs).
+__global__ void k_blocks_in(const double2* __restrict__ in, int64_t total, double scale, double2* o64,
                             float2* o32) {
-  const int64_t tot = nblk * n * n;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = e / ((int64_t)n * n);
-    const int64_t r = e - b * n * n;
-    const int p = (int)(r / n), q = (int)(r - (int64_t)p * n);  // row-major destination (p, q)
-    const double2 a = in[b * n * n + (int64_t)q * n + p];      // column-major source
-    const double2 v = make_double2(a.x * scale, a.y * scale);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = make_double2(in[e].x * scale, in[e].y * scale);
     if (o64) o64[e] = v;
     if (o32) o32[e] = make_float2((float)v.x, (float)v.y);
   }
 }
 
-__global__ void k_blocks_out(const double2* __restrict__ i64, const float2* __restrict__ i32, int64_t nblk, int n,
+__global__ void k_blocks_out(const double2* __restrict__ i64, const float2* __restrict__ i32, int64_t total,
                              double scale, double2* __restrict__ out) {
-  const int64_t tot = nblk * n * n;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = e / ((int64_t)n * n);
-    const int64_t r = e - b * n * n;
-    const int q = (int)(r / n), p = (int)(r - (int64_t)q * n);  // column-major destination (p, q)
-    const int64_t src = b * n * n + (int64_t)p * n + q;
-    const double2 a = i64 ? i64[src] : make_double2(i32[src].x, i32[src].y);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const double2 a = i64 ? i64[e] : make_double2(i32[e].x, i32[e].y);
     out[e] = make_double2(a.x * scale, a.y * scale);
   }
 }
@@ -517,12 +507,12 @@ int vs_prec_create(vs_op* op, const double* shift, const double* d, int64_t nd, 
     const double scale = 1.0 / (double)LM;
     if (precisions & VS_BUILD_C64) {
       pr->inv32.alloc(LM * n * n * sizeof(float2));
-      vs::assemble_invert<float>(l2.as<double2>(), op->L, op->M, op->N, sh, dptr, ds, true, false, scale,
+      vs::assemble_invert<float>(l2.as<double2>(), op->L, op->M, op->N, sh, dptr, ds, true, true, scale,
                                  pr->inv32.as<float2>(), status.as<int>(), st);
     }
     if (precisions & VS_BUILD_C128) {
       pr->inv64.alloc(LM * n * n * sizeof(double2));
-      vs::assemble_invert<double>(l2.as<double2>(), op->L, op->M, op->N, sh, dptr, ds, true, false, scale,
+      vs::assemble_invert<double>(l2.as<double2>(), op->L, op->M, op->N, sh, dptr, ds, true, true, scale,
                                   pr->inv64.as<double2>(), status.as<int>(), st);
     }
     int hs = 0;
@@ -568,7 +558,7 @@ int vs_prec_create_blocks(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const do
     if (precisions & VS_BUILD_C128) pr->inv64.alloc(LM * n * n * sizeof(double2));
     const int64_t tot = LM * n * n;
     k_blocks_in<<<(int)std::min<int64_t>(vs::ceil_div(tot, 256), 152 * 32), 256, 0, st>>>(
-        raw.as<double2>(), LM, (int)n, 1.0 / (double)LM, (precisions & VS_BUILD_C128) ? pr->inv64.as<double2>() : nullptr,
+        raw.as<double2>(), tot, 1.0 / (double)LM, (precisions & VS_BUILD_C128) ? pr->inv64.as<double2>() : nullptr,
         (precisions & VS_BUILD_C64) ? pr->inv32.as<float2>() : nullptr);
     VS_LAUNCH_CHECK();
     VS_CUDA(cudaStreamSynchronize(st));
@@ -640,7 +630,7 @@ int vs_prec_get_blocks(vs_prec* prec, int precision, double* out) {
     o.alloc(LM * n * n * sizeof(double2));
     k_blocks_out<<<(int)std::min<int64_t>(vs::ceil_div(LM * n * n, 256), 152 * 32), 256, 0, st>>>(
         precision == VS_C128 ? prec->inv64.as<double2>() : nullptr,
-        precision == VS_C64 ? prec->inv32.as<float2>() : nullptr, LM, (int)n, (double)LM, o.as<double2>());
+        precision == VS_C64 ? prec->inv32.as<float2>() : nullptr, LM * n * n, (double)LM, o.as<double2>());
     VS_LAUNCH_CHECK();
     VS_CUDA(cudaMemcpyAsync(out, o.p, LM * n * n * sizeof(double2), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));

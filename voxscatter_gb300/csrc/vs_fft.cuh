@@ -81,14 +81,21 @@ inline std::vector<double> twiddle_table(int n) {
   return t;
 }
 
-// Smallest m >= n whose prime factors are all in {2,3,5,7}.
+// Smallest m >= n whose prime factors are all in {2,3,5}: lengths the
+// small-radix kernels (radices 2,3,4,5,8 only) transform.
 inline int smooth_size(int n) {
   for (int m = n > 1 ? n : 1;; ++m) {
     int r = m;
-    for (int f : {2, 3, 5, 7})
+    for (int f : {2, 3, 5})
       while (r % f == 0) r /= f;
     if (r == 1) return m;
   }
+}
+
+inline bool plan_is_small_radix(const FftPlan& p) {
+  for (int s = 0; s < p.nstages; ++s)
+    if (!(p.radix[s] == 2 || p.radix[s] == 3 || p.radix[s] == 4 || p.radix[s] == 5 || p.radix[s] == 8)) return false;
+  return true;
 }
 
 #if defined(__CUDACC__) || defined(VS_FFT_HOST_EMULATION)
@@ -287,13 +294,28 @@ __device__ __noinline__ void fft_stage_generic(const C* __restrict__ src, C* __r
 // Transforms `nlines` lines held in `a` (scratch `b` of the same shape).
 // Caller syncs before the call; the function ends with a __syncthreads() and
 // returns the buffer that holds the result.
-template <bool INV, typename C>
+// SMALL = true compiles only the radix-2/3/4/5/8 stages (host dispatches on
+// plan_is_small_radix), which keeps register use down.
+template <bool INV, typename C, bool SMALL = false>
 __device__ C* fft_lines(C* a, C* b, const FftPlan& pl, int nlines, int ls, int es, bool lines_fast,
                         const C* __restrict__ tw) {
   const int n = pl.n;
   int Ns = 1;
   for (int s = 0; s < pl.nstages; ++s) {
     const int R = pl.radix[s];
+    if (SMALL) {
+      switch (R) {
+        case 2: fft_stage<2, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
+        case 3: fft_stage<3, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
+        case 4: fft_stage<4, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
+        case 5: fft_stage<5, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
+        default: fft_stage<8, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
+      }
+      __syncthreads();
+      C* t = a; a = b; b = t;
+      Ns *= R;
+      continue;
+    }
     switch (R) {
       case 2: fft_stage<2, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
       case 3: fft_stage<3, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;

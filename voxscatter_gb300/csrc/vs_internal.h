@@ -89,7 +89,7 @@ struct vs_prec {
   int L = 0, M = 0, N = 0;
   int64_t V = 0, n3 = 0;
   vs::DevBuf map3;          // int32[3V] unknown position of each grid entry (-1: absent)
-  vs::DevBuf inv32, inv64;  // L*M blocks of (3N)^2, row-major, scaled by 1/(L*M)
+  vs::DevBuf inv32, inv64;  // L*M blocks of (3N)^2, column-major, scaled by 1/(L*M)
   vs::FftAxis axL, axM;
   vs::DevBuf t;             // apply scratch (L,M,N,3) per right-hand side
   vs::DevBuf xin, yout;

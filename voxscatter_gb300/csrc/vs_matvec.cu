@@ -18,7 +18,7 @@
 namespace vs {
 
 constexpr int kThreads = 256;
-constexpr size_t kSmemBudget = 100 * 1024;
+constexpr size_t kSmemBudget = 48 * 1024;  // per-CTA tile budget: >= 4 CTAs per SM
 
 void FftAxis::init(int n, cudaStream_t st) {
   plan = make_fft_plan(n);
@@ -33,7 +33,7 @@ void FftAxis::init(int n, cudaStream_t st) {
 }
 
 // ---- pass XF: gather + forward FFT along x ------------------------------
-template <typename T, int MODE>
+template <typename T, int MODE, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_xf(PipeArgs<T> a) {
   using C = cplx_t<T>;
   if (a.skip && *a.skip) return;
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(kThreads) k_xf(PipeArgs<T> a) {
     s0[u] = v;
   }
   __syncthreads();
-  C* res = fft_lines<false>(s0, s1, a.pP, a.lpb, a.P, 1, false, a.twP);
+  C* res = fft_lines<false, C, SMALL>(s0, s1, a.pP, a.lpb, a.P, 1, false, a.twP);
   for (int u = threadIdx.x; u < tot; u += blockDim.x) {
     const int l = u / a.P;
     if (line0 + l < nlines) t1[(int64_t)line0 * a.P + u] = res[u];
@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(kThreads) k_xf(PipeArgs<T> a) {
 }
 
 // ---- pass XI: inverse FFT along x + diagonal + scatter ------------------
-template <typename T, int MODE>
+template <typename T, int MODE, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_xi(PipeArgs<T> a) {
   using C = cplx_t<T>;
   if (a.skip && *a.skip) return;
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(kThreads) k_xi(PipeArgs<T> a) {
     s0[u] = (line0 + l < nlines) ? t1[(int64_t)line0 * a.P + u] : czero<C>();
   }
   __syncthreads();
-  C* res = fft_lines<true>(s0, s1, a.pP, a.lpb, a.P, 1, false, a.twP);
+  C* res = fft_lines<true, C, SMALL>(s0, s1, a.pP, a.lpb, a.P, 1, false, a.twP);
   const int totL = a.lpb * a.L;
   for (int u = threadIdx.x; u < totL; u += blockDim.x) {
     const int l = u / a.L;
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(kThreads) k_xi(PipeArgs<T> a) {
   }
 }
 
-template <typename T, bool INV>
+template <typename T, bool INV, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_strided(StridedArgs<T> a) {
   using C = cplx_t<T>;
   if (a.skip && *a.skip) return;
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kThreads) k_strided(StridedArgs<T> a) {
     s0[u] = (row < a.n_in && x < a.xext) ? src[row * a.s_row + x] : czero<C>();
   }
   __syncthreads();
-  C* res = fft_lines<INV>(s0, s1, a.plan, a.tx, 1, a.tx, true, a.tw);
+  C* res = fft_lines<INV, C, SMALL>(s0, s1, a.plan, a.tx, 1, a.tx, true, a.tw);
   const int totO = a.n_out * a.tx;
   for (int u = threadIdx.x; u < totO; u += blockDim.x) {
     const int row = u / a.tx;
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kThreads) k_strided(StridedArgs<T> a) {
 }
 
 // ---- pass Z: FFT_z ⊗ tensor multiply ⊗ IFFT_z, in place in T2 -----------
-template <typename T>
+template <typename T, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_z(PipeArgs<T> a) {
   using C = cplx_t<T>;
   if (a.skip && *a.skip) return;
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kThreads) k_z(PipeArgs<T> a) {
     s0[u] = (z < a.N && x < a.P) ? t2[x + a.P * (ky + (int64_t)a.Q * (z + (int64_t)a.N * c))] : czero<C>();
   }
   __syncthreads();
-  C* res = fft_lines<false>(s0, s1, a.pR, w, 1, w, true, a.twR);
+  C* res = fft_lines<false, C, SMALL>(s0, s1, a.pR, w, 1, w, true, a.twR);
   const int64_t PQR = PQ * R;
   const int totm = R * tx;
   for (int u = threadIdx.x; u < totm; u += blockDim.x) {
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kThreads) k_z(PipeArgs<T> a) {
   }
   __syncthreads();
   C* other = (res == s0) ? s1 : s0;
-  C* out = fft_lines<true>(res, other, a.pR, w, 1, w, true, a.twR);
+  C* out = fft_lines<true, C, SMALL>(res, other, a.pR, w, 1, w, true, a.twR);
   const int toto = a.N * w;
   for (int u = threadIdx.x; u < toto; u += blockDim.x) {
     const int z = u / w;
@@ -225,11 +225,18 @@ void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaS
   const int nlines = a.M * a.N * 3;
   dim3 grid(ceil_div(nlines, a.lpb), nrhs);
   const size_t smem = 2ull * a.lpb * a.P * sizeof(cplx_t<T>);
-#define VS_X(KER, MD)                              \
-  {                                                \
-    auto k = KER<T, MD>;                           \
-    set_smem(k, smem);                             \
-    k<<<grid, kThreads, smem, st>>>(a);            \
+  const bool small = plan_is_small_radix(a.pP);
+#define VS_X(KER, MD)                                        \
+  {                                                          \
+    if (small) {                                             \
+      auto k = KER<T, MD, true>;                             \
+      set_smem(k, smem);                                     \
+      k<<<grid, kThreads, smem, st>>>(a);                    \
+    } else {                                                 \
+      auto k = KER<T, MD, false>;                            \
+      set_smem(k, smem);                                     \
+      k<<<grid, kThreads, smem, st>>>(a);                    \
+    }                                                        \
   }
   if (!inverse) {
     if (mode == VS_NOTRANSP) VS_X(k_xf, VS_NOTRANSP)
@@ -250,9 +257,15 @@ template <typename T, bool INV>
 void launch_strided_pass(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st) {
   dim3 grid(ceil_div(a.xext, a.tx), nplanes, nrhs);
   const size_t smem = 2ull * a.plan.n * a.tx * sizeof(cplx_t<T>);
-  auto k = k_strided<T, INV>;
-  set_smem(k, smem);
-  k<<<grid, kThreads, smem, st>>>(a);
+  if (plan_is_small_radix(a.plan)) {
+    auto k = k_strided<T, INV, true>;
+    set_smem(k, smem);
+    k<<<grid, kThreads, smem, st>>>(a);
+  } else {
+    auto k = k_strided<T, INV, false>;
+    set_smem(k, smem);
+    k<<<grid, kThreads, smem, st>>>(a);
+  }
   VS_LAUNCH_CHECK();
 }
 
@@ -311,9 +324,15 @@ void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, in
     case 2: {
       dim3 grid(ceil_div(op.P, a.tx), op.Q, nrhs);
       const size_t smem = 2ull * op.R * 3 * a.tx * sizeof(C);
-      auto k = k_z<T>;
-      set_smem(k, smem);
-      k<<<grid, kThreads, smem, st>>>(a);
+      if (plan_is_small_radix(a.pR)) {
+        auto k = k_z<T, true>;
+        set_smem(k, smem);
+        k<<<grid, kThreads, smem, st>>>(a);
+      } else {
+        auto k = k_z<T, false>;
+        set_smem(k, smem);
+        k<<<grid, kThreads, smem, st>>>(a);
+      }
       VS_LAUNCH_CHECK();
       break;
     }

@@ -204,6 +204,9 @@ template void assemble_invert<double>(const double2*, int, int, int, double2, co
                                       double, double2*, int*, cudaStream_t);
 
 // ---- apply: block GEMV on the (x,y)-frequency planes --------------------
+// Inverse blocks are stored column-major (element (r, q) at q*n + r), so the
+// threads that compute consecutive output rows read consecutive addresses of
+// each column; each thread forms one full row sum, no cross-lane reduction.
 template <typename T>
 __global__ void __launch_bounds__(256) k_block_gemv(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ inv, int L,
                                                     int M, int N, int ti, int64_t rhs_stride, const int* skip) {
@@ -223,20 +226,21 @@ __global__ void __launch_bounds__(256) k_block_gemv(cplx_t<T>* __restrict__ t, c
     v[il * n + s] = (i < L) ? tt[i + (int64_t)L * j + LM * s] : czero<C>();
   }
   __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int rr = warp; rr < ti * n; rr += nw) {
+  for (int rr = threadIdx.x; rr < ti * n; rr += blockDim.x) {
     const int il = rr / n, r = rr - il * n;
     const int i = i0 + il;
     if (i >= L) continue;
-    const C* row = inv + (((int64_t)i + (int64_t)L * j) * n + r) * n;
-    C acc = czero<C>();
-    for (int s = lane; s < n; s += 32) acc = cfma(__ldg(row + s), v[il * n + s], acc);
-#pragma unroll
-    for (int off = 16; off; off >>= 1) {
-      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, off);
-      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, off);
+    const C* A = inv + ((int64_t)i + (int64_t)L * j) * n * n + r;
+    const C* x = v + il * n;
+    C acc0 = czero<C>(), acc1 = czero<C>();
+    int q = 0;
+#pragma unroll 4
+    for (; q + 1 < n; q += 2) {
+      acc0 = cfma(__ldg(A + (int64_t)q * n), x[q], acc0);
+      acc1 = cfma(__ldg(A + (int64_t)(q + 1) * n), x[q + 1], acc1);
     }
-    if (lane == 0) o[il * n + r] = acc;
+    if (q < n) acc0 = cfma(__ldg(A + (int64_t)q * n), x[q], acc0);
+    o[il * n + r] = cadd(acc0, acc1);
   }
   __syncthreads();
   for (int u = threadIdx.x; u < ti * n; u += blockDim.x) {
@@ -268,7 +272,7 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
   s.src = t; s.dst = t;
   s.xext = L; s.n_in = M; s.n_out = M;
   int tx = 32;
-  while (tx > 1 && 2ull * M * tx * sizeof(C) > 100 * 1024) tx >>= 1;
+  while (tx > 1 && 2ull * M * tx * sizeof(C) > 48 * 1024) tx >>= 1;
   s.tx = tx;
   s.na = 3 * N;
   s.s_row = s.d_row = L;
