@@ -1,7 +1,8 @@
 // Sequential host emulation of the device Stockham FFT (vs_fft.cuh).
-// Every stage reads one buffer and writes the other, so running all butterflies
-// of a stage in one "thread" is exactly what the CTA computes.  Compares
-// forward and inverse transforms against a naive O(n^2) DFT in long double.
+// Every stage reads one buffer and writes the other, so running the 256
+// threads of a CTA one after another, stage by stage, computes exactly what
+// the CTA computes.  Compares forward and inverse transforms against a naive
+// O(n^2) DFT in long double, for several thread layouts.
 #include <cuda_runtime.h>
 struct VsDim { unsigned x = 0, y = 0, z = 0; };
 static VsDim threadIdx;
@@ -16,8 +17,20 @@ static VsDim blockDim = {1, 1, 1};
 #include <cstdlib>
 #include <vector>
 
+template <bool INV, typename C, bool SMALL>
+static C* emulate(C* a, C* b, const vs::FftPlan& pl, int nlines, int ls, int es, vs::FftLayout lay, const C* tw) {
+  int Ns = 1;
+  for (int s = 0; s < pl.nstages; ++s) {
+    for (int t = 0; t < vs::kFftThreads; ++t)
+      vs::fft_stage_any<INV, C, SMALL>(a, b, pl.n, pl.radix[s], Ns, nlines, ls, es, lay, tw, t);
+    C* tmp = a; a = b; b = tmp;
+    Ns *= pl.radix[s];
+  }
+  return a;
+}
+
 template <typename T, bool INV>
-static double check(int n, int nlines, bool lines_fast) {
+static double check(int n, int nlines, bool lines_fast, int lg_nl = 0) {
   using C = vs::cplx_t<T>;
   vs::FftPlan pl = vs::make_fft_plan(n);
   std::vector<double> tw = vs::twiddle_table(n);
@@ -33,7 +46,9 @@ static double check(int n, int nlines, bool lines_fast) {
       a[l * ls + p * es].x = (T)re; a[l * ls + p * es].y = (T)im;
       in_re[l * n + p] = (T)re; in_im[l * n + p] = (T)im;
     }
-  C* res = vs::fft_lines<INV>(a.data(), b.data(), pl, nlines, ls, es, lines_fast, twc.data());
+  const vs::FftLayout lay{lg_nl, lines_fast};
+  C* res = vs::plan_is_small_radix(pl) ? emulate<INV, C, true>(a.data(), b.data(), pl, nlines, ls, es, lay, twc.data())
+                                       : emulate<INV, C, false>(a.data(), b.data(), pl, nlines, ls, es, lay, twc.data());
   double err = 0, ref = 0;
   const long double sg = INV ? 1.0L : -1.0L;
   for (int l = 0; l < nlines; ++l)
@@ -58,9 +73,10 @@ int main() {
   int bad = 0;
   for (int n : sizes) {
     for (int lf = 0; lf < 2; ++lf) {
-      const int nl = lf ? 3 : 2;
-      double e1 = check<double, false>(n, nl, lf), e2 = check<double, true>(n, nl, lf);
-      double e3 = check<float, false>(n, nl, lf), e4 = check<float, true>(n, nl, lf);
+      const int nl = lf ? 5 : 3;
+      const int lg = (n % 3) + (lf ? 2 : 0);  // vary the number of line slots (1..16)
+      double e1 = check<double, false>(n, nl, lf, lg), e2 = check<double, true>(n, nl, lf, lg);
+      double e3 = check<float, false>(n, nl, lf, lg), e4 = check<float, true>(n, nl, lf, lg);
       const bool ok = e1 < 1e-14 && e2 < 1e-14 && e3 < 2e-6 && e4 < 2e-6;
       if (!ok) ++bad;
       printf("n=%5d lines_fast=%d  f64 %.2e %.2e  f32 %.2e %.2e %s\n", n, lf, e1, e2, e3, e4, ok ? "ok" : "BAD");

@@ -235,100 +235,141 @@ struct Butterfly {
   }
 };
 
+// Thread layout of a CTA of kFftThreads threads over a batch of lines: NL =
+// 2^lg_nl line slots times NJ = kFftThreads/NL butterfly slots.  With
+// lines_fast, consecutive threads take consecutive line slots (lines
+// interleaved in shared memory, ls = 1); otherwise consecutive threads take
+// consecutive butterflies of one line (lines contiguous, es = 1).  Lines
+// beyond NL are handled by the same slot in steps of NL.
+constexpr int kFftThreads = 256;
+
+struct FftLayout {
+  int lg_nl;       // log2 of the number of line slots
+  bool lines_fast; // see above
+  __host__ __device__ int nl() const { return 1 << lg_nl; }
+};
+
+// One radix-R Stockham stage over all lines for thread `t`.
+// Butterfly j of a line reads R points at stride m = n/R, applies the twiddles
+// w_n^(r*k*n/(Ns*R)) with k = j mod Ns, and writes the R outputs at
+// (j - k)*R + k + q*Ns.  j advances by NJ per iteration; (j div Ns, j mod Ns)
+// are advanced incrementally, so there is one runtime division per stage.
 template <int R, bool INV, typename C>
 __device__ __forceinline__ void fft_stage(const C* __restrict__ src, C* __restrict__ dst, int n, int Ns, int nlines,
-                                          int ls, int es, bool lines_fast, const C* __restrict__ tw) {
+                                          int ls, int es, FftLayout lay, const C* __restrict__ tw, int t) {
+  const int lg_nl = lay.lg_nl;
+  const int NL = 1 << lg_nl;
+  const int lg_nj = 8 - lg_nl;  // kFftThreads = 256
+  const int NJ = 1 << lg_nj;
+  const int lslot = lay.lines_fast ? (t & (NL - 1)) : (t >> lg_nj);
+  const int jt = lay.lines_fast ? (t >> lg_nl) : (t & (NJ - 1));
   const int m = n / R;
-  const int total = nlines * m;
+  if (jt >= m) return;
   const int step = n / (Ns * R);
-  for (int u = threadIdx.x; u < total; u += blockDim.x) {
-    int line, j;
-    if (lines_fast) { line = u % nlines; j = u / nlines; }
-    else { line = u / m; j = u - line * m; }
+  const int q0 = jt / Ns, k0 = jt - q0 * Ns;
+  const int dq = NJ / Ns, dk = NJ - dq * Ns;
+  const int me = m * es, nse = Ns * es, rnse = R * nse;
+  for (int line = lslot; line < nlines; line += NL) {
     const C* s = src + line * ls;
     C* d = dst + line * ls;
-    const int k = j % Ns;
-    C v[R];
+    int q = q0, k = k0;
+    for (int j = jt; j < m; j += NJ) {
+      C v[R];
+      const C* sj = s + j * es;
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = s[(j + r * m) * es];
-    if (Ns > 1) {
+      for (int r = 0; r < R; ++r) v[r] = sj[r * me];
+      if (Ns > 1) {
+        const int ks = k * step;
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], twid<INV>(tw, r * k * step));
+        for (int r = 1; r < R; ++r) v[r] = cmul(v[r], twid<INV>(tw, r * ks));
+      }
+      Butterfly<R, INV, C>::run(v, tw, n);
+      C* dq_ = d + q * rnse + k * es;
+#pragma unroll
+      for (int qq = 0; qq < R; ++qq) dq_[qq * nse] = v[qq];
+      k += dk;
+      q += dq;
+      if (k >= Ns) { k -= Ns; ++q; }
     }
-    Butterfly<R, INV, C>::run(v, tw, n);
-    const int base = (j - k) * R + k;
-#pragma unroll
-    for (int q = 0; q < R; ++q) d[(base + q * Ns) * es] = v[q];
   }
 }
 
 template <bool INV, typename C>
 __device__ __noinline__ void fft_stage_generic(const C* __restrict__ src, C* __restrict__ dst, int n, int R, int Ns,
-                                               int nlines, int ls, int es, bool lines_fast,
-                                               const C* __restrict__ tw) {
+                                               int nlines, int ls, int es, FftLayout lay, const C* __restrict__ tw,
+                                               int t) {
+  const int lg_nl = lay.lg_nl;
+  const int NL = 1 << lg_nl;
+  const int lg_nj = 8 - lg_nl;
+  const int NJ = 1 << lg_nj;
+  const int lslot = lay.lines_fast ? (t & (NL - 1)) : (t >> lg_nj);
+  const int jt = lay.lines_fast ? (t >> lg_nl) : (t & (NJ - 1));
   const int m = n / R;
-  const int total = nlines * m;
+  if (jt >= m) return;
   const int step = n / (Ns * R);
   const int st = n / R;
   C v[FFT_MAX_GENERIC_RADIX];
-  for (int u = threadIdx.x; u < total; u += blockDim.x) {
-    int line, j;
-    if (lines_fast) { line = u % nlines; j = u / nlines; }
-    else { line = u / m; j = u - line * m; }
+  for (int line = lslot; line < nlines; line += NL) {
     const C* s = src + line * ls;
     C* d = dst + line * ls;
-    const int k = j % Ns;
-    for (int r = 0; r < R; ++r) {
-      C a = s[(j + r * m) * es];
-      v[r] = (r > 0 && Ns > 1) ? cmul(a, twid<INV>(tw, r * k * step)) : a;
-    }
-    const int base = (j - k) * R + k;
-    for (int q = 0; q < R; ++q) {
-      C acc = v[0];
-      for (int r = 1; r < R; ++r) acc = cfma(v[r], twid<INV>(tw, ((r * q) % R) * st), acc);
-      d[(base + q * Ns) * es] = acc;
+    for (int j = jt; j < m; j += NJ) {
+      const int k = j % Ns;
+      for (int r = 0; r < R; ++r) {
+        const C a = s[(j + r * m) * es];
+        v[r] = (r > 0 && Ns > 1) ? cmul(a, twid<INV>(tw, r * k * step)) : a;
+      }
+      const int base = (j - k) * R + k;
+      for (int q = 0; q < R; ++q) {
+        C acc = v[0];
+        int idx = 0;
+        for (int r = 1; r < R; ++r) {
+          idx += q;
+          if (idx >= R) idx -= R;
+          acc = cfma(v[r], twid<INV>(tw, idx * st), acc);
+        }
+        d[(base + q * Ns) * es] = acc;
+      }
     }
   }
 }
 
+// One stage for thread t; SMALL compiles only radices 2,3,4,5,8.
+template <bool INV, typename C, bool SMALL>
+__device__ __forceinline__ void fft_stage_any(const C* src, C* dst, int n, int R, int Ns, int nlines, int ls, int es,
+                                              FftLayout lay, const C* tw, int t) {
+  switch (R) {
+    case 2: fft_stage<2, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+    case 3: fft_stage<3, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+    case 4: fft_stage<4, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+    case 5: fft_stage<5, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+    case 8: fft_stage<8, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+    default:
+      if (!SMALL) {
+        switch (R) {
+          case 7: fft_stage<7, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+          case 11: fft_stage<11, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+          case 13: fft_stage<13, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+          default: fft_stage_generic<INV>(src, dst, n, R, Ns, nlines, ls, es, lay, tw, t); break;
+        }
+      }
+      break;
+  }
+}
+
 // Transforms `nlines` lines held in `a` (scratch `b` of the same shape).
-// Caller syncs before the call; the function ends with a __syncthreads() and
-// returns the buffer that holds the result.
-// SMALL = true compiles only the radix-2/3/4/5/8 stages (host dispatches on
-// plan_is_small_radix), which keeps register use down.
+// Element p of line b is at buf[b*ls + p*es].  The caller syncs before the
+// call; the function ends with a __syncthreads() and returns the buffer that
+// holds the result.
 template <bool INV, typename C, bool SMALL = false>
-__device__ C* fft_lines(C* a, C* b, const FftPlan& pl, int nlines, int ls, int es, bool lines_fast,
+__device__ C* fft_lines(C* a, C* b, const FftPlan& pl, int nlines, int ls, int es, FftLayout lay,
                         const C* __restrict__ tw) {
   const int n = pl.n;
   int Ns = 1;
   for (int s = 0; s < pl.nstages; ++s) {
     const int R = pl.radix[s];
-    if (SMALL) {
-      switch (R) {
-        case 2: fft_stage<2, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
-        case 3: fft_stage<3, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
-        case 4: fft_stage<4, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
-        case 5: fft_stage<5, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
-        default: fft_stage<8, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
-      }
-      __syncthreads();
-      C* t = a; a = b; b = t;
-      Ns *= R;
-      continue;
-    }
-    switch (R) {
-      case 2: fft_stage<2, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
-      case 3: fft_stage<3, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
-      case 4: fft_stage<4, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
-      case 5: fft_stage<5, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
-      case 7: fft_stage<7, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
-      case 8: fft_stage<8, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
-      case 11: fft_stage<11, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
-      case 13: fft_stage<13, INV>(a, b, n, Ns, nlines, ls, es, lines_fast, tw); break;
-      default: fft_stage_generic<INV>(a, b, n, R, Ns, nlines, ls, es, lines_fast, tw); break;
-    }
+    fft_stage_any<INV, C, SMALL>(a, b, n, R, Ns, nlines, ls, es, lay, tw, (int)threadIdx.x);
     __syncthreads();
-    C* t = a; a = b; b = t;
+    C* tmp = a; a = b; b = tmp;
     Ns *= R;
   }
   return a;

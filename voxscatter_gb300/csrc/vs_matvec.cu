@@ -32,43 +32,55 @@ void FftAxis::init(int n, cudaStream_t st) {
   VS_CUDA(cudaStreamSynchronize(st));
 }
 
+// log2 of a power of two
+__host__ __device__ __forceinline__ int ilog2(int v) {
+  int l = 0;
+  while ((1 << l) < v) ++l;
+  return l;
+}
+
 // ---- pass XF: gather + forward FFT along x ------------------------------
+// One line (j, k, comp) per line slot; lines contiguous in shared memory.
 template <typename T, int MODE, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_xf(PipeArgs<T> a) {
   using C = cplx_t<T>;
   if (a.skip && *a.skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lg_nl = a.lg_lpb, lg_nj = 8 - lg_nl, NJ = 1 << lg_nj;
+  const int nlpb = 1 << lg_nl;
   C* s0 = reinterpret_cast<C*>(smem_raw);
-  C* s1 = s0 + a.lpb * a.P;
+  C* s1 = s0 + nlpb * a.P;
   const int rhs = blockIdx.y;
   const C* x = a.x + (int64_t)rhs * a.n3;
   C* t1 = a.t1 + (int64_t)rhs * a.P * a.M * a.N * 3;
   const int nlines = a.M * a.N * 3;
-  const int line0 = blockIdx.x * a.lpb;
   const int MN = a.M * a.N;
-  const int tot = a.lpb * a.P;
-  for (int u = threadIdx.x; u < tot; u += blockDim.x) {
-    const int l = u / a.P;
-    const int i = u - l * a.P;
-    const int line = line0 + l;
+  const int l = threadIdx.x >> lg_nj, jt = threadIdx.x & (NJ - 1);
+  const int line = blockIdx.x * nlpb + l;
+  const bool live = line < nlines;
+  const int c = live ? line / MN : 0;
+  const int jk = line - c * MN;
+  const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
+  C* row = s0 + l * a.P;
+  for (int i = jt; i < a.P; i += NJ) {
     C v = czero<C>();
-    if (line < nlines && i < a.L) {
-      const int c = line / MN;
-      const int jk = line - c * MN;
-      const int pos = __ldg(a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L + i);
+    if (live && i < a.L) {
+      const int pos = __ldg(map + i);
       if (pos >= 0) {
         v = x[pos];
         if (MODE == VS_TRANSP) v = cmul(a.d2.at(pos), v);
         if (MODE == VS_CONJTRANSP) v = cmul(a.d2.at(pos), cconj(v));
       }
     }
-    s0[u] = v;
+    row[i] = v;
   }
   __syncthreads();
-  C* res = fft_lines<false, C, SMALL>(s0, s1, a.pP, a.lpb, a.P, 1, false, a.twP);
-  for (int u = threadIdx.x; u < tot; u += blockDim.x) {
-    const int l = u / a.P;
-    if (line0 + l < nlines) t1[(int64_t)line0 * a.P + u] = res[u];
+  const FftLayout lay{lg_nl, false};
+  C* res = fft_lines<false, C, SMALL>(s0, s1, a.pP, nlpb, a.P, 1, lay, a.twP);
+  if (live) {
+    C* out = t1 + (int64_t)line * a.P;
+    const C* r = res + l * a.P;
+    for (int i = jt; i < a.P; i += NJ) out[i] = r[i];
   }
 }
 
@@ -78,134 +90,143 @@ __global__ void __launch_bounds__(kThreads) k_xi(PipeArgs<T> a) {
   using C = cplx_t<T>;
   if (a.skip && *a.skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lg_nl = a.lg_lpb, lg_nj = 8 - lg_nl, NJ = 1 << lg_nj;
+  const int nlpb = 1 << lg_nl;
   C* s0 = reinterpret_cast<C*>(smem_raw);
-  C* s1 = s0 + a.lpb * a.P;
+  C* s1 = s0 + nlpb * a.P;
   const int rhs = blockIdx.y;
   const C* x = a.x + (int64_t)rhs * a.n3;
   C* y = a.y + (int64_t)rhs * a.n3;
   const C* t1 = a.t1 + (int64_t)rhs * a.P * a.M * a.N * 3;
   const int nlines = a.M * a.N * 3;
-  const int line0 = blockIdx.x * a.lpb;
   const int MN = a.M * a.N;
-  const int tot = a.lpb * a.P;
-  for (int u = threadIdx.x; u < tot; u += blockDim.x) {
-    const int l = u / a.P;
-    s0[u] = (line0 + l < nlines) ? t1[(int64_t)line0 * a.P + u] : czero<C>();
+  const int l = threadIdx.x >> lg_nj, jt = threadIdx.x & (NJ - 1);
+  const int line = blockIdx.x * nlpb + l;
+  const bool live = line < nlines;
+  {
+    C* row = s0 + l * a.P;
+    const C* in = t1 + (int64_t)line * a.P;
+    for (int i = jt; i < a.P; i += NJ) row[i] = live ? in[i] : czero<C>();
   }
   __syncthreads();
-  C* res = fft_lines<true, C, SMALL>(s0, s1, a.pP, a.lpb, a.P, 1, false, a.twP);
-  const int totL = a.lpb * a.L;
-  for (int u = threadIdx.x; u < totL; u += blockDim.x) {
-    const int l = u / a.L;
-    const int i = u - l * a.L;
-    const int line = line0 + l;
-    if (line >= nlines) continue;
-    const int c = line / MN;
-    const int jk = line - c * MN;
-    const int pos = __ldg(a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L + i);
+  const FftLayout lay{lg_nl, false};
+  C* res = fft_lines<true, C, SMALL>(s0, s1, a.pP, nlpb, a.P, 1, lay, a.twP);
+  if (!live) return;
+  const int c = line / MN;
+  const int jk = line - c * MN;
+  const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
+  const C* r = res + l * a.P;
+  for (int i = jt; i < a.L; i += NJ) {
+    const int pos = __ldg(map + i);
     if (pos < 0) continue;
-    const C conv = res[l * a.P + i];
-    const C xv = (MODE == MODE_PLAIN) ? conv : x[pos];
+    const C conv = r[i];
     C out;
-    if (MODE == VS_NOTRANSP) out = csub(cmul(a.d1.at(pos), xv), cmul(a.d2.at(pos), conv));
-    else if (MODE == VS_TRANSP) out = csub(cmul(a.d1.at(pos), xv), conv);
-    else if (MODE == VS_CONJTRANSP) out = csub(cmul(a.d1c.at(pos), xv), cconj(conv));
-    else out = conv;
+    if (MODE == MODE_PLAIN) {
+      out = conv;
+    } else {
+      const C xv = x[pos];
+      if (MODE == VS_NOTRANSP) out = csub(cmul(a.d1.at(pos), xv), cmul(a.d2.at(pos), conv));
+      else if (MODE == VS_TRANSP) out = csub(cmul(a.d1.at(pos), xv), conv);
+      else out = csub(cmul(a.d1c.at(pos), xv), cconj(conv));
+    }
     y[pos] = out;
   }
 }
 
+// ---- strided-axis pass (y of the pipeline; y and z of the setup FFTs) ----
 template <typename T, bool INV, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_strided(StridedArgs<T> a) {
   using C = cplx_t<T>;
   if (a.skip && *a.skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = a.plan.n;
+  const int lg_nl = a.lg_tx, tx = 1 << lg_nl, NJ = kThreads >> lg_nl;
   C* s0 = reinterpret_cast<C*>(smem_raw);
-  C* s1 = s0 + n * a.tx;
-  const int x0 = blockIdx.x * a.tx;
+  C* s1 = s0 + n * tx;
+  const int x0 = blockIdx.x * tx;
   const int pa = blockIdx.y % a.na;
   const int pb = blockIdx.y / a.na;
   const C* src = a.src + pa * a.s_a + pb * a.s_b + (int64_t)blockIdx.z * a.s_rhs;
   C* dst = a.dst + pa * a.d_a + pb * a.d_b + (int64_t)blockIdx.z * a.d_rhs;
-  const int tot = n * a.tx;
-  for (int u = threadIdx.x; u < tot; u += blockDim.x) {
-    const int row = u / a.tx;
-    const int xl = u - row * a.tx;
-    const int x = x0 + xl;
-    s0[u] = (row < a.n_in && x < a.xext) ? src[row * a.s_row + x] : czero<C>();
-  }
+  const int xl = threadIdx.x & (tx - 1), r0 = threadIdx.x >> lg_nl;
+  const int x = x0 + xl;
+  const bool xin = x < a.xext;
+  for (int row = r0; row < n; row += NJ)
+    s0[row * tx + xl] = (row < a.n_in && xin) ? src[row * a.s_row + x] : czero<C>();
   __syncthreads();
-  C* res = fft_lines<INV, C, SMALL>(s0, s1, a.plan, a.tx, 1, a.tx, true, a.tw);
-  const int totO = a.n_out * a.tx;
-  for (int u = threadIdx.x; u < totO; u += blockDim.x) {
-    const int row = u / a.tx;
-    const int xl = u - row * a.tx;
-    const int x = x0 + xl;
-    if (x < a.xext) dst[row * a.d_row + x] = res[u];
-  }
+  const FftLayout lay{lg_nl, true};
+  C* res = fft_lines<INV, C, SMALL>(s0, s1, a.plan, tx, 1, tx, lay, a.tw);
+  if (xin)
+    for (int row = r0; row < a.n_out; row += NJ) dst[row * a.d_row + x] = res[row * tx + xl];
 }
 
 // ---- pass Z: FFT_z ⊗ tensor multiply ⊗ IFFT_z, in place in T2 -----------
+// Lines (comp c, x) are interleaved: element z of line c*tx + xl at
+// z*(3*tx) + c*tx + xl.
 template <typename T, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_z(PipeArgs<T> a) {
   using C = cplx_t<T>;
   if (a.skip && *a.skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int R = a.R, tx = a.tx, w = 3 * tx;
+  const int R = a.R;
+  const int lg_nl = a.lg_tx, tx = 1 << lg_nl, NJ = kThreads >> lg_nl;
+  const int w = 3 * tx;
   C* s0 = reinterpret_cast<C*>(smem_raw);
   C* s1 = s0 + R * w;
   const int x0 = blockIdx.x * tx;
   const int ky = blockIdx.y;
   const int64_t PQ = (int64_t)a.P * a.Q;
-  C* t2 = a.t2 + (int64_t)blockIdx.z * PQ * a.N * 3;
-  const int tot = R * w;
-  for (int u = threadIdx.x; u < tot; u += blockDim.x) {
-    const int z = u / w;
-    const int rem = u - z * w;
-    const int c = rem / tx;
-    const int xl = rem - c * tx;
-    const int x = x0 + xl;
-    s0[u] = (z < a.N && x < a.P) ? t2[x + a.P * (ky + (int64_t)a.Q * (z + (int64_t)a.N * c))] : czero<C>();
-  }
+  const int64_t zs = PQ, cs = PQ * a.N;  // T2 strides of z and comp
+  C* t2 = a.t2 + (int64_t)blockIdx.z * PQ * a.N * 3 + (int64_t)ky * a.P;
+  const int xl = threadIdx.x & (tx - 1), r0 = threadIdx.x >> lg_nl;
+  const int x = x0 + xl;
+  const bool xin = x < a.P;
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    for (int z = r0; z < R; z += NJ)
+      s0[z * w + c * tx + xl] = (z < a.N && xin) ? t2[x + z * zs + c * cs] : czero<C>();
   __syncthreads();
-  C* res = fft_lines<false, C, SMALL>(s0, s1, a.pR, w, 1, w, true, a.twR);
+  const FftLayout lay{lg_nl, true};
+  C* res = fft_lines<false, C, SMALL>(s0, s1, a.pR, w, 1, w, lay, a.twR);
   const int64_t PQR = PQ * R;
-  const int totm = R * tx;
-  for (int u = threadIdx.x; u < totm; u += blockDim.x) {
-    const int kz = u / tx;
-    const int xl = u - kz * tx;
-    const int x = x0 + xl;
-    if (x >= a.P) continue;
-    const int64_t gi = x + a.P * (ky + (int64_t)a.Q * kz);
-    const C g0 = __ldg(a.G + gi), g1 = __ldg(a.G + PQR + gi), g2 = __ldg(a.G + 2 * PQR + gi);
-    const C g3 = __ldg(a.G + 3 * PQR + gi), g4 = __ldg(a.G + 4 * PQR + gi), g5 = __ldg(a.G + 5 * PQR + gi);
-    C* p = res + kz * w + xl;
-    const C v0 = p[0], v1 = p[tx], v2 = p[2 * tx];
-    p[0] = cmul(g0, v0); p[0] = cfma(g1, v1, p[0]); p[0] = cfma(g2, v2, p[0]);
-    C o1 = cmul(g1, v0); o1 = cfma(g3, v1, o1); o1 = cfma(g4, v2, o1);
-    C o2 = cmul(g2, v0); o2 = cfma(g4, v1, o2); o2 = cfma(g5, v2, o2);
-    p[tx] = o1;
-    p[2 * tx] = o2;
+  if (xin) {
+    const C* G = a.G + x + (int64_t)a.P * ky;
+    for (int kz = r0; kz < R; kz += NJ) {
+      const int64_t gi = kz * PQ;
+      const C g0 = __ldg(G + gi), g1 = __ldg(G + PQR + gi), g2 = __ldg(G + 2 * PQR + gi);
+      const C g3 = __ldg(G + 3 * PQR + gi), g4 = __ldg(G + 4 * PQR + gi), g5 = __ldg(G + 5 * PQR + gi);
+      C* p = res + kz * w + xl;
+      const C v0 = p[0], v1 = p[tx], v2 = p[2 * tx];
+      C o0 = cmul(g0, v0); o0 = cfma(g1, v1, o0); o0 = cfma(g2, v2, o0);
+      C o1 = cmul(g1, v0); o1 = cfma(g3, v1, o1); o1 = cfma(g4, v2, o1);
+      C o2 = cmul(g2, v0); o2 = cfma(g4, v1, o2); o2 = cfma(g5, v2, o2);
+      p[0] = o0;
+      p[tx] = o1;
+      p[2 * tx] = o2;
+    }
   }
   __syncthreads();
   C* other = (res == s0) ? s1 : s0;
-  C* out = fft_lines<true, C, SMALL>(res, other, a.pR, w, 1, w, true, a.twR);
-  const int toto = a.N * w;
-  for (int u = threadIdx.x; u < toto; u += blockDim.x) {
-    const int z = u / w;
-    const int rem = u - z * w;
-    const int c = rem / tx;
-    const int xl = rem - c * tx;
-    const int x = x0 + xl;
-    if (x < a.P) t2[x + a.P * (ky + (int64_t)a.Q * (z + (int64_t)a.N * c))] = out[u];
+  C* out = fft_lines<true, C, SMALL>(res, other, a.pR, w, 1, w, lay, a.twR);
+  if (xin) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      for (int z = r0; z < a.N; z += NJ) t2[x + z * zs + c * cs] = out[z * w + c * tx + xl];
   }
 }
 
+// Largest power-of-two tile width <= 16 whose two buffers fit the budget.
 static int pick_tile(int n, size_t csize, int width_mult) {
-  int tx = 32;
+  int tx = 16;
   while (tx > 1 && 2ull * n * tx * width_mult * csize > kSmemBudget) tx >>= 1;
   return tx;
+}
+
+// Lines per CTA of the x passes: power of two <= 8 within the budget.
+static int pick_lpb(int n, size_t csize) {
+  int l = 8;
+  while (l > 1 && 2ull * n * l * csize > kSmemBudget) l >>= 1;
+  return l;
 }
 
 template <typename K>
@@ -223,8 +244,9 @@ void ensure_scratch(vs_op& op, int nrhs, size_t elem_bytes) {
 template <typename T>
 void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaStream_t st) {
   const int nlines = a.M * a.N * 3;
-  dim3 grid(ceil_div(nlines, a.lpb), nrhs);
-  const size_t smem = 2ull * a.lpb * a.P * sizeof(cplx_t<T>);
+  const int lpb = 1 << a.lg_lpb;
+  dim3 grid(ceil_div(nlines, lpb), nrhs);
+  const size_t smem = 2ull * lpb * a.P * sizeof(cplx_t<T>);
   const bool small = plan_is_small_radix(a.pP);
 #define VS_X(KER, MD)                                        \
   {                                                          \
@@ -255,8 +277,9 @@ void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaS
 
 template <typename T, bool INV>
 void launch_strided_pass(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st) {
-  dim3 grid(ceil_div(a.xext, a.tx), nplanes, nrhs);
-  const size_t smem = 2ull * a.plan.n * a.tx * sizeof(cplx_t<T>);
+  const int tx = 1 << a.lg_tx;
+  dim3 grid(ceil_div(a.xext, tx), nplanes, nrhs);
+  const size_t smem = 2ull * a.plan.n * tx * sizeof(cplx_t<T>);
   if (plan_is_small_radix(a.plan)) {
     auto k = k_strided<T, INV, true>;
     set_smem(k, smem);
@@ -278,7 +301,7 @@ static StridedArgs<T> y_pass_args(const vs_op& op, const PipeArgs<T>& a, bool in
   s.xext = op.P;
   s.n_in = inverse ? op.Q : op.M;
   s.n_out = inverse ? op.M : op.Q;
-  s.tx = pick_tile(op.Q, sizeof(cplx_t<T>), 1);
+  s.lg_tx = ilog2(pick_tile(op.Q, sizeof(cplx_t<T>), 1));
   s.na = op.N * 3;
   s.s_row = op.P; s.d_row = op.P;
   s.s_a = inverse ? pq : pm; s.d_a = inverse ? pm : pq;
@@ -306,8 +329,8 @@ static PipeArgs<T> pipe_args(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, 
   a.G = std::is_same<T, float>::value ? (const C*)op.G32.p : (const C*)op.G64.p;
   a.twP = op.ax[0].tw<T>(); a.twQ = op.ax[1].tw<T>(); a.twR = op.ax[2].tw<T>();
   a.pP = op.ax[0].plan; a.pQ = op.ax[1].plan; a.pR = op.ax[2].plan;
-  a.lpb = std::max(1, 2048 / op.P);
-  a.tx = pick_tile(op.R, sizeof(C), 3);
+  a.lg_lpb = ilog2(pick_lpb(op.P, sizeof(C)));
+  a.lg_tx = ilog2(pick_tile(op.R, sizeof(C), 3));
   a.skip = skip;
   return a;
 }
@@ -322,8 +345,9 @@ void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, in
     case 0: launch_x_pass<T>(a, false, mode, nrhs, st); break;
     case 1: launch_strided_pass<T, false>(y_pass_args<T>(op, a, false), op.N * 3, nrhs, st); break;
     case 2: {
-      dim3 grid(ceil_div(op.P, a.tx), op.Q, nrhs);
-      const size_t smem = 2ull * op.R * 3 * a.tx * sizeof(C);
+      const int tx = 1 << a.lg_tx;
+      dim3 grid(ceil_div(op.P, tx), op.Q, nrhs);
+      const size_t smem = 2ull * op.R * 3 * tx * sizeof(C);
       if (plan_is_small_radix(a.pR)) {
         auto k = k_z<T, true>;
         set_smem(k, smem);
@@ -361,30 +385,32 @@ template void matvec<double>(const vs_op&, const double2*, double2*, int, int, c
 
 // ---- generic batched FFTs (operator setup, preconditioner) --------------
 template <typename T, bool INV>
-__global__ void __launch_bounds__(kThreads) k_axis0(cplx_t<T>* data, int n, int64_t nlines, int lpb, FftPlan plan,
+__global__ void __launch_bounds__(kThreads) k_axis0(cplx_t<T>* data, int n, int64_t nlines, int lg_lpb, FftPlan plan,
                                                     const cplx_t<T>* tw) {
   using C = cplx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lpb = 1 << lg_lpb, lg_nj = 8 - lg_lpb, NJ = 1 << lg_nj;
   C* s0 = reinterpret_cast<C*>(smem_raw);
   C* s1 = s0 + lpb * n;
-  const int64_t line0 = (int64_t)blockIdx.x * lpb;
-  const int tot = lpb * n;
-  C* base = data + line0 * n;
-  for (int u = threadIdx.x; u < tot; u += blockDim.x)
-    s0[u] = (line0 + u / n < nlines) ? base[u] : czero<C>();
+  const int l = threadIdx.x >> lg_nj, jt = threadIdx.x & (NJ - 1);
+  const int64_t line = (int64_t)blockIdx.x * lpb + l;
+  const bool live = line < nlines;
+  C* base = data + line * n;
+  for (int i = jt; i < n; i += NJ) s0[l * n + i] = live ? base[i] : czero<C>();
   __syncthreads();
-  C* res = fft_lines<INV>(s0, s1, plan, lpb, n, 1, false, tw);
-  for (int u = threadIdx.x; u < tot; u += blockDim.x)
-    if (line0 + u / n < nlines) base[u] = res[u];
+  const FftLayout lay{lg_lpb, false};
+  C* res = fft_lines<INV, C, false>(s0, s1, plan, lpb, n, 1, lay, tw);
+  if (live)
+    for (int i = jt; i < n; i += NJ) base[i] = res[l * n + i];
 }
 
 template <typename T, bool INV>
 void fft_axis0(cplx_t<T>* data, int n, int64_t nlines, const FftAxis& ax, cudaStream_t st) {
-  const int lpb = std::max(1, 2048 / n);
+  const int lpb = pick_lpb(n, sizeof(cplx_t<T>));
   const size_t smem = 2ull * lpb * n * sizeof(cplx_t<T>);
   auto k = k_axis0<T, INV>;
   set_smem(k, smem);
-  k<<<ceil_div(nlines, lpb), kThreads, smem, st>>>(data, n, nlines, lpb, ax.plan, ax.tw<T>());
+  k<<<ceil_div(nlines, lpb), kThreads, smem, st>>>(data, n, nlines, ilog2(lpb), ax.plan, ax.tw<T>());
   VS_LAUNCH_CHECK();
 }
 
@@ -394,7 +420,7 @@ void fft_strided(cplx_t<T>* data, int xext, int n, int64_t row_stride, int na, i
   StridedArgs<T> s;
   s.src = data; s.dst = data;
   s.xext = xext; s.n_in = n; s.n_out = n;
-  s.tx = pick_tile(n, sizeof(cplx_t<T>), 1);
+  s.lg_tx = ilog2(pick_tile(n, sizeof(cplx_t<T>), 1));
   s.na = na;
   s.s_row = s.d_row = row_stride;
   s.s_a = s.d_a = stride_a;

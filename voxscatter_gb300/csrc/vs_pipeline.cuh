@@ -31,8 +31,8 @@ struct PipeArgs {
   const C* twQ;
   const C* twR;
   FftPlan pP, pQ, pR;
-  int lpb;  // lines per block in the x passes
-  int tx;   // x-tile width of the y and z passes
+  int lg_lpb;  // log2 lines per block in the x passes
+  int lg_tx;   // log2 x-tile width of the z pass
   const int* skip;
 };
 
@@ -46,7 +46,7 @@ struct StridedArgs {
   using C = cplx_t<T>;
   const C* src;
   C* dst;
-  int xext, n_in, n_out, tx, na;
+  int xext, n_in, n_out, lg_tx, na;
   int64_t s_row, s_a, s_b, s_rhs;
   int64_t d_row, d_a, d_b, d_rhs;
   FftPlan plan;

@@ -266,14 +266,24 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
   a.t1 = t; a.t2 = t;
   a.twP = pr.axL.tw<T>();
   a.pP = pr.axL.plan;
-  a.lpb = std::max(1, 2048 / L);
+  {
+    int l = 8;
+    while (l > 1 && 2ull * L * l * sizeof(C) > 48 * 1024) l >>= 1;
+    int lg = 0;
+    while ((1 << lg) < l) ++lg;
+    a.lg_lpb = lg;
+  }
   a.skip = skip;
   StridedArgs<T> s{};
   s.src = t; s.dst = t;
   s.xext = L; s.n_in = M; s.n_out = M;
-  int tx = 32;
-  while (tx > 1 && 2ull * M * tx * sizeof(C) > 48 * 1024) tx >>= 1;
-  s.tx = tx;
+  {
+    int tx = 16;
+    while (tx > 1 && 2ull * M * tx * sizeof(C) > 48 * 1024) tx >>= 1;
+    int lg = 0;
+    while ((1 << lg) < tx) ++lg;
+    s.lg_tx = lg;
+  }
   s.na = 3 * N;
   s.s_row = s.d_row = L;
   s.s_a = s.d_a = (int64_t)L * M;
