@@ -144,3 +144,22 @@ def test_config2_full_size_c64(api):
     assert rel(y64, y_o) < C64_TOL
     y2 = op.apply(np.concatenate([x, 2 * x - 1j * x]), "notransp", "c64").reshape(2, -1)
     assert rel(y2[1], (2 - 1j) * y64) < C64_TOL
+
+
+def test_full_storage_when_parity_is_not_exact(api):
+    """Odd components made non-zero on their zero-offset planes: the library
+    must fall back to full spectrum storage and still match the oracle."""
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, chi = _problem(p)
+    Toep = O.green_toeplitz(p["r"], p["ko"]).copy()
+    rng = np.random.default_rng(9)
+    Toep[0, :, :, 1] += 1e-3 * rng.normal(size=(M, N))
+    Toep[:, :, 0, 4] += 1e-3 * rng.normal(size=(L, M))
+    fN = O.fft_operator(O.circulant_nop_const(Toep))
+    alpha = O.alpha_ldr(p["refInd"], p["ko"], p["d"], p["kvec"], p["Eo"])
+    dV = p["d"] ** 3
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    x = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
+    y_o = O.MVP(x, fN, np.ones((L, M, N)), dV * chi, 1 / alpha, "notransp", idx3)
+    assert rel(op.apply(x, "notransp", "c128"), y_o) < C128_TOL
+    assert rel(op.apply(x, "notransp", "c64"), y_o) < C64_TOL

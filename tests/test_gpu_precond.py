@@ -101,3 +101,19 @@ def test_prec_config1_size(api):
     y_o = O.mvp_circ_2_level(inv_o, x, L, M, N, idx3)
     assert rel(pr.apply(x, "c128"), y_o) < 1e-10
     assert rel(pr.apply(x, "c64"), y_o) < 1e-4
+
+
+def test_prec_full_storage_when_parity_is_not_exact(api):
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, Toep, alpha, dV = _setup(p)
+    Toep = Toep.copy()
+    rng = np.random.default_rng(10)
+    Toep[0, :, :, 2] += 1e-3 * rng.normal(size=(M, N))
+    _, c1_o = O.circ_1_level(Toep, L, M, N, 0, "off")
+    _, blk_o = O.circ_2_level(c1_o, L, M, N)
+    inv_o = O.invert_blocks(blk_o, 1 / alpha, dV)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
+    assert rel(pr.blocks(L, M, N, "c128"), inv_o) < 1e-10
+    x = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
+    assert rel(pr.apply(x, "c128"), O.mvp_circ_2_level(inv_o, x, L, M, N, idx3)) < 1e-10

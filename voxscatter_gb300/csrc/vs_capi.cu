@@ -120,6 +120,14 @@ void axes_init(vs_op* op) {
 
 void spectrum_from_full(vs_op* op, const double2* full) {
   const int64_t PQR = (int64_t)op->P * op->Q * op->R;
+  if (op->gsym) {
+    const int64_t oct = (int64_t)(op->P / 2 + 1) * (op->Q / 2 + 1) * (op->R / 2 + 1);
+    op->G64.alloc(6 * oct * sizeof(double2));
+    op->G32.alloc(6 * oct * sizeof(float2));
+    vs::octant_spectrum(full, op->P, op->Q, op->R, 1.0 / (double)PQR, op->G64.as<double2>(), op->G32.as<float2>(),
+                        op->ctx->stream);
+    return;
+  }
   op->G64.alloc(6 * PQR * sizeof(double2));
   op->G32.alloc(6 * PQR * sizeof(float2));
   vs::finalize_spectrum(full, 6 * PQR, 1.0 / (double)PQR, op->G64.as<double2>(), op->G32.as<float2>(),
@@ -136,11 +144,27 @@ __global__ void k_blocks_in(const double2* __restrict__ in, int64_t total, doubl
   }
 }
 
-__global__ void k_blocks_out(const double2* __restrict__ i64, const float2* __restrict__ i32, int64_t total,
-                             double scale, double2* __restrict__ out) {
+// Expands stored blocks to the full L*M set; with sym, block (i, j) comes from
+// the stored (min(i, L-i), min(j, M-j)) with the parity signs of the x/y
+// component rows and columns.
+__global__ void k_blocks_out(const double2* __restrict__ i64, const float2* __restrict__ i32, int L, int M, int N,
+                             int sym, double scale, double2* __restrict__ out) {
+  const int n = 3 * N;
+  const int64_t nn = (int64_t)n * n, total = (int64_t)L * M * nn;
+  const int Lb = sym ? L / 2 + 1 : L;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const double2 a = i64 ? i64[e] : make_double2(i32[e].x, i32[e].y);
-    out[e] = make_double2(a.x * scale, a.y * scale);
+    const int64_t b = e / nn, r = e - b * nn;
+    const int i = (int)(b % L), j = (int)(b / L);
+    const int q = (int)(r / n), p = (int)(r - (int64_t)q * n);  // column-major (p, q)
+    const bool fx = sym && i > L / 2, fy = sym && j > M / 2;
+    const int is = fx ? L - i : i, js = fy ? M - j : j;
+    const int64_t src = ((int64_t)is + (int64_t)Lb * js) * nn + r;
+    const double2 a = i64 ? i64[src] : make_double2(i32[src].x, i32[src].y);
+    const int cp = p / N, cq = q / N;
+    const bool fp = (cp == 0 && fx) != (cp == 1 && fy);
+    const bool fq = (cq == 0 && fx) != (cq == 1 && fy);
+    const double sg = (fp != fq) ? -scale : scale;
+    out[e] = make_double2(a.x * sg, a.y * sg);
   }
 }
 
@@ -318,6 +342,7 @@ int vs_op_create(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* toe
     op->P = (int)P; op->Q = (int)Q; op->R = (int)R;
     op->V = L * M * N;
     op_common(op, idx3, n3, Mr, Mc, Gram);
+    op->gsym = vs::toeplitz_has_exact_parity(toep, op->L, op->M, op->N);
     cudaStream_t st = ctx->stream;
     op->toep64.alloc(6 * op->V * sizeof(double2));
     VS_CUDA(cudaMemcpyAsync(op->toep64.p, toep, 6 * op->V * sizeof(double2), cudaMemcpyHostToDevice, st));
@@ -505,15 +530,17 @@ int vs_prec_create(vs_op* op, const double* shift, const double* d, int64_t nd, 
       dptr = dv.as<double2>();
     }
     const double scale = 1.0 / (double)LM;
+    pr->sym = op->gsym;  // exact parity of the Toeplitz tensor: quadrant storage suffices
+    const int64_t nblk = pr->sym ? (int64_t)(op->L / 2 + 1) * (op->M / 2 + 1) : LM;
     if (precisions & VS_BUILD_C64) {
-      pr->inv32.alloc(LM * n * n * sizeof(float2));
+      pr->inv32.alloc(nblk * n * n * sizeof(float2));
       vs::assemble_invert<float>(l2.as<double2>(), op->L, op->M, op->N, sh, dptr, ds, true, true, scale,
-                                 pr->inv32.as<float2>(), status.as<int>(), st);
+                                 pr->inv32.as<float2>(), status.as<int>(), st, pr->sym);
     }
     if (precisions & VS_BUILD_C128) {
-      pr->inv64.alloc(LM * n * n * sizeof(double2));
+      pr->inv64.alloc(nblk * n * n * sizeof(double2));
       vs::assemble_invert<double>(l2.as<double2>(), op->L, op->M, op->N, sh, dptr, ds, true, true, scale,
-                                  pr->inv64.as<double2>(), status.as<int>(), st);
+                                  pr->inv64.as<double2>(), status.as<int>(), st, pr->sym);
     }
     int hs = 0;
     VS_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -630,7 +657,8 @@ int vs_prec_get_blocks(vs_prec* prec, int precision, double* out) {
     o.alloc(LM * n * n * sizeof(double2));
     k_blocks_out<<<(int)std::min<int64_t>(vs::ceil_div(LM * n * n, 256), 152 * 32), 256, 0, st>>>(
         precision == VS_C128 ? prec->inv64.as<double2>() : nullptr,
-        precision == VS_C64 ? prec->inv32.as<float2>() : nullptr, LM * n * n, (double)LM, o.as<double2>());
+        precision == VS_C64 ? prec->inv32.as<float2>() : nullptr, prec->L, prec->M, prec->N, prec->sym ? 1 : 0,
+        (double)LM, o.as<double2>());
     VS_LAUNCH_CHECK();
     VS_CUDA(cudaMemcpyAsync(out, o.p, LM * n * n * sizeof(double2), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));

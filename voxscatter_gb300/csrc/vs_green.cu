@@ -199,6 +199,53 @@ __global__ void k_finalize(const double2* __restrict__ in, int64_t n, double sca
   }
 }
 
+// First-octant copy kx <= P/2, ky <= Q/2, kz <= R/2 of the scaled spectrum
+// (the rest follows from the per-axis parity of each component).
+__global__ void k_octant(const double2* __restrict__ in, int P, int Q, int R, double scale, double2* __restrict__ g64,
+                         float2* __restrict__ g32) {
+  const int Ph = P / 2 + 1, Qh = Q / 2 + 1, Rh = R / 2 + 1;
+  const int64_t oct = (int64_t)Ph * Qh * Rh, PQR = (int64_t)P * Q * R;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 6 * oct; e += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(e / oct);
+    const int64_t g = e - c * oct;
+    const int x = (int)(g % Ph);
+    const int y = (int)((g / Ph) % Qh);
+    const int z = (int)(g / ((int64_t)Ph * Qh));
+    const double2 a = in[c * PQR + x + (int64_t)P * (y + (int64_t)Q * z)];
+    const double2 v = make_double2(a.x * scale, a.y * scale);
+    if (g64) g64[e] = v;
+    if (g32) g32[e] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+void octant_spectrum(const double2* fN, int P, int Q, int R, double scale, double2* g64, float2* g32, cudaStream_t st) {
+  const int64_t oct = (int64_t)(P / 2 + 1) * (Q / 2 + 1) * (R / 2 + 1);
+  k_octant<<<(int)std::min<int64_t>(ceil_div(6 * oct, 256), 152 * 32), 256, 0, st>>>(fN, P, Q, R, scale, g64, g32);
+  VS_LAUNCH_CHECK();
+}
+
+// True when every odd tensor component vanishes exactly on its zero-offset
+// plane: then the embedded tensor is exactly even/odd along each axis and its
+// spectrum (and the circulant blocks) inherit that parity.
+bool toeplitz_has_exact_parity(const double* toep, int L, int M, int N) {
+  const int64_t V = (int64_t)L * M * N;
+  // component -> odd along x / y / z (xx, xy, xz, yy, yz, zz)
+  const bool ox[6] = {false, true, true, false, false, false};
+  const bool oy[6] = {false, true, false, false, true, false};
+  const bool oz[6] = {false, false, true, false, true, false};
+  for (int c = 0; c < 6; ++c) {
+    const double* t = toep + 2 * c * V;
+    for (int k = 0; k < N; ++k)
+      for (int j = 0; j < M; ++j)
+        for (int i = 0; i < L; ++i) {
+          if (!((ox[c] && i == 0) || (oy[c] && j == 0) || (oz[c] && k == 0))) continue;
+          const int64_t e = 2 * (i + (int64_t)L * (j + (int64_t)M * k));
+          if (t[e] != 0.0 || t[e + 1] != 0.0) return false;
+        }
+  }
+  return true;
+}
+
 void finalize_spectrum(const double2* fN, int64_t total, double scale, double2* g64, float2* g32, cudaStream_t st) {
   k_finalize<<<(int)std::min<int64_t>(ceil_div(total, 256), 152 * 32), 256, 0, st>>>(fN, total, scale, g64, g32);
   VS_LAUNCH_CHECK();

@@ -75,7 +75,8 @@ struct vs_op {
   vs::DevBuf map3;      // int32[3V]: unknown position of each grid entry, -1 if absent
   vs::DevBuf pos2grid;  // int32[n3]: grid entry of each unknown
   VsDiagDev d1, d1c, d2;  // Gram.*Mr, Gram.*conj(Mr), Mc at the unknowns
-  vs::DevBuf G32, G64;  // spectrum of the embedded tensor / (P*Q*R), 6 x P*Q*R
+  bool gsym = false;    // G holds only the first octant (exact per-axis parity)
+  vs::DevBuf G32, G64;  // spectrum of the embedded tensor / (P*Q*R): 6 x P*Q*R, or 6 x octant
   vs::DevBuf toep64;    // first-octant Toeplitz tensor, L*M*N*6 (double2)
   vs::FftAxis ax[3];
   vs::DevBuf t1, t2;    // pipeline intermediates
@@ -87,9 +88,10 @@ struct vs_op {
 struct vs_prec {
   vs_ctx* ctx = nullptr;
   int L = 0, M = 0, N = 0;
+  bool sym = false;         // blocks stored for i <= L/2, j <= M/2 only (parity of the operator)
   int64_t V = 0, n3 = 0;
   vs::DevBuf map3;          // int32[3V] unknown position of each grid entry (-1: absent)
-  vs::DevBuf inv32, inv64;  // L*M blocks of (3N)^2, column-major, scaled by 1/(L*M)
+  vs::DevBuf inv32, inv64;  // blocks of (3N)^2 (L*M, or (L/2+1)(M/2+1) when sym), column-major, / (L*M)
   vs::FftAxis axL, axM;
   vs::DevBuf t;             // apply scratch (L,M,N,3) per right-hand side
   vs::DevBuf xin, yout;
@@ -121,6 +123,8 @@ void embed_fft_device(int L, int M, int N, const double2* toep, int P, int Q, in
                       FftAxis* ax, cudaStream_t st);
 void toep_from_fN_device(int L, int M, int N, int P, int Q, int R, double2* fN_inplace, double2* toep,
                          FftAxis* ax, cudaStream_t st);
+void octant_spectrum(const double2* fN, int P, int Q, int R, double scale, double2* g64, float2* g32, cudaStream_t st);
+bool toeplitz_has_exact_parity(const double* toep, int L, int M, int N);
 void finalize_spectrum(const double2* fN, int64_t total, double scale, double2* g64, float2* g32,
                        cudaStream_t st);
 
@@ -129,7 +133,8 @@ void circ_levels_device(int L, int M, int N, const double2* toep, double2* lev1,
                         const FftAxis& axM, cudaStream_t st);
 template <typename T>
 void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, const double2* dvec, double2 dscal,
-                     bool invert, bool colmajor, double scale, cplx_t<T>* out, int* status, cudaStream_t st);
+                     bool invert, bool colmajor, double scale, cplx_t<T>* out, int* status, cudaStream_t st,
+                     bool sym = false);
 template <typename T>
 void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
                      cudaStream_t st, int pass);

@@ -163,7 +163,10 @@ __global__ void __launch_bounds__(kThreads) k_strided(StridedArgs<T> a) {
 // ---- pass Z: FFT_z ⊗ tensor multiply ⊗ IFFT_z, in place in T2 -----------
 // Lines (comp c, x) are interleaved: element z of line c*tx + xl at
 // z*(3*tx) + c*tx + xl.
-template <typename T, bool SMALL>
+// SYM: G holds the first octant only; entries outside it are read from the
+// mirrored frequency with the component's parity sign (xy odd in x and y, xz
+// odd in x and z, yz odd in y and z; diagonal components even).
+template <typename T, bool SMALL, bool SYM>
 __global__ void __launch_bounds__(kThreads) k_z(PipeArgs<T> a) {
   using C = cplx_t<T>;
   if (a.skip && *a.skip) return;
@@ -188,13 +191,30 @@ __global__ void __launch_bounds__(kThreads) k_z(PipeArgs<T> a) {
   __syncthreads();
   const FftLayout lay{lg_nl, true};
   C* res = fft_lines<false, C, SMALL>(s0, s1, a.pR, w, 1, w, lay, a.twR);
-  const int64_t PQR = PQ * R;
   if (xin) {
-    const C* G = a.G + x + (int64_t)a.P * ky;
+    int gx = x, gy = ky, Pg = a.P, Qg = a.Q, Rg = R;
+    bool fx = false, fy = false;
+    if (SYM) {
+      Pg = a.P / 2 + 1; Qg = a.Q / 2 + 1; Rg = R / 2 + 1;
+      if (x > a.P / 2) { gx = a.P - x; fx = true; }
+      if (ky > a.Q / 2) { gy = a.Q - ky; fy = true; }
+    }
+    const int64_t PQg = (int64_t)Pg * Qg, PQRg = PQg * Rg;
+    const C* G = a.G + gx + (int64_t)Pg * gy;
     for (int kz = r0; kz < R; kz += NJ) {
-      const int64_t gi = kz * PQ;
-      const C g0 = __ldg(G + gi), g1 = __ldg(G + PQR + gi), g2 = __ldg(G + 2 * PQR + gi);
-      const C g3 = __ldg(G + 3 * PQR + gi), g4 = __ldg(G + 4 * PQR + gi), g5 = __ldg(G + 5 * PQR + gi);
+      int gz = kz;
+      bool fz = false;
+      if (SYM && kz > R / 2) { gz = R - kz; fz = true; }
+      const int64_t gi = gz * PQg;
+      C g0 = __ldg(G + gi), g1 = __ldg(G + PQRg + gi), g2 = __ldg(G + 2 * PQRg + gi);
+      const C g3 = __ldg(G + 3 * PQRg + gi);
+      C g4 = __ldg(G + 4 * PQRg + gi);
+      const C g5 = __ldg(G + 5 * PQRg + gi);
+      if (SYM) {
+        if (fx != fy) { g1.x = -g1.x; g1.y = -g1.y; }
+        if (fx != fz) { g2.x = -g2.x; g2.y = -g2.y; }
+        if (fy != fz) { g4.x = -g4.x; g4.y = -g4.y; }
+      }
       C* p = res + kz * w + xl;
       const C v0 = p[0], v1 = p[tx], v2 = p[2 * tx];
       C o0 = cmul(g0, v0); o0 = cfma(g1, v1, o0); o0 = cfma(g2, v2, o0);
@@ -348,15 +368,19 @@ void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, in
       const int tx = 1 << a.lg_tx;
       dim3 grid(ceil_div(op.P, tx), op.Q, nrhs);
       const size_t smem = 2ull * op.R * 3 * tx * sizeof(C);
-      if (plan_is_small_radix(a.pR)) {
-        auto k = k_z<T, true>;
-        set_smem(k, smem);
-        k<<<grid, kThreads, smem, st>>>(a);
+      const bool small = plan_is_small_radix(a.pR);
+#define VS_Z(SM, SY)                   \
+  {                                    \
+    auto k = k_z<T, SM, SY>;           \
+    set_smem(k, smem);                 \
+    k<<<grid, kThreads, smem, st>>>(a);\
+  }
+      if (op.gsym) {
+        if (small) VS_Z(true, true) else VS_Z(false, true)
       } else {
-        auto k = k_z<T, false>;
-        set_smem(k, smem);
-        k<<<grid, kThreads, smem, st>>>(a);
+        if (small) VS_Z(true, false) else VS_Z(false, false)
       }
+#undef VS_Z
       VS_LAUNCH_CHECK();
       break;
     }

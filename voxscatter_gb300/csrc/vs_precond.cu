@@ -86,7 +86,8 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_assemble_invert(const double2* __restrict__ lev2, int L, int M, int N,
                                                          double2 shift, const double2* __restrict__ dvec,
                                                          double2 dscal, int invert, int colmajor, double scale,
-                                                         cplx_t<T>* __restrict__ out, int* __restrict__ status) {
+                                                         cplx_t<T>* __restrict__ out, int* __restrict__ status,
+                                                         int Lb) {
   using C = cplx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = 3 * N;
@@ -172,7 +173,7 @@ __global__ void __launch_bounds__(256) k_assemble_invert(const double2* __restri
       __syncthreads();
     }
   }
-  C* o = out + ((int64_t)i + (int64_t)L * j) * n * n;
+  C* o = out + ((int64_t)i + (int64_t)Lb * j) * n * n;
   for (int u = threadIdx.x; u < n * n; u += blockDim.x) {
     const int p = u / n, q = u - p * n;
     const C a = A[u];
@@ -188,28 +189,35 @@ size_t assemble_smem(int N, size_t csize) {
 
 template <typename T>
 void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, const double2* dvec, double2 dscal,
-                     bool invert, bool colmajor, double scale, cplx_t<T>* out, int* status, cudaStream_t st) {
+                     bool invert, bool colmajor, double scale, cplx_t<T>* out, int* status, cudaStream_t st,
+                     bool sym) {
   const size_t smem = assemble_smem(N, sizeof(cplx_t<T>));
   if (smem > 227 * 1024)
     throw Error(VS_ERR_UNSUPPORTED, "3N x 3N block of " + std::to_string(3 * N) + " does not fit in shared memory");
   auto k = k_assemble_invert<T>;
   set_kernel_smem((const void*)k, smem);
-  k<<<dim3(L, M), 256, smem, st>>>(lev2, L, M, N, shift, dvec, dscal, invert ? 1 : 0, colmajor ? 1 : 0, scale, out,
-                                   status);
+  const int Lb = sym ? L / 2 + 1 : L, Mb = sym ? M / 2 + 1 : M;
+  k<<<dim3(Lb, Mb), 256, smem, st>>>(lev2, L, M, N, shift, dvec, dscal, invert ? 1 : 0, colmajor ? 1 : 0, scale, out,
+                                     status, Lb);
   VS_LAUNCH_CHECK();
 }
 template void assemble_invert<float>(const double2*, int, int, int, double2, const double2*, double2, bool, bool,
-                                     double, float2*, int*, cudaStream_t);
+                                     double, float2*, int*, cudaStream_t, bool);
 template void assemble_invert<double>(const double2*, int, int, int, double2, const double2*, double2, bool, bool,
-                                      double, double2*, int*, cudaStream_t);
+                                      double, double2*, int*, cudaStream_t, bool);
 
 // ---- apply: block GEMV on the (x,y)-frequency planes --------------------
 // Inverse blocks are stored column-major (element (r, q) at q*n + r), so the
 // threads that compute consecutive output rows read consecutive addresses of
 // each column; each thread forms one full row sum, no cross-lane reduction.
+// With sym, only blocks i <= L/2, j <= M/2 are stored; block (L-i, j) equals
+// Dx B(i,j) Dx and (i, M-j) equals Dy B(i,j) Dy, Dx/Dy negating the x/y
+// component entries, so the input and output entries of those components are
+// negated around the product with the stored block.
 template <typename T>
 __global__ void __launch_bounds__(256) k_block_gemv(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ inv, int L,
-                                                    int M, int N, int ti, int64_t rhs_stride, const int* skip) {
+                                                    int M, int N, int ti, int64_t rhs_stride, const int* skip,
+                                                    int sym) {
   using C = cplx_t<T>;
   if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -219,18 +227,25 @@ __global__ void __launch_bounds__(256) k_block_gemv(cplx_t<T>* __restrict__ t, c
   const int i0 = blockIdx.x * ti, j = blockIdx.y;
   C* tt = t + (int64_t)blockIdx.z * rhs_stride;
   const int64_t LM = (int64_t)L * M;
+  const int Lb = sym ? L / 2 + 1 : L;
+  const bool fy = sym && j > M / 2;
+  const int js = fy ? M - j : j;
   for (int u = threadIdx.x; u < ti * n; u += blockDim.x) {
     const int s = u / ti, il = u - s * ti;
     const int i = i0 + il;
     // s = comp*N + z  ->  grid entry (i, j, z, comp)
-    v[il * n + s] = (i < L) ? tt[i + (int64_t)L * j + LM * s] : czero<C>();
+    C val = (i < L) ? tt[i + (int64_t)L * j + LM * s] : czero<C>();
+    const int comp = s / N;
+    if ((comp == 0 && sym && i > L / 2) != (comp == 1 && fy)) { val.x = -val.x; val.y = -val.y; }
+    v[il * n + s] = val;
   }
   __syncthreads();
   for (int rr = threadIdx.x; rr < ti * n; rr += blockDim.x) {
     const int il = rr / n, r = rr - il * n;
     const int i = i0 + il;
     if (i >= L) continue;
-    const C* A = inv + ((int64_t)i + (int64_t)L * j) * n * n + r;
+    const int is = (sym && i > L / 2) ? L - i : i;
+    const C* A = inv + ((int64_t)is + (int64_t)Lb * js) * n * n + r;
     const C* x = v + il * n;
     C acc0 = czero<C>(), acc1 = czero<C>();
     int q = 0;
@@ -240,7 +255,10 @@ __global__ void __launch_bounds__(256) k_block_gemv(cplx_t<T>* __restrict__ t, c
       acc1 = cfma(__ldg(A + (int64_t)(q + 1) * n), x[q + 1], acc1);
     }
     if (q < n) acc0 = cfma(__ldg(A + (int64_t)q * n), x[q], acc0);
-    o[il * n + r] = cadd(acc0, acc1);
+    C res = cadd(acc0, acc1);
+    const int comp = r / N;
+    if ((comp == 0 && sym && i > L / 2) != (comp == 1 && fy)) { res.x = -res.x; res.y = -res.y; }
+    o[il * n + r] = res;
   }
   __syncthreads();
   for (int u = threadIdx.x; u < ti * n; u += blockDim.x) {
@@ -301,7 +319,8 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
       const size_t smem = 2ull * ti * n * sizeof(C);
       auto k = k_block_gemv<T>;
       set_kernel_smem((const void*)k, smem);
-      k<<<dim3(ceil_div(L, ti), M, nrhs), 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
+      k<<<dim3(ceil_div(L, ti), M, nrhs), 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip,
+                                                           pr.sym ? 1 : 0);
       VS_LAUNCH_CHECK();
       break;
     }
