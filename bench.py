@@ -122,24 +122,26 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def _pass_bytes(p, PQR, n3, e=8):
+def _pass_bytes(p, PQR, n3, e=8, sym=True):
     """Algorithmic DRAM bytes of each launch of the c64 pipelines (one rhs)."""
     L, M, N = p["L"], p["M"], p["N"]
     P, Q, R = PQR
     V = L * M * N
     i4 = 4
+    G = 6 * (P // 2 + 1) * (Q // 2 + 1) * (R // 2 + 1) * e if sym else 6 * P * Q * R * e
     mv = [n3 * e + 3 * V * i4 + 3 * P * M * N * e,
           3 * P * M * N * e + 3 * P * Q * N * e,
-          2 * 3 * P * Q * N * e + 6 * P * Q * R * e,
+          2 * 3 * P * Q * N * e + G,
           3 * P * Q * N * e + 3 * P * M * N * e,
           3 * P * M * N * e + 3 * V * i4 + 2 * n3 * e]
     n = 3 * N
+    nblk = (L // 2 + 1) * (M // 2 + 1) if sym else L * M
     pc = [n3 * e + 3 * V * i4 + 3 * V * e,
           2 * 3 * V * e,
-          L * M * n * n * e + 2 * 3 * V * e,
+          nblk * n * n * e + 2 * 3 * V * e,
           2 * 3 * V * e,
           3 * V * e + 3 * V * i4 + n3 * e]
-    pinned = e * (9 * V + 1.5 * V + 12 * P * M * N + 12 * P * Q * N) + 6 * P * Q * R * e
+    pinned = e * (9 * V + 1.5 * V + 12 * P * M * N + 12 * P * Q * N) + G
     return mv, pc, pinned
 
 

@@ -48,6 +48,9 @@ __host__ __device__ __forceinline__ double2 cfma(double2 b, double2 c, double2 a
   return make_double2(fma(b.x, c.x, fma(-b.y, c.y, a.x)), fma(b.x, c.y, fma(b.y, c.x, a.y)));
 }
 template <typename C> __host__ __device__ __forceinline__ C czero() { C c; c.x = 0; c.y = 0; return c; }
+template <typename C, typename R> __host__ __device__ __forceinline__ C make_c(R re, R im) {
+  C c; c.x = re; c.y = im; return c;
+}
 template <typename D, typename S> __host__ __device__ __forceinline__ D ccast(S s) {
   D d; d.x = (decltype(d.x))s.x; d.y = (decltype(d.y))s.y; return d;
 }

@@ -268,6 +268,82 @@ __global__ void __launch_bounds__(256) k_block_gemv(cplx_t<T>* __restrict__ t, c
   }
 }
 
+// Quadrant-symmetric apply: CTA (blockIdx.x, blockIdx.y) owns stored blocks
+// is = blockIdx.x*ti + il (il < ti), js = blockIdx.y, and applies each one to
+// the up to four frequencies (is, js), (L-is, js), (is, M-js), (L-is, M-js)
+// that share it, so every stored block is read from memory once per apply.
+// Variant v has flips fx = v&1, fy = v>>1 (negate the x / y component entries
+// of the input and of the output).
+template <typename T>
+__global__ void __launch_bounds__(256) k_block_gemv_sym(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ inv,
+                                                        int L, int M, int N, int ti, int64_t rhs_stride,
+                                                        const int* skip) {
+  using C = cplx_t<T>;
+  if (skip && *skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = 3 * N;
+  const int Lb = L / 2 + 1;
+  C* v = reinterpret_cast<C*>(smem_raw);  // [il][variant][n]
+  C* o = v + ti * 4 * n;
+  const int is0 = blockIdx.x * ti, js = blockIdx.y;
+  C* tt = t + (int64_t)blockIdx.z * rhs_stride;
+  const int64_t LM = (int64_t)L * M;
+  const bool jmir = (js != 0) && (2 * js != M);
+  for (int u = threadIdx.x; u < ti * 4 * n; u += blockDim.x) {
+    const int s = u % n;
+    const int rest = u / n;
+    const int var = rest & 3, il = rest >> 2;
+    const int is = is0 + il;
+    const bool imir = (is != 0) && (2 * is != L);
+    const bool fx = var & 1, fy = var >> 1;
+    C val = czero<C>();
+    if (is < Lb && (!fx || imir) && (!fy || jmir)) {
+      const int i = fx ? L - is : is, j = fy ? M - js : js;
+      val = tt[i + (int64_t)L * j + LM * s];
+      const int comp = s / N;
+      if ((comp == 0 && fx) != (comp == 1 && fy)) { val.x = -val.x; val.y = -val.y; }
+    }
+    v[u] = val;
+  }
+  __syncthreads();
+  for (int rr = threadIdx.x; rr < ti * n; rr += blockDim.x) {
+    const int il = rr / n, r = rr - il * n;
+    const int is = is0 + il;
+    if (is >= Lb) continue;
+    const C* A = inv + ((int64_t)is + (int64_t)Lb * js) * n * n + r;
+    const C* x = v + il * 4 * n;
+    C a0 = czero<C>(), a1 = czero<C>(), a2 = czero<C>(), a3 = czero<C>();
+#pragma unroll 4
+    for (int q = 0; q < n; ++q) {
+      const C m = __ldg(A + (int64_t)q * n);
+      a0 = cfma(m, x[q], a0);
+      a1 = cfma(m, x[n + q], a1);
+      a2 = cfma(m, x[2 * n + q], a2);
+      a3 = cfma(m, x[3 * n + q], a3);
+    }
+    const int comp = r / N;
+    C* out = o + il * 4 * n + r;
+    // variant flips of the output rows
+    out[0] = a0;
+    out[n] = (comp == 0) ? make_c<C>(-a1.x, -a1.y) : a1;
+    out[2 * n] = (comp == 1) ? make_c<C>(-a2.x, -a2.y) : a2;
+    out[3 * n] = (comp == 0 || comp == 1) ? make_c<C>(-a3.x, -a3.y) : a3;
+  }
+  __syncthreads();
+  for (int u = threadIdx.x; u < ti * 4 * n; u += blockDim.x) {
+    const int s = u % n;
+    const int rest = u / n;
+    const int var = rest & 3, il = rest >> 2;
+    const int is = is0 + il;
+    const bool imir = (is != 0) && (2 * is != L);
+    const bool fx = var & 1, fy = var >> 1;
+    if (is < Lb && (!fx || imir) && (!fy || jmir)) {
+      const int i = fx ? L - is : is, j = fy ? M - js : js;
+      tt[i + (int64_t)L * j + LM * s] = o[u];
+    }
+  }
+}
+
 template <typename T>
 void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
                      cudaStream_t st, int pass) {
@@ -314,13 +390,23 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
     case 0: launch_x_pass<T>(a, false, MODE_PLAIN, nrhs, st); break;
     case 1: launch_strided_pass<T, false>(s, 3 * N, nrhs, st); break;
     case 2: {
-      const int ti = std::min(L, 8);
       const int n = 3 * N;
+      if (pr.sym) {
+        const int Lb = L / 2 + 1, Mb = M / 2 + 1;
+        int ti = std::min(Lb, 4);
+        while (ti > 1 && 2ull * ti * 4 * n * sizeof(C) > 64 * 1024) --ti;
+        const size_t smem = 2ull * ti * 4 * n * sizeof(C);
+        auto k = k_block_gemv_sym<T>;
+        set_kernel_smem((const void*)k, smem);
+        k<<<dim3(ceil_div(Lb, ti), Mb, nrhs), 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
+        VS_LAUNCH_CHECK();
+        break;
+      }
+      const int ti = std::min(L, 8);
       const size_t smem = 2ull * ti * n * sizeof(C);
       auto k = k_block_gemv<T>;
       set_kernel_smem((const void*)k, smem);
-      k<<<dim3(ceil_div(L, ti), M, nrhs), 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip,
-                                                           pr.sym ? 1 : 0);
+      k<<<dim3(ceil_div(L, ti), M, nrhs), 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip, 0);
       VS_LAUNCH_CHECK();
       break;
     }
