@@ -12,18 +12,24 @@ static VsDim blockDim = {1, 1, 1};
 #define __ldg(p) (*(p))
 #define VS_FFT_HOST_EMULATION 1
 #include "../../voxscatter_gb300/csrc/vs_fft.cuh"
+
+// The emulated CTA's dynamic shared memory (referenced by vs::shmem()).
+namespace vs {
+alignas(16) unsigned char smem_raw[1 << 22];
+}
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
 
+// Runs the stages of one CTA: shared buffers at offsets a and b, twiddles at tw.
 template <bool INV, typename C, bool SMALL>
-static C* emulate(C* a, C* b, const vs::FftPlan& pl, int nlines, int ls, int es, vs::FftLayout lay, const C* tw) {
+static int emulate(int a, int b, const vs::FftPlan& pl, int nlines, int ls, int es, vs::FftLayout lay, int tw) {
   int Ns = 1;
   for (int s = 0; s < pl.nstages; ++s) {
     for (int t = 0; t < vs::kFftThreads; ++t)
       vs::fft_stage_any<INV, C, SMALL>(a, b, pl.n, pl.radix[s], Ns, nlines, ls, es, lay, tw, t);
-    C* tmp = a; a = b; b = tmp;
+    const int tmp = a; a = b; b = tmp;
     Ns *= pl.radix[s];
   }
   return a;
@@ -34,9 +40,11 @@ static double check(int n, int nlines, bool lines_fast, int lg_nl = 0) {
   using C = vs::cplx_t<T>;
   vs::FftPlan pl = vs::make_fft_plan(n);
   std::vector<double> tw = vs::twiddle_table(n);
-  std::vector<C> twc(n);
-  for (int k = 0; k < n; ++k) { twc[k].x = (T)tw[2 * k]; twc[k].y = (T)tw[2 * k + 1]; }
-  std::vector<C> a((size_t)n * nlines), b((size_t)n * nlines);
+  C* sm = reinterpret_cast<C*>(vs::smem_raw);
+  const int total = n * nlines;
+  const int off_b = total, off_tw = 2 * total;
+  for (int k = 0; k < n; ++k) { sm[off_tw + k].x = (T)tw[2 * k]; sm[off_tw + k].y = (T)tw[2 * k + 1]; }
+  C* a = sm;
   std::vector<long double> in_re((size_t)n * nlines), in_im((size_t)n * nlines);
   srand(n * 7 + nlines);
   const int ls = lines_fast ? 1 : n, es = lines_fast ? nlines : 1;
@@ -47,8 +55,9 @@ static double check(int n, int nlines, bool lines_fast, int lg_nl = 0) {
       in_re[l * n + p] = (T)re; in_im[l * n + p] = (T)im;
     }
   const vs::FftLayout lay{lg_nl, lines_fast};
-  C* res = vs::plan_is_small_radix(pl) ? emulate<INV, C, true>(a.data(), b.data(), pl, nlines, ls, es, lay, twc.data())
-                                       : emulate<INV, C, false>(a.data(), b.data(), pl, nlines, ls, es, lay, twc.data());
+  const int roff = vs::plan_is_small_radix(pl) ? emulate<INV, C, true>(0, off_b, pl, nlines, ls, es, lay, off_tw)
+                                               : emulate<INV, C, false>(0, off_b, pl, nlines, ls, es, lay, off_tw);
+  const C* res = sm + roff;
   double err = 0, ref = 0;
   const long double sg = INV ? 1.0L : -1.0L;
   for (int l = 0; l < nlines; ++l)
@@ -68,7 +77,7 @@ static double check(int n, int nlines, bool lines_fast, int lg_nl = 0) {
 }
 
 int main() {
-  const int sizes[] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 11, 12, 13, 16, 17, 23, 26, 27, 32, 49, 52, 54, 56, 64,
+  const int sizes[] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 11, 12, 13, 16, 17, 18, 23, 26, 27, 32, 36, 49, 52, 54, 56, 64, 72, 81,
                        91, 105, 121, 126, 128, 169, 182, 189, 192, 210, 127, 254, 256, 384, 512, 625, 1024};
   int bad = 0;
   for (int n : sizes) {

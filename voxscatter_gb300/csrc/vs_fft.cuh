@@ -32,7 +32,7 @@ inline FftPlan make_fft_plan(int n) {
   FftPlan p;
   p.n = n;
   int m = n;
-  const int pref[] = {8, 4, 2, 3, 5, 7, 11, 13};
+  const int pref[] = {9, 8, 6, 5, 4, 3, 2, 7, 11, 13};
   for (int r : pref) {
     while (m % r == 0) {
       VS_REQUIRE(p.nstages < FFT_MAX_STAGES, "FFT length has too many factors");
@@ -93,16 +93,28 @@ inline int smooth_size(int n) {
 }
 
 inline bool plan_is_small_radix(const FftPlan& p) {
-  for (int s = 0; s < p.nstages; ++s)
-    if (!(p.radix[s] == 2 || p.radix[s] == 3 || p.radix[s] == 4 || p.radix[s] == 5 || p.radix[s] == 8)) return false;
+  for (int s = 0; s < p.nstages; ++s) {
+    const int r = p.radix[s];
+    if (!(r == 2 || r == 3 || r == 4 || r == 5 || r == 6 || r == 8 || r == 9)) return false;
+  }
   return true;
 }
 
 #if defined(__CUDACC__) || defined(VS_FFT_HOST_EMULATION)
 
+// Dynamic shared memory of the calling kernel, typed.  All FFT buffers and
+// the twiddle table are addressed as 32-bit offsets into it, so every access
+// is a shared-memory access.
+template <typename C>
+__device__ __forceinline__ C* shmem() {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  return reinterpret_cast<C*>(smem_raw);
+}
+
+// Twiddle w_n^idx (conjugated for the inverse) from the table in shared memory.
 template <bool INV, typename C>
-__device__ __forceinline__ C twid(const C* __restrict__ tw, int idx) {
-  C w = __ldg(tw + idx);
+__device__ __forceinline__ C twid(const C* tw, int idx) {
+  C w = tw[idx];
   if (INV) w.y = -w.y;
   return w;
 }
@@ -216,6 +228,57 @@ struct Butterfly<5, INV, C> {
   }
 };
 
+// 6 = 3 x 2: three-point DFTs over n = 2*n1 + n2, twiddles w6^(n2*k1), then
+// two-point DFTs; output k = k1 + 3*k2.
+template <bool INV, typename C>
+struct Butterfly<6, INV, C> {
+  __device__ __forceinline__ static void run(C* v, const C* tw, int n) {
+    using T = decltype(v[0].x);
+    C a[3] = {v[0], v[2], v[4]}, b[3] = {v[1], v[3], v[5]};
+    Butterfly<3, INV, C>::run(a, tw, n);
+    Butterfly<3, INV, C>::run(b, tw, n);
+    const T h = (T)0.5, s3 = INV ? (T)0.86602540378443864676 : (T)-0.86602540378443864676;
+    // b1 *= w6 = (1/2, s3) ; b2 *= w6^2 = (-1/2, s3)
+    C t1, t2;
+    t1.x = h * b[1].x - s3 * b[1].y; t1.y = h * b[1].y + s3 * b[1].x;
+    t2.x = -h * b[2].x - s3 * b[2].y; t2.y = -h * b[2].y + s3 * b[2].x;
+    v[0] = cadd(a[0], b[0]); v[3] = csub(a[0], b[0]);
+    v[1] = cadd(a[1], t1); v[4] = csub(a[1], t1);
+    v[2] = cadd(a[2], t2); v[5] = csub(a[2], t2);
+  }
+};
+
+// 9 = 3 x 3: three-point DFTs over n = 3*n1 + n2, twiddles w9^(n2*k1), then
+// three-point DFTs over n2; output k = k1 + 3*k2.
+template <bool INV, typename C>
+struct Butterfly<9, INV, C> {
+  __device__ __forceinline__ static void run(C* v, const C* tw, int n) {
+    using T = decltype(v[0].x);
+    C y[3][3];
+#pragma unroll
+    for (int n2 = 0; n2 < 3; ++n2) {
+      y[n2][0] = v[n2]; y[n2][1] = v[3 + n2]; y[n2][2] = v[6 + n2];
+      Butterfly<3, INV, C>::run(y[n2], tw, n);
+    }
+    const T sg = INV ? (T)1 : (T)-1;
+    // w9^1, w9^2, w9^4
+    const T c1 = (T)0.76604444311897803520, s1 = sg * (T)0.64278760968653932632;
+    const T c2 = (T)0.17364817766693034885, s2 = sg * (T)0.98480775301220805936;
+    const T c4 = (T)-0.93969262078590838405, s4 = sg * (T)0.34202014332566873304;
+    auto rot = [](C a, T c, T s) { C r; r.x = a.x * c - a.y * s; r.y = a.x * s + a.y * c; return r; };
+    y[1][1] = rot(y[1][1], c1, s1);
+    y[1][2] = rot(y[1][2], c2, s2);
+    y[2][1] = rot(y[2][1], c2, s2);
+    y[2][2] = rot(y[2][2], c4, s4);
+#pragma unroll
+    for (int k1 = 0; k1 < 3; ++k1) {
+      C z[3] = {y[0][k1], y[1][k1], y[2][k1]};
+      Butterfly<3, INV, C>::run(z, tw, n);
+      v[k1] = z[0]; v[k1 + 3] = z[1]; v[k1 + 6] = z[2];
+    }
+  }
+};
+
 // Compile-time-size DFT for the remaining small primes, roots read from the
 // length-n twiddle table: w_R^k = tw[k*n/R].
 template <int R, bool INV, typename C>
@@ -250,13 +313,17 @@ struct FftLayout {
 };
 
 // One radix-R Stockham stage over all lines for thread `t`.
+// Buffers are offsets (in elements) into the kernel's shared memory: src, dst
+// and the twiddle table tw (n entries of exp(-2 pi i k/n)).
 // Butterfly j of a line reads R points at stride m = n/R, applies the twiddles
 // w_n^(r*k*n/(Ns*R)) with k = j mod Ns, and writes the R outputs at
 // (j - k)*R + k + q*Ns.  j advances by NJ per iteration; (j div Ns, j mod Ns)
 // are advanced incrementally, so there is one runtime division per stage.
 template <int R, bool INV, typename C>
-__device__ __forceinline__ void fft_stage(const C* __restrict__ src, C* __restrict__ dst, int n, int Ns, int nlines,
-                                          int ls, int es, FftLayout lay, const C* __restrict__ tw, int t) {
+__device__ __forceinline__ void fft_stage(int src, int dst, int n, int Ns, int nlines, int ls, int es, FftLayout lay,
+                                          int tw, int t) {
+  C* sm = shmem<C>();
+  const C* twp = sm + tw;
   const int lg_nl = lay.lg_nl;
   const int NL = 1 << lg_nl;
   const int lg_nj = 8 - lg_nl;  // kFftThreads = 256
@@ -270,23 +337,23 @@ __device__ __forceinline__ void fft_stage(const C* __restrict__ src, C* __restri
   const int dq = NJ / Ns, dk = NJ - dq * Ns;
   const int me = m * es, nse = Ns * es, rnse = R * nse;
   for (int line = lslot; line < nlines; line += NL) {
-    const C* s = src + line * ls;
-    C* d = dst + line * ls;
+    const int s = src + line * ls;
+    const int d = dst + line * ls;
     int q = q0, k = k0;
     for (int j = jt; j < m; j += NJ) {
       C v[R];
-      const C* sj = s + j * es;
+      const int sj = s + j * es;
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[r] = sj[r * me];
+      for (int r = 0; r < R; ++r) v[r] = sm[sj + r * me];
       if (Ns > 1) {
         const int ks = k * step;
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[r] = cmul(v[r], twid<INV>(tw, r * ks));
+        for (int r = 1; r < R; ++r) v[r] = cmul(v[r], twid<INV>(twp, r * ks));
       }
-      Butterfly<R, INV, C>::run(v, tw, n);
-      C* dq_ = d + q * rnse + k * es;
+      Butterfly<R, INV, C>::run(v, twp, n);
+      const int dd = d + q * rnse + k * es;
 #pragma unroll
-      for (int qq = 0; qq < R; ++qq) dq_[qq * nse] = v[qq];
+      for (int qq = 0; qq < R; ++qq) sm[dd + qq * nse] = v[qq];
       k += dk;
       q += dq;
       if (k >= Ns) { k -= Ns; ++q; }
@@ -295,9 +362,10 @@ __device__ __forceinline__ void fft_stage(const C* __restrict__ src, C* __restri
 }
 
 template <bool INV, typename C>
-__device__ __noinline__ void fft_stage_generic(const C* __restrict__ src, C* __restrict__ dst, int n, int R, int Ns,
-                                               int nlines, int ls, int es, FftLayout lay, const C* __restrict__ tw,
-                                               int t) {
+__device__ __noinline__ void fft_stage_generic(int src, int dst, int n, int R, int Ns, int nlines, int ls, int es,
+                                               FftLayout lay, int tw, int t) {
+  C* sm = shmem<C>();
+  const C* twp = sm + tw;
   const int lg_nl = lay.lg_nl;
   const int NL = 1 << lg_nl;
   const int lg_nj = 8 - lg_nl;
@@ -310,13 +378,13 @@ __device__ __noinline__ void fft_stage_generic(const C* __restrict__ src, C* __r
   const int st = n / R;
   C v[FFT_MAX_GENERIC_RADIX];
   for (int line = lslot; line < nlines; line += NL) {
-    const C* s = src + line * ls;
-    C* d = dst + line * ls;
+    const int s = src + line * ls;
+    const int d = dst + line * ls;
     for (int j = jt; j < m; j += NJ) {
       const int k = j % Ns;
       for (int r = 0; r < R; ++r) {
-        const C a = s[(j + r * m) * es];
-        v[r] = (r > 0 && Ns > 1) ? cmul(a, twid<INV>(tw, r * k * step)) : a;
+        const C a = sm[s + (j + r * m) * es];
+        v[r] = (r > 0 && Ns > 1) ? cmul(a, twid<INV>(twp, r * k * step)) : a;
       }
       const int base = (j - k) * R + k;
       for (int q = 0; q < R; ++q) {
@@ -325,54 +393,63 @@ __device__ __noinline__ void fft_stage_generic(const C* __restrict__ src, C* __r
         for (int r = 1; r < R; ++r) {
           idx += q;
           if (idx >= R) idx -= R;
-          acc = cfma(v[r], twid<INV>(tw, idx * st), acc);
+          acc = cfma(v[r], twid<INV>(twp, idx * st), acc);
         }
-        d[(base + q * Ns) * es] = acc;
+        sm[d + (base + q * Ns) * es] = acc;
       }
     }
   }
 }
 
-// One stage for thread t; SMALL compiles only radices 2,3,4,5,8.
+// One stage for thread t; SMALL compiles only radices 2,3,4,5,6,8,9.
 template <bool INV, typename C, bool SMALL>
-__device__ __forceinline__ void fft_stage_any(const C* src, C* dst, int n, int R, int Ns, int nlines, int ls, int es,
-                                              FftLayout lay, const C* tw, int t) {
+__device__ __forceinline__ void fft_stage_any(int src, int dst, int n, int R, int Ns, int nlines, int ls, int es,
+                                              FftLayout lay, int tw, int t) {
   switch (R) {
-    case 2: fft_stage<2, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
-    case 3: fft_stage<3, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
-    case 4: fft_stage<4, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
-    case 5: fft_stage<5, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
-    case 8: fft_stage<8, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+    case 2: fft_stage<2, INV, C>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+    case 3: fft_stage<3, INV, C>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+    case 4: fft_stage<4, INV, C>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+    case 5: fft_stage<5, INV, C>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+    case 6: fft_stage<6, INV, C>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+    case 8: fft_stage<8, INV, C>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+    case 9: fft_stage<9, INV, C>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
     default:
       if (!SMALL) {
         switch (R) {
-          case 7: fft_stage<7, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
-          case 11: fft_stage<11, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
-          case 13: fft_stage<13, INV>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
-          default: fft_stage_generic<INV>(src, dst, n, R, Ns, nlines, ls, es, lay, tw, t); break;
+          case 7: fft_stage<7, INV, C>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+          case 11: fft_stage<11, INV, C>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+          case 13: fft_stage<13, INV, C>(src, dst, n, Ns, nlines, ls, es, lay, tw, t); break;
+          default: fft_stage_generic<INV, C>(src, dst, n, R, Ns, nlines, ls, es, lay, tw, t); break;
         }
       }
       break;
   }
 }
 
-// Transforms `nlines` lines held in `a` (scratch `b` of the same shape).
-// Element p of line b is at buf[b*ls + p*es].  The caller syncs before the
-// call; the function ends with a __syncthreads() and returns the buffer that
-// holds the result.
+// Transforms `nlines` lines held at shared offset a (scratch at b, same
+// shape; twiddle table at tw).  Element p of line l is at a + l*ls + p*es.
+// The caller syncs before the call; the function ends with a __syncthreads()
+// and returns the offset that holds the result.
 template <bool INV, typename C, bool SMALL = false>
-__device__ C* fft_lines(C* a, C* b, const FftPlan& pl, int nlines, int ls, int es, FftLayout lay,
-                        const C* __restrict__ tw) {
+__device__ int fft_lines(int a, int b, const FftPlan& pl, int nlines, int ls, int es, FftLayout lay, int tw) {
   const int n = pl.n;
   int Ns = 1;
   for (int s = 0; s < pl.nstages; ++s) {
     const int R = pl.radix[s];
     fft_stage_any<INV, C, SMALL>(a, b, n, R, Ns, nlines, ls, es, lay, tw, (int)threadIdx.x);
     __syncthreads();
-    C* tmp = a; a = b; b = tmp;
+    const int tmp = a; a = b; b = tmp;
     Ns *= R;
   }
   return a;
+}
+
+// Copy the length-n twiddle table from global memory to shared offset tw
+// (callers sync afterwards, together with their data loads).
+template <typename C>
+__device__ __forceinline__ void load_twiddles(const C* __restrict__ g, int n, int tw) {
+  C* sm = shmem<C>();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sm[tw + i] = __ldg(g + i);
 }
 
 #endif  // __CUDACC__ || VS_FFT_HOST_EMULATION

@@ -39,17 +39,20 @@ __host__ __device__ __forceinline__ int ilog2(int v) {
   return l;
 }
 
+// Shared-memory layout of every pass: buffer 0 at offset 0, buffer 1 right
+// after it, then the n-entry twiddle table of the transformed axis.
+
 // ---- pass XF: gather + forward FFT along x ------------------------------
 // One line (j, k, comp) per line slot; lines contiguous in shared memory.
 template <typename T, int MODE, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_xf(PipeArgs<T> a) {
   using C = cplx_t<T>;
   if (a.skip && *a.skip) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* sm = shmem<C>();
   const int lg_nl = a.lg_lpb, lg_nj = 8 - lg_nl, NJ = 1 << lg_nj;
   const int nlpb = 1 << lg_nl;
-  C* s0 = reinterpret_cast<C*>(smem_raw);
-  C* s1 = s0 + nlpb * a.P;
+  const int b1 = nlpb * a.P, tw = 2 * nlpb * a.P;
+  load_twiddles(a.twP, a.P, tw);
   const int rhs = blockIdx.y;
   const C* x = a.x + (int64_t)rhs * a.n3;
   C* t1 = a.t1 + (int64_t)rhs * a.P * a.M * a.N * 3;
@@ -61,7 +64,7 @@ __global__ void __launch_bounds__(kThreads) k_xf(PipeArgs<T> a) {
   const int c = live ? line / MN : 0;
   const int jk = line - c * MN;
   const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
-  C* row = s0 + l * a.P;
+  const int row = l * a.P;
   for (int i = jt; i < a.P; i += NJ) {
     C v = czero<C>();
     if (live && i < a.L) {
@@ -72,15 +75,14 @@ __global__ void __launch_bounds__(kThreads) k_xf(PipeArgs<T> a) {
         if (MODE == VS_CONJTRANSP) v = cmul(a.d2.at(pos), cconj(v));
       }
     }
-    row[i] = v;
+    sm[row + i] = v;
   }
   __syncthreads();
   const FftLayout lay{lg_nl, false};
-  C* res = fft_lines<false, C, SMALL>(s0, s1, a.pP, nlpb, a.P, 1, lay, a.twP);
+  const int res = fft_lines<false, C, SMALL>(0, b1, a.pP, nlpb, a.P, 1, lay, tw);
   if (live) {
     C* out = t1 + (int64_t)line * a.P;
-    const C* r = res + l * a.P;
-    for (int i = jt; i < a.P; i += NJ) out[i] = r[i];
+    for (int i = jt; i < a.P; i += NJ) out[i] = sm[res + row + i];
   }
 }
 
@@ -89,11 +91,11 @@ template <typename T, int MODE, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_xi(PipeArgs<T> a) {
   using C = cplx_t<T>;
   if (a.skip && *a.skip) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* sm = shmem<C>();
   const int lg_nl = a.lg_lpb, lg_nj = 8 - lg_nl, NJ = 1 << lg_nj;
   const int nlpb = 1 << lg_nl;
-  C* s0 = reinterpret_cast<C*>(smem_raw);
-  C* s1 = s0 + nlpb * a.P;
+  const int b1 = nlpb * a.P, tw = 2 * nlpb * a.P;
+  load_twiddles(a.twP, a.P, tw);
   const int rhs = blockIdx.y;
   const C* x = a.x + (int64_t)rhs * a.n3;
   C* y = a.y + (int64_t)rhs * a.n3;
@@ -103,23 +105,22 @@ __global__ void __launch_bounds__(kThreads) k_xi(PipeArgs<T> a) {
   const int l = threadIdx.x >> lg_nj, jt = threadIdx.x & (NJ - 1);
   const int line = blockIdx.x * nlpb + l;
   const bool live = line < nlines;
+  const int row = l * a.P;
   {
-    C* row = s0 + l * a.P;
     const C* in = t1 + (int64_t)line * a.P;
-    for (int i = jt; i < a.P; i += NJ) row[i] = live ? in[i] : czero<C>();
+    for (int i = jt; i < a.P; i += NJ) sm[row + i] = live ? in[i] : czero<C>();
   }
   __syncthreads();
   const FftLayout lay{lg_nl, false};
-  C* res = fft_lines<true, C, SMALL>(s0, s1, a.pP, nlpb, a.P, 1, lay, a.twP);
+  const int res = fft_lines<true, C, SMALL>(0, b1, a.pP, nlpb, a.P, 1, lay, tw);
   if (!live) return;
   const int c = line / MN;
   const int jk = line - c * MN;
   const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
-  const C* r = res + l * a.P;
   for (int i = jt; i < a.L; i += NJ) {
     const int pos = __ldg(map + i);
     if (pos < 0) continue;
-    const C conv = r[i];
+    const C conv = sm[res + row + i];
     C out;
     if (MODE == MODE_PLAIN) {
       out = conv;
@@ -138,11 +139,11 @@ template <typename T, bool INV, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_strided(StridedArgs<T> a) {
   using C = cplx_t<T>;
   if (a.skip && *a.skip) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* sm = shmem<C>();
   const int n = a.plan.n;
   const int lg_nl = a.lg_tx, tx = 1 << lg_nl, NJ = kThreads >> lg_nl;
-  C* s0 = reinterpret_cast<C*>(smem_raw);
-  C* s1 = s0 + n * tx;
+  const int b1 = n * tx, tw = 2 * n * tx;
+  load_twiddles(a.tw, n, tw);
   const int x0 = blockIdx.x * tx;
   const int pa = blockIdx.y % a.na;
   const int pb = blockIdx.y / a.na;
@@ -152,12 +153,12 @@ __global__ void __launch_bounds__(kThreads) k_strided(StridedArgs<T> a) {
   const int x = x0 + xl;
   const bool xin = x < a.xext;
   for (int row = r0; row < n; row += NJ)
-    s0[row * tx + xl] = (row < a.n_in && xin) ? src[row * a.s_row + x] : czero<C>();
+    sm[row * tx + xl] = (row < a.n_in && xin) ? src[row * a.s_row + x] : czero<C>();
   __syncthreads();
   const FftLayout lay{lg_nl, true};
-  C* res = fft_lines<INV, C, SMALL>(s0, s1, a.plan, tx, 1, tx, lay, a.tw);
+  const int res = fft_lines<INV, C, SMALL>(0, b1, a.plan, tx, 1, tx, lay, tw);
   if (xin)
-    for (int row = r0; row < a.n_out; row += NJ) dst[row * a.d_row + x] = res[row * tx + xl];
+    for (int row = r0; row < a.n_out; row += NJ) dst[row * a.d_row + x] = sm[res + row * tx + xl];
 }
 
 // ---- pass Z: FFT_z ⊗ tensor multiply ⊗ IFFT_z, in place in T2 -----------
@@ -170,12 +171,12 @@ template <typename T, bool SMALL, bool SYM>
 __global__ void __launch_bounds__(kThreads) k_z(PipeArgs<T> a) {
   using C = cplx_t<T>;
   if (a.skip && *a.skip) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* sm = shmem<C>();
   const int R = a.R;
   const int lg_nl = a.lg_tx, tx = 1 << lg_nl, NJ = kThreads >> lg_nl;
   const int w = 3 * tx;
-  C* s0 = reinterpret_cast<C*>(smem_raw);
-  C* s1 = s0 + R * w;
+  const int b1 = R * w, tw = 2 * R * w;
+  load_twiddles(a.twR, R, tw);
   const int x0 = blockIdx.x * tx;
   const int ky = blockIdx.y;
   const int64_t PQ = (int64_t)a.P * a.Q;
@@ -187,10 +188,10 @@ __global__ void __launch_bounds__(kThreads) k_z(PipeArgs<T> a) {
 #pragma unroll
   for (int c = 0; c < 3; ++c)
     for (int z = r0; z < R; z += NJ)
-      s0[z * w + c * tx + xl] = (z < a.N && xin) ? t2[x + z * zs + c * cs] : czero<C>();
+      sm[z * w + c * tx + xl] = (z < a.N && xin) ? t2[x + z * zs + c * cs] : czero<C>();
   __syncthreads();
   const FftLayout lay{lg_nl, true};
-  C* res = fft_lines<false, C, SMALL>(s0, s1, a.pR, w, 1, w, lay, a.twR);
+  const int res = fft_lines<false, C, SMALL>(0, b1, a.pR, w, 1, w, lay, tw);
   if (xin) {
     int gx = x, gy = ky, Pg = a.P, Qg = a.Q, Rg = R;
     bool fx = false, fy = false;
@@ -206,7 +207,8 @@ __global__ void __launch_bounds__(kThreads) k_z(PipeArgs<T> a) {
       bool fz = false;
       if (SYM && kz > R / 2) { gz = R - kz; fz = true; }
       const int64_t gi = gz * PQg;
-      C g0 = __ldg(G + gi), g1 = __ldg(G + PQRg + gi), g2 = __ldg(G + 2 * PQRg + gi);
+      const C g0 = __ldg(G + gi);
+      C g1 = __ldg(G + PQRg + gi), g2 = __ldg(G + 2 * PQRg + gi);
       const C g3 = __ldg(G + 3 * PQRg + gi);
       C g4 = __ldg(G + 4 * PQRg + gi);
       const C g5 = __ldg(G + 5 * PQRg + gi);
@@ -215,23 +217,23 @@ __global__ void __launch_bounds__(kThreads) k_z(PipeArgs<T> a) {
         if (fx != fz) { g2.x = -g2.x; g2.y = -g2.y; }
         if (fy != fz) { g4.x = -g4.x; g4.y = -g4.y; }
       }
-      C* p = res + kz * w + xl;
-      const C v0 = p[0], v1 = p[tx], v2 = p[2 * tx];
+      const int p = res + kz * w + xl;
+      const C v0 = sm[p], v1 = sm[p + tx], v2 = sm[p + 2 * tx];
       C o0 = cmul(g0, v0); o0 = cfma(g1, v1, o0); o0 = cfma(g2, v2, o0);
       C o1 = cmul(g1, v0); o1 = cfma(g3, v1, o1); o1 = cfma(g4, v2, o1);
       C o2 = cmul(g2, v0); o2 = cfma(g4, v1, o2); o2 = cfma(g5, v2, o2);
-      p[0] = o0;
-      p[tx] = o1;
-      p[2 * tx] = o2;
+      sm[p] = o0;
+      sm[p + tx] = o1;
+      sm[p + 2 * tx] = o2;
     }
   }
   __syncthreads();
-  C* other = (res == s0) ? s1 : s0;
-  C* out = fft_lines<true, C, SMALL>(res, other, a.pR, w, 1, w, lay, a.twR);
+  const int other = (res == 0) ? b1 : 0;
+  const int out = fft_lines<true, C, SMALL>(res, other, a.pR, w, 1, w, lay, tw);
   if (xin) {
 #pragma unroll
     for (int c = 0; c < 3; ++c)
-      for (int z = r0; z < a.N; z += NJ) t2[x + z * zs + c * cs] = out[z * w + c * tx + xl];
+      for (int z = r0; z < a.N; z += NJ) t2[x + z * zs + c * cs] = sm[out + z * w + c * tx + xl];
   }
 }
 
@@ -266,7 +268,7 @@ void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaS
   const int nlines = a.M * a.N * 3;
   const int lpb = 1 << a.lg_lpb;
   dim3 grid(ceil_div(nlines, lpb), nrhs);
-  const size_t smem = 2ull * lpb * a.P * sizeof(cplx_t<T>);
+  const size_t smem = (2ull * lpb * a.P + a.P) * sizeof(cplx_t<T>);
   const bool small = plan_is_small_radix(a.pP);
 #define VS_X(KER, MD)                                        \
   {                                                          \
@@ -299,7 +301,7 @@ template <typename T, bool INV>
 void launch_strided_pass(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st) {
   const int tx = 1 << a.lg_tx;
   dim3 grid(ceil_div(a.xext, tx), nplanes, nrhs);
-  const size_t smem = 2ull * a.plan.n * tx * sizeof(cplx_t<T>);
+  const size_t smem = (2ull * a.plan.n * tx + a.plan.n) * sizeof(cplx_t<T>);
   if (plan_is_small_radix(a.plan)) {
     auto k = k_strided<T, INV, true>;
     set_smem(k, smem);
@@ -367,7 +369,7 @@ void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, in
     case 2: {
       const int tx = 1 << a.lg_tx;
       dim3 grid(ceil_div(op.P, tx), op.Q, nrhs);
-      const size_t smem = 2ull * op.R * 3 * tx * sizeof(C);
+      const size_t smem = (2ull * op.R * 3 * tx + op.R) * sizeof(C);
       const bool small = plan_is_small_radix(a.pR);
 #define VS_Z(SM, SY)                   \
   {                                    \
@@ -410,28 +412,28 @@ template void matvec<double>(const vs_op&, const double2*, double2*, int, int, c
 // ---- generic batched FFTs (operator setup, preconditioner) --------------
 template <typename T, bool INV>
 __global__ void __launch_bounds__(kThreads) k_axis0(cplx_t<T>* data, int n, int64_t nlines, int lg_lpb, FftPlan plan,
-                                                    const cplx_t<T>* tw) {
+                                                    const cplx_t<T>* twg) {
   using C = cplx_t<T>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* sm = shmem<C>();
   const int lpb = 1 << lg_lpb, lg_nj = 8 - lg_lpb, NJ = 1 << lg_nj;
-  C* s0 = reinterpret_cast<C*>(smem_raw);
-  C* s1 = s0 + lpb * n;
+  const int b1 = lpb * n, tw = 2 * lpb * n;
+  load_twiddles(twg, n, tw);
   const int l = threadIdx.x >> lg_nj, jt = threadIdx.x & (NJ - 1);
   const int64_t line = (int64_t)blockIdx.x * lpb + l;
   const bool live = line < nlines;
   C* base = data + line * n;
-  for (int i = jt; i < n; i += NJ) s0[l * n + i] = live ? base[i] : czero<C>();
+  for (int i = jt; i < n; i += NJ) sm[l * n + i] = live ? base[i] : czero<C>();
   __syncthreads();
   const FftLayout lay{lg_lpb, false};
-  C* res = fft_lines<INV, C, false>(s0, s1, plan, lpb, n, 1, lay, tw);
+  const int res = fft_lines<INV, C, false>(0, b1, plan, lpb, n, 1, lay, tw);
   if (live)
-    for (int i = jt; i < n; i += NJ) base[i] = res[l * n + i];
+    for (int i = jt; i < n; i += NJ) base[i] = sm[res + l * n + i];
 }
 
 template <typename T, bool INV>
 void fft_axis0(cplx_t<T>* data, int n, int64_t nlines, const FftAxis& ax, cudaStream_t st) {
   const int lpb = pick_lpb(n, sizeof(cplx_t<T>));
-  const size_t smem = 2ull * lpb * n * sizeof(cplx_t<T>);
+  const size_t smem = (2ull * lpb * n + n) * sizeof(cplx_t<T>);
   auto k = k_axis0<T, INV>;
   set_smem(k, smem);
   k<<<ceil_div(nlines, lpb), kThreads, smem, st>>>(data, n, nlines, ilog2(lpb), ax.plan, ax.tw<T>());

@@ -274,7 +274,9 @@ __global__ void __launch_bounds__(256) k_block_gemv(cplx_t<T>* __restrict__ t, c
 // that share it, so every stored block is read from memory once per apply.
 // Variant v has flips fx = v&1, fy = v>>1 (negate the x / y component entries
 // of the input and of the output).
-template <typename T>
+// PAIR (c64 with even n): each thread forms two adjacent rows from 16-byte
+// loads of column entries (r, r+1).
+template <typename T, bool PAIR>
 __global__ void __launch_bounds__(256) k_block_gemv_sym(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ inv,
                                                         int L, int M, int N, int ti, int64_t rhs_stride,
                                                         const int* skip) {
@@ -306,28 +308,54 @@ __global__ void __launch_bounds__(256) k_block_gemv_sym(cplx_t<T>* __restrict__ 
     v[u] = val;
   }
   __syncthreads();
-  for (int rr = threadIdx.x; rr < ti * n; rr += blockDim.x) {
-    const int il = rr / n, r = rr - il * n;
-    const int is = is0 + il;
-    if (is >= Lb) continue;
-    const C* A = inv + ((int64_t)is + (int64_t)Lb * js) * n * n + r;
-    const C* x = v + il * 4 * n;
-    C a0 = czero<C>(), a1 = czero<C>(), a2 = czero<C>(), a3 = czero<C>();
-#pragma unroll 4
-    for (int q = 0; q < n; ++q) {
-      const C m = __ldg(A + (int64_t)q * n);
-      a0 = cfma(m, x[q], a0);
-      a1 = cfma(m, x[n + q], a1);
-      a2 = cfma(m, x[2 * n + q], a2);
-      a3 = cfma(m, x[3 * n + q], a3);
-    }
+  auto put = [&](int il, int r, C a0, C a1, C a2, C a3) {
     const int comp = r / N;
-    C* out = o + il * 4 * n + r;
+    const int o0 = il * 4 * n + r;
     // variant flips of the output rows
-    out[0] = a0;
-    out[n] = (comp == 0) ? make_c<C>(-a1.x, -a1.y) : a1;
-    out[2 * n] = (comp == 1) ? make_c<C>(-a2.x, -a2.y) : a2;
-    out[3 * n] = (comp == 0 || comp == 1) ? make_c<C>(-a3.x, -a3.y) : a3;
+    o[o0] = a0;
+    o[o0 + n] = (comp == 0) ? make_c<C>(-a1.x, -a1.y) : a1;
+    o[o0 + 2 * n] = (comp == 1) ? make_c<C>(-a2.x, -a2.y) : a2;
+    o[o0 + 3 * n] = (comp == 0 || comp == 1) ? make_c<C>(-a3.x, -a3.y) : a3;
+  };
+  if (PAIR) {
+    const int h = n >> 1;
+    for (int rr = threadIdx.x; rr < ti * h; rr += blockDim.x) {
+      const int il = rr / h, r = 2 * (rr - il * h);
+      const int is = is0 + il;
+      if (is >= Lb) continue;
+      const float4* A = reinterpret_cast<const float4*>(inv + ((int64_t)is + (int64_t)Lb * js) * n * n + r);
+      const C* x = v + il * 4 * n;
+      C a0 = czero<C>(), a1 = czero<C>(), a2 = czero<C>(), a3 = czero<C>();
+      C b0 = czero<C>(), b1 = czero<C>(), b2 = czero<C>(), b3 = czero<C>();
+#pragma unroll 4
+      for (int q = 0; q < n; ++q) {
+        const float4 mm = __ldg(A + (int64_t)q * h);
+        const C m0 = make_c<C>(mm.x, mm.y), m1 = make_c<C>(mm.z, mm.w);
+        const C x0 = x[q], x1 = x[n + q], x2 = x[2 * n + q], x3 = x[3 * n + q];
+        a0 = cfma(m0, x0, a0); a1 = cfma(m0, x1, a1); a2 = cfma(m0, x2, a2); a3 = cfma(m0, x3, a3);
+        b0 = cfma(m1, x0, b0); b1 = cfma(m1, x1, b1); b2 = cfma(m1, x2, b2); b3 = cfma(m1, x3, b3);
+      }
+      put(il, r, a0, a1, a2, a3);
+      put(il, r + 1, b0, b1, b2, b3);
+    }
+  } else {
+    for (int rr = threadIdx.x; rr < ti * n; rr += blockDim.x) {
+      const int il = rr / n, r = rr - il * n;
+      const int is = is0 + il;
+      if (is >= Lb) continue;
+      const C* A = inv + ((int64_t)is + (int64_t)Lb * js) * n * n + r;
+      const C* x = v + il * 4 * n;
+      C a0 = czero<C>(), a1 = czero<C>(), a2 = czero<C>(), a3 = czero<C>();
+#pragma unroll 4
+      for (int q = 0; q < n; ++q) {
+        const C m = __ldg(A + (int64_t)q * n);
+        a0 = cfma(m, x[q], a0);
+        a1 = cfma(m, x[n + q], a1);
+        a2 = cfma(m, x[2 * n + q], a2);
+        a3 = cfma(m, x[3 * n + q], a3);
+      }
+      put(il, r, a0, a1, a2, a3);
+    }
   }
   __syncthreads();
   for (int u = threadIdx.x; u < ti * 4 * n; u += blockDim.x) {
@@ -396,9 +424,16 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
         int ti = std::min(Lb, 4);
         while (ti > 1 && 2ull * ti * 4 * n * sizeof(C) > 64 * 1024) --ti;
         const size_t smem = 2ull * ti * 4 * n * sizeof(C);
-        auto k = k_block_gemv_sym<T>;
-        set_kernel_smem((const void*)k, smem);
-        k<<<dim3(ceil_div(Lb, ti), Mb, nrhs), 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
+        const dim3 grid(ceil_div(Lb, ti), Mb, nrhs);
+        if (std::is_same<T, float>::value && n % 2 == 0) {
+          auto k = k_block_gemv_sym<T, true>;
+          set_kernel_smem((const void*)k, smem);
+          k<<<grid, 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
+        } else {
+          auto k = k_block_gemv_sym<T, false>;
+          set_kernel_smem((const void*)k, smem);
+          k<<<grid, 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
+        }
         VS_LAUNCH_CHECK();
         break;
       }
