@@ -4,6 +4,7 @@
 #include "vs_internal.h"
 #include "vs_krylov.h"
 #include <chrono>
+#include <atomic>
 #include <complex>
 #include <cstring>
 #include <cmath>
@@ -11,6 +12,11 @@
 namespace {
 
 thread_local std::string g_last_error;
+
+uint64_t next_object_id() {
+  static std::atomic<uint64_t> counter{1};
+  return counter.fetch_add(1);
+}
 
 template <typename F>
 int guarded(vs_ctx* ctx, F&& f) {
@@ -506,6 +512,7 @@ int vs_prec_create(vs_op* op, const double* shift, const double* d, int64_t nd, 
     VS_REQUIRE(shift && d && out, "NULL argument");
     VS_REQUIRE(nd == 1 || nd == 3 * (int64_t)op->N, "d must have 1 or 3N entries");
     pr = new vs_prec();
+    pr->id = next_object_id();
     pr->ctx = op->ctx;
     pr->L = op->L; pr->M = op->M; pr->N = op->N;
     pr->V = op->V; pr->n3 = op->n3;
@@ -560,6 +567,7 @@ int vs_prec_create_blocks(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const do
     check_grid(L, M, N);
     VS_REQUIRE(inv_blocks && idx3 && out, "NULL argument");
     pr = new vs_prec();
+    pr->id = next_object_id();
     pr->ctx = ctx;
     pr->L = (int)L; pr->M = (int)M; pr->N = (int)N;
     pr->V = L * M * N;

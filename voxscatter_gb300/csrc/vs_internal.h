@@ -42,10 +42,23 @@ template <> inline const float2* FftAxis::tw<float>() const { return tw32.as<flo
 template <> inline const double2* FftAxis::tw<double>() const { return tw64.as<double2>(); }
 
 // Work vectors and device scalars of the Krylov solvers (vs_krylov.cu).
+// A captured iteration graph and the buffers/settings it was captured with.
+struct GraphCache {
+  cudaGraphExec_t exec = nullptr;
+  std::vector<const void*> key;
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    key.clear();
+  }
+  ~GraphCache() { reset(); }
+};
+
 struct KrylovWork {
   DevBuf r, rt, p, v_, s, t, ph, sh, x;  // in the inner solver's precision
   DevBuf r64, y64;                       // FP64 residual / matvec output
   DevBuf partials, state, scal, resvec;
+  GraphCache graph32, graph64;           // BiCGSTAB iteration graphs (c64 / c128)
   template <typename T> void ensure(int64_t n);
 };
 
@@ -87,6 +100,7 @@ struct vs_op {
 // 2-level circulant preconditioner: inverse blocks per (x,y) frequency.
 struct vs_prec {
   vs_ctx* ctx = nullptr;
+  uint64_t id = 0;          // unique per preconditioner object (keys cached solver graphs)
   int L = 0, M = 0, N = 0;
   bool sym = false;         // blocks stored for i <= L/2, j <= M/2 only (parity of the operator)
   int64_t V = 0, n3 = 0;

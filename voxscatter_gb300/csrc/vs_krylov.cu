@@ -295,6 +295,10 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* x, cplx_t<T>
     s->iter2 = k;
     s->res = res;
     s->rho_prev = s->rho;
+    if (res < 0.99 * s->best_res) {
+      s->best_res = res;
+      s->best_iter2 = k;
+    }
     if (!isfinite(res)) {
       s->flag = 5;
       s->skip = 1;
@@ -303,6 +307,9 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* x, cplx_t<T>
       s->skip = 1;
     } else if (k >= 2 * s->maxit) {
       s->flag = 1;
+      s->skip = 1;
+    } else if (s->stag_window > 0 && k - s->best_iter2 >= 2 * s->stag_window) {
+      s->flag = 3;  // stagnated (MATLAB flag 3)
       s->skip = 1;
     }
   }
@@ -350,6 +357,11 @@ __global__ void k_update64(double2* x, const float2* d, int64_t n, double sc) {
     x[i].y = fma(sc, (double)d[i].y, x[i].y);
   }
 }
+
+// Inner (c64) solves stop when the residual has not improved by 1% for this
+// many iterations: the c64 recurrence has reached its floor and the FP64
+// refinement takes over.
+constexpr int kStagnationWindow = 8;
 
 static int vec_grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), kRedBlocks)); }
 
@@ -408,7 +420,7 @@ static int kernels_per_iteration(const vs_prec* pr) { return 7 + 10 + (pr ? 10 :
 template <typename T>
 static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t n, double bnorm, double tol,
                             int maxit, double res_scale, double* resvec_dev, int resvec_cap, int per_graph,
-                            cudaStream_t st, int64_t* launches) {
+                            cudaStream_t st, int64_t* launches, int stag_window) {
   using C = cplx_t<T>;
   KState h{};
   h.tol_abs = tol * bnorm;
@@ -418,6 +430,8 @@ static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, i
   h.resvec_cap = resvec_cap;
   h.partials = w.partials.as<double>();
   h.flag = 1;
+  h.stag_window = stag_window;
+  h.best_res = INFINITY;
   KState* s = w.state.as<KState>();
   // r0 norm
   upload_state(s, h, st);
@@ -438,39 +452,50 @@ static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, i
     h.flag = (r0 <= h.tol_abs) ? 0 : 1;
     return h;
   }
-  // One launch sequence with skip set, outside capture: every kernel returns at
-  // once, but first-use attribute calls happen here rather than in the capture.
-  {
+  h.best_res = r0;
+  // The iteration graph depends only on the buffers, the preconditioner and
+  // the graph length (scalars live in the device state), so it is captured
+  // once and reused by later solves on this operator.
+  GraphCache& gc = std::is_same<T, float>::value ? w.graph32 : w.graph64;
+  std::vector<const void*> key = {w.r.p, w.rt.p, w.p.p, w.v_.p, w.s.p, w.t.p, w.ph.p, w.sh.p, w.x.p,
+                                  w.state.p, w.partials.p, op.t1.p, op.t2.p,
+                                  (const void*)(uintptr_t)(pr ? pr->id : 0), pr ? pr->t.p : nullptr,
+                                  (const void*)(uintptr_t)per_graph};
+  if (gc.exec == nullptr || gc.key != key) {
+    gc.reset();
+    // One launch sequence with skip set, outside capture: every kernel returns
+    // at once, but first-use attribute calls happen here rather than in the
+    // capture.
     KState idle = h;
     idle.skip = 1;
     upload_state(s, idle, st);
     bicg_iteration<T>(op, pr, w, s, n, st);
     *launches += kernels_per_iteration(pr);
+    cudaGraph_t graph = nullptr;
+    VS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+      for (int k = 0; k < per_graph; ++k) bicg_iteration<T>(op, pr, w, s, n, st);
+    } catch (...) {
+      cudaStreamEndCapture(st, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    VS_CUDA(cudaStreamEndCapture(st, &graph));
+    cudaError_t e = cudaGraphInstantiate(&gc.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    VS_CUDA(e);
+    gc.key = key;
   }
   upload_state(s, h, st);
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  VS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  try {
-    for (int k = 0; k < per_graph; ++k) bicg_iteration<T>(op, pr, w, s, n, st);
-  } catch (...) {
-    cudaStreamEndCapture(st, &graph);
-    if (graph) cudaGraphDestroy(graph);
-    throw;
-  }
-  VS_CUDA(cudaStreamEndCapture(st, &graph));
-  VS_CUDA(cudaGraphInstantiate(&exec, graph, 0));
   KState cur{};
   const int max_launch = (maxit + per_graph - 1) / per_graph + 1;
   for (int it = 0; it < max_launch; ++it) {
-    VS_CUDA(cudaGraphLaunch(exec, st));
+    VS_CUDA(cudaGraphLaunch(gc.exec, st));
     *launches += (int64_t)per_graph * kernels_per_iteration(pr);
     VS_CUDA(cudaMemcpyAsync(&cur, s, sizeof(KState), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
     if (cur.skip) break;
   }
-  cudaGraphExecDestroy(exec);
-  cudaGraphDestroy(graph);
   if (!cur.skip) cur.flag = 1;
   return cur;
 }
@@ -531,9 +556,16 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
     w.y64.alloc(n * sizeof(double2));
     // x0 -> w.x ; r = b - A x0
     k_copy<double><<<vec_grid(n), 256, 0, st>>>(w.x.as<double2>(), x, n);
-    residual64(op, w, b, x, w.r.as<double2>(), n, st, &launches);
+    if (norm64(w, x, n, st, &launches) == 0.0) {  // x0 = 0: r = b exactly, no matvec
+      k_copy<double><<<vec_grid(n), 256, 0, st>>>(w.r.as<double2>(), b, n);
+      VS_LAUNCH_CHECK();
+      launches += 1;
+    } else {
+      residual64(op, w, b, x, w.r.as<double2>(), n, st, &launches);
+    }
     launches += 1;
-    KState fs = bicgstab_core<double>(op, pr, w, n, bnorm, prm.tol, prm.maxit, 1.0 / bnorm, rv, cap, prm.per_graph, st, &launches);
+    KState fs = bicgstab_core<double>(op, pr, w, n, bnorm, prm.tol, prm.maxit, 1.0 / bnorm, rv, cap, prm.per_graph, st,
+                                      &launches, 0);
     launches += 1;
     k_copy<double><<<vec_grid(n), 256, 0, st>>>(x, w.x.as<double2>(), n);
     VS_LAUNCH_CHECK();
@@ -550,7 +582,15 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
     w.y64.alloc(n * sizeof(double2));
     w.r64.alloc(n * sizeof(double2));
     double2* r64 = w.r64.as<double2>();
-    double rn = residual64(op, w, b, x, r64, n, st, &launches);
+    double rn;
+    if (norm64(w, x, n, st, &launches) == 0.0) {  // x0 = 0: r = b exactly, no matvec
+      k_copy<double><<<vec_grid(n), 256, 0, st>>>(r64, b, n);
+      VS_LAUNCH_CHECK();
+      launches += 1;
+      rn = bnorm;
+    } else {
+      rn = residual64(op, w, b, x, r64, n, st, &launches);
+    }
     int inner_total2 = 0;
     int64_t nres = 0;
     int flag = 1;
@@ -561,7 +601,9 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
         break;
       }
       if (refine == prm.max_refine || inner_total2 >= 2 * prm.maxit) break;
-      double itol = prm.inner_tol > 0 ? prm.inner_tol : std::max(0.5 * prm.tol * bnorm / rn, prm.inner_floor);
+      // Aim one inner solve at the whole remaining reduction (with margin for
+      // the c64 rounding of the operator), but not below what c64 can reach.
+      double itol = prm.inner_tol > 0 ? prm.inner_tol : std::max(0.3 * prm.tol * bnorm / rn, prm.inner_floor);
       itol = std::min(itol, 0.5);
       k_scale_down<<<vec_grid(n), 256, 0, st>>>(r64, w.r.as<float2>(), n, 1.0 / rn);
       k_zero<float><<<vec_grid(n), 256, 0, st>>>(w.x.as<float2>(), n);
@@ -569,7 +611,7 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
       double* rvk = (rv && nres < cap) ? rv + nres : nullptr;
       const int capk = rv ? (int)(cap - nres) : 0;
       KState fs = bicgstab_core<float>(op, pr, w, n, 1.0, itol, prm.maxit - inner_total2 / 2, rn / bnorm, rvk, capk,
-                                       prm.per_graph, st, &launches);
+                                       prm.per_graph, st, &launches, kStagnationWindow);
       launches += 2;
       inner_total2 += fs.iter2;
       nres += std::min<int64_t>(fs.nres, capk);

@@ -9,10 +9,13 @@ namespace vs {
 struct KState {
   double2 rho, rho_prev, alpha, omega, beta;
   double tol_abs, res, res_scale;
+  double best_res;  // smallest full-step residual so far (stagnation guard)
   double* partials;
   double* resvec;
   unsigned counter;
   int skip, flag, half_pending, iter2, maxit, nres, resvec_cap;
+  int best_iter2;   // half-step count at best_res
+  int stag_window;  // stop with flag 3 after this many iterations without a 1% improvement (0: off)
 };
 
 struct SolveParams {
@@ -20,7 +23,7 @@ struct SolveParams {
   double tol = 1e-6;
   int maxit = 2000;
   double inner_tol = 0;  // 0: automatic
-  double inner_floor = 1e-6;
+  double inner_floor = 1e-7;
   int max_refine = 10;
   int per_graph = 4;
   int resvec_cap = 0;
