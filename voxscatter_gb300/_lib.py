@@ -43,6 +43,7 @@ SIGNATURES = {
     "vs_op_info": (C.c_int, [_vp, _pi64, _pi64, _pi64]),
     "vs_op_apply": (C.c_int, [_vp, _pd, _pd, _i64, C.c_int, C.c_int]),
     "vs_op_apply_device": (C.c_int, [_vp, _vp, _vp, _i64, C.c_int, C.c_int]),
+    "vs_op_apply_device_noalloc": (C.c_int, [_vp, _vp, _vp, _i64, C.c_int, C.c_int]),
     "vs_circ_levels": (C.c_int, [_vp, _i64, _i64, _i64, _pd, _pd, _pd, _pd]),
     "vs_prec_create": (C.c_int, [_vp, _pd, _pd, _i64, C.c_int, C.POINTER(_vp)]),
     "vs_prec_create_blocks": (C.c_int, [_vp, _i64, _i64, _i64, _pd, _pi64, _i64, C.c_int, C.POINTER(_vp)]),

@@ -119,6 +119,9 @@ template <typename T>
 void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
                  cudaStream_t st, int pass);
 template <typename T>
+void matvec_scratch(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, cplx_t<T>* t1,
+                    cplx_t<T>* t2, cudaStream_t st);
+template <typename T>
 void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
             cudaStream_t st);
 void ensure_scratch(vs_op& op, int nrhs, size_t elem_bytes);

@@ -404,6 +404,46 @@ template void launch_strided_pass<float, true>(const StridedArgs<float>&, int, i
 template void launch_strided_pass<double, false>(const StridedArgs<double>&, int, int, cudaStream_t);
 template void launch_strided_pass<double, true>(const StridedArgs<double>&, int, int, cudaStream_t);
 
+// The same five launches with caller-provided intermediates (t1: P*M*N*3,
+// t2: P*Q*N*3 elements per right-hand side) instead of the operator's own.
+template <typename T>
+void matvec_scratch(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, cplx_t<T>* t1,
+                    cplx_t<T>* t2, cudaStream_t st) {
+  VS_REQUIRE(mode >= VS_NOTRANSP && mode <= VS_CONJTRANSP, "mode must be VS_NOTRANSP, VS_TRANSP or VS_CONJTRANSP");
+  PipeArgs<T> a = pipe_args<T>(op, x, y, nullptr);
+  a.t1 = t1;
+  a.t2 = t2;
+  launch_x_pass<T>(a, false, mode, nrhs, st);
+  StridedArgs<T> yf = y_pass_args<T>(op, a, false);
+  launch_strided_pass<T, false>(yf, op.N * 3, nrhs, st);
+  {
+    using C = cplx_t<T>;
+    const int tx = 1 << a.lg_tx;
+    dim3 grid(ceil_div(op.P, tx), op.Q, nrhs);
+    const size_t smem = (2ull * op.R * 3 * tx + op.R) * sizeof(C);
+    const bool small = plan_is_small_radix(a.pR);
+#define VS_Z2(SM, SY)                  \
+  {                                    \
+    auto k = k_z<T, SM, SY>;           \
+    set_smem(k, smem);                 \
+    k<<<grid, kThreads, smem, st>>>(a);\
+  }
+    if (op.gsym) {
+      if (small) VS_Z2(true, true) else VS_Z2(false, true)
+    } else {
+      if (small) VS_Z2(true, false) else VS_Z2(false, false)
+    }
+#undef VS_Z2
+    VS_LAUNCH_CHECK();
+  }
+  StridedArgs<T> yi = y_pass_args<T>(op, a, true);
+  launch_strided_pass<T, true>(yi, op.N * 3, nrhs, st);
+  launch_x_pass<T>(a, true, mode, nrhs, st);
+}
+template void matvec_scratch<float>(const vs_op&, const float2*, float2*, int, int, float2*, float2*, cudaStream_t);
+template void matvec_scratch<double>(const vs_op&, const double2*, double2*, int, int, double2*, double2*,
+                                     cudaStream_t);
+
 template void matvec_pass<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t, int);
 template void matvec_pass<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t, int);
 template void matvec<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t);
