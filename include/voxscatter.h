@@ -201,6 +201,7 @@ typedef struct vs_solve_opts {
   int iters_per_graph; /* iterations captured per CUDA graph launch (host polls in between)  */
   double* resvec;      /* optional: relative residual norms at every half step               */
   int64_t resvec_cap;  /* capacity of resvec                                                 */
+  int transpose;       /* 0: solve A x = b; 1: solve A^T x = b (plain transpose, adjoints)   */
 } vs_solve_opts;
 
 typedef struct vs_solve_info {
@@ -226,6 +227,32 @@ int vs_solve(vs_op* op, vs_prec* prec, const double* b, double* x, const vs_solv
 
 /* Same with b and x in device memory (double2, n3 each). */
 int vs_solve_device(vs_op* op, vs_prec* prec, const void* b, void* x, const vs_solve_opts* opts, vs_solve_info* info);
+
+/* ---- excitation, extinction cross section, gradient ------------------- */
+
+/* Plane wave E0 .* exp(1i k.r) at op's unknowns: PlaneWavePointWise.m:7-19
+ * followed by the Einc(idx3) gather of main_DDA.m:81, FP64 on the device.
+ *   x[L], y[M], z[N]: voxel-centre coordinates (grid3d.m:41-61); E0: 3
+ *   complex.  b_out: n3 complex (host). */
+int vs_plane_wave(vs_op* op, const double* x, const double* y, const double* z, const double kvec[3],
+                  const double* E0, double* b_out);
+
+/* Extinction cross section of a DDA solution P (n3 complex, the reference's
+ * dipole moment per volume) under the incident field Einc at the same
+ * unknowns: C_ext = 4 pi ko dV / |E0|^2 sum Im(conj(Einc) P) (Draine &
+ * Flatau 1994, eq. 8).  Absent from the reference (README.md:35). */
+int vs_cext(vs_op* op, const double* P, const double* Einc, double ko, double dV, double e0norm2, double* cext);
+
+/* C_ext and its gradient with respect to each voxel's permittivity by the
+ * adjoint method: solves A P = Einc and A^T lam = conj(Einc) with opts (the
+ * operator must carry Gram = 1/alpha_LDR(eps) per voxel and Mc = dV, the DDA
+ * system of main_DDA.m:75), then dC/d eps_j = -c Im/Re(d(1/alpha)/d eps_j *
+ * sum_comp lam_j P_j).  eps: one complex per voxel in idx order (n3/3);
+ * grad_re/grad_im: dC/dRe(eps_j), dC/dIm(eps_j); P_out optional (n3).
+ * Requires idx3 in the [idx; V+idx; 2V+idx] form. */
+int vs_cext_grad(vs_op* op, vs_prec* prec, const double* Einc, const double* eps, double ko, double d,
+                 const double kvec[3], const double E0[3], const vs_solve_opts* opts, double* cext, double* grad_re,
+                 double* grad_im, double* P_out, vs_solve_info* info_fwd, vs_solve_info* info_adj);
 
 /* ---- diagnostics ----------------------------------------------------- */
 

@@ -60,7 +60,7 @@ VS_SOLVE_MIXED, VS_SOLVE_FP64 = 0, 1
 class vs_solve_opts(C.Structure):
     _fields_ = [("method", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("maxit", C.c_int),
                 ("inner_tol", C.c_double), ("max_refine", C.c_int), ("iters_per_graph", C.c_int),
-                ("resvec", _pd), ("resvec_cap", _i64)]
+                ("resvec", _pd), ("resvec_cap", _i64), ("transpose", C.c_int)]
 
 
 class vs_solve_info(C.Structure):
@@ -69,6 +69,11 @@ class vs_solve_info(C.Structure):
 
 
 SIGNATURES.update({
+    "vs_plane_wave": (C.c_int, [_vp, _pd, _pd, _pd, _pd, _pd, _pd]),
+    "vs_cext": (C.c_int, [_vp, _pd, _pd, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double)]),
+    "vs_cext_grad": (C.c_int, [_vp, _vp, _pd, _pd, C.c_double, C.c_double, _pd, _pd, C.POINTER(vs_solve_opts),
+                               C.POINTER(C.c_double), _pd, _pd, _pd, C.POINTER(vs_solve_info),
+                               C.POINTER(vs_solve_info)]),
     "vs_op_time_passes": (C.c_int, [_vp, _vp, _vp, _i64, C.c_int, C.c_int, C.POINTER(C.c_float)]),
     "vs_prec_time_passes": (C.c_int, [_vp, _vp, _vp, _i64, C.c_int, C.c_int, C.POINTER(C.c_float)]),
     "vs_solve_opts_default": (None, [C.POINTER(vs_solve_opts)]),

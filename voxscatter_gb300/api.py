@@ -312,7 +312,7 @@ def mvp_circ_2_level(inv_blocks, JIn, Lx, My, Nz, idx, precision="c128", ctx=Non
 
 
 def solve(op, b, prec=None, tol=1e-6, maxit=2000, precision="mixed", x0=None, inner_tol=0.0, max_refine=10,
-          iters_per_graph=4, want_resvec=True):
+          iters_per_graph=4, want_resvec=True, transpose=False):
     """Device Krylov solve; returns (x, info dict, resvec)."""
     lib = op.ctx._lib
     b = np.ascontiguousarray(np.asarray(b, dtype=np.complex128).ravel())
@@ -322,6 +322,7 @@ def solve(op, b, prec=None, tol=1e-6, maxit=2000, precision="mixed", x0=None, in
     o.precision = L.VS_SOLVE_MIXED if precision == "mixed" else L.VS_SOLVE_FP64
     o.tol = float(tol); o.maxit = int(maxit); o.inner_tol = float(inner_tol); o.max_refine = int(max_refine)
     o.iters_per_graph = int(iters_per_graph)
+    o.transpose = 1 if transpose else 0
     rv = np.zeros(4 * int(maxit) + 64 if want_resvec else 1)
     if want_resvec:
         o.resvec = L.dptr(rv); o.resvec_cap = rv.size
@@ -372,3 +373,54 @@ def bicgstab(A, b, tol=1e-6, maxit=20, M1=None, M2=None, x0=None, precision="mix
     x, info, rv = solve(A, b, prec=M1, tol=tol, maxit=maxit, precision=precision, x0=x0)
     nb = np.linalg.norm(np.asarray(b))
     return x, info["flag"], info["relres"], info["iter"], rv * nb
+
+
+def _solve_opts(lib, tol, maxit, precision):
+    o = L.vs_solve_opts()
+    lib.vs_solve_opts_default(C.byref(o))
+    o.precision = L.VS_SOLVE_MIXED if precision == "mixed" else L.VS_SOLVE_FP64
+    o.tol = float(tol)
+    o.maxit = int(maxit)
+    return o
+
+
+def plane_wave(op, r, kvec, Eo):
+    """Einc(idx3) = PlaneWavePointWise(Eo, kvec, r)(idx3) on the device (FP64)."""
+    r = np.asarray(r, dtype=float)
+    x = np.ascontiguousarray(r[:, 0, 0, 0]); y = np.ascontiguousarray(r[0, :, 0, 1])
+    z = np.ascontiguousarray(r[0, 0, :, 2])
+    kv = np.ascontiguousarray(np.asarray(kvec, dtype=float))
+    e0 = np.ascontiguousarray(np.asarray(Eo, dtype=np.complex128))
+    b = np.zeros(op.n3, dtype=np.complex128)
+    L.check(op.ctx._lib.vs_plane_wave(op.h, L.dptr(x), L.dptr(y), L.dptr(z), L.dptr(kv), L.dptr(e0), L.dptr(b)),
+            op.ctx.h)
+    return b
+
+
+def cext(op, P, Einc, ko, dV, Eo):
+    """Extinction cross section of the polarisation P."""
+    P = np.ascontiguousarray(np.asarray(P, dtype=np.complex128))
+    E = np.ascontiguousarray(np.asarray(Einc, dtype=np.complex128))
+    out = C.c_double()
+    L.check(op.ctx._lib.vs_cext(op.h, L.dptr(P), L.dptr(E), float(ko), float(dV),
+                                float(np.sum(np.abs(np.asarray(Eo)) ** 2)), C.byref(out)), op.ctx.h)
+    return out.value
+
+
+def cext_grad(op, prec, Einc, eps, ko, d, kvec, Eo, tol=1e-6, maxit=2000, precision="mixed"):
+    """(C_ext, dC/dRe(eps), dC/dIm(eps), P, info_fwd, info_adj) by the adjoint method."""
+    lib = op.ctx._lib
+    E = np.ascontiguousarray(np.asarray(Einc, dtype=np.complex128))
+    ep = np.ascontiguousarray(np.asarray(eps, dtype=np.complex128))
+    kv = np.ascontiguousarray(np.asarray(kvec, dtype=float))
+    e0 = np.ascontiguousarray(np.asarray(Eo, dtype=float))
+    o = _solve_opts(lib, tol, maxit, precision)
+    c = C.c_double()
+    gre = np.zeros(ep.size); gim = np.zeros(ep.size)
+    P = np.zeros(op.n3, dtype=np.complex128)
+    i1, i2 = L.vs_solve_info(), L.vs_solve_info()
+    L.check(lib.vs_cext_grad(op.h, prec.h if prec is not None else None, L.dptr(E), L.dptr(ep), float(ko), float(d),
+                             L.dptr(kv), L.dptr(e0), C.byref(o), C.byref(c), L.dptr(gre), L.dptr(gim), L.dptr(P),
+                             C.byref(i1), C.byref(i2)), op.ctx.h)
+    info = lambda i: dict(flag=i.flag, relres=i.relres, iter=i.iter, time_ms=i.time_ms)
+    return c.value, gre, gim, P, info(i1), info(i2)

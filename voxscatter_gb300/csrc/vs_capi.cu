@@ -99,6 +99,9 @@ void op_common(vs_op* op, const int64_t* idx3, int64_t n3, vs_diag Mr, vs_diag M
     p2g[e] = (int)g;
   }
   op->n3 = n3;
+  op->std3 = (n3 % 3 == 0);
+  for (int64_t e = 0; op->std3 && e < n3 / 3; ++e)
+    op->std3 = idx3[e] < V && idx3[e + n3 / 3] == idx3[e] + V && idx3[e + 2 * n3 / 3] == idx3[e] + 2 * V;
   op->map3.alloc(map3.size() * sizeof(int));
   op->pos2grid.alloc(p2g.size() * sizeof(int));
   VS_CUDA(cudaMemcpyAsync(op->map3.p, map3.data(), map3.size() * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -215,6 +218,41 @@ void time_passes(cudaStream_t st, int nrep, float* ms_out, F&& launch) {
   }
   for (auto& e : ev) cudaEventDestroy(e);
   for (int p = 0; p < 5; ++p) ms_out[p] = acc[p] / nrep;
+}
+
+void solve_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, const vs_solve_opts* o,
+                       vs_solve_info* info) {
+  VS_REQUIRE(o && info, "NULL argument");
+  VS_REQUIRE(o->method == VS_BICGSTAB, "unsupported method");
+  VS_REQUIRE(o->precision == VS_SOLVE_MIXED || o->precision == VS_SOLVE_FP64, "bad precision");
+  VS_REQUIRE(o->tol > 0 && o->maxit >= 0 && o->iters_per_graph >= 1 && o->iters_per_graph <= 64, "bad options");
+  VS_REQUIRE(!prec || (prec->L == op->L && prec->M == op->M && prec->N == op->N && prec->n3 == op->n3),
+             "preconditioner does not match the operator");
+  VS_REQUIRE(!prec || (o->precision == VS_SOLVE_MIXED ? prec->inv32.p != nullptr : prec->inv64.p != nullptr),
+             "preconditioner not built in the precision this solve needs");
+  vs::SolveParams prm;
+  prm.mode = o->precision;
+  prm.tol = o->tol;
+  prm.maxit = o->maxit;
+  prm.inner_tol = o->inner_tol;
+  prm.max_refine = o->max_refine;
+  prm.per_graph = o->iters_per_graph;
+  prm.resvec_cap = (int)std::min<int64_t>(o->resvec ? o->resvec_cap : 0, 1 << 30);
+  prm.resvec_host = o->resvec;
+  VS_REQUIRE(o->transpose == 0 || o->transpose == 1, "transpose must be 0 or 1");
+  prm.op_mode = o->transpose ? VS_TRANSP : VS_NOTRANSP;
+  if (prec) {
+    const int64_t need = (int64_t)prec->L * prec->M * prec->N * 3 * sizeof(double2);
+    if ((int64_t)prec->t.bytes < need) prec->t.alloc(need);
+  }
+  vs::SolveResult r;
+  vs::solve_bicgstab(*op, prec, b, x, prm, r, op->ctx->stream);
+  info->flag = r.flag;
+  info->relres = r.relres;
+  info->iter = r.iter;
+  info->refinements = r.refinements;
+  info->n_resvec = r.n_resvec;
+  info->kernel_launches = r.launches;
 }
 
 }  // namespace
@@ -686,40 +724,9 @@ void vs_solve_opts_default(vs_solve_opts* o) {
   o->iters_per_graph = 4;
   o->resvec = nullptr;
   o->resvec_cap = 0;
+  o->transpose = 0;
 }
 
-static void solve_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, const vs_solve_opts* o,
-                       vs_solve_info* info) {
-  VS_REQUIRE(o && info, "NULL argument");
-  VS_REQUIRE(o->method == VS_BICGSTAB, "unsupported method");
-  VS_REQUIRE(o->precision == VS_SOLVE_MIXED || o->precision == VS_SOLVE_FP64, "bad precision");
-  VS_REQUIRE(o->tol > 0 && o->maxit >= 0 && o->iters_per_graph >= 1 && o->iters_per_graph <= 64, "bad options");
-  VS_REQUIRE(!prec || (prec->L == op->L && prec->M == op->M && prec->N == op->N && prec->n3 == op->n3),
-             "preconditioner does not match the operator");
-  VS_REQUIRE(!prec || (o->precision == VS_SOLVE_MIXED ? prec->inv32.p != nullptr : prec->inv64.p != nullptr),
-             "preconditioner not built in the precision this solve needs");
-  vs::SolveParams prm;
-  prm.mode = o->precision;
-  prm.tol = o->tol;
-  prm.maxit = o->maxit;
-  prm.inner_tol = o->inner_tol;
-  prm.max_refine = o->max_refine;
-  prm.per_graph = o->iters_per_graph;
-  prm.resvec_cap = (int)std::min<int64_t>(o->resvec ? o->resvec_cap : 0, 1 << 30);
-  prm.resvec_host = o->resvec;
-  if (prec) {
-    const int64_t need = (int64_t)prec->L * prec->M * prec->N * 3 * sizeof(double2);
-    if ((int64_t)prec->t.bytes < need) prec->t.alloc(need);
-  }
-  vs::SolveResult r;
-  vs::solve_bicgstab(*op, prec, b, x, prm, r, op->ctx->stream);
-  info->flag = r.flag;
-  info->relres = r.relres;
-  info->iter = r.iter;
-  info->refinements = r.refinements;
-  info->n_resvec = r.n_resvec;
-  info->kernel_launches = r.launches;
-}
 
 int vs_solve_device(vs_op* op, vs_prec* prec, const void* b, void* x, const vs_solve_opts* opts, vs_solve_info* info) {
   if (!op) return VS_ERR_ARG;
@@ -787,6 +794,87 @@ int vs_prec_time_passes(vs_prec* prec, const void* x, void* y, int64_t nrhs, int
       time_passes(st, nrep, ms_out, [&](int p) {
         vs::prec_apply_pass<double>(*prec, (const double2*)x, (double2*)y, (int)nrhs, nullptr, st, p);
       });
+  });
+}
+
+// ---- excitation, extinction, gradient --------------------------------------
+
+int vs_plane_wave(vs_op* op, const double* x, const double* y, const double* z, const double kvec[3],
+                  const double* E0, double* b_out) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(x && y && z && kvec && E0 && b_out, "NULL argument");
+    cudaStream_t st = op->ctx->stream;
+    vs::DevBuf dx, dy, dz, db;
+    dx.alloc(op->L * sizeof(double)); dy.alloc(op->M * sizeof(double)); dz.alloc(op->N * sizeof(double));
+    db.alloc(op->n3 * sizeof(double2));
+    VS_CUDA(cudaMemcpyAsync(dx.p, x, op->L * sizeof(double), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemcpyAsync(dy.p, y, op->M * sizeof(double), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemcpyAsync(dz.p, z, op->N * sizeof(double), cudaMemcpyHostToDevice, st));
+    const double2 e[3] = {make_double2(E0[0], E0[1]), make_double2(E0[2], E0[3]), make_double2(E0[4], E0[5])};
+    vs::plane_wave_device(*op, dx.as<double>(), dy.as<double>(), dz.as<double>(), kvec, e, db.as<double2>(), st);
+    VS_CUDA(cudaMemcpyAsync(b_out, db.p, op->n3 * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+int vs_cext(vs_op* op, const double* P, const double* Einc, double ko, double dV, double e0norm2, double* cext) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(P && Einc && cext && e0norm2 > 0, "bad argument");
+    cudaStream_t st = op->ctx->stream;
+    vs::DevBuf dp, de;
+    dp.alloc(op->n3 * sizeof(double2));
+    de.alloc(op->n3 * sizeof(double2));
+    VS_CUDA(cudaMemcpyAsync(dp.p, P, op->n3 * sizeof(double2), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemcpyAsync(de.p, Einc, op->n3 * sizeof(double2), cudaMemcpyHostToDevice, st));
+    *cext = vs::cext_device(dp.as<double2>(), de.as<double2>(), op->n3, 4.0 * M_PI * ko * dV / e0norm2, st);
+  });
+}
+
+int vs_cext_grad(vs_op* op, vs_prec* prec, const double* Einc, const double* eps, double ko, double d,
+                 const double kvec[3], const double E0[3], const vs_solve_opts* opts, double* cext, double* grad_re,
+                 double* grad_im, double* P_out, vs_solve_info* info_fwd, vs_solve_info* info_adj) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(Einc && eps && kvec && E0 && opts && cext && grad_re && grad_im && info_fwd && info_adj,
+               "NULL argument");
+    VS_REQUIRE(op->std3, "the gradient needs idx3 in the reference's [idx; V+idx; 2V+idx] form");
+    cudaStream_t st = op->ctx->stream;
+    const int64_t n = op->n3, nvox = n / 3;
+    vs::DevBuf de, dc, dP, dl, deps, dgr, dgi;
+    de.alloc(n * sizeof(double2)); dc.alloc(n * sizeof(double2));
+    dP.alloc(n * sizeof(double2)); dl.alloc(n * sizeof(double2));
+    deps.alloc(nvox * sizeof(double2));
+    dgr.alloc(nvox * sizeof(double)); dgi.alloc(nvox * sizeof(double));
+    VS_CUDA(cudaMemcpyAsync(de.p, Einc, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemcpyAsync(deps.p, eps, nvox * sizeof(double2), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemsetAsync(dP.p, 0, n * sizeof(double2), st));
+    VS_CUDA(cudaMemsetAsync(dl.p, 0, n * sizeof(double2), st));
+    vs_solve_opts o = *opts;
+    o.transpose = 0;
+    const auto t0 = std::chrono::steady_clock::now();
+    solve_impl(op, prec, de.as<double2>(), dP.as<double2>(), &o, info_fwd);
+    const auto t1 = std::chrono::steady_clock::now();
+    info_fwd->time_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    vs::conj_device(de.as<double2>(), dc.as<double2>(), n, st);
+    o.transpose = 1;
+    solve_impl(op, prec, dc.as<double2>(), dl.as<double2>(), &o, info_adj);
+    info_adj->time_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
+    const double e2 = E0[0] * E0[0] + E0[1] * E0[1] + E0[2] * E0[2];
+    const double c = 4.0 * M_PI * ko * d * d * d / e2;
+    *cext = vs::cext_device(dP.as<double2>(), de.as<double2>(), n, c, st);
+    const double nk = std::sqrt(kvec[0] * kvec[0] + kvec[1] * kvec[1] + kvec[2] * kvec[2]);
+    const double ne = std::sqrt(e2);
+    double S = 0;
+    for (int j = 0; j < 3; ++j) S += (kvec[j] / nk * E0[j] / ne) * (kvec[j] / nk * E0[j] / ne);
+    const double bterm = (0.1648469 + -1.7700004 * S) * (ko * d) * (ko * d);
+    vs::cext_grad_device(dP.as<double2>(), dl.as<double2>(), deps.as<double2>(), nvox, c, bterm, dgr.as<double>(),
+                         dgi.as<double>(), st);
+    VS_CUDA(cudaMemcpyAsync(grad_re, dgr.p, nvox * sizeof(double), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaMemcpyAsync(grad_im, dgi.p, nvox * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (P_out) VS_CUDA(cudaMemcpyAsync(P_out, dP.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
   });
 }
 

@@ -95,6 +95,7 @@ struct vs_op {
   vs::DevBuf t1, t2;    // pipeline intermediates
   vs::DevBuf xin, yout; // device staging for host-buffer applies
   vs::KrylovWork kw;    // solver state for vs_solve on this operator
+  bool std3 = false;    // idx3 = [idx; V+idx; 2V+idx] (the reference's idx3 form)
 };
 
 // 2-level circulant preconditioner: inverse blocks per (x,y) frequency.
@@ -157,6 +158,14 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
                      cudaStream_t st, int pass);
 template <typename T>
 void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip, cudaStream_t st);
+
+// Physics (vs_physics.cu)
+void plane_wave_device(const vs_op& op, const double* x, const double* y, const double* z, const double kvec[3],
+                       const double2 E0[3], double2* b, cudaStream_t st);
+void conj_device(const double2* a, double2* b, int64_t n, cudaStream_t st);
+double cext_device(const double2* P, const double2* E, int64_t n, double scale, cudaStream_t st);
+void cext_grad_device(const double2* P, const double2* lam, const double2* eps, int64_t nvox, double c, double bterm,
+                      double* gre, double* gim, cudaStream_t st);
 
 // Elementwise helpers (vs_matvec.cu)
 void c128_to_c64(const double2* in, float2* out, int64_t n, cudaStream_t st);

@@ -381,7 +381,8 @@ static void upload_state(KState* d, const KState& h, cudaStream_t st) {
 
 // One BiCGSTAB iteration (two half steps) as a fixed launch sequence.
 template <typename T>
-static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KState* s, int64_t n, cudaStream_t st) {
+static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KState* s, int64_t n, int mode,
+                           cudaStream_t st) {
   using C = cplx_t<T>;
   C* r = w.r.as<C>();
   C* rt = w.rt.as<C>();
@@ -398,13 +399,13 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
   k_bicg_p<T><<<g, 256, 0, st>>>(p, r, v, n, s);
   if (pr) prec_apply<T>(*pr, p, ph, 1, skip, st);
   else k_copy<T><<<g, 256, 0, st>>>(ph, p, n);
-  matvec<T>(op, ph, v, 1, VS_NOTRANSP, skip, st);
+  matvec<T>(op, ph, v, 1, mode, skip, st);
   k_bicg_alpha<T><<<g, kRedThreads, 0, st>>>(rt, v, n, s);
   k_bicg_s<T><<<g, kRedThreads, 0, st>>>(sv, r, v, n, s);
   k_bicg_xhalf<T><<<g, kRedThreads, 0, st>>>(x, ph, n, s);
   if (pr) prec_apply<T>(*pr, sv, sh, 1, skip, st);
   else k_copy<T><<<g, 256, 0, st>>>(sh, sv, n);
-  matvec<T>(op, sh, t, 1, VS_NOTRANSP, skip, st);
+  matvec<T>(op, sh, t, 1, mode, skip, st);
   k_bicg_omega<T><<<g, kRedThreads, 0, st>>>(t, sv, n, s);
   k_bicg_xr<T><<<g, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, n, s);
   VS_LAUNCH_CHECK();
@@ -420,7 +421,7 @@ static int kernels_per_iteration(const vs_prec* pr) { return 7 + 10 + (pr ? 10 :
 template <typename T>
 static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t n, double bnorm, double tol,
                             int maxit, double res_scale, double* resvec_dev, int resvec_cap, int per_graph,
-                            cudaStream_t st, int64_t* launches, int stag_window) {
+                            cudaStream_t st, int64_t* launches, int stag_window, int mode) {
   using C = cplx_t<T>;
   KState h{};
   h.tol_abs = tol * bnorm;
@@ -460,7 +461,7 @@ static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, i
   std::vector<const void*> key = {w.r.p, w.rt.p, w.p.p, w.v_.p, w.s.p, w.t.p, w.ph.p, w.sh.p, w.x.p,
                                   w.state.p, w.partials.p, op.t1.p, op.t2.p,
                                   (const void*)(uintptr_t)(pr ? pr->id : 0), pr ? pr->t.p : nullptr,
-                                  (const void*)(uintptr_t)per_graph};
+                                  (const void*)(uintptr_t)per_graph, (const void*)(uintptr_t)mode};
   if (gc.exec == nullptr || gc.key != key) {
     gc.reset();
     // One launch sequence with skip set, outside capture: every kernel returns
@@ -469,12 +470,12 @@ static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, i
     KState idle = h;
     idle.skip = 1;
     upload_state(s, idle, st);
-    bicg_iteration<T>(op, pr, w, s, n, st);
+    bicg_iteration<T>(op, pr, w, s, n, mode, st);
     *launches += kernels_per_iteration(pr);
     cudaGraph_t graph = nullptr;
     VS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     try {
-      for (int k = 0; k < per_graph; ++k) bicg_iteration<T>(op, pr, w, s, n, st);
+      for (int k = 0; k < per_graph; ++k) bicg_iteration<T>(op, pr, w, s, n, mode, st);
     } catch (...) {
       cudaStreamEndCapture(st, &graph);
       if (graph) cudaGraphDestroy(graph);
@@ -513,11 +514,11 @@ static double norm64(KrylovWork& w, const double2* u, int64_t n, cudaStream_t st
 
 // r64 = b - A x64 (c128 pipeline); returns ||r64||.
 static double residual64(const vs_op& op, KrylovWork& w, const double2* b, const double2* x, double2* r, int64_t n,
-                         cudaStream_t st, int64_t* launches) {
+                         cudaStream_t st, int64_t* launches, int mode) {
   *launches += 6;
   KState* s = w.state.as<KState>();
   double2* y = w.y64.as<double2>();
-  matvec<double>(op, x, y, 1, VS_NOTRANSP, nullptr, st);
+  matvec<double>(op, x, y, 1, mode, nullptr, st);
   k_resid64<<<vec_grid(n), kRedThreads, 0, st>>>(b, y, r, n, s, w.scal.as<double>());
   VS_LAUNCH_CHECK();
   double h = 0;
@@ -561,11 +562,11 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
       VS_LAUNCH_CHECK();
       launches += 1;
     } else {
-      residual64(op, w, b, x, w.r.as<double2>(), n, st, &launches);
+      residual64(op, w, b, x, w.r.as<double2>(), n, st, &launches, prm.op_mode);
     }
     launches += 1;
     KState fs = bicgstab_core<double>(op, pr, w, n, bnorm, prm.tol, prm.maxit, 1.0 / bnorm, rv, cap, prm.per_graph, st,
-                                      &launches, 0);
+                                      &launches, 0, prm.op_mode);
     launches += 1;
     k_copy<double><<<vec_grid(n), 256, 0, st>>>(x, w.x.as<double2>(), n);
     VS_LAUNCH_CHECK();
@@ -573,7 +574,7 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
     out.iter = fs.iter2 * 0.5;
     out.inner_iters = fs.iter2 * 0.5;
     out.n_resvec = std::min<int64_t>(fs.nres, cap);
-    const double rn = residual64(op, w, b, x, w.r.as<double2>(), n, st, &launches);
+    const double rn = residual64(op, w, b, x, w.r.as<double2>(), n, st, &launches, prm.op_mode);
     out.relres = rn / bnorm;
     if (out.flag == 0 && out.relres > prm.tol) out.flag = 1;
   } else {
@@ -589,7 +590,7 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
       launches += 1;
       rn = bnorm;
     } else {
-      rn = residual64(op, w, b, x, r64, n, st, &launches);
+      rn = residual64(op, w, b, x, r64, n, st, &launches, prm.op_mode);
     }
     int inner_total2 = 0;
     int64_t nres = 0;
@@ -611,7 +612,7 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
       double* rvk = (rv && nres < cap) ? rv + nres : nullptr;
       const int capk = rv ? (int)(cap - nres) : 0;
       KState fs = bicgstab_core<float>(op, pr, w, n, 1.0, itol, prm.maxit - inner_total2 / 2, rn / bnorm, rvk, capk,
-                                       prm.per_graph, st, &launches, kStagnationWindow);
+                                       prm.per_graph, st, &launches, kStagnationWindow, prm.op_mode);
       launches += 2;
       inner_total2 += fs.iter2;
       nres += std::min<int64_t>(fs.nres, capk);
@@ -622,7 +623,7 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
       k_update64<<<vec_grid(n), 256, 0, st>>>(x, w.x.as<float2>(), n, rn);
       VS_LAUNCH_CHECK();
       launches += 1;
-      rn = residual64(op, w, b, x, r64, n, st, &launches);
+      rn = residual64(op, w, b, x, r64, n, st, &launches, prm.op_mode);
     }
     out.flag = (rn <= prm.tol * bnorm) ? 0 : (flag >= 4 ? flag : 1);
     out.relres = rn / bnorm;

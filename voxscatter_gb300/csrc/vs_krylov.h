@@ -28,6 +28,7 @@ struct SolveParams {
   int per_graph = 4;
   int resvec_cap = 0;
   double* resvec_host = nullptr;
+  int op_mode = 0;  // VS_NOTRANSP: solve A x = b; VS_TRANSP: solve A^T x = b
 };
 
 struct SolveResult {
