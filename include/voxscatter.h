@@ -185,7 +185,10 @@ int vs_prec_get_blocks(vs_prec* prec, int precision, double* out);
 
 /* ---- Krylov solve ---------------------------------------------------- */
 
-enum vs_solve_method { VS_BICGSTAB = 0 };
+/* VS_BICGSTAB: MATLAB bicgstab(A, b, tol, maxit, M1) (right preconditioned);
+ * VS_GMRES: MATLAB gmres(A, b, restart, tol, maxit, M1) (left preconditioned,
+ * restarted), here as the inner solver of the FP64 refinement loop. */
+enum vs_solve_method { VS_BICGSTAB = 0, VS_GMRES = 1 };
 enum vs_solve_precision {
   VS_SOLVE_MIXED = 0, /* c64 inner solve on the c64 pipeline inside FP64 iterative refinement */
   VS_SOLVE_FP64 = 1   /* the same Krylov method on the c128 pipeline throughout               */
@@ -202,6 +205,7 @@ typedef struct vs_solve_opts {
   double* resvec;      /* optional: relative residual norms at every half step               */
   int64_t resvec_cap;  /* capacity of resvec                                                 */
   int transpose;       /* 0: solve A x = b; 1: solve A^T x = b (plain transpose, adjoints)   */
+  int restart;         /* VS_GMRES: restart length (Krylov basis size)                        */
 } vs_solve_opts;
 
 typedef struct vs_solve_info {
@@ -215,7 +219,8 @@ typedef struct vs_solve_info {
 } vs_solve_info;
 
 /* Fill opts with defaults: BiCGSTAB, MIXED, tol 1e-6, maxit 2000, automatic
- * inner tolerance, 10 refinements, 4 iterations per graph, no resvec. */
+ * inner tolerance, 10 refinements, 4 iterations per graph, no resvec, no
+ * transpose, GMRES restart 50. */
 void vs_solve_opts_default(vs_solve_opts* opts);
 
 /* Solve A x = b with the (optional, may be NULL) preconditioner, right

@@ -101,3 +101,51 @@ def test_config1_mixed_and_fp64_agree(api):
     for x in (xm, xf):
         assert np.linalg.norm(b - Aor(x)) / np.linalg.norm(b) <= 1e-6 * 1.01
     assert np.linalg.norm(xm - xf) / np.linalg.norm(xf) < 1e-4
+
+
+@pytest.mark.parametrize("precision,tol", [("mixed", 1e-6), ("fp64", 1e-10)])
+@pytest.mark.parametrize("use_prec", [False, True])
+@pytest.mark.parametrize("restart", [5, 60])
+def test_gmres_small(api, precision, tol, use_prec, restart):
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, Toep, alpha, dV, b, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV) if use_prec else None
+    x, flag, relres, it, resvec = api.gmres(op, b, restart, tol, 400, pr, precision=precision)
+    assert flag == 0, (flag, relres, it)
+    assert np.linalg.norm(b - Aor(x)) / np.linalg.norm(b) <= tol * 1.01
+    Ad = O.dense_dda_matrix(p["r"], p["idx"], p["ko"], 1 / alpha, dV)
+    xd = np.linalg.solve(Ad, b)
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 100 * tol
+    assert len(resvec) >= 2
+
+
+def test_gmres_matches_oracle_gmres_steps(api):
+    """FP64 device GMRES(restart large) needs the same number of Arnoldi steps
+    as the oracle's left-preconditioned GMRES to reach a preconditioned
+    residual below tol (both follow the same Krylov space)."""
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, Toep, alpha, dV, b, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
+    _, circL = O.circ_1_level(Toep, L, M, N, 0, "off")
+    _, blk = O.circ_2_level(circL, L, M, N)
+    inv = O.invert_blocks(blk, 1 / alpha, dV)
+    Pm = lambda v: O.mvp_circ_2_level(inv, v, L, M, N, idx3)
+    xo, fo, ro, ito, rvo = O.gmres(Aor, b, 200, 1e-9, 1, Pm)
+    x, info, rv = api.solve(op, b, pr, tol=1e-30, maxit=ito[1], precision="fp64", method="gmres", restart=200,
+                            inner_tol=1e-9, max_refine=1)
+    assert fo == 0
+    assert info["iter"] == ito[1]
+    n = min(len(rv), len(rvo))
+    assert np.allclose(rv[:n] / rv[0], rvo[:n] / rvo[0], rtol=1e-6, atol=1e-12)
+
+
+def test_config1_gmres_mixed(api):
+    p = W.config1()
+    L, M, N, idx3, Toep, alpha, dV, b, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
+    x, info, rv = api.solve(op, b, pr, tol=1e-6, precision="mixed", method="gmres", restart=50)
+    assert info["flag"] == 0
+    assert np.linalg.norm(b - Aor(x)) / np.linalg.norm(b) <= 1e-6 * 1.01

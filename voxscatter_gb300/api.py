@@ -312,7 +312,7 @@ def mvp_circ_2_level(inv_blocks, JIn, Lx, My, Nz, idx, precision="c128", ctx=Non
 
 
 def solve(op, b, prec=None, tol=1e-6, maxit=2000, precision="mixed", x0=None, inner_tol=0.0, max_refine=10,
-          iters_per_graph=4, want_resvec=True, transpose=False):
+          iters_per_graph=4, want_resvec=True, transpose=False, method="bicgstab", restart=50):
     """Device Krylov solve; returns (x, info dict, resvec)."""
     lib = op.ctx._lib
     b = np.ascontiguousarray(np.asarray(b, dtype=np.complex128).ravel())
@@ -323,6 +323,8 @@ def solve(op, b, prec=None, tol=1e-6, maxit=2000, precision="mixed", x0=None, in
     o.tol = float(tol); o.maxit = int(maxit); o.inner_tol = float(inner_tol); o.max_refine = int(max_refine)
     o.iters_per_graph = int(iters_per_graph)
     o.transpose = 1 if transpose else 0
+    o.method = L.VS_GMRES if method == "gmres" else L.VS_BICGSTAB
+    o.restart = int(restart)
     rv = np.zeros(4 * int(maxit) + 64 if want_resvec else 1)
     if want_resvec:
         o.resvec = L.dptr(rv); o.resvec_cap = rv.size
@@ -362,6 +364,27 @@ def solve_host_ptr(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision=
                          C.cast(C.c_void_p(x_ptr), L._pd), C.byref(o), C.byref(info)), op.ctx.h)
     return dict(flag=info.flag, relres=info.relres, iter=info.iter, refinements=info.refinements,
                 time_ms=info.time_ms, launches=info.kernel_launches)
+
+
+def gmres(A, b, restart=None, tol=1e-6, maxit=None, M1=None, M2=None, x0=None, precision="mixed"):
+    """[x, flag, relres, iter, resvec] = gmres(A, b, restart, tol, maxit, M1, M2, x0)
+    with A an Operator and M1 a Preconditioner.  Left preconditioned and
+    restarted like MATLAB's gmres; iter = [outer, inner]; resvec holds the
+    preconditioned residual norms relative to ||M^-1 b|| scaled to ||b||.
+    relres is the true FP64 relative residual."""
+    if M2 is not None:
+        raise NotImplementedError("a second preconditioner factor is not supported")
+    n = A.n3
+    restart = n if restart is None else min(int(restart), n)
+    maxit = min(int(np.ceil(n / restart)), 10) if maxit is None else int(maxit)
+    total = min(restart * maxit, 1 << 30)
+    x, info, rv = solve(A, b, prec=M1, tol=tol, maxit=total, precision=precision, x0=x0, method="gmres",
+                        restart=min(restart, 2048))
+    steps = int(info["iter"])
+    outer = max(1, -(-steps // restart))
+    inner = steps - (outer - 1) * restart
+    nb = np.linalg.norm(np.asarray(b))
+    return x, info["flag"], info["relres"], [outer, inner], rv * nb
 
 
 def bicgstab(A, b, tol=1e-6, maxit=20, M1=None, M2=None, x0=None, precision="mixed"):

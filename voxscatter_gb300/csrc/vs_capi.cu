@@ -223,7 +223,8 @@ void time_passes(cudaStream_t st, int nrep, float* ms_out, F&& launch) {
 void solve_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, const vs_solve_opts* o,
                        vs_solve_info* info) {
   VS_REQUIRE(o && info, "NULL argument");
-  VS_REQUIRE(o->method == VS_BICGSTAB, "unsupported method");
+  VS_REQUIRE(o->method == VS_BICGSTAB || o->method == VS_GMRES, "unsupported method");
+  VS_REQUIRE(o->method != VS_GMRES || (o->restart >= 1 && o->restart <= 2048), "GMRES restart must be in [1, 2048]");
   VS_REQUIRE(o->precision == VS_SOLVE_MIXED || o->precision == VS_SOLVE_FP64, "bad precision");
   VS_REQUIRE(o->tol > 0 && o->maxit >= 0 && o->iters_per_graph >= 1 && o->iters_per_graph <= 64, "bad options");
   VS_REQUIRE(!prec || (prec->L == op->L && prec->M == op->M && prec->N == op->N && prec->n3 == op->n3),
@@ -245,8 +246,10 @@ void solve_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, const vs
     const int64_t need = (int64_t)prec->L * prec->M * prec->N * 3 * sizeof(double2);
     if ((int64_t)prec->t.bytes < need) prec->t.alloc(need);
   }
+  prm.restart = o->restart;
   vs::SolveResult r;
-  vs::solve_bicgstab(*op, prec, b, x, prm, r, op->ctx->stream);
+  if (o->method == VS_GMRES) vs::solve_gmres(*op, prec, b, x, prm, r, op->ctx->stream);
+  else vs::solve_bicgstab(*op, prec, b, x, prm, r, op->ctx->stream);
   info->flag = r.flag;
   info->relres = r.relres;
   info->iter = r.iter;
@@ -725,6 +728,7 @@ void vs_solve_opts_default(vs_solve_opts* o) {
   o->resvec = nullptr;
   o->resvec_cap = 0;
   o->transpose = 0;
+  o->restart = 50;
 }
 
 

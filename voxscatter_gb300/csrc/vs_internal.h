@@ -59,6 +59,10 @@ struct KrylovWork {
   DevBuf r64, y64;                       // FP64 residual / matvec output
   DevBuf partials, state, scal, resvec;
   GraphCache graph32, graph64;           // BiCGSTAB iteration graphs (c64 / c128)
+  // GMRES(m): Krylov basis, Hessenberg (column-major, m+1 rows), rotations,
+  // right-hand side g, solution y, pass coefficients, partial dots, state,
+  // and the vectors w, tmp and the correction d.
+  DevBuf gV, gH, gcs, gsn, gg, gy, ghp, gpart, gstate, gw, gtmp, gd;
   template <typename T> void ensure(int64_t n);
 };
 

@@ -639,3 +639,455 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
 }
 
 }  // namespace vs
+
+// ===========================================================================
+// GMRES(m), left preconditioned as MATLAB's gmres(A, b, restart, tol, maxit, M1)
+// (main_DDA.m:89,128-129; Saad & Schultz 1986): Arnoldi with classical
+// Gram-Schmidt and one reorthogonalisation pass (two batched dot/axpy passes
+// per step), Givens rotations and the small triangular solve on the device.
+// Convergence is tested on the preconditioned residual estimate |g_{k+1}|
+// relative to ||M^-1 r0||.  It runs as the inner solver of the FP64 refinement
+// loop below (c64 or c128 pipeline), so the reported relres is always the
+// true FP64 residual.
+// ===========================================================================
+namespace vs {
+
+constexpr int kDotChunk = 4096;  // elements per CTA of the batched dots
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_gm_dots(const cplx_t<T>* __restrict__ V, const cplx_t<T>* __restrict__ w,
+                                                 int64_t n, double2* __restrict__ part, int nchunk,
+                                                 const GState* st) {
+  if (st->skip) return;
+  const int j = blockIdx.y;
+  const cplx_t<T>* v = V + (int64_t)j * n;
+  const int64_t i0 = (int64_t)blockIdx.x * kDotChunk;
+  const int64_t i1 = (n < i0 + kDotChunk) ? n : i0 + kDotChunk;
+  Acc<T> a;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) a.dot(v[i], w[i]);
+  __shared__ double sre[8], sim[8];
+  double re = a.value().x, im = a.value().y;
+  for (int off = 16; off; off >>= 1) {
+    re += __shfl_xor_sync(0xffffffffu, re, off);
+    im += __shfl_xor_sync(0xffffffffu, im, off);
+  }
+  if ((threadIdx.x & 31) == 0) { sre[threadIdx.x >> 5] = re; sim[threadIdx.x >> 5] = im; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0, q = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { r += sre[k]; q += sim[k]; }
+    part[(int64_t)j * nchunk + blockIdx.x] = make_double2(r, q);
+  }
+}
+
+// hp[j] = sum of the partials of vector j; H(:,k) += hp (column k of the Hessenberg)
+__global__ void k_gm_dots_final(const double2* __restrict__ part, int nchunk, double2* __restrict__ hp,
+                                double2* __restrict__ Hcol, GState* st) {
+  if (st->skip) return;
+  const int j = blockIdx.x;
+  double r = 0, q = 0;
+  for (int c = threadIdx.x; c < nchunk; c += blockDim.x) { r += part[(int64_t)j * nchunk + c].x; q += part[(int64_t)j * nchunk + c].y; }
+  for (int off = 16; off; off >>= 1) {
+    r += __shfl_xor_sync(0xffffffffu, r, off);
+    q += __shfl_xor_sync(0xffffffffu, q, off);
+  }
+  __shared__ double sr[8], sq[8];
+  if ((threadIdx.x & 31) == 0) { sr[threadIdx.x >> 5] = r; sq[threadIdx.x >> 5] = q; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0, b = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { a += sr[k]; b += sq[k]; }
+    hp[j] = make_double2(a, b);
+    Hcol[j].x += a;
+    Hcol[j].y += b;
+  }
+}
+
+// w -= sum_j hp[j] V_j
+template <typename T>
+__global__ void k_gm_axpy(const cplx_t<T>* __restrict__ V, cplx_t<T>* __restrict__ w, int64_t n, int kk,
+                          const double2* __restrict__ hp, const GState* st) {
+  using C = cplx_t<T>;
+  if (st->skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* h = reinterpret_cast<C*>(smem_raw);
+  for (int j = threadIdx.x; j < kk; j += blockDim.x) h[j] = ccast<C>(hp[j]);
+  __syncthreads();
+  GRID_LOOP(i, n) {
+    C acc = w[i];
+    for (int j = 0; j < kk; ++j) {
+      const C v = V[(int64_t)j * n + i];
+      acc = csub(acc, cmul(h[j], v));
+    }
+    w[i] = acc;
+  }
+}
+
+// H(k+1,k) = ||w|| (grid reduction; the last CTA writes it)
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_gm_norm(const cplx_t<T>* w, int64_t n, double* partials,
+                                                         unsigned* counter, double2* Hk1, const GState* st) {
+  if (st->skip) return;
+  Acc<T> a;
+  GRID_LOOP(i, n) a.norm2(w[i]);
+  double v[1] = {a.value().x}, t[1];
+  if (grid_reduce<1>(v, partials, counter, t) && threadIdx.x == 0) *Hk1 = make_double2(sqrt(t[0]), 0.0);
+}
+
+// V_{k+1} = w / H(k+1,k)
+template <typename T>
+__global__ void k_gm_scale(const cplx_t<T>* __restrict__ w, cplx_t<T>* __restrict__ vnext, int64_t n,
+                           const double2* Hk1, const GState* st) {
+  if (st->skip) return;
+  const double h = Hk1->x;
+  const T s = (T)(h > 0 ? 1.0 / h : 0.0);
+  GRID_LOOP(i, n) vnext[i] = cscale(w[i], s);
+}
+
+// Apply the previous rotations to column k, form rotation k, update g and the
+// residual estimate (one thread).
+__global__ void k_gm_givens(GState* st, double2* H, double* cs, double2* sn, double2* g) {
+  if (st->skip || threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int k = st->k, m1 = st->m + 1;
+  double2* h = H + (int64_t)k * m1;
+  for (int j = 0; j < k; ++j) {
+    const double2 a = h[j], b = h[j + 1];
+    // [c s; -conj(s) c] [a; b]
+    const double2 t = cadd(cscale(a, cs[j]), cmul(sn[j], b));
+    const double2 u = csub(cscale(b, cs[j]), cmul(cconj(sn[j]), a));
+    h[j] = t;
+    h[j + 1] = u;
+  }
+  const double2 a = h[k], b = h[k + 1];
+  const double na = sqrt(a.x * a.x + a.y * a.y), nb = sqrt(b.x * b.x + b.y * b.y);
+  const double den = sqrt(na * na + nb * nb);
+  double c;
+  double2 s;
+  if (na == 0.0) {
+    c = 0.0;
+    s = make_double2(1.0, 0.0);
+  } else {
+    c = na / den;
+    s = cscale(cmul(make_double2(a.x / na, a.y / na), cconj(b)), 1.0 / den);
+  }
+  cs[k] = c;
+  sn[k] = s;
+  h[k] = cadd(cscale(a, c), cmul(s, b));
+  h[k + 1] = make_double2(0, 0);
+  const double2 gk = g[k];
+  g[k + 1] = cscale(cmul(cconj(s), gk), -1.0);
+  g[k] = cscale(gk, c);
+  const double res = sqrt(g[k + 1].x * g[k + 1].x + g[k + 1].y * g[k + 1].y);
+  st->res = res;
+  st->k = k + 1;
+  if (st->nres < st->resvec_cap) st->resvec[st->nres] = res * st->res_scale;
+  st->nres += 1;
+  if (!isfinite(res)) {
+    st->flag = 5;
+    st->skip = 1;
+  } else if (res <= st->tol_abs) {
+    st->flag = 0;
+    st->skip = 1;
+  } else if (st->k >= st->m) {
+    st->skip = 1;  // cycle complete; the host restarts
+  }
+}
+
+// Back substitution H(0:k,0:k) y = g(0:k) (upper triangular after the rotations).
+__global__ void k_gm_solve(const GState* st, const double2* H, const double2* g, double2* y) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int k = st->k, m1 = st->m + 1;
+  for (int i = k - 1; i >= 0; --i) {
+    double2 acc = g[i];
+    for (int j = i + 1; j < k; ++j) acc = csub(acc, cmul(H[(int64_t)j * m1 + i], y[j]));
+    const double2 d = H[(int64_t)i * m1 + i];
+    const double dd = d.x * d.x + d.y * d.y;
+    y[i] = dd > 0 ? make_double2((acc.x * d.x + acc.y * d.y) / dd, (acc.y * d.x - acc.x * d.y) / dd)
+                  : make_double2(0, 0);
+  }
+}
+
+// d += sum_j y[j] V_j
+template <typename T>
+__global__ void k_gm_xupdate(cplx_t<T>* __restrict__ d, const cplx_t<T>* __restrict__ V, int64_t n, int k,
+                             const double2* __restrict__ y) {
+  using C = cplx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* ys = reinterpret_cast<C*>(smem_raw);
+  for (int j = threadIdx.x; j < k; j += blockDim.x) ys[j] = ccast<C>(y[j]);
+  __syncthreads();
+  GRID_LOOP(i, n) {
+    C acc = d[i];
+    for (int j = 0; j < k; ++j) acc = cfma(ys[j], V[(int64_t)j * n + i], acc);
+    d[i] = acc;
+  }
+}
+
+// r - A d  (T precision), into out
+template <typename T>
+__global__ void k_sub(const cplx_t<T>* __restrict__ a, const cplx_t<T>* __restrict__ b, cplx_t<T>* __restrict__ o,
+                      int64_t n) {
+  GRID_LOOP(i, n) o[i] = csub(a[i], b[i]);
+}
+
+template <typename T>
+__global__ void k_scale_by(const cplx_t<T>* __restrict__ a, cplx_t<T>* __restrict__ o, int64_t n, const double* nrm) {
+  const double h = *nrm;
+  const T s = (T)(h > 0 ? 1.0 / h : 0.0);
+  GRID_LOOP(i, n) o[i] = cscale(a[i], s);
+}
+
+__global__ void k_r64_to(const double2* r, float2* o, int64_t n, double sc) {
+  GRID_LOOP(i, n) o[i] = make_float2((float)(r[i].x * sc), (float)(r[i].y * sc));
+}
+__global__ void k_r64_to(const double2* r, double2* o, int64_t n, double sc) {
+  GRID_LOOP(i, n) o[i] = make_double2(r[i].x * sc, r[i].y * sc);
+}
+__global__ void k_update64_from(double2* x, const float2* d, int64_t n, double sc) {
+  GRID_LOOP(i, n) {
+    x[i].x = fma(sc, (double)d[i].x, x[i].x);
+    x[i].y = fma(sc, (double)d[i].y, x[i].y);
+  }
+}
+__global__ void k_update64_from(double2* x, const double2* d, int64_t n, double sc) {
+  GRID_LOOP(i, n) {
+    x[i].x = fma(sc, d[i].x, x[i].x);
+    x[i].y = fma(sc, d[i].y, x[i].y);
+  }
+}
+
+// Inner GMRES on A d = rin (rin, d in precision T; d starts at 0).  Returns
+// the number of Arnoldi steps and sets *flag (0 converged, 1 not).
+template <typename T>
+static int gmres_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t n, const cplx_t<T>* rin,
+                      cplx_t<T>* d, double itol, int m, int maxit, int op_mode, double res_scale, double* resvec_dev,
+                      int resvec_cap, int64_t* nres_out, int* flag, cudaStream_t st, int64_t* launches) {
+  using C = cplx_t<T>;
+  const int g = vec_grid(n);
+  const int nchunk = ceil_div(n, kDotChunk);
+  C* V = w.gV.as<C>();
+  C* wv = w.gw.as<C>();
+  C* tmp = w.gtmp.as<C>();
+  double2* H = w.gH.as<double2>();
+  double2* hp = w.ghp.as<double2>();
+  double2* part = w.gpart.as<double2>();
+  GState* gs = w.gstate.as<GState>();
+  KState* ks = w.state.as<KState>();
+  auto minv = [&](const C* in, C* out) {
+    if (pr) prec_apply<T>(*pr, in, out, 1, &gs->skip, st);
+    else k_copy<T><<<g, 256, 0, st>>>(out, in, n);
+    *launches += pr ? 5 : 1;
+  };
+  VS_CUDA(cudaMemsetAsync(d, 0, n * sizeof(C), st));
+  GState h{};
+  h.m = m;
+  h.resvec = resvec_dev;
+  h.resvec_cap = resvec_cap;
+  h.res_scale = res_scale;
+  int steps = 0;
+  *flag = 1;
+  double beta0 = -1;
+  int64_t nres = 0;
+  for (int cycle = 0; steps < maxit; ++cycle) {
+    // z = M^-1 (rin - A d) into V_0 (un-normalised), beta = ||z||
+    h.skip = 0;
+    VS_CUDA(cudaMemcpyAsync(gs, &h, sizeof(GState), cudaMemcpyHostToDevice, st));
+    if (cycle == 0) {
+      minv(rin, V);
+    } else {
+      matvec<T>(op, d, tmp, 1, op_mode, nullptr, st);
+      k_sub<T><<<g, 256, 0, st>>>(rin, tmp, tmp, n);
+      minv(tmp, V);
+      *launches += 6;
+    }
+    k_norm<T><<<g, kRedThreads, 0, st>>>(V, n, ks, w.scal.as<double>());
+    double beta = 0;
+    VS_CUDA(cudaMemcpyAsync(&beta, w.scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+    *launches += 1;
+    if (beta0 < 0) {
+      beta0 = beta;
+      h.tol_abs = itol * beta0;
+      if (resvec_dev && resvec_cap > 0) {
+        const double v0 = beta * res_scale;
+        VS_CUDA(cudaMemcpyAsync(resvec_dev, &v0, sizeof(double), cudaMemcpyHostToDevice, st));
+      }
+      nres = 1;
+    }
+    if (!(beta > h.tol_abs)) {
+      *flag = 0;
+      break;
+    }
+    k_scale_by<T><<<g, 256, 0, st>>>(V, V, n, w.scal.as<double>());
+    // fresh Hessenberg and g = [beta, 0, ...]
+    VS_CUDA(cudaMemsetAsync(H, 0, (size_t)(m + 1) * m * sizeof(double2), st));
+    VS_CUDA(cudaMemsetAsync(w.gg.p, 0, (m + 1) * sizeof(double2), st));
+    const double2 g0 = make_double2(beta, 0);
+    VS_CUDA(cudaMemcpyAsync(w.gg.p, &g0, sizeof(double2), cudaMemcpyHostToDevice, st));
+    h.k = 0;
+    h.skip = 0;
+    h.flag = 1;
+    h.res = beta;
+    h.nres = (int)nres;
+    VS_CUDA(cudaMemcpyAsync(gs, &h, sizeof(GState), cudaMemcpyHostToDevice, st));
+    *launches += 1;
+    const int kmax = std::min(m, maxit - steps);
+    GState cur{};
+    int issued = 0;
+    for (int k = 0; k < kmax; ++k) {
+      const C* vk = V + (int64_t)k * n;
+      matvec<T>(op, vk, tmp, 1, op_mode, &gs->skip, st);
+      minv(tmp, wv);
+      double2* Hcol = H + (int64_t)k * (m + 1);
+      for (int pass = 0; pass < 2; ++pass) {
+        k_gm_dots<T><<<dim3(nchunk, k + 1), 256, 0, st>>>(V, wv, n, part, nchunk, gs);
+        k_gm_dots_final<<<k + 1, 256, 0, st>>>(part, nchunk, hp, Hcol, gs);
+        k_gm_axpy<T><<<g, 256, (k + 1) * sizeof(C), st>>>(V, wv, n, k + 1, hp, gs);
+      }
+      // partial sums and counter of the shared reduction state (device addresses)
+      k_gm_norm<T><<<g, kRedThreads, 0, st>>>(wv, n, w.partials.as<double>(), &ks->counter, Hcol + k + 1, gs);
+      k_gm_scale<T><<<g, 256, 0, st>>>(wv, V + (int64_t)(k + 1) * n, n, Hcol + k + 1, gs);
+      k_gm_givens<<<1, 32, 0, st>>>(gs, H, w.gcs.as<double>(), w.gsn.as<double2>(), w.gg.as<double2>());
+      VS_LAUNCH_CHECK();
+      *launches += 5 + 9;
+      ++issued;
+      if (issued % 4 == 0 || k == kmax - 1) {
+        VS_CUDA(cudaMemcpyAsync(&cur, gs, sizeof(GState), cudaMemcpyDeviceToHost, st));
+        VS_CUDA(cudaStreamSynchronize(st));
+        if (cur.skip) break;
+      }
+    }
+    VS_CUDA(cudaMemcpyAsync(&cur, gs, sizeof(GState), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+    const int kd = cur.k;
+    steps += kd;
+    nres = cur.nres;
+    if (kd > 0) {
+      k_gm_solve<<<1, 32, 0, st>>>(gs, H, w.gg.as<double2>(), w.gy.as<double2>());
+      k_gm_xupdate<T><<<g, 256, kd * sizeof(C), st>>>(d, V, n, kd, w.gy.as<double2>());
+      VS_LAUNCH_CHECK();
+      *launches += 2;
+    }
+    if (cur.flag == 0) {
+      *flag = 0;
+      break;
+    }
+    if (cur.flag == 5 || kd == 0) {
+      *flag = cur.flag == 5 ? 5 : 4;
+      break;
+    }
+  }
+  *nres_out = std::min<int64_t>(nres, resvec_cap);
+  return steps;
+}
+
+template <typename T>
+static void gmres_buffers(KrylovWork& w, int64_t n, int m) {
+  using C = cplx_t<T>;
+  w.gV.alloc((size_t)(m + 1) * n * sizeof(C));
+  w.gw.alloc(n * sizeof(C));
+  w.gtmp.alloc(n * sizeof(C));
+  w.gd.alloc(n * sizeof(C));
+  w.r.alloc(n * sizeof(C));
+  w.gH.alloc((size_t)(m + 1) * m * sizeof(double2));
+  w.gcs.alloc(m * sizeof(double));
+  w.gsn.alloc(m * sizeof(double2));
+  w.gg.alloc((m + 1) * sizeof(double2));
+  w.gy.alloc(m * sizeof(double2));
+  w.ghp.alloc((m + 1) * sizeof(double2));
+  w.gpart.alloc((size_t)(m + 1) * ceil_div(n, kDotChunk) * sizeof(double2));
+  w.gstate.alloc(sizeof(GState));
+}
+
+template <typename T>
+static void gmres_refine(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm,
+                         SolveResult& out, cudaStream_t st, double bnorm, int64_t& launches, double* rv, int cap) {
+  using C = cplx_t<T>;
+  KrylovWork& w = op.kw;
+  const int64_t n = op.n3;
+  const int m = std::max(1, std::min(prm.restart, prm.maxit));
+  gmres_buffers<T>(w, n, m);
+  w.y64.alloc(n * sizeof(double2));
+  w.r64.alloc(n * sizeof(double2));
+  double2* r64 = w.r64.as<double2>();
+  double rn;
+  if (norm64(w, x, n, st, &launches) == 0.0) {
+    k_copy<double><<<vec_grid(n), 256, 0, st>>>(r64, b, n);
+    VS_LAUNCH_CHECK();
+    launches += 1;
+    rn = bnorm;
+  } else {
+    rn = residual64(op, w, b, x, r64, n, st, &launches, prm.op_mode);
+  }
+  const bool fp64 = std::is_same<T, double>::value;
+  int steps = 0, flag = 1, refine = 0;
+  int64_t nres = 0;
+  for (; refine <= prm.max_refine; ++refine) {
+    if (rn <= prm.tol * bnorm) {
+      flag = 0;
+      break;
+    }
+    if (refine == prm.max_refine || steps >= prm.maxit) break;
+    double itol = prm.inner_tol > 0 ? prm.inner_tol
+                                    : std::max((fp64 ? 0.5 : 0.3) * prm.tol * bnorm / rn, fp64 ? 1e-15 : prm.inner_floor);
+    itol = std::min(itol, 0.5);
+    k_r64_to<<<vec_grid(n), 256, 0, st>>>(r64, w.r.as<C>(), n, 1.0 / rn);
+    VS_LAUNCH_CHECK();
+    launches += 1;
+    double* rvk = (rv && nres < cap) ? rv + nres : nullptr;
+    const int capk = rv ? (int)(cap - nres) : 0;
+    int64_t nk = 0;
+    int f = 1;
+    steps += gmres_core<T>(op, pr, w, n, w.r.as<C>(), w.gd.as<C>(), itol, m, prm.maxit - steps, prm.op_mode,
+                           rn / bnorm, rvk, capk, &nk, &f, st, &launches);
+    nres += nk;
+    k_update64_from<<<vec_grid(n), 256, 0, st>>>(x, w.gd.as<C>(), n, rn);
+    VS_LAUNCH_CHECK();
+    launches += 1;
+    rn = residual64(op, w, b, x, r64, n, st, &launches, prm.op_mode);
+    if (f == 5) {
+      flag = 5;
+      break;
+    }
+  }
+  out.flag = (rn <= prm.tol * bnorm) ? 0 : (flag >= 4 ? flag : 1);
+  out.relres = rn / bnorm;
+  out.iter = steps;
+  out.inner_iters = steps;
+  out.refinements = refine;
+  out.n_resvec = nres;
+}
+
+void solve_gmres(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
+                 cudaStream_t st) {
+  const int64_t n = op.n3;
+  KrylovWork& w = op.kw;
+  w.partials.alloc(kRedBlocks * 4 * sizeof(double));
+  w.state.alloc(sizeof(KState));
+  w.scal.alloc(4 * sizeof(double));
+  KState zero{};
+  zero.partials = w.partials.as<double>();
+  upload_state(w.state.as<KState>(), zero, st);
+  const int cap = prm.resvec_cap;
+  w.resvec.alloc(std::max(1, cap) * sizeof(double));
+  double* rv = cap > 0 ? w.resvec.as<double>() : nullptr;
+  ensure_scratch(op, 1, sizeof(double2));
+  int64_t launches = 0;
+  const double bnorm = norm64(w, b, n, st, &launches);
+  if (!std::isfinite(bnorm)) throw Error(VS_ERR_NONFINITE, "right-hand side has NaN or Inf entries");
+  out = SolveResult{};
+  if (bnorm == 0) {
+    VS_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double2), st));
+    VS_CUDA(cudaStreamSynchronize(st));
+    out.flag = 0;
+    return;
+  }
+  if (prm.mode == VS_SOLVE_FP64) gmres_refine<double>(op, pr, b, x, prm, out, st, bnorm, launches, rv, cap);
+  else gmres_refine<float>(op, pr, b, x, prm, out, st, bnorm, launches, rv, cap);
+  out.launches = launches;
+  if (cap > 0 && prm.resvec_host && out.n_resvec > 0)
+    VS_CUDA(cudaMemcpyAsync(prm.resvec_host, rv, out.n_resvec * sizeof(double), cudaMemcpyDeviceToHost, st));
+  VS_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace vs

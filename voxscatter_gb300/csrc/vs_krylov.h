@@ -18,6 +18,17 @@ struct KState {
   int stag_window;  // stop with flag 3 after this many iterations without a 1% improvement (0: off)
 };
 
+// Scalars of one GMRES cycle, resident in device memory.
+struct GState {
+  double tol_abs;    // stop when the preconditioned residual estimate |g_{k+1}| <= tol_abs
+  double res;        // current estimate
+  double res_scale;  // resvec entries are res * res_scale
+  double* resvec;
+  int k;             // Arnoldi steps done in this cycle
+  int m;             // restart length
+  int skip, flag, nres, resvec_cap;
+};
+
 struct SolveParams {
   int mode = 0;  // 0 mixed, 1 fp64
   double tol = 1e-6;
@@ -29,6 +40,7 @@ struct SolveParams {
   int resvec_cap = 0;
   double* resvec_host = nullptr;
   int op_mode = 0;  // VS_NOTRANSP: solve A x = b; VS_TRANSP: solve A^T x = b
+  int restart = 50; // GMRES restart length
 };
 
 struct SolveResult {
@@ -41,5 +53,7 @@ struct SolveResult {
 
 void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
                     cudaStream_t st);
+void solve_gmres(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
+                 cudaStream_t st);
 
 }  // namespace vs
