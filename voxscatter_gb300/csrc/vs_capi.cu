@@ -401,6 +401,8 @@ int vs_op_create(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* toe
                          op->ax, st);
     spectrum_from_full(op, full.as<double2>());
     vs::ensure_scratch(*op, 1, sizeof(float2));
+    vs::autotune_op<float>(*op, st);
+    vs::autotune_op<double>(*op, st);
     VS_CUDA(cudaStreamSynchronize(st));
     *out = op;
   });
@@ -434,6 +436,8 @@ int vs_op_create_fN(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* 
     vs::toep_from_fN_device(op->L, op->M, op->N, op->P, op->Q, op->R, full.as<double2>(), op->toep64.as<double2>(),
                             op->ax, st);
     vs::ensure_scratch(*op, 1, sizeof(float2));
+    vs::autotune_op<float>(*op, st);
+    vs::autotune_op<double>(*op, st);
     VS_CUDA(cudaStreamSynchronize(st));
     *out = op;
   });
@@ -594,6 +598,9 @@ int vs_prec_create(vs_op* op, const double* shift, const double* d, int64_t nd, 
     VS_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
     VS_REQUIRE(hs == 0, "a preconditioner block is singular or its inverse is not finite");
+    prec_scratch_impl(pr, 1);
+    vs::autotune_prec<float>(*pr, st);
+    vs::autotune_prec<double>(*pr, st);
     *out = pr;
   });
   if (s != VS_OK) delete pr;

@@ -41,6 +41,16 @@ struct FftAxis {
 template <> inline const float2* FftAxis::tw<float>() const { return tw32.as<float2>(); }
 template <> inline const double2* FftAxis::tw<double>() const { return tw64.as<double2>(); }
 
+// Launch shape of the FFT passes and of the block GEMV, chosen per operator /
+// preconditioner and precision by the autotuner (log2 values; -1 = default).
+struct PassShape {
+  int lg_lpb_x = -1;   // x passes: lines per CTA
+  int lg_tx_y = -1;    // y passes: x-tile width
+  int lg_tx_z = -1;    // z pass: x-tile width
+  int gemv_ti = 0;     // preconditioner GEMV: stored blocks per CTA (0 = default)
+  int gemv_threads = 0;
+};
+
 // Work vectors and device scalars of the Krylov solvers (vs_krylov.cu).
 // A captured iteration graph and the buffers/settings it was captured with.
 struct GraphCache {
@@ -99,6 +109,7 @@ struct vs_op {
   vs::DevBuf t1, t2;    // pipeline intermediates
   vs::DevBuf xin, yout; // device staging for host-buffer applies
   vs::KrylovWork kw;    // solver state for vs_solve on this operator
+  vs::PassShape shape[2];  // [0] c64, [1] c128 pipeline launch shapes
   bool std3 = false;    // idx3 = [idx; V+idx; 2V+idx] (the reference's idx3 form)
 };
 
@@ -115,6 +126,7 @@ struct vs_prec {
   vs::DevBuf t;             // apply scratch (L,M,N,3) per right-hand side
   vs::DevBuf xin, yout;
   int nrhs_cap = 0;
+  vs::PassShape shape[2];   // [0] c64, [1] c128 apply launch shapes
 };
 
 namespace vs {
@@ -170,6 +182,13 @@ void conj_device(const double2* a, double2* b, int64_t n, cudaStream_t st);
 double cext_device(const double2* P, const double2* E, int64_t n, double scale, cudaStream_t st);
 void cext_grad_device(const double2* P, const double2* lam, const double2* eps, int64_t nvox, double c, double bterm,
                       double* gre, double* gim, cudaStream_t st);
+
+// Autotuning of the launch shapes (vs_matvec.cu / vs_precond.cu): times a few
+// candidate shapes of every pass with CUDA events and keeps the fastest.
+template <typename T>
+void autotune_op(vs_op& op, cudaStream_t st);
+template <typename T>
+void autotune_prec(vs_prec& pr, cudaStream_t st);
 
 // Elementwise helpers (vs_matvec.cu)
 void c128_to_c64(const double2* in, float2* out, int64_t n, cudaStream_t st);

@@ -323,7 +323,8 @@ static StridedArgs<T> y_pass_args(const vs_op& op, const PipeArgs<T>& a, bool in
   s.xext = op.P;
   s.n_in = inverse ? op.Q : op.M;
   s.n_out = inverse ? op.M : op.Q;
-  s.lg_tx = ilog2(pick_tile(op.Q, sizeof(cplx_t<T>), 1));
+  const PassShape& sh = op.shape[std::is_same<T, float>::value ? 0 : 1];
+  s.lg_tx = sh.lg_tx_y >= 0 ? sh.lg_tx_y : ilog2(pick_tile(op.Q, sizeof(cplx_t<T>), 1));
   s.na = op.N * 3;
   s.s_row = op.P; s.d_row = op.P;
   s.s_a = inverse ? pq : pm; s.d_a = inverse ? pm : pq;
@@ -351,8 +352,9 @@ static PipeArgs<T> pipe_args(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, 
   a.G = std::is_same<T, float>::value ? (const C*)op.G32.p : (const C*)op.G64.p;
   a.twP = op.ax[0].tw<T>(); a.twQ = op.ax[1].tw<T>(); a.twR = op.ax[2].tw<T>();
   a.pP = op.ax[0].plan; a.pQ = op.ax[1].plan; a.pR = op.ax[2].plan;
-  a.lg_lpb = ilog2(pick_lpb(op.P, sizeof(C)));
-  a.lg_tx = ilog2(pick_tile(op.R, sizeof(C), 3));
+  const PassShape& sh = op.shape[std::is_same<T, float>::value ? 0 : 1];
+  a.lg_lpb = sh.lg_lpb_x >= 0 ? sh.lg_lpb_x : ilog2(pick_lpb(op.P, sizeof(C)));
+  a.lg_tx = sh.lg_tx_z >= 0 ? sh.lg_tx_z : ilog2(pick_tile(op.R, sizeof(C), 3));
   a.skip = skip;
   return a;
 }
@@ -506,6 +508,70 @@ template void fft_strided<double, false>(double2*, int, int, int64_t, int, int64
 template void fft_strided<double, true>(double2*, int, int, int64_t, int, int64_t, int, int64_t, const FftAxis&, cudaStream_t);
 template void fft_strided<float, false>(float2*, int, int, int64_t, int, int64_t, int, int64_t, const FftAxis&, cudaStream_t);
 template void fft_strided<float, true>(float2*, int, int, int64_t, int, int64_t, int, int64_t, const FftAxis&, cudaStream_t);
+
+// ---- autotuning of the pass shapes -------------------------------------
+// Times pass pairs (x forward+inverse, y forward+inverse, z) for each
+// candidate shape on scratch vectors and keeps the fastest; candidates whose
+// tiles exceed the shared-memory limit are skipped.
+template <typename F>
+static float time_ms(cudaStream_t st, int reps, F&& f) {
+  cudaEvent_t a, b;
+  VS_CUDA(cudaEventCreate(&a));
+  VS_CUDA(cudaEventCreate(&b));
+  f();  // warm-up (first-use attribute calls, caches)
+  VS_CUDA(cudaEventRecord(a, st));
+  for (int r = 0; r < reps; ++r) f();
+  VS_CUDA(cudaEventRecord(b, st));
+  VS_CUDA(cudaEventSynchronize(b));
+  float ms = 0;
+  VS_CUDA(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / reps;
+}
+
+template <typename T>
+void autotune_op(vs_op& op, cudaStream_t st) {
+  using C = cplx_t<T>;
+  const int pi = std::is_same<T, float>::value ? 0 : 1;
+  ensure_scratch(op, 1, sizeof(C));
+  DevBuf xb, yb;
+  xb.alloc(op.n3 * sizeof(C));
+  yb.alloc(op.n3 * sizeof(C));
+  VS_CUDA(cudaMemsetAsync(xb.p, 0, op.n3 * sizeof(C), st));
+  const C* x = xb.as<C>();
+  C* y = yb.as<C>();
+  const size_t cs = sizeof(C);
+  const size_t lim = 227 * 1024;
+  PassShape& sh = op.shape[pi];
+  const int reps = std::is_same<T, float>::value ? 3 : 1;
+  auto best_of = [&](int* field, int lo, int hi, auto fits, auto run) {
+    float best = 1e30f;
+    int arg = -1;
+    for (int v = lo; v <= hi; ++v) {
+      if (!fits(v)) continue;
+      *field = v;
+      const float t = time_ms(st, reps, run);
+      if (t < best) { best = t; arg = v; }
+    }
+    *field = arg;
+  };
+  best_of(&sh.lg_lpb_x, 0, 4, [&](int v) { return (2ull * (1 << v) * op.P + op.P) * cs <= lim && (1 << v) <= 256; },
+          [&] {
+            matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 0);
+            matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 4);
+          });
+  best_of(&sh.lg_tx_y, 1, 5, [&](int v) { return (2ull * op.Q * (1 << v) + op.Q) * cs <= lim; },
+          [&] {
+            matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 1);
+            matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 3);
+          });
+  best_of(&sh.lg_tx_z, 1, 5, [&](int v) { return (2ull * op.R * 3 * (1 << v) + op.R) * cs <= lim; },
+          [&] { matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 2); });
+  VS_CUDA(cudaStreamSynchronize(st));
+}
+template void autotune_op<float>(vs_op&, cudaStream_t);
+template void autotune_op<double>(vs_op&, cudaStream_t);
 
 // ---- precision conversions ----------------------------------------------
 __global__ void k_c128_to_c64(const double2* __restrict__ in, float2* __restrict__ out, int64_t n) {

@@ -388,7 +388,10 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
   a.t1 = t; a.t2 = t;
   a.twP = pr.axL.tw<T>();
   a.pP = pr.axL.plan;
-  {
+  const PassShape& sh = pr.shape[std::is_same<T, float>::value ? 0 : 1];
+  if (sh.lg_lpb_x >= 0) {
+    a.lg_lpb = sh.lg_lpb_x;
+  } else {
     int l = 8;
     while (l > 1 && 2ull * L * l * sizeof(C) > 48 * 1024) l >>= 1;
     int lg = 0;
@@ -399,7 +402,9 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
   StridedArgs<T> s{};
   s.src = t; s.dst = t;
   s.xext = L; s.n_in = M; s.n_out = M;
-  {
+  if (sh.lg_tx_y >= 0) {
+    s.lg_tx = sh.lg_tx_y;
+  } else {
     int tx = 16;
     while (tx > 1 && 2ull * M * tx * sizeof(C) > 48 * 1024) tx >>= 1;
     int lg = 0;
@@ -421,18 +426,19 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
       const int n = 3 * N;
       if (pr.sym) {
         const int Lb = L / 2 + 1, Mb = M / 2 + 1;
-        int ti = std::min(Lb, 4);
+        int ti = sh.gemv_ti > 0 ? std::min(sh.gemv_ti, Lb) : std::min(Lb, 4);
         while (ti > 1 && 2ull * ti * 4 * n * sizeof(C) > 64 * 1024) --ti;
+        const int nthr = sh.gemv_threads > 0 ? sh.gemv_threads : 256;
         const size_t smem = 2ull * ti * 4 * n * sizeof(C);
         const dim3 grid(ceil_div(Lb, ti), Mb, nrhs);
         if (std::is_same<T, float>::value && n % 2 == 0) {
           auto k = k_block_gemv_sym<T, true>;
           set_kernel_smem((const void*)k, smem);
-          k<<<grid, 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
+          k<<<grid, nthr, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
         } else {
           auto k = k_block_gemv_sym<T, false>;
           set_kernel_smem((const void*)k, smem);
-          k<<<grid, 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
+          k<<<grid, nthr, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
         }
         VS_LAUNCH_CHECK();
         break;
@@ -454,6 +460,79 @@ template <typename T>
 void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip, cudaStream_t st) {
   for (int pass = 0; pass < 5; ++pass) prec_apply_pass<T>(pr, x, y, nrhs, skip, st, pass);
 }
+template <typename F>
+static float time_ms_prec(cudaStream_t st, int reps, F&& f) {
+  cudaEvent_t a, b;
+  VS_CUDA(cudaEventCreate(&a));
+  VS_CUDA(cudaEventCreate(&b));
+  f();
+  VS_CUDA(cudaEventRecord(a, st));
+  for (int r = 0; r < reps; ++r) f();
+  VS_CUDA(cudaEventRecord(b, st));
+  VS_CUDA(cudaEventSynchronize(b));
+  float ms = 0;
+  VS_CUDA(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / reps;
+}
+
+// Autotune the preconditioner apply: lines per CTA of the x passes, x-tile of
+// the y passes, and (symmetric storage) blocks per CTA and CTA size of the GEMV.
+template <typename T>
+void autotune_prec(vs_prec& pr, cudaStream_t st) {
+  using C = cplx_t<T>;
+  const int pi = std::is_same<T, float>::value ? 0 : 1;
+  if ((pi == 0 && !pr.inv32.p) || (pi == 1 && !pr.inv64.p)) return;
+  DevBuf xb, yb;
+  xb.alloc(pr.n3 * sizeof(C));
+  yb.alloc(pr.n3 * sizeof(C));
+  VS_CUDA(cudaMemsetAsync(xb.p, 0, pr.n3 * sizeof(C), st));
+  const C* x = xb.as<C>();
+  C* y = yb.as<C>();
+  const size_t cs = sizeof(C), lim = 227 * 1024;
+  PassShape& sh = pr.shape[pi];
+  const int reps = std::is_same<T, float>::value ? 3 : 1;
+  auto best_of = [&](int* field, int lo, int hi, auto fits, auto run) {
+    float best = 1e30f;
+    int arg = -1;
+    for (int v = lo; v <= hi; ++v) {
+      if (!fits(v)) continue;
+      *field = v;
+      const float t = time_ms_prec(st, reps, run);
+      if (t < best) { best = t; arg = v; }
+    }
+    *field = arg;
+  };
+  best_of(&sh.lg_lpb_x, 0, 4, [&](int v) { return (2ull * (1 << v) * pr.L + pr.L) * cs <= lim; },
+          [&] {
+            prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 0);
+            prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 4);
+          });
+  best_of(&sh.lg_tx_y, 1, 5, [&](int v) { return (2ull * pr.M * (1 << v) + pr.M) * cs <= lim; },
+          [&] {
+            prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 1);
+            prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 3);
+          });
+  if (pr.sym) {
+    float best = 1e30f;
+    int bti = 0, bth = 0;
+    for (int ti : {1, 2, 4}) {
+      for (int th : {64, 128, 256}) {
+        sh.gemv_ti = ti;
+        sh.gemv_threads = th;
+        const float t = time_ms_prec(st, reps, [&] { prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 2); });
+        if (t < best) { best = t; bti = ti; bth = th; }
+      }
+    }
+    sh.gemv_ti = bti;
+    sh.gemv_threads = bth;
+  }
+  VS_CUDA(cudaStreamSynchronize(st));
+}
+template void autotune_prec<float>(vs_prec&, cudaStream_t);
+template void autotune_prec<double>(vs_prec&, cudaStream_t);
+
 template void prec_apply_pass<float>(const vs_prec&, const float2*, float2*, int, const int*, cudaStream_t, int);
 template void prec_apply_pass<double>(const vs_prec&, const double2*, double2*, int, const int*, cudaStream_t, int);
 template void prec_apply<float>(const vs_prec&, const float2*, float2*, int, const int*, cudaStream_t);
