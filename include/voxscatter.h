@@ -233,6 +233,18 @@ int vs_solve(vs_op* op, vs_prec* prec, const double* b, double* x, const vs_solv
 /* Same with b and x in device memory (double2, n3 each). */
 int vs_solve_device(vs_op* op, vs_prec* prec, const void* b, void* x, const vs_solve_opts* opts, vs_solve_info* info);
 
+/* nrhs right-hand sides of the same operator (incident directions and
+ * polarisations of one particle), stored one after another (n3 each); infos
+ * has nrhs entries and opts->resvec, if given, holds resvec_cap entries per
+ * right-hand side.  BiCGSTAB solves the batch together: every pipeline launch
+ * serves all right-hand sides (the Green spectrum and the preconditioner
+ * blocks are read once per launch), each right-hand side keeping its own
+ * scalars and convergence test.  GMRES solves them one after another. */
+int vs_solve_batch(vs_op* op, vs_prec* prec, const double* b, double* x, int64_t nrhs, const vs_solve_opts* opts,
+                   vs_solve_info* infos);
+int vs_solve_batch_device(vs_op* op, vs_prec* prec, const void* b, void* x, int64_t nrhs, const vs_solve_opts* opts,
+                          vs_solve_info* infos);
+
 /* ---- excitation, extinction cross section, gradient ------------------- */
 
 /* Plane wave E0 .* exp(1i k.r) at op's unknowns: PlaneWavePointWise.m:7-19

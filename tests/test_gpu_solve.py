@@ -149,3 +149,31 @@ def test_config1_gmres_mixed(api):
     x, info, rv = api.solve(op, b, pr, tol=1e-6, precision="mixed", method="gmres", restart=50)
     assert info["flag"] == 0
     assert np.linalg.norm(b - Aor(x)) / np.linalg.norm(b) <= 1e-6 * 1.01
+
+
+@pytest.mark.parametrize("precision,tol", [("mixed", 1e-6), ("fp64", 1e-10)])
+def test_batched_rhs_match_single_solves(api, precision, tol):
+    """8 incident directions x 2 polarisations of one plate solved as one batch:
+    every solution meets tol (FP64 oracle check) and the FP64 batch reproduces
+    the single-rhs iteration counts."""
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, Toep, alpha, dV, b0, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
+    rng = np.random.default_rng(5)
+    B = []
+    for _ in range(8):
+        v = rng.normal(size=3); v /= np.linalg.norm(v)
+        a = np.cross(v, [0, 0, 1.0]); a /= np.linalg.norm(a)
+        for pol in (a, np.cross(v, a)):
+            B.append(O.PlaneWavePointWise(pol, p["ko"] * v, p["r"]).ravel(order="F")[idx3])
+    B = np.array(B)
+    X, infos = api.solve_batch(op, B, pr, tol=tol, precision=precision)
+    for k in range(len(B)):
+        assert infos[k]["flag"] == 0, infos[k]
+        assert np.linalg.norm(B[k] - Aor(X[k])) / np.linalg.norm(B[k]) <= tol * 1.01
+    if precision == "fp64":
+        for k in (0, 5, 11):
+            x1, i1, _ = api.solve(op, B[k], pr, tol=tol, precision="fp64")
+            assert i1["iter"] == infos[k]["iter"]
+            assert np.linalg.norm(x1 - X[k]) <= 1e-12 * np.linalg.norm(x1)

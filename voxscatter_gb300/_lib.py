@@ -69,6 +69,9 @@ class vs_solve_info(C.Structure):
 
 
 SIGNATURES.update({
+    "vs_solve_batch": (C.c_int, [_vp, _vp, _pd, _pd, _i64, C.POINTER(vs_solve_opts), C.POINTER(vs_solve_info)]),
+    "vs_solve_batch_device": (C.c_int, [_vp, _vp, _vp, _vp, _i64, C.POINTER(vs_solve_opts),
+                                        C.POINTER(vs_solve_info)]),
     "vs_plane_wave": (C.c_int, [_vp, _pd, _pd, _pd, _pd, _pd, _pd]),
     "vs_cext": (C.c_int, [_vp, _pd, _pd, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double)]),
     "vs_cext_grad": (C.c_int, [_vp, _vp, _pd, _pd, C.c_double, C.c_double, _pd, _pd, C.POINTER(vs_solve_opts),

@@ -447,3 +447,35 @@ def cext_grad(op, prec, Einc, eps, ko, d, kvec, Eo, tol=1e-6, maxit=2000, precis
                              C.byref(i1), C.byref(i2)), op.ctx.h)
     info = lambda i: dict(flag=i.flag, relres=i.relres, iter=i.iter, time_ms=i.time_ms)
     return c.value, gre, gim, P, info(i1), info(i2)
+
+
+def solve_batch(op, B, prec=None, tol=1e-6, maxit=2000, precision="mixed", method="bicgstab", restart=50,
+                iters_per_graph=4):
+    """Solve A x_r = b_r for every row b_r of B (nrhs x n3) as one batch; returns
+    (X, list of info dicts)."""
+    lib = op.ctx._lib
+    B = np.ascontiguousarray(np.asarray(B, dtype=np.complex128))
+    nrhs = B.shape[0]
+    X = np.zeros_like(B)
+    o = _solve_opts(lib, tol, maxit, precision)
+    o.method = L.VS_GMRES if method == "gmres" else L.VS_BICGSTAB
+    o.restart = int(restart)
+    o.iters_per_graph = int(iters_per_graph)
+    infos = (L.vs_solve_info * nrhs)()
+    L.check(lib.vs_solve_batch(op.h, prec.h if prec is not None else None, L.dptr(B), L.dptr(X), nrhs, C.byref(o),
+                               infos), op.ctx.h)
+    return X, [dict(flag=i.flag, relres=i.relres, iter=i.iter, refinements=i.refinements, time_ms=i.time_ms,
+                    launches=i.kernel_launches) for i in infos]
+
+
+def solve_batch_device(op, b_ptr, x_ptr, nrhs, prec=None, tol=1e-6, maxit=2000, precision="mixed",
+                       iters_per_graph=4):
+    """vs_solve_batch_device on device buffers (double2, nrhs*n3 each)."""
+    lib = op.ctx._lib
+    o = _solve_opts(lib, tol, maxit, precision)
+    o.iters_per_graph = int(iters_per_graph)
+    infos = (L.vs_solve_info * nrhs)()
+    L.check(lib.vs_solve_batch_device(op.h, prec.h if prec is not None else None, C.c_void_p(b_ptr),
+                                      C.c_void_p(x_ptr), nrhs, C.byref(o), infos), op.ctx.h)
+    return [dict(flag=i.flag, relres=i.relres, iter=i.iter, refinements=i.refinements, time_ms=i.time_ms,
+                 launches=i.kernel_launches) for i in infos]

@@ -220,9 +220,8 @@ void time_passes(cudaStream_t st, int nrep, float* ms_out, F&& launch) {
   for (int p = 0; p < 5; ++p) ms_out[p] = acc[p] / nrep;
 }
 
-void solve_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, const vs_solve_opts* o,
-                       vs_solve_info* info) {
-  VS_REQUIRE(o && info, "NULL argument");
+vs::SolveParams solve_params(vs_op* op, vs_prec* prec, const vs_solve_opts* o) {
+  VS_REQUIRE(o, "NULL argument");
   VS_REQUIRE(o->method == VS_BICGSTAB || o->method == VS_GMRES, "unsupported method");
   VS_REQUIRE(o->method != VS_GMRES || (o->restart >= 1 && o->restart <= 2048), "GMRES restart must be in [1, 2048]");
   VS_REQUIRE(o->precision == VS_SOLVE_MIXED || o->precision == VS_SOLVE_FP64, "bad precision");
@@ -231,6 +230,7 @@ void solve_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, const vs
              "preconditioner does not match the operator");
   VS_REQUIRE(!prec || (o->precision == VS_SOLVE_MIXED ? prec->inv32.p != nullptr : prec->inv64.p != nullptr),
              "preconditioner not built in the precision this solve needs");
+  VS_REQUIRE(o->transpose == 0 || o->transpose == 1, "transpose must be 0 or 1");
   vs::SolveParams prm;
   prm.mode = o->precision;
   prm.tol = o->tol;
@@ -240,22 +240,51 @@ void solve_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, const vs
   prm.per_graph = o->iters_per_graph;
   prm.resvec_cap = (int)std::min<int64_t>(o->resvec ? o->resvec_cap : 0, 1 << 30);
   prm.resvec_host = o->resvec;
-  VS_REQUIRE(o->transpose == 0 || o->transpose == 1, "transpose must be 0 or 1");
   prm.op_mode = o->transpose ? VS_TRANSP : VS_NOTRANSP;
-  if (prec) {
-    const int64_t need = (int64_t)prec->L * prec->M * prec->N * 3 * sizeof(double2);
-    if ((int64_t)prec->t.bytes < need) prec->t.alloc(need);
-  }
   prm.restart = o->restart;
-  vs::SolveResult r;
-  if (o->method == VS_GMRES) vs::solve_gmres(*op, prec, b, x, prm, r, op->ctx->stream);
-  else vs::solve_bicgstab(*op, prec, b, x, prm, r, op->ctx->stream);
+  return prm;
+}
+
+void fill_info(const vs::SolveResult& r, vs_solve_info* info) {
   info->flag = r.flag;
   info->relres = r.relres;
   info->iter = r.iter;
   info->refinements = r.refinements;
   info->n_resvec = r.n_resvec;
   info->kernel_launches = r.launches;
+}
+
+void solve_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, const vs_solve_opts* o,
+                vs_solve_info* info) {
+  VS_REQUIRE(info, "NULL argument");
+  vs::SolveParams prm = solve_params(op, prec, o);
+  vs::SolveResult r;
+  if (o->method == VS_GMRES) vs::solve_gmres(*op, prec, b, x, prm, r, op->ctx->stream);
+  else vs::solve_bicgstab(*op, prec, b, x, prm, r, op->ctx->stream);
+  fill_info(r, info);
+}
+
+// nrhs right-hand sides: BiCGSTAB runs them as one batch (every launch serves
+// all of them); GMRES runs them one after another.
+void solve_batch_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, int64_t nrhs, const vs_solve_opts* o,
+                      vs_solve_info* infos) {
+  VS_REQUIRE(infos, "NULL argument");
+  VS_REQUIRE(nrhs >= 1 && nrhs <= 4096, "nrhs must be in [1, 4096]");
+  vs::SolveParams prm = solve_params(op, prec, o);
+  const int64_t n = op->n3;
+  if (o->method == VS_GMRES) {
+    for (int64_t r = 0; r < nrhs; ++r) {
+      vs::SolveParams p1 = prm;
+      p1.resvec_host = prm.resvec_host ? prm.resvec_host + r * prm.resvec_cap : nullptr;
+      vs::SolveResult res;
+      vs::solve_gmres(*op, prec, b + r * n, x + r * n, p1, res, op->ctx->stream);
+      fill_info(res, infos + r);
+    }
+    return;
+  }
+  std::vector<vs::SolveResult> res;
+  vs::solve_bicgstab_batch(*op, prec, b, x, (int)nrhs, prm, res, op->ctx->stream);
+  for (int64_t r = 0; r < nrhs; ++r) fill_info(res[r], infos + r);
 }
 
 }  // namespace
@@ -886,6 +915,39 @@ int vs_cext_grad(vs_op* op, vs_prec* prec, const double* Einc, const double* eps
     VS_CUDA(cudaMemcpyAsync(grad_im, dgi.p, nvox * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (P_out) VS_CUDA(cudaMemcpyAsync(P_out, dP.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+int vs_solve_batch_device(vs_op* op, vs_prec* prec, const void* b, void* x, int64_t nrhs, const vs_solve_opts* opts,
+                          vs_solve_info* infos) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(b && x, "NULL argument");
+    const auto t0 = std::chrono::steady_clock::now();
+    solve_batch_impl(op, prec, (const double2*)b, (double2*)x, nrhs, opts, infos);
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    for (int64_t r = 0; r < nrhs; ++r) infos[r].time_ms = ms;
+  });
+}
+
+int vs_solve_batch(vs_op* op, vs_prec* prec, const double* b, double* x, int64_t nrhs, const vs_solve_opts* opts,
+                   vs_solve_info* infos) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(b && x, "NULL argument");
+    VS_REQUIRE(nrhs >= 1 && nrhs <= 4096, "nrhs must be in [1, 4096]");
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t st = op->ctx->stream;
+    const int64_t n = op->n3 * nrhs;
+    op->xin.alloc(n * sizeof(double2));
+    op->yout.alloc(n * sizeof(double2));
+    VS_CUDA(cudaMemcpyAsync(op->xin.p, b, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemcpyAsync(op->yout.p, x, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    solve_batch_impl(op, prec, op->xin.as<double2>(), op->yout.as<double2>(), nrhs, opts, infos);
+    VS_CUDA(cudaMemcpyAsync(x, op->yout.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    for (int64_t r = 0; r < nrhs; ++r) infos[r].time_ms = ms;
   });
 }
 

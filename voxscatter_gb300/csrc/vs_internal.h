@@ -134,13 +134,15 @@ namespace vs {
 // Launchers (vs_matvec.cu)
 template <typename T>
 void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
-                 cudaStream_t st, int pass);
+                 cudaStream_t st, int pass, int skip_stride = 0);
 template <typename T>
 void matvec_scratch(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, cplx_t<T>* t1,
                     cplx_t<T>* t2, cudaStream_t st);
+// skip: optional device flags; right-hand side r is skipped (no work) when
+// skip[r * skip_stride] != 0.
 template <typename T>
 void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
-            cudaStream_t st);
+            cudaStream_t st, int skip_stride = 0);
 void ensure_scratch(vs_op& op, int nrhs, size_t elem_bytes);
 
 // Generic batched FFT passes (vs_matvec.cu)
@@ -171,9 +173,10 @@ void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, co
                      bool sym = false);
 template <typename T>
 void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
-                     cudaStream_t st, int pass);
+                     cudaStream_t st, int pass, int skip_stride = 0);
 template <typename T>
-void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip, cudaStream_t st);
+void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip, cudaStream_t st,
+                int skip_stride = 0);
 
 // Physics (vs_physics.cu)
 void plane_wave_device(const vs_op& op, const double* x, const double* y, const double* z, const double kvec[3],

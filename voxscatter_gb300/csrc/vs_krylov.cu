@@ -140,10 +140,18 @@ __device__ __forceinline__ bool cfinite(double2 a) { return isfinite(a.x) && isf
 
 #define GRID_LOOP(i, n) for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
 
+// All BiCGSTAB kernels below run on a batch of right-hand sides sharing one
+// operator: blockIdx.y is the right-hand side, its vectors start at
+// rhs * n, and its scalars live in states[rhs] (each state carries its own
+// reduction partials and counter).
+
 // rho = rt^H r ; beta = (rho/rho_prev)(alpha/omega)
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_bicg_rho(const cplx_t<T>* rt, const cplx_t<T>* r, int64_t n, KState* s) {
+__global__ void __launch_bounds__(kRedThreads) k_bicg_rho(const cplx_t<T>* rt, const cplx_t<T>* r, int64_t n,
+                                                         KState* states) {
+  KState* s = states + blockIdx.y;
   if (s->skip) return;
+  rt += blockIdx.y * n; r += blockIdx.y * n;
   Acc<T> a;
   GRID_LOOP(i, n) a.dot(rt[i], r[i]);
   double v[2] = {a.value().x, a.value().y}, t[2];
@@ -161,9 +169,11 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_rho(const cplx_t<T>* rt, c
 
 // p = r (first iteration) or r + beta (p - omega v)
 template <typename T>
-__global__ void k_bicg_p(cplx_t<T>* p, const cplx_t<T>* r, const cplx_t<T>* v, int64_t n, const KState* s) {
+__global__ void k_bicg_p(cplx_t<T>* p, const cplx_t<T>* r, const cplx_t<T>* v, int64_t n, const KState* states) {
   using C = cplx_t<T>;
+  const KState* s = states + blockIdx.y;
   if (s->skip) return;
+  p += blockIdx.y * n; r += blockIdx.y * n; v += blockIdx.y * n;
   if (s->iter2 == 0) {
     GRID_LOOP(i, n) p[i] = r[i];
     return;
@@ -174,8 +184,11 @@ __global__ void k_bicg_p(cplx_t<T>* p, const cplx_t<T>* r, const cplx_t<T>* v, i
 
 // alpha = rho / (rt^H v)
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_bicg_alpha(const cplx_t<T>* rt, const cplx_t<T>* v, int64_t n, KState* s) {
+__global__ void __launch_bounds__(kRedThreads) k_bicg_alpha(const cplx_t<T>* rt, const cplx_t<T>* v, int64_t n,
+                                                           KState* states) {
+  KState* s = states + blockIdx.y;
   if (s->skip) return;
+  rt += blockIdx.y * n; v += blockIdx.y * n;
   Acc<T> a;
   GRID_LOOP(i, n) a.dot(rt[i], v[i]);
   double w[2] = {a.value().x, a.value().y}, t[2];
@@ -192,9 +205,12 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_alpha(const cplx_t<T>* rt,
 
 // s = r - alpha v ; ||s|| ; half-step convergence test
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_bicg_s(cplx_t<T>* sv, const cplx_t<T>* r, const cplx_t<T>* v, int64_t n, KState* s) {
+__global__ void __launch_bounds__(kRedThreads) k_bicg_s(cplx_t<T>* sv, const cplx_t<T>* r, const cplx_t<T>* v,
+                                                       int64_t n, KState* states) {
   using C = cplx_t<T>;
+  KState* s = states + blockIdx.y;
   if (s->skip) return;
+  sv += blockIdx.y * n; r += blockIdx.y * n; v += blockIdx.y * n;
   const C al = ccast<C>(s->alpha);
   Acc<T> a;
   GRID_LOOP(i, n) {
@@ -223,13 +239,16 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_s(cplx_t<T>* sv, const cpl
 
 // x += alpha ph when the half step converged (runs regardless of skip).
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_bicg_xhalf(cplx_t<T>* x, const cplx_t<T>* ph, int64_t n, KState* s) {
+__global__ void __launch_bounds__(kRedThreads) k_bicg_xhalf(cplx_t<T>* x, const cplx_t<T>* ph, int64_t n,
+                                                           KState* states) {
   using C = cplx_t<T>;
+  KState* s = states + blockIdx.y;
   __shared__ int s_go;
   __shared__ bool s_last;
   if (threadIdx.x == 0) s_go = s->half_pending;
   __syncthreads();
   if (!s_go) return;
+  x += blockIdx.y * n; ph += blockIdx.y * n;
   const C al = ccast<C>(s->alpha);
   GRID_LOOP(i, n) x[i] = cfma(al, ph[i], x[i]);
   __syncthreads();
@@ -246,8 +265,11 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_xhalf(cplx_t<T>* x, const 
 
 // omega = (t^H s)/(t^H t)
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_bicg_omega(const cplx_t<T>* t, const cplx_t<T>* sv, int64_t n, KState* s) {
+__global__ void __launch_bounds__(kRedThreads) k_bicg_omega(const cplx_t<T>* t, const cplx_t<T>* sv, int64_t n,
+                                                           KState* states) {
+  KState* s = states + blockIdx.y;
   if (s->skip) return;
+  t += blockIdx.y * n; sv += blockIdx.y * n;
   Acc<T> a, b;
   GRID_LOOP(i, n) {
     a.dot(t[i], sv[i]);
@@ -274,10 +296,14 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_omega(const cplx_t<T>* t, 
 
 // x += alpha ph + omega sh ; r = s - omega t ; ||r|| ; full-step test
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* x, cplx_t<T>* r, const cplx_t<T>* ph, const cplx_t<T>* sh,
-                                                        const cplx_t<T>* sv, const cplx_t<T>* t, int64_t n, KState* s) {
+__global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* x, cplx_t<T>* r, const cplx_t<T>* ph,
+                                                        const cplx_t<T>* sh, const cplx_t<T>* sv, const cplx_t<T>* t,
+                                                        int64_t n, KState* states) {
   using C = cplx_t<T>;
+  KState* s = states + blockIdx.y;
   if (s->skip) return;
+  const int64_t o = blockIdx.y * n;
+  x += o; r += o; ph += o; sh += o; sv += o; t += o;
   const C al = ccast<C>(s->alpha), om = ccast<C>(s->omega);
   Acc<T> a;
   GRID_LOOP(i, n) {
@@ -315,13 +341,15 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* x, cplx_t<T>
   }
 }
 
-// ||u||^2 into s->aux (and u^H v optional) -- used for the initial residual.
+// out[rhs] = ||u_rhs|| (states supply the reduction buffers)
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_norm(const cplx_t<T>* u, int64_t n, KState* s, double* out) {
+__global__ void __launch_bounds__(kRedThreads) k_norm(const cplx_t<T>* u, int64_t n, KState* states, double* out) {
+  KState* s = states + blockIdx.y;
+  u += blockIdx.y * n;
   Acc<T> a;
   GRID_LOOP(i, n) a.norm2(u[i]);
   double w[1] = {a.value().x}, t[1];
-  if (grid_reduce<1>(w, s->partials, &s->counter, t) && threadIdx.x == 0) *out = sqrt(t[0]);
+  if (grid_reduce<1>(w, s->partials, &s->counter, t) && threadIdx.x == 0) out[blockIdx.y] = sqrt(t[0]);
 }
 
 template <typename T>
@@ -333,9 +361,12 @@ __global__ void k_zero(cplx_t<T>* dst, int64_t n) {
   GRID_LOOP(i, n) dst[i] = czero<cplx_t<T>>();
 }
 
-// r64 = b - y64 and its compensated norm
-__global__ void __launch_bounds__(kRedThreads) k_resid64(const double2* b, const double2* y, double2* r, int64_t n, KState* s,
-                                                        double* out) {
+// r64 = b - y64 and its compensated norm, per right-hand side
+__global__ void __launch_bounds__(kRedThreads) k_resid64(const double2* b, const double2* y, double2* r, int64_t n,
+                                                        KState* states, double* out) {
+  KState* s = states + blockIdx.y;
+  const int64_t o = blockIdx.y * n;
+  b += o; y += o; r += o;
   Acc<double> a;
   GRID_LOOP(i, n) {
     const double2 v = csub(b[i], y[i]);
@@ -343,18 +374,22 @@ __global__ void __launch_bounds__(kRedThreads) k_resid64(const double2* b, const
     a.norm2(v);
   }
   double w[1] = {a.value().x}, t[1];
-  if (grid_reduce<1>(w, s->partials, &s->counter, t) && threadIdx.x == 0) *out = sqrt(t[0]);
+  if (grid_reduce<1>(w, s->partials, &s->counter, t) && threadIdx.x == 0) out[blockIdx.y] = sqrt(t[0]);
 }
 
-// r32 = r64 * sc
-__global__ void k_scale_down(const double2* r, float2* o, int64_t n, double sc) {
-  GRID_LOOP(i, n) o[i] = make_float2((float)(r[i].x * sc), (float)(r[i].y * sc));
+// r32 = r64 * sc[rhs]
+__global__ void k_scale_down(const double2* r, float2* o, int64_t n, const double* sc) {
+  const int64_t off = blockIdx.y * n;
+  const double f = sc[blockIdx.y];
+  GRID_LOOP(i, n) o[off + i] = make_float2((float)(r[off + i].x * f), (float)(r[off + i].y * f));
 }
-// x64 += sc * d32
-__global__ void k_update64(double2* x, const float2* d, int64_t n, double sc) {
+// x64 += sc[rhs] * d32
+__global__ void k_update64(double2* x, const float2* d, int64_t n, const double* sc) {
+  const int64_t off = blockIdx.y * n;
+  const double f = sc[blockIdx.y];
   GRID_LOOP(i, n) {
-    x[i].x = fma(sc, (double)d[i].x, x[i].x);
-    x[i].y = fma(sc, (double)d[i].y, x[i].y);
+    x[off + i].x = fma(f, (double)d[off + i].x, x[off + i].x);
+    x[off + i].y = fma(f, (double)d[off + i].y, x[off + i].y);
   }
 }
 
@@ -375,14 +410,33 @@ void KrylovWork::ensure(int64_t n) {
   for (DevBuf* d : v) d->alloc(b);
 }
 
-static void upload_state(KState* d, const KState& h, cudaStream_t st) {
-  VS_CUDA(cudaMemcpyAsync(d, &h, sizeof(KState), cudaMemcpyHostToDevice, st));
+// Per-rhs reduction buffers: kRedBlocks * 4 doubles each.
+static void reduction_buffers(KrylovWork& w, int nrhs) {
+  w.partials.alloc((size_t)nrhs * kRedBlocks * 4 * sizeof(double));
+  w.state.alloc((size_t)nrhs * sizeof(KState));
+  w.scal.alloc((size_t)std::max(4, nrhs) * sizeof(double));
 }
 
-// One BiCGSTAB iteration (two half steps) as a fixed launch sequence.
+static void upload_states(KrylovWork& w, std::vector<KState>& h, cudaStream_t st) {
+  for (size_t r = 0; r < h.size(); ++r) {
+    h[r].partials = w.partials.as<double>() + r * kRedBlocks * 4;
+    h[r].counter = 0;
+  }
+  VS_CUDA(cudaMemcpyAsync(w.state.p, h.data(), h.size() * sizeof(KState), cudaMemcpyHostToDevice, st));
+}
+
+static std::vector<double> read_scal(KrylovWork& w, int nrhs, cudaStream_t st) {
+  std::vector<double> v(nrhs);
+  VS_CUDA(cudaMemcpyAsync(v.data(), w.scal.p, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
+  VS_CUDA(cudaStreamSynchronize(st));
+  return v;
+}
+
+// One BiCGSTAB iteration (two half steps) for all right-hand sides as a fixed
+// launch sequence.
 template <typename T>
-static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KState* s, int64_t n, int mode,
-                           cudaStream_t st) {
+static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KState* s, int64_t n, int nrhs,
+                           int mode, cudaStream_t st) {
   using C = cplx_t<T>;
   C* r = w.r.as<C>();
   C* rt = w.rt.as<C>();
@@ -393,19 +447,20 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
   C* ph = w.ph.as<C>();
   C* sh = w.sh.as<C>();
   C* x = w.x.as<C>();
-  const int g = vec_grid(n);
+  const dim3 g(vec_grid(n), nrhs);
   const int* skip = &s->skip;
+  const int ss = (int)(sizeof(KState) / sizeof(int));
   k_bicg_rho<T><<<g, kRedThreads, 0, st>>>(rt, r, n, s);
   k_bicg_p<T><<<g, 256, 0, st>>>(p, r, v, n, s);
-  if (pr) prec_apply<T>(*pr, p, ph, 1, skip, st);
-  else k_copy<T><<<g, 256, 0, st>>>(ph, p, n);
-  matvec<T>(op, ph, v, 1, mode, skip, st);
+  if (pr) prec_apply<T>(*pr, p, ph, nrhs, skip, st, ss);
+  else k_copy<T><<<dim3(vec_grid(n * nrhs)), 256, 0, st>>>(ph, p, n * nrhs);
+  matvec<T>(op, ph, v, nrhs, mode, skip, st, ss);
   k_bicg_alpha<T><<<g, kRedThreads, 0, st>>>(rt, v, n, s);
   k_bicg_s<T><<<g, kRedThreads, 0, st>>>(sv, r, v, n, s);
   k_bicg_xhalf<T><<<g, kRedThreads, 0, st>>>(x, ph, n, s);
-  if (pr) prec_apply<T>(*pr, sv, sh, 1, skip, st);
-  else k_copy<T><<<g, 256, 0, st>>>(sh, sv, n);
-  matvec<T>(op, sh, t, 1, mode, skip, st);
+  if (pr) prec_apply<T>(*pr, sv, sh, nrhs, skip, st, ss);
+  else k_copy<T><<<dim3(vec_grid(n * nrhs)), 256, 0, st>>>(sh, sv, n * nrhs);
+  matvec<T>(op, sh, t, nrhs, mode, skip, st, ss);
   k_bicg_omega<T><<<g, kRedThreads, 0, st>>>(t, sv, n, s);
   k_bicg_xr<T><<<g, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, n, s);
   VS_LAUNCH_CHECK();
@@ -415,67 +470,77 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
 // 2 preconditioner applies of 5 passes (or 2 copies without preconditioner).
 static int kernels_per_iteration(const vs_prec* pr) { return 7 + 10 + (pr ? 10 : 2); }
 
-// Runs BiCGSTAB on w.x (initial guess already there) for A x = w.r0-based
-// system: the caller has put the initial residual in w.r.  Returns the final
-// state.  Iterations are launched as a CUDA graph of `per_graph` iterations.
+// BiCGSTAB on w.x (initial guesses already there) with initial residuals in
+// w.r, for nrhs right-hand sides.  The absolute tolerance of rhs r is
+// tol * bnorm[r].  Iterations are launched as a CUDA graph of `per_graph`
+// iterations; the host polls the states between graph launches.
 template <typename T>
-static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t n, double bnorm, double tol,
-                            int maxit, double res_scale, double* resvec_dev, int resvec_cap, int per_graph,
-                            cudaStream_t st, int64_t* launches, int stag_window, int mode) {
+static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t n, int nrhs,
+                                         const std::vector<double>& bnorm, double tol, int maxit,
+                                         const std::vector<double>& res_scale, double* resvec_dev, int resvec_cap,
+                                         int per_graph, cudaStream_t st, int64_t* launches, int stag_window,
+                                         int mode) {
   using C = cplx_t<T>;
-  KState h{};
-  h.tol_abs = tol * bnorm;
-  h.maxit = maxit;
-  h.res_scale = res_scale;
-  h.resvec = resvec_dev;
-  h.resvec_cap = resvec_cap;
-  h.partials = w.partials.as<double>();
-  h.flag = 1;
-  h.stag_window = stag_window;
-  h.best_res = INFINITY;
+  std::vector<KState> h(nrhs);
+  for (int r = 0; r < nrhs; ++r) {
+    KState& k = h[r];
+    k = KState{};
+    k.tol_abs = tol * bnorm[r];
+    k.maxit = maxit;
+    k.res_scale = res_scale[r];
+    k.resvec = resvec_dev ? resvec_dev + (int64_t)r * resvec_cap : nullptr;
+    k.resvec_cap = resvec_dev ? resvec_cap : 0;
+    k.flag = 1;
+    k.stag_window = stag_window;
+    k.best_res = INFINITY;
+  }
   KState* s = w.state.as<KState>();
-  // r0 norm
-  upload_state(s, h, st);
-  const int g = vec_grid(n);
-  k_copy<T><<<g, 256, 0, st>>>(w.rt.as<C>(), w.r.as<C>(), n);
-  k_norm<T><<<g, kRedThreads, 0, st>>>(w.r.as<C>(), n, s, w.scal.as<double>());
+  upload_states(w, h, st);
+  const int gn = vec_grid(n * nrhs);
+  k_copy<T><<<gn, 256, 0, st>>>(w.rt.as<C>(), w.r.as<C>(), n * nrhs);
+  k_norm<T><<<dim3(vec_grid(n), nrhs), kRedThreads, 0, st>>>(w.r.as<C>(), n, s, w.scal.as<double>());
   *launches += 2;
-  double r0 = 0;
-  VS_CUDA(cudaMemcpyAsync(&r0, w.scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
-  VS_CUDA(cudaStreamSynchronize(st));
-  if (resvec_dev && resvec_cap > 0) {
-    const double v0 = r0 * res_scale;
-    VS_CUDA(cudaMemcpyAsync(resvec_dev, &v0, sizeof(double), cudaMemcpyHostToDevice, st));
+  const std::vector<double> r0 = read_scal(w, nrhs, st);
+  bool any_active = false;
+  for (int r = 0; r < nrhs; ++r) {
+    if (h[r].resvec && resvec_cap > 0) {
+      const double v0 = r0[r] * res_scale[r];
+      VS_CUDA(cudaMemcpyAsync(h[r].resvec, &v0, sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    h[r].res = r0[r];
+    h[r].nres = 1;
+    h[r].best_res = r0[r];
+    if (!(r0[r] > h[r].tol_abs) || maxit <= 0) {
+      h[r].flag = (r0[r] <= h[r].tol_abs) ? 0 : 1;
+      h[r].skip = 1;
+    } else {
+      any_active = true;
+    }
   }
-  h.res = r0;
-  h.nres = 1;
-  if (!(r0 > h.tol_abs) || maxit <= 0) {
-    h.flag = (r0 <= h.tol_abs) ? 0 : 1;
-    return h;
-  }
-  h.best_res = r0;
-  // The iteration graph depends only on the buffers, the preconditioner and
-  // the graph length (scalars live in the device state), so it is captured
-  // once and reused by later solves on this operator.
+  if (!any_active) return h;
+  // The iteration graph depends only on the buffers, the preconditioner, the
+  // batch size and the graph length (scalars live in the device states), so
+  // it is captured once and reused by later solves on this operator.
   GraphCache& gc = std::is_same<T, float>::value ? w.graph32 : w.graph64;
   std::vector<const void*> key = {w.r.p, w.rt.p, w.p.p, w.v_.p, w.s.p, w.t.p, w.ph.p, w.sh.p, w.x.p,
                                   w.state.p, w.partials.p, op.t1.p, op.t2.p,
                                   (const void*)(uintptr_t)(pr ? pr->id : 0), pr ? pr->t.p : nullptr,
-                                  (const void*)(uintptr_t)per_graph, (const void*)(uintptr_t)mode};
+                                  (const void*)(uintptr_t)per_graph, (const void*)(uintptr_t)mode,
+                                  (const void*)(uintptr_t)nrhs};
   if (gc.exec == nullptr || gc.key != key) {
     gc.reset();
-    // One launch sequence with skip set, outside capture: every kernel returns
-    // at once, but first-use attribute calls happen here rather than in the
-    // capture.
-    KState idle = h;
-    idle.skip = 1;
-    upload_state(s, idle, st);
-    bicg_iteration<T>(op, pr, w, s, n, mode, st);
+    // One launch sequence with every rhs skipped, outside capture: all
+    // kernels return at once, but first-use attribute calls happen here
+    // rather than in the capture.
+    std::vector<KState> idle = h;
+    for (auto& k : idle) k.skip = 1;
+    upload_states(w, idle, st);
+    bicg_iteration<T>(op, pr, w, s, n, nrhs, mode, st);
     *launches += kernels_per_iteration(pr);
     cudaGraph_t graph = nullptr;
     VS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     try {
-      for (int k = 0; k < per_graph; ++k) bicg_iteration<T>(op, pr, w, s, n, mode, st);
+      for (int k = 0; k < per_graph; ++k) bicg_iteration<T>(op, pr, w, s, n, nrhs, mode, st);
     } catch (...) {
       cudaStreamEndCapture(st, &graph);
       if (graph) cudaGraphDestroy(graph);
@@ -487,155 +552,207 @@ static KState bicgstab_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, i
     VS_CUDA(e);
     gc.key = key;
   }
-  upload_state(s, h, st);
-  KState cur{};
+  upload_states(w, h, st);
+  std::vector<KState> cur(nrhs);
   const int max_launch = (maxit + per_graph - 1) / per_graph + 1;
   for (int it = 0; it < max_launch; ++it) {
     VS_CUDA(cudaGraphLaunch(gc.exec, st));
     *launches += (int64_t)per_graph * kernels_per_iteration(pr);
-    VS_CUDA(cudaMemcpyAsync(&cur, s, sizeof(KState), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaMemcpyAsync(cur.data(), s, nrhs * sizeof(KState), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
-    if (cur.skip) break;
+    bool all = true;
+    for (int r = 0; r < nrhs; ++r) all = all && cur[r].skip;
+    if (all) break;
   }
-  if (!cur.skip) cur.flag = 1;
+  for (int r = 0; r < nrhs; ++r)
+    if (!cur[r].skip) cur[r].flag = 1;
   return cur;
 }
 
-static double norm64(KrylovWork& w, const double2* u, int64_t n, cudaStream_t st, int64_t* launches) {
-  *launches += 1;
-  KState* s = w.state.as<KState>();
-  k_norm<double><<<vec_grid(n), kRedThreads, 0, st>>>(u, n, s, w.scal.as<double>());
+// ||u_r|| for every rhs (compensated for c128)
+static std::vector<double> norms64(KrylovWork& w, const double2* u, int64_t n, int nrhs, cudaStream_t st,
+                                   int64_t* launches) {
+  std::vector<KState> h(nrhs);
+  upload_states(w, h, st);
+  k_norm<double><<<dim3(vec_grid(n), nrhs), kRedThreads, 0, st>>>(u, n, w.state.as<KState>(), w.scal.as<double>());
   VS_LAUNCH_CHECK();
-  double h = 0;
-  VS_CUDA(cudaMemcpyAsync(&h, w.scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
-  VS_CUDA(cudaStreamSynchronize(st));
-  return h;
+  *launches += 1;
+  return read_scal(w, nrhs, st);
 }
 
-// r64 = b - A x64 (c128 pipeline); returns ||r64||.
+// r64 = b - A x64 (c128 pipeline); returns ||r64|| per rhs.
+static std::vector<double> residuals64(const vs_op& op, KrylovWork& w, const double2* b, const double2* x, double2* r,
+                                       int64_t n, int nrhs, cudaStream_t st, int64_t* launches, int mode) {
+  std::vector<KState> h(nrhs);
+  upload_states(w, h, st);
+  double2* y = w.y64.as<double2>();
+  matvec<double>(op, x, y, nrhs, mode, nullptr, st);
+  k_resid64<<<dim3(vec_grid(n), nrhs), kRedThreads, 0, st>>>(b, y, r, n, w.state.as<KState>(), w.scal.as<double>());
+  VS_LAUNCH_CHECK();
+  *launches += 6;
+  return read_scal(w, nrhs, st);
+}
+
+// Single-rhs helpers used by GMRES.
+static double norm64(KrylovWork& w, const double2* u, int64_t n, cudaStream_t st, int64_t* launches) {
+  return norms64(w, u, n, 1, st, launches)[0];
+}
 static double residual64(const vs_op& op, KrylovWork& w, const double2* b, const double2* x, double2* r, int64_t n,
                          cudaStream_t st, int64_t* launches, int mode) {
-  *launches += 6;
-  KState* s = w.state.as<KState>();
-  double2* y = w.y64.as<double2>();
-  matvec<double>(op, x, y, 1, mode, nullptr, st);
-  k_resid64<<<vec_grid(n), kRedThreads, 0, st>>>(b, y, r, n, s, w.scal.as<double>());
-  VS_LAUNCH_CHECK();
-  double h = 0;
-  VS_CUDA(cudaMemcpyAsync(&h, w.scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
-  VS_CUDA(cudaStreamSynchronize(st));
-  return h;
+  return residuals64(op, w, b, x, r, n, 1, st, launches, mode)[0];
 }
 
-void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
-                    cudaStream_t st) {
+void solve_bicgstab_batch(vs_op& op, vs_prec* pr, const double2* b, double2* x, int nrhs, const SolveParams& prm,
+                          std::vector<SolveResult>& out, cudaStream_t st) {
   const int64_t n = op.n3;
   KrylovWork& w = op.kw;
-  w.partials.alloc(kRedBlocks * 4 * sizeof(double));
-  w.state.alloc(sizeof(KState));
-  w.scal.alloc(4 * sizeof(double));
-  VS_CUDA(cudaMemsetAsync(w.partials.p, 0, kRedBlocks * 4 * sizeof(double), st));
-  KState zero{};
-  zero.partials = w.partials.as<double>();  // every reduction needs its partial-sum buffer
-  upload_state(w.state.as<KState>(), zero, st);
+  reduction_buffers(w, nrhs);
   const int cap = prm.resvec_cap;
-  w.resvec.alloc(std::max(1, cap) * sizeof(double));
+  w.resvec.alloc((size_t)std::max(1, cap) * nrhs * sizeof(double));
   double* rv = cap > 0 ? w.resvec.as<double>() : nullptr;
-  ensure_scratch(op, 1, sizeof(double2));
-  int64_t launches = 0;
-  const double bnorm = norm64(w, b, n, st, &launches);
-  if (!std::isfinite(bnorm)) throw Error(VS_ERR_NONFINITE, "right-hand side has NaN or Inf entries");
-  out = SolveResult{};
-  if (bnorm == 0) {
-    VS_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double2), st));
-    VS_CUDA(cudaStreamSynchronize(st));
-    out.flag = 0;
-    return;
+  ensure_scratch(op, nrhs, sizeof(double2));
+  if (pr) {
+    const size_t need = (size_t)pr->L * pr->M * pr->N * 3 * sizeof(double2) * nrhs;
+    if (pr->t.bytes < need) pr->t.alloc(need);
   }
+  int64_t launches = 0;
+  const std::vector<double> bnorm = norms64(w, b, n, nrhs, st, &launches);
+  out.assign(nrhs, SolveResult{});
+  for (int r = 0; r < nrhs; ++r)
+    if (!std::isfinite(bnorm[r])) throw Error(VS_ERR_NONFINITE, "right-hand side has NaN or Inf entries");
+  // zero right-hand sides: x = 0, converged
+  std::vector<double> bsafe(nrhs);
+  for (int r = 0; r < nrhs; ++r) {
+    bsafe[r] = bnorm[r] > 0 ? bnorm[r] : 1.0;
+    if (bnorm[r] == 0) VS_CUDA(cudaMemsetAsync(x + r * n, 0, n * sizeof(double2), st));
+  }
+  const std::vector<double> xn = norms64(w, x, n, nrhs, st, &launches);
+  bool x0zero = true;
+  for (double v : xn) x0zero = x0zero && v == 0.0;
+  std::vector<double> rn;
+  std::vector<int> inner2(nrhs, 0), flag(nrhs, 1), refine(nrhs, 0);
+  std::vector<int64_t> nres(nrhs, 0);
   if (prm.mode == VS_SOLVE_FP64) {
-    w.ensure<double>(n);
-    w.y64.alloc(n * sizeof(double2));
-    // x0 -> w.x ; r = b - A x0
-    k_copy<double><<<vec_grid(n), 256, 0, st>>>(w.x.as<double2>(), x, n);
-    if (norm64(w, x, n, st, &launches) == 0.0) {  // x0 = 0: r = b exactly, no matvec
-      k_copy<double><<<vec_grid(n), 256, 0, st>>>(w.r.as<double2>(), b, n);
-      VS_LAUNCH_CHECK();
-      launches += 1;
-    } else {
-      residual64(op, w, b, x, w.r.as<double2>(), n, st, &launches, prm.op_mode);
-    }
-    launches += 1;
-    KState fs = bicgstab_core<double>(op, pr, w, n, bnorm, prm.tol, prm.maxit, 1.0 / bnorm, rv, cap, prm.per_graph, st,
-                                      &launches, 0, prm.op_mode);
-    launches += 1;
-    k_copy<double><<<vec_grid(n), 256, 0, st>>>(x, w.x.as<double2>(), n);
+    w.ensure<double>(n * nrhs);
+    w.y64.alloc(n * nrhs * sizeof(double2));
+    k_copy<double><<<vec_grid(n * nrhs), 256, 0, st>>>(w.x.as<double2>(), x, n * nrhs);
+    if (x0zero) k_copy<double><<<vec_grid(n * nrhs), 256, 0, st>>>(w.r.as<double2>(), b, n * nrhs);
+    else residuals64(op, w, b, x, w.r.as<double2>(), n, nrhs, st, &launches, prm.op_mode);
+    launches += 2;
+    std::vector<double> sc(nrhs);
+    for (int r = 0; r < nrhs; ++r) sc[r] = 1.0 / bsafe[r];
+    std::vector<KState> fs = bicgstab_core<double>(op, pr, w, n, nrhs, bsafe, prm.tol, prm.maxit, sc, rv, cap,
+                                                   prm.per_graph, st, &launches, 0, prm.op_mode);
+    k_copy<double><<<vec_grid(n * nrhs), 256, 0, st>>>(x, w.x.as<double2>(), n * nrhs);
     VS_LAUNCH_CHECK();
-    out.flag = fs.flag;
-    out.iter = fs.iter2 * 0.5;
-    out.inner_iters = fs.iter2 * 0.5;
-    out.n_resvec = std::min<int64_t>(fs.nres, cap);
-    const double rn = residual64(op, w, b, x, w.r.as<double2>(), n, st, &launches, prm.op_mode);
-    out.relres = rn / bnorm;
-    if (out.flag == 0 && out.relres > prm.tol) out.flag = 1;
+    launches += 1;
+    rn = residuals64(op, w, b, x, w.r.as<double2>(), n, nrhs, st, &launches, prm.op_mode);
+    for (int r = 0; r < nrhs; ++r) {
+      out[r].flag = fs[r].flag;
+      out[r].iter = fs[r].iter2 * 0.5;
+      out[r].inner_iters = out[r].iter;
+      out[r].n_resvec = std::min<int64_t>(fs[r].nres, cap);
+      out[r].relres = bnorm[r] > 0 ? rn[r] / bnorm[r] : 0.0;
+      if (bnorm[r] == 0) out[r].flag = 0;
+      else if (out[r].flag == 0 && out[r].relres > prm.tol) out[r].flag = 1;
+    }
   } else {
-    // mixed: c64 inner BiCGSTAB inside FP64 refinement
-    w.ensure<float>(n);
-    w.y64.alloc(n * sizeof(double2));
-    w.r64.alloc(n * sizeof(double2));
+    // mixed: c64 inner BiCGSTAB inside FP64 refinement, all rhs together
+    w.ensure<float>(n * nrhs);
+    w.y64.alloc(n * nrhs * sizeof(double2));
+    w.r64.alloc(n * nrhs * sizeof(double2));
     double2* r64 = w.r64.as<double2>();
-    double rn;
-    if (norm64(w, x, n, st, &launches) == 0.0) {  // x0 = 0: r = b exactly, no matvec
-      k_copy<double><<<vec_grid(n), 256, 0, st>>>(r64, b, n);
+    if (x0zero) {
+      k_copy<double><<<vec_grid(n * nrhs), 256, 0, st>>>(r64, b, n * nrhs);
       VS_LAUNCH_CHECK();
       launches += 1;
       rn = bnorm;
     } else {
-      rn = residual64(op, w, b, x, r64, n, st, &launches, prm.op_mode);
+      rn = residuals64(op, w, b, x, r64, n, nrhs, st, &launches, prm.op_mode);
     }
-    int inner_total2 = 0;
-    int64_t nres = 0;
-    int flag = 1;
-    int refine = 0;
-    for (; refine <= prm.max_refine; ++refine) {
-      if (rn <= prm.tol * bnorm) {
-        flag = 0;
-        break;
+    DevBuf scd;
+    scd.alloc(nrhs * sizeof(double));
+    for (int step = 0; step <= prm.max_refine; ++step) {
+      bool all_done = true;
+      for (int r = 0; r < nrhs; ++r) {
+        const bool done = rn[r] <= prm.tol * bnorm[r] || flag[r] >= 4;
+        if (rn[r] <= prm.tol * bnorm[r]) flag[r] = 0;
+        all_done = all_done && done;
       }
-      if (refine == prm.max_refine || inner_total2 >= 2 * prm.maxit) break;
-      // Aim one inner solve at the whole remaining reduction (with margin for
-      // the c64 rounding of the operator), but not below what c64 can reach.
-      double itol = prm.inner_tol > 0 ? prm.inner_tol : std::max(0.3 * prm.tol * bnorm / rn, prm.inner_floor);
-      itol = std::min(itol, 0.5);
-      k_scale_down<<<vec_grid(n), 256, 0, st>>>(r64, w.r.as<float2>(), n, 1.0 / rn);
-      k_zero<float><<<vec_grid(n), 256, 0, st>>>(w.x.as<float2>(), n);
+      if (all_done || step == prm.max_refine) break;
+      int used = 0;
+      for (int r = 0; r < nrhs; ++r) used = std::max(used, inner2[r]);
+      if (used >= 2 * prm.maxit) break;
+      // per-rhs inner tolerance relative to the scaled residual (norm 1);
+      // converged rhs get tol 1 (they stop at iteration 0)
+      std::vector<double> scale(nrhs), one(nrhs, 1.0), rscale(nrhs), itol(nrhs);
+      for (int r = 0; r < nrhs; ++r) {
+        const bool done = rn[r] <= prm.tol * bnorm[r] || flag[r] >= 4;
+        scale[r] = rn[r] > 0 ? 1.0 / rn[r] : 0.0;
+        double t = prm.inner_tol > 0 ? prm.inner_tol : std::max(0.3 * prm.tol * bnorm[r] / rn[r], prm.inner_floor);
+        itol[r] = done ? 2.0 : std::min(t, 0.5);
+        rscale[r] = bnorm[r] > 0 ? rn[r] / bnorm[r] : 0.0;
+        refine[r] += done ? 0 : 1;
+      }
+      VS_CUDA(cudaMemcpyAsync(scd.p, scale.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, st));
+      k_scale_down<<<dim3(vec_grid(n), nrhs), 256, 0, st>>>(r64, w.r.as<float2>(), n, scd.as<double>());
+      k_zero<float><<<vec_grid(n * nrhs), 256, 0, st>>>(w.x.as<float2>(), n * nrhs);
       VS_LAUNCH_CHECK();
-      double* rvk = (rv && nres < cap) ? rv + nres : nullptr;
-      const int capk = rv ? (int)(cap - nres) : 0;
-      KState fs = bicgstab_core<float>(op, pr, w, n, 1.0, itol, prm.maxit - inner_total2 / 2, rn / bnorm, rvk, capk,
-                                       prm.per_graph, st, &launches, kStagnationWindow, prm.op_mode);
       launches += 2;
-      inner_total2 += fs.iter2;
-      nres += std::min<int64_t>(fs.nres, capk);
-      if (fs.flag >= 4 && fs.iter2 == 0) {
-        flag = fs.flag;
-        break;
+      // one inner solve with a common tolerance: use the tightest active one,
+      // expressed per rhs through bnorm = itol_r / itol_min
+      double tmin = 1.0;
+      for (int r = 0; r < nrhs; ++r) tmin = std::min(tmin, itol[r]);
+      std::vector<double> bn(nrhs);
+      for (int r = 0; r < nrhs; ++r) bn[r] = itol[r] / tmin;
+      double* rvk = nullptr;
+      int capk = 0;
+      if (rv && nrhs == 1 && nres[0] < cap) {
+        rvk = rv + nres[0];
+        capk = (int)(cap - nres[0]);
       }
-      k_update64<<<vec_grid(n), 256, 0, st>>>(x, w.x.as<float2>(), n, rn);
+      std::vector<KState> fs = bicgstab_core<float>(op, pr, w, n, nrhs, bn, tmin, prm.maxit - used / 2, rscale, rvk,
+                                                    capk, prm.per_graph, st, &launches, kStagnationWindow,
+                                                    prm.op_mode);
+      bool progressed = false;
+      for (int r = 0; r < nrhs; ++r) {
+        inner2[r] += fs[r].iter2;
+        if (nrhs == 1) nres[0] += std::min<int64_t>(fs[0].nres, capk);
+        if (fs[r].flag >= 4 && fs[r].iter2 == 0 && !(rn[r] <= prm.tol * bnorm[r])) flag[r] = fs[r].flag;
+        progressed = progressed || fs[r].iter2 > 0;
+      }
+      VS_CUDA(cudaMemcpyAsync(scd.p, rn.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, st));
+      k_update64<<<dim3(vec_grid(n), nrhs), 256, 0, st>>>(x, w.x.as<float2>(), n, scd.as<double>());
       VS_LAUNCH_CHECK();
       launches += 1;
-      rn = residual64(op, w, b, x, r64, n, st, &launches, prm.op_mode);
+      rn = residuals64(op, w, b, x, r64, n, nrhs, st, &launches, prm.op_mode);
+      if (!progressed) break;
     }
-    out.flag = (rn <= prm.tol * bnorm) ? 0 : (flag >= 4 ? flag : 1);
-    out.relres = rn / bnorm;
-    out.iter = inner_total2 * 0.5;
-    out.inner_iters = inner_total2 * 0.5;
-    out.refinements = refine;
-    out.n_resvec = nres;
+    for (int r = 0; r < nrhs; ++r) {
+      out[r].flag = (rn[r] <= prm.tol * bnorm[r]) ? 0 : (flag[r] >= 4 ? flag[r] : 1);
+      out[r].relres = bnorm[r] > 0 ? rn[r] / bnorm[r] : 0.0;
+      out[r].iter = inner2[r] * 0.5;
+      out[r].inner_iters = out[r].iter;
+      out[r].refinements = refine[r];
+      out[r].n_resvec = nrhs == 1 ? nres[0] : 0;
+      if (bnorm[r] == 0) out[r].flag = 0;
+    }
   }
-  out.launches = launches;
-  if (cap > 0 && prm.resvec_host && out.n_resvec > 0)
-    VS_CUDA(cudaMemcpyAsync(prm.resvec_host, rv, out.n_resvec * sizeof(double), cudaMemcpyDeviceToHost, st));
+  for (auto& o : out) o.launches = launches;
+  if (cap > 0 && prm.resvec_host) {
+    for (int r = 0; r < nrhs; ++r)
+      if (out[r].n_resvec > 0)
+        VS_CUDA(cudaMemcpyAsync(prm.resvec_host + (int64_t)r * cap, rv + (int64_t)r * cap,
+                                out[r].n_resvec * sizeof(double), cudaMemcpyDeviceToHost, st));
+  }
   VS_CUDA(cudaStreamSynchronize(st));
+}
+
+void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
+                    cudaStream_t st) {
+  std::vector<SolveResult> r;
+  solve_bicgstab_batch(op, pr, b, x, 1, prm, r, st);
+  out = r[0];
 }
 
 }  // namespace vs
@@ -1062,12 +1179,9 @@ void solve_gmres(vs_op& op, vs_prec* pr, const double2* b, double2* x, const Sol
                  cudaStream_t st) {
   const int64_t n = op.n3;
   KrylovWork& w = op.kw;
-  w.partials.alloc(kRedBlocks * 4 * sizeof(double));
-  w.state.alloc(sizeof(KState));
-  w.scal.alloc(4 * sizeof(double));
-  KState zero{};
-  zero.partials = w.partials.as<double>();
-  upload_state(w.state.as<KState>(), zero, st);
+  reduction_buffers(w, 1);
+  std::vector<KState> zero(1);
+  upload_states(w, zero, st);
   const int cap = prm.resvec_cap;
   w.resvec.alloc(std::max(1, cap) * sizeof(double));
   double* rv = cap > 0 ? w.resvec.as<double>() : nullptr;

@@ -53,6 +53,8 @@ struct SolveResult {
 
 void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
                     cudaStream_t st);
+void solve_bicgstab_batch(vs_op& op, vs_prec* pr, const double2* b, double2* x, int nrhs, const SolveParams& prm,
+                          std::vector<SolveResult>& out, cudaStream_t st);
 void solve_gmres(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
                  cudaStream_t st);
 

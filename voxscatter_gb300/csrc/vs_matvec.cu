@@ -47,7 +47,7 @@ __host__ __device__ __forceinline__ int ilog2(int v) {
 template <typename T, int MODE, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_xf(PipeArgs<T> a) {
   using C = cplx_t<T>;
-  if (a.skip && *a.skip) return;
+  if (a.skip && a.skip[blockIdx.y * a.skip_stride]) return;
   C* sm = shmem<C>();
   const int lg_nl = a.lg_lpb, lg_nj = 8 - lg_nl, NJ = 1 << lg_nj;
   const int nlpb = 1 << lg_nl;
@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(kThreads) k_xf(PipeArgs<T> a) {
 template <typename T, int MODE, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_xi(PipeArgs<T> a) {
   using C = cplx_t<T>;
-  if (a.skip && *a.skip) return;
+  if (a.skip && a.skip[blockIdx.y * a.skip_stride]) return;
   C* sm = shmem<C>();
   const int lg_nl = a.lg_lpb, lg_nj = 8 - lg_nl, NJ = 1 << lg_nj;
   const int nlpb = 1 << lg_nl;
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kThreads) k_xi(PipeArgs<T> a) {
 template <typename T, bool INV, bool SMALL>
 __global__ void __launch_bounds__(kThreads) k_strided(StridedArgs<T> a) {
   using C = cplx_t<T>;
-  if (a.skip && *a.skip) return;
+  if (a.skip && a.skip[blockIdx.z * a.skip_stride]) return;
   C* sm = shmem<C>();
   const int n = a.plan.n;
   const int lg_nl = a.lg_tx, tx = 1 << lg_nl, NJ = kThreads >> lg_nl;
@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(kThreads) k_strided(StridedArgs<T> a) {
 template <typename T, bool SMALL, bool SYM>
 __global__ void __launch_bounds__(kThreads) k_z(PipeArgs<T> a) {
   using C = cplx_t<T>;
-  if (a.skip && *a.skip) return;
+  if (a.skip && a.skip[blockIdx.z * a.skip_stride]) return;
   C* sm = shmem<C>();
   const int R = a.R;
   const int lg_nl = a.lg_tx, tx = 1 << lg_nl, NJ = kThreads >> lg_nl;
@@ -333,11 +333,13 @@ static StridedArgs<T> y_pass_args(const vs_op& op, const PipeArgs<T>& a, bool in
   s.plan = op.ax[1].plan;
   s.tw = a.twQ;
   s.skip = a.skip;
+  s.skip_stride = a.skip_stride;
   return s;
 }
 
 template <typename T>
-static PipeArgs<T> pipe_args(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, const int* skip) {
+static PipeArgs<T> pipe_args(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, const int* skip,
+                             int skip_stride = 0) {
   using C = cplx_t<T>;
   PipeArgs<T> a{};
   a.L = op.L; a.M = op.M; a.N = op.N; a.P = op.P; a.Q = op.Q; a.R = op.R;
@@ -356,15 +358,16 @@ static PipeArgs<T> pipe_args(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, 
   a.lg_lpb = sh.lg_lpb_x >= 0 ? sh.lg_lpb_x : ilog2(pick_lpb(op.P, sizeof(C)));
   a.lg_tx = sh.lg_tx_z >= 0 ? sh.lg_tx_z : ilog2(pick_tile(op.R, sizeof(C), 3));
   a.skip = skip;
+  a.skip_stride = skip_stride;
   return a;
 }
 
 template <typename T>
 void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
-                 cudaStream_t st, int pass) {
+                 cudaStream_t st, int pass, int skip_stride) {
   using C = cplx_t<T>;
   VS_REQUIRE(mode >= VS_NOTRANSP && mode <= VS_CONJTRANSP, "mode must be VS_NOTRANSP, VS_TRANSP or VS_CONJTRANSP");
-  const PipeArgs<T> a = pipe_args<T>(op, x, y, skip);
+  const PipeArgs<T> a = pipe_args<T>(op, x, y, skip, skip_stride);
   switch (pass) {
     case 0: launch_x_pass<T>(a, false, mode, nrhs, st); break;
     case 1: launch_strided_pass<T, false>(y_pass_args<T>(op, a, false), op.N * 3, nrhs, st); break;
@@ -395,8 +398,8 @@ void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, in
 
 template <typename T>
 void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
-            cudaStream_t st) {
-  for (int pass = 0; pass < 5; ++pass) matvec_pass<T>(op, x, y, nrhs, mode, skip, st, pass);
+            cudaStream_t st, int skip_stride) {
+  for (int pass = 0; pass < 5; ++pass) matvec_pass<T>(op, x, y, nrhs, mode, skip, st, pass, skip_stride);
 }
 
 template void launch_x_pass<float>(const PipeArgs<float>&, bool, int, int, cudaStream_t);
@@ -446,10 +449,10 @@ template void matvec_scratch<float>(const vs_op&, const float2*, float2*, int, i
 template void matvec_scratch<double>(const vs_op&, const double2*, double2*, int, int, double2*, double2*,
                                      cudaStream_t);
 
-template void matvec_pass<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t, int);
-template void matvec_pass<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t, int);
-template void matvec<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t);
-template void matvec<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t);
+template void matvec_pass<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t, int, int);
+template void matvec_pass<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t, int, int);
+template void matvec<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t, int);
+template void matvec<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t, int);
 
 // ---- generic batched FFTs (operator setup, preconditioner) --------------
 template <typename T, bool INV>
@@ -497,6 +500,7 @@ void fft_strided(cplx_t<T>* data, int xext, int n, int64_t row_stride, int na, i
   s.plan = ax.plan;
   s.tw = ax.tw<T>();
   s.skip = nullptr;
+  s.skip_stride = 0;
   launch_strided_pass<T, INV>(s, na * nb, 1, st);
 }
 

@@ -33,7 +33,8 @@ struct PipeArgs {
   FftPlan pP, pQ, pR;
   int lg_lpb;  // log2 lines per block in the x passes
   int lg_tx;   // log2 x-tile width of the z pass
-  const int* skip;
+  const int* skip;   // right-hand side r is skipped when skip[r * skip_stride] != 0
+  int skip_stride;
 };
 
 // ---- strided-axis pass (y of the pipeline; y and z of the setup FFTs) ----
@@ -52,6 +53,7 @@ struct StridedArgs {
   FftPlan plan;
   const C* tw;
   const int* skip;
+  int skip_stride;
 };
 
 template <typename T>

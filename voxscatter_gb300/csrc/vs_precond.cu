@@ -217,9 +217,9 @@ template void assemble_invert<double>(const double2*, int, int, int, double2, co
 template <typename T>
 __global__ void __launch_bounds__(256) k_block_gemv(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ inv, int L,
                                                     int M, int N, int ti, int64_t rhs_stride, const int* skip,
-                                                    int sym) {
+                                                    int sym, int skip_stride) {
   using C = cplx_t<T>;
-  if (skip && *skip) return;
+  if (skip && skip[blockIdx.z * skip_stride]) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = 3 * N;
   C* v = reinterpret_cast<C*>(smem_raw);
@@ -279,9 +279,9 @@ __global__ void __launch_bounds__(256) k_block_gemv(cplx_t<T>* __restrict__ t, c
 template <typename T, bool PAIR>
 __global__ void __launch_bounds__(256) k_block_gemv_sym(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ inv,
                                                         int L, int M, int N, int ti, int64_t rhs_stride,
-                                                        const int* skip) {
+                                                        const int* skip, int skip_stride) {
   using C = cplx_t<T>;
-  if (skip && *skip) return;
+  if (skip && skip[blockIdx.z * skip_stride]) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = 3 * N;
   const int Lb = L / 2 + 1;
@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(256) k_block_gemv_sym(cplx_t<T>* __restrict__ 
 
 template <typename T>
 void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
-                     cudaStream_t st, int pass) {
+                     cudaStream_t st, int pass, int skip_stride) {
   using C = cplx_t<T>;
   const int L = pr.L, M = pr.M, N = pr.N;
   const C* inv = std::is_same<T, float>::value ? (const C*)pr.inv32.p : (const C*)pr.inv64.p;
@@ -399,6 +399,7 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
     a.lg_lpb = lg;
   }
   a.skip = skip;
+  a.skip_stride = skip_stride;
   StridedArgs<T> s{};
   s.src = t; s.dst = t;
   s.xext = L; s.n_in = M; s.n_out = M;
@@ -419,6 +420,7 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
   s.plan = pr.axM.plan;
   s.tw = pr.axM.tw<T>();
   s.skip = skip;
+  s.skip_stride = skip_stride;
   switch (pass) {
     case 0: launch_x_pass<T>(a, false, MODE_PLAIN, nrhs, st); break;
     case 1: launch_strided_pass<T, false>(s, 3 * N, nrhs, st); break;
@@ -434,11 +436,11 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
         if (std::is_same<T, float>::value && n % 2 == 0) {
           auto k = k_block_gemv_sym<T, true>;
           set_kernel_smem((const void*)k, smem);
-          k<<<grid, nthr, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
+          k<<<grid, nthr, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip, skip_stride);
         } else {
           auto k = k_block_gemv_sym<T, false>;
           set_kernel_smem((const void*)k, smem);
-          k<<<grid, nthr, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip);
+          k<<<grid, nthr, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip, skip_stride);
         }
         VS_LAUNCH_CHECK();
         break;
@@ -447,7 +449,8 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
       const size_t smem = 2ull * ti * n * sizeof(C);
       auto k = k_block_gemv<T>;
       set_kernel_smem((const void*)k, smem);
-      k<<<dim3(ceil_div(L, ti), M, nrhs), 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip, 0);
+      k<<<dim3(ceil_div(L, ti), M, nrhs), 256, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip, 0,
+                                                            skip_stride);
       VS_LAUNCH_CHECK();
       break;
     }
@@ -457,8 +460,9 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
 }
 
 template <typename T>
-void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip, cudaStream_t st) {
-  for (int pass = 0; pass < 5; ++pass) prec_apply_pass<T>(pr, x, y, nrhs, skip, st, pass);
+void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip, cudaStream_t st,
+                int skip_stride) {
+  for (int pass = 0; pass < 5; ++pass) prec_apply_pass<T>(pr, x, y, nrhs, skip, st, pass, skip_stride);
 }
 template <typename F>
 static float time_ms_prec(cudaStream_t st, int reps, F&& f) {
@@ -533,9 +537,9 @@ void autotune_prec(vs_prec& pr, cudaStream_t st) {
 template void autotune_prec<float>(vs_prec&, cudaStream_t);
 template void autotune_prec<double>(vs_prec&, cudaStream_t);
 
-template void prec_apply_pass<float>(const vs_prec&, const float2*, float2*, int, const int*, cudaStream_t, int);
-template void prec_apply_pass<double>(const vs_prec&, const double2*, double2*, int, const int*, cudaStream_t, int);
-template void prec_apply<float>(const vs_prec&, const float2*, float2*, int, const int*, cudaStream_t);
-template void prec_apply<double>(const vs_prec&, const double2*, double2*, int, const int*, cudaStream_t);
+template void prec_apply_pass<float>(const vs_prec&, const float2*, float2*, int, const int*, cudaStream_t, int, int);
+template void prec_apply_pass<double>(const vs_prec&, const double2*, double2*, int, const int*, cudaStream_t, int, int);
+template void prec_apply<float>(const vs_prec&, const float2*, float2*, int, const int*, cudaStream_t, int);
+template void prec_apply<double>(const vs_prec&, const double2*, double2*, int, const int*, cudaStream_t, int);
 
 }  // namespace vs
