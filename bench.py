@@ -222,6 +222,80 @@ def run_reference(args):
     return 0
 
 
+def _directions(seed, count):
+    """`count` seeded incident directions, two polarisations each."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        v = rng.normal(size=3); v /= np.linalg.norm(v)
+        a = np.cross(v, [0, 0, 1.0] if abs(v[2]) < 0.9 else [1.0, 0, 0]); a /= np.linalg.norm(a)
+        out.append((v, a)); out.append((v, np.cross(v, a)))
+    return out
+
+
+def _batched(api, ctx, stream, p, op, prec, steps):
+    """16 right-hand sides (8 directions x 2 polarisations) of the plate, one
+    batched mixed solve; and the 32-plate x 16-rhs configuration (512 rhs)."""
+    import torch
+    from voxscatter_gb300 import workloads as W
+    out = {}
+    B = np.array([api.plane_wave(op, p["r"], p["ko"] * v, pol) for v, pol in _directions(7, 8)])
+    Bd = torch.from_numpy(B).cuda()
+    Xd = torch.zeros_like(Bd)
+    torch.cuda.synchronize()
+    api.solve_batch_device(op, Bd.data_ptr(), Xd.data_ptr(), len(B), prec, tol=TOL)  # warm-up / graph capture
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            Xd.zero_()
+        infos = api.solve_batch_device(op, Bd.data_ptr(), Xd.data_ptr(), len(B), prec, tol=TOL)
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    out["plate_16rhs"] = {"ms_per_batch": ms, "ms_per_rhs": ms / len(B),
+                          "converged": all(i["flag"] == 0 for i in infos),
+                          "max_relres": max(i["relres"] for i in infos),
+                          "max_iterations": max(i["iter"] for i in infos)}
+    # 32 plates, diameters U[1,6] lambda (seeded), 16 rhs each
+    t0 = time.perf_counter()
+    parts = []
+    for q in W.config3_particles(seed=0):
+        L, M, N = q["L"], q["M"], q["N"]
+        nD = L * M * N
+        idx3 = np.concatenate([q["idx"], nD + q["idx"], 2 * nD + q["idx"]])
+        dV = q["d"] ** 3
+        Tq = api.green_dda(q["r"], q["ko"], ctx=ctx)
+        ainv = 1 / api.alpha_ldr(q["refInd"], q["ko"], q["d"], q["kvec"], q["Eo"])
+        opq = api.Operator(L, M, N, idx3, 1.0, dV, ainv, toep=Tq, ctx=ctx)
+        prq = api.Preconditioner(opq, shift=ainv, d=dV, precisions=("c64", "c128"))
+        Bq = np.array([api.plane_wave(opq, q["r"], q["ko"] * v, pol) for v, pol in q["rhs"]])
+        parts.append((opq, prq, torch.from_numpy(Bq).cuda(), len(Bq), len(q["idx"])))
+    torch.cuda.synchronize()
+    setup = (time.perf_counter() - t0) * 1e3
+    Xs = [torch.zeros_like(Bq) for (_, _, Bq, _, _) in parts]
+    for (opq, prq, Bq, nr, _), Xq in zip(parts, Xs):  # warm-up (graph capture per operator)
+        api.solve_batch_device(opq, Bq.data_ptr(), Xq.data_ptr(), nr, prq, tol=TOL)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    conv, worst = True, 0.0
+    for _ in range(steps):
+        for (opq, prq, Bq, nr, _), Xq in zip(parts, Xs):
+            with torch.cuda.stream(stream):
+                Xq.zero_()
+            inf = api.solve_batch_device(opq, Bq.data_ptr(), Xq.data_ptr(), nr, prq, tol=TOL)
+            conv = conv and all(i["flag"] == 0 for i in inf)
+            worst = max(worst, max(i["relres"] for i in inf))
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    nrhs = sum(nr for (_, _, _, nr, _) in parts)
+    out["plates32_512rhs"] = {"ms_total": ms, "ms_per_rhs": ms / nrhs, "rhs": nrhs, "particles": len(parts),
+                              "dipoles": int(sum(nv for (_, _, _, _, nv) in parts)), "setup_ms": setup,
+                              "converged": conv, "max_relres": worst}
+    return out
+
+
 def run_ours(args):
     import torch
     rank = _env_int("RANK", 0)
@@ -335,6 +409,8 @@ def run_ours(args):
               "prec_apply_ms": sum(pc_ms), "prec_passes_ms": pc_ms,
               "prec_GBps": sum(pc_bytes) / (sum(pc_ms) * 1e-3) / 1e9}
 
+    batched = _batched(api, ctx, stream, p, op, prec, max(1, min(args.steps, 2))) if not args.no_batched else None
+
     line = {"metric": METRIC, "value": ms_mixed, "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64 (FP64 refinement, dots, norms)",
@@ -347,7 +423,7 @@ def run_ours(args):
             "roofline": roof, "matvec": matvec,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(b_pin.numel() * 16 * 2),
                     "d2h_bytes_per_step": int(x_pin.numel() * 16)},
-            "gpu_launches": launches * args.steps, "clocks": clk.summary()}
+            "gpu_launches": launches * args.steps, "clocks": clk.summary(), "batched": batched}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         workers = os.cpu_count() or 1
         A, Pm, b = _cpu_oracle_setup(p, workers)
@@ -398,6 +474,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched (16- and 512-rhs) measurements")
     ap.add_argument("--mode", default="solve", choices=["solve", "passes"],
                     help="passes: only build the operator/preconditioner and time each pipeline launch "
                          "(a short command for ncu captures)")
