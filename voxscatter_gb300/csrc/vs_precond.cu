@@ -268,54 +268,58 @@ __global__ void __launch_bounds__(256) k_block_gemv(cplx_t<T>* __restrict__ t, c
   }
 }
 
-// Quadrant-symmetric apply: CTA (blockIdx.x, blockIdx.y) owns stored blocks
-// is = blockIdx.x*ti + il (il < ti), js = blockIdx.y, and applies each one to
-// the up to four frequencies (is, js), (L-is, js), (is, M-js), (L-is, M-js)
-// that share it, so every stored block is read from memory once per apply.
-// Variant v has flips fx = v&1, fy = v>>1 (negate the x / y component entries
-// of the input and of the output).
-// PAIR (c64 with even n): each thread forms two adjacent rows from 16-byte
-// loads of column entries (r, r+1).
-template <typename T, bool PAIR>
+// Quadrant-symmetric apply: CTA (blockIdx.x, blockIdx.y, blockIdx.z) owns the
+// stored blocks is = blockIdx.x*ti + il (il < ti), js = blockIdx.y, and the
+// right-hand sides rhs = blockIdx.z*RG + rg (rg < RG).  Each stored block is
+// applied to the up to four frequencies (is, js), (L-is, js), (is, M-js),
+// (L-is, M-js) that share it, for all RG right-hand sides: W = 4*RG vectors
+// per block, so every element of a stored block read from memory feeds W
+// products.  Variant v has flips fx = v&1, fy = v>>1 (negate the x / y
+// component entries of the input and of the output).
+template <typename T, bool PAIR, int RG>
 __global__ void __launch_bounds__(256) k_block_gemv_sym(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ inv,
-                                                        int L, int M, int N, int ti, int64_t rhs_stride,
+                                                        int L, int M, int N, int ti, int64_t rhs_stride, int nrhs,
                                                         const int* skip, int skip_stride) {
   using C = cplx_t<T>;
-  if (skip && skip[blockIdx.z * skip_stride]) return;
+  constexpr int W = 4 * RG;
+  const int rhs0 = blockIdx.z * RG;
+  const int nr = min(RG, nrhs - rhs0);
+  if (skip) {
+    bool all = true;
+    for (int g = 0; g < nr; ++g) all = all && skip[(rhs0 + g) * skip_stride];
+    if (all) return;
+  }
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = 3 * N;
   const int Lb = L / 2 + 1;
-  C* v = reinterpret_cast<C*>(smem_raw);  // [il][variant][n]
-  C* o = v + ti * 4 * n;
+  C* v = reinterpret_cast<C*>(smem_raw);  // [il][col = rg*4 + variant][n]
+  C* o = v + ti * W * n;
   const int is0 = blockIdx.x * ti, js = blockIdx.y;
-  C* tt = t + (int64_t)blockIdx.z * rhs_stride;
   const int64_t LM = (int64_t)L * M;
   const bool jmir = (js != 0) && (2 * js != M);
-  for (int u = threadIdx.x; u < ti * 4 * n; u += blockDim.x) {
+  for (int u = threadIdx.x; u < ti * W * n; u += blockDim.x) {
     const int s = u % n;
     const int rest = u / n;
-    const int var = rest & 3, il = rest >> 2;
+    const int col = rest % W, il = rest / W;
+    const int var = col & 3, rg = col >> 2;
     const int is = is0 + il;
     const bool imir = (is != 0) && (2 * is != L);
     const bool fx = var & 1, fy = var >> 1;
     C val = czero<C>();
-    if (is < Lb && (!fx || imir) && (!fy || jmir)) {
+    if (is < Lb && rg < nr && (!fx || imir) && (!fy || jmir)) {
       const int i = fx ? L - is : is, j = fy ? M - js : js;
-      val = tt[i + (int64_t)L * j + LM * s];
+      val = t[(int64_t)(rhs0 + rg) * rhs_stride + i + (int64_t)L * j + LM * s];
       const int comp = s / N;
       if ((comp == 0 && fx) != (comp == 1 && fy)) { val.x = -val.x; val.y = -val.y; }
     }
     v[u] = val;
   }
   __syncthreads();
-  auto put = [&](int il, int r, C a0, C a1, C a2, C a3) {
-    const int comp = r / N;
-    const int o0 = il * 4 * n + r;
-    // variant flips of the output rows
-    o[o0] = a0;
-    o[o0 + n] = (comp == 0) ? make_c<C>(-a1.x, -a1.y) : a1;
-    o[o0 + 2 * n] = (comp == 1) ? make_c<C>(-a2.x, -a2.y) : a2;
-    o[o0 + 3 * n] = (comp == 0 || comp == 1) ? make_c<C>(-a3.x, -a3.y) : a3;
+  // output row r of column col, with the variant's output flips
+  auto put = [&](int il, int r, int col, C a) {
+    const int comp = r / N, var = col & 3;
+    const bool neg = (comp == 0 && (var & 1)) || (comp == 1 && (var >> 1));
+    o[(il * W + col) * n + r] = neg ? make_c<C>(-a.x, -a.y) : a;
   };
   if (PAIR) {
     const int h = n >> 1;
@@ -324,19 +328,26 @@ __global__ void __launch_bounds__(256) k_block_gemv_sym(cplx_t<T>* __restrict__ 
       const int is = is0 + il;
       if (is >= Lb) continue;
       const float4* A = reinterpret_cast<const float4*>(inv + ((int64_t)is + (int64_t)Lb * js) * n * n + r);
-      const C* x = v + il * 4 * n;
-      C a0 = czero<C>(), a1 = czero<C>(), a2 = czero<C>(), a3 = czero<C>();
-      C b0 = czero<C>(), b1 = czero<C>(), b2 = czero<C>(), b3 = czero<C>();
-#pragma unroll 4
+      const C* x = v + il * W * n;
+      C a[W], b[W];
+#pragma unroll
+      for (int c = 0; c < W; ++c) { a[c] = czero<C>(); b[c] = czero<C>(); }
+#pragma unroll 2
       for (int q = 0; q < n; ++q) {
         const float4 mm = __ldg(A + (int64_t)q * h);
         const C m0 = make_c<C>(mm.x, mm.y), m1 = make_c<C>(mm.z, mm.w);
-        const C x0 = x[q], x1 = x[n + q], x2 = x[2 * n + q], x3 = x[3 * n + q];
-        a0 = cfma(m0, x0, a0); a1 = cfma(m0, x1, a1); a2 = cfma(m0, x2, a2); a3 = cfma(m0, x3, a3);
-        b0 = cfma(m1, x0, b0); b1 = cfma(m1, x1, b1); b2 = cfma(m1, x2, b2); b3 = cfma(m1, x3, b3);
+#pragma unroll
+        for (int c = 0; c < W; ++c) {
+          const C xv = x[c * n + q];
+          a[c] = cfma(m0, xv, a[c]);
+          b[c] = cfma(m1, xv, b[c]);
+        }
       }
-      put(il, r, a0, a1, a2, a3);
-      put(il, r + 1, b0, b1, b2, b3);
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        put(il, r, c, a[c]);
+        put(il, r + 1, c, b[c]);
+      }
     }
   } else {
     for (int rr = threadIdx.x; rr < ti * n; rr += blockDim.x) {
@@ -344,30 +355,32 @@ __global__ void __launch_bounds__(256) k_block_gemv_sym(cplx_t<T>* __restrict__ 
       const int is = is0 + il;
       if (is >= Lb) continue;
       const C* A = inv + ((int64_t)is + (int64_t)Lb * js) * n * n + r;
-      const C* x = v + il * 4 * n;
-      C a0 = czero<C>(), a1 = czero<C>(), a2 = czero<C>(), a3 = czero<C>();
-#pragma unroll 4
+      const C* x = v + il * W * n;
+      C a[W];
+#pragma unroll
+      for (int c = 0; c < W; ++c) a[c] = czero<C>();
+#pragma unroll 2
       for (int q = 0; q < n; ++q) {
         const C m = __ldg(A + (int64_t)q * n);
-        a0 = cfma(m, x[q], a0);
-        a1 = cfma(m, x[n + q], a1);
-        a2 = cfma(m, x[2 * n + q], a2);
-        a3 = cfma(m, x[3 * n + q], a3);
+#pragma unroll
+        for (int c = 0; c < W; ++c) a[c] = cfma(m, x[c * n + q], a[c]);
       }
-      put(il, r, a0, a1, a2, a3);
+#pragma unroll
+      for (int c = 0; c < W; ++c) put(il, r, c, a[c]);
     }
   }
   __syncthreads();
-  for (int u = threadIdx.x; u < ti * 4 * n; u += blockDim.x) {
+  for (int u = threadIdx.x; u < ti * W * n; u += blockDim.x) {
     const int s = u % n;
     const int rest = u / n;
-    const int var = rest & 3, il = rest >> 2;
+    const int col = rest % W, il = rest / W;
+    const int var = col & 3, rg = col >> 2;
     const int is = is0 + il;
     const bool imir = (is != 0) && (2 * is != L);
     const bool fx = var & 1, fy = var >> 1;
-    if (is < Lb && (!fx || imir) && (!fy || jmir)) {
+    if (is < Lb && rg < nr && (!fx || imir) && (!fy || jmir)) {
       const int i = fx ? L - is : is, j = fy ? M - js : js;
-      tt[i + (int64_t)L * j + LM * s] = o[u];
+      t[(int64_t)(rhs0 + rg) * rhs_stride + i + (int64_t)L * j + LM * s] = o[u];
     }
   }
 }
@@ -428,20 +441,26 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
       const int n = 3 * N;
       if (pr.sym) {
         const int Lb = L / 2 + 1, Mb = M / 2 + 1;
-        int ti = sh.gemv_ti > 0 ? std::min(sh.gemv_ti, Lb) : std::min(Lb, 4);
-        while (ti > 1 && 2ull * ti * 4 * n * sizeof(C) > 64 * 1024) --ti;
         const int nthr = sh.gemv_threads > 0 ? sh.gemv_threads : 256;
-        const size_t smem = 2ull * ti * 4 * n * sizeof(C);
-        const dim3 grid(ceil_div(Lb, ti), Mb, nrhs);
-        if (std::is_same<T, float>::value && n % 2 == 0) {
-          auto k = k_block_gemv_sym<T, true>;
-          set_kernel_smem((const void*)k, smem);
-          k<<<grid, nthr, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip, skip_stride);
+        int ti = sh.gemv_ti > 0 ? std::min(sh.gemv_ti, Lb) : std::min(Lb, 4);
+        const bool pair = std::is_same<T, float>::value && n % 2 == 0;
+        // right-hand sides per CTA: 4 when batching, so each block element feeds 16 products
+        const int rg = nrhs >= 4 ? 4 : 1;
+        while (ti > 1 && 2ull * ti * 4 * rg * n * sizeof(C) > 96 * 1024) --ti;
+        const size_t smem = 2ull * ti * 4 * rg * n * sizeof(C);
+        const dim3 grid(ceil_div(Lb, ti), Mb, ceil_div(nrhs, rg));
+#define VS_GEMV(PR, RGV)                                                                              \
+  {                                                                                                   \
+    auto k = k_block_gemv_sym<T, PR, RGV>;                                                            \
+    set_kernel_smem((const void*)k, smem);                                                            \
+    k<<<grid, nthr, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, nrhs, skip, skip_stride); \
+  }
+        if (pair) {
+          if (rg == 4) VS_GEMV(true, 4) else VS_GEMV(true, 1)
         } else {
-          auto k = k_block_gemv_sym<T, false>;
-          set_kernel_smem((const void*)k, smem);
-          k<<<grid, nthr, smem, st>>>(t, inv, L, M, N, ti, (int64_t)L * M * N * 3, skip, skip_stride);
+          if (rg == 4) VS_GEMV(false, 4) else VS_GEMV(false, 1)
         }
+#undef VS_GEMV
         VS_LAUNCH_CHECK();
         break;
       }
