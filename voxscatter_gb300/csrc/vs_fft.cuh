@@ -279,6 +279,87 @@ struct Butterfly<9, INV, C> {
   }
 };
 
+// cos(2 pi j/R), sin(2 pi j/R) for j = 1..(R-1)/2 of the odd prime radices
+// (constant-folded once the butterfly loops are unrolled).
+template <int R> __host__ __device__ constexpr double odd_cos(int j);
+template <int R> __host__ __device__ constexpr double odd_sin(int j);
+template <> __host__ __device__ constexpr double odd_cos<7>(int j) {
+  return j == 1 ? 0.62348980185873359439 : j == 2 ? -0.22252093395631433737 : -0.90096886790241903498;
+}
+template <> __host__ __device__ constexpr double odd_sin<7>(int j) {
+  return j == 1 ? 0.78183148246802980363 : j == 2 ? 0.97492791218182361934 : 0.43388373911755823142;
+}
+template <> __host__ __device__ constexpr double odd_cos<11>(int j) {
+  return j == 1 ? 0.84125353283118120551 : j == 2 ? 0.41541501300188643508 : j == 3 ? -0.14231483827328500480 : j == 4 ? -0.65486073394528498959 : -0.95949297361449736865;
+}
+template <> __host__ __device__ constexpr double odd_sin<11>(int j) {
+  return j == 1 ? 0.54064081745559755543 : j == 2 ? 0.90963199535451833011 : j == 3 ? 0.98982144188093279524 : j == 4 ? 0.75574957435425826890 : 0.28173255684142967104;
+}
+template <> __host__ __device__ constexpr double odd_cos<13>(int j) {
+  return j == 1 ? 0.88545602565320991051 : j == 2 ? 0.56806474673115592289 : j == 3 ? 0.12053668025532300601 : j == 4 ? -0.35460488704253545489 : j == 5 ? -0.74851074817110119231 : -0.97094181742605201180;
+}
+template <> __host__ __device__ constexpr double odd_sin<13>(int j) {
+  return j == 1 ? 0.46472317204376850652 : j == 2 ? 0.82298386589365635224 : j == 3 ? 0.99270887409805397272 : j == 4 ? 0.93501624268541483342 : j == 5 ? 0.66312265824079519305 : 0.23931566428755768339;
+}
+
+// Odd prime R by symmetric pairs: with s_r = v_r + v_{R-r}, d_r = v_r - v_{R-r},
+//   out[k], out[R-k] = v_0 + sum_r cos(2 pi rk/R) s_r  -/+  i sum_r sin(2 pi rk/R) d_r
+// (signs swapped for the inverse): (R-1)^2 real multiply-adds per R points
+// instead of (R-1)^2 complex ones.
+template <int R, bool INV, typename C>
+struct OddButterfly {
+  __device__ __forceinline__ static void run(C* v) {
+    using T = decltype(v[0].x);
+    constexpr int h = (R - 1) / 2;
+    C sp[h], dm[h];
+    C sum = v[0];
+#pragma unroll
+    for (int r = 0; r < h; ++r) {
+      sp[r] = cadd(v[r + 1], v[R - 1 - r]);
+      dm[r] = csub(v[r + 1], v[R - 1 - r]);
+      sum = cadd(sum, sp[r]);
+    }
+    C out[R];
+    out[0] = sum;
+#pragma unroll
+    for (int k = 1; k <= h; ++k) {
+      C re = v[0];
+      T imx = 0, imy = 0;
+#pragma unroll
+      for (int r = 1; r <= h; ++r) {
+        const int m = (r * k) % R;
+        const T ct = (T)(m <= h ? odd_cos<R>(m) : odd_cos<R>(R - m));
+        const T st = (T)(m <= h ? odd_sin<R>(m) : -odd_sin<R>(R - m));
+        re.x += ct * sp[r - 1].x;
+        re.y += ct * sp[r - 1].y;
+        imx += st * dm[r - 1].x;
+        imy += st * dm[r - 1].y;
+      }
+      // forward: out[k] = re - i*im, out[R-k] = re + i*im ; inverse: swapped
+      C a, b;
+      a.x = re.x + imy; a.y = re.y - imx;  // re - i*im
+      b.x = re.x - imy; b.y = re.y + imx;  // re + i*im
+      out[k] = INV ? b : a;
+      out[R - k] = INV ? a : b;
+    }
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = out[q];
+  }
+};
+
+template <bool INV, typename C>
+struct Butterfly<7, INV, C> {
+  __device__ __forceinline__ static void run(C* v, const C*, int) { OddButterfly<7, INV, C>::run(v); }
+};
+template <bool INV, typename C>
+struct Butterfly<11, INV, C> {
+  __device__ __forceinline__ static void run(C* v, const C*, int) { OddButterfly<11, INV, C>::run(v); }
+};
+template <bool INV, typename C>
+struct Butterfly<13, INV, C> {
+  __device__ __forceinline__ static void run(C* v, const C*, int) { OddButterfly<13, INV, C>::run(v); }
+};
+
 // Compile-time-size DFT for the remaining small primes, roots read from the
 // length-n twiddle table: w_R^k = tw[k*n/R].
 template <int R, bool INV, typename C>
