@@ -273,6 +273,18 @@ int vs_cext_grad(vs_op* op, vs_prec* prec, const double* Einc, const double* eps
 
 /* ---- diagnostics ----------------------------------------------------- */
 
+/* Launch shape of an operator's pipeline in one precision, as chosen by the
+ * autotuner at creation (log2 values, -1 = built-in default).  Setting it pins
+ * the shape, e.g. for reproducible timings. */
+typedef struct vs_shape {
+  int lg_lines_x;  /* x passes: log2 lines per CTA                                 */
+  int lg_tile_y;   /* y passes: log2 x-tile width                                  */
+  int lg_tile_z;   /* z pass (shared-memory kernel): log2 x-tile width             */
+  int z_reg;       /* c64 z pass: 1 register-resident lines, 0 shared memory        */
+} vs_shape;
+int vs_op_get_shape(const vs_op* op, int precision, vs_shape* shape);
+int vs_op_set_shape(vs_op* op, int precision, const vs_shape* shape);
+
 /* Time each of the 5 launches of one apply (matvec: X-forward gather, Y
  * forward, Z FFT x tensor x inverse, Y inverse, X inverse + diagonal; the
  * preconditioner: X-forward gather, Y forward, block GEMV, Y inverse, X

@@ -163,3 +163,43 @@ def test_full_storage_when_parity_is_not_exact(api):
     y_o = O.MVP(x, fN, np.ones((L, M, N)), dV * chi, 1 / alpha, "notransp", idx3)
     assert rel(op.apply(x, "notransp", "c128"), y_o) < C128_TOL
     assert rel(op.apply(x, "notransp", "c64"), y_o) < C64_TOL
+
+
+@pytest.mark.parametrize("nper,diameter,aspect", [(4, 2.5, 0.5), (10, 2.0, 0.5), (6, 3.0, 0.35), (3, 2.0, 0.9)])
+def test_every_launch_shape_matches_oracle(api, nper, diameter, aspect):
+    """Both z-pass kernels (register-resident lines and shared-memory Stockham)
+    and several x/y/z tiles give the same c64 matvec as the oracle."""
+    p = W.small_hex(m=1.31 + 0.05j, diameter=diameter, nper=nper, aspect_ratio=aspect)
+    L, M, N, idx3, chi = _problem(p)
+    Toep = O.green_toeplitz(p["r"], p["ko"])
+    fN = O.fft_operator(O.circulant_nop_const(Toep))
+    alpha = O.alpha_ldr(p["refInd"], p["ko"], p["d"], p["kvec"], p["Eo"])
+    dV = p["d"] ** 3
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    rng = np.random.default_rng(N)
+    x = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
+    y_o = O.MVP(x, fN, np.ones((L, M, N)), dV * chi, 1 / alpha, "notransp", idx3)
+    for z_reg in (0, 1):
+        for lg in (1, 3):
+            op.set_shape("c64", z_reg=z_reg, lg_tile_z=lg, lg_tile_y=lg + 1, lg_lines_x=lg)
+            assert rel(op.apply(x, "notransp", "c64"), y_o) < C64_TOL, (z_reg, lg, op.PQR)
+
+
+@pytest.mark.parametrize("N", [13, 26, 27])
+def test_tall_grids_both_z_kernels(api, N):
+    """z lengths 27, 54 and 54 (5-smooth >= 2N-1): register and shared-memory z
+    passes against the oracle on a 6 x 5 x N block of voxels."""
+    from voxscatter_gb300.geometry import grid3d
+    L, M = 6, 5
+    d = 0.07
+    r = grid3d(np.arange(L) * d, np.arange(M) * d, np.arange(N) * d)
+    ko = 2 * np.pi
+    Toep = O.green_toeplitz(r, ko)
+    fN = O.fft_operator(O.circulant_nop_const(Toep))
+    idx3 = np.arange(3 * L * M * N)
+    op = api.Operator(L, M, N, idx3, 1.0, d ** 3, 3.0, toep=Toep)
+    x = np.random.default_rng(N).normal(size=idx3.size) + 1j * np.random.default_rng(N + 1).normal(size=idx3.size)
+    y_o = O.MVP(x, fN, np.ones((L, M, N)), d ** 3, 3.0, "notransp", idx3)
+    for z_reg in (0, 1):
+        op.set_shape("c64", z_reg=z_reg)
+        assert rel(op.apply(x, "notransp", "c64"), y_o) < C64_TOL, (z_reg, op.PQR)

@@ -166,6 +166,18 @@ class Operator:
                                                 L.VS_C64 if precision == "c64" else L.VS_C128, nrep, out), self.ctx.h)
         return list(out)
 
+    def shape(self, precision="c64"):
+        sh = L.vs_shape()
+        L.check(self.ctx._lib.vs_op_get_shape(self.h, L.VS_C64 if precision == "c64" else L.VS_C128, C.byref(sh)))
+        return dict(lg_lines_x=sh.lg_lines_x, lg_tile_y=sh.lg_tile_y, lg_tile_z=sh.lg_tile_z, z_reg=sh.z_reg)
+
+    def set_shape(self, precision="c64", **kw):
+        cur = self.shape(precision)
+        cur.update(kw)
+        sh = L.vs_shape(**cur)
+        L.check(self.ctx._lib.vs_op_set_shape(self.h, L.VS_C64 if precision == "c64" else L.VS_C128, C.byref(sh)),
+                self.ctx.h)
+
     def close(self):
         if getattr(self, "h", None):
             self.ctx._lib.vs_op_destroy(self.h)

@@ -798,6 +798,41 @@ int vs_solve(vs_op* op, vs_prec* prec, const double* b, double* x, const vs_solv
 
 // ---- diagnostics ----------------------------------------------------------
 
+int vs_op_get_shape(const vs_op* op, int precision, vs_shape* shape) {
+  if (!op || !shape || (precision != VS_C64 && precision != VS_C128)) return VS_ERR_ARG;
+  const vs::PassShape& s = op->shape[precision == VS_C64 ? 0 : 1];
+  shape->lg_lines_x = s.lg_lpb_x;
+  shape->lg_tile_y = s.lg_tx_y;
+  shape->lg_tile_z = s.lg_tx_z;
+  shape->z_reg = s.z_reg;
+  return VS_OK;
+}
+
+int vs_op_set_shape(vs_op* op, int precision, const vs_shape* shape) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(shape && (precision == VS_C64 || precision == VS_C128), "bad argument");
+    const size_t cs = precision == VS_C64 ? sizeof(float2) : sizeof(double2);
+    const size_t lim = 227 * 1024;
+    VS_REQUIRE(shape->lg_lines_x >= -1 && shape->lg_lines_x <= 8, "lg_lines_x out of range");
+    VS_REQUIRE(shape->lg_tile_y >= -1 && shape->lg_tile_y <= 8, "lg_tile_y out of range");
+    VS_REQUIRE(shape->lg_tile_z >= -1 && shape->lg_tile_z <= 8, "lg_tile_z out of range");
+    VS_REQUIRE(shape->lg_lines_x < 0 || (2ull * (1 << shape->lg_lines_x) * op->P + op->P) * cs <= lim,
+               "x tile exceeds shared memory");
+    VS_REQUIRE(shape->lg_tile_y < 0 || (2ull * op->Q * (1 << shape->lg_tile_y) + op->Q) * cs <= lim,
+               "y tile exceeds shared memory");
+    VS_REQUIRE(shape->lg_tile_z < 0 || (2ull * op->R * 3 * (1 << shape->lg_tile_z) + op->R) * cs <= lim,
+               "z tile exceeds shared memory");
+    vs::PassShape& s = op->shape[precision == VS_C64 ? 0 : 1];
+    s.lg_lpb_x = shape->lg_lines_x;
+    s.lg_tx_y = shape->lg_tile_y;
+    s.lg_tx_z = shape->lg_tile_z;
+    s.z_reg = shape->z_reg;
+    op->kw.graph32.reset();
+    op->kw.graph64.reset();
+  });
+}
+
 int vs_op_time_passes(vs_op* op, const void* x, void* y, int64_t nrhs, int precision, int nrep, float* ms_out) {
   if (!op) return VS_ERR_ARG;
   return guarded(op->ctx, [&] {

@@ -49,6 +49,7 @@ struct PassShape {
   int lg_tx_z = -1;    // z pass: x-tile width
   int gemv_ti = 0;     // preconditioner GEMV: stored blocks per CTA (0 = default)
   int gemv_threads = 0;
+  int z_reg = -1;      // c64 z pass: 1 register-resident lines, 0 shared-memory Stockham, -1 default
 };
 
 // Work vectors and device scalars of the Krylov solvers (vs_krylov.cu).

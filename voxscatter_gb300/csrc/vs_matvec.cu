@@ -362,6 +362,34 @@ static PipeArgs<T> pipe_args(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, 
   return a;
 }
 
+// z pass: the register-resident kernel for c64 with a first-octant spectrum
+// when the operator's shape selects it (and R has one), else the shared-memory
+// Stockham kernel.
+template <typename T>
+static void launch_z(const vs_op& op, const PipeArgs<T>& a, int nrhs, cudaStream_t st) {
+  using C = cplx_t<T>;
+  if constexpr (std::is_same<T, float>::value) {
+    if (op.gsym && op.shape[0].z_reg == 1 && z_pass_reg(a, nrhs, st)) return;
+  }
+  const int tx = 1 << a.lg_tx;
+  dim3 grid(ceil_div(op.P, tx), op.Q, nrhs);
+  const size_t smem = (2ull * op.R * 3 * tx + op.R) * sizeof(C);
+  const bool small = plan_is_small_radix(a.pR);
+#define VS_Z(SM, SY)                   \
+  {                                    \
+    auto k = k_z<T, SM, SY>;           \
+    set_smem(k, smem);                 \
+    k<<<grid, kThreads, smem, st>>>(a);\
+  }
+  if (op.gsym) {
+    if (small) VS_Z(true, true) else VS_Z(false, true)
+  } else {
+    if (small) VS_Z(true, false) else VS_Z(false, false)
+  }
+#undef VS_Z
+  VS_LAUNCH_CHECK();
+}
+
 template <typename T>
 void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
                  cudaStream_t st, int pass, int skip_stride) {
@@ -371,26 +399,7 @@ void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, in
   switch (pass) {
     case 0: launch_x_pass<T>(a, false, mode, nrhs, st); break;
     case 1: launch_strided_pass<T, false>(y_pass_args<T>(op, a, false), op.N * 3, nrhs, st); break;
-    case 2: {
-      const int tx = 1 << a.lg_tx;
-      dim3 grid(ceil_div(op.P, tx), op.Q, nrhs);
-      const size_t smem = (2ull * op.R * 3 * tx + op.R) * sizeof(C);
-      const bool small = plan_is_small_radix(a.pR);
-#define VS_Z(SM, SY)                   \
-  {                                    \
-    auto k = k_z<T, SM, SY>;           \
-    set_smem(k, smem);                 \
-    k<<<grid, kThreads, smem, st>>>(a);\
-  }
-      if (op.gsym) {
-        if (small) VS_Z(true, true) else VS_Z(false, true)
-      } else {
-        if (small) VS_Z(true, false) else VS_Z(false, false)
-      }
-#undef VS_Z
-      VS_LAUNCH_CHECK();
-      break;
-    }
+    case 2: launch_z<T>(op, a, nrhs, st); break;
     case 3: launch_strided_pass<T, true>(y_pass_args<T>(op, a, true), op.N * 3, nrhs, st); break;
     default: launch_x_pass<T>(a, true, mode, nrhs, st); break;
   }
@@ -421,26 +430,7 @@ void matvec_scratch(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs,
   launch_x_pass<T>(a, false, mode, nrhs, st);
   StridedArgs<T> yf = y_pass_args<T>(op, a, false);
   launch_strided_pass<T, false>(yf, op.N * 3, nrhs, st);
-  {
-    using C = cplx_t<T>;
-    const int tx = 1 << a.lg_tx;
-    dim3 grid(ceil_div(op.P, tx), op.Q, nrhs);
-    const size_t smem = (2ull * op.R * 3 * tx + op.R) * sizeof(C);
-    const bool small = plan_is_small_radix(a.pR);
-#define VS_Z2(SM, SY)                  \
-  {                                    \
-    auto k = k_z<T, SM, SY>;           \
-    set_smem(k, smem);                 \
-    k<<<grid, kThreads, smem, st>>>(a);\
-  }
-    if (op.gsym) {
-      if (small) VS_Z2(true, true) else VS_Z2(false, true)
-    } else {
-      if (small) VS_Z2(true, false) else VS_Z2(false, false)
-    }
-#undef VS_Z2
-    VS_LAUNCH_CHECK();
-  }
+  launch_z<T>(op, a, nrhs, st);
   StridedArgs<T> yi = y_pass_args<T>(op, a, true);
   launch_strided_pass<T, true>(yi, op.N * 3, nrhs, st);
   launch_x_pass<T>(a, true, mode, nrhs, st);
@@ -570,8 +560,16 @@ void autotune_op(vs_op& op, cudaStream_t st) {
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 1);
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 3);
           });
+  sh.z_reg = 0;
   best_of(&sh.lg_tx_z, 1, 5, [&](int v) { return (2ull * op.R * 3 * (1 << v) + op.R) * cs <= lim; },
           [&] { matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 2); });
+  if (std::is_same<T, float>::value && op.gsym) {
+    // the shared-memory kernel with its best tile against the register kernel
+    const float t_smem = time_ms(st, reps, [&] { matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 2); });
+    sh.z_reg = 1;
+    const float t_reg = time_ms(st, reps, [&] { matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 2); });
+    sh.z_reg = t_reg < t_smem ? 1 : 0;
+  }
   VS_CUDA(cudaStreamSynchronize(st));
 }
 template void autotune_op<float>(vs_op&, cudaStream_t);

@@ -56,6 +56,9 @@ struct StridedArgs {
   int skip_stride;
 };
 
+// Register-resident z pass (vs_zreg.cu); false when R has no register kernel.
+bool z_pass_reg(const PipeArgs<float>& a, int nrhs, cudaStream_t st);
+
 template <typename T>
 void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaStream_t st);
 template <typename T, bool INV>

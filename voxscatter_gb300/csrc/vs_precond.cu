@@ -282,6 +282,7 @@ __global__ void __launch_bounds__(256) k_block_gemv_sym(cplx_t<T>* __restrict__ 
                                                         const int* skip, int skip_stride) {
   using C = cplx_t<T>;
   constexpr int W = 4 * RG;
+  constexpr int UNR = RG == 1 ? 4 : 2;  // column loads kept in flight per thread
   const int rhs0 = blockIdx.z * RG;
   const int nr = min(RG, nrhs - rhs0);
   if (skip) {
@@ -332,7 +333,7 @@ __global__ void __launch_bounds__(256) k_block_gemv_sym(cplx_t<T>* __restrict__ 
       C a[W], b[W];
 #pragma unroll
       for (int c = 0; c < W; ++c) { a[c] = czero<C>(); b[c] = czero<C>(); }
-#pragma unroll 2
+#pragma unroll UNR
       for (int q = 0; q < n; ++q) {
         const float4 mm = __ldg(A + (int64_t)q * h);
         const C m0 = make_c<C>(mm.x, mm.y), m1 = make_c<C>(mm.z, mm.w);
@@ -359,7 +360,7 @@ __global__ void __launch_bounds__(256) k_block_gemv_sym(cplx_t<T>* __restrict__ 
       C a[W];
 #pragma unroll
       for (int c = 0; c < W; ++c) a[c] = czero<C>();
-#pragma unroll 2
+#pragma unroll UNR
       for (int q = 0; q < n; ++q) {
         const C m = __ldg(A + (int64_t)q * n);
 #pragma unroll
