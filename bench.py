@@ -460,9 +460,27 @@ def run_passes(args):
     xs = torch.randn(op.n3, dtype=torch.complex64, device="cuda")
     ys = torch.empty_like(xs)
     torch.cuda.synchronize()
-    out = {"fft_grid": op.PQR,
+    out = {"fft_grid": op.PQR, "op_shape": op.shape("c64"), "prec_shape": prec.shape("c64"),
            "matvec_c64_ms": op.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", args.steps),
            "prec_c64_ms": prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", args.steps)}
+    if args.sweep:
+        tuned_op, tuned_pr = op.shape("c64"), prec.shape("c64")
+        zs = {}
+        for z_reg in (0, 1):
+            for lg in (2, 3, 4, 5):
+                op.set_shape("c64", z_reg=z_reg, lg_tile_z=lg)
+                zs[f"z_reg={z_reg},lg_tile_z={lg}"] = op.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64",
+                                                                     args.steps)[2]
+        op.set_shape("c64", **tuned_op)
+        gs = {}
+        for b in (1, 2, 4):
+            for th in (64, 128, 256):
+                prec.set_shape("c64", gemv_blocks=b, gemv_threads=th)
+                gs[f"blocks={b},threads={th}"] = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64",
+                                                                  args.steps)[2]
+        prec.set_shape("c64", **tuned_pr)
+        out["z_pass_ms"] = zs
+        out["gemv_ms"] = gs
     print(json.dumps(out), flush=True)
     return 0
 
@@ -475,6 +493,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (16- and 512-rhs) measurements")
+    ap.add_argument("--sweep", action="store_true", help="passes mode: also time every z-pass and GEMV shape")
     ap.add_argument("--mode", default="solve", choices=["solve", "passes"],
                     help="passes: only build the operator/preconditioner and time each pipeline launch "
                          "(a short command for ncu captures)")

@@ -285,6 +285,17 @@ typedef struct vs_shape {
 int vs_op_get_shape(const vs_op* op, int precision, vs_shape* shape);
 int vs_op_set_shape(vs_op* op, int precision, const vs_shape* shape);
 
+/* Launch shape of a preconditioner apply: x/y tiles of its FFT passes and the
+ * block GEMV's stored blocks per CTA and threads per CTA (0 = default). */
+typedef struct vs_prec_shape {
+  int lg_lines_x;
+  int lg_tile_y;
+  int gemv_blocks;
+  int gemv_threads;
+} vs_prec_shape;
+int vs_prec_get_shape(const vs_prec* prec, int precision, vs_prec_shape* shape);
+int vs_prec_set_shape(vs_prec* prec, int precision, const vs_prec_shape* shape);
+
 /* Time each of the 5 launches of one apply (matvec: X-forward gather, Y
  * forward, Z FFT x tensor x inverse, Y inverse, X inverse + diagonal; the
  * preconditioner: X-forward gather, Y forward, block GEMV, Y inverse, X

@@ -72,7 +72,13 @@ class vs_shape(C.Structure):
     _fields_ = [("lg_lines_x", C.c_int), ("lg_tile_y", C.c_int), ("lg_tile_z", C.c_int), ("z_reg", C.c_int)]
 
 
+class vs_prec_shape(C.Structure):
+    _fields_ = [("lg_lines_x", C.c_int), ("lg_tile_y", C.c_int), ("gemv_blocks", C.c_int), ("gemv_threads", C.c_int)]
+
+
 SIGNATURES.update({
+    "vs_prec_get_shape": (C.c_int, [_vp, C.c_int, C.POINTER(vs_prec_shape)]),
+    "vs_prec_set_shape": (C.c_int, [_vp, C.c_int, C.POINTER(vs_prec_shape)]),
     "vs_op_get_shape": (C.c_int, [_vp, C.c_int, C.POINTER(vs_shape)]),
     "vs_op_set_shape": (C.c_int, [_vp, C.c_int, C.POINTER(vs_shape)]),
     "vs_solve_batch": (C.c_int, [_vp, _vp, _pd, _pd, _i64, C.POINTER(vs_solve_opts), C.POINTER(vs_solve_info)]),

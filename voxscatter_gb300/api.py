@@ -293,6 +293,20 @@ class Preconditioner:
                 self.ctx.h)
         return list(out)
 
+    def shape(self, precision="c64"):
+        sh = L.vs_prec_shape()
+        L.check(self.ctx._lib.vs_prec_get_shape(self.h, L.VS_C64 if precision == "c64" else L.VS_C128,
+                                                C.byref(sh)))
+        return dict(lg_lines_x=sh.lg_lines_x, lg_tile_y=sh.lg_tile_y, gemv_blocks=sh.gemv_blocks,
+                    gemv_threads=sh.gemv_threads)
+
+    def set_shape(self, precision="c64", **kw):
+        cur = self.shape(precision)
+        cur.update(kw)
+        sh = L.vs_prec_shape(**cur)
+        L.check(self.ctx._lib.vs_prec_set_shape(self.h, L.VS_C64 if precision == "c64" else L.VS_C128,
+                                                C.byref(sh)), self.ctx.h)
+
     def blocks(self, Lx, My, Nz, precision="c128"):
         n = 3 * Nz
         out = np.zeros(Lx * My * n * n, dtype=np.complex128)

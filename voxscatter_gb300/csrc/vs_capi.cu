@@ -808,6 +808,40 @@ int vs_op_get_shape(const vs_op* op, int precision, vs_shape* shape) {
   return VS_OK;
 }
 
+int vs_prec_get_shape(const vs_prec* prec, int precision, vs_prec_shape* shape) {
+  if (!prec || !shape || (precision != VS_C64 && precision != VS_C128)) return VS_ERR_ARG;
+  const vs::PassShape& s = prec->shape[precision == VS_C64 ? 0 : 1];
+  shape->lg_lines_x = s.lg_lpb_x;
+  shape->lg_tile_y = s.lg_tx_y;
+  shape->gemv_blocks = s.gemv_ti;
+  shape->gemv_threads = s.gemv_threads;
+  return VS_OK;
+}
+
+int vs_prec_set_shape(vs_prec* prec, int precision, const vs_prec_shape* shape) {
+  if (!prec) return VS_ERR_ARG;
+  return guarded(prec->ctx, [&] {
+    VS_REQUIRE(shape && (precision == VS_C64 || precision == VS_C128), "bad argument");
+    const size_t cs = precision == VS_C64 ? sizeof(float2) : sizeof(double2);
+    const size_t lim = 227 * 1024;
+    VS_REQUIRE(shape->lg_lines_x >= -1 && shape->lg_lines_x <= 8 && shape->lg_tile_y >= -1 && shape->lg_tile_y <= 8,
+               "tile out of range");
+    VS_REQUIRE(shape->lg_lines_x < 0 || (2ull * (1 << shape->lg_lines_x) * prec->L + prec->L) * cs <= lim,
+               "x tile exceeds shared memory");
+    VS_REQUIRE(shape->lg_tile_y < 0 || (2ull * prec->M * (1 << shape->lg_tile_y) + prec->M) * cs <= lim,
+               "y tile exceeds shared memory");
+    VS_REQUIRE(shape->gemv_blocks >= 0 && shape->gemv_blocks <= 64, "gemv_blocks out of range");
+    VS_REQUIRE(shape->gemv_threads == 0 || (shape->gemv_threads >= 32 && shape->gemv_threads <= 256 &&
+                                            shape->gemv_threads % 32 == 0),
+               "gemv_threads must be 0 or a multiple of 32 in [32, 256]");
+    vs::PassShape& s = prec->shape[precision == VS_C64 ? 0 : 1];
+    s.lg_lpb_x = shape->lg_lines_x;
+    s.lg_tx_y = shape->lg_tile_y;
+    s.gemv_ti = shape->gemv_blocks;
+    s.gemv_threads = shape->gemv_threads;
+  });
+}
+
 int vs_op_set_shape(vs_op* op, int precision, const vs_shape* shape) {
   if (!op) return VS_ERR_ARG;
   return guarded(op->ctx, [&] {
