@@ -117,3 +117,27 @@ def test_prec_full_storage_when_parity_is_not_exact(api):
     assert rel(pr.blocks(L, M, N, "c128"), inv_o) < 1e-10
     x = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
     assert rel(pr.apply(x, "c128"), O.mvp_circ_2_level(inv_o, x, L, M, N, idx3)) < 1e-10
+
+
+@pytest.mark.parametrize("N,L,M", [(48, 5, 6), (64, 6, 5)])
+def test_prec_large_blocks(api, N, L, M):
+    """3N x 3N blocks beyond the shared-memory inversion: n = 144 inverts in
+    FP32 in shared memory and in FP64 with the blocked global-memory kernel;
+    n = 192 (the 256x256x64 snowflake's block size) uses the blocked kernel in
+    both precisions.  Largest block condition number here is about 115."""
+    p = W.config5(level=2, L=L, M=M, N=N, layers=N - 8)
+    L, M, N, idx3, Toep, alpha, dV = _setup(p)
+    _, c1_o = O.circ_1_level(Toep, L, M, N, 0, "off")
+    _, blk_o = O.circ_2_level(c1_o, L, M, N)
+    inv_o = O.invert_blocks(blk_o, 1 / alpha, dV)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
+    assert rel(pr.blocks(L, M, N, "c128"), inv_o) < 1e-10
+    assert rel(pr.blocks(L, M, N, "c64"), inv_o) < 1e-4
+    _, blk = api.circ_2_level(api.circ_1_level(Toep, L, M, N, 0, "off")[1], L, M, N, opToeplitz=Toep)
+    assert rel(blk, blk_o) < 1e-12
+    rng = np.random.default_rng(5)
+    x = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
+    y_o = O.mvp_circ_2_level(inv_o, x, L, M, N, idx3)
+    assert rel(pr.apply(x, "c128"), y_o) < 1e-10
+    assert rel(pr.apply(x, "c64"), y_o) < 1e-4

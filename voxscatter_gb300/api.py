@@ -363,7 +363,7 @@ def solve(op, b, prec=None, tol=1e-6, maxit=2000, precision="mixed", x0=None, in
 
 
 def solve_device(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="mixed", inner_tol=0.0,
-                 max_refine=10, iters_per_graph=4):
+                 max_refine=10, iters_per_graph=4, method="bicgstab", restart=50):
     """vs_solve_device on device buffers (double2, n3 each); returns the info dict."""
     lib = op.ctx._lib
     o = L.vs_solve_opts()
@@ -371,6 +371,8 @@ def solve_device(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="m
     o.precision = L.VS_SOLVE_MIXED if precision == "mixed" else L.VS_SOLVE_FP64
     o.tol = float(tol); o.maxit = int(maxit); o.inner_tol = float(inner_tol); o.max_refine = int(max_refine)
     o.iters_per_graph = int(iters_per_graph)
+    o.method = L.VS_GMRES if method == "gmres" else L.VS_BICGSTAB
+    o.restart = int(restart)
     info = L.vs_solve_info()
     L.check(lib.vs_solve_device(op.h, prec.h if prec is not None else None, C.c_void_p(b_ptr), C.c_void_p(x_ptr),
                                 C.byref(o), C.byref(info)), op.ctx.h)
@@ -378,13 +380,16 @@ def solve_device(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="m
                 time_ms=info.time_ms, launches=info.kernel_launches)
 
 
-def solve_host_ptr(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="mixed", iters_per_graph=4):
+def solve_host_ptr(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="mixed", iters_per_graph=4,
+                   method="bicgstab", restart=50):
     """vs_solve on host buffers given as raw pointers (e.g. pinned torch tensors)."""
     lib = op.ctx._lib
     o = L.vs_solve_opts()
     lib.vs_solve_opts_default(C.byref(o))
     o.precision = L.VS_SOLVE_MIXED if precision == "mixed" else L.VS_SOLVE_FP64
     o.tol = float(tol); o.maxit = int(maxit); o.iters_per_graph = int(iters_per_graph)
+    o.method = L.VS_GMRES if method == "gmres" else L.VS_BICGSTAB
+    o.restart = int(restart)
     info = L.vs_solve_info()
     L.check(lib.vs_solve(op.h, prec.h if prec is not None else None, C.cast(C.c_void_p(b_ptr), L._pd),
                          C.cast(C.c_void_p(x_ptr), L._pd), C.byref(o), C.byref(info)), op.ctx.h)

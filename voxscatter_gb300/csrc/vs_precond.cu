@@ -80,6 +80,28 @@ __host__ __device__ __forceinline__ double2 crecip(double2 a) {
   return make_double2(a.x / d, -a.y / d);
 }
 
+// Entry (p, q) of block (i, j): shift*[p==q] - d_p * C_ij(p, q), where C_ij is
+// the 3x3 arrangement of N x N Toeplitz pieces of circ_2_level.m:82-154 (the
+// (a, b) piece uses component comp_pair(a, b); entries above the diagonal of
+// an xz / yz piece change sign).
+__device__ __forceinline__ double2 block_entry(const double2* __restrict__ lev2, int L, int M, int N, int i, int j, int p,
+                                               int q, double2 shift, const double2* __restrict__ dvec, double2 dscal) {
+  const int a = p / N, zp = p - a * N, b = q / N, zq = q - b * N;
+  const int c = comp_pair(a, b);
+  const bool negcol = (a == 2) != (b == 2);
+  int dz = zp - zq;
+  double sg = 1.0;
+  if (dz < 0) dz = -dz;
+  else if (negcol && dz > 0) sg = -1.0;
+  const double2 v = lev2[i + (int64_t)L * (j + (int64_t)M * (dz + (int64_t)N * c))];
+  const double2 dd = dvec ? dvec[p] : dscal;
+  double2 e = cmul(dd, v);
+  e.x *= -sg;
+  e.y *= -sg;
+  if (p == q) { e.x += shift.x; e.y += shift.y; }
+  return e;
+}
+
 // One CTA per block (i, j) = (blockIdx.x, blockIdx.y).  With invert = false
 // the assembled matrix is stored as is (used to return circ_2_level's blocks).
 template <typename T>
@@ -99,20 +121,7 @@ __global__ void __launch_bounds__(256) k_assemble_invert(const double2* __restri
   const int i = blockIdx.x, j = blockIdx.y;
   for (int u = threadIdx.x; u < n * n; u += blockDim.x) {
     const int p = u / n, q = u - p * n;
-    const int a = p / N, zp = p - a * N, b = q / N, zq = q - b * N;
-    const int c = comp_pair(a, b);
-    const bool negcol = (a == 2) != (b == 2);
-    int dz = zp - zq;
-    double sg = 1.0;
-    if (dz < 0) dz = -dz;
-    else if (negcol && dz > 0) sg = -1.0;
-    const double2 v = lev2[i + (int64_t)L * (j + (int64_t)M * (dz + (int64_t)N * c))];
-    const double2 dd = dvec ? dvec[p] : dscal;
-    double2 e = cmul(dd, v);
-    e.x *= -sg;
-    e.y *= -sg;
-    if (p == q) { e.x += shift.x; e.y += shift.y; }
-    A[u] = ccast<C>(e);
+    A[u] = ccast<C>(block_entry(lev2, L, M, N, i, j, p, q, shift, dvec, dscal));
   }
   __syncthreads();
   if (invert) {
@@ -187,16 +196,264 @@ size_t assemble_smem(int N, size_t csize) {
   return (size_t)n * n * csize + n * csize + n * sizeof(int) + 16;
 }
 
+// Element-wise assembly of all stored blocks, for any block size: entry (p, q)
+// of block b = i + Lb*j goes to out[b*n*n + q*n + p] (colmajor) or
+// out[b*n*n + p*n + q], times scale.
+template <typename T>
+__global__ void k_assemble(const double2* __restrict__ lev2, int L, int M, int N, double2 shift,
+                           const double2* __restrict__ dvec, double2 dscal, int colmajor, double scale,
+                           cplx_t<T>* __restrict__ out, int Lb, int Mb) {
+  const int n = 3 * N;
+  const int64_t nn = (int64_t)n * n, total = nn * Lb * Mb;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / nn;
+    const int u = (int)(e - b * nn);
+    const int hi = u / n, lo = u - hi * n;
+    const int p = colmajor ? lo : hi, q = colmajor ? hi : lo;
+    const int j = (int)(b / Lb), i = (int)(b - (int64_t)j * Lb);
+    const double2 v = block_entry(lev2, L, M, N, i, j, p, q, shift, dvec, dscal);
+    out[e] = ccast<cplx_t<T>>(make_double2(v.x * scale, v.y * scale));
+  }
+}
+
+// Blocked Gauss-Jordan inversion with partial pivoting of nmat row-major n x n
+// matrices held in global memory, one CTA per matrix at a time (persistent
+// over the batch).  For blocks too large for the shared-memory kernel.
+//
+// Columns are processed in panels of NB.  A panel (all n rows) is loaded into
+// shared memory and reduced by the unblocked in-place steps (pivot search down
+// the column among the rows not yet used, row swap, scale the pivot row,
+// eliminate the column from every other row; the eliminated column is
+// replaced by the corresponding column of the inverse).  Afterwards the panel
+// holds [A_KK^-1 ; -A_OK A_KK^-1] for the pivot rows K of the panel and the
+// other rows O, and every column c outside the panel transforms as
+//     c_new = (c with rows K zeroed) + Panel * c_K,
+// with the panel's row swaps applied to c first -- a rank-NB update done as a
+// register-tiled complex GEMM over column tiles of TQ = 16*CN.  The swaps of
+// one panel move only rows of K and rows swapped in from below the panel, and
+// a row below the panel always receives a row of K, so each column tile
+// gathers its new K rows and the changed rows below into shared memory before
+// it is overwritten.  After the last panel the column interchanges are undone
+// in one composed permutation, the result is scaled, and non-finite entries
+// or a zero pivot set status bits 2 / 1.
+template <typename T, int NB, int CN>
+__global__ void __launch_bounds__(256) k_gj_blocked(cplx_t<T>* __restrict__ mats, int n, int64_t nmat, double scale,
+                                                    int* __restrict__ status) {
+  using C = cplx_t<T>;
+  constexpr int TQ = 16 * CN, RM = 4, PS = NB + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* P = reinterpret_cast<C*>(smem_raw);  // [n][PS]
+  C* Bsw = P + (size_t)n * PS;            // [NB][TQ]  new pivot rows of a column tile
+  C* Osw = Bsw + NB * TQ;                 // [NB][TQ]  new rows below the panel that a swap changed
+  C* colk = Osw + NB * TQ;                // [n]
+  int* perm = reinterpret_cast<int*>(colk + n);
+  int* rowsrc = perm + n;  // row r of the panel's result comes from row rowsrc[r]
+  int* oidx = rowsrc + n;  // slot in Osw of a changed row below the panel, or -1
+  int* olist = oidx + n;   // [NB]
+  int* cmap = olist + NB;  // [n]
+  __shared__ int s_piv, s_ocnt;
+  __shared__ T s_pmag;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  for (int64_t b = blockIdx.x; b < nmat; b += gridDim.x) {
+    C* B = mats + b * (int64_t)n * n;
+    for (int r = tid; r < n; r += blockDim.x) {
+      rowsrc[r] = r;
+      oidx[r] = -1;
+    }
+    for (int k0 = 0; k0 < n; k0 += NB) {
+      const int nb = min(NB, n - k0);
+      for (int u = tid; u < n * NB; u += blockDim.x) {
+        const int r = u / NB, c = u - r * NB;
+        P[r * PS + c] = c < nb ? B[(int64_t)r * n + k0 + c] : czero<C>();
+      }
+      __syncthreads();
+      for (int kk = 0; kk < nb; ++kk) {
+        const int k = k0 + kk;
+        if (tid < 32) {
+          T best = -1;
+          int bi = k;
+          for (int r = k + tid; r < n; r += 32) {
+            const C a = P[r * PS + kk];
+            const T m = a.x * a.x + a.y * a.y;
+            if (m > best) { best = m; bi = r; }
+          }
+          for (int off = 16; off; off >>= 1) {
+            const T ob = __shfl_xor_sync(0xffffffffu, best, off);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+          }
+          if (tid == 0) {
+            s_piv = bi;
+            s_pmag = best;
+            perm[k] = bi;
+            const int t = rowsrc[k];
+            rowsrc[k] = rowsrc[bi];
+            rowsrc[bi] = t;
+          }
+        }
+        __syncthreads();
+        const int p = s_piv;
+        if (tid == 0 && !(s_pmag > 0)) atomicOr(status, 1);
+        if (p != k && tid < NB) {
+          const C t = P[k * PS + tid];
+          P[k * PS + tid] = P[p * PS + tid];
+          P[p * PS + tid] = t;
+        }
+        __syncthreads();
+        for (int r = tid; r < n; r += blockDim.x) colk[r] = P[r * PS + kk];
+        __syncthreads();
+        const C rinv = crecip(colk[k]);
+        if (tid < NB) P[k * PS + tid] = (tid == kk) ? rinv : cmul(P[k * PS + tid], rinv);
+        __syncthreads();
+        for (int u = tid; u < n * NB; u += blockDim.x) {
+          const int r = u / NB, c = u - r * NB;
+          if (r == k) continue;
+          const C base = (c == kk) ? czero<C>() : P[r * PS + c];
+          P[r * PS + c] = csub(base, cmul(colk[r], P[k * PS + c]));
+        }
+        __syncthreads();
+      }
+      if (tid == 0) {
+        int cnt = 0;
+        for (int kk = 0; kk < nb; ++kk) {
+          const int p = perm[k0 + kk];
+          if (p >= k0 + nb && oidx[p] < 0) {
+            oidx[p] = cnt;
+            olist[cnt++] = p;
+          }
+        }
+        s_ocnt = cnt;
+      }
+      for (int u = tid; u < n * NB; u += blockDim.x) {
+        const int r = u / NB, c = u - r * NB;
+        if (c < nb) B[(int64_t)r * n + k0 + c] = P[r * PS + c];
+      }
+      __syncthreads();
+      const int ocnt = s_ocnt, nrest = n - nb;
+      for (int q0 = 0; q0 < nrest; q0 += TQ) {
+        for (int u = tid; u < (nb + ocnt) * TQ; u += blockDim.x) {
+          const int rr = u / TQ, qi = u - rr * TQ;
+          const int qv = q0 + qi;
+          if (qv >= nrest) continue;
+          const int q = qv < k0 ? qv : qv + nb;
+          if (rr < nb) Bsw[rr * TQ + qi] = B[(int64_t)rowsrc[k0 + rr] * n + q];
+          else Osw[(rr - nb) * TQ + qi] = B[(int64_t)rowsrc[olist[rr - nb]] * n + q];
+        }
+        __syncthreads();
+        for (int rs = 0; rs < n; rs += 16 * RM) {
+          C acc[RM][CN];
+#pragma unroll
+          for (int m = 0; m < RM; ++m)
+#pragma unroll
+            for (int c = 0; c < CN; ++c) acc[m][c] = czero<C>();
+#pragma unroll 4
+          for (int kk = 0; kk < nb; ++kk) {
+            C pv[RM], bv[CN];
+#pragma unroll
+            for (int m = 0; m < RM; ++m) {
+              const int r = rs + ty + 16 * m;
+              pv[m] = r < n ? P[r * PS + kk] : czero<C>();
+            }
+#pragma unroll
+            for (int c = 0; c < CN; ++c) bv[c] = Bsw[kk * TQ + tx + 16 * c];
+#pragma unroll
+            for (int m = 0; m < RM; ++m)
+#pragma unroll
+              for (int c = 0; c < CN; ++c) acc[m][c] = cfma(pv[m], bv[c], acc[m][c]);
+          }
+#pragma unroll
+          for (int m = 0; m < RM; ++m) {
+            const int r = rs + ty + 16 * m;
+            if (r >= n) continue;
+            const bool inK = r >= k0 && r < k0 + nb;
+            const int oi = oidx[r];
+#pragma unroll
+            for (int c = 0; c < CN; ++c) {
+              const int qi = tx + 16 * c, qv = q0 + qi;
+              if (qv >= nrest) continue;
+              const int q = qv < k0 ? qv : qv + nb;
+              C* dst = B + (int64_t)r * n + q;
+              const C base = inK ? czero<C>() : (oi >= 0 ? Osw[oi * TQ + qi] : *dst);
+              *dst = cadd(base, acc[m][c]);
+            }
+          }
+        }
+        __syncthreads();
+      }
+      for (int r = tid; r < n; r += blockDim.x) rowsrc[r] = r;
+      if (tid < ocnt) oidx[olist[tid]] = -1;
+      __syncthreads();
+    }
+    if (tid == 0) {
+      for (int c = 0; c < n; ++c) cmap[c] = c;
+      for (int k = n - 1; k >= 0; --k) {
+        const int p = perm[k];
+        if (p != k) {
+          const int t = cmap[k];
+          cmap[k] = cmap[p];
+          cmap[p] = t;
+        }
+      }
+    }
+    __syncthreads();
+    for (int r0 = 0; r0 < n; r0 += PS) {
+      const int nr = min(PS, n - r0);
+      for (int u = tid; u < nr * n; u += blockDim.x) P[u] = B[(int64_t)r0 * n + u];
+      __syncthreads();
+      for (int u = tid; u < nr * n; u += blockDim.x) {
+        const int rl = u / n, c = u - rl * n;
+        const C a = cscale(P[rl * n + cmap[c]], (T)scale);
+        if (!(isfinite(a.x) && isfinite(a.y))) atomicOr(status, 2);
+        B[(int64_t)r0 * n + u] = a;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <typename T>
+constexpr int gj_cn() { return std::is_same<T, float>::value ? 4 : 2; }
+
+size_t gj_blocked_smem(int n, size_t csize) {
+  constexpr int NB = 32;
+  const int TQ = 16 * (csize == sizeof(float2) ? 4 : 2);
+  return ((size_t)n * (NB + 1) + 2ull * NB * TQ + n) * csize + (4ull * n + NB) * sizeof(int) + 64;
+}
+
 template <typename T>
 void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, const double2* dvec, double2 dscal,
                      bool invert, bool colmajor, double scale, cplx_t<T>* out, int* status, cudaStream_t st,
                      bool sym) {
   const size_t smem = assemble_smem(N, sizeof(cplx_t<T>));
-  if (smem > 227 * 1024)
-    throw Error(VS_ERR_UNSUPPORTED, "3N x 3N block of " + std::to_string(3 * N) + " does not fit in shared memory");
+  const int Lb = sym ? L / 2 + 1 : L, Mb = sym ? M / 2 + 1 : M;
+  const int n = 3 * N;
+  const int64_t nmat = (int64_t)Lb * Mb;
+  if (!invert || smem > 227 * 1024) {
+    // element-wise assembly; the inverse of A^T in row-major order is A^-1 in column-major order
+    const int64_t total = nmat * n * n;
+    const int blocks = (int)std::min<int64_t>(ceil_div(total, 256), 152 * 64);
+    k_assemble<T><<<blocks, 256, 0, st>>>(lev2, L, M, N, shift, dvec, dscal, (invert || colmajor) ? 1 : 0,
+                                          invert ? 1.0 : scale, out, Lb, Mb);
+    VS_LAUNCH_CHECK();
+    if (!invert) return;
+    VS_REQUIRE(colmajor, "large blocks are only produced column-major");
+    const size_t gsm = gj_blocked_smem(n, sizeof(cplx_t<T>));
+    if (gsm > 227 * 1024)
+      throw Error(VS_ERR_UNSUPPORTED, "3N x 3N block of " + std::to_string(n) + " is too large to invert");
+    auto k = k_gj_blocked<T, 32, gj_cn<T>()>;
+    set_kernel_smem((const void*)k, gsm);
+    int per_sm = 0;
+    VS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, gsm));
+    int dev = 0, nsm = 0;
+    VS_CUDA(cudaGetDevice(&dev));
+    VS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int grid = (int)std::min<int64_t>(nmat, (int64_t)nsm * std::max(per_sm, 1));
+    k<<<grid, 256, gsm, st>>>(out, n, nmat, scale, status);
+    VS_LAUNCH_CHECK();
+    return;
+  }
   auto k = k_assemble_invert<T>;
   set_kernel_smem((const void*)k, smem);
-  const int Lb = sym ? L / 2 + 1 : L, Mb = sym ? M / 2 + 1 : M;
   k<<<dim3(Lb, Mb), 256, smem, st>>>(lev2, L, M, N, shift, dvec, dscal, invert ? 1 : 0, colmajor ? 1 : 0, scale, out,
                                      status, Lb);
   VS_LAUNCH_CHECK();
