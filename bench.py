@@ -466,8 +466,8 @@ def run_passes(args):
     if args.sweep:
         tuned_op, tuned_pr = op.shape("c64"), prec.shape("c64")
         zs = {}
-        for z_reg in (0, 1):
-            for lg in (2, 3, 4, 5):
+        for z_reg in (0, 1, 2):
+            for lg in ((2, 3, 4, 5) if z_reg == 0 else (4,)):
                 op.set_shape("c64", z_reg=z_reg, lg_tile_z=lg)
                 zs[f"z_reg={z_reg},lg_tile_z={lg}"] = op.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64",
                                                                      args.steps)[2]
@@ -475,9 +475,14 @@ def run_passes(args):
         gs = {}
         for b in (1, 2, 4):
             for th in (64, 128, 256):
-                prec.set_shape("c64", gemv_blocks=b, gemv_threads=th)
-                gs[f"blocks={b},threads={th}"] = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64",
-                                                                  args.steps)[2]
+                prec.set_shape("c64", gemv_mode=0, gemv_blocks=b, gemv_threads=th, gemv_chunk=0)
+                gs[f"direct,blocks={b},threads={th}"] = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64",
+                                                                         args.steps)[2]
+        for b in (1, 2):
+            for cq in (0, 8, 16, 32):
+                prec.set_shape("c64", gemv_mode=1, gemv_blocks=b, gemv_threads=0, gemv_chunk=cq)
+                gs[f"stream,ctas={b},chunk={cq}"] = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64",
+                                                                     args.steps)[2]
         prec.set_shape("c64", **tuned_pr)
         out["z_pass_ms"] = zs
         out["gemv_ms"] = gs

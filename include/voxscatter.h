@@ -280,18 +280,24 @@ typedef struct vs_shape {
   int lg_lines_x;  /* x passes: log2 lines per CTA                                 */
   int lg_tile_y;   /* y passes: log2 x-tile width                                  */
   int lg_tile_z;   /* z pass (shared-memory kernel): log2 x-tile width             */
-  int z_reg;       /* c64 z pass: 1 register-resident lines, 0 shared memory        */
+  int z_reg;       /* z pass: 0 shared-memory Stockham, 1 two-level registers,
+                      2 two-level with a register cap for occupancy          */
 } vs_shape;
 int vs_op_get_shape(const vs_op* op, int precision, vs_shape* shape);
 int vs_op_set_shape(vs_op* op, int precision, const vs_shape* shape);
 
-/* Launch shape of a preconditioner apply: x/y tiles of its FFT passes and the
- * block GEMV's stored blocks per CTA and threads per CTA (0 = default). */
+/* Launch shape of a preconditioner apply: x/y tiles of its FFT passes and
+ * the block GEMV.  gemv_mode 0 is the register-direct GEMV (gemv_blocks
+ * stored blocks per CTA, gemv_threads per CTA); gemv_mode 1 streams each block
+ * through shared memory with bulk asynchronous copies (gemv_blocks CTAs per SM,
+ * gemv_chunk block columns per copy).  0 / -1 select the defaults. */
 typedef struct vs_prec_shape {
   int lg_lines_x;
   int lg_tile_y;
   int gemv_blocks;
   int gemv_threads;
+  int gemv_mode;
+  int gemv_chunk;
 } vs_prec_shape;
 int vs_prec_get_shape(const vs_prec* prec, int precision, vs_prec_shape* shape);
 int vs_prec_set_shape(vs_prec* prec, int precision, const vs_prec_shape* shape);

@@ -167,7 +167,7 @@ def test_full_storage_when_parity_is_not_exact(api):
 
 @pytest.mark.parametrize("nper,diameter,aspect", [(4, 2.5, 0.5), (10, 2.0, 0.5), (6, 3.0, 0.35), (3, 2.0, 0.9)])
 def test_every_launch_shape_matches_oracle(api, nper, diameter, aspect):
-    """Both z-pass kernels (register-resident lines and shared-memory Stockham)
+    """Both z-pass kernels (two-level registers and shared-memory Stockham)
     and several x/y/z tiles give the same c64 matvec as the oracle."""
     p = W.small_hex(m=1.31 + 0.05j, diameter=diameter, nper=nper, aspect_ratio=aspect)
     L, M, N, idx3, chi = _problem(p)
@@ -179,27 +179,41 @@ def test_every_launch_shape_matches_oracle(api, nper, diameter, aspect):
     rng = np.random.default_rng(N)
     x = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
     y_o = O.MVP(x, fN, np.ones((L, M, N)), dV * chi, 1 / alpha, "notransp", idx3)
-    for z_reg in (0, 1):
+    for z_reg in (0, 1, 2):
         for lg in (1, 3):
             op.set_shape("c64", z_reg=z_reg, lg_tile_z=lg, lg_tile_y=lg + 1, lg_lines_x=lg)
             assert rel(op.apply(x, "notransp", "c64"), y_o) < C64_TOL, (z_reg, lg, op.PQR)
 
 
-@pytest.mark.parametrize("N", [13, 26, 27])
-def test_tall_grids_both_z_kernels(api, N):
-    """z lengths 27, 54 and 54 (5-smooth >= 2N-1): register and shared-memory z
-    passes against the oracle on a 6 x 5 x N block of voxels."""
+Z_LENGTHS = [4, 6, 8, 9, 10, 12, 15, 16, 18, 20, 24, 27, 30, 32, 36, 40, 45, 48, 54, 60, 64, 72, 80, 90, 96, 108,
+             120, 128, 144, 160, 180, 192, 216, 240, 256]
+
+
+@pytest.mark.parametrize("R", Z_LENGTHS)
+def test_z_lengths_both_z_kernels(api, R):
+    """Every z length with a two-level register kernel (R = R1*R2), forced on a
+    3 x 2 x ceil(R/2) block of voxels: the two-level and the shared-memory
+    Stockham z passes (two-level with and without its register cap) in c64
+    and c128, with the first-octant spectrum and,
+    after breaking the Toeplitz parity, with the full spectrum."""
     from voxscatter_gb300.geometry import grid3d
-    L, M = 6, 5
+    L, M, N = 3, 2, (R + 1) // 2
     d = 0.07
     r = grid3d(np.arange(L) * d, np.arange(M) * d, np.arange(N) * d)
     ko = 2 * np.pi
-    Toep = O.green_toeplitz(r, ko)
-    fN = O.fft_operator(O.circulant_nop_const(Toep))
-    idx3 = np.arange(3 * L * M * N)
-    op = api.Operator(L, M, N, idx3, 1.0, d ** 3, 3.0, toep=Toep)
-    x = np.random.default_rng(N).normal(size=idx3.size) + 1j * np.random.default_rng(N + 1).normal(size=idx3.size)
-    y_o = O.MVP(x, fN, np.ones((L, M, N)), d ** 3, 3.0, "notransp", idx3)
-    for z_reg in (0, 1):
-        op.set_shape("c64", z_reg=z_reg)
-        assert rel(op.apply(x, "notransp", "c64"), y_o) < C64_TOL, (z_reg, op.PQR)
+    rng = np.random.default_rng(R)
+    for exact_parity in (True, False):
+        Toep = O.green_toeplitz(r, ko)
+        if not exact_parity:
+            Toep = Toep.copy()
+            Toep[0, :, :, 2] += 1e-2 * np.abs(Toep).max() * rng.normal(size=(M, N))
+        fN = O.fft_operator(O.circulant_nop_const(Toep))
+        idx3 = np.arange(3 * L * M * N)
+        op = api.Operator(L, M, N, idx3, 1.0, d ** 3, 3.0, toep=Toep, PQR=(0, 0, R))
+        assert op.PQR[2] == R
+        x = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
+        y_o = O.MVP(x, fN, np.ones((L, M, N)), d ** 3, 3.0, "notransp", idx3)
+        for prec, tol in (("c64", C64_TOL), ("c128", C128_TOL)):
+            for z_reg in (0, 1, 2):
+                op.set_shape(prec, z_reg=z_reg)
+                assert rel(op.apply(x, "notransp", prec), y_o) < tol, (prec, z_reg, exact_parity, op.PQR)

@@ -66,6 +66,16 @@ def test_prec_build_and_apply(api, shape):
     y_o = O.mvp_circ_2_level(inv_o, x, L, M, N, idx3)
     assert rel(pr.apply(x, "c128"), y_o) < 1e-10
     assert rel(pr.apply(x, "c64"), y_o) < 1e-4
+    # both GEMV kernels (register-direct; streamed in whole blocks or in
+    # column chunks), one and five right-hand sides (5: 4 per CTA + 1)
+    X = rng.normal(size=(5, idx3.size)) + 1j * rng.normal(size=(5, idx3.size))
+    Y_o = np.array([O.mvp_circ_2_level(inv_o, X[k], L, M, N, idx3) for k in range(5)])
+    for prec, tol in (("c128", 1e-10), ("c64", 1e-4)):
+        for mode, chunk, ctas in ((0, 0, 2), (1, 0, 1), (1, 0, 2), (1, 2, 2), (1, 5, 1)):
+            pr.set_shape(prec, gemv_mode=mode, gemv_chunk=min(chunk, 3 * N), gemv_blocks=ctas, gemv_threads=0)
+            assert rel(pr.apply(x, prec), y_o) < tol, (prec, mode, chunk)
+            Y = pr.apply(X.ravel(), prec).reshape(5, -1)
+            assert rel(Y, Y_o) < tol, (prec, mode, chunk, "batched")
     # the MATLAB-style call with caller-supplied inverse blocks
     assert rel(api.mvp_circ_2_level(inv_o, x, L, M, N, idx3), y_o) < 1e-10
 
@@ -139,5 +149,28 @@ def test_prec_large_blocks(api, N, L, M):
     rng = np.random.default_rng(5)
     x = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
     y_o = O.mvp_circ_2_level(inv_o, x, L, M, N, idx3)
-    assert rel(pr.apply(x, "c128"), y_o) < 1e-10
-    assert rel(pr.apply(x, "c64"), y_o) < 1e-4
+    for prec, tol in (("c128", 1e-10), ("c64", 1e-4)):
+        for mode, chunk in ((0, 0), (1, 0), (1, 16), (1, 7)):
+            pr.set_shape(prec, gemv_mode=mode, gemv_chunk=chunk, gemv_blocks=1, gemv_threads=0)
+            assert rel(pr.apply(x, prec), y_o) < tol, (prec, mode, chunk)
+
+
+def test_context_outlives_its_objects(api):
+    """vs_ctx_destroy before the operator and preconditioner made on the
+    context: both keep working (they hold the context) and are released
+    afterwards in any order."""
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.0, nper=3)
+    L, M, N, idx3, Toep, alpha, dV = _setup(p)
+    ctx = api.Context(0)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep, ctx=ctx)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
+    x = np.random.default_rng(3).normal(size=idx3.size) + 0j
+    y0, z0 = op.apply(x, "notransp", "c128"), pr.apply(x, "c128")
+    raw = ctx.h
+    ctx.h = None  # the Python wrapper forgets it; the library keeps it for op and pr
+    ctx._lib.vs_ctx_destroy(raw)
+    assert rel(op.apply(x, "notransp", "c128"), y0) < 1e-14
+    assert rel(pr.apply(x, "c128"), z0) < 1e-14
+    op.close()
+    assert rel(pr.apply(x, "c128"), z0) < 1e-14
+    pr.close()

@@ -298,7 +298,7 @@ class Preconditioner:
         L.check(self.ctx._lib.vs_prec_get_shape(self.h, L.VS_C64 if precision == "c64" else L.VS_C128,
                                                 C.byref(sh)))
         return dict(lg_lines_x=sh.lg_lines_x, lg_tile_y=sh.lg_tile_y, gemv_blocks=sh.gemv_blocks,
-                    gemv_threads=sh.gemv_threads)
+                    gemv_threads=sh.gemv_threads, gemv_mode=sh.gemv_mode, gemv_chunk=sh.gemv_chunk)
 
     def set_shape(self, precision="c64", **kw):
         cur = self.shape(precision)

@@ -184,6 +184,17 @@ void prec_common_impl(vs_prec* pr, int precisions) {
   pr->axM.init(pr->M, st);
   pr->t.alloc((size_t)pr->L * pr->M * pr->N * 3 * sizeof(double2));
   pr->nrhs_cap = 1;
+  pr->gemv_status.alloc(sizeof(int));
+  VS_CUDA(cudaMemsetAsync(pr->gemv_status.p, 0, sizeof(int), st));
+}
+
+// Raises if a streamed-GEMV wait of this preconditioner ever ran out (the
+// stream must be idle).
+void check_prec_status(vs_prec* pr) {
+  if (!pr || !pr->gemv_status.p) return;
+  int hs = 0;
+  VS_CUDA(cudaMemcpy(&hs, pr->gemv_status.p, sizeof(int), cudaMemcpyDeviceToHost));
+  VS_REQUIRE(hs == 0, "a streamed preconditioner copy did not complete in time");
 }
 
 void prec_scratch_impl(vs_prec* pr, int64_t nrhs) {
@@ -261,6 +272,7 @@ void solve_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, const vs
   vs::SolveResult r;
   if (o->method == VS_GMRES) vs::solve_gmres(*op, prec, b, x, prm, r, op->ctx->stream);
   else vs::solve_bicgstab(*op, prec, b, x, prm, r, op->ctx->stream);
+  check_prec_status(prec);
   fill_info(r, info);
 }
 
@@ -280,14 +292,27 @@ void solve_batch_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, in
       vs::solve_gmres(*op, prec, b + r * n, x + r * n, p1, res, op->ctx->stream);
       fill_info(res, infos + r);
     }
+    check_prec_status(prec);
     return;
   }
   std::vector<vs::SolveResult> res;
   vs::solve_bicgstab_batch(*op, prec, b, x, (int)nrhs, prm, res, op->ctx->stream);
+  check_prec_status(prec);
   for (int64_t r = 0; r < nrhs; ++r) fill_info(res[r], infos + r);
 }
 
 }  // namespace
+
+void ctx_retain(vs_ctx* ctx) {
+  if (ctx) ctx->refs.fetch_add(1);
+}
+
+void ctx_release(vs_ctx* ctx) {
+  if (!ctx || ctx->refs.fetch_sub(1) != 1) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
 
 extern "C" {
 
@@ -317,8 +342,7 @@ int vs_ctx_create(int device, vs_ctx** out) {
 int vs_ctx_destroy(vs_ctx* ctx) {
   if (!ctx) return VS_OK;
   int st = guarded(ctx, [&] { VS_CUDA(cudaStreamSynchronize(ctx->stream)); });
-  cudaStreamDestroy(ctx->stream);
-  delete ctx;
+  ctx_release(ctx);
   return st;
 }
 
@@ -410,10 +434,11 @@ int vs_op_create(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* toe
     VS_REQUIRE(toep && out, "NULL argument");
     if (P <= 0) P = vs::smooth_size((int)(2 * L - 1));
     if (Q <= 0) Q = vs::smooth_size((int)(2 * M - 1));
-    if (R <= 0) R = vs::smooth_size((int)(2 * N - 1));
+    if (R <= 0) R = vs::z_pass_length((int)(2 * N - 1));
     check_fft_len(P, L, "P"); check_fft_len(Q, M, "Q"); check_fft_len(R, N, "R");
     op = new vs_op();
     op->ctx = ctx;
+    ctx_retain(ctx);
     op->L = (int)L; op->M = (int)M; op->N = (int)N;
     op->P = (int)P; op->Q = (int)Q; op->R = (int)R;
     op->V = L * M * N;
@@ -450,6 +475,7 @@ int vs_op_create_fN(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* 
     check_fft_len(P, L, "P"); check_fft_len(Q, M, "Q"); check_fft_len(R, N, "R");
     op = new vs_op();
     op->ctx = ctx;
+    ctx_retain(ctx);
     op->L = (int)L; op->M = (int)M; op->N = (int)N;
     op->P = (int)P; op->Q = (int)Q; op->R = (int)R;
     op->V = L * M * N;
@@ -588,6 +614,7 @@ int vs_prec_create(vs_op* op, const double* shift, const double* d, int64_t nd, 
     pr = new vs_prec();
     pr->id = next_object_id();
     pr->ctx = op->ctx;
+    ctx_retain(pr->ctx);
     pr->L = op->L; pr->M = op->M; pr->N = op->N;
     pr->V = op->V; pr->n3 = op->n3;
     cudaStream_t st = op->ctx->stream;
@@ -614,12 +641,12 @@ int vs_prec_create(vs_op* op, const double* shift, const double* d, int64_t nd, 
     pr->sym = op->gsym;  // exact parity of the Toeplitz tensor: quadrant storage suffices
     const int64_t nblk = pr->sym ? (int64_t)(op->L / 2 + 1) * (op->M / 2 + 1) : LM;
     if (precisions & VS_BUILD_C64) {
-      pr->inv32.alloc(nblk * n * n * sizeof(float2));
+      pr->inv32.alloc(nblk * n * n * sizeof(float2) + 64);
       vs::assemble_invert<float>(l2.as<double2>(), op->L, op->M, op->N, sh, dptr, ds, true, true, scale,
                                  pr->inv32.as<float2>(), status.as<int>(), st, pr->sym);
     }
     if (precisions & VS_BUILD_C128) {
-      pr->inv64.alloc(nblk * n * n * sizeof(double2));
+      pr->inv64.alloc(nblk * n * n * sizeof(double2) + 64);
       vs::assemble_invert<double>(l2.as<double2>(), op->L, op->M, op->N, sh, dptr, ds, true, true, scale,
                                   pr->inv64.as<double2>(), status.as<int>(), st, pr->sym);
     }
@@ -646,6 +673,7 @@ int vs_prec_create_blocks(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const do
     pr = new vs_prec();
     pr->id = next_object_id();
     pr->ctx = ctx;
+    ctx_retain(ctx);
     pr->L = (int)L; pr->M = (int)M; pr->N = (int)N;
     pr->V = L * M * N;
     cudaStream_t st = ctx->stream;
@@ -666,8 +694,8 @@ int vs_prec_create_blocks(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const do
     vs::DevBuf raw;
     raw.alloc(LM * n * n * sizeof(double2));
     VS_CUDA(cudaMemcpyAsync(raw.p, inv_blocks, LM * n * n * sizeof(double2), cudaMemcpyHostToDevice, st));
-    if (precisions & VS_BUILD_C64) pr->inv32.alloc(LM * n * n * sizeof(float2));
-    if (precisions & VS_BUILD_C128) pr->inv64.alloc(LM * n * n * sizeof(double2));
+    if (precisions & VS_BUILD_C64) pr->inv32.alloc(LM * n * n * sizeof(float2) + 64);
+    if (precisions & VS_BUILD_C128) pr->inv64.alloc(LM * n * n * sizeof(double2) + 64);
     const int64_t tot = LM * n * n;
     k_blocks_in<<<(int)std::min<int64_t>(vs::ceil_div(tot, 256), 152 * 32), 256, 0, st>>>(
         raw.as<double2>(), tot, 1.0 / (double)LM, (precisions & VS_BUILD_C128) ? pr->inv64.as<double2>() : nullptr,
@@ -727,6 +755,7 @@ int vs_prec_apply(vs_prec* prec, const double* x, double* y, int64_t nrhs, int p
       VS_CUDA(cudaMemcpyAsync(y, prec->yout.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
       VS_CUDA(cudaStreamSynchronize(st));
     }
+    check_prec_status(prec);
   });
 }
 
@@ -815,6 +844,8 @@ int vs_prec_get_shape(const vs_prec* prec, int precision, vs_prec_shape* shape) 
   shape->lg_tile_y = s.lg_tx_y;
   shape->gemv_blocks = s.gemv_ti;
   shape->gemv_threads = s.gemv_threads;
+  shape->gemv_mode = s.gemv_mode;
+  shape->gemv_chunk = s.gemv_chunk;
   return VS_OK;
 }
 
@@ -837,8 +868,13 @@ int vs_prec_set_shape(vs_prec* prec, int precision, const vs_prec_shape* shape) 
     vs::PassShape& s = prec->shape[precision == VS_C64 ? 0 : 1];
     s.lg_lpb_x = shape->lg_lines_x;
     s.lg_tx_y = shape->lg_tile_y;
+    VS_REQUIRE(shape->gemv_mode >= -1 && shape->gemv_mode <= 1, "gemv_mode must be -1, 0 or 1");
+    VS_REQUIRE(shape->gemv_chunk >= 0 && shape->gemv_chunk <= 3 * prec->N, "gemv_chunk out of range");
+    VS_REQUIRE(shape->gemv_mode != 1 || shape->gemv_blocks <= 2, "streamed GEMV takes 1 or 2 CTAs per SM");
     s.gemv_ti = shape->gemv_blocks;
     s.gemv_threads = shape->gemv_threads;
+    s.gemv_mode = shape->gemv_mode;
+    s.gemv_chunk = shape->gemv_chunk;
   });
 }
 

@@ -5,6 +5,7 @@
 #include <memory>
 #include <vector>
 #include <string>
+#include <atomic>
 
 namespace vs {
 
@@ -47,9 +48,11 @@ struct PassShape {
   int lg_lpb_x = -1;   // x passes: lines per CTA
   int lg_tx_y = -1;    // y passes: x-tile width
   int lg_tx_z = -1;    // z pass: x-tile width
-  int gemv_ti = 0;     // preconditioner GEMV: stored blocks per CTA (0 = default)
+  int gemv_ti = 0;     // preconditioner GEMV: stored blocks per CTA (direct) or CTAs per SM (streamed); 0 = default
   int gemv_threads = 0;
-  int z_reg = -1;      // c64 z pass: 1 register-resident lines, 0 shared-memory Stockham, -1 default
+  int gemv_mode = -1;  // 0 register-direct GEMV, 1 streamed through shared memory, -1 default (streamed)
+  int gemv_chunk = 0;  // streamed GEMV: block columns per bulk copy (0 = default)
+  int z_reg = -1;      // z pass: 0 shared-memory Stockham, 1 two-level, 2 two-level with register cap, -1 default
 };
 
 // Work vectors and device scalars of the Krylov solvers (vs_krylov.cu).
@@ -79,12 +82,18 @@ struct KrylovWork {
 
 }  // namespace vs
 
+// A context lives until vs_ctx_destroy has been called and the last operator
+// or preconditioner created on it is destroyed (each holds a reference), so
+// handles can be released in any order.
 struct vs_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
   vs::DevBuf stage;  // host<->device staging for the host-buffer entry points
+  std::atomic<int> refs{1};
 };
+void ctx_retain(vs_ctx* ctx);
+void ctx_release(vs_ctx* ctx);
 
 // Diagonal coefficients of an operator at the n3 unknown positions.
 struct VsDiagDev {
@@ -97,7 +106,8 @@ template <> inline const float2* VsDiagDev::ptr<float>() const { return arr ? v3
 template <> inline const double2* VsDiagDev::ptr<double>() const { return arr ? v64.as<double2>() : nullptr; }
 
 struct vs_op {
-  vs_ctx* ctx = nullptr;
+  vs_ctx* ctx = nullptr;  // retained while the operator exists
+  ~vs_op() { ctx_release(ctx); }
   int L = 0, M = 0, N = 0, P = 0, Q = 0, R = 0;
   int64_t V = 0, n3 = 0;
   vs::DevBuf map3;      // int32[3V]: unknown position of each grid entry, -1 if absent
@@ -116,7 +126,8 @@ struct vs_op {
 
 // 2-level circulant preconditioner: inverse blocks per (x,y) frequency.
 struct vs_prec {
-  vs_ctx* ctx = nullptr;
+  vs_ctx* ctx = nullptr;    // retained while the preconditioner exists
+  ~vs_prec() { ctx_release(ctx); }
   uint64_t id = 0;          // unique per preconditioner object (keys cached solver graphs)
   int L = 0, M = 0, N = 0;
   bool sym = false;         // blocks stored for i <= L/2, j <= M/2 only (parity of the operator)
@@ -128,6 +139,7 @@ struct vs_prec {
   vs::DevBuf xin, yout;
   int nrhs_cap = 0;
   vs::PassShape shape[2];   // [0] c64, [1] c128 apply launch shapes
+  vs::DevBuf gemv_status;   // int: bit 4 set when a streamed-GEMV wait ran out
 };
 
 namespace vs {
@@ -168,6 +180,8 @@ void finalize_spectrum(const double2* fN, int64_t total, double scale, double2* 
 // Preconditioner (vs_precond.cu)
 void circ_levels_device(int L, int M, int N, const double2* toep, double2* lev1, double2* lev2, const FftAxis& axL,
                         const FftAxis& axM, cudaStream_t st);
+// Smallest instantiated two-level z length >= min_len (5-smooth beyond 256).
+int z_pass_length(int min_len);
 template <typename T>
 void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, const double2* dvec, double2 dscal,
                      bool invert, bool colmajor, double scale, cplx_t<T>* out, int* status, cudaStream_t st,

@@ -362,15 +362,13 @@ static PipeArgs<T> pipe_args(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, 
   return a;
 }
 
-// z pass: the register-resident kernel for c64 with a first-octant spectrum
-// when the operator's shape selects it (and R has one), else the shared-memory
-// Stockham kernel.
+// z pass: the two-level register kernel when the operator's shape selects it
+// (and R has one), else the shared-memory Stockham kernel.
 template <typename T>
 static void launch_z(const vs_op& op, const PipeArgs<T>& a, int nrhs, cudaStream_t st) {
   using C = cplx_t<T>;
-  if constexpr (std::is_same<T, float>::value) {
-    if (op.gsym && op.shape[0].z_reg == 1 && z_pass_reg(a, nrhs, st)) return;
-  }
+  const int zr = op.shape[std::is_same<T, float>::value ? 0 : 1].z_reg;
+  if ((zr == 1 || zr == 2) && z_pass_two_level<T>(a, op.gsym, zr == 2, nrhs, st)) return;
   const int tx = 1 << a.lg_tx;
   dim3 grid(ceil_div(op.P, tx), op.Q, nrhs);
   const size_t smem = (2ull * op.R * 3 * tx + op.R) * sizeof(C);
@@ -563,12 +561,17 @@ void autotune_op(vs_op& op, cudaStream_t st) {
   sh.z_reg = 0;
   best_of(&sh.lg_tx_z, 1, 5, [&](int v) { return (2ull * op.R * 3 * (1 << v) + op.R) * cs <= lim; },
           [&] { matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 2); });
-  if (std::is_same<T, float>::value && op.gsym) {
-    // the shared-memory kernel with its best tile against the register kernel
-    const float t_smem = time_ms(st, reps, [&] { matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 2); });
-    sh.z_reg = 1;
-    const float t_reg = time_ms(st, reps, [&] { matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 2); });
-    sh.z_reg = t_reg < t_smem ? 1 : 0;
+  {
+    // the shared-memory kernel with its best tile against the two-level
+    // kernel, with and without the register cap
+    float best = time_ms(st, reps, [&] { matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 2); });
+    int arg = 0;
+    for (int v = 1; v <= 2; ++v) {
+      sh.z_reg = v;
+      const float t = time_ms(st, reps, [&] { matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 2); });
+      if (t < best) { best = t; arg = v; }
+    }
+    sh.z_reg = arg;
   }
   VS_CUDA(cudaStreamSynchronize(st));
 }

@@ -57,7 +57,9 @@ struct StridedArgs {
 };
 
 // Register-resident z pass (vs_zreg.cu); false when R has no register kernel.
-bool z_pass_reg(const PipeArgs<float>& a, int nrhs, cudaStream_t st);
+// Two-level register z pass (vs_zpass.cuh); false when R has no instantiation.
+template <typename T>
+bool z_pass_two_level(const PipeArgs<T>& a, bool sym, bool cap, int nrhs, cudaStream_t st);
 
 template <typename T>
 void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaStream_t st);

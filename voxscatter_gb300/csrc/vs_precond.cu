@@ -643,6 +643,347 @@ __global__ void __launch_bounds__(256) k_block_gemv_sym(cplx_t<T>* __restrict__ 
   }
 }
 
+// ---- streamed quadrant-symmetric apply ------------------------------------
+// Bulk asynchronous copies (cp.async.bulk) complete on an mbarrier; every wait
+// is bounded and a wait that runs out sets status bit 4 and ends the CTA
+// after its outstanding copies land (again with a bounded wait).
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_to_shared(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+// Bulk copy whose lines are the first candidates for L2 eviction (a one-pass
+// stream that should not displace data the next passes re-read).
+__device__ __forceinline__ void bulk_to_shared_stream(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar,
+                                                      uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+          dst),
+      "l"(src), "r"(bytes), "r"(bar), "l"(policy)
+      : "memory");
+}
+
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int i = 0; i < (1 << 20); ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// Grid position of variant var (bit 0: mirror in x, bit 1: mirror in y) of the
+// stored block (is, js); false when that mirror coincides with the block itself.
+__device__ __forceinline__ bool mirror_of(int is, int js, int var, int L, int M, int& i, int& j) {
+  const bool fx = var & 1, fy = var >> 1;
+  if (fx && (is == 0 || 2 * is == L)) return false;
+  if (fy && (js == 0 || 2 * js == M)) return false;
+  i = fx ? L - is : is;
+  j = fy ? M - js : js;
+  return true;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Persistent apply over the stored blocks b = blockIdx.x + k*gridDim.x for the
+// right-hand sides blockIdx.y*RG .. +RG, with three warp roles:
+//  * producer warp (lane 0): streams the blocks (column-major 3N x 3N, in
+//    chunks of cq columns) through a ring of nstage shared-memory stages with
+//    bulk asynchronous copies, reusing a stage once every consumer warp has
+//    arrived on its "empty" barrier;
+//  * nv vector warps: gather the W = 4*RG vectors of a block (its four mirrored
+//    frequencies per right-hand side, x/y component flips applied) into one
+//    of two buffers [q][W] ahead of the consumers, and after the consumers
+//    are done with a block add its G partial sums and write the results
+//    (flips applied again) over the grid entries the inputs came from;
+//  * consumer warps: thread (g, rp) forms rows RW*rp .. +RW-1 (RW = 2 with
+//    PAIR: one 16-byte load per column) over the chunk columns q = g (mod G).
+// Block boundaries therefore never stop the stream.  Hand-offs use mbarriers:
+// vfull[b] (vector warp -> consumers: buffer b holds the block's vectors),
+// done[b] (consumers -> vector warp: partial sums of buffer b written, its
+// vectors no longer needed) and rfree[b] (vector warp -> consumers: partial
+// sums of buffer b consumed).  Every wait is bounded; a wait that runs out
+// sets status bit 4 and the abort flag, every role leaves its loop, and the
+// producer waits (bounded) for its last copies to land before the CTA ends.
+// A chunk is fetched from the 16-byte boundary at or below its start, so with
+// c64 elements and odd 3N the data may begin one element into the stage (the
+// block buffers carry 64 bytes of tail padding for the rounded-up last copy);
+// PAIR is used only when 3N is even, where every chunk starts aligned.
+template <typename T, int RG, bool PAIR>
+__global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ inv,
+                                                           int L, int M, int N, int64_t rhs_stride, int nrhs,
+                                                           const int* skip, int skip_stride, int cq, int nstage,
+                                                           int stage_elems, int G, int nc, int nv,
+                                                           int* __restrict__ status) {
+  using C = cplx_t<T>;
+  constexpr int W = 4 * RG, RW = PAIR ? 2 : 1;
+  const int rhs0 = blockIdx.y * RG;
+  const int nr = min(RG, nrhs - rhs0);
+  if (skip) {
+    bool all = true;
+    for (int g = 0; g < nr; ++g) all = all && skip[(rhs0 + g) * skip_stride];
+    if (all) return;
+  }
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);  // [8]
+  uint64_t* empty = full + 8;                               // [8]
+  uint64_t* vfull = empty + 8;                              // [2]
+  uint64_t* done = vfull + 2;                               // [2]
+  uint64_t* rfree = done + 2;                               // [2]
+  volatile int* ctl = reinterpret_cast<volatile int*>(rfree + 2);  // [0] abort, [1] chunks issued
+  C* stg = reinterpret_cast<C*>(smem_raw + 256);
+  const int n = 3 * N, Lb = L / 2 + 1, Mb = M / 2 + 1;
+  C* vt0 = stg + (size_t)nstage * stage_elems;  // 2 x [n][W]
+  C* red0 = vt0 + 2 * n * W;                    // 2 x [G][n][W]
+  const int64_t nblk = (int64_t)Lb * Mb, LM = (int64_t)L * M;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int64_t nmine = blockIdx.x < nblk ? (nblk - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int cpb = (n + cq - 1) / cq;
+  const int64_t total = nmine * cpb;
+  const int nW = n * W;
+  const int ncw = nc / 32;
+  if (tid == 0) {
+    for (int s = 0; s < nstage; ++s) {
+      mbar_init(smem_addr(full + s), 1);
+      mbar_init(smem_addr(empty + s), ncw);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_addr(vfull + b), nv);
+      mbar_init(smem_addr(done + b), ncw);
+      mbar_init(smem_addr(rfree + b), nv);
+    }
+    ctl[0] = 0;
+    ctl[1] = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto fail = [&] {
+    atomicOr(status, 4);
+    ctl[0] = 1;
+  };
+
+  if (tid >= nc + 32) {  // vector warps: vthread vl of nv*32 handles elements vl, vl + nv*32, ...
+    const int vl = tid - nc - 32, vstride = nv * 32;
+    // grid offsets of the four mirrors of block kb (-1: coincides with the block)
+    auto bases = [&](int64_t kb, int64_t (&base)[4]) {
+      const int64_t b = blockIdx.x + kb * gridDim.x;
+      const int js = (int)(b / Lb), is = (int)(b - (int64_t)js * Lb);
+#pragma unroll
+      for (int var = 0; var < 4; ++var) {
+        int i, j;
+        base[var] = mirror_of(is, js, var, L, M, i, j) ? i + (int64_t)L * j : -1;
+      }
+    };
+    auto gather = [&](int64_t kb) {
+      int64_t base[4];
+      bases(kb, base);
+      C* vt = vt0 + (kb & 1) * nW;
+      constexpr int B = 8;  // independent loads in flight per lane
+      for (int u0 = vl; u0 < nW; u0 += vstride * B) {
+        C v[B];
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+          const int u = u0 + vstride * k;
+          const int q = u / W, col = u - q * W;
+          const int var = col & 3, rg = col >> 2;
+          v[k] = (u < nW && rg < nr && base[var] >= 0) ? t[(int64_t)(rhs0 + rg) * rhs_stride + base[var] + LM * q]
+                                                       : czero<C>();
+        }
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+          const int u = u0 + vstride * k;
+          if (u >= nW) break;
+          const int q = u / W, col = u - q * W;
+          const int var = col & 3;
+          const int comp = (q >= N) + (q >= 2 * N);
+          C x = v[k];
+          if ((comp == 0 && (var & 1)) != (comp == 1 && (var >> 1))) { x.x = -x.x; x.y = -x.y; }
+          vt[u] = x;
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_addr(vfull + (kb & 1)));
+    };
+    for (int64_t kb = 0; kb < nmine && kb < 2; ++kb) gather(kb);
+    for (int64_t kb = 0; kb < nmine; ++kb) {
+      const int b = (int)(kb & 1);
+      bool ok = true;
+      if (lane == 0) ok = !ctl[0] && mbar_wait(smem_addr(done + b), (uint32_t)((kb >> 1) & 1));
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) {
+        if (lane == 0) fail();
+        break;
+      }
+      int64_t base[4];
+      bases(kb, base);
+      const C* red = red0 + (size_t)b * G * nW;
+      for (int u = vl; u < nW; u += vstride) {
+        const int q = u / W, col = u - q * W;
+        const int var = col & 3, rg = col >> 2;
+        if (rg >= nr || base[var] < 0) continue;
+        C sum = red[u];
+        for (int gg = 1; gg < G; ++gg) sum = cadd(sum, red[(size_t)gg * nW + u]);
+        const int comp = (q >= N) + (q >= 2 * N);
+        if ((comp == 0 && (var & 1)) != (comp == 1 && (var >> 1))) { sum.x = -sum.x; sum.y = -sum.y; }
+        t[(int64_t)(rhs0 + rg) * rhs_stride + base[var] + LM * q] = sum;
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_addr(rfree + b));
+      if (kb + 2 < nmine) gather(kb + 2);
+    }
+    return;
+  }
+
+  if (tid >= nc) {  // producer warp
+    if (lane == 0) {
+      const uint64_t policy = l2_evict_first_policy();
+      int64_t ch = 0;
+      for (; ch < total; ++ch) {
+        if (ctl[0]) break;
+        const int s = (int)(ch % nstage);
+        const int64_t use = ch / nstage;
+        if (use > 0 && !mbar_wait(smem_addr(empty + s), (uint32_t)((use - 1) & 1))) {
+          fail();
+          break;
+        }
+        const int64_t kb = ch / cpb;
+        const int c0 = (int)(ch - kb * cpb) * cq;
+        const int ncols = min(cq, n - c0);
+        const C* src = inv + (blockIdx.x + kb * gridDim.x) * (int64_t)n * n + (int64_t)c0 * n;
+        const uintptr_t a = reinterpret_cast<uintptr_t>(src), al = a & ~(uintptr_t)15;
+        const uint32_t bytes = (uint32_t)(((a - al) + (size_t)ncols * n * sizeof(C) + 15) & ~(size_t)15);
+        const uint32_t bar = smem_addr(full + s);
+        mbar_expect_tx(bar, bytes);
+        bulk_to_shared_stream(smem_addr(stg + (size_t)s * stage_elems), reinterpret_cast<const void*>(al), bytes, bar,
+                              policy);
+      }
+      // the copies still in flight land before the CTA may end
+      for (int64_t k = ch > nstage ? ch - nstage : 0; k < ch; ++k)
+        if (!mbar_wait(smem_addr(full + (k % nstage)), (uint32_t)((k / nstage) & 1))) atomicOr(status, 4);
+    }
+    return;
+  }
+
+  // consumer warps
+  const int nrow = n / RW;
+  const int nact = G * nrow;
+  const int g = tid / nrow, rp = tid - g * nrow;
+  int64_t ch = 0;
+  for (int64_t kb = 0; kb < nmine; ++kb) {
+    const int b = (int)(kb & 1);
+    bool ok = !ctl[0] && mbar_wait(smem_addr(vfull + b), (uint32_t)((kb >> 1) & 1));
+    const C* vt = vt0 + (size_t)b * nW;
+    C acc[RW][W];
+#pragma unroll
+    for (int h = 0; h < RW; ++h)
+#pragma unroll
+      for (int c = 0; c < W; ++c) acc[h][c] = czero<C>();
+    for (int cc = 0; cc < cpb && ok; ++cc, ++ch) {
+      const int s = (int)(ch % nstage);
+      ok = !ctl[0] && mbar_wait(smem_addr(full + s), (uint32_t)((ch / nstage) & 1));
+      if (!ok) break;
+      if (tid < nact) {
+        const int c0 = cc * cq;
+        const int ncols = min(cq, n - c0);
+        const C* src = inv + (blockIdx.x + kb * gridDim.x) * (int64_t)n * n + (int64_t)c0 * n;
+        const int shift = (int)((reinterpret_cast<uintptr_t>(src) & 15) / sizeof(C));
+        const C* A = stg + (size_t)s * stage_elems + shift + RW * rp;
+        const C* xv = vt + (size_t)c0 * W;
+#pragma unroll 2
+        for (int ql = g; ql < ncols; ql += G) {
+          C m[RW];
+          if constexpr (PAIR) {
+            const float4 mm = *reinterpret_cast<const float4*>(A + ql * n);
+            m[0] = make_c<C>(mm.x, mm.y);
+            m[1] = make_c<C>(mm.z, mm.w);
+          } else {
+            m[0] = A[ql * n];
+          }
+          const C* xq = xv + ql * W;
+#pragma unroll
+          for (int c = 0; c < W; ++c) {
+            const C xc = xq[c];
+#pragma unroll
+            for (int h = 0; h < RW; ++h) acc[h][c] = cfma(m[h], xc, acc[h][c]);
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_addr(empty + s));
+    }
+    if (ok && kb >= 2) ok = !ctl[0] && mbar_wait(smem_addr(rfree + b), (uint32_t)(((kb >> 1) - 1) & 1));
+    if (!ok) {
+      if (lane == 0) fail();
+      break;
+    }
+    if (tid < nact) {
+      C* red = red0 + (size_t)b * G * nW;
+#pragma unroll
+      for (int h = 0; h < RW; ++h)
+#pragma unroll
+        for (int c = 0; c < W; ++c) red[((size_t)g * n + RW * rp + h) * W + c] = acc[h][c];
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(smem_addr(done + b));
+  }
+}
+
+// Stream-kernel launch geometry: chunk columns, stages, stage size, column
+// groups, consumer threads, shared memory and CTAs per SM.
+struct GemvStream {
+  int cq, nstage, stage_elems, G, nc, nv, ctas;
+  size_t smem;
+};
+
+// cq = 0 when no stage of even one column fits beside the vectors.
+template <typename T>
+static GemvStream gemv_stream_geometry(int n, int rg, int chunk_cols, bool pair) {
+  const size_t cs = sizeof(cplx_t<T>);
+  GemvStream g{};
+  const int nrow = pair ? n / 2 : n;
+  g.G = std::max(1, std::min(4, 256 / nrow));
+  g.nc = (g.G * nrow + 31) / 32 * 32;
+  g.nv = std::max(1, std::min(4, (384 - g.nc - 32) / 32));
+  const size_t fixed = 256 + (size_t)2 * n * 4 * rg * cs + (size_t)2 * g.G * n * 4 * rg * cs;
+  const size_t budget = 112 * 1024;  // two CTAs per SM
+  const size_t stage_target = 16 * 1024;
+  int cq = chunk_cols > 0 ? std::min(chunk_cols, n) : std::max(1, (int)(stage_target / ((size_t)n * cs)));
+  cq = std::min(cq, n);
+  auto stage_bytes = [&](int c) { return (((size_t)n * c + 2) * cs + 15) / 16 * 16; };
+  while (cq > 1 && fixed + 2 * stage_bytes(cq) > 220 * 1024) --cq;
+  if (fixed + 2 * stage_bytes(cq) > 220 * 1024) { g.cq = 0; return g; }
+  g.cq = cq;
+  g.stage_elems = (int)(stage_bytes(cq) / cs);
+  g.nstage = 8;
+  while (g.nstage > 2 && fixed + (size_t)g.nstage * stage_bytes(cq) > budget) --g.nstage;
+  g.smem = fixed + (size_t)g.nstage * stage_bytes(cq);
+  g.ctas = g.smem <= budget ? 2 : 1;
+  return g;
+}
+
 template <typename T>
 void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
                      cudaStream_t st, int pass, int skip_stride) {
@@ -697,6 +1038,41 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
     case 1: launch_strided_pass<T, false>(s, 3 * N, nrhs, st); break;
     case 2: {
       const int n = 3 * N;
+      const int rg_s = nrhs >= 4 ? 4 : 1;
+      const bool pair = std::is_same<T, float>::value && n % 2 == 0;
+      const GemvStream g = gemv_stream_geometry<T>(n, rg_s, sh.gemv_chunk, pair);
+      if (pr.sym && sh.gemv_mode != 0 && pr.gemv_status.p && n <= 192 && g.cq > 0) {
+        const int rg = rg_s;
+        int dev = 0, nsm = 0;
+        VS_CUDA(cudaGetDevice(&dev));
+        VS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        const int64_t nblk = (int64_t)(L / 2 + 1) * (M / 2 + 1);
+        const int want = sh.gemv_ti > 0 ? std::min(sh.gemv_ti, 2) : g.ctas;
+        int* status = pr.gemv_status.as<int>();
+#define VS_GS(RGV, PR)                                                                                        \
+  {                                                                                                           \
+    auto k = k_block_gemv_stream<T, RGV, PR>;                                                                 \
+    set_kernel_smem((const void*)k, g.smem);                                                                  \
+    int fit = 0;                                                                                              \
+    VS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k, g.nc + 32 + 32 * g.nv, g.smem));          \
+    const dim3 grid((unsigned)std::min<int64_t>(nblk, (int64_t)nsm * std::max(1, std::min(want, fit))),     \
+                    ceil_div(nrhs, rg));                                                                      \
+    k<<<grid, g.nc + 32 + 32 * g.nv, g.smem, st>>>(t, inv, L, M, N, (int64_t)L * M * N * 3, nrhs, skip,        \
+                                                   skip_stride, g.cq, g.nstage, g.stage_elems, g.G, g.nc,     \
+                                                   g.nv, status);                                             \
+  }
+        if constexpr (std::is_same<T, float>::value) {
+          if (pair) {
+            if (rg == 4) VS_GS(4, true) else VS_GS(1, true)
+            VS_LAUNCH_CHECK();
+            break;
+          }
+        }
+        if (rg == 4) VS_GS(4, false) else VS_GS(1, false)
+#undef VS_GS
+        VS_LAUNCH_CHECK();
+        break;
+      }
       if (pr.sym) {
         const int Lb = L / 2 + 1, Mb = M / 2 + 1;
         const int nthr = sh.gemv_threads > 0 ? sh.gemv_threads : 256;
@@ -796,8 +1172,11 @@ void autotune_prec(vs_prec& pr, cudaStream_t st) {
             prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 3);
           });
   if (pr.sym) {
+    // register-direct kernel over blocks per CTA and CTA size, against the
+    // streamed kernel over CTAs per SM and chunk width
     float best = 1e30f;
-    int bti = 0, bth = 0;
+    int bti = 0, bth = 0, bmode = 0, bchunk = 0;
+    sh.gemv_mode = 0;
     for (int ti : {1, 2, 4}) {
       for (int th : {64, 128, 256}) {
         sh.gemv_ti = ti;
@@ -806,8 +1185,22 @@ void autotune_prec(vs_prec& pr, cudaStream_t st) {
         if (t < best) { best = t; bti = ti; bth = th; }
       }
     }
+    sh.gemv_mode = 1;
+    sh.gemv_threads = 0;
+    const int n = 3 * pr.N;
+    for (int ctas : {1, 2}) {
+      for (int cq : {0, 16, 32}) {
+        if (cq >= n) continue;
+        sh.gemv_ti = ctas;
+        sh.gemv_chunk = cq;
+        const float t = time_ms_prec(st, reps, [&] { prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 2); });
+        if (t < best) { best = t; bti = ctas; bth = 0; bmode = 1; bchunk = cq; }
+      }
+    }
     sh.gemv_ti = bti;
     sh.gemv_threads = bth;
+    sh.gemv_mode = bmode;
+    sh.gemv_chunk = bchunk;
   }
   VS_CUDA(cudaStreamSynchronize(st));
 }
