@@ -56,7 +56,6 @@ struct StridedArgs {
   int skip_stride;
 };
 
-// Register-resident z pass (vs_zreg.cu); false when R has no register kernel.
 // Two-level register z pass (vs_zpass.cuh); false when R has no instantiation.
 template <typename T>
 bool z_pass_two_level(const PipeArgs<T>& a, bool sym, bool cap, int nrhs, cudaStream_t st);

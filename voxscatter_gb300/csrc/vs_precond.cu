@@ -720,7 +720,8 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 //    are done with a block add its G partial sums and write the results
 //    (flips applied again) over the grid entries the inputs came from;
 //  * consumer warps: thread (g, rp) forms rows RW*rp .. +RW-1 (RW = 2 with
-//    PAIR: one 16-byte load per column) over the chunk columns q = g (mod G).
+//    PAIR: one 16-byte load per column) over the chunk columns q = g (mod G)
+//    and leaves its partial sums as [g][W][row].
 // Block boundaries therefore never stop the stream.  Hand-offs use mbarriers:
 // vfull[b] (vector warp -> consumers: buffer b holds the block's vectors),
 // done[b] (consumers -> vector warp: partial sums of buffer b written, its
@@ -844,8 +845,8 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
         const int q = u / W, col = u - q * W;
         const int var = col & 3, rg = col >> 2;
         if (rg >= nr || base[var] < 0) continue;
-        C sum = red[u];
-        for (int gg = 1; gg < G; ++gg) sum = cadd(sum, red[(size_t)gg * nW + u]);
+        C sum = red[(size_t)col * n + q];
+        for (int gg = 1; gg < G; ++gg) sum = cadd(sum, red[((size_t)gg * W + col) * n + q]);
         const int comp = (q >= N) + (q >= 2 * N);
         if ((comp == 0 && (var & 1)) != (comp == 1 && (var >> 1))) { sum.x = -sum.x; sum.y = -sum.y; }
         t[(int64_t)(rhs0 + rg) * rhs_stride + base[var] + LM * q] = sum;
@@ -940,11 +941,16 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
       break;
     }
     if (tid < nact) {
-      C* red = red0 + (size_t)b * G * nW;
+      // partial sums as [g][W][row]: the RW rows of a thread are adjacent
+      C* red = red0 + (size_t)b * G * nW + (size_t)g * W * n + RW * rp;
 #pragma unroll
-      for (int h = 0; h < RW; ++h)
-#pragma unroll
-        for (int c = 0; c < W; ++c) red[((size_t)g * n + RW * rp + h) * W + c] = acc[h][c];
+      for (int c = 0; c < W; ++c) {
+        if constexpr (PAIR) {
+          *reinterpret_cast<float4*>(red + (size_t)c * n) = make_float4(acc[0][c].x, acc[0][c].y, acc[1][c].x, acc[1][c].y);
+        } else {
+          red[(size_t)c * n] = acc[0][c];
+        }
+      }
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(smem_addr(done + b));

@@ -60,13 +60,18 @@ __device__ __forceinline__ void reg_dft(C (&a)[N], const C* tw) {
   }
 }
 
+// x columns per CTA: 16 (c64) / 8 (c128), doubled while TX*R2 leaves a partial
+// warp and the CTA stays within 512 (c64) / 256 (c128) threads.
 template <typename T>
-constexpr int z2_tx() { return std::is_same<T, float>::value ? 16 : 8; }
-
-constexpr int z2_threads(int R1, int R2, int tx) {
-  const int w = 3 * R1 > R2 ? 3 * R1 : R2;
-  return ((w * tx + 31) / 32) * 32;
+constexpr int z2_tx(int R2) {
+  const bool f = std::is_same<T, float>::value;
+  int tx = f ? 16 : 8;
+  while ((tx * R2) % 32 != 0 && 2 * tx * R2 <= (f ? 512 : 256)) tx *= 2;
+  return tx;
 }
+
+// One thread per stage-B item (TX * R2); stage A loops over its 3*R1*TX items.
+constexpr int z2_threads(int R2, int tx) { return ((R2 * tx + 31) / 32) * 32; }
 
 // CTAs per SM the capped variant holds the register allocation to: the live values of the
 // larger of stage A (a line of R2 points and its Stockham copy) and stage B
@@ -77,15 +82,15 @@ constexpr int z2_min_blocks(int R1, int R2) {
   const int cw = (int)(sizeof(T) / 4);
   const int a = 4 * R2 * cw, b = (6 * R1 + 12) * cw;
   const int need = (a > b ? a : b) + 24;
-  const int nb = 65536 / (z2_threads(R1, R2, z2_tx<T>()) * need);
+  const int nb = 65536 / (z2_threads(R2, z2_tx<T>(R2)) * need);
   return nb < 1 ? 1 : (nb > 8 ? 8 : nb);
 }
 
 template <typename T, int R1, int R2, bool CAP>
-__global__ void __launch_bounds__(z2_threads(R1, R2, z2_tx<T>()), CAP ? z2_min_blocks<T>(R1, R2) : 1)
+__global__ void __launch_bounds__(z2_threads(R2, z2_tx<T>(R2)), CAP ? z2_min_blocks<T>(R1, R2) : 1)
     k_z2(PipeArgs<T> a, int sym) {
   using C = cplx_t<T>;
-  constexpr int R = R1 * R2, TX = z2_tx<T>(), NT = z2_threads(R1, R2, TX);
+  constexpr int R = R1 * R2, TX = z2_tx<T>(R2), NT = z2_threads(R2, TX);
   if (a.skip && a.skip[blockIdx.z * a.skip_stride]) return;
   C* S = shmem<C>();  // [3][R1][R2][TX]
   C* tw = S + 3 * R * TX;
@@ -210,7 +215,7 @@ static constexpr ZSplit kZSplits[] = {
 
 template <typename T, int R1, int R2>
 static void launch_z2(const PipeArgs<T>& a, int sym, bool cap, int nrhs, cudaStream_t st) {
-  constexpr int TX = z2_tx<T>(), NT = z2_threads(R1, R2, TX);
+  constexpr int TX = z2_tx<T>(R2), NT = z2_threads(R2, TX);
   const size_t smem = (3ull * R1 * R2 * TX + R1 * R2) * sizeof(cplx_t<T>);
   auto k = cap ? k_z2<T, R1, R2, true> : k_z2<T, R1, R2, false>;
   set_kernel_smem((const void*)k, smem);
