@@ -49,21 +49,41 @@ __device__ __forceinline__ DD dd_fma(DD a, double x, double y) {
   return r;
 }
 
-// Accumulators: float inputs accumulate exactly-rounded products in double.
+// Accumulators.  c64 inputs: every product of two floats is formed exactly as
+// a float pair (p = a*b rounded, e = fma(a, b, -p)) and added into a
+// float-float sum by TwoSum (Knuth), about 48 bits of significand for the
+// few elements a thread visits; the pair is widened to double once, and the
+// grid-wide sums are taken in double.  This keeps compensated inner products
+// without a double-precision FMA per element.
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float b) {
+  const float s = __fadd_rn(hi, b);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  hi = s;
+  lo = __fadd_rn(lo, err);
+}
+__device__ __forceinline__ void ff_fma(float& hi, float& lo, float a, float b) {
+  const float pr = __fmul_rn(a, b);
+  const float e = __fmaf_rn(a, b, -pr);
+  ff_add(hi, lo, pr);
+  lo = __fadd_rn(lo, e);
+}
 template <typename T>
 struct Acc {
-  double re = 0, im = 0;
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
   __device__ __forceinline__ void dot(cplx_t<T> u, cplx_t<T> v) {  // += conj(u) v
-    re = fma((double)u.x, (double)v.x, re);
-    re = fma((double)u.y, (double)v.y, re);
-    im = fma((double)u.x, (double)v.y, im);
-    im = fma(-(double)u.y, (double)v.x, im);
+    ff_fma(rh, rl, u.x, v.x);
+    ff_fma(rh, rl, u.y, v.y);
+    ff_fma(ih, il, u.x, v.y);
+    ff_fma(ih, il, -u.y, v.x);
   }
   __device__ __forceinline__ void norm2(cplx_t<T> u) {
-    re = fma((double)u.x, (double)u.x, re);
-    re = fma((double)u.y, (double)u.y, re);
+    ff_fma(rh, rl, u.x, u.x);
+    ff_fma(rh, rl, u.y, u.y);
   }
-  __device__ __forceinline__ double2 value() const { return make_double2(re, im); }
+  __device__ __forceinline__ double2 value() const {
+    return make_double2((double)rh + (double)rl, (double)ih + (double)il);
+  }
 };
 template <>
 struct Acc<double> {
@@ -294,26 +314,29 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_omega(const cplx_t<T>* t, 
   }
 }
 
-// x += alpha ph + omega sh ; r = s - omega t ; ||r|| ; full-step test
+// x += alpha ph + omega sh ; r = s - omega t ; ||r|| ; full-step test ; and,
+// when the iteration continues, the next rho = rt^H r with its breakdown test
+// and beta = (rho_new/rho)(alpha/omega) (the first rho comes from k_bicg_rho)
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* x, cplx_t<T>* r, const cplx_t<T>* ph,
                                                         const cplx_t<T>* sh, const cplx_t<T>* sv, const cplx_t<T>* t,
-                                                        int64_t n, KState* states) {
+                                                        const cplx_t<T>* rt, int64_t n, KState* states) {
   using C = cplx_t<T>;
   KState* s = states + blockIdx.y;
   if (s->skip) return;
   const int64_t o = blockIdx.y * n;
-  x += o; r += o; ph += o; sh += o; sv += o; t += o;
+  x += o; r += o; ph += o; sh += o; sv += o; t += o; rt += o;
   const C al = ccast<C>(s->alpha), om = ccast<C>(s->omega);
-  Acc<T> a;
+  Acc<T> a, d;
   GRID_LOOP(i, n) {
     x[i] = cfma(om, sh[i], cfma(al, ph[i], x[i]));
     const C ri = csub(sv[i], cmul(om, t[i]));
     r[i] = ri;
     a.norm2(ri);
+    d.dot(rt[i], ri);
   }
-  double w[1] = {a.value().x}, tt[1];
-  if (grid_reduce<1>(w, s->partials, &s->counter, tt) && threadIdx.x == 0) {
+  double w[3] = {a.value().x, d.value().x, d.value().y}, tt[3];
+  if (grid_reduce<3>(w, s->partials, &s->counter, tt) && threadIdx.x == 0) {
     const double res = sqrt(tt[0]);
     const int k = s->iter2 + 2;
     if (k < s->resvec_cap) s->resvec[k] = res * s->res_scale;
@@ -337,6 +360,16 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* x, cplx_t<T>
     } else if (s->stag_window > 0 && k - s->best_iter2 >= 2 * s->stag_window) {
       s->flag = 3;  // stagnated (MATLAB flag 3)
       s->skip = 1;
+    }
+    if (!s->skip) {
+      const double2 rho = make_double2(tt[1], tt[2]);
+      if (cz(rho) || !cfinite(rho)) {
+        s->flag = cfinite(rho) ? 4 : 5;
+        s->skip = 1;
+      } else {
+        s->beta = cmul(cdiv(rho, s->rho), cdiv(s->alpha, s->omega));
+        s->rho = rho;
+      }
     }
   }
 }
@@ -450,7 +483,6 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
   const dim3 g(vec_grid(n), nrhs);
   const int* skip = &s->skip;
   const int ss = (int)(sizeof(KState) / sizeof(int));
-  k_bicg_rho<T><<<g, kRedThreads, 0, st>>>(rt, r, n, s);
   k_bicg_p<T><<<g, 256, 0, st>>>(p, r, v, n, s);
   if (pr) prec_apply<T>(*pr, p, ph, nrhs, skip, st, ss);
   else k_copy<T><<<dim3(vec_grid(n * nrhs)), 256, 0, st>>>(ph, p, n * nrhs);
@@ -462,13 +494,13 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
   else k_copy<T><<<dim3(vec_grid(n * nrhs)), 256, 0, st>>>(sh, sv, n * nrhs);
   matvec<T>(op, sh, t, nrhs, mode, skip, st, ss);
   k_bicg_omega<T><<<g, kRedThreads, 0, st>>>(t, sv, n, s);
-  k_bicg_xr<T><<<g, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, n, s);
+  k_bicg_xr<T><<<g, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, rt, n, s);
   VS_LAUNCH_CHECK();
 }
 
-// Kernels in one bicg_iteration: 7 solver kernels, 2 matvecs of 5 passes, and
+// Kernels in one bicg_iteration: 6 solver kernels, 2 matvecs of 5 passes, and
 // 2 preconditioner applies of 5 passes (or 2 copies without preconditioner).
-static int kernels_per_iteration(const vs_prec* pr) { return 7 + 10 + (pr ? 10 : 2); }
+static int kernels_per_iteration(const vs_prec* pr) { return 6 + 10 + (pr ? 10 : 2); }
 
 // BiCGSTAB on w.x (initial guesses already there) with initial residuals in
 // w.r, for nrhs right-hand sides.  The absolute tolerance of rhs r is
@@ -553,6 +585,10 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
     gc.key = key;
   }
   upload_states(w, h, st);
+  // rho of the initial residual; later ones come out of k_bicg_xr
+  k_bicg_rho<T><<<dim3(vec_grid(n), nrhs), kRedThreads, 0, st>>>(w.rt.as<C>(), w.r.as<C>(), n, s);
+  VS_LAUNCH_CHECK();
+  *launches += 1;
   std::vector<KState> cur(nrhs);
   const int max_launch = (maxit + per_graph - 1) / per_graph + 1;
   for (int it = 0; it < max_launch; ++it) {
