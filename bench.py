@@ -526,6 +526,16 @@ def run_passes(args):
                 gs[f"stream,ctas={b},chunk={cq}"] = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64",
                                                                      args.steps)[2]
         prec.set_shape("c64", **tuned_pr)
+        ys_ = {}
+        for yr in (0, 1):
+            op.set_shape("c64", y_reg=yr)
+            t = op.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", args.steps)
+            prec.set_shape("c64", y_reg=yr)
+            tp = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", args.steps)
+            ys_[f"y_reg={yr}"] = {"matvec": [t[1], t[3]], "prec": [tp[1], tp[3]]}
+        op.set_shape("c64", **tuned_op)
+        prec.set_shape("c64", **tuned_pr)
+        out["y_pass_ms"] = ys_
         out["z_pass_ms"] = zs
         out["gemv_ms"] = gs
     print(json.dumps(out), flush=True)

@@ -217,3 +217,52 @@ def test_z_lengths_both_z_kernels(api, R):
             for z_reg in (0, 1, 2):
                 op.set_shape(prec, z_reg=z_reg)
                 assert rel(op.apply(x, "notransp", prec), y_o) < tol, (prec, z_reg, exact_parity, op.PQR)
+
+
+Y_LENGTHS = [8, 9, 10, 12, 15, 16, 18, 20, 24, 25, 27, 30, 32, 36, 40, 45, 48, 50, 54, 60, 64, 72, 75, 80, 81, 90,
+             91, 96, 100, 108, 120, 125, 128, 135, 144, 150, 160, 162, 180, 192, 200, 216, 225, 240, 243, 250, 256]
+
+
+@pytest.mark.parametrize("n", Y_LENGTHS)
+def test_y_lengths_both_y_kernels(api, n):
+    """Every strided length with a two-level register kernel: the matvec's
+    y passes with Q = n forced (M = ceil(n/2)) and the preconditioner's y
+    passes with M = n, in c64 and c128, two-level and shared-memory Stockham,
+    against the oracle on a 3 x M x 2 block of voxels (tolerances in the
+    body)."""
+    from voxscatter_gb300.geometry import grid3d
+    rng = np.random.default_rng(n)
+    d, ko = 0.07, 2 * np.pi
+    for M, PQR, check_prec in (((n + 1) // 2, (0, n, 0), False), (n, (0, 0, 0), True)):
+        L, N = 3, 2
+        r = grid3d(np.arange(L) * d, np.arange(M) * d, np.arange(N) * d)
+        Toep = O.green_toeplitz(r, ko)
+        fN = O.fft_operator(O.circulant_nop_const(Toep))
+        idx3 = np.arange(3 * L * M * N)
+        op = api.Operator(L, M, N, idx3, 1.0, d ** 3, 3.0, toep=Toep, PQR=PQR)
+        if not check_prec:
+            assert op.PQR[1] == n
+        x = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
+        y_o = O.MVP(x, fN, np.ones((L, M, N)), d ** 3, 3.0, "notransp", idx3)
+        for prec, tol in (("c64", C64_TOL), ("c128", C128_TOL)):
+            for y_reg in (0, 1):
+                op.set_shape(prec, y_reg=y_reg)
+                assert rel(op.apply(x, "notransp", prec), y_o) < tol, (prec, y_reg, op.PQR)
+        if check_prec:
+            _, c1 = O.circ_1_level(Toep, L, M, N, 0, "off")
+            _, blk = O.circ_2_level(c1, L, M, N)
+            inv = O.invert_blocks(blk, 3.0, d ** 3)
+            pr = api.Preconditioner(op, shift=3.0, d=d ** 3)
+            z_o = O.mvp_circ_2_level(inv, x, L, M, N, idx3)
+            for y_reg in (0, 1):
+                pr.set_shape("c128", y_reg=y_reg)
+                assert rel(pr.apply(x, "c128"), z_o) < 1e-10, ("c128", y_reg, M)
+            # c64: the two kernels on the same FP32-inverted blocks agree to FFT
+            # rounding; against the FP64 oracle the FP32 inversion of these
+            # blocks (shift 3, d = 0.07) bounds the error
+            pr.set_shape("c64", y_reg=0)
+            z0 = pr.apply(x, "c64")
+            pr.set_shape("c64", y_reg=1)
+            z1 = pr.apply(x, "c64")
+            assert rel(z1, z0) < 2e-6, M
+            assert rel(z1, z_o) < 1e-3, M

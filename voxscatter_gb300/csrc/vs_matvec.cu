@@ -299,6 +299,7 @@ void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaS
 
 template <typename T, bool INV>
 void launch_strided_pass(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st) {
+  if (a.two_level == 1 && strided_two_level<T, INV>(a, nplanes, nrhs, st)) return;
   const int tx = 1 << a.lg_tx;
   dim3 grid(ceil_div(a.xext, tx), nplanes, nrhs);
   const size_t smem = (2ull * a.plan.n * tx + a.plan.n) * sizeof(cplx_t<T>);
@@ -334,6 +335,7 @@ static StridedArgs<T> y_pass_args(const vs_op& op, const PipeArgs<T>& a, bool in
   s.tw = a.twQ;
   s.skip = a.skip;
   s.skip_stride = a.skip_stride;
+  s.two_level = sh.y_reg == 1 ? 1 : 0;
   return s;
 }
 
@@ -489,6 +491,7 @@ void fft_strided(cplx_t<T>* data, int xext, int n, int64_t row_stride, int na, i
   s.tw = ax.tw<T>();
   s.skip = nullptr;
   s.skip_stride = 0;
+  s.two_level = 0;
   launch_strided_pass<T, INV>(s, na * nb, 1, st);
 }
 
@@ -553,7 +556,13 @@ void autotune_op(vs_op& op, cudaStream_t st) {
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 0);
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 4);
           });
+  sh.y_reg = 0;
   best_of(&sh.lg_tx_y, 1, 5, [&](int v) { return (2ull * op.Q * (1 << v) + op.Q) * cs <= lim; },
+          [&] {
+            matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 1);
+            matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 3);
+          });
+  best_of(&sh.y_reg, 0, 1, [&](int) { return true; },
           [&] {
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 1);
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 3);

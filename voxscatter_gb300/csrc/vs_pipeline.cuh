@@ -54,7 +54,12 @@ struct StridedArgs {
   const C* tw;
   const int* skip;
   int skip_stride;
+  int two_level;  // 1: two-level register kernel (vs_spass.cuh) when the length has one
 };
+
+// Two-level strided pass (vs_spass.cuh); false when the length has no instantiation.
+template <typename T, bool INV>
+bool strided_two_level(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st);
 
 // Two-level register z pass (vs_zpass.cuh); false when R has no instantiation.
 template <typename T>

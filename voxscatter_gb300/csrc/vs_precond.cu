@@ -1039,6 +1039,7 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
   s.tw = pr.axM.tw<T>();
   s.skip = skip;
   s.skip_stride = skip_stride;
+  s.two_level = sh.y_reg == 1 ? 1 : 0;
   switch (pass) {
     case 0: launch_x_pass<T>(a, false, MODE_PLAIN, nrhs, st); break;
     case 1: launch_strided_pass<T, false>(s, 3 * N, nrhs, st); break;
@@ -1172,7 +1173,13 @@ void autotune_prec(vs_prec& pr, cudaStream_t st) {
             prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 0);
             prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 4);
           });
+  sh.y_reg = 0;
   best_of(&sh.lg_tx_y, 1, 5, [&](int v) { return (2ull * pr.M * (1 << v) + pr.M) * cs <= lim; },
+          [&] {
+            prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 1);
+            prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 3);
+          });
+  best_of(&sh.y_reg, 0, 1, [&](int) { return true; },
           [&] {
             prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 1);
             prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 3);
