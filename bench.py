@@ -156,11 +156,16 @@ def _apply_shapes(args, op, prec):
 
 def _pass_names(op, prec):
     """Kernel of each pipeline launch under the tuned c64 launch shapes."""
-    zr = op.shape("c64")["z_reg"]
-    gm = prec.shape("c64")["gemv_mode"]
-    names_mv = ["k_xf", "k_strided_fwd", "k_z2" if zr in (1, 2) else "k_z", "k_strided_inv", "k_xi"]
-    names_pc = ["prec_k_xf", "prec_k_strided_fwd", "k_block_gemv_stream" if gm == 1 else "k_block_gemv_sym",
-                "prec_k_strided_inv", "prec_k_xi"]
+    so, sp = op.shape("c64"), prec.shape("c64")
+
+    def xy(sh, pre):
+        x2, y2 = sh["x_reg"] == 1, sh["y_reg"] == 1
+        return (pre + ("k_x2_fwd" if x2 else "k_xf"), pre + ("k_s2_fwd" if y2 else "k_strided_fwd"),
+                pre + ("k_s2_inv" if y2 else "k_strided_inv"), pre + ("k_x2_inv" if x2 else "k_xi"))
+    a, b, c, d = xy(so, "")
+    names_mv = [a, b, "k_z2" if so["z_reg"] in (1, 2) else "k_z", c, d]
+    a, b, c, d = xy(sp, "prec_")
+    names_pc = [a, b, "k_block_gemv_stream" if sp["gemv_mode"] == 1 else "k_block_gemv_sym", c, d]
     return names_mv, names_pc
 
 

@@ -283,6 +283,7 @@ typedef struct vs_shape {
   int z_reg;       /* z pass: 0 shared-memory Stockham, 1 two-level registers,
                       2 two-level with a register cap for occupancy          */
   int y_reg;       /* y passes: 0 shared-memory Stockham, 1 two-level registers */
+  int x_reg;       /* x passes: 0 shared-memory Stockham, 1 two-level registers */
 } vs_shape;
 int vs_op_get_shape(const vs_op* op, int precision, vs_shape* shape);
 int vs_op_set_shape(vs_op* op, int precision, const vs_shape* shape);
@@ -300,6 +301,7 @@ typedef struct vs_prec_shape {
   int gemv_mode;
   int gemv_chunk;
   int y_reg;       /* y passes: 0 shared-memory Stockham, 1 two-level registers */
+  int x_reg;       /* x passes: 0 shared-memory Stockham, 1 two-level registers */
 } vs_prec_shape;
 int vs_prec_get_shape(const vs_prec* prec, int precision, vs_prec_shape* shape);
 int vs_prec_set_shape(vs_prec* prec, int precision, const vs_prec_shape* shape);

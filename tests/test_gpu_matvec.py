@@ -266,3 +266,52 @@ def test_y_lengths_both_y_kernels(api, n):
             z1 = pr.apply(x, "c64")
             assert rel(z1, z0) < 2e-6, M
             assert rel(z1, z_o) < 1e-3, M
+
+
+X_LENGTHS = Y_LENGTHS + [105]
+
+
+@pytest.mark.parametrize("n", X_LENGTHS)
+def test_x_lengths_both_x_kernels(api, n):
+    """Every x length with a two-level register kernel: the matvec's x passes
+    with P = n forced (L = ceil(n/2), a quarter of the voxels absent, varying
+    diagonals, all three modes) and the preconditioner's x passes with L = n,
+    c64 and c128, two-level and shared-memory Stockham, against the oracle
+    (tolerances in the body)."""
+    from voxscatter_gb300.geometry import grid3d
+    rng = np.random.default_rng(1000 + n)
+    d, ko = 0.07, 2 * np.pi
+    for L, PQR, check_prec in (((n + 1) // 2, (n, 0, 0), False), (n, (0, 0, 0), True)):
+        M, N = 2, 2
+        r = grid3d(np.arange(L) * d, np.arange(M) * d, np.arange(N) * d)
+        Toep = O.green_toeplitz(r, ko)
+        fN = O.fft_operator(O.circulant_nop_const(Toep))
+        nD = L * M * N
+        vox = np.sort(rng.choice(nD, size=max(1, (3 * nD) // 4), replace=False))
+        idx3 = np.concatenate([vox, nD + vox, 2 * nD + vox])
+        Mc = d ** 3 * ((1 + 0.3 * rng.normal(size=(L, M, N))) + 0.1j * rng.normal(size=(L, M, N)))
+        Mr = 1 + 0.2j * rng.normal(size=(L, M, N))
+        Gram = 3.0 + 0.05 * rng.normal(size=(L, M, N))
+        op = api.Operator(L, M, N, idx3, Mr, Mc, Gram, toep=Toep, PQR=PQR)
+        if not check_prec:
+            assert op.PQR[0] == n
+        x = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
+        for flag in ("notransp", "transp"):
+            y_o = O.MVP(x, fN, Mr, Mc, Gram, flag, idx3)
+            for prec, tol in (("c64", C64_TOL), ("c128", C128_TOL)):
+                for x_reg in (0, 1):
+                    op.set_shape(prec, x_reg=x_reg)
+                    assert rel(op.apply(x, flag, prec), y_o) < tol, (flag, prec, x_reg, op.PQR)
+        y_t = MVP_plain_transpose(x, fN, Mr, Mc, Gram, idx3)
+        for x_reg in (0, 1):
+            op.set_shape("c128", x_reg=x_reg)
+            assert rel(op.apply(x, "plain_transp", "c128"), y_t) < C128_TOL, (x_reg, op.PQR)
+        if check_prec:
+            pr = api.Preconditioner(op, shift=3.0, d=d ** 3)
+            z = {}
+            for prec in ("c64", "c128"):
+                for x_reg in (0, 1):
+                    pr.set_shape(prec, x_reg=x_reg)
+                    z[prec, x_reg] = pr.apply(x, prec)
+            assert rel(z["c128", 1], z["c128", 0]) < 1e-12, L
+            assert rel(z["c64", 1], z["c64", 0]) < 2e-6, L

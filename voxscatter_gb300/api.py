@@ -170,7 +170,7 @@ class Operator:
         sh = L.vs_shape()
         L.check(self.ctx._lib.vs_op_get_shape(self.h, L.VS_C64 if precision == "c64" else L.VS_C128, C.byref(sh)))
         return dict(lg_lines_x=sh.lg_lines_x, lg_tile_y=sh.lg_tile_y, lg_tile_z=sh.lg_tile_z, z_reg=sh.z_reg,
-                    y_reg=sh.y_reg)
+                    y_reg=sh.y_reg, x_reg=sh.x_reg)
 
     def set_shape(self, precision="c64", **kw):
         cur = self.shape(precision)
@@ -299,7 +299,8 @@ class Preconditioner:
         L.check(self.ctx._lib.vs_prec_get_shape(self.h, L.VS_C64 if precision == "c64" else L.VS_C128,
                                                 C.byref(sh)))
         return dict(lg_lines_x=sh.lg_lines_x, lg_tile_y=sh.lg_tile_y, gemv_blocks=sh.gemv_blocks,
-                    gemv_threads=sh.gemv_threads, gemv_mode=sh.gemv_mode, gemv_chunk=sh.gemv_chunk, y_reg=sh.y_reg)
+                    gemv_threads=sh.gemv_threads, gemv_mode=sh.gemv_mode, gemv_chunk=sh.gemv_chunk, y_reg=sh.y_reg,
+                    x_reg=sh.x_reg)
 
     def set_shape(self, precision="c64", **kw):
         cur = self.shape(precision)

@@ -835,6 +835,7 @@ int vs_op_get_shape(const vs_op* op, int precision, vs_shape* shape) {
   shape->lg_tile_z = s.lg_tx_z;
   shape->z_reg = s.z_reg;
   shape->y_reg = s.y_reg;
+  shape->x_reg = s.x_reg;
   return VS_OK;
 }
 
@@ -848,6 +849,7 @@ int vs_prec_get_shape(const vs_prec* prec, int precision, vs_prec_shape* shape) 
   shape->gemv_mode = s.gemv_mode;
   shape->gemv_chunk = s.gemv_chunk;
   shape->y_reg = s.y_reg;
+  shape->x_reg = s.x_reg;
   return VS_OK;
 }
 
@@ -877,8 +879,10 @@ int vs_prec_set_shape(vs_prec* prec, int precision, const vs_prec_shape* shape) 
     s.gemv_threads = shape->gemv_threads;
     VS_REQUIRE(shape->y_reg >= -1 && shape->y_reg <= 1, "y_reg must be -1, 0 or 1");
     s.gemv_mode = shape->gemv_mode;
+    VS_REQUIRE(shape->x_reg >= -1 && shape->x_reg <= 1, "x_reg must be -1, 0 or 1");
     s.gemv_chunk = shape->gemv_chunk;
     s.y_reg = shape->y_reg;
+    s.x_reg = shape->x_reg;
   });
 }
 
@@ -903,8 +907,10 @@ int vs_op_set_shape(vs_op* op, int precision, const vs_shape* shape) {
     s.lg_tx_z = shape->lg_tile_z;
     VS_REQUIRE(shape->z_reg >= -1 && shape->z_reg <= 2, "z_reg must be -1, 0, 1 or 2");
     VS_REQUIRE(shape->y_reg >= -1 && shape->y_reg <= 1, "y_reg must be -1, 0 or 1");
+    VS_REQUIRE(shape->x_reg >= -1 && shape->x_reg <= 1, "x_reg must be -1, 0 or 1");
     s.z_reg = shape->z_reg;
     s.y_reg = shape->y_reg;
+    s.x_reg = shape->x_reg;
     op->kw.graph32.reset();
     op->kw.graph64.reset();
   });

@@ -48,6 +48,7 @@ struct PassShape {
   int lg_lpb_x = -1;   // x passes: lines per CTA
   int lg_tx_y = -1;    // y passes: x-tile width
   int y_reg = -1;      // y passes: 1 two-level register kernel, 0 shared-memory Stockham, -1 default (Stockham)
+  int x_reg = -1;      // x passes: 1 two-level register kernel, 0 shared-memory Stockham, -1 default (Stockham)
   int lg_tx_z = -1;    // z pass: x-tile width
   int gemv_ti = 0;     // preconditioner GEMV: stored blocks per CTA (direct) or CTAs per SM (streamed); 0 = default
   int gemv_threads = 0;

@@ -265,6 +265,10 @@ void ensure_scratch(vs_op& op, int nrhs, size_t elem_bytes) {
 
 template <typename T>
 void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaStream_t st) {
+  if (a.two_level == 1) {
+    if (!inverse && x_two_level<T, false>(a, mode, nrhs, st)) return;
+    if (inverse && x_two_level<T, true>(a, mode, nrhs, st)) return;
+  }
   const int nlines = a.M * a.N * 3;
   const int lpb = 1 << a.lg_lpb;
   dim3 grid(ceil_div(nlines, lpb), nrhs);
@@ -358,6 +362,7 @@ static PipeArgs<T> pipe_args(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, 
   a.pP = op.ax[0].plan; a.pQ = op.ax[1].plan; a.pR = op.ax[2].plan;
   const PassShape& sh = op.shape[std::is_same<T, float>::value ? 0 : 1];
   a.lg_lpb = sh.lg_lpb_x >= 0 ? sh.lg_lpb_x : ilog2(pick_lpb(op.P, sizeof(C)));
+  a.two_level = sh.x_reg == 1 ? 1 : 0;
   a.lg_tx = sh.lg_tx_z >= 0 ? sh.lg_tx_z : ilog2(pick_tile(op.R, sizeof(C), 3));
   a.skip = skip;
   a.skip_stride = skip_stride;
@@ -551,7 +556,13 @@ void autotune_op(vs_op& op, cudaStream_t st) {
     }
     *field = arg;
   };
+  sh.x_reg = 0;
   best_of(&sh.lg_lpb_x, 0, 4, [&](int v) { return (2ull * (1 << v) * op.P + op.P) * cs <= lim && (1 << v) <= 256; },
+          [&] {
+            matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 0);
+            matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 4);
+          });
+  best_of(&sh.x_reg, 0, 1, [&](int) { return true; },
           [&] {
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 0);
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 4);

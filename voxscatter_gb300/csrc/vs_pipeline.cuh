@@ -35,6 +35,7 @@ struct PipeArgs {
   int lg_tx;   // log2 x-tile width of the z pass
   const int* skip;   // right-hand side r is skipped when skip[r * skip_stride] != 0
   int skip_stride;
+  int two_level;     // x passes: 1 two-level register kernel (vs_xpass.cuh) when P has one
 };
 
 // ---- strided-axis pass (y of the pipeline; y and z of the setup FFTs) ----
@@ -56,6 +57,10 @@ struct StridedArgs {
   int skip_stride;
   int two_level;  // 1: two-level register kernel (vs_spass.cuh) when the length has one
 };
+
+// Two-level x pass (vs_xpass.cuh); false when P has no instantiation.
+template <typename T, bool INV>
+bool x_two_level(const PipeArgs<T>& a, int mode, int nrhs, cudaStream_t st);
 
 // Two-level strided pass (vs_spass.cuh); false when the length has no instantiation.
 template <typename T, bool INV>

@@ -1018,6 +1018,7 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
   }
   a.skip = skip;
   a.skip_stride = skip_stride;
+  a.two_level = sh.x_reg == 1 ? 1 : 0;
   StridedArgs<T> s{};
   s.src = t; s.dst = t;
   s.xext = L; s.n_in = M; s.n_out = M;
@@ -1168,7 +1169,13 @@ void autotune_prec(vs_prec& pr, cudaStream_t st) {
     }
     *field = arg;
   };
+  sh.x_reg = 0;
   best_of(&sh.lg_lpb_x, 0, 4, [&](int v) { return (2ull * (1 << v) * pr.L + pr.L) * cs <= lim; },
+          [&] {
+            prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 0);
+            prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 4);
+          });
+  best_of(&sh.x_reg, 0, 1, [&](int) { return true; },
           [&] {
             prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 0);
             prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 4);

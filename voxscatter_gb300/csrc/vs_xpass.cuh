@@ -1,0 +1,155 @@
+// Two-level x passes: gather + zero-pad + FFT along x (XF), and IFFT along x
+// + crop + diagonal term + scatter (XI), for lines of length P = R1 * R2
+// (R1 the largest divisor <= sqrt(P), R2 <= 32).  Same arithmetic as k_xf /
+// k_xi in vs_matvec.cu (which handle the lengths not instantiated here).
+//
+// A CTA owns NL = 256 / R2 lines (line = (j, k, comp), x contiguous):
+//   XF A : item (n1, line): x points n1 + R1*n2 (< L) gathered through map3
+//          (with the mode's conjugation / diagonal) into registers, R2-point
+//          DFT, twiddle, one shared store;
+//      B : item (k2, line): R1-point DFT, outputs k2 + R2*k1 stored to T1;
+//   XI B': item (k2, line): T1 entries k2 + R2*k1, inverse R1-point DFT,
+//          conjugate twiddle, one shared store;
+//      A': item (n1, line): inverse R2-point DFT, entries n1 + R1*n2 (< L)
+//          combined with the diagonal term and scattered through map3.
+// Shared layout [line][n1][k2] with an odd row stride R2 | 1, so consecutive
+// n1 (stage A, A') and consecutive k2 (stage B, B') are both conflict-free
+// while the global accesses of every stage run along x.
+// Instantiated per precision in vs_xpass_c64.cu and vs_xpass_c128.cu.
+#pragma once
+#include "vs_spass.cuh"
+
+namespace vs {
+
+constexpr int kX2Threads = 256;
+
+template <typename T>
+__device__ __forceinline__ cplx_t<T> x2_gather(const PipeArgs<T>& a, const cplx_t<T>* x, int pos, int mode) {
+  using C = cplx_t<T>;
+  if (pos < 0) return czero<C>();
+  C v = x[pos];
+  if (mode == VS_TRANSP) v = cmul(a.d2.at(pos), v);
+  else if (mode == VS_CONJTRANSP) v = cmul(a.d2.at(pos), cconj(v));
+  return v;
+}
+
+template <typename T, int R1, int R2, bool INV>
+__global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
+  using C = cplx_t<T>;
+  constexpr int P = R1 * R2, NL = kX2Threads / R2, RS = R2 | 1;
+  if (a.skip && a.skip[blockIdx.y * a.skip_stride]) return;
+  C* S = shmem<C>();  // [NL][R1][RS]
+  C* tw = S + NL * R1 * RS;
+  for (int i = threadIdx.x; i < P; i += kX2Threads) tw[i] = __ldg(a.twP + i);
+  const int rhs = blockIdx.y;
+  const C* x = a.x + (int64_t)rhs * a.n3;
+  const int64_t t1off = (int64_t)rhs * P * a.M * a.N * 3;
+  const int nlines = a.M * a.N * 3, MN = a.M * a.N;
+  const int line0 = blockIdx.x * NL;
+  __syncthreads();
+  if constexpr (!INV) {
+    C* t1 = a.t1 + t1off;
+    for (int it = threadIdx.x; it < R1 * NL; it += kX2Threads) {
+      const int n1 = it % R1, l = it / R1, line = line0 + l;
+      C v[R2];
+      if (line < nlines) {
+        const int c = line / MN, jk = line - c * MN;
+        const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2) {
+          const int i = n1 + R1 * n2;
+          v[n2] = i < a.L ? x2_gather(a, x, __ldg(map + i), mode) : czero<C>();
+        }
+      } else {
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2) v[n2] = czero<C>();
+      }
+      reg_dft<R2, R2, 1, R1, false, C>(v, tw);
+      C* s = S + (l * R1 + n1) * RS;
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2) s[k2] = (k2 == 0 || n1 == 0) ? v[k2] : cmul(v[k2], tw[n1 * k2]);
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < R2 * NL; it += kX2Threads) {
+      const int k2 = it % R2, l = it / R2, line = line0 + l;
+      if (line >= nlines) continue;
+      C u[R1];
+#pragma unroll
+      for (int n1 = 0; n1 < R1; ++n1) u[n1] = S[(l * R1 + n1) * RS + k2];
+      reg_dft<R1, R1, 1, R2, false, C>(u, tw);
+      C* out = t1 + (int64_t)line * P;
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) out[k2 + R2 * k1] = u[k1];
+    }
+  } else {
+    const C* t1 = a.t1 + t1off;
+    C* y = a.y + (int64_t)rhs * a.n3;
+    for (int it = threadIdx.x; it < R2 * NL; it += kX2Threads) {
+      const int k2 = it % R2, l = it / R2, line = line0 + l;
+      C u[R1];
+      const C* in = t1 + (int64_t)line * P;
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) u[k1] = line < nlines ? in[k2 + R2 * k1] : czero<C>();
+      reg_dft<R1, R1, 1, R2, true, C>(u, tw);
+#pragma unroll
+      for (int n1 = 0; n1 < R1; ++n1)
+        S[(l * R1 + n1) * RS + k2] = (n1 == 0 || k2 == 0) ? u[n1] : cmul(u[n1], twid<true>(tw, n1 * k2));
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < R1 * NL; it += kX2Threads) {
+      const int n1 = it % R1, l = it / R1, line = line0 + l;
+      if (line >= nlines || n1 >= a.L) continue;
+      C v[R2];
+      const C* s = S + (l * R1 + n1) * RS;
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2) v[k2] = s[k2];
+      reg_dft<R2, R2, 1, R1, true, C>(v, tw);
+      const int c = line / MN, jk = line - c * MN;
+      const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
+#pragma unroll
+      for (int n2 = 0; n2 < R2; ++n2) {
+        const int i = n1 + R1 * n2;
+        if (i >= a.L) continue;
+        const int pos = __ldg(map + i);
+        if (pos < 0) continue;
+        const C conv = v[n2];
+        C out;
+        if (mode == MODE_PLAIN) {
+          out = conv;
+        } else {
+          const C xv = x[pos];
+          if (mode == VS_NOTRANSP) out = csub(cmul(a.d1.at(pos), xv), cmul(a.d2.at(pos), conv));
+          else if (mode == VS_TRANSP) out = csub(cmul(a.d1.at(pos), xv), conv);
+          else out = csub(cmul(a.d1c.at(pos), xv), cconj(conv));
+        }
+        y[pos] = out;
+      }
+    }
+  }
+}
+
+template <typename T, int R1, int R2, bool INV>
+static void launch_x2(const PipeArgs<T>& a, int mode, int nrhs, cudaStream_t st) {
+  constexpr int NL = kX2Threads / R2, RS = R2 | 1;
+  const size_t smem = (size_t)(NL * R1 * RS + R1 * R2) * sizeof(cplx_t<T>);
+  auto k = k_x2<T, R1, R2, INV>;
+  set_kernel_smem((const void*)k, smem);
+  const int nlines = a.M * a.N * 3;
+  k<<<dim3(ceil_div(nlines, NL), nrhs), kX2Threads, smem, st>>>(a, mode);
+  VS_LAUNCH_CHECK();
+}
+
+template <typename T, bool INV>
+bool x_two_level(const PipeArgs<T>& a, int mode, int nrhs, cudaStream_t st) {
+  switch (a.P) {
+#define VS_X2_CASE(R1, R2)                      \
+  case R1 * R2:                                 \
+    launch_x2<T, R1, R2, INV>(a, mode, nrhs, st); \
+    return true;
+    VS_S2_LIST(VS_X2_CASE)
+#undef VS_X2_CASE
+    default: return false;
+  }
+}
+
+}  // namespace vs
