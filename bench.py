@@ -506,7 +506,12 @@ def run_passes(args):
     ctx.synchronize()
     torch.cuda.nvtx.range_pop()
     names_mv, names_pc = _pass_names(op, prec)
+    xd = torch.randn(op.n3, dtype=torch.complex128, device="cuda")
+    yd = torch.empty_like(xd)
+    torch.cuda.synchronize()
     out = {"fft_grid": op.PQR, "op_shape": op.shape("c64"), "prec_shape": prec.shape("c64"),
+           "op_shape_c128": op.shape("c128"),
+           "matvec_c128_ms": op.time_passes(xd.data_ptr(), yd.data_ptr(), 1, "c128", max(3, args.steps // 4)),
            "kernels": names_mv + names_pc,
            "matvec_c64_ms": op.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", args.steps),
            "prec_c64_ms": prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", args.steps)}
