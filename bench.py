@@ -552,6 +552,70 @@ def run_passes(args):
     return 0
 
 
+def run_koch(args):
+    """256x256x64 Koch snowflake (level 3, 16 central layers, m = 1.78+0.005i):
+    setup times, per-launch pipeline times, the matvec's model bandwidth, and a
+    bounded mixed GMRES(50) solve (this system converges slowly; relres after
+    the iteration budget is reported).  One JSON line."""
+    import torch
+    from voxscatter_gb300 import api, workloads as W
+    ctx = api.Context(0)
+    p = W.config5()
+    L, M, N = p["L"], p["M"], p["N"]
+    nD = L * M * N
+    idx = p["idx"]
+    idx3 = np.concatenate([idx, nD + idx, 2 * nD + idx])
+    dV = p["d"] ** 3
+    t = time.perf_counter()
+    Toep = api.green_dda(p["r"], p["ko"], ctx=ctx)
+    ctx.synchronize()
+    green_s = time.perf_counter() - t
+    alpha = api.alpha_ldr(p["refInd"], p["ko"], p["d"], p["kvec"], p["Eo"])
+    t = time.perf_counter()
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep, ctx=ctx)
+    ctx.synchronize()
+    op_s = time.perf_counter() - t
+    t = time.perf_counter()
+    prec = api.Preconditioner(op, shift=1 / alpha, d=dV, precisions=("c64",))
+    ctx.synchronize()
+    prec_s = time.perf_counter() - t
+    n3 = op.n3
+    xs = torch.randn(n3, dtype=torch.complex64, device="cuda")
+    ys = torch.empty_like(xs)
+    torch.cuda.synchronize()
+    mv = op.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", args.steps)
+    pc = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", args.steps)
+    mv_bytes, pc_bytes, pinned = _pass_bytes(p, op.PQR, n3)
+    b = api.plane_wave(op, p["r"], p["kvec"], p["Eo"])
+    bd = torch.from_numpy(np.ascontiguousarray(b)).cuda()
+    xd = torch.zeros_like(bd)
+    maxit = 200
+    api.solve_device(op, bd.data_ptr(), xd.data_ptr(), prec, tol=1e-6, maxit=50, precision="mixed",
+                     method="gmres", restart=50)
+    xd.zero_()
+    ctx.synchronize()
+    t = time.perf_counter()
+    info = api.solve_device(op, bd.data_ptr(), xd.data_ptr(), prec, tol=1e-6, maxit=maxit, precision="mixed",
+                            method="gmres", restart=50)
+    ctx.synchronize()
+    solve_ms = (time.perf_counter() - t) * 1e3
+    peak, peak_kind = _peaks()
+    mv_ms = sum(mv)
+    line = {"metric": "koch 256x256x64: pipeline launch times and bounded GMRES(50)", "unit": "ms",
+            "config": {"workload": f"Koch snowflake level 3, grid {L}x{M}x{N}, {len(idx)} dipoles, "
+                                   f"{n3} unknowns, m=1.78+0.005i", "fft_grid": "x".join(map(str, op.PQR))},
+            "setup_s": {"green": green_s, "operator": op_s, "preconditioner_c64": prec_s},
+            "shapes": {"op": op.shape("c64"), "prec": prec.shape("c64")},
+            "matvec_c64_ms": mv, "prec_c64_ms": pc,
+            "matvec_model_bytes": pinned, "matvec_model_GBps": pinned / (mv_ms * 1e-3) / 1e9,
+            "matvec_model_frac": pinned / (mv_ms * 1e-3) / 1e9 / peak, "peak_GBps": peak, "peak_source": peak_kind,
+            "gemv_GBps": pc_bytes[2] / (pc[2] * 1e-3) / 1e9,
+            "gmres50": {"maxit": maxit, "ms": solve_ms, "ms_per_iteration": solve_ms / max(1.0, info["iter"]),
+                        "flag": info["flag"], "relres": info["relres"], "iter": info["iter"]}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -564,12 +628,15 @@ def main():
     ap.add_argument("--shapes", default=None,
                     help='JSON {"op": {...}, "prec": {...}} c64 launch shapes applied after autotuning '
                          '(replays a tuned configuration, e.g. under a profiler)')
-    ap.add_argument("--mode", default="solve", choices=["solve", "passes"],
+    ap.add_argument("--mode", default="solve", choices=["solve", "passes", "koch"],
                     help="passes: only build the operator/preconditioner and time each pipeline launch "
-                         "(a short command for ncu captures)")
+                         "(a short command for ncu captures); koch: the 256x256x64 snowflake's pipeline "
+                         "times and a bounded GMRES(50) solve")
     args = ap.parse_args()
     if args.mode == "passes":
         return run_passes(args)
+    if args.mode == "koch":
+        return run_koch(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

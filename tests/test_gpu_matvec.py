@@ -220,7 +220,8 @@ def test_z_lengths_both_z_kernels(api, R):
 
 
 Y_LENGTHS = [8, 9, 10, 12, 15, 16, 18, 20, 24, 25, 27, 30, 32, 36, 40, 45, 48, 50, 54, 60, 64, 72, 75, 80, 81, 90,
-             91, 96, 100, 108, 120, 125, 128, 135, 144, 150, 160, 162, 180, 192, 200, 216, 225, 240, 243, 250, 256]
+             91, 96, 100, 108, 120, 125, 128, 135, 144, 150, 160, 162, 180, 192, 200, 216, 225, 240, 243, 250, 256,
+             288, 320, 384, 432, 480, 512]
 
 
 @pytest.mark.parametrize("n", Y_LENGTHS)

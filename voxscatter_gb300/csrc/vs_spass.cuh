@@ -2,8 +2,8 @@
 // axis (y) of many lines, x tiles contiguous -- the y passes of the matvec and
 // of the preconditioner apply.
 //
-// The line length is factored n = R1 * R2 (R1 the largest divisor <= sqrt(n),
-// R2 <= 32).  With row = n1 + R1*n2 and k = k2 + R2*k1,
+// The line length is factored n = R1 * R2 (R1 <= 16, R2 <= 32, R1 near
+// sqrt(n)).  With row = n1 + R1*n2 and k = k2 + R2*k1,
 //   X[k2 + R2 k1] = sum_n1 w_R1^(n1 k1) w_n^(n1 k2) sum_n2 x[n1 + R1 n2] w_R2^(n2 k2).
 // A CTA owns TX consecutive x columns of one plane:
 //   forward  A : item (n1, x): rows n1 + R1*n2 (< n_in) straight from global
@@ -124,14 +124,14 @@ static void launch_s2(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream
   VS_LAUNCH_CHECK();
 }
 
-// Every instantiated two-level length (5-smooth 8..256, 91 = 7*13 and
-// 105 = 7*15) with its split n = R1 * R2.
+// Every instantiated two-level length (5-smooth 8..256, 288, 320, 384, 432,
+// 480, 512, 91 = 7*13 and 105 = 7*15) with its split n = R1 * R2.
 #define VS_S2_LIST(X)                                                                                      \
   X(2, 4) X(3, 3) X(2, 5) X(3, 4) X(3, 5) X(4, 4) X(3, 6) X(4, 5) X(4, 6) X(5, 5) X(3, 9) X(5, 6) X(4, 8)   \
   X(6, 6) X(5, 8) X(5, 9) X(6, 8) X(5, 10) X(6, 9) X(6, 10) X(8, 8) X(8, 9) X(5, 15) X(8, 10) X(9, 9)      \
   X(9, 10) X(8, 12) X(10, 10) X(9, 12) X(10, 12) X(5, 25) X(8, 16) X(9, 15) X(12, 12) X(10, 15) X(10, 16)  \
   X(9, 18) X(12, 15) X(12, 16) X(10, 20) X(12, 18) X(15, 15) X(12, 20) X(9, 27) X(10, 25) X(16, 16) X(7, 13)   \
-  X(7, 15)
+  X(7, 15) X(12, 24) X(16, 20) X(16, 24) X(16, 27) X(16, 30) X(16, 32)
 
 template <typename T, bool INV>
 bool strided_two_level(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st) {

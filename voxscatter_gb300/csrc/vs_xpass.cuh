@@ -1,6 +1,6 @@
 // Two-level x passes: gather + zero-pad + FFT along x (XF), and IFFT along x
 // + crop + diagonal term + scatter (XI), for lines of length P = R1 * R2
-// (R1 the largest divisor <= sqrt(P), R2 <= 32).  Same arithmetic as k_xf /
+// (R1 <= 16, R2 <= 32, R1 near sqrt(P)).  Same arithmetic as k_xf /
 // k_xi in vs_matvec.cu (which handle the lengths not instantiated here).
 //
 // A CTA owns NL = 256 / R2 lines (line = (j, k, comp), x contiguous):
