@@ -616,6 +616,37 @@ def run_koch(args):
     return 0
 
 
+def run_nop(args):
+    """Galerkin N-operator Toeplitz assembly (far + medium cells of
+    assembly_nop_const.m) on a 128x128x64 grid: device time, against the FP64
+    NumPy restatement timed on a sample of offsets (scaled to the grid)."""
+    from voxscatter_gb300 import api
+    from oracle import nop
+    ctx = api.Context(0)
+    L, M, N, ko, dx = 128, 128, 64, 2 * np.pi, 0.05
+    api.nop_assemble(8, 8, 8, ko, dx, ctx=ctx)
+    ts = []
+    for _ in range(max(1, args.steps)):
+        t = time.perf_counter()
+        api.nop_assemble(L, M, N, ko, dx, ctx=ctx)
+        ts.append(time.perf_counter() - t)
+    Rf = nop.cube_faces(dx)
+    W, U, V = nop.gauss_2d(nop.NP_FAR)
+    rng = np.random.default_rng(0)
+    offs = rng.integers(5, [L, M, N], size=(200, 3))
+    t = time.perf_counter()
+    for o in offs:
+        nop.cubature_nop(W, U, V, o * dx, np.zeros(3), Rf, ko, dx)
+    cpu_per_offset = (time.perf_counter() - t) / len(offs)
+    line = {"metric": "N-operator Toeplitz assembly (far + medium face-pair cubature), 128x128x64", "unit": "s",
+            "value": float(np.median(ts)), "offsets": L * M * N,
+            "point_pairs": L * M * N * 21 * 256, "cpu_baseline": {
+                "value": cpu_per_offset * L * M * N, "unit": "s", "cores": 1, "kind": "port",
+                "sample": "200 far-cell offsets of the NumPy restatement (4x4 rule), scaled to 1,048,576 offsets"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -628,7 +659,7 @@ def main():
     ap.add_argument("--shapes", default=None,
                     help='JSON {"op": {...}, "prec": {...}} c64 launch shapes applied after autotuning '
                          '(replays a tuned configuration, e.g. under a profiler)')
-    ap.add_argument("--mode", default="solve", choices=["solve", "passes", "koch"],
+    ap.add_argument("--mode", default="solve", choices=["solve", "passes", "koch", "nop"],
                     help="passes: only build the operator/preconditioner and time each pipeline launch "
                          "(a short command for ncu captures); koch: the 256x256x64 snowflake's pipeline "
                          "times and a bounded GMRES(50) solve")
@@ -637,6 +668,8 @@ def main():
         return run_passes(args)
     if args.mode == "koch":
         return run_koch(args)
+    if args.mode == "nop":
+        return run_nop(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

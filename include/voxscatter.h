@@ -71,6 +71,21 @@ int vs_ctx_stream(vs_ctx* ctx, void** stream);
 int vs_green_dda(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* ox, const double* oy,
                  const double* oz, double ko, int near_quad, double* toep_out);
 
+/* Galerkin N-operator (JVIE) Toeplitz tensor, the far- and medium-cell part
+ * of src/src_vie/src_operators/assembly_nop_const.m:44-92,150-165: face-pair
+ * cubature of exp(-i ko R)/R (cubature_nop_const.cpp:8-124) over the 21
+ * distinct pairs of the voxel faces, 4x4 Gauss-Legendre points per face for
+ * all offsets, 10x10 for offsets < 5 per axis, projected onto the 6 tensor
+ * components and divided by 4 pi.  FP64 on the device.
+ *   near_J: NULL or the singular near block of assembly_nop_const.m:94-146
+ *   (the caller's DIRECTFN/DEMCEM result), nL*nM*nN*6*6 complex, column-major
+ *   (mx,my,mz,k,l), nL = min(2,L), nM = min(2,M), nN = min(2,N); with NULL
+ *   those cells are zero.
+ *   G_out: L*M*N*6 complex, column-major (L,M,N,6) -- the opToeplitz that
+ *   vs_op_create takes. */
+int vs_nop_assemble(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, double ko, double dx, const double* near_J,
+                    double* G_out);
+
 /* LDR polarisability per element, getOPERATOR_DDA.m:7-26 (host arithmetic).
  *   m: n complex values, refractive index (is_eps = 0) or permittivity m^2
  *   (is_eps = 1).  alpha_out: n complex (dimensionless, i.e. divided by d^3). */

@@ -1,5 +1,6 @@
 """The FP64 oracle against independent mathematics (CPU only)."""
 import math
+import os
 
 import numpy as np
 import pytest
@@ -236,3 +237,38 @@ def test_cext_gradient_central_differences():
             cm = O.cext_dda(solve(em, b), b, ko, dV, p["Eo"])
             fd = (cp - cm) / (2 * h)
             assert abs(fd - g[j]) <= 1e-5 * max(abs(g).max(), 1e-30)
+
+
+def test_nop_cubature_matches_reference_source():
+    """The face-pair cubature restatement against the reference's own
+    cubature_nop_const.cpp compiled here (skipped where it cannot be
+    compiled), 4x4, 10x10 and 20x20 rules."""
+    from oracle import nop
+    ref = nop.reference_cubature()
+    if ref is None:
+        pytest.skip("reference cubature source not available")
+    ko, dx = 2 * np.pi * 0.7, 0.08
+    Rf = nop.cube_faces(dx)
+    for n in (4, 10, 20):
+        W, U, V = nop.gauss_2d(n)
+        for m in ([3, 2, 1], [0, 1, 1], [9, 0, 4], [2, 2, 2]):
+            a = nop.cubature_nop(W, U, V, np.array(m) * dx, np.zeros(3), Rf, ko, dx)
+            b = ref(W, U, V, np.array(m) * dx, np.zeros(3), Rf, ko, dx)
+            assert np.abs(a - b).max() <= 1e-13 * np.abs(b).max(), (n, m)
+
+
+def test_nop_assembly_matches_golden():
+    """N-operator Toeplitz tensor (far + medium cells) against the fixtures
+    made with the reference's own cubature (tests/golden/make_nop_golden.py)."""
+    from oracle import nop
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "nop_assembly.npz"))
+    ko, dx = float(g["ko"]), float(g["dx"])
+    Rf = nop.cube_faces(dx)
+    for n in (4, 10, 20):
+        W, U, V = nop.gauss_2d(n)
+        for o, Jref in zip(g["J_offsets"], g[f"J_rule{n}"]):
+            J = nop.cubature_nop(W, U, V, o * dx, np.zeros(3), Rf, ko, dx)
+            assert np.abs(J - Jref).max() <= 1e-13 * np.abs(Jref).max(), (n, o)
+    for name, shape in (("G_7x6x5", (7, 6, 5)), ("G_1x1x6", (1, 1, 6))):
+        G = nop.assembly_nop(*shape, ko, dx)
+        assert np.linalg.norm(G - g[name]) <= 1e-12 * np.linalg.norm(g[name]), name

@@ -35,6 +35,7 @@ SIGNATURES = {
     "vs_green_dda": (C.c_int, [_vp, _i64, _i64, _i64, _pd, _pd, _pd, C.c_double, C.c_int, _pd]),
     "vs_alpha_ldr": (C.c_int, [_pd, _i64, C.c_int, C.c_double, C.c_double, _pd, _pd, _pd]),
     "vs_circulant_fft": (C.c_int, [_vp, _i64, _i64, _i64, _pd, _i64, _i64, _i64, _pd]),
+    "vs_nop_assemble": (C.c_int, [_vp, _i64, _i64, _i64, C.c_double, C.c_double, _pd, _pd]),
     "vs_op_create": (C.c_int, [_vp, _i64, _i64, _i64, _pd, _i64, _i64, _i64, _pi64, _i64, vs_diag, vs_diag,
                                vs_diag, C.POINTER(_vp)]),
     "vs_op_create_fN": (C.c_int, [_vp, _i64, _i64, _i64, _pd, _i64, _i64, _i64, _pi64, _i64, vs_diag, vs_diag,

@@ -91,6 +91,21 @@ def alpha_ldr(m, ko, d, kvec, Eo, is_eps=False):
     return out[0] if np.ndim(m) == 0 else out.reshape(np.shape(m))
 
 
+def nop_assemble(L_, M_, N_, ko, dx, near_J=None, ctx=None):
+    """Galerkin N-operator Toeplitz tensor G (L, M, N, 6) of assembly_nop_const.m
+    (far and medium cells on the device); near_J: the singular near block
+    (min(2,L), min(2,M), min(2,N), 6, 6) or None (those cells zero)."""
+    ctx = ctx or default_context()
+    G = np.zeros(L_ * M_ * N_ * 6, dtype=np.complex128)
+    nj = None
+    if near_J is not None:
+        shape = (min(2, L_), min(2, M_), min(2, N_), 6, 6)
+        nj = np.ascontiguousarray(np.asarray(near_J, dtype=np.complex128).reshape(shape).ravel(order="F"))
+    L.check(ctx._lib.vs_nop_assemble(ctx.h, L_, M_, N_, float(ko), float(dx), L.dptr(nj) if nj is not None else None,
+                                     L.dptr(G)), ctx.h)
+    return G.reshape((L_, M_, N_, 6), order="F")
+
+
 def circulant_fft(Toep, P=None, Q=None, R=None, ctx=None):
     """fN = fft_operator(circulant_nop_const(Toep)) for (P,Q,R) = (2L,2M,2N) by default."""
     ctx = ctx or default_context()

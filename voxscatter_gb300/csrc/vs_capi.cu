@@ -404,6 +404,29 @@ int vs_green_dda(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* ox,
   });
 }
 
+int vs_nop_assemble(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, double ko, double dx, const double* near_J,
+                    double* G_out) {
+  if (!ctx) return VS_ERR_ARG;
+  return guarded(ctx, [&] {
+    check_grid(L, M, N);
+    VS_REQUIRE(G_out, "G_out is NULL");
+    VS_REQUIRE(dx > 0 && std::isfinite(dx) && std::isfinite(ko), "dx must be positive and ko finite");
+    cudaStream_t st = ctx->stream;
+    const int64_t V = L * M * N;
+    const int64_t nb = std::min<int64_t>(2, L) * std::min<int64_t>(2, M) * std::min<int64_t>(2, N);
+    vs::DevBuf g, nj;
+    g.alloc(6 * V * sizeof(double2));
+    if (near_J) {
+      nj.alloc(36 * nb * sizeof(double2));
+      VS_CUDA(cudaMemcpyAsync(nj.p, near_J, 36 * nb * sizeof(double2), cudaMemcpyHostToDevice, st));
+    }
+    vs::nop_assemble_device((int)L, (int)M, (int)N, ko, dx, near_J ? nj.as<double2>() : nullptr,
+                            g.as<double2>(), st);
+    VS_CUDA(cudaMemcpyAsync(G_out, g.p, 6 * V * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
 int vs_circulant_fft(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* toep, int64_t P, int64_t Q,
                      int64_t R, double* fN_out) {
   if (!ctx) return VS_ERR_ARG;

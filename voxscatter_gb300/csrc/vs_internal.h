@@ -182,6 +182,11 @@ void finalize_spectrum(const double2* fN, int64_t total, double scale, double2* 
 // Preconditioner (vs_precond.cu)
 void circ_levels_device(int L, int M, int N, const double2* toep, double2* lev1, double2* lev2, const FftAxis& axL,
                         const FftAxis& axM, cudaStream_t st);
+// Galerkin N-operator Toeplitz tensor G (L, M, N, 6) on the device (vs_nop.cu);
+// near: NULL or the (min(2,L), min(2,M), min(2,N), 6, 6) singular block.
+void nop_assemble_device(int L, int M, int N, double ko, double dx, const double2* near, double2* G,
+                         cudaStream_t st);
+
 // Smallest instantiated two-level z length >= min_len (5-smooth beyond 256).
 int z_pass_length(int min_len);
 template <typename T>
