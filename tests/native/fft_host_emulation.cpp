@@ -78,7 +78,8 @@ static double check(int n, int nlines, bool lines_fast, int lg_nl = 0) {
 
 int main() {
   const int sizes[] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 11, 12, 13, 16, 17, 18, 23, 26, 27, 32, 36, 49, 52, 54, 56, 64, 72, 81,
-                       91, 105, 121, 126, 128, 169, 182, 189, 192, 210, 127, 254, 256, 384, 512, 625, 1024};
+                       53, 61, 68, 79, 91, 101, 105, 113, 121, 126, 128, 169, 182, 189, 192, 210, 127, 254, 256, 384,
+                       512, 625, 1024};
   int bad = 0;
   for (int n : sizes) {
     for (int lf = 0; lf < 2; ++lf) {

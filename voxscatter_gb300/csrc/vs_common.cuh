@@ -7,6 +7,9 @@
 #include <cstdio>
 #include <string>
 #include <stdexcept>
+#include <mutex>
+#include <set>
+#include <utility>
 #include "../../include/voxscatter.h"
 
 namespace vs {
@@ -79,23 +82,31 @@ struct Error : std::runtime_error {
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
-// Raise a kernel's dynamic shared-memory limit once (not per launch, so that
-// launches captured into CUDA graphs issue no attribute calls).
+// Raise a kernel's dynamic shared-memory limit once per process and device
+// (not per launch, so that launches captured into CUDA graphs issue no
+// attribute calls).  The limit is a property of the function shared by every
+// host thread, so it is raised straight to the hardware maximum and never
+// lowered: launches from concurrent threads with different tile sizes all fit.
 inline void set_kernel_smem(const void* kernel, size_t bytes) {
-  if (bytes > 227 * 1024)
+  constexpr size_t kMax = 227 * 1024;
+  if (bytes > kMax)
     throw Error(VS_ERR_UNSUPPORTED, "kernel tile needs " + std::to_string(bytes) + " bytes of shared memory (> 227 KB)");
   if (bytes <= 48 * 1024) return;
-  struct Entry { const void* k; int dev; size_t bytes; };
-  static thread_local Entry cache[64];
-  static thread_local int ncache = 0;
   int dev = 0;
   VS_CUDA(cudaGetDevice(&dev));
-  for (int i = 0; i < ncache; ++i)
-    if (cache[i].k == kernel && cache[i].dev == dev && cache[i].bytes >= bytes) return;
-  VS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  for (int i = 0; i < ncache; ++i)
-    if (cache[i].k == kernel && cache[i].dev == dev) { cache[i].bytes = bytes; return; }
-  if (ncache < 64) cache[ncache++] = Entry{kernel, dev, bytes};
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count({kernel, dev})) return;
+  // the per-CTA limit covers static and dynamic shared memory together
+  cudaFuncAttributes fa;
+  VS_CUDA(cudaFuncGetAttributes(&fa, kernel));
+  const size_t cap = kMax - fa.sharedSizeBytes;
+  if (bytes > cap)
+    throw Error(VS_ERR_UNSUPPORTED, "kernel tile needs " + std::to_string(bytes) + " bytes of shared memory (> " +
+                                        std::to_string(cap) + " available)");
+  VS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+  done.insert({kernel, dev});
 }
 
 }  // namespace vs

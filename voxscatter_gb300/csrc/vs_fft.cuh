@@ -442,6 +442,13 @@ __device__ __forceinline__ void fft_stage(int src, int dst, int n, int Ns, int n
   }
 }
 
+// Stage of any radix R (primes without a closed-form butterfly, up to
+// FFT_MAX_GENERIC_RADIX).  The work items are the (butterfly j, output q)
+// pairs of a line, spread over all butterfly slots, so a long prime (one
+// butterfly per line) is computed by every thread of the line rather than by
+// one.  Output q of butterfly j (k = j mod Ns) is
+//   sum_r x[j + r*m] * w_n^(r*k*step) * w_R^(r*q) = sum_r x[j + r*m] * w_n^(r*(k*step + q*n/R)),
+// one table root per term with the index advanced modulo n.
 template <bool INV, typename C>
 __device__ __noinline__ void fft_stage_generic(int src, int dst, int n, int R, int Ns, int nlines, int ls, int es,
                                                FftLayout lay, int tw, int t) {
@@ -454,30 +461,25 @@ __device__ __noinline__ void fft_stage_generic(int src, int dst, int n, int R, i
   const int lslot = lay.lines_fast ? (t & (NL - 1)) : (t >> lg_nj);
   const int jt = lay.lines_fast ? (t >> lg_nl) : (t & (NJ - 1));
   const int m = n / R;
-  if (jt >= m) return;
+  const int items = m * R;
+  if (jt >= items) return;
   const int step = n / (Ns * R);
   const int st = n / R;
-  C v[FFT_MAX_GENERIC_RADIX];
   for (int line = lslot; line < nlines; line += NL) {
     const int s = src + line * ls;
     const int d = dst + line * ls;
-    for (int j = jt; j < m; j += NJ) {
+    for (int it = jt; it < items; it += NJ) {
+      const int j = it / R, q = it - j * R;
       const int k = j % Ns;
-      for (int r = 0; r < R; ++r) {
-        const C a = sm[s + (j + r * m) * es];
-        v[r] = (r > 0 && Ns > 1) ? cmul(a, twid<INV>(twp, r * k * step)) : a;
+      const int inc = k * step + q * st;  // < n
+      C acc = sm[s + j * es];
+      int idx = 0;
+      for (int r = 1; r < R; ++r) {
+        idx += inc;
+        if (idx >= n) idx -= n;
+        acc = cfma(sm[s + (j + r * m) * es], twid<INV>(twp, idx), acc);
       }
-      const int base = (j - k) * R + k;
-      for (int q = 0; q < R; ++q) {
-        C acc = v[0];
-        int idx = 0;
-        for (int r = 1; r < R; ++r) {
-          idx += q;
-          if (idx >= R) idx -= R;
-          acc = cfma(v[r], twid<INV>(twp, idx * st), acc);
-        }
-        sm[d + (base + q * Ns) * es] = acc;
-      }
+      sm[d + ((j - k) * R + k + q * Ns) * es] = acc;
     }
   }
 }

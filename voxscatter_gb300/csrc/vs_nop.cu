@@ -204,8 +204,12 @@ NopConst make_nop_const(double dx) {
 
 }  // namespace
 
+// The rule, face and projection tables live in one __constant__ block, so
+// calls from concurrent host threads are serialised until their kernel is done.
 void nop_assemble_device(int L, int M, int N, double ko, double dx, const double2* near, double2* G,
                          cudaStream_t st) {
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
   const NopConst h = make_nop_const(dx);
   VS_CUDA(cudaMemcpyToSymbolAsync(c_nop, &h, sizeof(NopConst), 0, cudaMemcpyHostToDevice, st));
   const int64_t V = (int64_t)L * M * N;
@@ -215,6 +219,7 @@ void nop_assemble_device(int L, int M, int N, double ko, double dx, const double
   k_nop<<<(unsigned)blocks, threads, 0, st>>>(L, M, N, ko, dx, std::min(2, L), std::min(2, M), std::min(2, N),
                                              near, G);
   VS_LAUNCH_CHECK();
+  VS_CUDA(cudaStreamSynchronize(st));
 }
 
 }  // namespace vs
