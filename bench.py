@@ -165,7 +165,7 @@ def _pass_names(op, prec):
     a, b, c, d = xy(so, "")
     names_mv = [a, b, "k_z2" if so["z_reg"] in (1, 2) else "k_z", c, d]
     a, b, c, d = xy(sp, "prec_")
-    names_pc = [a, b, "k_block_gemv_stream" if sp["gemv_mode"] in (1, 2) else "k_block_gemv_sym", c, d]
+    names_pc = [a, b, "k_block_gemv_stream" if sp["gemv_mode"] == 1 else "k_block_gemv_sym", c, d]
     return names_mv, names_pc
 
 
@@ -530,12 +530,12 @@ def run_passes(args):
                 prec.set_shape("c64", gemv_mode=0, gemv_blocks=b, gemv_threads=th, gemv_chunk=0)
                 gs[f"direct,blocks={b},threads={th}"] = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64",
                                                                          args.steps)[2]
-        for mode in (1, 2):
-            for b in (1, 2):
-                for cq in (0, 8, 16, 32):
-                    prec.set_shape("c64", gemv_mode=mode, gemv_blocks=b, gemv_threads=0, gemv_chunk=cq)
-                    gs[f"stream{mode},ctas={b},chunk={cq}"] = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1,
-                                                                               "c64", args.steps)[2]
+        n = 3 * N
+        for b in (1, 2, 3, 4):
+            for cq in (0, 8, 16, 32, (n + 1) // 2):
+                prec.set_shape("c64", gemv_mode=1, gemv_blocks=b, gemv_threads=0, gemv_chunk=cq)
+                gs[f"stream,ctas={b},chunk={cq}"] = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64",
+                                                                     args.steps)[2]
         prec.set_shape("c64", **tuned_pr)
         ys_ = {}
         for yr in (0, 1):

@@ -306,10 +306,8 @@ int vs_op_set_shape(vs_op* op, int precision, const vs_shape* shape);
 /* Launch shape of a preconditioner apply: x/y tiles of its FFT passes and
  * the block GEMV.  gemv_mode 0 is the register-direct GEMV (gemv_blocks
  * stored blocks per CTA, gemv_threads per CTA); gemv_mode 1 streams each block
- * through shared memory with bulk asynchronous copies (gemv_blocks CTAs per SM,
- * gemv_chunk block columns per copy); gemv_mode 2 is the same stream with the
- * vectors gathered by element-wise asynchronous copies several blocks ahead.
- * 0 / -1 select the defaults. */
+ * through shared memory with bulk asynchronous copies (gemv_blocks CTAs per SM, 1-4,
+ * gemv_chunk block columns per copy).  0 / -1 select the defaults. */
 typedef struct vs_prec_shape {
   int lg_lines_x;
   int lg_tile_y;

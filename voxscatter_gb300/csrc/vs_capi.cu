@@ -895,9 +895,9 @@ int vs_prec_set_shape(vs_prec* prec, int precision, const vs_prec_shape* shape) 
     vs::PassShape& s = prec->shape[precision == VS_C64 ? 0 : 1];
     s.lg_lpb_x = shape->lg_lines_x;
     s.lg_tx_y = shape->lg_tile_y;
-    VS_REQUIRE(shape->gemv_mode >= -1 && shape->gemv_mode <= 2, "gemv_mode must be -1, 0, 1 or 2");
+    VS_REQUIRE(shape->gemv_mode >= -1 && shape->gemv_mode <= 1, "gemv_mode must be -1, 0 or 1");
     VS_REQUIRE(shape->gemv_chunk >= 0 && shape->gemv_chunk <= 3 * prec->N, "gemv_chunk out of range");
-    VS_REQUIRE(shape->gemv_mode < 1 || shape->gemv_blocks <= 2, "streamed GEMV takes 1 or 2 CTAs per SM");
+    VS_REQUIRE(shape->gemv_mode < 1 || shape->gemv_blocks <= 4, "streamed GEMV takes 1 to 4 CTAs per SM");
     s.gemv_ti = shape->gemv_blocks;
     s.gemv_threads = shape->gemv_threads;
     VS_REQUIRE(shape->y_reg >= -1 && shape->y_reg <= 1, "y_reg must be -1, 0 or 1");

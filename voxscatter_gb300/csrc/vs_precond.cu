@@ -708,35 +708,6 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-// Element-wise asynchronous copy of BYTES (8 or 16) from global to shared
-// memory, zero-filled when !ok (src must still be a valid address).
-template <int BYTES>
-__device__ __forceinline__ void cp_async_zfill(uint32_t dst, const void* src, bool ok) {
-  const uint32_t sz = ok ? BYTES : 0;
-  if constexpr (BYTES == 16)
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(sz) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(sz) : "memory");
-}
-
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-
-// Wait until at most n (0..3) of this thread's latest cp.async groups are pending.
-__device__ __forceinline__ void cp_async_wait_pending(int n) {
-  switch (n) {
-    case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
-    case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
-    case 2: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
-    default: asm volatile("cp.async.wait_group 3;" ::: "memory"); break;
-  }
-}
-
-// x/y component flip of mirror var (bit 0: mirrored in x, bit 1: in y) at row q.
-__device__ __forceinline__ bool mirror_flip(int q, int N, int var) {
-  const int comp = (q >= N) + (q >= 2 * N);
-  return (comp == 0 && (var & 1)) != (comp == 1 && (var >> 1));
-}
-
 // Persistent apply over the stored blocks b = blockIdx.x + k*gridDim.x for the
 // right-hand sides blockIdx.y*RG .. +RG, with three warp roles:
 //  * producer warp (lane 0): streams the blocks (column-major 3N x 3N, in
@@ -745,34 +716,30 @@ __device__ __forceinline__ bool mirror_flip(int q, int N, int var) {
 //    arrived on its "empty" barrier;
 //  * nv vector warps: gather the W = 4*RG vectors of a block (its four
 //    mirrored frequencies per right-hand side, x/y component flips applied)
-//    into a ring of nvb buffers [q][W] ahead of the consumers, and after the
-//    consumers are done with a block add its G partial sums and write the
-//    results (flips applied again) over the grid entries the inputs came
-//    from.  With AG the gathers are element-wise asynchronous copies issued
-//    nvb blocks ahead and completed (flips applied) two blocks ahead, so the
-//    gather latency is off the vector warps' path; without AG a block's
-//    gather is loaded and stored in one go, two blocks ahead;
+//    into one of two buffers [q][W] two blocks ahead of the consumers, and
+//    after the consumers are done with a block add its G partial sums and
+//    write the results (flips applied again) over the grid entries the
+//    inputs came from;
 //  * consumer warps: thread (g, rp) forms rows RW*rp .. +RW-1 (RW = 2 with
 //    PAIR: one 16-byte load per column) over the chunk columns q = g (mod G)
 //    and leaves its partial sums as [g][W][row].
 // Block boundaries therefore never stop the stream.  Hand-offs use mbarriers:
-// vfull[v] (vector warps -> consumers: buffer v holds the block's vectors),
+// vfull[b] (vector warps -> consumers: buffer b holds the block's vectors),
 // done[b] (consumers -> vector warps: partial sums of buffer b written, the
 // block's vectors no longer needed) and rfree[b] (vector warps -> consumers:
 // partial sums of buffer b consumed).  Ring positions and phases advance by
 // counters (no divisions on the loops).  Every wait is bounded; a wait that
 // runs out sets status bit 4 and the abort flag, every role leaves its loop,
-// the producer waits (bounded) for its last copies and the vector warps for
-// their gathers before the CTA ends.
+// and the producer waits (bounded) for its last copies before the CTA ends.
 // A chunk is fetched from the 16-byte boundary at or below its start, so with
 // c64 elements and odd 3N the data may begin one element into the stage (the
 // block buffers carry 64 bytes of tail padding for the rounded-up last copy);
 // PAIR is used only when 3N is even, where every chunk starts aligned.
-template <typename T, int RG, bool PAIR, bool AG>
+template <typename T, int RG, bool PAIR>
 __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ inv,
                                                            int L, int M, int N, int64_t rhs_stride, int nrhs,
                                                            const int* skip, int skip_stride, int cq, int nstage,
-                                                           int stage_elems, int G, int nc, int nv, int nvb,
+                                                           int stage_elems, int G, int nc, int nv,
                                                            int* __restrict__ status) {
   using C = cplx_t<T>;
   constexpr int W = 4 * RG, RW = PAIR ? 2 : 1;
@@ -786,14 +753,14 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);  // [8]
   uint64_t* empty = full + 8;                               // [8]
-  uint64_t* vfull = empty + 8;                              // [4]
-  uint64_t* done = vfull + 4;                               // [2]
+  uint64_t* vfull = empty + 8;                              // [2]
+  uint64_t* done = vfull + 2;                               // [2]
   uint64_t* rfree = done + 2;                               // [2]
   volatile int* ctl = reinterpret_cast<volatile int*>(rfree + 2);  // [0] abort
   C* stg = reinterpret_cast<C*>(smem_raw + 256);
   const int n = 3 * N, Lb = L / 2 + 1, Mb = M / 2 + 1;
-  C* vt0 = stg + (size_t)nstage * stage_elems;  // nvb x [n][W]
-  C* red0 = vt0 + (size_t)nvb * n * W;          // 2 x [G][n][W]
+  C* vt0 = stg + (size_t)nstage * stage_elems;  // 2 x [n][W]
+  C* red0 = vt0 + (size_t)2 * n * W;            // 2 x [G][n][W]
   const int64_t nblk = (int64_t)Lb * Mb, LM = (int64_t)L * M;
   const int tid = threadIdx.x, lane = tid & 31;
   const int64_t nmine = blockIdx.x < nblk ? (nblk - 1 - blockIdx.x) / gridDim.x + 1 : 0;
@@ -806,8 +773,8 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
       mbar_init(smem_addr(full + s), 1);
       mbar_init(smem_addr(empty + s), ncw);
     }
-    for (int v = 0; v < nvb; ++v) mbar_init(smem_addr(vfull + v), nv);
     for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_addr(vfull + b), nv);
       mbar_init(smem_addr(done + b), ncw);
       mbar_init(smem_addr(rfree + b), nv);
     }
@@ -821,91 +788,48 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
   };
 
   if (tid >= nc + 32) {  // vector warps: vthread vl of nv*32 handles elements vl, vl + nv*32, ...
+    // vstride is a multiple of W (a power of two), so a thread keeps one
+    // column col = (mirror var, right-hand side rg) and walks the rows q
     const int vl = tid - nc - 32, vstride = nv * 32;
-    // grid offsets of the four mirrors of block kb (-1: coincides with the block)
-    struct Bases {
-      int64_t b[4];
-      __device__ int64_t at(int var) const { return var == 0 ? b[0] : var == 1 ? b[1] : var == 2 ? b[2] : b[3]; }
+    const int col = vl & (W - 1), var = col & 3, rg = col >> 2;
+    const int q0 = vl / W, qstep = vstride / W;
+    const bool fx = var & 1, fy = var >> 1;
+    auto flip_at = [&](int q) { return q < N ? fx : (q < 2 * N ? fy : false); };
+    // grid offset of this thread's mirror of block kb (-1: coincides with the block)
+    auto base_of = [&](int64_t kb) -> int64_t {
+      const int blk = (int)blockIdx.x + (int)kb * (int)gridDim.x;  // < Lb * Mb
+      const int js = blk / Lb, is = blk - js * Lb;
+      int i, j;
+      return mirror_of(is, js, var, L, M, i, j) ? i + (int64_t)L * j : -1;
     };
-    auto bases = [&](int64_t kb) {
-      Bases r;
-      const int64_t blk = blockIdx.x + kb * gridDim.x;
-      const int js = (int)(blk / Lb), is = (int)(blk - (int64_t)js * Lb);
-#pragma unroll
-      for (int var = 0; var < 4; ++var) {
-        int i, j;
-        r.b[var] = mirror_of(is, js, var, L, M, i, j) ? i + (int64_t)L * j : -1;
-      }
-      return r;
-    };
-    auto src_of = [&](const Bases& bs, int u, bool& ok) -> const C* {
-      const int q = u / W, col = u - q * W;
-      const int var = col & 3, rg = col >> 2;
-      const int64_t base = bs.at(var);
-      ok = rg < nr && base >= 0;
-      return ok ? t + (int64_t)(rhs0 + rg) * rhs_stride + base + LM * q : t;
-    };
-    // AG: issue the copies of block kb (one cp.async group)
-    auto issue = [&](int64_t kb) {
-      const Bases bs = bases(kb);
-      C* vt = vt0 + (size_t)(kb % nvb) * nW;
-      for (int u = vl; u < nW; u += vstride) {
-        bool ok;
-        const C* src = src_of(bs, u, ok);
-        cp_async_zfill<(int)sizeof(C)>(smem_addr(vt + u), src, ok);
-      }
-      cp_async_commit();
-    };
-    // AG: apply the flips to this thread's landed elements of block kb and publish it
-    auto finish = [&](int64_t kb, int pending) {
-      cp_async_wait_pending(pending);
-      C* vt = vt0 + (size_t)(kb % nvb) * nW;
-      for (int u = vl; u < nW; u += vstride) {
-        const int q = u / W, col = u - q * W;
-        if (mirror_flip(q, N, col & 3)) {
-          C x = vt[u];
-          x.x = -x.x;
-          x.y = -x.y;
-          vt[u] = x;
-        }
-      }
-      __syncwarp();
-      if (lane == 0) mbar_arrive(smem_addr(vfull + kb % nvb));
-    };
-    // without AG: load and store block kb in one go
+    C* const trg = t + (int64_t)(rhs0 + rg) * rhs_stride;
+    // load and store block kb in one go
     auto gather = [&](int64_t kb) {
-      const Bases bs = bases(kb);
-      C* vt = vt0 + (size_t)(kb & 1) * nW;
+      const int64_t base = base_of(kb);
+      const bool on = rg < nr && base >= 0;
+      const C* src = trg + (on ? base : 0);
+      C* vt = vt0 + (size_t)(kb & 1) * nW + col;
       constexpr int B = 8;  // independent loads in flight per lane
-      for (int u0 = vl; u0 < nW; u0 += vstride * B) {
+      for (int q = q0; q < n; q += qstep * B) {
         C v[B];
 #pragma unroll
         for (int k = 0; k < B; ++k) {
-          const int u = u0 + vstride * k;
-          bool ok = false;
-          const C* src = u < nW ? src_of(bs, u, ok) : t;
-          v[k] = ok ? *src : czero<C>();
+          const int qq = q + k * qstep;
+          v[k] = (on && qq < n) ? src[LM * qq] : czero<C>();
         }
 #pragma unroll
         for (int k = 0; k < B; ++k) {
-          const int u = u0 + vstride * k;
-          if (u >= nW) break;
-          const int q = u / W, col = u - q * W;
+          const int qq = q + k * qstep;
+          if (qq >= n) break;
           C x = v[k];
-          if (mirror_flip(q, N, col & 3)) { x.x = -x.x; x.y = -x.y; }
-          vt[u] = x;
+          if (flip_at(qq)) { x.x = -x.x; x.y = -x.y; }
+          vt[(size_t)qq * W] = x;
         }
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(smem_addr(vfull + (kb & 1)));
     };
-    int64_t issued = 0;
-    if constexpr (AG) {
-      for (; issued < nmine && issued < nvb; ++issued) issue(issued);
-      for (int64_t k = 0; k < nmine && k < 2; ++k) finish(k, (int)(issued - 1 - k));
-    } else {
-      for (int64_t kb = 0; kb < nmine && kb < 2; ++kb) gather(kb);
-    }
+    for (int64_t kb = 0; kb < nmine && kb < 2; ++kb) gather(kb);
     for (int64_t kb = 0; kb < nmine; ++kb) {
       const int b = (int)(kb & 1);
       bool ok = true;
@@ -915,28 +839,21 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
         if (lane == 0) fail();
         break;
       }
-      const Bases bs = bases(kb);
-      const C* red = red0 + (size_t)b * G * nW;
-      for (int u = vl; u < nW; u += vstride) {
-        const int q = u / W, col = u - q * W;
-        const int var = col & 3, rg = col >> 2;
-        const int64_t base = bs.at(var);
-        if (rg >= nr || base < 0) continue;
-        C sum = red[(size_t)col * n + q];
-        for (int gg = 1; gg < G; ++gg) sum = cadd(sum, red[((size_t)gg * W + col) * n + q]);
-        if (mirror_flip(q, N, var)) { sum.x = -sum.x; sum.y = -sum.y; }
-        t[(int64_t)(rhs0 + rg) * rhs_stride + base + LM * q] = sum;
+      const int64_t base = base_of(kb);
+      if (rg < nr && base >= 0) {
+        const C* red = red0 + (size_t)b * G * nW + (size_t)col * n;
+        C* dst = trg + base;
+        for (int q = q0; q < n; q += qstep) {
+          C sum = red[q];
+          for (int gg = 1; gg < G; ++gg) sum = cadd(sum, red[(size_t)gg * nW + q]);
+          if (flip_at(q)) { sum.x = -sum.x; sum.y = -sum.y; }
+          dst[LM * q] = sum;
+        }
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(smem_addr(rfree + b));
-      if constexpr (AG) {
-        if (kb + nvb < nmine) issue(issued++);
-        if (kb + 2 < nmine) finish(kb + 2, (int)(issued - 1 - (kb + 2)));
-      } else {
-        if (kb + 2 < nmine) gather(kb + 2);
-      }
+      if (kb + 2 < nmine) gather(kb + 2);
     }
-    if constexpr (AG) cp_async_wait_pending(0);  // no gather may land after the CTA ends (abort path)
     return;
   }
 
@@ -980,17 +897,12 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
   const int nrow = n / RW;
   const int nact = G * nrow;
   const int g = tid / nrow, rp = tid - g * nrow;
-  int s = 0, vi = 0;
-  uint32_t sph = 0, vph = 0;
+  int s = 0;
+  uint32_t sph = 0;
   for (int64_t kb = 0; kb < nmine; ++kb) {
     const int b = (int)(kb & 1);
-    const int vb = AG ? vi : b;
-    bool ok = !ctl[0] && mbar_wait(smem_addr(vfull + vb), AG ? vph : (uint32_t)((kb >> 1) & 1));
-    if (++vi == nvb) {
-      vi = 0;
-      vph ^= 1;
-    }
-    const C* vt = vt0 + (size_t)vb * nW;
+    bool ok = !ctl[0] && mbar_wait(smem_addr(vfull + b), (uint32_t)((kb >> 1) & 1));
+    const C* vt = vt0 + (size_t)b * nW;
     C acc[RW][W];
 #pragma unroll
     for (int h = 0; h < RW; ++h)
@@ -1007,7 +919,7 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
         const C* A = stg + (size_t)s * stage_elems + shift + RW * rp + (size_t)g * n;
         const C* xq = vt + (size_t)(c0 + g) * W;
 #pragma unroll 2
-        for (int ql = g; ql < ncols; ql += G, A += (size_t)G * n, xq += G * W) {
+        for (int ql = g; ql < ncols; ql += G, A += (size_t)G * n, xq += G * W) {  // column loop
           C m[RW];
           if constexpr (PAIR) {
             const float4 mm = *reinterpret_cast<const float4*>(A);
@@ -1016,11 +928,25 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
           } else {
             m[0] = *A;
           }
+          if constexpr (sizeof(C) == 8) {
+            // two vector entries per 16-byte load (W is a multiple of 4)
 #pragma unroll
-          for (int c = 0; c < W; ++c) {
-            const C xc = xq[c];
+            for (int c = 0; c < W; c += 2) {
+              const float4 xx = *reinterpret_cast<const float4*>(xq + c);
+              const C x0 = make_c<C>(xx.x, xx.y), x1 = make_c<C>(xx.z, xx.w);
 #pragma unroll
-            for (int h = 0; h < RW; ++h) acc[h][c] = cfma(m[h], xc, acc[h][c]);
+              for (int h = 0; h < RW; ++h) {
+                acc[h][c] = cfma(m[h], x0, acc[h][c]);
+                acc[h][c + 1] = cfma(m[h], x1, acc[h][c + 1]);
+              }
+            }
+          } else {
+#pragma unroll
+            for (int c = 0; c < W; ++c) {
+              const C xc = xq[c];
+#pragma unroll
+              for (int h = 0; h < RW; ++h) acc[h][c] = cfma(m[h], xc, acc[h][c]);
+            }
           }
         }
       }
@@ -1056,36 +982,41 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
 // Stream-kernel launch geometry: chunk columns, stages, stage size, column
 // groups, consumer threads, shared memory and CTAs per SM.
 struct GemvStream {
-  int cq, nstage, stage_elems, G, nc, nv, nvb, ctas;
+  int cq, nstage, stage_elems, G, nc, nv, ctas;
   size_t smem;
 };
 
-// cq = 0 when no stage of even one column fits beside the vectors.
+// Geometry for up to `ctas` CTAs per SM: the CTAs share the SM's 228 KB of
+// shared memory (1 KB of each is reserved); when even two stages of one
+// column do not fit beside the vectors, fewer CTAs per SM are tried, and
+// cq = 0 when not even one CTA fits.
 template <typename T>
-static GemvStream gemv_stream_geometry(int n, int rg, int chunk_cols, bool pair, bool ag) {
+static GemvStream gemv_stream_geometry(int n, int rg, int chunk_cols, bool pair, int ctas) {
   const size_t cs = sizeof(cplx_t<T>);
   GemvStream g{};
   const int nrow = pair ? n / 2 : n;
   g.G = std::max(1, std::min(4, 256 / nrow));
   g.nc = (g.G * nrow + 31) / 32 * 32;
   g.nv = std::max(1, std::min(4, (384 - g.nc - 32) / 32));
-  // asynchronous gathers run up to nvb blocks ahead of the consumers
   const size_t vbytes = (size_t)n * 4 * rg * cs;
-  g.nvb = !ag ? 2 : vbytes <= 8192 ? 4 : vbytes <= 16384 ? 3 : 2;
-  const size_t fixed = 256 + (size_t)g.nvb * vbytes + (size_t)2 * g.G * vbytes;
-  const size_t budget = 112 * 1024;  // two CTAs per SM
+  const size_t fixed = 256 + (size_t)2 * vbytes + (size_t)2 * g.G * vbytes;
   const size_t stage_target = 16 * 1024;
-  int cq = chunk_cols > 0 ? std::min(chunk_cols, n) : std::max(1, (int)(stage_target / ((size_t)n * cs)));
-  cq = std::min(cq, n);
   auto stage_bytes = [&](int c) { return (((size_t)n * c + 2) * cs + 15) / 16 * 16; };
-  while (cq > 1 && fixed + 2 * stage_bytes(cq) > 220 * 1024) --cq;
-  if (fixed + 2 * stage_bytes(cq) > 220 * 1024) { g.cq = 0; return g; }
-  g.cq = cq;
-  g.stage_elems = (int)(stage_bytes(cq) / cs);
-  g.nstage = 8;
-  while (g.nstage > 2 && fixed + (size_t)g.nstage * stage_bytes(cq) > budget) --g.nstage;
-  g.smem = fixed + (size_t)g.nstage * stage_bytes(cq);
-  g.ctas = g.smem <= budget ? 2 : 1;
+  for (int c = std::max(1, std::min(ctas, 4)); c >= 1; --c) {
+    const size_t budget = c == 1 ? 220 * 1024 : (228 * 1024) / c - 1024;
+    int cq = chunk_cols > 0 ? std::min(chunk_cols, n) : std::max(1, (int)(stage_target / ((size_t)n * cs)));
+    cq = std::min(cq, n);
+    while (cq > 1 && fixed + 2 * stage_bytes(cq) > budget) --cq;
+    if (fixed + 2 * stage_bytes(cq) > budget) continue;
+    g.cq = cq;
+    g.stage_elems = (int)(stage_bytes(cq) / cs);
+    g.nstage = 8;
+    while (g.nstage > 2 && fixed + (size_t)g.nstage * stage_bytes(cq) > budget) --g.nstage;
+    g.smem = fixed + (size_t)g.nstage * stage_bytes(cq);
+    g.ctas = c;
+    return g;
+  }
+  g.cq = 0;
   return g;
 }
 
@@ -1147,27 +1078,26 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
       const int n = 3 * N;
       const int rg_s = nrhs >= 4 ? 4 : 1;
       const bool pair = std::is_same<T, float>::value && n % 2 == 0;
-      const bool ag = sh.gemv_mode == 2;
-      const GemvStream g = gemv_stream_geometry<T>(n, rg_s, sh.gemv_chunk, pair, ag);
+      const int want = sh.gemv_ti > 0 ? std::min(sh.gemv_ti, 4) : 2;
+      const GemvStream g = gemv_stream_geometry<T>(n, rg_s, sh.gemv_chunk, pair, want);
       if (pr.sym && sh.gemv_mode != 0 && pr.gemv_status.p && n <= 192 && g.cq > 0) {
         const int rg = rg_s;
         int dev = 0, nsm = 0;
         VS_CUDA(cudaGetDevice(&dev));
         VS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
         const int64_t nblk = (int64_t)(L / 2 + 1) * (M / 2 + 1);
-        const int want = sh.gemv_ti > 0 ? std::min(sh.gemv_ti, 2) : g.ctas;
         int* status = pr.gemv_status.as<int>();
 #define VS_GS(RGV, PR)                                                                                        \
   {                                                                                                           \
-    auto k = ag ? k_block_gemv_stream<T, RGV, PR, true> : k_block_gemv_stream<T, RGV, PR, false>;             \
+    auto k = k_block_gemv_stream<T, RGV, PR>;                                                                 \
     set_kernel_smem((const void*)k, g.smem);                                                                  \
     int fit = 0;                                                                                              \
     VS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k, g.nc + 32 + 32 * g.nv, g.smem));          \
-    const dim3 grid((unsigned)std::min<int64_t>(nblk, (int64_t)nsm * std::max(1, std::min(want, fit))),     \
+    const dim3 grid((unsigned)std::min<int64_t>(nblk, (int64_t)nsm * std::max(1, std::min(g.ctas, fit))),   \
                     ceil_div(nrhs, rg));                                                                      \
     k<<<grid, g.nc + 32 + 32 * g.nv, g.smem, st>>>(t, inv, L, M, N, (int64_t)L * M * N * 3, nrhs, skip,        \
                                                    skip_stride, g.cq, g.nstage, g.stage_elems, g.G, g.nc,     \
-                                                   g.nv, g.nvb, status);                                      \
+                                                   g.nv, status);                                             \
   }
         if constexpr (std::is_same<T, float>::value) {
           if (pair) {
@@ -1307,16 +1237,14 @@ void autotune_prec(vs_prec& pr, cudaStream_t st) {
     }
     sh.gemv_threads = 0;
     const int n = 3 * pr.N;
-    for (int mode : {1, 2}) {
-      sh.gemv_mode = mode;
-      for (int ctas : {1, 2}) {
-        for (int cq : {0, 16, 32}) {
-          if (cq >= n) continue;
-          sh.gemv_ti = ctas;
-          sh.gemv_chunk = cq;
-          const float t = time_ms_prec(st, reps, [&] { prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 2); });
-          if (t < best) { best = t; bti = ctas; bth = 0; bmode = mode; bchunk = cq; }
-        }
+    sh.gemv_mode = 1;
+    for (int ctas : {1, 2, 3, 4}) {
+      for (int cq : {0, 16, 32, (n + 1) / 2}) {
+        if (cq >= n) continue;
+        sh.gemv_ti = ctas;
+        sh.gemv_chunk = cq;
+        const float t = time_ms_prec(st, reps, [&] { prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 2); });
+        if (t < best) { best = t; bti = ctas; bth = 0; bmode = 1; bchunk = cq; }
       }
     }
     sh.gemv_ti = bti;
