@@ -275,6 +275,35 @@ int vs_plane_wave(vs_op* op, const double* x, const double* y, const double* z, 
  * Flatau 1994, eq. 8).  Absent from the reference (README.md:35). */
 int vs_cext(vs_op* op, const double* P, const double* Einc, double ko, double dV, double e0norm2, double* cext);
 
+/* Whole-domain apply over every entry of the (L,M,N,3) grid (column-major,
+ * 3*L*M*N complex per right-hand side, zeros where there is no material):
+ *   y = a x + b crop(G * x),   a, b complex scalars,
+ * with op's operator spectrum.  Replaces the MVP_eval handle of
+ * main_DDA.m:142-145 (MVP over idxAll with Mr = 1, Mc = dV, Gram = 1/alpha:
+ * a = 1/alpha, b = -dV) and mv_L_const.m:1-80 as called by
+ * E_field_Nop_const.m:76-84 (JOut = crop(fN * J) - Gram J: a = -Gram, b = 1).
+ * Host buffers, complex double; precision VS_C64 or VS_C128. */
+int vs_op_apply_domain(vs_op* op, const double* x_grid, double* y_grid, int64_t nrhs, const double a[2],
+                       const double b[2], int precision);
+
+/* Total field on the whole grid after a DDA solve (main_DDA.m:136-148):
+ *   Pout = P on op's unknowns, 0 elsewhere;  E = Einc - (Pout/alpha - dV crop(G * Pout)) + Pout/chi.
+ *   P: n3 per right-hand side; Einc_grid, E_grid: 3*L*M*N per right-hand side
+ *   (the incident field on the whole grid, PlaneWavePointWise.m over r);
+ *   alpha, chi: complex scalars (alpha_LDR and (m^2-1)/(4 pi) of main_DDA.m:139). */
+int vs_field_dda(vs_op* op, const double* P, const double* Einc_grid, int64_t nrhs, const double alpha[2],
+                 double dV, const double chi[2], double* E_grid, int precision);
+
+/* Far-field amplitude of the dipoles p_j = dV P_j in ndir unit directions n:
+ *   F(n) = ko^2 dV (I - n n^T) sum_j P_j exp(-i ko n . r_j),   E_sca -> exp(i ko r)/r F(n)
+ * (far zone of the DDA Green tensor of getOPERATOR_DDA.m:99-113; Draine &
+ * Flatau 1994).  The reference has no far-field routine (README.md:35).  With
+ * F(k_inc) the optical theorem gives C_ext = 4 pi / ko Im(conj(E0) . F) / |E0|^2.
+ *   P: n3 per right-hand side; x, y, z: the grid axes (as vs_plane_wave);
+ *   dirs: ndir x 3 unit vectors; F: nrhs x ndir x 3 complex.  FP64. */
+int vs_far_field(vs_op* op, const double* P, int64_t nrhs, const double* x, const double* y, const double* z,
+                 double ko, double dV, const double* dirs, int64_t ndir, double* F);
+
 /* C_ext and its gradient with respect to each voxel's permittivity by the
  * adjoint method: solves A P = Einc and A^T lam = conj(Einc) with opts (the
  * operator must carry Gram = 1/alpha_LDR(eps) per voxel and Mc = dV, the DDA

@@ -27,6 +27,6 @@ from .mvp import MVP, mv_AN_const, dense_dda_matrix, dense_from_toeplitz
 from .precond import (circ_1_level, circ_2_level, invert_blocks,
                       mvp_circ_2_level, chan_mvp_idx, circ_1_level_blocks)
 from .krylov import bicgstab, gmres, pgmres
-from .physics import (PlaneWavePointWise, cext_dda, cext_grad_dda, mie_qext)
+from .physics import (PlaneWavePointWise, cext_dda, cext_grad_dda, far_field, field_dda, mie_qext)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -9,9 +9,15 @@ FP64 restatement / published methods (test infrastructure only).
 * Gradient: adjoint method on A(eps) P = E_inc with A = diag(1/alpha_LDR(eps)) - dV*G;
   A is complex symmetric, so the adjoint system is A^T lam = conj(E_inc).
 * Mie: Bohren & Huffman (1983) BHMIE series for the extinction efficiency.
+* Whole-domain field: main_DDA.m:136-148 (Pout/Eout on the grid, MVP over idxAll
+  with Mr = 1, Mc = dV, Gram = 1/alpha, E = Einc - Etemp + Eout).
+* Far field: absent from the reference (README.md:35); the far zone of the DDA
+  Green tensor (getOPERATOR_DDA.m:99-113), E_sca -> exp(ik r)/r F(n) with
+  F(n) = k^2 (I - n n) sum_j p_j exp(-ik n.r_j), p_j = dV P_j.
 """
 import numpy as np
 
+from .mvp import MVP
 from .operators import alpha_ldr, dalpha_inv_deps
 
 
@@ -66,3 +72,30 @@ def mie_qext(x, m, nstop=None):
         chi0, chi1 = chi1, chi
         xi1 = complex(psi1, -chi1)
     return 2.0 / x ** 2 * q
+
+
+def field_dda(P, idx3, Einc_grid, fN, alpha, dV, chi, L, M, N):
+    """E on the whole (L,M,N,3) grid (column-major flat), main_DDA.m:136-148."""
+    nD = L * M * N
+    Pout = np.zeros(3 * nD, dtype=complex)
+    Pout[np.asarray(idx3)] = P
+    idx_all = np.arange(3 * nD)
+    temp = MVP(Pout, fN, np.ones((L, M, N)), dV, 1.0 / alpha, "notransp", idx_all)
+    return np.asarray(Einc_grid, dtype=complex) - temp + Pout / chi
+
+
+def far_field(P, idx3, r, ko, dV, dirs):
+    """F(n) (ndir, 3) by the direct sum over the unknowns (P in idx3 order)."""
+    r = np.asarray(r, dtype=float)
+    L, M, N = r.shape[:3]
+    nD = L * M * N
+    idx3 = np.asarray(idx3)
+    vox = idx3[: len(idx3) // 3] % nD
+    pos = r.reshape(nD, 3, order="F")[vox]  # (nvox, 3)
+    Pv = np.asarray(P, dtype=complex).reshape(3, -1)  # (3, nvox)
+    out = []
+    for n in np.asarray(dirs, dtype=float).reshape(-1, 3):
+        ph = np.exp(-1j * ko * (pos @ n))
+        s = Pv @ ph
+        out.append(ko ** 2 * dV * (s - n * (n @ s)))
+    return np.array(out)

@@ -120,3 +120,71 @@ def test_slab_64x64x16_gradient_central_differences(api):
             worst = max(worst, abs(fd - g[j]) / sc)
             assert abs(fd - g[j]) <= 1e-3 * sc, (j, step, fd, g[j], sc)
     print(f"central differences: worst |fd - adjoint| / max|grad| = {worst:.2e}")
+
+
+def _hex_op(api, m=1.31 + 0.05j):
+    p = W.small_hex(m=m, diameter=2.5, nper=4)
+    L, M, N = p["L"], p["M"], p["N"]
+    nD = L * M * N
+    idx3 = np.concatenate([p["idx"], nD + p["idx"], 2 * nD + p["idx"]])
+    fN, Toep, alpha = O.getOPERATOR_DDA(p["r"], p["ko"], p["refInd"], p["kvec"], p["Eo"])
+    dV = p["d"] ** 3
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    return p, idx3, fN, Toep, alpha, op
+
+
+def test_whole_domain_field_matches_oracle(api):
+    """main_DDA.m:136-148 (total field over the grid) and the mv_L_const.m form
+    of the whole-domain apply, c128 <= 1e-12 and c64 <= 2e-6 relative."""
+    p, idx3, fN, Toep, alpha, op = _hex_op(api)
+    L, M, N = p["L"], p["M"], p["N"]
+    nD = L * M * N
+    dV = p["d"] ** 3
+    rng = np.random.default_rng(11)
+    P = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
+    Einc = O.PlaneWavePointWise(p["Eo"], p["kvec"], p["r"]).ravel(order="F")
+    chi = (p["refInd"] ** 2 - 1) / (4 * np.pi)
+    E_o = O.field_dda(P, idx3, Einc, fN, alpha, dV, chi, L, M, N)
+    for prec, tol in (("c128", 1e-12), ("c64", 2e-6)):
+        E = api.field_dda(op, P, Einc, alpha, dV, chi, precision=prec)
+        assert np.linalg.norm(E - E_o) <= tol * np.linalg.norm(E_o), prec
+    # two right-hand sides in one call
+    P2 = np.stack([P, 1j * P[::-1]])
+    E2 = api.field_dda(op, P2, np.stack([Einc, Einc]), alpha, dV, chi)
+    E2_o = O.field_dda(P2[1], idx3, Einc, fN, alpha, dV, chi, L, M, N)
+    assert np.linalg.norm(E2[0] - E_o) <= 1e-12 * np.linalg.norm(E_o)
+    assert np.linalg.norm(E2[1] - E2_o) <= 1e-12 * np.linalg.norm(E2_o)
+    # JOut = crop(fN * J) - Gram J over the whole domain (a = -Gram, b = 1)
+    gram = 0.7 - 0.2j
+    J = rng.normal(size=3 * nD) + 1j * rng.normal(size=3 * nD)
+    Y_o = O.MVP(J, fN, np.ones((L, M, N)), -1.0, -gram, "notransp", np.arange(3 * nD))
+    for prec, tol in (("c128", 1e-12), ("c64", 2e-6)):
+        Y = api.apply_domain(op, J, -gram, 1.0, precision=prec)
+        assert np.linalg.norm(Y - Y_o) <= tol * np.linalg.norm(Y_o), prec
+
+
+def test_far_field_and_optical_theorem(api):
+    """F(n) against the direct sum (<= 1e-12 relative) and the optical theorem:
+    4 pi / ko Im(conj(E0).F(k_inc)) / |E0|^2 equals the C_ext sum for any P
+    (E0 orthogonal to k_inc), here on the solved polarisation."""
+    p, idx3, fN, Toep, alpha, op = _hex_op(api)
+    dV = p["d"] ** 3
+    ko = p["ko"]
+    rng = np.random.default_rng(12)
+    dirs = rng.normal(size=(7, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    khat = np.asarray(p["kvec"]) / ko
+    dirs = np.vstack([khat, dirs])
+    Einc = api.plane_wave(op, p["r"], p["kvec"], p["Eo"])
+    P, info, _ = api.solve(op, Einc, tol=1e-10, precision="fp64")
+    F = api.far_field(op, P, p["r"], ko, dV, dirs)
+    F_o = O.far_field(P, idx3, p["r"], ko, dV, dirs)
+    assert np.linalg.norm(F - F_o) <= 1e-12 * np.linalg.norm(F_o)
+    E0 = np.asarray(p["Eo"], dtype=complex)
+    c_ot = 4 * np.pi / ko * np.imag(np.vdot(E0, F[0])) / np.sum(np.abs(E0) ** 2)
+    c_sum = api.cext(op, P, Einc, ko, dV, p["Eo"])
+    assert abs(c_ot - c_sum) <= 1e-11 * abs(c_sum)
+    # transversality and two right-hand sides
+    assert np.abs(np.einsum("dc,dc->d", F, dirs)).max() <= 1e-12 * np.abs(F).max()
+    F2 = api.far_field(op, np.stack([P, 2 * P]), p["r"], ko, dV, dirs)
+    assert np.linalg.norm(F2[1] - 2 * F) <= 1e-13 * np.linalg.norm(F)

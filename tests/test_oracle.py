@@ -272,3 +272,22 @@ def test_nop_assembly_matches_golden():
     for name, shape in (("G_7x6x5", (7, 6, 5)), ("G_1x1x6", (1, 1, 6))):
         G = nop.assembly_nop(*shape, ko, dx)
         assert np.linalg.norm(G - g[name]) <= 1e-12 * np.linalg.norm(g[name]), name
+
+
+def test_far_field_optical_theorem_identity():
+    """The oracle's far-field amplitude in the incident direction reproduces the
+    C_ext sum (Draine & Flatau 1994) for any polarisation: with E_inc = E0
+    exp(i k.r) and E0 orthogonal to k, conj(E0).F(k_hat) = k^2 dV sum conj(E_inc).P."""
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.0, nper=3)
+    L, M, N = p["L"], p["M"], p["N"]
+    nD = L * M * N
+    idx3 = np.concatenate([p["idx"], nD + p["idx"], 2 * nD + p["idx"]])
+    rng = np.random.default_rng(2)
+    P = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
+    ko, dV = p["ko"], p["d"] ** 3
+    E0 = np.asarray(p["Eo"], dtype=complex)
+    Einc = O.PlaneWavePointWise(E0, p["kvec"], p["r"]).ravel(order="F")[idx3]
+    F = O.far_field(P, idx3, p["r"], ko, dV, np.asarray(p["kvec"]) / ko)
+    c_ot = 4 * np.pi / ko * np.imag(np.vdot(E0, F[0])) / np.sum(np.abs(E0) ** 2)
+    c = O.cext_dda(P, Einc, ko, dV, E0)
+    assert abs(c_ot - c) <= 1e-12 * abs(c)

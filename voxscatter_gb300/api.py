@@ -478,6 +478,56 @@ def cext(op, P, Einc, ko, dV, Eo):
     return out.value
 
 
+def _prec_code(precision):
+    return {"c64": L.VS_C64, "c128": L.VS_C128}[precision]
+
+
+def apply_domain(op, x_grid, a, b, precision="c128"):
+    """y = a x + b crop(G * x) on every entry of the (L,M,N,3) grid (column-major
+    flattening, one right-hand side per row of a 2-D x_grid): the whole-domain
+    MVP of main_DDA.m:142-145 (a = 1/alpha, b = -dV) and mv_L_const.m (a = -Gram,
+    b = 1) with op's operator spectrum."""
+    X = np.ascontiguousarray(np.asarray(x_grid, dtype=np.complex128))
+    nrhs = 1 if X.ndim == 1 else X.shape[0]
+    Y = np.zeros_like(X)
+    av = np.array([complex(a).real, complex(a).imag]); bv = np.array([complex(b).real, complex(b).imag])
+    L.check(op.ctx._lib.vs_op_apply_domain(op.h, L.dptr(X), L.dptr(Y), nrhs, L.dptr(av), L.dptr(bv),
+                                           _prec_code(precision)), op.ctx.h)
+    return Y
+
+
+def field_dda(op, P, Einc_grid, alpha, dV, chi, precision="c128"):
+    """Total field on the whole grid after a DDA solve, main_DDA.m:136-148:
+    E = Einc - (Pout/alpha - dV crop(G * Pout)) + Pout/chi with Pout = P on the
+    unknowns and 0 elsewhere.  P: n3 (or nrhs x n3); Einc_grid: 3LMN (or
+    nrhs x 3LMN), column-major (L,M,N,3).  Returns E in the layout of Einc_grid."""
+    Pa = np.ascontiguousarray(np.asarray(P, dtype=np.complex128))
+    Ea = np.ascontiguousarray(np.asarray(Einc_grid, dtype=np.complex128))
+    nrhs = 1 if Pa.ndim == 1 else Pa.shape[0]
+    out = np.zeros_like(Ea)
+    al = np.array([complex(alpha).real, complex(alpha).imag]); ch = np.array([complex(chi).real, complex(chi).imag])
+    L.check(op.ctx._lib.vs_field_dda(op.h, L.dptr(Pa), L.dptr(Ea), nrhs, L.dptr(al), float(dV), L.dptr(ch),
+                                     L.dptr(out), _prec_code(precision)), op.ctx.h)
+    return out
+
+
+def far_field(op, P, r, ko, dV, dirs):
+    """Far-field amplitude F(n) = ko^2 dV (I - n n^T) sum_j P_j exp(-i ko n.r_j)
+    for the unit directions dirs (ndir x 3); returns (ndir, 3), or (nrhs, ndir, 3)
+    for a 2-D P.  E_sca -> exp(i ko r)/r F(n); the optical theorem gives
+    C_ext = 4 pi / ko Im(conj(E0).F(k_inc)) / |E0|^2."""
+    Pa = np.ascontiguousarray(np.asarray(P, dtype=np.complex128))
+    nrhs = 1 if Pa.ndim == 1 else Pa.shape[0]
+    r = np.asarray(r, dtype=float)
+    x = np.ascontiguousarray(r[:, 0, 0, 0]); y = np.ascontiguousarray(r[0, :, 0, 1])
+    z = np.ascontiguousarray(r[0, 0, :, 2])
+    D = np.ascontiguousarray(np.asarray(dirs, dtype=float).reshape(-1, 3))
+    F = np.zeros((nrhs, D.shape[0], 3), dtype=np.complex128)
+    L.check(op.ctx._lib.vs_far_field(op.h, L.dptr(Pa), nrhs, L.dptr(x), L.dptr(y), L.dptr(z), float(ko), float(dV),
+                                     L.dptr(D), D.shape[0], L.dptr(F)), op.ctx.h)
+    return F[0] if Pa.ndim == 1 else F
+
+
 def cext_grad(op, prec, Einc, eps, ko, d, kvec, Eo, tol=1e-6, maxit=2000, precision="mixed"):
     """(C_ext, dC/dRe(eps), dC/dIm(eps), P, info_fwd, info_adj) by the adjoint method."""
     lib = op.ctx._lib

@@ -314,6 +314,19 @@ void ctx_release(vs_ctx* ctx) {
   delete ctx;
 }
 
+// host complex double -> device buffer of the precision's type
+static void upload_as(const double* h, int64_t n, bool c64, vs::DevBuf& stage, vs::DevBuf& out, cudaStream_t st) {
+  if (c64) {
+    stage.alloc(n * sizeof(double2));
+    out.alloc(n * sizeof(float2));
+    VS_CUDA(cudaMemcpyAsync(stage.p, h, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    vs::c128_to_c64(stage.as<double2>(), out.as<float2>(), n, st);
+  } else {
+    out.alloc(n * sizeof(double2));
+    VS_CUDA(cudaMemcpyAsync(out.p, h, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+  }
+}
+
 extern "C" {
 
 int vs_ctx_create(int device, vs_ctx** out) {
@@ -995,6 +1008,104 @@ int vs_plane_wave(vs_op* op, const double* x, const double* y, const double* z, 
     const double2 e[3] = {make_double2(E0[0], E0[1]), make_double2(E0[2], E0[3]), make_double2(E0[4], E0[5])};
     vs::plane_wave_device(*op, dx.as<double>(), dy.as<double>(), dz.as<double>(), kvec, e, db.as<double2>(), st);
     VS_CUDA(cudaMemcpyAsync(b_out, db.p, op->n3 * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+int vs_op_apply_domain(vs_op* op, const double* x_grid, double* y_grid, int64_t nrhs, const double* a,
+                       const double* b, int precision) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(x_grid && y_grid && a && b, "NULL argument");
+    VS_REQUIRE(nrhs >= 1 && nrhs <= 65535, "nrhs must be in [1, 65535]");
+    VS_REQUIRE(precision == VS_C64 || precision == VS_C128, "precision must be VS_C64 or VS_C128");
+    cudaStream_t st = op->ctx->stream;
+    const int64_t n = 3 * op->V * nrhs;
+    const bool c64 = precision == VS_C64;
+    vs::DevBuf stage, xd, yd, y64;
+    upload_as(x_grid, n, c64, stage, xd, st);
+    if (c64) {
+      yd.alloc(n * sizeof(float2));
+      vs::ensure_scratch(*op, (int)nrhs, sizeof(float2));
+      vs::matvec_domain<float>(*op, xd.as<float2>(), yd.as<float2>(), (int)nrhs, make_float2((float)a[0], (float)a[1]),
+                               make_float2((float)b[0], (float)b[1]), st);
+      y64.alloc(n * sizeof(double2));
+      vs::c64_to_c128(yd.as<float2>(), y64.as<double2>(), n, st);
+      VS_CUDA(cudaMemcpyAsync(y_grid, y64.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    } else {
+      yd.alloc(n * sizeof(double2));
+      vs::ensure_scratch(*op, (int)nrhs, sizeof(double2));
+      vs::matvec_domain<double>(*op, xd.as<double2>(), yd.as<double2>(), (int)nrhs, make_double2(a[0], a[1]),
+                                make_double2(b[0], b[1]), st);
+      VS_CUDA(cudaMemcpyAsync(y_grid, yd.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    }
+    VS_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+int vs_field_dda(vs_op* op, const double* P, const double* Einc_grid, int64_t nrhs, const double* alpha, double dV,
+                 const double* chi, double* E_grid, int precision) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(P && Einc_grid && alpha && chi && E_grid, "NULL argument");
+    VS_REQUIRE(nrhs >= 1 && nrhs <= 65535, "nrhs must be in [1, 65535]");
+    VS_REQUIRE(precision == VS_C64 || precision == VS_C128, "precision must be VS_C64 or VS_C128");
+    const double a2 = alpha[0] * alpha[0] + alpha[1] * alpha[1], c2 = chi[0] * chi[0] + chi[1] * chi[1];
+    VS_REQUIRE(a2 > 0 && c2 > 0, "alpha and chi must be nonzero");
+    cudaStream_t st = op->ctx->stream;
+    const int64_t ng = 3 * op->V * nrhs, np = op->n3 * nrhs;
+    const bool c64 = precision == VS_C64;
+    const double ia_re = alpha[0] / a2, ia_im = -alpha[1] / a2;  // 1/alpha
+    const double2 inv_chi = make_double2(chi[0] / c2, -chi[1] / c2);
+    vs::DevBuf stage, stage2, pd, pg, yd, ed, ein;
+    upload_as(P, np, c64, stage, pd, st);
+    ed.alloc(ng * sizeof(double2));
+    if (c64) {
+      pg.alloc(ng * sizeof(float2));
+      yd.alloc(ng * sizeof(float2));
+      vs::to_grid<float2>(*op, pd.as<float2>(), pg.as<float2>(), (int)nrhs, st);
+      vs::ensure_scratch(*op, (int)nrhs, sizeof(float2));
+      vs::matvec_domain<float>(*op, pg.as<float2>(), yd.as<float2>(), (int)nrhs, make_float2((float)ia_re, (float)ia_im),
+                               make_float2((float)-dV, 0.f), st);
+      upload_as(Einc_grid, ng, true, stage2, ein, st);
+      vs::field_combine<float2>(ein.as<float2>(), yd.as<float2>(), pg.as<float2>(), inv_chi, ng, ed.as<double2>(), st);
+    } else {
+      pg.alloc(ng * sizeof(double2));
+      yd.alloc(ng * sizeof(double2));
+      vs::to_grid<double2>(*op, pd.as<double2>(), pg.as<double2>(), (int)nrhs, st);
+      vs::ensure_scratch(*op, (int)nrhs, sizeof(double2));
+      vs::matvec_domain<double>(*op, pg.as<double2>(), yd.as<double2>(), (int)nrhs, make_double2(ia_re, ia_im),
+                                make_double2(-dV, 0.0), st);
+      upload_as(Einc_grid, ng, false, stage2, ein, st);
+      vs::field_combine<double2>(ein.as<double2>(), yd.as<double2>(), pg.as<double2>(), inv_chi, ng, ed.as<double2>(),
+                                 st);
+    }
+    VS_CUDA(cudaMemcpyAsync(E_grid, ed.p, ng * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+int vs_far_field(vs_op* op, const double* P, int64_t nrhs, const double* x, const double* y, const double* z,
+                 double ko, double dV, const double* dirs, int64_t ndir, double* F) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(P && x && y && z && dirs && F, "NULL argument");
+    VS_REQUIRE(nrhs >= 1 && nrhs <= 65535, "nrhs must be in [1, 65535]");
+    VS_REQUIRE(ndir >= 1 && ndir <= (int64_t)1 << 30, "ndir must be in [1, 2^30]");
+    cudaStream_t st = op->ctx->stream;
+    vs::DevBuf dp, dx, dy, dz, dd, df;
+    dp.alloc(op->n3 * nrhs * sizeof(double2));
+    dx.alloc(op->L * sizeof(double)); dy.alloc(op->M * sizeof(double)); dz.alloc(op->N * sizeof(double));
+    dd.alloc(ndir * 3 * sizeof(double));
+    df.alloc(nrhs * ndir * 3 * sizeof(double2));
+    VS_CUDA(cudaMemcpyAsync(dp.p, P, op->n3 * nrhs * sizeof(double2), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemcpyAsync(dx.p, x, op->L * sizeof(double), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemcpyAsync(dy.p, y, op->M * sizeof(double), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemcpyAsync(dz.p, z, op->N * sizeof(double), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemcpyAsync(dd.p, dirs, ndir * 3 * sizeof(double), cudaMemcpyHostToDevice, st));
+    vs::far_field_device(*op, dp.as<double2>(), (int)nrhs, dx.as<double>(), dy.as<double>(), dz.as<double>(),
+                         dd.as<double>(), (int)ndir, ko, dV, df.as<double2>(), st);
+    VS_CUDA(cudaMemcpyAsync(F, df.p, nrhs * ndir * 3 * sizeof(double2), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
   });
 }

@@ -114,6 +114,7 @@ struct vs_op {
   int64_t V = 0, n3 = 0;
   vs::DevBuf map3;      // int32[3V]: unknown position of each grid entry, -1 if absent
   vs::DevBuf pos2grid;  // int32[n3]: grid entry of each unknown
+  vs::DevBuf map_all;   // int32[3V]: identity map of whole-domain applies (built on first use)
   VsDiagDev d1, d1c, d2;  // Gram.*Mr, Gram.*conj(Mr), Mc at the unknowns
   bool gsym = false;    // G holds only the first octant (exact per-axis parity)
   vs::DevBuf G32, G64;  // spectrum of the embedded tensor / (P*Q*R): 6 x P*Q*R, or 6 x octant
@@ -201,6 +202,18 @@ void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, c
                 int skip_stride = 0);
 
 // Physics (vs_physics.cu)
+const int* domain_map(vs_op& op, cudaStream_t st);
+template <typename T>
+void matvec_domain(vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, cplx_t<T> ca, cplx_t<T> cb,
+                   cudaStream_t st);
+template <typename C>
+void to_grid(const vs_op& op, const C* x, C* grid, int nrhs, cudaStream_t st);
+template <typename C>
+void field_combine(const C* einc, const C* y, const C* pgrid, double2 inv_chi, int64_t n, double2* e,
+                   cudaStream_t st);
+void far_field_device(const vs_op& op, const double2* P, int nrhs, const double* xs, const double* ys,
+                      const double* zs, const double* dirs, int ndir, double ko, double dV, double2* F,
+                      cudaStream_t st);
 void plane_wave_device(const vs_op& op, const double* x, const double* y, const double* z, const double kvec[3],
                        const double2 E0[3], double2* b, cudaStream_t st);
 void conj_device(const double2* a, double2* b, int64_t n, cudaStream_t st);

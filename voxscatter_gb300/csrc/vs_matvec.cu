@@ -440,6 +440,29 @@ void matvec_scratch(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs,
   launch_strided_pass<T, true>(yi, op.N * 3, nrhs, st);
   launch_x_pass<T>(a, true, mode, nrhs, st);
 }
+// y = a x + b crop(G * x) on every entry of the (L,M,N,3) grid: the same five
+// launches with the identity unknown map and scalar diagonals (d1 = a,
+// d2 = -b of the 'notransp' form y = d1 x - d2 conv).  MVP_eval of
+// main_DDA.m:142-145 (a = 1/alpha, b = -dV) and mv_L_const.m (a = -Gram, b = 1).
+template <typename T>
+void matvec_domain(vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, cplx_t<T> ca, cplx_t<T> cb,
+                   cudaStream_t st) {
+  using C = cplx_t<T>;
+  PipeArgs<T> a = pipe_args<T>(op, x, y, nullptr);
+  a.map3 = domain_map(op, st);
+  a.n3 = 3 * op.V;
+  a.d1 = {nullptr, ca};
+  a.d1c = {nullptr, ca};
+  a.d2 = {nullptr, mk<C>(-cb.x, -cb.y)};
+  launch_x_pass<T>(a, false, VS_NOTRANSP, nrhs, st);
+  launch_strided_pass<T, false>(y_pass_args<T>(op, a, false), op.N * 3, nrhs, st);
+  launch_z<T>(op, a, nrhs, st);
+  launch_strided_pass<T, true>(y_pass_args<T>(op, a, true), op.N * 3, nrhs, st);
+  launch_x_pass<T>(a, true, VS_NOTRANSP, nrhs, st);
+}
+template void matvec_domain<float>(vs_op&, const float2*, float2*, int, float2, float2, cudaStream_t);
+template void matvec_domain<double>(vs_op&, const double2*, double2*, int, double2, double2, cudaStream_t);
+
 template void matvec_scratch<float>(const vs_op&, const float2*, float2*, int, int, float2*, float2*, cudaStream_t);
 template void matvec_scratch<double>(const vs_op&, const double2*, double2*, int, int, double2*, double2*,
                                      cudaStream_t);
