@@ -169,6 +169,14 @@ enum vs_prec_mask { VS_BUILD_C64 = 1, VS_BUILD_C128 = 2 };
 int vs_circ_levels(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* toep, double* circL_out,
                    double* circM_out, double* blocks_out);
 
+/* Face vector of the JVIE 2-level preconditioner from the relative
+ * permittivity grid (scatteringHumanHead.m:157-177): the mean of eps_r over x
+ * and then y in each z layer, face_2(k) = (t_k - 1) / t_k, and
+ * face3 = [face_2; face_2; face_2] (3N complex) -- the d argument of
+ * vs_prec_create with shift = Gram.  eps_r: L*M*N complex, column-major.
+ * Host arithmetic. */
+int vs_eps_layer_average(int64_t L, int64_t M, int64_t N, const double* eps_r, double* face3);
+
 /* Preconditioner inv(shift*I - diag(d)*C_ij) for every (x,y) frequency of the
  * 2-level circulant approximation of op's Toeplitz tensor:
  * main_DDA.m:98-116 (shift = 1/alpha_LDR, d = dV) and

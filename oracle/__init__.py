@@ -24,7 +24,7 @@ from .operators import (alpha_ldr, green_toeplitz, circulant_nop_const,
                         gperiodic_coeff_nop, fft_operator, getOPERATOR_DDA,
                         dalpha_inv_deps)
 from .mvp import MVP, mv_AN_const, dense_dda_matrix, dense_from_toeplitz
-from .precond import (circ_1_level, circ_2_level, invert_blocks,
+from .precond import (circ_1_level, circ_2_level, eps_layer_average, invert_blocks,
                       mvp_circ_2_level, chan_mvp_idx, circ_1_level_blocks)
 from .krylov import bicgstab, gmres, pgmres
 from .physics import (PlaneWavePointWise, cext_dda, cext_grad_dda, far_field, field_dda, mie_qext)

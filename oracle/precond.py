@@ -144,3 +144,13 @@ def chan_mvp_idx(inv_blocks, JIn, L, M, N, idx):
     temp = np.einsum("iab,ib->ia", inv_blocks, temp)
     temp = _F.ifft(temp, axis=0)
     return temp.ravel(order="F")[np.asarray(idx)]
+
+
+def eps_layer_average(eps_r):
+    """face3_2 of scatteringHumanHead.m:157-177: average eps_r over x, then over
+    y, per z layer; (t - 1)/t repeated for the three components."""
+    e = np.asarray(eps_r, dtype=complex)
+    hey = e.sum(axis=0) / e.shape[0]          # (M, N): sum(epsilon_r, 1) ./ L
+    kk = hey.sum(axis=0) / e.shape[1]         # (N,): sum(er_av_x, 2) ./ M
+    face_2 = (kk - 1) / kk
+    return np.concatenate([face_2, face_2, face_2])

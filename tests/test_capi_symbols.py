@@ -43,3 +43,17 @@ def test_no_gpu_fails_loudly(lib):
     st = lib.vs_ctx_create(0, ctypes.byref(h))
     assert st != _lib.VS_OK
     assert lib.vs_last_error(None)
+
+
+def test_eps_layer_average_host(lib):
+    """vs_eps_layer_average is host arithmetic: against the restatement of
+    scatteringHumanHead.m:157-177 without a GPU (<= 1e-14 relative)."""
+    import numpy as np
+    import oracle as O
+    from voxscatter_gb300 import api
+    rng = np.random.default_rng(4)
+    eps = 2.0 + rng.normal(size=(7, 5, 4)) + 0.1j * rng.normal(size=(7, 5, 4))
+    f = api.eps_layer_average(eps)
+    f_o = O.eps_layer_average(eps)
+    assert f.shape == (12,)
+    assert np.abs(f - f_o).max() <= 1e-14 * np.abs(f_o).max()

@@ -87,8 +87,11 @@ def test_prec_jvie_face_vector_and_batch(api):
     _, c1_o = O.circ_1_level(Toep, L, M, N, 0, "off")
     _, blk_o = O.circ_2_level(c1_o, L, M, N)
     rng = np.random.default_rng(2)
-    face = (0.3 + 0.1 * rng.normal(size=N)) + 0.05j * rng.normal(size=N)
-    face3 = np.concatenate([face, face, face])
+    # the face vector of scatteringHumanHead.m:157-177 from an inhomogeneous
+    # permittivity grid (the library's averaging against the oracle's)
+    eps_r = 1.8 + 0.4 * rng.normal(size=(L, M, N)) + 0.05j * rng.normal(size=(L, M, N))
+    face3 = api.eps_layer_average(eps_r)
+    assert rel(face3, O.eps_layer_average(eps_r)) < 1e-14
     gram = 0.8
     inv_o = O.invert_blocks(blk_o, gram, face3)
     op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)

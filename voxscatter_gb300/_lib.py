@@ -90,6 +90,7 @@ SIGNATURES.update({
     "vs_plane_wave": (C.c_int, [_vp, _pd, _pd, _pd, _pd, _pd, _pd]),
     "vs_cext": (C.c_int, [_vp, _pd, _pd, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double)]),
     "vs_op_apply_domain": (C.c_int, [_vp, _pd, _pd, C.c_int64, _pd, _pd, C.c_int]),
+    "vs_eps_layer_average": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, _pd, _pd]),
     "vs_field_dda": (C.c_int, [_vp, _pd, _pd, C.c_int64, _pd, C.c_double, _pd, _pd, C.c_int]),
     "vs_far_field": (C.c_int, [_vp, _pd, C.c_int64, _pd, _pd, _pd, C.c_double, C.c_double, _pd, C.c_int64, _pd]),
     "vs_cext_grad": (C.c_int, [_vp, _vp, _pd, _pd, C.c_double, C.c_double, _pd, _pd, C.POINTER(vs_solve_opts),

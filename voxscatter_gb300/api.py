@@ -91,6 +91,19 @@ def alpha_ldr(m, ko, d, kvec, Eo, is_eps=False):
     return out[0] if np.ndim(m) == 0 else out.reshape(np.shape(m))
 
 
+def eps_layer_average(eps_r):
+    """face3 (3N) of the JVIE 2-level preconditioner from the relative
+    permittivity grid eps_r (L, M, N): (t - 1)/t with t the x- then y-average of
+    each z layer, repeated for the three components (scatteringHumanHead.m:157-177)."""
+    lib = L.load()
+    e = np.asarray(eps_r, dtype=np.complex128)
+    L_, M_, N_ = e.shape
+    ef = np.ascontiguousarray(e.ravel(order="F"))
+    out = np.zeros(3 * N_, dtype=np.complex128)
+    L.check(lib.vs_eps_layer_average(L_, M_, N_, L.dptr(ef), L.dptr(out)))
+    return out
+
+
 def nop_assemble(L_, M_, N_, ko, dx, near_J=None, ctx=None):
     """Galerkin N-operator Toeplitz tensor G (L, M, N, 6) of assembly_nop_const.m
     (far and medium cells on the device); near_J: the singular near block

@@ -396,6 +396,30 @@ int vs_alpha_ldr(const double* m, int64_t n, int is_eps, double ko, double d, co
   });
 }
 
+int vs_eps_layer_average(int64_t L, int64_t M, int64_t N, const double* eps_r, double* face3) {
+  return guarded(nullptr, [&] {
+    VS_REQUIRE(eps_r && face3, "NULL argument");
+    VS_REQUIRE(L >= 1 && M >= 1 && N >= 1, "L, M, N must be positive");
+    const cd* e = reinterpret_cast<const cd*>(eps_r);
+    cd* f = reinterpret_cast<cd*>(face3);
+    for (int64_t k = 0; k < N; ++k) {
+      // mean over x, then over y (the order of the reference's two averages)
+      cd sy = 0;
+      for (int64_t j = 0; j < M; ++j) {
+        cd sx = 0;
+        for (int64_t i = 0; i < L; ++i) sx += e[i + L * (j + M * k)];
+        sy += sx / (double)L;
+      }
+      const cd t = sy / (double)M;
+      VS_REQUIRE(std::abs(t) > 0, "layer-average permittivity is zero");
+      const cd fk = (t - 1.0) / t;
+      f[k] = fk;
+      f[N + k] = fk;
+      f[2 * N + k] = fk;
+    }
+  });
+}
+
 int vs_green_dda(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* ox, const double* oy,
                  const double* oz, double ko, int near_quad, double* toep_out) {
   if (!ctx) return VS_ERR_ARG;
