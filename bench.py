@@ -165,6 +165,8 @@ def _pass_names(op, prec):
     a, b, c, d = xy(so, "")
     names_mv = [a, b, "k_z2" if so["z_reg"] in (1, 2) else "k_z", c, d]
     a, b, c, d = xy(sp, "prec_")
+    if sp.get("fuse_xy") == 1:  # one plane kernel each way, passes 1 and 3 launch nothing
+        a, b, c, d = "prec_k_plane_fwd", "none", "none", "prec_k_plane_inv"
     names_pc = [a, b, "k_block_gemv_stream" if sp["gemv_mode"] == 1 else "k_block_gemv_sym", c, d]
     return names_mv, names_pc
 

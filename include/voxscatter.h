@@ -354,6 +354,8 @@ typedef struct vs_prec_shape {
   int gemv_chunk;
   int y_reg;       /* y passes: 0 shared-memory Stockham, 1 two-level registers */
   int x_reg;       /* x passes: 0 shared-memory Stockham, 1 two-level registers */
+  int fuse_xy;     /* 1: both FFTs of each (z, component) plane in one CTA when the
+                      plane fits in shared memory; 0 / -1: separate x and y passes */
 } vs_prec_shape;
 int vs_prec_get_shape(const vs_prec* prec, int precision, vs_prec_shape* shape);
 int vs_prec_set_shape(vs_prec* prec, int precision, const vs_prec_shape* shape);

@@ -77,6 +77,13 @@ def test_prec_build_and_apply(api, shape):
             assert rel(pr.apply(x, prec), y_o) < tol, (prec, mode, chunk)
             Y = pr.apply(X.ravel(), prec).reshape(5, -1)
             assert rel(Y, Y_o) < tol, (prec, mode, chunk, "batched")
+    # both FFTs of each plane in one CTA (c64; c128 planes of this size fit too)
+    for prec, tol in (("c128", 1e-10), ("c64", 1e-4)):
+        pr.set_shape(prec, gemv_mode=1, gemv_chunk=0, gemv_blocks=2, gemv_threads=0, fuse_xy=1)
+        assert rel(pr.apply(x, prec), y_o) < tol, (prec, "fused")
+        Y = pr.apply(X.ravel(), prec).reshape(5, -1)
+        assert rel(Y, Y_o) < tol, (prec, "fused batched")
+        pr.set_shape(prec, fuse_xy=0)
     # the MATLAB-style call with caller-supplied inverse blocks
     assert rel(api.mvp_circ_2_level(inv_o, x, L, M, N, idx3), y_o) < 1e-10
 
@@ -115,6 +122,9 @@ def test_prec_config1_size(api):
     y_o = O.mvp_circ_2_level(inv_o, x, L, M, N, idx3)
     assert rel(pr.apply(x, "c128"), y_o) < 1e-10
     assert rel(pr.apply(x, "c64"), y_o) < 1e-4
+    for fuse in (0, 1):  # fused x/y planes with the generic radix-23 stage
+        pr.set_shape("c64", fuse_xy=fuse)
+        assert rel(pr.apply(x, "c64"), y_o) < 1e-4, fuse
 
 
 def test_prec_full_storage_when_parity_is_not_exact(api):
@@ -178,3 +188,26 @@ def test_context_outlives_its_objects(api):
     op.close()
     assert rel(pr.apply(x, "c128"), z0) < 1e-14
     pr.close()
+
+
+def test_prec_fused_planes_hexplate_105x91x26(api):
+    """The fused x/y plane kernel (105 x 91 planes, 78 of them) against the
+    separate two-level passes at the bench size, c64, 1 and 4 right-hand sides
+    (<= 2e-6 relative: the two paths round differently)."""
+    p = W.config2()
+    L, M, N = p["L"], p["M"], p["N"]
+    nD = L * M * N
+    idx3 = np.concatenate([p["idx"], nD + p["idx"], 2 * nD + p["idx"]])
+    Toep = api.green_dda(p["r"], p["ko"])
+    alpha = api.alpha_ldr(p["refInd"], p["ko"], p["d"], p["kvec"], p["Eo"])
+    dV = p["d"] ** 3
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV, precisions=("c64",))
+    rng = np.random.default_rng(8)
+    X = rng.normal(size=(4, idx3.size)) + 1j * rng.normal(size=(4, idx3.size))
+    pr.set_shape("c64", x_reg=1, y_reg=1, fuse_xy=0)
+    y_sep = pr.apply(X[0], "c64")
+    Y_sep = pr.apply(X.ravel(), "c64").reshape(4, -1)
+    pr.set_shape("c64", fuse_xy=1)
+    assert rel(pr.apply(X[0], "c64"), y_sep) < 2e-6
+    assert rel(pr.apply(X.ravel(), "c64").reshape(4, -1), Y_sep) < 2e-6

@@ -76,7 +76,8 @@ class vs_shape(C.Structure):
 
 class vs_prec_shape(C.Structure):
     _fields_ = [("lg_lines_x", C.c_int), ("lg_tile_y", C.c_int), ("gemv_blocks", C.c_int), ("gemv_threads", C.c_int),
-                ("gemv_mode", C.c_int), ("gemv_chunk", C.c_int), ("y_reg", C.c_int), ("x_reg", C.c_int)]
+                ("gemv_mode", C.c_int), ("gemv_chunk", C.c_int), ("y_reg", C.c_int), ("x_reg", C.c_int),
+                ("fuse_xy", C.c_int)]
 
 
 SIGNATURES.update({

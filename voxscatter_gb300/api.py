@@ -328,7 +328,7 @@ class Preconditioner:
                                                 C.byref(sh)))
         return dict(lg_lines_x=sh.lg_lines_x, lg_tile_y=sh.lg_tile_y, gemv_blocks=sh.gemv_blocks,
                     gemv_threads=sh.gemv_threads, gemv_mode=sh.gemv_mode, gemv_chunk=sh.gemv_chunk, y_reg=sh.y_reg,
-                    x_reg=sh.x_reg)
+                    x_reg=sh.x_reg, fuse_xy=sh.fuse_xy)
 
     def set_shape(self, precision="c64", **kw):
         cur = self.shape(precision)

@@ -910,6 +910,7 @@ int vs_prec_get_shape(const vs_prec* prec, int precision, vs_prec_shape* shape) 
   shape->gemv_chunk = s.gemv_chunk;
   shape->y_reg = s.y_reg;
   shape->x_reg = s.x_reg;
+  shape->fuse_xy = s.fuse_xy;
   return VS_OK;
 }
 
@@ -940,9 +941,11 @@ int vs_prec_set_shape(vs_prec* prec, int precision, const vs_prec_shape* shape) 
     VS_REQUIRE(shape->y_reg >= -1 && shape->y_reg <= 1, "y_reg must be -1, 0 or 1");
     s.gemv_mode = shape->gemv_mode;
     VS_REQUIRE(shape->x_reg >= -1 && shape->x_reg <= 1, "x_reg must be -1, 0 or 1");
+    VS_REQUIRE(shape->fuse_xy >= -1 && shape->fuse_xy <= 1, "fuse_xy must be -1, 0 or 1");
     s.gemv_chunk = shape->gemv_chunk;
     s.y_reg = shape->y_reg;
     s.x_reg = shape->x_reg;
+    s.fuse_xy = shape->fuse_xy;
   });
 }
 

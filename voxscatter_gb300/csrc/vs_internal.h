@@ -55,6 +55,7 @@ struct PassShape {
   int gemv_mode = -1;  // 0 register-direct GEMV, 1 streamed through shared memory, -1 default (streamed)
   int gemv_chunk = 0;  // streamed GEMV: block columns per bulk copy (0 = default)
   int z_reg = -1;      // z pass: 0 shared-memory Stockham, 1 two-level, 2 two-level with register cap, -1 default
+  int fuse_xy = -1;    // preconditioner: 1 both x/y FFTs of a plane in one CTA (when it fits), 0/-1 separate passes
 };
 
 // Work vectors and device scalars of the Krylov solvers (vs_krylov.cu).
@@ -197,6 +198,9 @@ void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, co
 template <typename T>
 void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
                      cudaStream_t st, int pass, int skip_stride = 0);
+// kernel launches of one preconditioner apply (3 with fused x/y planes, else 5)
+template <typename T>
+int prec_launches(const vs_prec& pr);
 template <typename T>
 void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip, cudaStream_t st,
                 int skip_stride = 0);

@@ -499,8 +499,9 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
 }
 
 // Kernels in one bicg_iteration: 6 solver kernels, 2 matvecs of 5 passes, and
-// 2 preconditioner applies of 5 passes (or 2 copies without preconditioner).
-static int kernels_per_iteration(const vs_prec* pr) { return 6 + 10 + (pr ? 10 : 2); }
+// 2 preconditioner applies (or 2 copies without preconditioner).
+template <typename T>
+static int kernels_per_iteration(const vs_prec* pr) { return 6 + 10 + (pr ? 2 * prec_launches<T>(*pr) : 2); }
 
 // BiCGSTAB on w.x (initial guesses already there) with initial residuals in
 // w.r, for nrhs right-hand sides.  The absolute tolerance of rhs r is
@@ -568,7 +569,7 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
     for (auto& k : idle) k.skip = 1;
     upload_states(w, idle, st);
     bicg_iteration<T>(op, pr, w, s, n, nrhs, mode, st);
-    *launches += kernels_per_iteration(pr);
+    *launches += kernels_per_iteration<T>(pr);
     cudaGraph_t graph = nullptr;
     VS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     try {
@@ -593,7 +594,7 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
   const int max_launch = (maxit + per_graph - 1) / per_graph + 1;
   for (int it = 0; it < max_launch; ++it) {
     VS_CUDA(cudaGraphLaunch(gc.exec, st));
-    *launches += (int64_t)per_graph * kernels_per_iteration(pr);
+    *launches += (int64_t)per_graph * kernels_per_iteration<T>(pr);
     VS_CUDA(cudaMemcpyAsync(cur.data(), s, nrhs * sizeof(KState), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
     bool all = true;
@@ -1029,7 +1030,7 @@ static int gmres_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t
   auto minv = [&](const C* in, C* out) {
     if (pr) prec_apply<T>(*pr, in, out, 1, &gs->skip, st);
     else k_copy<T><<<g, 256, 0, st>>>(out, in, n);
-    *launches += pr ? 5 : 1;
+    *launches += pr ? prec_launches<T>(*pr) : 1;
   };
   VS_CUDA(cudaMemsetAsync(d, 0, n * sizeof(C), st));
   GState h{};

@@ -1020,6 +1020,81 @@ static GemvStream gemv_stream_geometry(int n, int rg, int chunk_cols, bool pair,
   return g;
 }
 
+// ---- fused x/y passes of the preconditioner -----------------------------
+// One CTA per (z, component) plane and right-hand side does both FFTs of the
+// plane in shared memory (the whole L x M plane plus a Stockham scratch copy
+// and the two twiddle tables), so the plane crosses global memory once each
+// way instead of twice and one launch replaces two.  Forward: gather through
+// map3, FFT along x (M rows of length L, rows contiguous), FFT along y (L
+// columns of length M, columns interleaved), store the plane to t for the
+// block GEMV; inverse: load the plane, inverse FFT along y then x, scatter to
+// the unknowns.  Used when 2*L*M elements and the tables fit beside each
+// other (c64 planes up to about 14,000 points).
+template <typename T>
+static size_t prec_plane_smem(int L, int M) {
+  return (size_t)(2 * L * M + L + M) * sizeof(cplx_t<T>);
+}
+
+template <typename T>
+static bool prec_plane_fits(int L, int M) {
+  return prec_plane_smem<T>(L, M) <= 220 * 1024;
+}
+
+template <typename T, bool INV>
+__global__ void __launch_bounds__(kFftThreads) k_prec_plane(const int* __restrict__ map3, const cplx_t<T>* __restrict__ x,
+                                                           cplx_t<T>* __restrict__ y, cplx_t<T>* __restrict__ t,
+                                                           const cplx_t<T>* __restrict__ twL,
+                                                           const cplx_t<T>* __restrict__ twM, FftPlan pL, FftPlan pM,
+                                                           int L, int M, int N, int64_t n3, const int* skip,
+                                                           int skip_stride) {
+  using C = cplx_t<T>;
+  const int rhs = blockIdx.y;
+  if (skip && skip[rhs * skip_stride]) return;
+  C* sm = shmem<C>();
+  const int LM = L * M, b1 = LM, tL = 2 * LM, tM = 2 * LM + L;
+  load_twiddles(twL, L, tL);
+  load_twiddles(twM, M, tM);
+  const int plane = blockIdx.x;  // z + N * comp
+  const int c = plane / N, z = plane - c * N;
+  const int* map = map3 + ((int64_t)c * N + z) * LM;  // c*V + z*L*M
+  C* tp = t + ((int64_t)rhs * 3 * N + plane) * LM;
+  const FftLayout rows{4, false}, cols{5, true};
+  if constexpr (!INV) {
+    const C* xr = x + (int64_t)rhs * n3;
+    for (int e = threadIdx.x; e < LM; e += kFftThreads) {
+      const int pos = __ldg(map + e);
+      sm[e] = pos >= 0 ? xr[pos] : czero<C>();
+    }
+    __syncthreads();
+    int r = fft_lines<false, C, false>(0, b1, pL, M, L, 1, rows, tL);
+    r = fft_lines<false, C, false>(r, r == 0 ? b1 : 0, pM, L, 1, L, cols, tM);
+    for (int e = threadIdx.x; e < LM; e += kFftThreads) tp[e] = sm[r + e];
+  } else {
+    for (int e = threadIdx.x; e < LM; e += kFftThreads) sm[e] = tp[e];
+    __syncthreads();
+    int r = fft_lines<true, C, false>(0, b1, pM, L, 1, L, cols, tM);
+    r = fft_lines<true, C, false>(r, r == 0 ? b1 : 0, pL, M, L, 1, rows, tL);
+    C* yr = y + (int64_t)rhs * n3;
+    for (int e = threadIdx.x; e < LM; e += kFftThreads) {
+      const int pos = __ldg(map + e);
+      if (pos >= 0) yr[pos] = sm[r + e];
+    }
+  }
+}
+
+template <typename T, bool INV>
+static void launch_prec_plane(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
+                              int skip_stride, cudaStream_t st) {
+  using C = cplx_t<T>;
+  const size_t smem = prec_plane_smem<T>(pr.L, pr.M);
+  auto k = k_prec_plane<T, INV>;
+  set_kernel_smem((const void*)k, smem);
+  k<<<dim3(3 * pr.N, nrhs), kFftThreads, smem, st>>>(pr.map3.as<int>(), x, y, (C*)pr.t.p, pr.axL.tw<T>(),
+                                                      pr.axM.tw<T>(), pr.axL.plan, pr.axM.plan, pr.L, pr.M, pr.N,
+                                                      pr.n3, skip, skip_stride);
+  VS_LAUNCH_CHECK();
+}
+
 template <typename T>
 void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
                      cudaStream_t st, int pass, int skip_stride) {
@@ -1071,9 +1146,16 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
   s.skip = skip;
   s.skip_stride = skip_stride;
   s.two_level = sh.y_reg == 1 ? 1 : 0;
+  // fused x/y planes: pass 0 does both forward FFTs, pass 4 both inverse ones
+  const bool fuse = sh.fuse_xy == 1 && prec_plane_fits<T>(L, M);
   switch (pass) {
-    case 0: launch_x_pass<T>(a, false, MODE_PLAIN, nrhs, st); break;
-    case 1: launch_strided_pass<T, false>(s, 3 * N, nrhs, st); break;
+    case 0:
+      if (fuse) launch_prec_plane<T, false>(pr, x, y, nrhs, skip, skip_stride, st);
+      else launch_x_pass<T>(a, false, MODE_PLAIN, nrhs, st);
+      break;
+    case 1:
+      if (!fuse) launch_strided_pass<T, false>(s, 3 * N, nrhs, st);
+      break;
     case 2: {
       const int n = 3 * N;
       const int rg_s = nrhs >= 4 ? 4 : 1;
@@ -1145,10 +1227,23 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
       VS_LAUNCH_CHECK();
       break;
     }
-    case 3: launch_strided_pass<T, true>(s, 3 * N, nrhs, st); break;
-    default: launch_x_pass<T>(a, true, MODE_PLAIN, nrhs, st); break;
+    case 3:
+      if (!fuse) launch_strided_pass<T, true>(s, 3 * N, nrhs, st);
+      break;
+    default:
+      if (fuse) launch_prec_plane<T, true>(pr, x, y, nrhs, skip, skip_stride, st);
+      else launch_x_pass<T>(a, true, MODE_PLAIN, nrhs, st);
+      break;
   }
 }
+
+template <typename T>
+int prec_launches(const vs_prec& pr) {
+  const PassShape& sh = pr.shape[std::is_same<T, float>::value ? 0 : 1];
+  return sh.fuse_xy == 1 && prec_plane_fits<T>(pr.L, pr.M) ? 3 : 5;
+}
+template int prec_launches<float>(const vs_prec&);
+template int prec_launches<double>(const vs_prec&);
 
 template <typename T>
 void prec_apply(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip, cudaStream_t st,
@@ -1220,6 +1315,12 @@ void autotune_prec(vs_prec& pr, cudaStream_t st) {
           [&] {
             prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 1);
             prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 3);
+          });
+  // the tuned separate x and y passes against the fused plane kernel
+  sh.fuse_xy = 0;
+  best_of(&sh.fuse_xy, 0, 1, [&](int v) { return v == 0 || prec_plane_fits<T>(pr.L, pr.M); },
+          [&] {
+            for (int pass : {0, 1, 3, 4}) prec_apply_pass<T>(pr, x, y, 1, nullptr, st, pass);
           });
   if (pr.sym) {
     // register-direct kernel over blocks per CTA and CTA size, against the
