@@ -449,7 +449,8 @@ def run_ours(args):
 
     line = {"metric": METRIC, "value": ms_mixed, "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c64 (FP64 refinement, dots, norms)",
+            "vs_baseline": None,
+            "dtype": "c64 (refinement residual on FP64 data, its z FFTs in double-float when faster; FP64 dots, norms)",
             "data": "synthetic (seeded reference-rule geometry, plane-wave RHS)",
             "config": dict(_config_dict(p, op.PQR), parallelism=f"replicas x{world}"),
             "converged": ok, "relres": last["relres"], "iterations": last["iter"],

@@ -336,6 +336,9 @@ typedef struct vs_shape {
                       2 two-level with a register cap for occupancy          */
   int y_reg;       /* y passes: 0 shared-memory Stockham, 1 two-level registers */
   int x_reg;       /* x passes: 0 shared-memory Stockham, 1 two-level registers */
+  int z_df;        /* VS_C128 only: 1 runs the two-level z pass in double-float
+                      arithmetic (pairs of floats, about 48 bits) on the FP64
+                      data; 0 / -1 FP64 arithmetic                            */
 } vs_shape;
 int vs_op_get_shape(const vs_op* op, int precision, vs_shape* shape);
 int vs_op_set_shape(vs_op* op, int precision, const vs_shape* shape);

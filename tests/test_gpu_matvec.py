@@ -215,8 +215,17 @@ def test_z_lengths_both_z_kernels(api, R):
         y_o = O.MVP(x, fN, np.ones((L, M, N)), d ** 3, 3.0, "notransp", idx3)
         for prec, tol in (("c64", C64_TOL), ("c128", C128_TOL)):
             for z_reg in (0, 1, 2):
-                op.set_shape(prec, z_reg=z_reg)
+                op.set_shape(prec, z_reg=z_reg, z_df=0)
                 assert rel(op.apply(x, "notransp", prec), y_o) < tol, (prec, z_reg, exact_parity, op.PQR)
+        # c128 with double-float arithmetic in the z pass (lengths up to 64; the
+        # others keep the FP64 kernel): the same FP64 tolerance, all modes
+        op.set_shape("c128", z_reg=2, z_df=1)
+        assert rel(op.apply(x, "notransp", "c128"), y_o) < C128_TOL, ("df", exact_parity, op.PQR)
+        for mode in ("transp", "plain_transp"):
+            op.set_shape("c128", z_df=0)
+            ref = op.apply(x, mode, "c128")
+            op.set_shape("c128", z_df=1)
+            assert rel(op.apply(x, mode, "c128"), ref) < C128_TOL, ("df", mode, exact_parity)
 
 
 Y_LENGTHS = [8, 9, 10, 12, 15, 16, 18, 20, 24, 25, 27, 30, 32, 36, 40, 45, 48, 50, 54, 60, 64, 72, 75, 80, 81, 90,

@@ -71,7 +71,7 @@ class vs_solve_info(C.Structure):
 
 class vs_shape(C.Structure):
     _fields_ = [("lg_lines_x", C.c_int), ("lg_tile_y", C.c_int), ("lg_tile_z", C.c_int), ("z_reg", C.c_int),
-                ("y_reg", C.c_int), ("x_reg", C.c_int)]
+                ("y_reg", C.c_int), ("x_reg", C.c_int), ("z_df", C.c_int)]
 
 
 class vs_prec_shape(C.Structure):

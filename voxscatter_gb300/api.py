@@ -198,7 +198,7 @@ class Operator:
         sh = L.vs_shape()
         L.check(self.ctx._lib.vs_op_get_shape(self.h, L.VS_C64 if precision == "c64" else L.VS_C128, C.byref(sh)))
         return dict(lg_lines_x=sh.lg_lines_x, lg_tile_y=sh.lg_tile_y, lg_tile_z=sh.lg_tile_z, z_reg=sh.z_reg,
-                    y_reg=sh.y_reg, x_reg=sh.x_reg)
+                    y_reg=sh.y_reg, x_reg=sh.x_reg, z_df=sh.z_df)
 
     def set_shape(self, precision="c64", **kw):
         cur = self.shape(precision)

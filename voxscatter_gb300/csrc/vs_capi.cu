@@ -896,6 +896,7 @@ int vs_op_get_shape(const vs_op* op, int precision, vs_shape* shape) {
   shape->z_reg = s.z_reg;
   shape->y_reg = s.y_reg;
   shape->x_reg = s.x_reg;
+  shape->z_df = s.z_df;
   return VS_OK;
 }
 
@@ -971,9 +972,12 @@ int vs_op_set_shape(vs_op* op, int precision, const vs_shape* shape) {
     VS_REQUIRE(shape->z_reg >= -1 && shape->z_reg <= 2, "z_reg must be -1, 0, 1 or 2");
     VS_REQUIRE(shape->y_reg >= -1 && shape->y_reg <= 1, "y_reg must be -1, 0 or 1");
     VS_REQUIRE(shape->x_reg >= -1 && shape->x_reg <= 1, "x_reg must be -1, 0 or 1");
+    VS_REQUIRE(shape->z_df >= -1 && shape->z_df <= 1, "z_df must be -1, 0 or 1");
+    VS_REQUIRE(shape->z_df != 1 || precision == VS_C128, "z_df applies to VS_C128 only");
     s.z_reg = shape->z_reg;
     s.y_reg = shape->y_reg;
     s.x_reg = shape->x_reg;
+    s.z_df = shape->z_df;
     op->kw.graph32.reset();
     op->kw.graph64.reset();
   });

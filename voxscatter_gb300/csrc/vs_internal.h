@@ -56,6 +56,7 @@ struct PassShape {
   int gemv_chunk = 0;  // streamed GEMV: block columns per bulk copy (0 = default)
   int z_reg = -1;      // z pass: 0 shared-memory Stockham, 1 two-level, 2 two-level with register cap, -1 default
   int fuse_xy = -1;    // preconditioner: 1 both x/y FFTs of a plane in one CTA (when it fits), 0/-1 separate passes
+  int z_df = -1;       // c128 z pass: 1 double-float arithmetic on the FP64 data (two-level kernel only)
 };
 
 // Work vectors and device scalars of the Krylov solvers (vs_krylov.cu).

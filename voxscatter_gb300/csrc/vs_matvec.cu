@@ -374,7 +374,11 @@ static PipeArgs<T> pipe_args(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, 
 template <typename T>
 static void launch_z(const vs_op& op, const PipeArgs<T>& a, int nrhs, cudaStream_t st) {
   using C = cplx_t<T>;
-  const int zr = op.shape[std::is_same<T, float>::value ? 0 : 1].z_reg;
+  const PassShape& sh = op.shape[std::is_same<T, float>::value ? 0 : 1];
+  const int zr = sh.z_reg;
+  if constexpr (std::is_same<T, double>::value) {
+    if ((zr == 1 || zr == 2) && sh.z_df == 1 && z_pass_two_level_df(a, op.gsym, nrhs, st)) return;
+  }
   if ((zr == 1 || zr == 2) && z_pass_two_level<T>(a, op.gsym, zr == 2, nrhs, st)) return;
   const int tx = 1 << a.lg_tx;
   dim3 grid(ceil_div(op.P, tx), op.Q, nrhs);
@@ -615,6 +619,22 @@ void autotune_op(vs_op& op, cudaStream_t st) {
       if (t < best) { best = t; arg = v; }
     }
     sh.z_reg = arg;
+    // FP64 data: the double-float two-level kernel against the choice so far
+    // (its results agree with the FP64 kernel to a few units of 2^-48)
+    sh.z_df = 0;
+    if constexpr (std::is_same<T, double>::value) {
+      sh.z_reg = 2;
+      sh.z_df = 1;
+      PipeArgs<T> a = pipe_args<T>(op, x, y, nullptr);
+      if (z_pass_two_level_df(a, op.gsym, 1, st)) {  // instantiated for this length
+        const float t = time_ms(st, reps, [&] { matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 2); });
+        if (t < best) arg = 2;
+        else sh.z_df = 0;
+      } else {
+        sh.z_df = 0;
+      }
+      sh.z_reg = arg;
+    }
   }
   VS_CUDA(cudaStreamSynchronize(st));
 }

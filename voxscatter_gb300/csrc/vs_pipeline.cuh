@@ -67,8 +67,10 @@ template <typename T, bool INV>
 bool strided_two_level(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st);
 
 // Two-level register z pass (vs_zpass.cuh); false when R has no instantiation.
-template <typename T>
+template <typename T, typename K = cplx_t<T>>
 bool z_pass_two_level(const PipeArgs<T>& a, bool sym, bool cap, int nrhs, cudaStream_t st);
+// c128 storage, double-float arithmetic (vs_zpass_df.cu)
+bool z_pass_two_level_df(const PipeArgs<double>& a, bool sym, int nrhs, cudaStream_t st);
 
 template <typename T>
 void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaStream_t st);

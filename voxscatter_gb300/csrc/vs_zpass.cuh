@@ -21,6 +21,7 @@
 // Instantiated per precision in vs_zpass_c64.cu and vs_zpass_c128.cu.
 #pragma once
 #include "vs_pipeline.cuh"
+#include "vs_df.cuh"
 
 namespace vs {
 
@@ -86,15 +87,16 @@ constexpr int z2_min_blocks(int R1, int R2) {
   return nb < 1 ? 1 : (nb > 8 ? 8 : nb);
 }
 
-template <typename T, int R1, int R2, bool CAP>
+template <typename T, int R1, int R2, bool CAP, typename K = cplx_t<T>>
 __global__ void __launch_bounds__(z2_threads(R2, z2_tx<T>(R2)), CAP ? z2_min_blocks<T>(R1, R2) : 1)
     k_z2(PipeArgs<T> a, int sym) {
-  using C = cplx_t<T>;
+  using C = cplx_t<T>;  // storage
+  static_assert(sizeof(K) == sizeof(C), "compute and storage elements share the shared-memory layout");
   constexpr int R = R1 * R2, TX = z2_tx<T>(R2), NT = z2_threads(R2, TX);
   if (a.skip && a.skip[blockIdx.z * a.skip_stride]) return;
-  C* S = shmem<C>();  // [3][R1][R2][TX]
-  C* tw = S + 3 * R * TX;
-  for (int i = threadIdx.x; i < R; i += NT) tw[i] = __ldg(a.twR + i);
+  K* S = shmem<K>();  // [3][R1][R2][TX]
+  K* tw = S + 3 * R * TX;
+  for (int i = threadIdx.x; i < R; i += NT) tw[i] = to_compute<K>(__ldg(a.twR + i));
   const int x0 = blockIdx.x * TX, ky = blockIdx.y;
   const int64_t PQ = (int64_t)a.P * a.Q;
   const int64_t zs = PQ, cs = PQ * a.N;
@@ -108,14 +110,14 @@ __global__ void __launch_bounds__(z2_threads(R2, z2_tx<T>(R2)), CAP ? z2_min_blo
     const int n1 = rest % R1, c = rest / R1;
     const int x = x0 + xl;
     const bool xin = x < a.P;
-    C v[R2];
+    K v[R2];
 #pragma unroll
     for (int n2 = 0; n2 < R2; ++n2) {
       const int z = n1 + R1 * n2;
-      v[n2] = (xin && z < N) ? t2[x + z * zs + c * cs] : czero<C>();
+      v[n2] = (xin && z < N) ? to_compute<K>(t2[x + z * zs + c * cs]) : czero<K>();
     }
-    reg_dft<R2, R2, 1, R1, false, C>(v, tw);
-    C* s = S + ((c * R1 + n1) * R2) * TX + xl;
+    reg_dft<R2, R2, 1, R1, false, K>(v, tw);
+    K* s = S + ((c * R1 + n1) * R2) * TX + xl;
 #pragma unroll
     for (int k2 = 0; k2 < R2; ++k2) s[k2 * TX] = k2 == 0 || n1 == 0 ? v[k2] : cmul(v[k2], tw[n1 * k2]);
   }
@@ -125,16 +127,16 @@ __global__ void __launch_bounds__(z2_threads(R2, z2_tx<T>(R2)), CAP ? z2_min_blo
   for (int it = threadIdx.x; it < R2 * TX; it += NT) {
     const int xl = it % TX, k2 = it / TX;
     const int x = x0 + xl;
-    C u0[R1], u1[R1], u2[R1];
+    K u0[R1], u1[R1], u2[R1];
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) {
       u0[n1] = S[((0 * R1 + n1) * R2 + k2) * TX + xl];
       u1[n1] = S[((1 * R1 + n1) * R2 + k2) * TX + xl];
       u2[n1] = S[((2 * R1 + n1) * R2 + k2) * TX + xl];
     }
-    reg_dft<R1, R1, 1, R2, false, C>(u0, tw);
-    reg_dft<R1, R1, 1, R2, false, C>(u1, tw);
-    reg_dft<R1, R1, 1, R2, false, C>(u2, tw);
+    reg_dft<R1, R1, 1, R2, false, K>(u0, tw);
+    reg_dft<R1, R1, 1, R2, false, K>(u1, tw);
+    reg_dft<R1, R1, 1, R2, false, K>(u2, tw);
     if (x < a.P) {
       int gx = x, gy = ky, Pg = a.P, Qg = a.Q, Rg = R;
       bool fx = false, fy = false;
@@ -152,30 +154,30 @@ __global__ void __launch_bounds__(z2_threads(R2, z2_tx<T>(R2)), CAP ? z2_min_blo
         bool fz = false;
         if (sym && kz > R / 2) { gz = R - kz; fz = true; }
         const int64_t gi = gz * PQg;
-        const C g0 = __ldg(G + gi);
-        C g1 = __ldg(G + PQRg + gi), g2 = __ldg(G + 2 * PQRg + gi);
-        const C g3 = __ldg(G + 3 * PQRg + gi);
-        C g4 = __ldg(G + 4 * PQRg + gi);
-        const C g5 = __ldg(G + 5 * PQRg + gi);
+        const K g0 = to_compute<K>(__ldg(G + gi));
+        K g1 = to_compute<K>(__ldg(G + PQRg + gi)), g2 = to_compute<K>(__ldg(G + 2 * PQRg + gi));
+        const K g3 = to_compute<K>(__ldg(G + 3 * PQRg + gi));
+        K g4 = to_compute<K>(__ldg(G + 4 * PQRg + gi));
+        const K g5 = to_compute<K>(__ldg(G + 5 * PQRg + gi));
         if (fx != fy) { g1.x = -g1.x; g1.y = -g1.y; }
         if (fx != fz) { g2.x = -g2.x; g2.y = -g2.y; }
         if (fy != fz) { g4.x = -g4.x; g4.y = -g4.y; }
-        const C v0 = u0[k1], v1 = u1[k1], v2 = u2[k1];
-        C o0 = cmul(g0, v0); o0 = cfma(g1, v1, o0); o0 = cfma(g2, v2, o0);
-        C o1 = cmul(g1, v0); o1 = cfma(g3, v1, o1); o1 = cfma(g4, v2, o1);
-        C o2 = cmul(g2, v0); o2 = cfma(g4, v1, o2); o2 = cfma(g5, v2, o2);
+        const K v0 = u0[k1], v1 = u1[k1], v2 = u2[k1];
+        K o0 = cmul(g0, v0); o0 = cfma(g1, v1, o0); o0 = cfma(g2, v2, o0);
+        K o1 = cmul(g1, v0); o1 = cfma(g3, v1, o1); o1 = cfma(g4, v2, o1);
+        K o2 = cmul(g2, v0); o2 = cfma(g4, v1, o2); o2 = cfma(g5, v2, o2);
         u0[k1] = o0;
         u1[k1] = o1;
         u2[k1] = o2;
       }
     }
-    reg_dft<R1, R1, 1, R2, true, C>(u0, tw);
-    reg_dft<R1, R1, 1, R2, true, C>(u1, tw);
-    reg_dft<R1, R1, 1, R2, true, C>(u2, tw);
+    reg_dft<R1, R1, 1, R2, true, K>(u0, tw);
+    reg_dft<R1, R1, 1, R2, true, K>(u1, tw);
+    reg_dft<R1, R1, 1, R2, true, K>(u2, tw);
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) {
       const bool plain = n1 == 0 || k2 == 0;
-      const C w = plain ? czero<C>() : twid<true>(tw, n1 * k2);
+      const K w = plain ? czero<K>() : twid<true>(tw, n1 * k2);
       S[((0 * R1 + n1) * R2 + k2) * TX + xl] = plain ? u0[n1] : cmul(u0[n1], w);
       S[((1 * R1 + n1) * R2 + k2) * TX + xl] = plain ? u1[n1] : cmul(u1[n1], w);
       S[((2 * R1 + n1) * R2 + k2) * TX + xl] = plain ? u2[n1] : cmul(u2[n1], w);
@@ -189,15 +191,15 @@ __global__ void __launch_bounds__(z2_threads(R2, z2_tx<T>(R2)), CAP ? z2_min_blo
     const int n1 = rest % R1, c = rest / R1;
     const int x = x0 + xl;
     if (x >= a.P || n1 >= N) continue;
-    C v[R2];
-    const C* s = S + ((c * R1 + n1) * R2) * TX + xl;
+    K v[R2];
+    const K* s = S + ((c * R1 + n1) * R2) * TX + xl;
 #pragma unroll
     for (int k2 = 0; k2 < R2; ++k2) v[k2] = s[k2 * TX];
-    reg_dft<R2, R2, 1, R1, true, C>(v, tw);
+    reg_dft<R2, R2, 1, R1, true, K>(v, tw);
 #pragma unroll
     for (int n2 = 0; n2 < R2; ++n2) {
       const int z = n1 + R1 * n2;
-      if (z < N) t2[x + z * zs + c * cs] = v[n2];
+      if (z < N) t2[x + z * zs + c * cs] = to_storage(v[n2], C{});
     }
   }
 }
@@ -213,22 +215,25 @@ static constexpr ZSplit kZSplits[] = {
     {72, 8, 9},   {80, 8, 10},  {90, 6, 15},  {96, 8, 12},  {108, 6, 18}, {120, 8, 15}, {128, 8, 16},
     {144, 8, 18}, {160, 8, 20}, {180, 6, 30}, {192, 8, 24}, {216, 8, 27}, {240, 8, 30}, {256, 8, 32}};
 
-template <typename T, int R1, int R2>
+// K: the arithmetic type (the storage type, or double-float for FP64 storage;
+// the double-float kernel is built only in its register-capped form).
+template <typename T, int R1, int R2, typename K>
 static void launch_z2(const PipeArgs<T>& a, int sym, bool cap, int nrhs, cudaStream_t st) {
   constexpr int TX = z2_tx<T>(R2), NT = z2_threads(R2, TX);
   const size_t smem = (3ull * R1 * R2 * TX + R1 * R2) * sizeof(cplx_t<T>);
-  auto k = cap ? k_z2<T, R1, R2, true> : k_z2<T, R1, R2, false>;
+  constexpr bool native = std::is_same<K, cplx_t<T>>::value;
+  auto k = (cap || !native) ? k_z2<T, R1, R2, true, K> : k_z2<T, R1, R2, native ? false : true, K>;
   set_kernel_smem((const void*)k, smem);
   k<<<dim3(ceil_div(a.P, TX), a.Q, nrhs), NT, smem, st>>>(a, sym);
   VS_LAUNCH_CHECK();
 }
 
-template <typename T>
+template <typename T, typename K>
 bool z_pass_two_level(const PipeArgs<T>& a, bool sym, bool cap, int nrhs, cudaStream_t st) {
   const int s = sym ? 1 : 0;
   switch (a.R) {
-#define VS_Z2(R1, R2)                                     \
-  case R1 * R2: launch_z2<T, R1, R2>(a, s, cap, nrhs, st); \
+#define VS_Z2(R1, R2)                                        \
+  case R1 * R2: launch_z2<T, R1, R2, K>(a, s, cap, nrhs, st); \
     return true;
     VS_Z2(2, 2) VS_Z2(2, 3) VS_Z2(2, 4) VS_Z2(3, 3) VS_Z2(2, 5) VS_Z2(3, 4) VS_Z2(3, 5)
     VS_Z2(4, 4) VS_Z2(3, 6) VS_Z2(4, 5) VS_Z2(4, 6) VS_Z2(3, 9) VS_Z2(5, 6) VS_Z2(4, 8)
