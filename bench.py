@@ -259,6 +259,30 @@ def _directions(seed, count):
     return out
 
 
+def _krylov_variants(api, stream, op, prec, b_dev, x_dev, steps):
+    """Mixed solves of the same plate with the reference's other Krylov
+    drivers: GMRES(20) (main_DDA.m:128-129) and GCRO-DR(20, 5 recycled
+    vectors) (pgmresDR.m, right preconditioned as the JVIE solvers call it)."""
+    import torch
+    out = {}
+    for name, kw in (("gmres20", dict(method="gmres", restart=20)),
+                     ("gmres_dr20_5", dict(method="gmres_dr", restart=20, ritz=5))):
+        with torch.cuda.stream(stream):
+            x_dev.zero_()
+        api.solve_device(op, b_dev.data_ptr(), x_dev.data_ptr(), prec, tol=TOL, precision="mixed", **kw)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                x_dev.zero_()
+            info = api.solve_device(op, b_dev.data_ptr(), x_dev.data_ptr(), prec, tol=TOL, precision="mixed", **kw)
+        ev1.record(stream)
+        ev1.synchronize()
+        out[name] = {"ms": ev0.elapsed_time(ev1) / steps, "iterations": info["iter"], "relres": info["relres"],
+                     "converged": info["flag"] == 0, "refinements": info["refinements"]}
+    return out
+
+
 def _batched(api, ctx, stream, p, op, prec, steps):
     """16 right-hand sides (8 directions x 2 polarisations) of the plate, one
     batched mixed solve; and the 32-plate x 16-rhs configuration (512 rhs)."""
@@ -446,6 +470,7 @@ def run_ours(args):
               "prec_GBps": sum(pc_bytes) / (sum(pc_ms) * 1e-3) / 1e9}
 
     batched = _batched(api, ctx, stream, p, op, prec, max(1, min(args.steps, 2))) if not args.no_batched else None
+    variants = _krylov_variants(api, stream, op, prec, b_dev, x_dev, max(1, min(args.steps, 2)))
 
     line = {"metric": METRIC, "value": ms_mixed, "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
@@ -461,7 +486,8 @@ def run_ours(args):
             "shapes": {"op": op.shape("c64"), "prec": prec.shape("c64")},
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(b_pin.numel() * 16 * 2),
                     "d2h_bytes_per_step": int(x_pin.numel() * 16)},
-            "gpu_launches": launches * args.steps, "clocks": clk.summary(), "batched": batched}
+            "gpu_launches": launches * args.steps, "clocks": clk.summary(), "batched": batched,
+            "krylov_variants": variants}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         workers = os.cpu_count() or 1
         A, Pm, b = _cpu_oracle_setup(p, workers)

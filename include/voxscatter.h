@@ -210,8 +210,12 @@ int vs_prec_get_blocks(vs_prec* prec, int precision, double* out);
 
 /* VS_BICGSTAB: MATLAB bicgstab(A, b, tol, maxit, M1) (right preconditioned);
  * VS_GMRES: MATLAB gmres(A, b, restart, tol, maxit, M1) (left preconditioned,
- * restarted), here as the inner solver of the FP64 refinement loop. */
-enum vs_solve_method { VS_BICGSTAB = 0, VS_GMRES = 1 };
+ * restarted); VS_GMRES_DR: the reference's pgmresDR(A, b, restart, tol,
+ * maxit, ritz, [], [], M) (src/src_numeric/src_iterative/pgmresDR.m:73,
+ * called by JVIE_Solver_const_GPU.m:400-447): GCRO-DR, right preconditioned,
+ * each restart recycling the `ritz` harmonic Ritz vectors of smallest
+ * magnitude.  Each is the inner solver of the FP64 refinement loop. */
+enum vs_solve_method { VS_BICGSTAB = 0, VS_GMRES = 1, VS_GMRES_DR = 2 };
 enum vs_solve_precision {
   VS_SOLVE_MIXED = 0, /* c64 inner solve on the c64 pipeline inside FP64 iterative refinement */
   VS_SOLVE_FP64 = 1   /* the same Krylov method on the c128 pipeline throughout               */
@@ -228,7 +232,8 @@ typedef struct vs_solve_opts {
   double* resvec;      /* optional: relative residual norms at every half step               */
   int64_t resvec_cap;  /* capacity of resvec                                                 */
   int transpose;       /* 0: solve A x = b; 1: solve A^T x = b (plain transpose, adjoints)   */
-  int restart;         /* VS_GMRES: restart length (Krylov basis size)                        */
+  int restart;         /* VS_GMRES: restart length (Krylov basis size); VS_GMRES_DR: 2..256   */
+  int ritz;            /* VS_GMRES_DR: recycled harmonic Ritz vectors, 1..restart-1           */
 } vs_solve_opts;
 
 typedef struct vs_solve_info {
@@ -243,7 +248,7 @@ typedef struct vs_solve_info {
 
 /* Fill opts with defaults: BiCGSTAB, MIXED, tol 1e-6, maxit 2000, automatic
  * inner tolerance, 10 refinements, 4 iterations per graph, no resvec, no
- * transpose, GMRES restart 50. */
+ * transpose, GMRES restart 50, 10 recycled vectors for GMRES-DR. */
 void vs_solve_opts_default(vs_solve_opts* opts);
 
 /* Solve A x = b with the (optional, may be NULL) preconditioner, right

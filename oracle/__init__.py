@@ -26,7 +26,7 @@ from .operators import (alpha_ldr, green_toeplitz, circulant_nop_const,
 from .mvp import MVP, mv_AN_const, dense_dda_matrix, dense_from_toeplitz
 from .precond import (circ_1_level, circ_2_level, eps_layer_average, invert_blocks,
                       mvp_circ_2_level, chan_mvp_idx, circ_1_level_blocks)
-from .krylov import bicgstab, gmres, pgmres
+from .krylov import bicgstab, gmres, pgmres, pgmres_dr, harm_vecs1, harm_vecs2
 from .physics import (PlaneWavePointWise, cext_dda, cext_grad_dda, far_field, field_dda, mie_qext)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

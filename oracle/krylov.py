@@ -17,6 +17,9 @@ src/src_numeric/src_iterative/pgmres.m:70-181 + pgmres_iter.m:22-150.
   preconditioned residual norm(M\\(b-Ax))/norm(M\\b) and reports iter=[outer, inner].
 * ``pgmres`` restates pgmres.m / pgmres_iter.m (classical Gram-Schmidt, dense
   least squares per step).
+* ``pgmres_dr`` restates pgmresDR.m / pgmresDR_iter.m / getHarmVecs1.m /
+  getHarmVecs2.m (GCRO-DR with harmonic Ritz recycling), with
+  ``numpy.linalg.eig`` / ``scipy.linalg.eig`` for MATLAB's ``eig``.
 
 Iteration counts cannot be pinned to MATLAB's closed built-ins.
 """
@@ -232,3 +235,139 @@ def _pgmres_iter(afun, x, r, m, L1, L2, R1, R2, tol):
     x = x + xupd
     r = V[:, :k + 1] @ res
     return x, r, k, resvec
+
+
+def pgmres_dr(A, b, restart=50, tol=1e-3, maxit=10, ritz=None, L1=None, L2=None, R1=None, R2=None, x0=None):
+    """[x,flag,relres,iter,resvec] = pgmresDR(A,b,restart,tol,maxit,ritz,L1,L2,R1,R2,x0),
+    src/src_numeric/src_iterative/pgmresDR.m:73-281 with its cycle
+    pgmresDR_iter.m:1-142 and the harmonic Ritz selections getHarmVecs1.m /
+    getHarmVecs2.m.  GCRO-DR (Parks, de Sturler, Mackey, Johnson, Maiti 2006):
+    after each cycle of ``restart`` Arnoldi steps the ``ritz`` harmonic Ritz
+    vectors of smallest magnitude span a recycled space U with C = A U
+    orthonormal, and the next cycle runs Arnoldi on (I - C C^H) A.  The
+    Arnoldi steps use classical Gram-Schmidt once against C and once against V
+    (pgmresDR_iter.m:99-107).  ``iter`` = [steps of the last cycle, outer
+    cycles after the first]; ``resvec`` holds the residual estimate of every
+    Arnoldi step relative to norm(L2\\(L1\\b))."""
+    afun = _as_fun(A)
+    b = np.asarray(b, dtype=complex).ravel()
+    n = b.size
+    if ritz is None:
+        ritz = min(10, int(round(restart / 2)))
+    else:
+        ritz = min(ritz, restart - 1)
+    x0 = np.zeros(n, dtype=complex) if x0 is None else np.asarray(x0, dtype=complex).ravel()
+    r = b - afun(x0)
+    bp = b.copy()
+    for Lf in (L1, L2):
+        if Lf is not None:
+            r = _as_fun(Lf)(r); bp = _as_fun(Lf)(bp)
+    bnorm = np.linalg.norm(bp)
+    resvec = [np.linalg.norm(r) / bnorm]
+
+    def right(v):
+        for Rf in (R2, R1):          # pgmresDR_iter.m:58-71: R2 first, then R1
+            if Rf is not None:
+                v = _as_fun(Rf)(v)
+        return v
+
+    def left(v):
+        for Lf in (L1, L2):
+            if Lf is not None:
+                v = _as_fun(Lf)(v)
+        return v
+
+    def cycle(r, C):
+        m = restart
+        V = np.zeros((n, m + 1), dtype=complex)
+        V[:, 0] = r / np.linalg.norm(r)
+        kc = 0 if C is None else C.shape[1]
+        B = np.zeros((kc, m), dtype=complex)
+        H = np.zeros((m + 1, m), dtype=complex)
+        rin = []
+        for k in range(1, m + 1):
+            w = left(afun(right(V[:, k - 1])))
+            if kc:
+                B[:, k - 1] = C.conj().T @ w
+                w = w - C @ B[:, k - 1]
+            H[:k, k - 1] = V[:, :k].conj().T @ w
+            w = w - V[:, :k] @ H[:k, k - 1]
+            H[k, k - 1] = np.linalg.norm(w)
+            V[:, k] = w / H[k, k - 1]
+            rhs = np.zeros(k + 1, dtype=complex); rhs[0] = np.linalg.norm(r)
+            Hk = H[:k + 1, :k]
+            y = np.linalg.lstsq(Hk, rhs, rcond=None)[0]
+            rin.append(np.linalg.norm(rhs - Hk @ y))
+            if rin[-1] < tol * bnorm:
+                return V[:, :k + 1], H[:k + 1, :k], B[:, :k], k, rin
+        return V, H, B, m, rin
+
+    # first cycle: plain GMRES, then the first recycled space (pgmresDR.m:181-221)
+    V, H, _, p, rin = cycle(r, None)
+    resvec.extend(np.asarray(rin) / bnorm)
+    y = np.linalg.lstsq(H, V.conj().T @ r, rcond=None)[0]
+    x = V[:, :p] @ y
+    r = r - V @ (H @ y)
+    U = C = None
+    if resvec[-1] > tol:
+        P = harm_vecs1(p, min(ritz, p - 1), H)
+        U = V[:, :p] @ P
+        Q, R = np.linalg.qr(H @ P)
+        C = V @ Q
+        U = np.linalg.solve(R.T, U.T).T      # U / R
+    outit = 0
+    while resvec[-1] > tol and outit < maxit:  # pgmresDR.m:226-260
+        outit += 1
+        V, H, B, p, rin = cycle(r, C)
+        resvec.extend(np.asarray(rin) / bnorm)
+        k = U.shape[1]
+        d = np.linalg.norm(U, axis=0)
+        D = np.diag(1.0 / d)
+        U = U @ D
+        H2 = np.block([[D.astype(complex), B], [np.zeros((H.shape[0], k), dtype=complex), H]])
+        CV = np.hstack([C, V])
+        y = np.linalg.lstsq(H2, CV.conj().T @ r, rcond=None)[0]
+        x = x + np.hstack([U, V[:, :p]]) @ y
+        r = r - CV @ (H2 @ y)
+        if resvec[-1] > tol:
+            P = harm_vecs2(p + k, k, H2, V, U, C)
+            U = np.hstack([U, V[:, :p]]) @ P
+            Q, R = np.linalg.qr(H2 @ P)
+            C = CV @ Q
+            U = np.linalg.solve(R.T, U.T).T
+    x = x0 + right(x)
+    relres = np.linalg.norm(b - afun(x)) / np.linalg.norm(b)
+    flag = 0 if relres <= tol else 1
+    return x, flag, relres, [p, outit], np.array(resvec)
+
+
+def _sorted_eig(M):
+    """Eigenpairs of M ordered by ascending |lambda| (sortrows on
+    [abs(lambda) vecs'], getHarmVecs1.m:15-19)."""
+    lam, X = np.linalg.eig(M)
+    order = np.argsort(np.abs(lam), kind="stable")
+    return lam[order], X[:, order]
+
+
+def harm_vecs1(m, k, H):
+    """getHarmVecs1.m: the k harmonic Ritz vectors of smallest magnitude of the
+    (m+1) x m Hessenberg H: eig(H_m + h_{m+1,m}^2 H_m^{-H} e_m e_m^T)."""
+    Hm = H[:m, :]
+    f = np.linalg.solve(Hm.conj().T, np.eye(m, dtype=complex)[:, m - 1])
+    M = Hm.copy()
+    M[:, m - 1] += H[m, m - 1] ** 2 * f
+    return _sorted_eig(M)[1][:, :k]
+
+
+def harm_vecs2(m, k, H2, V, U, C):
+    """getHarmVecs2.m: eig(H2^H W, H2^H H2) with W = [C V]^H [U V_{m-k}],
+    keeping the k eigenvectors of largest |lambda| (the harmonic Ritz values
+    of smallest magnitude)."""
+    W = np.zeros((m + 1, m), dtype=complex)
+    W[:k, :k] = C.conj().T @ U
+    W[k:, :k] = V.conj().T @ U
+    W[k:m, k:m] = np.eye(m - k)
+    import scipy.linalg as sl
+    lam, X = sl.eig(H2.conj().T @ W, H2.conj().T @ H2)
+    order = np.argsort(np.abs(lam), kind="stable")
+    return X[:, order][:, m - k:]

@@ -177,3 +177,61 @@ def test_batched_rhs_match_single_solves(api, precision, tol):
             x1, i1, _ = api.solve(op, B[k], pr, tol=tol, precision="fp64")
             assert i1["iter"] == infos[k]["iter"]
             assert np.linalg.norm(x1 - X[k]) <= 1e-12 * np.linalg.norm(x1)
+
+
+def _prec_oracle(p, Toep, alpha, dV, idx3):
+    L, M, N = p["L"], p["M"], p["N"]
+    _, circL = O.circ_1_level(Toep, L, M, N, 0, "off")
+    _, blk = O.circ_2_level(circL, L, M, N)
+    inv = O.invert_blocks(blk, 1 / alpha, dV)
+    return lambda v: O.mvp_circ_2_level(inv, v, L, M, N, idx3)
+
+
+@pytest.mark.parametrize("use_prec", [False, True])
+def test_gmres_dr_matches_oracle_history(api, use_prec):
+    """FP64 device GCRO-DR (restart 5, 2 recycled vectors, right
+    preconditioned) follows the oracle's pgmresDR.m restatement over several
+    cycles: the same Arnoldi residual estimates step by step, so the same
+    harmonic Ritz spaces were recycled."""
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, Toep, alpha, dV, b, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV) if use_prec else None
+    Pm = _prec_oracle(p, Toep, alpha, dV, idx3) if use_prec else None
+    restart, ritz, cycles = 5, 2, 4
+    xo, fo, ro, ito, rvo = O.pgmres_dr(Aor, b, restart, 1e-14, cycles - 1, ritz, R1=Pm)
+    assert len(rvo) == 1 + restart * cycles          # ran all cycles
+    x, info, rv = api.solve(op, b, pr, tol=1e-30, maxit=restart * cycles, precision="fp64", method="gmres_dr",
+                            restart=restart, ritz=ritz, inner_tol=1e-30, max_refine=1)
+    assert info["iter"] == restart * cycles
+    assert len(rv) == len(rvo)
+    assert np.allclose(rv, rvo, rtol=1e-6, atol=1e-13), np.max(np.abs(rv - rvo) / np.abs(rvo))
+    # the same iterate after the same cycles
+    assert np.linalg.norm(x - xo) <= 1e-8 * np.linalg.norm(xo)
+
+
+@pytest.mark.parametrize("precision,tol", [("mixed", 1e-6), ("fp64", 1e-10)])
+@pytest.mark.parametrize("use_prec", [False, True])
+def test_gmres_dr_solves(api, precision, tol, use_prec):
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, Toep, alpha, dV, b, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV) if use_prec else None
+    x, flag, relres, it, resvec = api.pgmresDR(op, b, 8, tol, 100, 3, R1=pr, precision=precision)
+    assert flag == 0, (flag, relres, it)
+    assert relres <= tol
+    assert np.linalg.norm(b - Aor(x)) / np.linalg.norm(b) <= tol * 1.01
+    Ad = O.dense_dda_matrix(p["r"], p["idx"], p["ko"], 1 / alpha, dV)
+    xd = np.linalg.solve(Ad, b)
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 100 * tol
+    assert resvec[0] == pytest.approx(1.0) and len(resvec) >= 2
+
+
+def test_config1_gmres_dr_mixed(api):
+    p = W.config1()
+    L, M, N, idx3, Toep, alpha, dV, b, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
+    x, info, rv = api.solve(op, b, pr, tol=1e-6, precision="mixed", method="gmres_dr", restart=20, ritz=5)
+    assert info["flag"] == 0
+    assert np.linalg.norm(b - Aor(x)) / np.linalg.norm(b) <= 1e-6 * 1.01

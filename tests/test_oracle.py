@@ -142,7 +142,7 @@ def test_circ_1_level_blocks_and_chan_apply():
     assert np.linalg.norm(z - x) <= 1e-10 * np.linalg.norm(x)
 
 
-@pytest.mark.parametrize("solver", ["bicgstab", "gmres", "pgmres"])
+@pytest.mark.parametrize("solver", ["bicgstab", "gmres", "pgmres", "pgmres_dr"])
 @pytest.mark.parametrize("prec", [False, True])
 def test_krylov_solves(solver, prec):
     p = W.small_hex(m=1.31 + 0.05j)
@@ -163,8 +163,11 @@ def test_krylov_solves(solver, prec):
         assert len(resvec) == int(round(2 * it)) + 1
     elif solver == "gmres":
         x, flag, relres, it, resvec = O.gmres(A, b, 200, tol, 1, Pm)
-    else:
+    elif solver == "pgmres":
         x, flag, relres, it, resvec = O.pgmres(A, b, 200, tol, 2, Pm)
+    else:  # restarts short enough that the recycled space is used
+        x, flag, relres, it, resvec = O.pgmres_dr(A, b, 6, tol, 100, 3, R1=Pm)
+        assert it[1] >= 2
     Ad = O.dense_dda_matrix(p["r"], p["idx"], p["ko"], 1 / alpha, dV)
     xd = np.linalg.solve(Ad, b)
     assert flag == 0
@@ -291,3 +294,23 @@ def test_far_field_optical_theorem_identity():
     c_ot = 4 * np.pi / ko * np.imag(np.vdot(E0, F[0])) / np.sum(np.abs(E0) ** 2)
     c = O.cext_dda(P, Einc, ko, dV, E0)
     assert abs(c_ot - c) <= 1e-12 * abs(c)
+
+
+def test_pgmres_dr_deflation_beats_restarted_gmres():
+    """GCRO-DR (pgmresDR.m) on a matrix with a cluster of small eigenvalues:
+    the recycled harmonic Ritz space removes them from later cycles, so it
+    needs far fewer Arnoldi steps than plain restarted GMRES (pgmres.m) of the
+    same restart length; both reach the tolerance."""
+    rng = np.random.default_rng(2)
+    n = 300
+    ev = np.concatenate([np.linspace(0.01, 0.1, 8), 1 + rng.random(n - 8)]) * np.exp(1j * rng.random(n) * 0.3)
+    X = np.eye(n) + 0.1 * rng.normal(size=(n, n)) / np.sqrt(n)
+    A = X @ np.diag(ev) @ np.linalg.inv(X)
+    b = rng.normal(size=n) + 1j * rng.normal(size=n)
+    x1, f1, r1, it1, rv1 = O.pgmres_dr(A, b, 20, 1e-10, 100, 10)
+    x2, f2, r2, it2, rv2 = O.pgmres(A, b, 20, 1e-10, 100)
+    assert f1 == 0 and f2 == 0
+    assert np.linalg.norm(A @ x1 - b) <= 1e-10 * np.linalg.norm(b)
+    assert len(rv1) < 0.5 * len(rv2)
+    # resvec: one entry per Arnoldi step after the initial 1
+    assert rv1[0] == 1.0 and len(rv1) == 1 + 20 * (it1[1]) + it1[0]

@@ -54,14 +54,15 @@ SIGNATURES = {
     "vs_prec_get_blocks": (C.c_int, [_vp, C.c_int, _pd]),
 }
 VS_BUILD_C64, VS_BUILD_C128 = 1, 2
-VS_BICGSTAB, VS_GMRES = 0, 1
+VS_BICGSTAB, VS_GMRES, VS_GMRES_DR = 0, 1, 2
 VS_SOLVE_MIXED, VS_SOLVE_FP64 = 0, 1
 
 
 class vs_solve_opts(C.Structure):
     _fields_ = [("method", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("maxit", C.c_int),
                 ("inner_tol", C.c_double), ("max_refine", C.c_int), ("iters_per_graph", C.c_int),
-                ("resvec", _pd), ("resvec_cap", _i64), ("transpose", C.c_int), ("restart", C.c_int)]
+                ("resvec", _pd), ("resvec_cap", _i64), ("transpose", C.c_int), ("restart", C.c_int),
+                ("ritz", C.c_int)]
 
 
 class vs_solve_info(C.Structure):

@@ -367,8 +367,17 @@ def mvp_circ_2_level(inv_blocks, JIn, Lx, My, Nz, idx, precision="c128", ctx=Non
         pr.close()
 
 
+_METHODS = {"bicgstab": L.VS_BICGSTAB, "gmres": L.VS_GMRES, "gmres_dr": L.VS_GMRES_DR}
+
+
+def _method(name):
+    if name not in _METHODS:
+        raise ValueError(f"unknown method {name!r}; expected one of {sorted(_METHODS)}")
+    return _METHODS[name]
+
+
 def solve(op, b, prec=None, tol=1e-6, maxit=2000, precision="mixed", x0=None, inner_tol=0.0, max_refine=10,
-          iters_per_graph=4, want_resvec=True, transpose=False, method="bicgstab", restart=50):
+          iters_per_graph=4, want_resvec=True, transpose=False, method="bicgstab", restart=50, ritz=10):
     """Device Krylov solve; returns (x, info dict, resvec)."""
     lib = op.ctx._lib
     b = np.ascontiguousarray(np.asarray(b, dtype=np.complex128).ravel())
@@ -379,8 +388,9 @@ def solve(op, b, prec=None, tol=1e-6, maxit=2000, precision="mixed", x0=None, in
     o.tol = float(tol); o.maxit = int(maxit); o.inner_tol = float(inner_tol); o.max_refine = int(max_refine)
     o.iters_per_graph = int(iters_per_graph)
     o.transpose = 1 if transpose else 0
-    o.method = L.VS_GMRES if method == "gmres" else L.VS_BICGSTAB
+    o.method = _method(method)
     o.restart = int(restart)
+    o.ritz = int(ritz)
     rv = np.zeros(4 * int(maxit) + 64 if want_resvec else 1)
     if want_resvec:
         o.resvec = L.dptr(rv); o.resvec_cap = rv.size
@@ -393,7 +403,7 @@ def solve(op, b, prec=None, tol=1e-6, maxit=2000, precision="mixed", x0=None, in
 
 
 def solve_device(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="mixed", inner_tol=0.0,
-                 max_refine=10, iters_per_graph=4, method="bicgstab", restart=50):
+                 max_refine=10, iters_per_graph=4, method="bicgstab", restart=50, ritz=10):
     """vs_solve_device on device buffers (double2, n3 each); returns the info dict."""
     lib = op.ctx._lib
     o = L.vs_solve_opts()
@@ -401,8 +411,9 @@ def solve_device(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="m
     o.precision = L.VS_SOLVE_MIXED if precision == "mixed" else L.VS_SOLVE_FP64
     o.tol = float(tol); o.maxit = int(maxit); o.inner_tol = float(inner_tol); o.max_refine = int(max_refine)
     o.iters_per_graph = int(iters_per_graph)
-    o.method = L.VS_GMRES if method == "gmres" else L.VS_BICGSTAB
+    o.method = _method(method)
     o.restart = int(restart)
+    o.ritz = int(ritz)
     info = L.vs_solve_info()
     L.check(lib.vs_solve_device(op.h, prec.h if prec is not None else None, C.c_void_p(b_ptr), C.c_void_p(x_ptr),
                                 C.byref(o), C.byref(info)), op.ctx.h)
@@ -411,15 +422,16 @@ def solve_device(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="m
 
 
 def solve_host_ptr(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="mixed", iters_per_graph=4,
-                   method="bicgstab", restart=50):
+                   method="bicgstab", restart=50, ritz=10):
     """vs_solve on host buffers given as raw pointers (e.g. pinned torch tensors)."""
     lib = op.ctx._lib
     o = L.vs_solve_opts()
     lib.vs_solve_opts_default(C.byref(o))
     o.precision = L.VS_SOLVE_MIXED if precision == "mixed" else L.VS_SOLVE_FP64
     o.tol = float(tol); o.maxit = int(maxit); o.iters_per_graph = int(iters_per_graph)
-    o.method = L.VS_GMRES if method == "gmres" else L.VS_BICGSTAB
+    o.method = _method(method)
     o.restart = int(restart)
+    o.ritz = int(ritz)
     info = L.vs_solve_info()
     L.check(lib.vs_solve(op.h, prec.h if prec is not None else None, C.cast(C.c_void_p(b_ptr), L._pd),
                          C.cast(C.c_void_p(x_ptr), L._pd), C.byref(o), C.byref(info)), op.ctx.h)
@@ -446,6 +458,30 @@ def gmres(A, b, restart=None, tol=1e-6, maxit=None, M1=None, M2=None, x0=None, p
     inner = steps - (outer - 1) * restart
     nb = np.linalg.norm(np.asarray(b))
     return x, info["flag"], info["relres"], [outer, inner], rv * nb
+
+
+def pgmresDR(A, b, restart=50, tol=1e-3, maxit=10, ritz=None, L1=None, L2=None, R1=None, R2=None, x0=None,
+             precision="mixed"):
+    """[x, flag, relres, iter, resvec] = pgmresDR(A, b, restart, tol, maxit, ritz, L1, L2, R1, R2, x0)
+    (src/src_numeric/src_iterative/pgmresDR.m:73) with A an Operator and R1 a
+    Preconditioner (right preconditioning, as JVIE_Solver_const_GPU.m:400-427
+    passes it).  GCRO-DR on the device: every cycle of ``restart`` Arnoldi
+    steps recycles the ``ritz`` harmonic Ritz vectors of smallest magnitude;
+    ``maxit`` counts the cycles after the first, as pgmresDR.m does.  iter =
+    [steps of the last cycle, cycles after the first]; resvec holds the
+    Arnoldi residual estimates relative to ||b||; relres is the true FP64
+    relative residual.  Left preconditioners and a second right factor are
+    not supported."""
+    if L1 is not None or L2 is not None or R2 is not None:
+        raise NotImplementedError("pgmresDR here takes the preconditioner as R1 only")
+    ritz = min(10, int(round(restart / 2))) if ritz is None else min(int(ritz), int(restart) - 1)
+    total = int(restart) * (int(maxit) + 1)
+    x, info, rv = solve(A, b, prec=R1, tol=tol, maxit=total, precision=precision, x0=x0, method="gmres_dr",
+                        restart=int(restart), ritz=ritz)
+    steps = int(info["iter"])
+    cycles = max(1, -(-steps // int(restart)))
+    last = steps - (cycles - 1) * int(restart)
+    return x, info["flag"], info["relres"], [last, cycles - 1], rv
 
 
 def bicgstab(A, b, tol=1e-6, maxit=20, M1=None, M2=None, x0=None, precision="mixed"):
@@ -561,7 +597,7 @@ def cext_grad(op, prec, Einc, eps, ko, d, kvec, Eo, tol=1e-6, maxit=2000, precis
 
 
 def solve_batch(op, B, prec=None, tol=1e-6, maxit=2000, precision="mixed", method="bicgstab", restart=50,
-                iters_per_graph=4):
+                iters_per_graph=4, ritz=10):
     """Solve A x_r = b_r for every row b_r of B (nrhs x n3) as one batch; returns
     (X, list of info dicts)."""
     lib = op.ctx._lib
@@ -569,8 +605,9 @@ def solve_batch(op, B, prec=None, tol=1e-6, maxit=2000, precision="mixed", metho
     nrhs = B.shape[0]
     X = np.zeros_like(B)
     o = _solve_opts(lib, tol, maxit, precision)
-    o.method = L.VS_GMRES if method == "gmres" else L.VS_BICGSTAB
+    o.method = _method(method)
     o.restart = int(restart)
+    o.ritz = int(ritz)
     o.iters_per_graph = int(iters_per_graph)
     infos = (L.vs_solve_info * nrhs)()
     L.check(lib.vs_solve_batch(op.h, prec.h if prec is not None else None, L.dptr(B), L.dptr(X), nrhs, C.byref(o),

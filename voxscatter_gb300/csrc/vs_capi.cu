@@ -233,8 +233,12 @@ void time_passes(cudaStream_t st, int nrep, float* ms_out, F&& launch) {
 
 vs::SolveParams solve_params(vs_op* op, vs_prec* prec, const vs_solve_opts* o) {
   VS_REQUIRE(o, "NULL argument");
-  VS_REQUIRE(o->method == VS_BICGSTAB || o->method == VS_GMRES, "unsupported method");
+  VS_REQUIRE(o->method == VS_BICGSTAB || o->method == VS_GMRES || o->method == VS_GMRES_DR, "unsupported method");
   VS_REQUIRE(o->method != VS_GMRES || (o->restart >= 1 && o->restart <= 2048), "GMRES restart must be in [1, 2048]");
+  VS_REQUIRE(o->method != VS_GMRES_DR || (o->restart >= 2 && o->restart <= 256),
+             "GMRES-DR restart must be in [2, 256]");
+  VS_REQUIRE(o->method != VS_GMRES_DR || (o->ritz >= 1 && o->ritz < o->restart),
+             "GMRES-DR ritz must be in [1, restart - 1]");
   VS_REQUIRE(o->precision == VS_SOLVE_MIXED || o->precision == VS_SOLVE_FP64, "bad precision");
   VS_REQUIRE(o->tol > 0 && o->maxit >= 0 && o->iters_per_graph >= 1 && o->iters_per_graph <= 64, "bad options");
   VS_REQUIRE(!prec || (prec->L == op->L && prec->M == op->M && prec->N == op->N && prec->n3 == op->n3),
@@ -253,6 +257,7 @@ vs::SolveParams solve_params(vs_op* op, vs_prec* prec, const vs_solve_opts* o) {
   prm.resvec_host = o->resvec;
   prm.op_mode = o->transpose ? VS_TRANSP : VS_NOTRANSP;
   prm.restart = o->restart;
+  prm.ritz = o->ritz;
   return prm;
 }
 
@@ -271,6 +276,7 @@ void solve_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, const vs
   vs::SolveParams prm = solve_params(op, prec, o);
   vs::SolveResult r;
   if (o->method == VS_GMRES) vs::solve_gmres(*op, prec, b, x, prm, r, op->ctx->stream);
+  else if (o->method == VS_GMRES_DR) vs::solve_gmres_dr(*op, prec, b, x, prm, r, op->ctx->stream);
   else vs::solve_bicgstab(*op, prec, b, x, prm, r, op->ctx->stream);
   check_prec_status(prec);
   fill_info(r, info);
@@ -284,12 +290,13 @@ void solve_batch_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, in
   VS_REQUIRE(nrhs >= 1 && nrhs <= 4096, "nrhs must be in [1, 4096]");
   vs::SolveParams prm = solve_params(op, prec, o);
   const int64_t n = op->n3;
-  if (o->method == VS_GMRES) {
+  if (o->method == VS_GMRES || o->method == VS_GMRES_DR) {
     for (int64_t r = 0; r < nrhs; ++r) {
       vs::SolveParams p1 = prm;
       p1.resvec_host = prm.resvec_host ? prm.resvec_host + r * prm.resvec_cap : nullptr;
       vs::SolveResult res;
-      vs::solve_gmres(*op, prec, b + r * n, x + r * n, p1, res, op->ctx->stream);
+      if (o->method == VS_GMRES) vs::solve_gmres(*op, prec, b + r * n, x + r * n, p1, res, op->ctx->stream);
+      else vs::solve_gmres_dr(*op, prec, b + r * n, x + r * n, p1, res, op->ctx->stream);
       fill_info(res, infos + r);
     }
     check_prec_status(prec);
@@ -854,6 +861,7 @@ void vs_solve_opts_default(vs_solve_opts* o) {
   o->resvec_cap = 0;
   o->transpose = 0;
   o->restart = 50;
+  o->ritz = 10;
 }
 
 

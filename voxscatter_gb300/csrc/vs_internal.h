@@ -81,6 +81,10 @@ struct KrylovWork {
   // right-hand side g, solution y, pass coefficients, partial dots, state,
   // and the vectors w, tmp and the correction d.
   DevBuf gV, gH, gcs, gsn, gg, gy, ghp, gpart, gstate, gw, gtmp, gd;
+  // GCRO-DR: recycled spaces U, C (and the next ones), the solution in the
+  // preconditioned space, the residual, the unrotated Hessenberg, C^H A V,
+  // partial and final Gram products, combination coefficients.
+  DevBuf rU, rC, rU2, rC2, rz, rr, rHraw, rB, rgpart, rgram, rcoef;
   template <typename T> void ensure(int64_t n);
 };
 

@@ -16,6 +16,7 @@
 // (Ogita-Rump-Oishi Dot2) FP64 norms, solves A d = r/||r|| in c64 and updates
 // x += ||r|| d in FP64 until ||r||/||b|| <= tol.
 #include "vs_krylov.h"
+#include "vs_dense.h"
 
 #include <chrono>
 #include <cmath>
@@ -1153,14 +1154,415 @@ static void gmres_buffers(KrylovWork& w, int64_t n, int m) {
   w.gstate.alloc(sizeof(GState));
 }
 
+// ===========================================================================
+// GCRO-DR, MATLAB-style pgmresDR(A, b, restart, tol, maxit, ritz, [], [], M)
+// (src/src_numeric/src_iterative/pgmresDR.m:73-281, pgmresDR_iter.m:1-142,
+// getHarmVecs1.m, getHarmVecs2.m; Parks, de Sturler, Mackey, Johnson and
+// Maiti, SIAM J. Sci. Comput. 28 (2006) 1651-1674), right preconditioned as
+// the JVIE solvers call it (JVIE_Solver_const_GPU.m:400-427).  Each cycle runs
+// up to `restart` Arnoldi steps on (I - C C^H) A M; after it the `ritz`
+// harmonic Ritz vectors of smallest magnitude span the recycled space U with
+// C = A M U orthonormal, which the next cycle deflates.  The Arnoldi steps
+// and their residual estimate reuse the GMRES kernels above (Gram-Schmidt
+// against C, then against V, each applied twice); the unrotated Hessenberg
+// is kept for the harmonic Ritz problems.  Between cycles the host solves the
+// small least-squares, QR and eigen problems (vs_dense.cu) from Gram products
+// formed on the device, and tall-skinny combinations on the device form the
+// solution update, the new residual and the next U and C.
+// ===========================================================================
+
+// Partial dots X_i^H Y_j over one chunk of kDotChunk entries, X = [Xa (na
+// vectors) | Xb], Y (ny vectors), all of stride n; grid (nchunk, nx, ny).
 template <typename T>
+__global__ void __launch_bounds__(256) k_dr_gram(const cplx_t<T>* __restrict__ Xa, int na,
+                                                 const cplx_t<T>* __restrict__ Xb, const cplx_t<T>* __restrict__ Y,
+                                                 int64_t n, double2* __restrict__ part, int nchunk) {
+  const int i = blockIdx.y, j = blockIdx.z;
+  const cplx_t<T>* x = i < na ? Xa + (int64_t)i * n : Xb + (int64_t)(i - na) * n;
+  const cplx_t<T>* y = Y + (int64_t)j * n;
+  const int64_t i0 = (int64_t)blockIdx.x * kDotChunk;
+  const int64_t i1 = (n < i0 + kDotChunk) ? n : i0 + kDotChunk;
+  Acc<T> a;
+  for (int64_t e = i0 + threadIdx.x; e < i1; e += blockDim.x) a.dot(x[e], y[e]);
+  __shared__ double sre[8], sim[8];
+  double re = a.value().x, im = a.value().y;
+  for (int off = 16; off; off >>= 1) {
+    re += __shfl_xor_sync(0xffffffffu, re, off);
+    im += __shfl_xor_sync(0xffffffffu, im, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sre[threadIdx.x >> 5] = re;
+    sim[threadIdx.x >> 5] = im;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0, q = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      r += sre[k];
+      q += sim[k];
+    }
+    part[((int64_t)i * gridDim.z + j) * nchunk + blockIdx.x] = make_double2(r, q);
+  }
+}
+
+// G(i, j) (column-major, nx rows) = sum of the chunk partials of pair (i, j);
+// one CTA per pair, block b = i * ny + j.
+__global__ void k_dr_gram_final(const double2* __restrict__ part, int nchunk, int nx, int ny, double2* __restrict__ G) {
+  const int b = blockIdx.x, i = b / ny, j = b - i * ny;
+  double r = 0, q = 0;
+  for (int c = threadIdx.x; c < nchunk; c += blockDim.x) {
+    r += part[(int64_t)b * nchunk + c].x;
+    q += part[(int64_t)b * nchunk + c].y;
+  }
+  for (int off = 16; off; off >>= 1) {
+    r += __shfl_xor_sync(0xffffffffu, r, off);
+    q += __shfl_xor_sync(0xffffffffu, q, off);
+  }
+  __shared__ double sr[8], sq[8];
+  if ((threadIdx.x & 31) == 0) {
+    sr[threadIdx.x >> 5] = r;
+    sq[threadIdx.x >> 5] = q;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0, c2 = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      a += sr[k];
+      c2 += sq[k];
+    }
+    G[i + (int64_t)j * nx] = make_double2(a, c2);
+  }
+}
+
+// out_c = (accumulate ? out_c : 0) + sum_j X_j coef(j, c) for c < ncol, with
+// X = [Xa (na vectors) | Xb (nb vectors)] and coef column-major (na + nb rows);
+// blockIdx.y picks a tile of 4 output columns, so each X entry is read once
+// per tile.
+template <typename T>
+__global__ void __launch_bounds__(256) k_dr_combine(const cplx_t<T>* __restrict__ Xa, int na,
+                                                    const cplx_t<T>* __restrict__ Xb, int nb,
+                                                    const double2* __restrict__ coef, int ncol,
+                                                    cplx_t<T>* __restrict__ out, int64_t n, int accumulate) {
+  using C = cplx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* cs = reinterpret_cast<C*>(smem_raw);  // [na + nb][4]
+  const int nx = na + nb, c0 = blockIdx.y * 4;
+  for (int u = threadIdx.x; u < nx * 4; u += blockDim.x) {
+    const int j = u >> 2, t = u & 3;
+    cs[u] = (c0 + t < ncol) ? ccast<C>(coef[j + (int64_t)(c0 + t) * nx]) : czero<C>();
+  }
+  __syncthreads();
+  const int nt = min(4, ncol - c0);
+  GRID_LOOP(e, n) {
+    C acc[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) acc[t] = (accumulate && t < nt) ? out[(int64_t)(c0 + t) * n + e] : czero<C>();
+    for (int j = 0; j < nx; ++j) {
+      const C v = j < na ? Xa[(int64_t)j * n + e] : Xb[(int64_t)(j - na) * n + e];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) acc[t] = cfma(cs[j * 4 + t], v, acc[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+      if (t < nt) out[(int64_t)(c0 + t) * n + e] = acc[t];
+  }
+}
+
+// Column k of the unrotated Hessenberg (len entries) into the copy that the
+// Givens kernel rotates.
+__global__ void k_dr_copycol(const GState* st, const double2* __restrict__ src, double2* __restrict__ dst, int len) {
+  if (st->skip) return;
+  for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = src[i];
+}
+
+using dense::cd;
+
+// G = [Xa | Xb]^H Y on the host ((na + nb) x ny, column-major).
+template <typename T>
+static std::vector<cd> dr_gram(KrylovWork& w, const cplx_t<T>* Xa, int na, const cplx_t<T>* Xb, int nb,
+                               const cplx_t<T>* Y, int ny, int64_t n, cudaStream_t st, int64_t* launches) {
+  const int nx = na + nb;
+  std::vector<cd> G((size_t)nx * ny, 0);
+  if (nx == 0 || ny == 0) return G;
+  const int nchunk = ceil_div(n, kDotChunk);
+  w.rgpart.alloc((size_t)nx * ny * nchunk * sizeof(double2));
+  w.rgram.alloc((size_t)nx * ny * sizeof(double2));
+  k_dr_gram<T><<<dim3(nchunk, nx, ny), 256, 0, st>>>(Xa, na, nb ? Xb : Xa, Y, n, w.rgpart.as<double2>(), nchunk);
+  k_dr_gram_final<<<nx * ny, 256, 0, st>>>(w.rgpart.as<double2>(), nchunk, nx, ny, w.rgram.as<double2>());
+  VS_LAUNCH_CHECK();
+  *launches += 2;
+  std::vector<double2> h((size_t)nx * ny);
+  VS_CUDA(cudaMemcpyAsync(h.data(), w.rgram.p, h.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
+  VS_CUDA(cudaStreamSynchronize(st));
+  for (size_t i = 0; i < h.size(); ++i) G[i] = cd(h[i].x, h[i].y);
+  return G;
+}
+
+// out (ncol vectors) (+)= [Xa | Xb] coef, coef (na + nb) x ncol column-major.
+template <typename T>
+static void dr_combine(KrylovWork& w, const cplx_t<T>* Xa, int na, const cplx_t<T>* Xb, int nb,
+                       const std::vector<cd>& coef, int ncol, cplx_t<T>* out, int64_t n, bool accumulate,
+                       cudaStream_t st, int64_t* launches) {
+  const int nx = na + nb;
+  if (nx == 0 || ncol == 0) return;
+  std::vector<double2> h((size_t)nx * ncol);
+  for (size_t i = 0; i < h.size(); ++i) h[i] = make_double2(coef[i].real(), coef[i].imag());
+  // stream-ordered: wait for the previous combine before its coefficients are overwritten
+  VS_CUDA(cudaStreamSynchronize(st));
+  w.rcoef.alloc(h.size() * sizeof(double2));
+  VS_CUDA(cudaMemcpy(w.rcoef.p, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  const size_t smem = (size_t)nx * 4 * sizeof(cplx_t<T>);
+  k_dr_combine<T><<<dim3(vec_grid(n), ceil_div(ncol, 4)), 256, smem, st>>>(
+      Xa, na, nb ? Xb : Xa, nb, w.rcoef.as<double2>(), ncol, out, n, accumulate ? 1 : 0);
+  VS_LAUNCH_CHECK();
+  *launches += 1;
+}
+
+template <typename T>
+static void gcrodr_buffers(KrylovWork& w, int64_t n, int m, int kr) {
+  using C = cplx_t<T>;
+  const size_t kv = (size_t)std::max(kr, 1) * n * sizeof(C);
+  w.rU.alloc(kv);
+  w.rC.alloc(kv);
+  w.rU2.alloc(kv);
+  w.rC2.alloc(kv);
+  w.rz.alloc(n * sizeof(C));
+  w.rr.alloc(n * sizeof(C));
+  w.rHraw.alloc((size_t)(m + 1) * m * sizeof(double2));
+  w.rB.alloc((size_t)std::max(kr, 1) * m * sizeof(double2));
+}
+
+// Inner GCRO-DR on A d = rin (precision T, d overwritten), right
+// preconditioned: A M z = rin, d = M z.  Convergence: the Arnoldi residual
+// estimate <= itol * ||rin||.  Returns the Arnoldi steps taken; *flag 0
+// converged, 1 not, 4 breakdown, 5 non-finite.
+template <typename T>
+static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t n, const cplx_t<T>* rin,
+                       cplx_t<T>* d, double itol, int m, int kr, int maxit, int op_mode, double res_scale,
+                       double* resvec_dev, int resvec_cap, int64_t* nres_out, int* flag, cudaStream_t st,
+                       int64_t* launches) {
+  using C = cplx_t<T>;
+  const int g = vec_grid(n);
+  const int nchunk = ceil_div(n, kDotChunk);
+  C* V = w.gV.as<C>();
+  C* wv = w.gw.as<C>();
+  C* tmp = w.gtmp.as<C>();
+  C* U = w.rU.as<C>();
+  C* Cm = w.rC.as<C>();
+  C* U2 = w.rU2.as<C>();
+  C* C2 = w.rC2.as<C>();
+  C* z = w.rz.as<C>();
+  C* r = w.rr.as<C>();
+  double2* H = w.gH.as<double2>();
+  double2* Hraw = w.rHraw.as<double2>();
+  double2* Bd = w.rB.as<double2>();
+  double2* hp = w.ghp.as<double2>();
+  double2* part = w.gpart.as<double2>();
+  GState* gs = w.gstate.as<GState>();
+  KState* ks = w.state.as<KState>();
+  auto rprec = [&](const C* in, C* out, const int* skip) {
+    if (pr) prec_apply<T>(*pr, in, out, 1, skip, st);
+    else k_copy<T><<<g, 256, 0, st>>>(out, in, n);
+    *launches += pr ? prec_launches<T>(*pr) : 1;
+  };
+  auto norm_dev = [&](const C* u) {
+    k_norm<T><<<g, kRedThreads, 0, st>>>(u, n, ks, w.scal.as<double>());
+    double v = 0;
+    VS_CUDA(cudaMemcpyAsync(&v, w.scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+    *launches += 1;
+    return v;
+  };
+  k_copy<T><<<g, 256, 0, st>>>(r, rin, n);
+  VS_CUDA(cudaMemsetAsync(z, 0, n * sizeof(C), st));
+  *launches += 1;
+  const double bn = norm_dev(r);
+  const double tol_abs = itol * bn;
+  if (resvec_dev && resvec_cap > 0) {
+    const double v0 = bn * res_scale;
+    VS_CUDA(cudaMemcpyAsync(resvec_dev, &v0, sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  int64_t nres = 1;
+  *flag = 1;
+  int steps = 0, kc = 0;
+  for (;;) {
+    const double beta = norm_dev(r);
+    if (!std::isfinite(beta)) {
+      *flag = 5;
+      break;
+    }
+    if (!(beta > tol_abs)) {
+      *flag = 0;
+      break;
+    }
+    if (steps >= maxit) break;
+    k_scale_by<T><<<g, 256, 0, st>>>(r, V, n, w.scal.as<double>());
+    VS_CUDA(cudaMemsetAsync(H, 0, (size_t)(m + 1) * m * sizeof(double2), st));
+    VS_CUDA(cudaMemsetAsync(Hraw, 0, (size_t)(m + 1) * m * sizeof(double2), st));
+    if (kc) VS_CUDA(cudaMemsetAsync(Bd, 0, (size_t)kc * m * sizeof(double2), st));
+    VS_CUDA(cudaMemsetAsync(w.gg.p, 0, (m + 1) * sizeof(double2), st));
+    const double2 g0 = make_double2(beta, 0);
+    VS_CUDA(cudaMemcpyAsync(w.gg.p, &g0, sizeof(double2), cudaMemcpyHostToDevice, st));
+    GState h{};
+    h.m = m;
+    h.resvec = resvec_dev;
+    h.resvec_cap = resvec_cap;
+    h.res_scale = res_scale;
+    h.tol_abs = tol_abs;
+    h.k = 0;
+    h.skip = 0;
+    h.flag = 1;
+    h.res = beta;
+    h.nres = (int)nres;
+    VS_CUDA(cudaMemcpyAsync(gs, &h, sizeof(GState), cudaMemcpyHostToDevice, st));
+    *launches += 1;
+    const int kmax = std::min(m, maxit - steps);
+    GState cur{};
+    for (int k = 0; k < kmax; ++k) {
+      rprec(V + (int64_t)k * n, tmp, &gs->skip);
+      matvec<T>(op, tmp, wv, 1, op_mode, &gs->skip, st);
+      *launches += 5;
+      if (kc) {
+        double2* Bcol = Bd + (int64_t)k * kc;
+        for (int pass = 0; pass < 2; ++pass) {
+          k_gm_dots<T><<<dim3(nchunk, kc), 256, 0, st>>>(Cm, wv, n, part, nchunk, gs);
+          k_gm_dots_final<<<kc, 256, 0, st>>>(part, nchunk, hp, Bcol, gs);
+          k_gm_axpy<T><<<g, 256, kc * sizeof(C), st>>>(Cm, wv, n, kc, hp, gs);
+        }
+        *launches += 6;
+      }
+      double2* Hcol = Hraw + (int64_t)k * (m + 1);
+      for (int pass = 0; pass < 2; ++pass) {
+        k_gm_dots<T><<<dim3(nchunk, k + 1), 256, 0, st>>>(V, wv, n, part, nchunk, gs);
+        k_gm_dots_final<<<k + 1, 256, 0, st>>>(part, nchunk, hp, Hcol, gs);
+        k_gm_axpy<T><<<g, 256, (k + 1) * sizeof(C), st>>>(V, wv, n, k + 1, hp, gs);
+      }
+      k_gm_norm<T><<<g, kRedThreads, 0, st>>>(wv, n, w.partials.as<double>(), &ks->counter, Hcol + k + 1, gs);
+      k_gm_scale<T><<<g, 256, 0, st>>>(wv, V + (int64_t)(k + 1) * n, n, Hcol + k + 1, gs);
+      k_dr_copycol<<<1, 64, 0, st>>>(gs, Hcol, H + (int64_t)k * (m + 1), k + 2);
+      k_gm_givens<<<1, 32, 0, st>>>(gs, H, w.gcs.as<double>(), w.gsn.as<double2>(), w.gg.as<double2>());
+      VS_LAUNCH_CHECK();
+      *launches += 10;
+      if ((k + 1) % 4 == 0 || k == kmax - 1) {
+        VS_CUDA(cudaMemcpyAsync(&cur, gs, sizeof(GState), cudaMemcpyDeviceToHost, st));
+        VS_CUDA(cudaStreamSynchronize(st));
+        if (cur.skip) break;
+      }
+    }
+    VS_CUDA(cudaMemcpyAsync(&cur, gs, sizeof(GState), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+    const int kd = cur.k;
+    steps += kd;
+    nres = cur.nres;
+    if (cur.flag == 5) {
+      *flag = 5;
+      break;
+    }
+    if (kd == 0) {
+      *flag = 4;
+      break;
+    }
+    const bool conv = cur.flag == 0;
+    const bool more = !conv && steps < maxit;
+    // the unrotated Hessenberg ((kd+1) x kd) and B = C^H A M V (kc x kd) on the host
+    std::vector<double2> hh((size_t)(m + 1) * kd), bh((size_t)kc * kd);
+    VS_CUDA(cudaMemcpyAsync(hh.data(), Hraw, hh.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    if (kc) VS_CUDA(cudaMemcpyAsync(bh.data(), Bd, bh.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+    std::vector<cd> Hh((size_t)(kd + 1) * kd);
+    for (int j = 0; j < kd; ++j)
+      for (int i = 0; i <= kd; ++i) Hh[i + (size_t)j * (kd + 1)] = cd(hh[i + (size_t)j * (m + 1)].x, hh[i + (size_t)j * (m + 1)].y);
+    if (kc == 0) {
+      // first cycle (pgmresDR.m:190-221)
+      std::vector<cd> rhs(kd + 1, 0);
+      rhs[0] = beta;
+      const std::vector<cd> y = dense::lstsq(Hh, kd + 1, kd, rhs);
+      dr_combine<T>(w, V, kd, nullptr, 0, y, 1, z, n, true, st, launches);
+      std::vector<cd> t(kd + 1, 0);
+      for (int j = 0; j < kd; ++j)
+        for (int i = 0; i <= kd; ++i) t[i] -= Hh[i + (size_t)j * (kd + 1)] * y[j];
+      dr_combine<T>(w, V, kd + 1, nullptr, 0, t, 1, r, n, true, st, launches);
+      const int kk = std::min(kr, kd - 1);
+      if (more && kk >= 1) {
+        const dense::Mat P = dense::harm_vecs1(kd, kk, Hh);
+        dense::Mat HP((size_t)(kd + 1) * kk, 0), Q, R;
+        for (int c = 0; c < kk; ++c)
+          for (int j = 0; j < kd; ++j)
+            for (int i = 0; i <= kd; ++i) HP[i + (size_t)c * (kd + 1)] += Hh[i + (size_t)j * (kd + 1)] * P[j + (size_t)c * kd];
+        dense::qr_econ(HP, kd + 1, kk, Q, R);
+        const dense::Mat cu = dense::right_div_upper(P, kd, kk, R);
+        dr_combine<T>(w, V, kd, nullptr, 0, cu, kk, U2, n, false, st, launches);
+        dr_combine<T>(w, V, kd + 1, nullptr, 0, Q, kk, C2, n, false, st, launches);
+        std::swap(U, U2);
+        std::swap(Cm, C2);
+        kc = kk;
+      }
+    } else {
+      // later cycles (pgmresDR.m:236-258): U scaled to unit columns by D
+      const int mm = kc + kd;
+      const std::vector<cd> G = dr_gram<T>(w, Cm, kc, V, kd + 1, U, kc, n, st, launches);     // [C V]^H U
+      const std::vector<cd> Gr = dr_gram<T>(w, Cm, kc, V, kd + 1, r, 1, n, st, launches);     // [C V]^H r
+      const std::vector<cd> UU = dr_gram<T>(w, U, kc, nullptr, 0, U, kc, n, st, launches);    // U^H U
+      std::vector<double> Dv(kc);
+      for (int i = 0; i < kc; ++i) Dv[i] = 1.0 / std::sqrt(UU[i + (size_t)i * kc].real());
+      dense::Mat H2((size_t)(mm + 1) * mm, 0);
+      for (int i = 0; i < kc; ++i) H2[i + (size_t)i * (mm + 1)] = Dv[i];
+      for (int j = 0; j < kd; ++j) {
+        for (int i = 0; i < kc; ++i) H2[i + (size_t)(kc + j) * (mm + 1)] = cd(bh[i + (size_t)j * kc].x, bh[i + (size_t)j * kc].y);
+        for (int i = 0; i <= kd; ++i) H2[kc + i + (size_t)(kc + j) * (mm + 1)] = Hh[i + (size_t)j * (kd + 1)];
+      }
+      const std::vector<cd> y = dense::lstsq(H2, mm + 1, mm, Gr);
+      std::vector<cd> cx(y);
+      for (int i = 0; i < kc; ++i) cx[i] *= Dv[i];
+      dr_combine<T>(w, U, kc, V, kd, cx, 1, z, n, true, st, launches);
+      std::vector<cd> t(mm + 1, 0);
+      for (int j = 0; j < mm; ++j)
+        for (int i = 0; i <= mm; ++i) t[i] -= H2[i + (size_t)j * (mm + 1)] * y[j];
+      dr_combine<T>(w, Cm, kc, V, kd + 1, t, 1, r, n, true, st, launches);
+      if (more) {
+        dense::Mat Wm((size_t)(mm + 1) * mm, 0);
+        for (int j = 0; j < kc; ++j)
+          for (int i = 0; i <= mm; ++i) Wm[i + (size_t)j * (mm + 1)] = G[i + (size_t)j * (mm + 1)] * Dv[j];
+        for (int j = kc; j < mm; ++j) Wm[j + (size_t)j * (mm + 1)] = 1;
+        const dense::Mat P = dense::harm_vecs2(mm, kc, H2, Wm);
+        dense::Mat HP((size_t)(mm + 1) * kc, 0), Q, R;
+        for (int c = 0; c < kc; ++c)
+          for (int j = 0; j < mm; ++j)
+            for (int i = 0; i <= mm; ++i) HP[i + (size_t)c * (mm + 1)] += H2[i + (size_t)j * (mm + 1)] * P[j + (size_t)c * mm];
+        dense::qr_econ(HP, mm + 1, kc, Q, R);
+        dense::Mat cu = dense::right_div_upper(P, mm, kc, R);
+        for (int c = 0; c < kc; ++c)
+          for (int i = 0; i < kc; ++i) cu[i + (size_t)c * mm] *= Dv[i];
+        dr_combine<T>(w, U, kc, V, kd, cu, kc, U2, n, false, st, launches);
+        dr_combine<T>(w, Cm, kc, V, kd + 1, Q, kc, C2, n, false, st, launches);
+        std::swap(U, U2);
+        std::swap(Cm, C2);
+      }
+    }
+    if (conv) {
+      *flag = 0;
+      break;
+    }
+    if (steps >= maxit) break;
+  }
+  rprec(z, d, nullptr);
+  VS_LAUNCH_CHECK();
+  *nres_out = std::min<int64_t>(nres, resvec_cap);
+  return steps;
+}
+
+// FP64 iterative refinement around the inner GMRES(m) (DR false) or GCRO-DR
+// (DR true) solve in precision T.
+template <typename T, bool DR = false>
 static void gmres_refine(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm,
                          SolveResult& out, cudaStream_t st, double bnorm, int64_t& launches, double* rv, int cap) {
   using C = cplx_t<T>;
   KrylovWork& w = op.kw;
   const int64_t n = op.n3;
   const int m = std::max(1, std::min(prm.restart, prm.maxit));
+  const int kr = std::max(0, std::min(prm.ritz, m - 1));
   gmres_buffers<T>(w, n, m);
+  if (DR) gcrodr_buffers<T>(w, n, m, kr);
   w.y64.alloc(n * sizeof(double2));
   w.r64.alloc(n * sizeof(double2));
   double2* r64 = w.r64.as<double2>();
@@ -1192,8 +1594,12 @@ static void gmres_refine(vs_op& op, vs_prec* pr, const double2* b, double2* x, c
     const int capk = rv ? (int)(cap - nres) : 0;
     int64_t nk = 0;
     int f = 1;
-    steps += gmres_core<T>(op, pr, w, n, w.r.as<C>(), w.gd.as<C>(), itol, m, prm.maxit - steps, prm.op_mode,
-                           rn / bnorm, rvk, capk, &nk, &f, st, &launches);
+    if (DR)
+      steps += gcrodr_core<T>(op, pr, w, n, w.r.as<C>(), w.gd.as<C>(), itol, m, kr, prm.maxit - steps, prm.op_mode,
+                              rn / bnorm, rvk, capk, &nk, &f, st, &launches);
+    else
+      steps += gmres_core<T>(op, pr, w, n, w.r.as<C>(), w.gd.as<C>(), itol, m, prm.maxit - steps, prm.op_mode,
+                             rn / bnorm, rvk, capk, &nk, &f, st, &launches);
     nres += nk;
     k_update64_from<<<vec_grid(n), 256, 0, st>>>(x, w.gd.as<C>(), n, rn);
     VS_LAUNCH_CHECK();
@@ -1212,8 +1618,9 @@ static void gmres_refine(vs_op& op, vs_prec* pr, const double2* b, double2* x, c
   out.n_resvec = nres;
 }
 
-void solve_gmres(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
-                 cudaStream_t st) {
+template <bool DR>
+static void solve_gmres_impl(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm,
+                             SolveResult& out, cudaStream_t st) {
   const int64_t n = op.n3;
   KrylovWork& w = op.kw;
   reduction_buffers(w, 1);
@@ -1233,12 +1640,22 @@ void solve_gmres(vs_op& op, vs_prec* pr, const double2* b, double2* x, const Sol
     out.flag = 0;
     return;
   }
-  if (prm.mode == VS_SOLVE_FP64) gmres_refine<double>(op, pr, b, x, prm, out, st, bnorm, launches, rv, cap);
-  else gmres_refine<float>(op, pr, b, x, prm, out, st, bnorm, launches, rv, cap);
+  if (prm.mode == VS_SOLVE_FP64) gmres_refine<double, DR>(op, pr, b, x, prm, out, st, bnorm, launches, rv, cap);
+  else gmres_refine<float, DR>(op, pr, b, x, prm, out, st, bnorm, launches, rv, cap);
   out.launches = launches;
   if (cap > 0 && prm.resvec_host && out.n_resvec > 0)
     VS_CUDA(cudaMemcpyAsync(prm.resvec_host, rv, out.n_resvec * sizeof(double), cudaMemcpyDeviceToHost, st));
   VS_CUDA(cudaStreamSynchronize(st));
+}
+
+void solve_gmres(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
+                 cudaStream_t st) {
+  solve_gmres_impl<false>(op, pr, b, x, prm, out, st);
+}
+
+void solve_gmres_dr(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
+                    cudaStream_t st) {
+  solve_gmres_impl<true>(op, pr, b, x, prm, out, st);
 }
 
 }  // namespace vs

@@ -41,6 +41,7 @@ struct SolveParams {
   double* resvec_host = nullptr;
   int op_mode = 0;  // VS_NOTRANSP: solve A x = b; VS_TRANSP: solve A^T x = b
   int restart = 50; // GMRES restart length
+  int ritz = 10;     // GCRO-DR: recycled harmonic Ritz vectors
 };
 
 struct SolveResult {
@@ -57,5 +58,7 @@ void solve_bicgstab_batch(vs_op& op, vs_prec* pr, const double2* b, double2* x, 
                           std::vector<SolveResult>& out, cudaStream_t st);
 void solve_gmres(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
                  cudaStream_t st);
+void solve_gmres_dr(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
+                    cudaStream_t st);
 
 }  // namespace vs
