@@ -273,6 +273,19 @@ int vs_solve_batch(vs_op* op, vs_prec* prec, const double* b, double* x, int64_t
 int vs_solve_batch_device(vs_op* op, vs_prec* prec, const void* b, void* x, int64_t nrhs, const vs_solve_opts* opts,
                           vs_solve_info* infos);
 
+/* Several particles at once (the reference solves its particles, incident
+ * directions and polarisations in a loop of bicgstab calls, main_DDA.m:61-82):
+ * nparticles operators, each with its own preconditioner (precs may be NULL,
+ * or hold NULL entries), right-hand sides b[i] and solutions x[i] (device,
+ * double2, nrhs[i] * n3 each, as vs_solve_batch_device).  Operators created on
+ * different contexts are solved concurrently, one host thread per context,
+ * each on its context's stream; operators that share a context run one after
+ * another.  infos holds sum(nrhs) entries, particle by particle.  Returns the
+ * first failing particle's status (its message in vs_last_error(NULL) and in
+ * its context); the other particles still run. */
+int vs_solve_particles_device(int64_t nparticles, vs_op* const* ops, vs_prec* const* precs, const void* const* b,
+                              void* const* x, const int64_t* nrhs, const vs_solve_opts* opts, vs_solve_info* infos);
+
 /* ---- excitation, extinction cross section, gradient ------------------- */
 
 /* Plane wave E0 .* exp(1i k.r) at op's unknowns: PlaneWavePointWise.m:7-19

@@ -57,3 +57,17 @@ def test_eps_layer_average_host(lib):
     f_o = O.eps_layer_average(eps)
     assert f.shape == (12,)
     assert np.abs(f - f_o).max() <= 1e-14 * np.abs(f_o).max()
+
+
+def test_particles_entry_rejects_bad_arguments_without_a_gpu(lib):
+    """vs_solve_particles_device checks its arguments before any CUDA call."""
+    import ctypes as C
+    from voxscatter_gb300 import _lib as L
+    o = L.vs_solve_opts()
+    lib.vs_solve_opts_default(C.byref(o))
+    info = (L.vs_solve_info * 1)()
+    nul = (C.c_void_p * 1)(None)
+    nr = (C.c_int64 * 1)(1)
+    assert lib.vs_solve_particles_device(0, nul, nul, nul, nul, nr, C.byref(o), info) == L.VS_ERR_ARG
+    assert lib.vs_solve_particles_device(1, nul, nul, nul, nul, nr, C.byref(o), info) == L.VS_ERR_ARG
+    assert b"NULL operator" in lib.vs_last_error(None)

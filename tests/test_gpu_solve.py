@@ -235,3 +235,39 @@ def test_config1_gmres_dr_mixed(api):
     x, info, rv = api.solve(op, b, pr, tol=1e-6, precision="mixed", method="gmres_dr", restart=20, ritz=5)
     assert info["flag"] == 0
     assert np.linalg.norm(b - Aor(x)) / np.linalg.norm(b) <= 1e-6 * 1.01
+
+
+def test_particles_solved_concurrently_match_batch_solves(api):
+    """vs_solve_particles_device: three plates of different sizes, two of them
+    on one context and one on another (so two host threads run at once), 4
+    rhs each; every particle's FP64 solutions and iteration counts equal those
+    of its own vs_solve_batch_device call."""
+    import torch
+    ctxs = [api.Context(0), api.Context(0)]
+    parts = []
+    for k, (diam, ctx) in enumerate(((2.5, ctxs[0]), (2.0, ctxs[1]), (3.0, ctxs[0]))):
+        p = W.small_hex(m=1.31 + 0.05j, diameter=diam, nper=4)
+        L, M, N, idx3, Toep, alpha, dV, b0, Aor = _system(p)
+        op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep, ctx=ctx)
+        pr = api.Preconditioner(op, shift=1 / alpha, d=dV, precisions=("c64", "c128"))
+        rng = np.random.default_rng(k)
+        B = np.array([b0 * np.exp(1j * rng.random()) + 0.1 * (rng.normal(size=b0.size) + 0j) for _ in range(4)])
+        parts.append((op, pr, torch.from_numpy(B).cuda(), Aor, B))
+    ref = []
+    for op, pr, Bd, _, B in parts:
+        X = torch.zeros_like(Bd)
+        torch.cuda.synchronize()
+        ref.append((X, api.solve_batch_device(op, Bd.data_ptr(), X.data_ptr(), len(B), pr, tol=1e-10,
+                                              precision="fp64")))
+    Xs = [torch.zeros_like(Bd) for (_, _, Bd, _, _) in parts]
+    torch.cuda.synchronize()
+    out = api.solve_particles_device([q[0] for q in parts], [q[1] for q in parts], [q[2].data_ptr() for q in parts],
+                                     [X.data_ptr() for X in Xs], [len(q[4]) for q in parts], tol=1e-10,
+                                     precision="fp64")
+    assert len(out) == 3
+    for (op, pr, Bd, Aor, B), X, (Xr, ir), inf in zip(parts, Xs, ref, out):
+        Xh = X.cpu().numpy()
+        for r in range(len(B)):
+            assert inf[r]["flag"] == 0 and inf[r]["iter"] == ir[r]["iter"]
+            assert np.linalg.norm(B[r] - Aor(Xh[r])) / np.linalg.norm(B[r]) <= 1e-10 * 1.01
+        assert np.linalg.norm(Xh - Xr.cpu().numpy()) <= 1e-12 * np.linalg.norm(Xh)

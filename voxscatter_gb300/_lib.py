@@ -89,6 +89,8 @@ SIGNATURES.update({
     "vs_solve_batch": (C.c_int, [_vp, _vp, _pd, _pd, _i64, C.POINTER(vs_solve_opts), C.POINTER(vs_solve_info)]),
     "vs_solve_batch_device": (C.c_int, [_vp, _vp, _vp, _vp, _i64, C.POINTER(vs_solve_opts),
                                         C.POINTER(vs_solve_info)]),
+    "vs_solve_particles_device": (C.c_int, [_i64, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp),
+                                            C.POINTER(_i64), C.POINTER(vs_solve_opts), C.POINTER(vs_solve_info)]),
     "vs_plane_wave": (C.c_int, [_vp, _pd, _pd, _pd, _pd, _pd, _pd]),
     "vs_cext": (C.c_int, [_vp, _pd, _pd, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double)]),
     "vs_op_apply_domain": (C.c_int, [_vp, _pd, _pd, C.c_int64, _pd, _pd, C.c_int]),

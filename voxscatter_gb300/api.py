@@ -616,6 +616,33 @@ def solve_batch(op, B, prec=None, tol=1e-6, maxit=2000, precision="mixed", metho
                     launches=i.kernel_launches) for i in infos]
 
 
+def solve_particles_device(ops, precs, b_ptrs, x_ptrs, nrhs, tol=1e-6, maxit=2000, precision="mixed",
+                           iters_per_graph=4):
+    """vs_solve_particles_device: several particles' batched solves at once
+    (device buffers, double2, nrhs[i]*n3 each).  Particles whose operators
+    live on different Contexts run concurrently, one host thread per context;
+    returns one list of info dicts per particle."""
+    if not ops:
+        return []
+    lib = ops[0].ctx._lib
+    k = len(ops)
+    o = _solve_opts(lib, tol, maxit, precision)
+    o.iters_per_graph = int(iters_per_graph)
+    raw = lambda v: v.value if isinstance(v, C.c_void_p) else v
+    arr = lambda vals: (C.c_void_p * k)(*[C.c_void_p(raw(v)) for v in vals])
+    pops = arr([op.h for op in ops])
+    ppr = arr([pr.h if pr is not None else None for pr in precs])
+    nr = (C.c_int64 * k)(*[int(v) for v in nrhs])
+    infos = (L.vs_solve_info * int(sum(nrhs)))()
+    L.check(lib.vs_solve_particles_device(k, pops, ppr, arr(b_ptrs), arr(x_ptrs), nr, C.byref(o), infos))
+    out, at = [], 0
+    for v in nrhs:
+        out.append([dict(flag=i.flag, relres=i.relres, iter=i.iter, refinements=i.refinements, time_ms=i.time_ms,
+                         launches=i.kernel_launches) for i in infos[at:at + int(v)]])
+        at += int(v)
+    return out
+
+
 def solve_batch_device(op, b_ptr, x_ptr, nrhs, prec=None, tol=1e-6, maxit=2000, precision="mixed",
                        iters_per_graph=4):
     """vs_solve_batch_device on device buffers (double2, nrhs*n3 each)."""

@@ -5,6 +5,7 @@
 #include "vs_krylov.h"
 #include <chrono>
 #include <atomic>
+#include <thread>
 #include <complex>
 #include <cstring>
 #include <cmath>
@@ -1219,6 +1220,60 @@ int vs_solve_batch_device(vs_op* op, vs_prec* prec, const void* b, void* x, int6
     const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     for (int64_t r = 0; r < nrhs; ++r) infos[r].time_ms = ms;
   });
+}
+
+int vs_solve_particles_device(int64_t nparticles, vs_op* const* ops, vs_prec* const* precs, const void* const* b,
+                              void* const* x, const int64_t* nrhs, const vs_solve_opts* opts, vs_solve_info* infos) {
+  if (nparticles < 1 || !ops || !b || !x || !nrhs || !opts || !infos) {
+    g_last_error = "vs_solve_particles_device: NULL argument or no particles";
+    return VS_ERR_ARG;
+  }
+  // particles grouped by context: one host thread per context
+  std::vector<vs_ctx*> ctxs;
+  std::vector<std::vector<int64_t>> groups;
+  std::vector<int64_t> first(nparticles);
+  int64_t off = 0;
+  for (int64_t i = 0; i < nparticles; ++i) {
+    if (!ops[i] || nrhs[i] < 1) {
+      g_last_error = "vs_solve_particles_device: NULL operator or nrhs < 1 for particle " + std::to_string(i);
+      return VS_ERR_ARG;
+    }
+    first[i] = off;
+    off += nrhs[i];
+    size_t g = 0;
+    while (g < ctxs.size() && ctxs[g] != ops[i]->ctx) ++g;
+    if (g == ctxs.size()) {
+      ctxs.push_back(ops[i]->ctx);
+      groups.emplace_back();
+    }
+    groups[g].push_back(i);
+  }
+  std::vector<int> status(groups.size(), VS_OK);
+  std::vector<int64_t> failed(groups.size(), -1);
+  auto run_group = [&](size_t g) {
+    for (int64_t i : groups[g]) {
+      const int st = vs_solve_batch_device(ops[i], precs ? precs[i] : nullptr, b[i], x[i], nrhs[i], opts,
+                                           infos + first[i]);
+      if (st != VS_OK && status[g] == VS_OK) {
+        status[g] = st;
+        failed[g] = i;
+      }
+    }
+  };
+  std::vector<std::thread> threads;
+  try {
+    for (size_t g = 1; g < groups.size(); ++g) threads.emplace_back(run_group, g);
+  } catch (const std::exception& e) {  // no thread could be started: run the rest here
+    for (size_t g = threads.size() + 1; g < groups.size(); ++g) run_group(g);
+  }
+  run_group(0);
+  for (auto& t : threads) t.join();
+  for (size_t g = 0; g < groups.size(); ++g)
+    if (status[g] != VS_OK) {
+      g_last_error = "particle " + std::to_string(failed[g]) + ": " + ops[failed[g]]->ctx->err;
+      return status[g];
+    }
+  return VS_OK;
 }
 
 int vs_solve_batch(vs_op* op, vs_prec* prec, const double* b, double* x, int64_t nrhs, const vs_solve_opts* opts,

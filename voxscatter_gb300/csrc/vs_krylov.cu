@@ -1307,10 +1307,10 @@ static void dr_combine(KrylovWork& w, const cplx_t<T>* Xa, int na, const cplx_t<
   if (nx == 0 || ncol == 0) return;
   std::vector<double2> h((size_t)nx * ncol);
   for (size_t i = 0; i < h.size(); ++i) h[i] = make_double2(coef[i].real(), coef[i].imag());
-  // stream-ordered: wait for the previous combine before its coefficients are overwritten
-  VS_CUDA(cudaStreamSynchronize(st));
+  // stream-ordered after the previous combine that read the coefficients; the
+  // copy from pageable memory is staged before the call returns
   w.rcoef.alloc(h.size() * sizeof(double2));
-  VS_CUDA(cudaMemcpy(w.rcoef.p, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  VS_CUDA(cudaMemcpyAsync(w.rcoef.p, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice, st));
   const size_t smem = (size_t)nx * 4 * sizeof(cplx_t<T>);
   k_dr_combine<T><<<dim3(vec_grid(n), ceil_div(ncol, 4)), 256, smem, st>>>(
       Xa, na, nb ? Xb : Xa, nb, w.rcoef.as<double2>(), ncol, out, n, accumulate ? 1 : 0);
