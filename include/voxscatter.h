@@ -282,7 +282,8 @@ int vs_solve_batch_device(vs_op* op, vs_prec* prec, const void* b, void* x, int6
  * each on its context's stream; operators that share a context run one after
  * another.  infos holds sum(nrhs) entries, particle by particle.  Returns the
  * first failing particle's status (its message in vs_last_error(NULL) and in
- * its context); the other particles still run. */
+ * its context); the other particles still run.  A preconditioner shared by
+ * particles on different contexts is rejected (VS_ERR_ARG) before any work. */
 int vs_solve_particles_device(int64_t nparticles, vs_op* const* ops, vs_prec* const* precs, const void* const* b,
                               void* const* x, const int64_t* nrhs, const vs_solve_opts* opts, vs_solve_info* infos);
 

@@ -271,3 +271,9 @@ def test_particles_solved_concurrently_match_batch_solves(api):
             assert inf[r]["flag"] == 0 and inf[r]["iter"] == ir[r]["iter"]
             assert np.linalg.norm(B[r] - Aor(Xh[r])) / np.linalg.norm(B[r]) <= 1e-10 * 1.01
         assert np.linalg.norm(Xh - Xr.cpu().numpy()) <= 1e-12 * np.linalg.norm(Xh)
+    # one preconditioner for particles on two contexts is refused before any work
+    from voxscatter_gb300._lib import VoxScatterError
+    with pytest.raises(VoxScatterError, match="share a preconditioner"):
+        api.solve_particles_device([parts[0][0], parts[1][0]], [parts[0][1], parts[0][1]],
+                                   [parts[0][2].data_ptr(), parts[1][2].data_ptr()], [Xs[0].data_ptr(), Xs[1].data_ptr()],
+                                   [4, 4], tol=1e-10, precision="fp64")

@@ -1248,6 +1248,16 @@ int vs_solve_particles_device(int64_t nparticles, vs_op* const* ops, vs_prec* co
     }
     groups[g].push_back(i);
   }
+  // a preconditioner keeps per-apply scratch, so one used by particles on two
+  // contexts would be applied by two threads at once
+  if (precs)
+    for (int64_t i = 0; i < nparticles; ++i)
+      for (int64_t j = i + 1; j < nparticles; ++j)
+        if (precs[i] && precs[i] == precs[j] && ops[i]->ctx != ops[j]->ctx) {
+          g_last_error = "vs_solve_particles_device: particles " + std::to_string(i) + " and " + std::to_string(j) +
+                         " share a preconditioner but not a context";
+          return VS_ERR_ARG;
+        }
   std::vector<int> status(groups.size(), VS_OK);
   std::vector<int64_t> failed(groups.size(), -1);
   auto run_group = [&](size_t g) {
