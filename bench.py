@@ -640,6 +640,78 @@ def run_passes(args):
     return 0
 
 
+def run_adjoint(args):
+    """64x64x16 random-permittivity slab (eps = (1.5+0.02i)^2 (1 + 0.1 g), g a
+    seeded Gaussian random field of correlation length 4 voxels), z incidence,
+    x polarisation: forward + plain-transpose adjoint solves for C_ext and
+    dC_ext/deps per voxel, mixed and FP64; the FP64 gradient checked by central
+    differences (h = 1e-6, re and im) on 16 seeded voxels.  One JSON line."""
+    import torch
+    from voxscatter_gb300 import api, workloads as W
+    ctx = api.Context(0)
+    p = W.config4(seed=0)
+    L, M, N = p["L"], p["M"], p["N"]
+    nD = L * M * N
+    idx = p["idx"]
+    idx3 = np.concatenate([idx, nD + idx, 2 * nD + idx])
+    d, ko = p["d"], p["ko"]
+    t = time.perf_counter()
+    Toep = api.green_dda(p["r"], ko, ctx=ctx)
+    ainv = 1 / api.alpha_ldr(p["eps"], ko, d, p["kvec"], p["Eo"], is_eps=True)
+    G = np.zeros(nD, complex); G[idx] = ainv
+    op = api.Operator(L, M, N, idx3, 1.0, d ** 3, G.reshape((L, M, N), order="F"), toep=Toep, ctx=ctx)
+    pr = api.Preconditioner(op, shift=np.mean(ainv), d=d ** 3, precisions=("c64", "c128"))
+    ctx.synchronize()
+    setup_s = time.perf_counter() - t
+    b = api.plane_wave(op, p["r"], p["kvec"], p["Eo"])
+    res = {}
+    for prec_name, tol in (("mixed", 1e-6), ("fp64", 1e-12)):
+        api.cext_grad(op, pr, b, p["eps"], ko, d, p["kvec"], p["Eo"], tol=tol, precision=prec_name)  # warm-up
+        times = []
+        for _ in range(max(1, args.steps)):
+            ctx.synchronize()
+            t = time.perf_counter()
+            c, gre, gim, P, i1, i2 = api.cext_grad(op, pr, b, p["eps"], ko, d, p["kvec"], p["Eo"], tol=tol,
+                                                   precision=prec_name)
+            times.append((time.perf_counter() - t) * 1e3)
+        res[prec_name] = dict(c=c, gre=gre, gim=gim, P=P, ms=float(np.median(times)), it=(i1["iter"], i2["iter"]),
+                              flags=(i1["flag"], i2["flag"]))
+    f = res["fp64"]
+    sc = max(np.abs(f["gre"]).max(), np.abs(f["gim"]).max())
+
+    def cext_of(eps):
+        ai = 1 / api.alpha_ldr(eps, ko, d, p["kvec"], p["Eo"], is_eps=True)
+        G2 = np.zeros(nD, complex); G2[idx] = ai
+        o2 = api.Operator(L, M, N, idx3, 1.0, d ** 3, G2.reshape((L, M, N), order="F"), toep=Toep, ctx=ctx)
+        x, info, _ = api.solve(o2, b, pr, tol=1e-12, precision="fp64", x0=f["P"], want_resvec=False)
+        return api.cext(o2, x, b, ko, d ** 3, p["Eo"])
+
+    h = 1e-6
+    rng = np.random.default_rng(1234)
+    worst = 0.0
+    t = time.perf_counter()
+    for j in rng.choice(len(idx), 16, replace=False):
+        for step, g in ((h, f["gre"]), (1j * h, f["gim"])):
+            ep = p["eps"].copy(); ep[j] += step
+            em = p["eps"].copy(); em[j] -= step
+            worst = max(worst, abs((cext_of(ep) - cext_of(em)) / (2 * h) - g[j]) / sc)
+    fd_s = time.perf_counter() - t
+    m = res["mixed"]
+    line = {"metric": "adjoint C_ext gradient: forward + adjoint solve time", "unit": "ms",
+            "config": {"workload": f"random-permittivity slab {L}x{M}x{N}, {len(idx)} dipoles, eps=(1.5+0.02i)^2"
+                                   f"(1+0.1 g), correlation length 4 voxels, seeded; z incidence, x polarisation"},
+            "setup_s": setup_s, "cext": f["c"],
+            "mixed": {"ms": m["ms"], "iterations_fwd_adj": m["it"], "flags": m["flags"],
+                      "cext_rel_err_vs_fp64": abs(m["c"] - f["c"]) / abs(f["c"]),
+                      "grad_max_err_vs_fp64": float(max(np.abs(m["gre"] - f["gre"]).max(),
+                                                        np.abs(m["gim"] - f["gim"]).max()) / sc)},
+            "fp64": {"ms": f["ms"], "iterations_fwd_adj": f["it"], "flags": f["flags"]},
+            "central_differences": {"h": h, "voxels": 16, "worst_abs_err_over_max_grad": worst, "seconds": fd_s},
+            "data": "synthetic (seeded random permittivity field)"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_koch(args):
     """256x256x64 Koch snowflake (level 3, 16 central layers, m = 1.78+0.005i):
     setup times, per-launch pipeline times, the matvec's model bandwidth, and a
@@ -747,7 +819,7 @@ def main():
     ap.add_argument("--shapes", default=None,
                     help='JSON {"op": {...}, "prec": {...}} c64 launch shapes applied after autotuning '
                          '(replays a tuned configuration, e.g. under a profiler)')
-    ap.add_argument("--mode", default="solve", choices=["solve", "passes", "koch", "nop"],
+    ap.add_argument("--mode", default="solve", choices=["solve", "passes", "koch", "nop", "adjoint"],
                     help="passes: only build the operator/preconditioner and time each pipeline launch "
                          "(a short command for ncu captures); koch: the 256x256x64 snowflake's pipeline "
                          "times and a bounded GMRES(50) solve")
@@ -756,6 +828,8 @@ def main():
         return run_passes(args)
     if args.mode == "koch":
         return run_koch(args)
+    if args.mode == "adjoint":
+        return run_adjoint(args)
     if args.mode == "nop":
         return run_nop(args)
     if args.impl == "reference":

@@ -81,10 +81,11 @@ struct KrylovWork {
   // right-hand side g, solution y, pass coefficients, partial dots, state,
   // and the vectors w, tmp and the correction d.
   DevBuf gV, gH, gcs, gsn, gg, gy, ghp, gpart, gstate, gw, gtmp, gd;
-  // GCRO-DR: recycled spaces U, C (and the next ones), the solution in the
-  // preconditioned space, the residual, the unrotated Hessenberg, C^H A V,
-  // partial and final Gram products, combination coefficients.
-  DevBuf rU, rC, rU2, rC2, rz, rr, rHraw, rB, rgpart, rgram, rcoef;
+  // GCRO-DR: the basis [C | V] in one array (C in the slots just below V),
+  // recycled U, the next U and C, the solution in the preconditioned space,
+  // the residual, the stacked [C^H A M V; Hessenberg] columns, partial and
+  // final Gram products, combination coefficients.
+  DevBuf rCV, rU, rU2, rC2, rz, rr, rBH, rgpart, rgram, rcoef;
   template <typename T> void ensure(int64_t n);
 };
 

@@ -1163,8 +1163,10 @@ static void gmres_buffers(KrylovWork& w, int64_t n, int m) {
 // up to `restart` Arnoldi steps on (I - C C^H) A M; after it the `ritz`
 // harmonic Ritz vectors of smallest magnitude span the recycled space U with
 // C = A M U orthonormal, which the next cycle deflates.  The Arnoldi steps
-// and their residual estimate reuse the GMRES kernels above (Gram-Schmidt
-// against C, then against V, each applied twice); the unrotated Hessenberg
+// and their residual estimate reuse the GMRES kernels above (classical
+// Gram-Schmidt against [C | V] at once, C stored just below V, applied twice;
+// C is orthogonal to V, so this equals projecting against C and then V as
+// pgmresDR_iter.m:99-107 does); the unrotated Hessenberg
 // is kept for the harmonic Ritz problems.  Between cycles the host solves the
 // small least-squares, QR and eigen problems (vs_dense.cu) from Gram products
 // formed on the device, and tall-skinny combinations on the device form the
@@ -1322,14 +1324,16 @@ template <typename T>
 static void gcrodr_buffers(KrylovWork& w, int64_t n, int m, int kr) {
   using C = cplx_t<T>;
   const size_t kv = (size_t)std::max(kr, 1) * n * sizeof(C);
+  w.rCV.alloc((size_t)(kr + m + 1) * n * sizeof(C));
   w.rU.alloc(kv);
-  w.rC.alloc(kv);
   w.rU2.alloc(kv);
   w.rC2.alloc(kv);
   w.rz.alloc(n * sizeof(C));
   w.rr.alloc(n * sizeof(C));
-  w.rHraw.alloc((size_t)(m + 1) * m * sizeof(double2));
-  w.rB.alloc((size_t)std::max(kr, 1) * m * sizeof(double2));
+  w.rBH.alloc((size_t)(kr + m + 1) * m * sizeof(double2));
+  // the Gram-Schmidt pass covers up to kr + m vectors of [C | V]
+  w.ghp.alloc((size_t)(kr + m + 1) * sizeof(double2));
+  w.gpart.alloc((size_t)(kr + m + 1) * ceil_div(n, kDotChunk) * sizeof(double2));
 }
 
 // Inner GCRO-DR on A d = rin (precision T, d overwritten), right
@@ -1344,18 +1348,18 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
   using C = cplx_t<T>;
   const int g = vec_grid(n);
   const int nchunk = ceil_div(n, kDotChunk);
-  C* V = w.gV.as<C>();
+  // [C | V]: the kc recycled C vectors sit in the slots just below V, so one
+  // Gram-Schmidt pass projects against both
+  C* V = w.rCV.as<C>() + (int64_t)kr * n;
   C* wv = w.gw.as<C>();
   C* tmp = w.gtmp.as<C>();
   C* U = w.rU.as<C>();
-  C* Cm = w.rC.as<C>();
   C* U2 = w.rU2.as<C>();
   C* C2 = w.rC2.as<C>();
   C* z = w.rz.as<C>();
   C* r = w.rr.as<C>();
   double2* H = w.gH.as<double2>();
-  double2* Hraw = w.rHraw.as<double2>();
-  double2* Bd = w.rB.as<double2>();
+  double2* BH = w.rBH.as<double2>();
   double2* hp = w.ghp.as<double2>();
   double2* part = w.gpart.as<double2>();
   GState* gs = w.gstate.as<GState>();
@@ -1385,6 +1389,7 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
   int64_t nres = 1;
   *flag = 1;
   int steps = 0, kc = 0;
+  C* Cm = V;  // first of the kc recycled vectors (none yet)
   for (;;) {
     const double beta = norm_dev(r);
     if (!std::isfinite(beta)) {
@@ -1397,9 +1402,11 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
     }
     if (steps >= maxit) break;
     k_scale_by<T><<<g, 256, 0, st>>>(r, V, n, w.scal.as<double>());
+    // column k of BH (leading dimension ld): rows 0..kc-1 = C^H A M v_k,
+    // rows kc..kc+k+1 = the unrotated Hessenberg column
+    const int ld = kc + m + 1;
     VS_CUDA(cudaMemsetAsync(H, 0, (size_t)(m + 1) * m * sizeof(double2), st));
-    VS_CUDA(cudaMemsetAsync(Hraw, 0, (size_t)(m + 1) * m * sizeof(double2), st));
-    if (kc) VS_CUDA(cudaMemsetAsync(Bd, 0, (size_t)kc * m * sizeof(double2), st));
+    VS_CUDA(cudaMemsetAsync(BH, 0, (size_t)ld * m * sizeof(double2), st));
     VS_CUDA(cudaMemsetAsync(w.gg.p, 0, (m + 1) * sizeof(double2), st));
     const double2 g0 = make_double2(beta, 0);
     VS_CUDA(cudaMemcpyAsync(w.gg.p, &g0, sizeof(double2), cudaMemcpyHostToDevice, st));
@@ -1422,21 +1429,14 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
       rprec(V + (int64_t)k * n, tmp, &gs->skip);
       matvec<T>(op, tmp, wv, 1, op_mode, &gs->skip, st);
       *launches += 5;
-      if (kc) {
-        double2* Bcol = Bd + (int64_t)k * kc;
-        for (int pass = 0; pass < 2; ++pass) {
-          k_gm_dots<T><<<dim3(nchunk, kc), 256, 0, st>>>(Cm, wv, n, part, nchunk, gs);
-          k_gm_dots_final<<<kc, 256, 0, st>>>(part, nchunk, hp, Bcol, gs);
-          k_gm_axpy<T><<<g, 256, kc * sizeof(C), st>>>(Cm, wv, n, kc, hp, gs);
-        }
-        *launches += 6;
-      }
-      double2* Hcol = Hraw + (int64_t)k * (m + 1);
+      double2* col = BH + (int64_t)k * ld;
+      const int nb = kc + k + 1;  // C_0..C_kc-1, V_0..V_k
       for (int pass = 0; pass < 2; ++pass) {
-        k_gm_dots<T><<<dim3(nchunk, k + 1), 256, 0, st>>>(V, wv, n, part, nchunk, gs);
-        k_gm_dots_final<<<k + 1, 256, 0, st>>>(part, nchunk, hp, Hcol, gs);
-        k_gm_axpy<T><<<g, 256, (k + 1) * sizeof(C), st>>>(V, wv, n, k + 1, hp, gs);
+        k_gm_dots<T><<<dim3(nchunk, nb), 256, 0, st>>>(Cm, wv, n, part, nchunk, gs);
+        k_gm_dots_final<<<nb, 256, 0, st>>>(part, nchunk, hp, col, gs);
+        k_gm_axpy<T><<<g, 256, nb * sizeof(C), st>>>(Cm, wv, n, nb, hp, gs);
       }
+      double2* Hcol = col + kc;
       k_gm_norm<T><<<g, kRedThreads, 0, st>>>(wv, n, w.partials.as<double>(), &ks->counter, Hcol + k + 1, gs);
       k_gm_scale<T><<<g, 256, 0, st>>>(wv, V + (int64_t)(k + 1) * n, n, Hcol + k + 1, gs);
       k_dr_copycol<<<1, 64, 0, st>>>(gs, Hcol, H + (int64_t)k * (m + 1), k + 2);
@@ -1464,14 +1464,17 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
     }
     const bool conv = cur.flag == 0;
     const bool more = !conv && steps < maxit;
-    // the unrotated Hessenberg ((kd+1) x kd) and B = C^H A M V (kc x kd) on the host
-    std::vector<double2> hh((size_t)(m + 1) * kd), bh((size_t)kc * kd);
-    VS_CUDA(cudaMemcpyAsync(hh.data(), Hraw, hh.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
-    if (kc) VS_CUDA(cudaMemcpyAsync(bh.data(), Bd, bh.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    // B = C^H A M V (kc x kd) and the unrotated Hessenberg ((kd+1) x kd) on the host
+    std::vector<double2> bhh((size_t)ld * kd);
+    VS_CUDA(cudaMemcpyAsync(bhh.data(), BH, bhh.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
     std::vector<cd> Hh((size_t)(kd + 1) * kd);
     for (int j = 0; j < kd; ++j)
-      for (int i = 0; i <= kd; ++i) Hh[i + (size_t)j * (kd + 1)] = cd(hh[i + (size_t)j * (m + 1)].x, hh[i + (size_t)j * (m + 1)].y);
+      for (int i = 0; i <= kd; ++i) {
+        const double2 e = bhh[kc + i + (size_t)j * ld];
+        Hh[i + (size_t)j * (kd + 1)] = cd(e.x, e.y);
+      }
+    auto bh = [&](int i, int j) { return cd(bhh[i + (size_t)j * ld].x, bhh[i + (size_t)j * ld].y); };
     if (kc == 0) {
       // first cycle (pgmresDR.m:190-221)
       std::vector<cd> rhs(kd + 1, 0);
@@ -1494,7 +1497,8 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
         dr_combine<T>(w, V, kd, nullptr, 0, cu, kk, U2, n, false, st, launches);
         dr_combine<T>(w, V, kd + 1, nullptr, 0, Q, kk, C2, n, false, st, launches);
         std::swap(U, U2);
-        std::swap(Cm, C2);
+        Cm = V - (int64_t)kk * n;
+        VS_CUDA(cudaMemcpyAsync(Cm, C2, (size_t)kk * n * sizeof(C), cudaMemcpyDeviceToDevice, st));
         kc = kk;
       }
     } else {
@@ -1508,7 +1512,7 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
       dense::Mat H2((size_t)(mm + 1) * mm, 0);
       for (int i = 0; i < kc; ++i) H2[i + (size_t)i * (mm + 1)] = Dv[i];
       for (int j = 0; j < kd; ++j) {
-        for (int i = 0; i < kc; ++i) H2[i + (size_t)(kc + j) * (mm + 1)] = cd(bh[i + (size_t)j * kc].x, bh[i + (size_t)j * kc].y);
+        for (int i = 0; i < kc; ++i) H2[i + (size_t)(kc + j) * (mm + 1)] = bh(i, j);
         for (int i = 0; i <= kd; ++i) H2[kc + i + (size_t)(kc + j) * (mm + 1)] = Hh[i + (size_t)j * (kd + 1)];
       }
       const std::vector<cd> y = dense::lstsq(H2, mm + 1, mm, Gr);
@@ -1536,7 +1540,7 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
         dr_combine<T>(w, U, kc, V, kd, cu, kc, U2, n, false, st, launches);
         dr_combine<T>(w, Cm, kc, V, kd + 1, Q, kc, C2, n, false, st, launches);
         std::swap(U, U2);
-        std::swap(Cm, C2);
+        VS_CUDA(cudaMemcpyAsync(Cm, C2, (size_t)kc * n * sizeof(C), cudaMemcpyDeviceToDevice, st));
       }
     }
     if (conv) {
