@@ -122,8 +122,9 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def _pass_bytes(p, PQR, n3, e=8, sym=True):
-    """Algorithmic DRAM bytes of each launch of the c64 pipelines (one rhs)."""
+def _pass_bytes(p, PQR, n3, e=8, sym=True, packed=False):
+    """Algorithmic DRAM bytes of each launch of the c64 pipelines (one rhs);
+    packed: the GEMV reads the padded lower triangles of the symmetric blocks."""
     L, M, N = p["L"], p["M"], p["N"]
     P, Q, R = PQR
     V = L * M * N
@@ -136,9 +137,10 @@ def _pass_bytes(p, PQR, n3, e=8, sym=True):
           3 * P * M * N * e + 3 * V * i4 + 2 * n3 * e]
     n = 3 * N
     nblk = (L // 2 + 1) * (M // 2 + 1) if sym else L * M
+    blk_elems = ((n * (n + 1) // 2 + 15) // 16 * 16) if packed else n * n
     pc = [n3 * e + 3 * V * i4 + 3 * V * e,
           2 * 3 * V * e,
-          nblk * n * n * e + 2 * 3 * V * e,
+          nblk * blk_elems * e + 2 * 3 * V * e,
           2 * 3 * V * e,
           3 * V * e + 3 * V * i4 + n3 * e]
     pinned = e * (9 * V + 1.5 * V + 12 * P * M * N + 12 * P * Q * N) + G
@@ -167,7 +169,8 @@ def _pass_names(op, prec):
     a, b, c, d = xy(sp, "prec_")
     if sp.get("fuse_xy") == 1:  # one plane kernel each way, passes 1 and 3 launch nothing
         a, b, c, d = "prec_k_plane_fwd", "none", "none", "prec_k_plane_inv"
-    names_pc = [a, b, "k_block_gemv_stream" if sp["gemv_mode"] == 1 else "k_block_gemv_sym", c, d]
+    gemv = {1: "k_block_gemv_stream", 2: "k_block_gemv_packed"}.get(sp["gemv_mode"], "k_block_gemv_sym")
+    names_pc = [a, b, gemv, c, d]
     return names_mv, names_pc
 
 
@@ -485,7 +488,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     mv_ms = op.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", 50)
     pc_ms = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", 50)
-    mv_bytes, pc_bytes, pinned = _pass_bytes(p, op.PQR, n3)
+    mv_bytes, pc_bytes, pinned = _pass_bytes(p, op.PQR, n3, packed=prec.shape("c64")["gemv_mode"] == 2)
     names_mv, names_pc = _pass_names(op, prec)
     allk = [(names_mv[i], mv_ms[i], mv_bytes[i]) for i in range(5)] + \
            [(names_pc[i], pc_ms[i], pc_bytes[i]) for i in range(5)]

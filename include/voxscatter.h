@@ -366,7 +366,12 @@ int vs_op_set_shape(vs_op* op, int precision, const vs_shape* shape);
  * the block GEMV.  gemv_mode 0 is the register-direct GEMV (gemv_blocks
  * stored blocks per CTA, gemv_threads per CTA); gemv_mode 1 streams each block
  * through shared memory with bulk asynchronous copies (gemv_blocks CTAs per SM, 1-4,
- * gemv_chunk block columns per copy).  0 / -1 select the defaults. */
+ * gemv_chunk block columns per copy); gemv_mode 2 streams the packed lower
+ * triangles of the symmetric blocks S = B D (D negating the x and y
+ * components; built by vs_prec_create when the operator has exact parity and
+ * d is one scalar, VS_ERR_UNSUPPORTED otherwise), one whole block per copy
+ * (gemv_blocks CTAs per SM, gemv_chunk = ring depth 2-8).  0 / -1 select the
+ * defaults. */
 typedef struct vs_prec_shape {
   int lg_lines_x;
   int lg_tile_y;

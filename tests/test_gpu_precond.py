@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+from voxscatter_gb300._lib import VoxScatterError
 from voxscatter_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -71,8 +72,9 @@ def test_prec_build_and_apply(api, shape):
     X = rng.normal(size=(5, idx3.size)) + 1j * rng.normal(size=(5, idx3.size))
     Y_o = np.array([O.mvp_circ_2_level(inv_o, X[k], L, M, N, idx3) for k in range(5)])
     for prec, tol in (("c128", 1e-10), ("c64", 1e-4)):
+        # mode 2: packed symmetric blocks, chunk = ring depth
         for mode, chunk, ctas in ((0, 0, 2), (1, 0, 1), (1, 0, 2), (1, 2, 2), (1, 5, 1), (1, 0, 3), (1, 3, 4),
-                                  (1, 0, 4)):
+                                  (1, 0, 4), (2, 2, 1), (2, 3, 2), (2, 4, 4)):
             pr.set_shape(prec, gemv_mode=mode, gemv_chunk=min(chunk, 3 * N), gemv_blocks=ctas, gemv_threads=0)
             assert rel(pr.apply(x, prec), y_o) < tol, (prec, mode, chunk)
             Y = pr.apply(X.ravel(), prec).reshape(5, -1)
@@ -103,6 +105,8 @@ def test_prec_jvie_face_vector_and_batch(api):
     inv_o = O.invert_blocks(blk_o, gram, face3)
     op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
     pr = api.Preconditioner(op, shift=gram, d=face3)
+    with pytest.raises(VoxScatterError, match="packed"):  # a face vector breaks the block symmetry
+        pr.set_shape("c128", gemv_mode=2, gemv_chunk=2)
     X = rng.normal(size=(3, idx3.size)) + 1j * rng.normal(size=(3, idx3.size))
     Y = pr.apply(X.ravel(), "c128").reshape(3, -1)
     for k in range(3):
@@ -141,6 +145,8 @@ def test_prec_full_storage_when_parity_is_not_exact(api):
     assert rel(pr.blocks(L, M, N, "c128"), inv_o) < 1e-10
     x = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
     assert rel(pr.apply(x, "c128"), O.mvp_circ_2_level(inv_o, x, L, M, N, idx3)) < 1e-10
+    with pytest.raises(VoxScatterError, match="packed"):  # no quadrant storage, no packed blocks
+        pr.set_shape("c64", gemv_mode=2, gemv_chunk=2)
 
 
 @pytest.mark.parametrize("N,L,M", [(48, 5, 6), (64, 6, 5)])
@@ -167,6 +173,14 @@ def test_prec_large_blocks(api, N, L, M):
         for mode, chunk in ((0, 0), (1, 0), (1, 16), (1, 7)):
             pr.set_shape(prec, gemv_mode=mode, gemv_chunk=chunk, gemv_blocks=1, gemv_threads=0)
             assert rel(pr.apply(x, prec), y_o) < tol, (prec, mode, chunk)
+        # packed symmetric blocks where a two-block ring fits in shared memory
+        # (n = 144 in c64); otherwise the mode is refused
+        if prec == "c64" and 3 * N == 144:
+            pr.set_shape(prec, gemv_mode=2, gemv_chunk=2, gemv_blocks=1, gemv_threads=0)
+            assert rel(pr.apply(x, prec), y_o) < tol, (prec, "packed")
+        else:
+            with pytest.raises(VoxScatterError, match="packed"):
+                pr.set_shape(prec, gemv_mode=2, gemv_chunk=2, gemv_blocks=1, gemv_threads=0)
 
 
 def test_context_outlives_its_objects(api):

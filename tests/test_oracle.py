@@ -314,3 +314,23 @@ def test_pgmres_dr_deflation_beats_restarted_gmres():
     assert len(rv1) < 0.5 * len(rv2)
     # resvec: one entry per Arnoldi step after the initial 1
     assert rv1[0] == 1.0 and len(rv1) == 1 + 20 * (it1[1]) + it1[0]
+
+
+def test_inverse_blocks_times_component_flips_are_symmetric():
+    """Every inverse block B of the 2-level circulant preconditioner of the DDA
+    operator satisfies (B D)^T = B D with D = diag(-1 on the x and y
+    components, +1 on z): the property that lets the packed GEMV store only
+    the lower triangle of B D.  A face vector d (JVIE) breaks it."""
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    fN, Toep, alpha, idx3, chi, dV = _setup(p)
+    L, M, N = p["L"], p["M"], p["N"]
+    _, c1 = O.circ_1_level(Toep, L, M, N, 0, "off")
+    _, blk = O.circ_2_level(c1, L, M, N)
+    D = np.r_[-np.ones(2 * N), np.ones(N)]
+    inv = O.invert_blocks(blk, 1 / alpha, dV)
+    worst = max(np.linalg.norm(S - S.T) / np.linalg.norm(S) for S in (inv[i, j] * D for i in range(L) for j in range(M)))
+    assert worst < 1e-13
+    face = 1 + 0.3 * np.random.default_rng(0).random(3 * N)
+    inv_f = O.invert_blocks(blk, 0.8, face)
+    worst_f = max(np.linalg.norm(S - S.T) / np.linalg.norm(S) for S in (inv_f[i, j] * D for i in range(L) for j in range(M)))
+    assert worst_f > 1e-3

@@ -722,6 +722,8 @@ int vs_prec_create(vs_op* op, const double* shift, const double* d, int64_t nd, 
     VS_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
     VS_REQUIRE(hs == 0, "a preconditioner block is singular or its inverse is not finite");
+    // with a uniform scaling d every block is symmetric up to the x/y sign flips
+    if (nd == 1) vs::pack_sym_blocks(*pr, st);
     prec_scratch_impl(pr, 1);
     vs::autotune_prec<float>(*pr, st);
     vs::autotune_prec<double>(*pr, st);
@@ -943,7 +945,9 @@ int vs_prec_set_shape(vs_prec* prec, int precision, const vs_prec_shape* shape) 
     vs::PassShape& s = prec->shape[precision == VS_C64 ? 0 : 1];
     s.lg_lpb_x = shape->lg_lines_x;
     s.lg_tx_y = shape->lg_tile_y;
-    VS_REQUIRE(shape->gemv_mode >= -1 && shape->gemv_mode <= 1, "gemv_mode must be -1, 0 or 1");
+    VS_REQUIRE(shape->gemv_mode >= -1 && shape->gemv_mode <= 2, "gemv_mode must be -1, 0, 1 or 2");
+    if (shape->gemv_mode == 2 && (precision == VS_C64 ? prec->pk32.p : prec->pk64.p) == nullptr)
+      throw vs::Error(VS_ERR_UNSUPPORTED, "packed symmetric blocks are not available for this preconditioner");
     VS_REQUIRE(shape->gemv_chunk >= 0 && shape->gemv_chunk <= 3 * prec->N, "gemv_chunk out of range");
     VS_REQUIRE(shape->gemv_mode < 1 || shape->gemv_blocks <= 4, "streamed GEMV takes 1 to 4 CTAs per SM");
     s.gemv_ti = shape->gemv_blocks;

@@ -52,7 +52,8 @@ struct PassShape {
   int lg_tx_z = -1;    // z pass: x-tile width
   int gemv_ti = 0;     // preconditioner GEMV: stored blocks per CTA (direct) or CTAs per SM (streamed); 0 = default
   int gemv_threads = 0;
-  int gemv_mode = -1;  // 0 register-direct GEMV, 1 streamed through shared memory, -1 default (streamed)
+  int gemv_mode = -1;  // 0 register-direct GEMV, 1 streamed through shared memory, 2 packed symmetric blocks,
+                       // -1 default (streamed)
   int gemv_chunk = 0;  // streamed GEMV: block columns per bulk copy (0 = default)
   int z_reg = -1;      // z pass: 0 shared-memory Stockham, 1 two-level, 2 two-level with register cap, -1 default
   int fuse_xy = -1;    // preconditioner: 1 both x/y FFTs of a plane in one CTA (when it fits), 0/-1 separate passes
@@ -150,6 +151,10 @@ struct vs_prec {
   int nrhs_cap = 0;
   vs::PassShape shape[2];   // [0] c64, [1] c128 apply launch shapes
   vs::DevBuf gemv_status;   // int: bit 4 set when a streamed-GEMV wait ran out
+  // lower triangles of S = B D (D negates the x and y components), packed per
+  // block with pk_stride entries; present when the blocks are symmetric so
+  vs::DevBuf pk32, pk64;
+  int64_t pk_stride = 0;
 };
 
 namespace vs {
@@ -237,6 +242,7 @@ template <typename T>
 void autotune_op(vs_op& op, cudaStream_t st);
 template <typename T>
 void autotune_prec(vs_prec& pr, cudaStream_t st);
+void pack_sym_blocks(vs_prec& pr, cudaStream_t st);
 
 // Elementwise helpers (vs_matvec.cu)
 void c128_to_c64(const double2* in, float2* out, int64_t n, cudaStream_t st);

@@ -979,6 +979,155 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
   }
 }
 
+// ---- packed symmetric apply ------------------------------------------------
+// With exact operator parity and a uniform block scaling, every inverse block
+// B satisfies B^T = D B D, D = diag(-1 on the x and y components, +1 on z)
+// (the 2-level circulant of a complex-symmetric Toeplitz operator: the block of
+// frequency (-i, -j) is both B^T and D B D), so S = B D is complex symmetric
+// and B x = S (D x).  Only the lower triangle of S is stored, column by column
+// (column q holds rows q..n-1 from offset q n - q (q - 1) / 2), padded to a
+// multiple of 16 entries per block: half the bytes of the full blocks.
+//
+// Persistent CTAs over the stored blocks b = blockIdx.x + k*gridDim.x; each
+// whole packed block arrives by one bulk asynchronous copy into a ring of
+// nstage stages (issued nstage blocks ahead, completing on the stage's
+// mbarrier).  Per block: all threads gather the W = 4*RG vectors (mirror and D
+// flips applied), thread (g, p) forms row p over the columns q = g (mod G)
+// from the shared packed block, the G partial rows are summed and scattered.
+// Every wait is bounded; a wait that runs out sets status bit 4, all threads
+// leave the loop together, and thread 0 waits (bounded) for its copies still
+// in flight before the CTA ends.
+template <typename T, int RG>
+__global__ void __launch_bounds__(256) k_block_gemv_packed(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ pk,
+                                                           int64_t pstride, int L, int M, int N, int64_t rhs_stride,
+                                                           int nrhs, const int* skip, int skip_stride, int nstage,
+                                                           int* __restrict__ status) {
+  using C = cplx_t<T>;
+  constexpr int W = 4 * RG;
+  const int rhs0 = blockIdx.y * RG;
+  const int nr = min(RG, nrhs - rhs0);
+  if (skip) {
+    bool all = true;
+    for (int g = 0; g < nr; ++g) all = all && skip[(rhs0 + g) * skip_stride];
+    if (all) return;
+  }
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);  // [8]
+  C* stg = reinterpret_cast<C*>(smem_raw + 128);
+  const int n = 3 * N, Lb = L / 2 + 1;
+  C* vt = stg + (size_t)nstage * pstride;  // [n][W]
+  C* red = vt + (size_t)n * W;              // [G][W][n]
+  const int64_t nblk = (int64_t)Lb * (M / 2 + 1), LM = (int64_t)L * M;
+  const int tid = threadIdx.x;
+  const int G = max(1, (int)blockDim.x / n);
+  const int g = tid / n, p = tid - g * n;
+  const bool active = g < G;
+  const int64_t nmine = blockIdx.x < nblk ? (nblk - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const uint32_t bytes = (uint32_t)(pstride * sizeof(C));
+  if (tid == 0) {
+    for (int s = 0; s < nstage; ++s) mbar_init(smem_addr(full + s), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  int64_t issued = 0;
+  auto issue = [&](int64_t k) {  // thread 0: block k of this CTA into stage k % nstage
+    const uint32_t bar = smem_addr(full + (k % nstage));
+    mbar_expect_tx(bar, bytes);
+    bulk_to_shared(smem_addr(stg + (size_t)(k % nstage) * pstride),
+                   pk + (blockIdx.x + k * gridDim.x) * pstride, bytes, bar);
+  };
+  if (tid == 0)
+    for (; issued < nmine && issued < nstage; ++issued) issue(issued);
+  int64_t k = 0;
+  for (; k < nmine; ++k) {
+    const int blk = (int)blockIdx.x + (int)k * (int)gridDim.x;
+    const int js = blk / Lb, is = blk - js * Lb;
+    for (int u = tid; u < n * W; u += blockDim.x) {
+      const int q = u / W, col = u - q * W, var = col & 3, rg = col >> 2;
+      int i, j;
+      C x = czero<C>();
+      if (rg < nr && mirror_of(is, js, var, L, M, i, j)) {
+        x = t[(int64_t)(rhs0 + rg) * rhs_stride + i + (int64_t)L * j + LM * q];
+        const bool fx = var & 1, fy = var >> 1;
+        // mirror flip, then D (both negate the x and y components)
+        const bool neg = q < N ? !fx : (q < 2 * N ? !fy : false);
+        if (neg) { x.x = -x.x; x.y = -x.y; }
+      }
+      vt[u] = x;
+    }
+    const int s = (int)(k % nstage);
+    bool ok = mbar_wait(smem_addr(full + s), (uint32_t)((k / nstage) & 1));
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicOr(status, 4);
+      break;
+    }
+    if (active) {
+      const C* S = stg + (size_t)s * pstride;
+      C acc[W];
+#pragma unroll
+      for (int c = 0; c < W; ++c) acc[c] = czero<C>();
+      const int64_t offp = (int64_t)p * n - (int64_t)p * (p - 1) / 2;
+      for (int q = g; q < n; q += G) {
+        const int64_t off = q <= p ? (int64_t)q * n - (int64_t)q * (q - 1) / 2 + (p - q) : offp + (q - p);
+        const C m = S[off];
+        const C* xq = vt + (size_t)q * W;
+        if constexpr (sizeof(C) == 8) {
+#pragma unroll
+          for (int c = 0; c < W; c += 2) {
+            const float4 xx = *reinterpret_cast<const float4*>(xq + c);
+            acc[c] = cfma(m, make_c<C>(xx.x, xx.y), acc[c]);
+            acc[c + 1] = cfma(m, make_c<C>(xx.z, xx.w), acc[c + 1]);
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < W; ++c) acc[c] = cfma(m, xq[c], acc[c]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < W; ++c) red[((size_t)g * W + c) * n + p] = acc[c];
+    }
+    __syncthreads();
+    if (tid == 0 && issued < nmine) issue(issued++);
+    for (int u = tid; u < n * W; u += blockDim.x) {
+      const int col = u / n, q = u - col * n, var = col & 3, rg = col >> 2;
+      int i, j;
+      if (rg < nr && mirror_of(is, js, var, L, M, i, j)) {
+        C sum = red[(size_t)col * n + q];
+        for (int gg = 1; gg < G; ++gg) sum = cadd(sum, red[((size_t)gg * W + col) * n + q]);
+        const bool fx = var & 1, fy = var >> 1;
+        if (q < N ? fx : (q < 2 * N ? fy : false)) { sum.x = -sum.x; sum.y = -sum.y; }
+        t[(int64_t)(rhs0 + rg) * rhs_stride + i + (int64_t)L * j + LM * q] = sum;
+      }
+    }
+  }
+  // copies issued but not consumed (only after a wait ran out) land before the CTA ends
+  if (tid == 0)
+    for (int64_t c = k; c < issued; ++c)
+      if (!mbar_wait(smem_addr(full + (c % nstage)), (uint32_t)((c / nstage) & 1))) atomicOr(status, 4);
+}
+
+// Lower triangle of S = B D per stored block into the packed layout above.
+template <typename T>
+__global__ void k_pack_sym(const cplx_t<T>* __restrict__ inv, cplx_t<T>* __restrict__ pk, int n, int N,
+                           int64_t nblk, int64_t pstride) {
+  const int64_t tri = (int64_t)n * (n + 1) / 2;
+  for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < nblk * pstride;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = u / pstride, e = u - b * pstride;
+    cplx_t<T> v = czero<cplx_t<T>>();
+    if (e < tri) {
+      // column q: the largest q with q n - q (q - 1) / 2 <= e
+      int q = (int)((2.0 * n + 1 - sqrt((2.0 * n + 1) * (2.0 * n + 1) - 8.0 * (double)e)) / 2);
+      while (q > 0 && (int64_t)q * n - (int64_t)q * (q - 1) / 2 > e) --q;
+      while ((int64_t)(q + 1) * n - (int64_t)(q + 1) * q / 2 <= e) ++q;
+      const int r = q + (int)(e - ((int64_t)q * n - (int64_t)q * (q - 1) / 2));
+      v = inv[b * (int64_t)n * n + (int64_t)q * n + r];  // column-major B(r, q)
+      if (q < 2 * N) { v.x = -v.x; v.y = -v.y; }           // S = B D
+    }
+    pk[u] = v;
+  }
+}
+
 // Stream-kernel launch geometry: chunk columns, stages, stage size, column
 // groups, consumer threads, shared memory and CTAs per SM.
 struct GemvStream {
@@ -1095,6 +1244,39 @@ static void launch_prec_plane(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* 
   VS_LAUNCH_CHECK();
 }
 
+// Packed symmetric blocks: entries per block (the lower triangle padded to a
+// multiple of 16, so every block starts on a 128-byte boundary for c64) and
+// the shared memory of k_block_gemv_packed.
+int64_t packed_stride(int n) { return ((int64_t)n * (n + 1) / 2 + 15) / 16 * 16; }
+
+template <typename T>
+size_t packed_smem(int n, int nstage, int rg) {
+  const int G = std::max(1, 256 / n);
+  return 128 + ((size_t)nstage * packed_stride(n) + (size_t)n * 4 * rg + (size_t)G * 4 * rg * n) * sizeof(cplx_t<T>);
+}
+
+// Packed copies of the inverse blocks for k_block_gemv_packed, in every
+// precision the preconditioner holds whose two-stage ring fits in shared
+// memory; only for quadrant-symmetric blocks with a uniform scaling (the
+// caller's guarantee that S = B D is symmetric).
+void pack_sym_blocks(vs_prec& pr, cudaStream_t st) {
+  const int n = 3 * pr.N;
+  if (!pr.sym || n > 256) return;
+  const int64_t nblk = (int64_t)(pr.L / 2 + 1) * (pr.M / 2 + 1), ps = packed_stride(n);
+  pr.pk_stride = ps;
+  const int grid = (int)std::min<int64_t>(ceil_div(nblk * ps, 256), 152 * 32);
+  if (pr.inv32.p && packed_smem<float>(n, 2, 1) <= 227 * 1024) {
+    pr.pk32.alloc((size_t)nblk * ps * sizeof(float2));
+    k_pack_sym<float><<<grid, 256, 0, st>>>(pr.inv32.as<float2>(), pr.pk32.as<float2>(), n, pr.N, nblk, ps);
+    VS_LAUNCH_CHECK();
+  }
+  if (pr.inv64.p && packed_smem<double>(n, 2, 1) <= 227 * 1024) {
+    pr.pk64.alloc((size_t)nblk * ps * sizeof(double2));
+    k_pack_sym<double><<<grid, 256, 0, st>>>(pr.inv64.as<double2>(), pr.pk64.as<double2>(), n, pr.N, nblk, ps);
+    VS_LAUNCH_CHECK();
+  }
+}
+
 template <typename T>
 void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
                      cudaStream_t st, int pass, int skip_stride) {
@@ -1159,6 +1341,28 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
     case 2: {
       const int n = 3 * N;
       const int rg_s = nrhs >= 4 ? 4 : 1;
+      const C* pk = std::is_same<T, float>::value ? (const C*)pr.pk32.p : (const C*)pr.pk64.p;
+      if (sh.gemv_mode == 2 && pk && pr.gemv_status.p) {
+        // packed symmetric blocks; gemv_chunk is the ring depth in this mode
+        const int nstage = std::min(std::max(sh.gemv_chunk, 2), 8);
+        const size_t smem = packed_smem<T>(n, nstage, rg_s);
+        if (smem <= 227 * 1024) {
+          auto k = rg_s == 4 ? k_block_gemv_packed<T, 4> : k_block_gemv_packed<T, 1>;
+          set_kernel_smem((const void*)k, smem);
+          int fit = 0, dev = 0, nsm = 0;
+          VS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k, 256, smem));
+          VS_CUDA(cudaGetDevice(&dev));
+          VS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+          const int want = sh.gemv_ti > 0 ? std::min(sh.gemv_ti, 4) : 2;
+          const int64_t nblk = (int64_t)(L / 2 + 1) * (M / 2 + 1);
+          const dim3 grid((unsigned)std::min<int64_t>(nblk, (int64_t)nsm * std::max(1, std::min(want, fit))),
+                          ceil_div(nrhs, rg_s));
+          k<<<grid, 256, smem, st>>>(t, pk, pr.pk_stride, L, M, N, (int64_t)L * M * N * 3, nrhs, skip, skip_stride,
+                                     nstage, pr.gemv_status.as<int>());
+          VS_LAUNCH_CHECK();
+          break;
+        }
+      }
       const bool pair = std::is_same<T, float>::value && n % 2 == 0;
       const int want = sh.gemv_ti > 0 ? std::min(sh.gemv_ti, 4) : 2;
       const GemvStream g = gemv_stream_geometry<T>(n, rg_s, sh.gemv_chunk, pair, want);
@@ -1346,6 +1550,19 @@ void autotune_prec(vs_prec& pr, cudaStream_t st) {
         sh.gemv_chunk = cq;
         const float t = time_ms_prec(st, reps, [&] { prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 2); });
         if (t < best) { best = t; bti = ctas; bth = 0; bmode = 1; bchunk = cq; }
+      }
+    }
+    // the packed symmetric kernel over CTAs per SM and ring depth
+    if ((pi == 0 ? pr.pk32.p : pr.pk64.p) != nullptr) {
+      sh.gemv_mode = 2;
+      for (int ctas : {1, 2, 3, 4}) {
+        for (int ns : {2, 3, 4}) {
+          if (packed_smem<T>(n, ns, 1) > 227 * 1024) continue;
+          sh.gemv_ti = ctas;
+          sh.gemv_chunk = ns;
+          const float t = time_ms_prec(st, reps, [&] { prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 2); });
+          if (t < best) { best = t; bti = ctas; bth = 0; bmode = 2; bchunk = ns; }
+        }
       }
     }
     sh.gemv_ti = bti;
