@@ -626,6 +626,14 @@ def run_passes(args):
                 prec.set_shape("c64", gemv_mode=1, gemv_blocks=b, gemv_threads=0, gemv_chunk=cq)
                 gs[f"stream,ctas={b},chunk={cq}"] = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64",
                                                                      args.steps)[2]
+        try:  # packed symmetric blocks, where the preconditioner has them
+            for b in (1, 2, 3, 4):
+                for ns in (2, 3, 4, 6, 8):
+                    prec.set_shape("c64", gemv_mode=2, gemv_blocks=b, gemv_threads=0, gemv_chunk=ns)
+                    gs[f"packed,ctas={b},stages={ns}"] = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64",
+                                                                          args.steps)[2]
+        except Exception as e:  # noqa: BLE001 - reported, not fatal
+            gs["packed"] = f"unavailable: {e}"
         prec.set_shape("c64", **tuned_pr)
         ys_ = {}
         for yr in (0, 1):

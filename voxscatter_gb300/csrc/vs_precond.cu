@@ -991,19 +991,21 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
 // Persistent CTAs over the stored blocks b = blockIdx.x + k*gridDim.x; each
 // whole packed block arrives by one bulk asynchronous copy into a ring of
 // nstage stages (issued nstage blocks ahead, completing on the stage's
-// mbarrier).  Per block: all threads gather the W = 4*RG vectors (mirror and D
-// flips applied), thread (g, p) forms row p over the columns q = g (mod G)
-// from the shared packed block, the G partial rows are summed and scattered.
+// mbarrier).  Per block: thread (g, p) forms row p over the columns q = g
+// (mod G) from the shared packed block and the W = 4*RG vectors in shared
+// memory (mirror and D flips applied), while the loads of the next block's
+// vectors are in flight in registers; the G partial rows are then summed and
+// scattered.
 // Every wait is bounded; a wait that runs out sets status bit 4, all threads
 // leave the loop together, and thread 0 waits (bounded) for its copies still
 // in flight before the CTA ends.
-template <typename T, int RG>
+template <typename T, int RG, int MAXG>
 __global__ void __launch_bounds__(256) k_block_gemv_packed(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ pk,
                                                            int64_t pstride, int L, int M, int N, int64_t rhs_stride,
                                                            int nrhs, const int* skip, int skip_stride, int nstage,
                                                            int* __restrict__ status) {
   using C = cplx_t<T>;
-  constexpr int W = 4 * RG;
+  constexpr int W = 4 * RG;  // gathered entries per thread: n * W <= 256 * MAXG
   const int rhs0 = blockIdx.y * RG;
   const int nr = min(RG, nrhs - rhs0);
   if (skip) {
@@ -1014,9 +1016,9 @@ __global__ void __launch_bounds__(256) k_block_gemv_packed(cplx_t<T>* __restrict
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);  // [8]
   C* stg = reinterpret_cast<C*>(smem_raw + 128);
-  const int n = 3 * N, Lb = L / 2 + 1;
-  C* vt = stg + (size_t)nstage * pstride;  // [n][W]
-  C* red = vt + (size_t)n * W;              // [G][W][n]
+  const int n = 3 * N, Lb = L / 2 + 1, nW = n * W;
+  C* vt0 = stg + (size_t)nstage * pstride;  // 2 x [n][W]
+  C* red = vt0 + (size_t)2 * nW;            // [G][W][n]
   const int64_t nblk = (int64_t)Lb * (M / 2 + 1), LM = (int64_t)L * M;
   const int tid = threadIdx.x;
   const int G = max(1, (int)blockDim.x / n);
@@ -1038,39 +1040,59 @@ __global__ void __launch_bounds__(256) k_block_gemv_packed(cplx_t<T>* __restrict
   };
   if (tid == 0)
     for (; issued < nmine && issued < nstage; ++issued) issue(issued);
-  int64_t k = 0;
-  for (; k < nmine; ++k) {
+  // the W vectors of block k, mirror and D flips applied (both negate the x
+  // and y components), loaded into registers; stored to vt[k & 1] later so
+  // that their latency overlaps the previous block's products
+  C gv[MAXG];
+  auto gather_load = [&](int64_t k) {
     const int blk = (int)blockIdx.x + (int)k * (int)gridDim.x;
     const int js = blk / Lb, is = blk - js * Lb;
-    for (int u = tid; u < n * W; u += blockDim.x) {
-      const int q = u / W, col = u - q * W, var = col & 3, rg = col >> 2;
-      int i, j;
-      C x = czero<C>();
-      if (rg < nr && mirror_of(is, js, var, L, M, i, j)) {
-        x = t[(int64_t)(rhs0 + rg) * rhs_stride + i + (int64_t)L * j + LM * q];
-        const bool fx = var & 1, fy = var >> 1;
-        // mirror flip, then D (both negate the x and y components)
-        const bool neg = q < N ? !fx : (q < 2 * N ? !fy : false);
-        if (neg) { x.x = -x.x; x.y = -x.y; }
+#pragma unroll
+    for (int a = 0; a < MAXG; ++a) {
+      const int u = tid + a * (int)blockDim.x;
+      gv[a] = czero<C>();
+      if (u < nW) {
+        const int q = u / W, col = u - q * W, var = col & 3, rg = col >> 2;
+        int i, j;
+        if (rg < nr && mirror_of(is, js, var, L, M, i, j)) {
+          C x = t[(int64_t)(rhs0 + rg) * rhs_stride + i + (int64_t)L * j + LM * q];
+          const bool fx = var & 1, fy = var >> 1;
+          if (q < N ? !fx : (q < 2 * N ? !fy : false)) { x.x = -x.x; x.y = -x.y; }
+          gv[a] = x;
+        }
       }
-      vt[u] = x;
     }
+  };
+  auto gather_store = [&](int64_t k) {
+    C* vt = vt0 + (size_t)(k & 1) * nW;
+#pragma unroll
+    for (int a = 0; a < MAXG; ++a) {
+      const int u = tid + a * (int)blockDim.x;
+      if (u < nW) vt[u] = gv[a];
+    }
+  };
+  if (nmine > 0) {
+    gather_load(0);
+    gather_store(0);
+  }
+  const int offp = p * n - p * (p - 1) / 2;  // start of stored column p
+  int64_t k = 0;
+  for (; k < nmine; ++k) {
     const int s = (int)(k % nstage);
-    bool ok = mbar_wait(smem_addr(full + s), (uint32_t)((k / nstage) & 1));
+    const bool ok = mbar_wait(smem_addr(full + s), (uint32_t)((k / nstage) & 1));
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicOr(status, 4);
       break;
     }
+    if (k + 1 < nmine) gather_load(k + 1);
     if (active) {
       const C* S = stg + (size_t)s * pstride;
+      const C* vt = vt0 + (size_t)(k & 1) * nW;
       C acc[W];
 #pragma unroll
       for (int c = 0; c < W; ++c) acc[c] = czero<C>();
-      const int64_t offp = (int64_t)p * n - (int64_t)p * (p - 1) / 2;
-      for (int q = g; q < n; q += G) {
-        const int64_t off = q <= p ? (int64_t)q * n - (int64_t)q * (q - 1) / 2 + (p - q) : offp + (q - p);
-        const C m = S[off];
-        const C* xq = vt + (size_t)q * W;
+      auto madd = [&](const C m, int q) {
+        const C* xq = vt + q * W;
         if constexpr (sizeof(C) == 8) {
 #pragma unroll
           for (int c = 0; c < W; c += 2) {
@@ -1082,18 +1104,32 @@ __global__ void __launch_bounds__(256) k_block_gemv_packed(cplx_t<T>* __restrict
 #pragma unroll
           for (int c = 0; c < W; ++c) acc[c] = cfma(m, xq[c], acc[c]);
         }
+      };
+      // columns q = g (mod G): q <= p from stored column q (row p), at
+      // off(q) + p - q, which advances by G (n - q) - G (G + 1) / 2 per step;
+      // q > p from stored column p (row q), at off(p) + q - p
+      int q = g;
+      int o = g * n - g * (g - 1) / 2 + p - g;
+      const int gg2 = G * (G + 1) / 2;
+      for (; q <= p; q += G) {
+        madd(S[o], q);
+        o += G * (n - q) - gg2;
       }
+      for (; q < n; q += G) madd(S[offp + q - p], q);
 #pragma unroll
-      for (int c = 0; c < W; ++c) red[((size_t)g * W + c) * n + p] = acc[c];
+      for (int c = 0; c < W; ++c) red[(g * W + c) * n + p] = acc[c];
     }
+    if (k + 1 < nmine) gather_store(k + 1);
     __syncthreads();
     if (tid == 0 && issued < nmine) issue(issued++);
-    for (int u = tid; u < n * W; u += blockDim.x) {
+    const int blk = (int)blockIdx.x + (int)k * (int)gridDim.x;
+    const int js = blk / Lb, is = blk - js * Lb;
+    for (int u = tid; u < nW; u += blockDim.x) {
       const int col = u / n, q = u - col * n, var = col & 3, rg = col >> 2;
       int i, j;
       if (rg < nr && mirror_of(is, js, var, L, M, i, j)) {
-        C sum = red[(size_t)col * n + q];
-        for (int gg = 1; gg < G; ++gg) sum = cadd(sum, red[((size_t)gg * W + col) * n + q]);
+        C sum = red[col * n + q];
+        for (int h = 1; h < G; ++h) sum = cadd(sum, red[(h * W + col) * n + q]);
         const bool fx = var & 1, fy = var >> 1;
         if (q < N ? fx : (q < 2 * N ? fy : false)) { sum.x = -sum.x; sum.y = -sum.y; }
         t[(int64_t)(rhs0 + rg) * rhs_stride + i + (int64_t)L * j + LM * q] = sum;
@@ -1252,7 +1288,7 @@ int64_t packed_stride(int n) { return ((int64_t)n * (n + 1) / 2 + 15) / 16 * 16;
 template <typename T>
 size_t packed_smem(int n, int nstage, int rg) {
   const int G = std::max(1, 256 / n);
-  return 128 + ((size_t)nstage * packed_stride(n) + (size_t)n * 4 * rg + (size_t)G * 4 * rg * n) * sizeof(cplx_t<T>);
+  return 128 + ((size_t)nstage * packed_stride(n) + 2ull * n * 4 * rg + (size_t)G * 4 * rg * n) * sizeof(cplx_t<T>);
 }
 
 // Packed copies of the inverse blocks for k_block_gemv_packed, in every
@@ -1342,12 +1378,20 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
       const int n = 3 * N;
       const int rg_s = nrhs >= 4 ? 4 : 1;
       const C* pk = std::is_same<T, float>::value ? (const C*)pr.pk32.p : (const C*)pr.pk64.p;
-      if (sh.gemv_mode == 2 && pk && pr.gemv_status.p) {
+      if (sh.gemv_mode == 2 && pk && pr.gemv_status.p && n * 4 * rg_s <= 256 * 16) {
         // packed symmetric blocks; gemv_chunk is the ring depth in this mode
         const int nstage = std::min(std::max(sh.gemv_chunk, 2), 8);
         const size_t smem = packed_smem<T>(n, nstage, rg_s);
         if (smem <= 227 * 1024) {
-          auto k = rg_s == 4 ? k_block_gemv_packed<T, 4> : k_block_gemv_packed<T, 1>;
+          // register slots for the gathered vectors: the fewest that cover n * W
+          const int slots = ceil_div(n * 4 * rg_s, 256);
+          auto pick = [&](auto rgc) {
+            constexpr int R = decltype(rgc)::value;
+            return slots <= 2 ? k_block_gemv_packed<T, R, 2>
+                 : slots <= 4 ? k_block_gemv_packed<T, R, 4>
+                 : slots <= 8 ? k_block_gemv_packed<T, R, 8> : k_block_gemv_packed<T, R, 16>;
+          };
+          auto k = rg_s == 4 ? pick(std::integral_constant<int, 4>{}) : pick(std::integral_constant<int, 1>{});
           set_kernel_smem((const void*)k, smem);
           int fit = 0, dev = 0, nsm = 0;
           VS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k, 256, smem));
