@@ -735,7 +735,7 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 // c64 elements and odd 3N the data may begin one element into the stage (the
 // block buffers carry 64 bytes of tail padding for the rounded-up last copy);
 // PAIR is used only when 3N is even, where every chunk starts aligned.
-template <typename T, int RG, bool PAIR>
+template <typename T, int RG, bool PAIR, bool PACKED = false>
 __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ inv,
                                                            int L, int M, int N, int64_t rhs_stride, int nrhs,
                                                            const int* skip, int skip_stride, int cq, int nstage,
@@ -822,7 +822,8 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
           const int qq = q + k * qstep;
           if (qq >= n) break;
           C x = v[k];
-          if (flip_at(qq)) { x.x = -x.x; x.y = -x.y; }
+          // packed blocks hold S = B D: D (negating the x and y components) on the input
+          if (flip_at(qq) != (PACKED && qq < 2 * N)) { x.x = -x.x; x.y = -x.y; }
           vt[(size_t)qq * W] = x;
         }
       }
@@ -870,9 +871,12 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
         }
         const int c0 = cc * cq;
         const int ncols = min(cq, n - c0);
-        const C* src = inv + (blockIdx.x + kb * gridDim.x) * (int64_t)n * n + (int64_t)c0 * n;
+        // packed: one stage holds a whole padded block (stage_elems entries, 16-byte multiple)
+        const C* src = PACKED ? inv + (blockIdx.x + kb * gridDim.x) * (int64_t)stage_elems
+                              : inv + (blockIdx.x + kb * gridDim.x) * (int64_t)n * n + (int64_t)c0 * n;
         const uintptr_t a = reinterpret_cast<uintptr_t>(src), al = a & ~(uintptr_t)15;
-        const uint32_t bytes = (uint32_t)(((a - al) + (size_t)ncols * n * sizeof(C) + 15) & ~(size_t)15);
+        const uint32_t bytes = PACKED ? (uint32_t)(stage_elems * sizeof(C))
+                                      : (uint32_t)(((a - al) + (size_t)ncols * n * sizeof(C) + 15) & ~(size_t)15);
         const uint32_t bar = smem_addr(full + s);
         mbar_expect_tx(bar, bytes);
         bulk_to_shared_stream(smem_addr(stg + (size_t)s * stage_elems), reinterpret_cast<const void*>(al), bytes, bar,
@@ -908,11 +912,39 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
     for (int h = 0; h < RW; ++h)
 #pragma unroll
       for (int c = 0; c < W; ++c) acc[h][c] = czero<C>();
-    const C* blk = inv + (blockIdx.x + kb * gridDim.x) * (int64_t)n * n;
+    const C* blk = PACKED ? inv : inv + (blockIdx.x + kb * gridDim.x) * (int64_t)n * n;
     for (int cc = 0; cc < cpb && ok; ++cc) {
       ok = !ctl[0] && mbar_wait(smem_addr(full + s), sph);
       if (!ok) break;
-      if (tid < nact) {
+      if (PACKED && tid < nact) {
+        // the lower triangle of S: column q (rows q..n-1) from q n - q (q - 1) / 2;
+        // row rp over the columns q = g (mod G): q <= rp from column q, q > rp
+        // from column rp
+        const C* S = stg + (size_t)s * stage_elems;
+        auto madd = [&](const C m, int q) {
+          const C* xq = vt + (size_t)q * W;
+          if constexpr (sizeof(C) == 8) {
+#pragma unroll
+            for (int c = 0; c < W; c += 2) {
+              const float4 xx = *reinterpret_cast<const float4*>(xq + c);
+              acc[0][c] = cfma(m, make_c<C>(xx.x, xx.y), acc[0][c]);
+              acc[0][c + 1] = cfma(m, make_c<C>(xx.z, xx.w), acc[0][c + 1]);
+            }
+          } else {
+#pragma unroll
+            for (int c = 0; c < W; ++c) acc[0][c] = cfma(m, xq[c], acc[0][c]);
+          }
+        };
+        int q = g;
+        int o = g * n - g * (g - 1) / 2 + rp - g;
+        const int gg2 = G * (G + 1) / 2;
+        for (; q <= rp; q += G) {
+          madd(S[o], q);
+          o += G * (n - q) - gg2;
+        }
+        const int offp = rp * n - rp * (rp - 1) / 2 - rp;
+        for (; q < n; q += G) madd(S[offp + q], q);
+      } else if (tid < nact) {
         const int c0 = cc * cq;
         const int ncols = min(cq, n - c0);
         const int shift = (int)((reinterpret_cast<uintptr_t>(blk + (int64_t)c0 * n) & 15) / sizeof(C));
@@ -979,168 +1011,16 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
   }
 }
 
-// ---- packed symmetric apply ------------------------------------------------
+// ---- packed symmetric blocks ---------------------------------------------
 // With exact operator parity and a uniform block scaling, every inverse block
 // B satisfies B^T = D B D, D = diag(-1 on the x and y components, +1 on z)
 // (the 2-level circulant of a complex-symmetric Toeplitz operator: the block of
 // frequency (-i, -j) is both B^T and D B D), so S = B D is complex symmetric
 // and B x = S (D x).  Only the lower triangle of S is stored, column by column
 // (column q holds rows q..n-1 from offset q n - q (q - 1) / 2), padded to a
-// multiple of 16 entries per block: half the bytes of the full blocks.
-//
-// Persistent CTAs over the stored blocks b = blockIdx.x + k*gridDim.x; each
-// whole packed block arrives by one bulk asynchronous copy into a ring of
-// nstage stages (issued nstage blocks ahead, completing on the stage's
-// mbarrier).  Per block: thread (g, p) forms row p over the columns q = g
-// (mod G) from the shared packed block and the W = 4*RG vectors in shared
-// memory (mirror and D flips applied), while the loads of the next block's
-// vectors are in flight in registers; the G partial rows are then summed and
-// scattered.
-// Every wait is bounded; a wait that runs out sets status bit 4, all threads
-// leave the loop together, and thread 0 waits (bounded) for its copies still
-// in flight before the CTA ends.
-template <typename T, int RG, int MAXG>
-__global__ void __launch_bounds__(256) k_block_gemv_packed(cplx_t<T>* __restrict__ t, const cplx_t<T>* __restrict__ pk,
-                                                           int64_t pstride, int L, int M, int N, int64_t rhs_stride,
-                                                           int nrhs, const int* skip, int skip_stride, int nstage,
-                                                           int* __restrict__ status) {
-  using C = cplx_t<T>;
-  constexpr int W = 4 * RG;  // gathered entries per thread: n * W <= 256 * MAXG
-  const int rhs0 = blockIdx.y * RG;
-  const int nr = min(RG, nrhs - rhs0);
-  if (skip) {
-    bool all = true;
-    for (int g = 0; g < nr; ++g) all = all && skip[(rhs0 + g) * skip_stride];
-    if (all) return;
-  }
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);  // [8]
-  C* stg = reinterpret_cast<C*>(smem_raw + 128);
-  const int n = 3 * N, Lb = L / 2 + 1, nW = n * W;
-  C* vt0 = stg + (size_t)nstage * pstride;  // 2 x [n][W]
-  C* red = vt0 + (size_t)2 * nW;            // [G][W][n]
-  const int64_t nblk = (int64_t)Lb * (M / 2 + 1), LM = (int64_t)L * M;
-  const int tid = threadIdx.x;
-  const int G = max(1, (int)blockDim.x / n);
-  const int g = tid / n, p = tid - g * n;
-  const bool active = g < G;
-  const int64_t nmine = blockIdx.x < nblk ? (nblk - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  const uint32_t bytes = (uint32_t)(pstride * sizeof(C));
-  if (tid == 0) {
-    for (int s = 0; s < nstage; ++s) mbar_init(smem_addr(full + s), 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
-  int64_t issued = 0;
-  auto issue = [&](int64_t k) {  // thread 0: block k of this CTA into stage k % nstage
-    const uint32_t bar = smem_addr(full + (k % nstage));
-    mbar_expect_tx(bar, bytes);
-    bulk_to_shared(smem_addr(stg + (size_t)(k % nstage) * pstride),
-                   pk + (blockIdx.x + k * gridDim.x) * pstride, bytes, bar);
-  };
-  if (tid == 0)
-    for (; issued < nmine && issued < nstage; ++issued) issue(issued);
-  // the W vectors of block k, mirror and D flips applied (both negate the x
-  // and y components), loaded into registers; stored to vt[k & 1] later so
-  // that their latency overlaps the previous block's products
-  C gv[MAXG];
-  auto gather_load = [&](int64_t k) {
-    const int blk = (int)blockIdx.x + (int)k * (int)gridDim.x;
-    const int js = blk / Lb, is = blk - js * Lb;
-#pragma unroll
-    for (int a = 0; a < MAXG; ++a) {
-      const int u = tid + a * (int)blockDim.x;
-      gv[a] = czero<C>();
-      if (u < nW) {
-        const int q = u / W, col = u - q * W, var = col & 3, rg = col >> 2;
-        int i, j;
-        if (rg < nr && mirror_of(is, js, var, L, M, i, j)) {
-          C x = t[(int64_t)(rhs0 + rg) * rhs_stride + i + (int64_t)L * j + LM * q];
-          const bool fx = var & 1, fy = var >> 1;
-          if (q < N ? !fx : (q < 2 * N ? !fy : false)) { x.x = -x.x; x.y = -x.y; }
-          gv[a] = x;
-        }
-      }
-    }
-  };
-  auto gather_store = [&](int64_t k) {
-    C* vt = vt0 + (size_t)(k & 1) * nW;
-#pragma unroll
-    for (int a = 0; a < MAXG; ++a) {
-      const int u = tid + a * (int)blockDim.x;
-      if (u < nW) vt[u] = gv[a];
-    }
-  };
-  if (nmine > 0) {
-    gather_load(0);
-    gather_store(0);
-  }
-  const int offp = p * n - p * (p - 1) / 2;  // start of stored column p
-  int64_t k = 0;
-  for (; k < nmine; ++k) {
-    const int s = (int)(k % nstage);
-    const bool ok = mbar_wait(smem_addr(full + s), (uint32_t)((k / nstage) & 1));
-    if (__syncthreads_or(!ok)) {
-      if (tid == 0) atomicOr(status, 4);
-      break;
-    }
-    if (k + 1 < nmine) gather_load(k + 1);
-    if (active) {
-      const C* S = stg + (size_t)s * pstride;
-      const C* vt = vt0 + (size_t)(k & 1) * nW;
-      C acc[W];
-#pragma unroll
-      for (int c = 0; c < W; ++c) acc[c] = czero<C>();
-      auto madd = [&](const C m, int q) {
-        const C* xq = vt + q * W;
-        if constexpr (sizeof(C) == 8) {
-#pragma unroll
-          for (int c = 0; c < W; c += 2) {
-            const float4 xx = *reinterpret_cast<const float4*>(xq + c);
-            acc[c] = cfma(m, make_c<C>(xx.x, xx.y), acc[c]);
-            acc[c + 1] = cfma(m, make_c<C>(xx.z, xx.w), acc[c + 1]);
-          }
-        } else {
-#pragma unroll
-          for (int c = 0; c < W; ++c) acc[c] = cfma(m, xq[c], acc[c]);
-        }
-      };
-      // columns q = g (mod G): q <= p from stored column q (row p), at
-      // off(q) + p - q, which advances by G (n - q) - G (G + 1) / 2 per step;
-      // q > p from stored column p (row q), at off(p) + q - p
-      int q = g;
-      int o = g * n - g * (g - 1) / 2 + p - g;
-      const int gg2 = G * (G + 1) / 2;
-      for (; q <= p; q += G) {
-        madd(S[o], q);
-        o += G * (n - q) - gg2;
-      }
-      for (; q < n; q += G) madd(S[offp + q - p], q);
-#pragma unroll
-      for (int c = 0; c < W; ++c) red[(g * W + c) * n + p] = acc[c];
-    }
-    if (k + 1 < nmine) gather_store(k + 1);
-    __syncthreads();
-    if (tid == 0 && issued < nmine) issue(issued++);
-    const int blk = (int)blockIdx.x + (int)k * (int)gridDim.x;
-    const int js = blk / Lb, is = blk - js * Lb;
-    for (int u = tid; u < nW; u += blockDim.x) {
-      const int col = u / n, q = u - col * n, var = col & 3, rg = col >> 2;
-      int i, j;
-      if (rg < nr && mirror_of(is, js, var, L, M, i, j)) {
-        C sum = red[col * n + q];
-        for (int h = 1; h < G; ++h) sum = cadd(sum, red[(h * W + col) * n + q]);
-        const bool fx = var & 1, fy = var >> 1;
-        if (q < N ? fx : (q < 2 * N ? fy : false)) { sum.x = -sum.x; sum.y = -sum.y; }
-        t[(int64_t)(rhs0 + rg) * rhs_stride + i + (int64_t)L * j + LM * q] = sum;
-      }
-    }
-  }
-  // copies issued but not consumed (only after a wait ran out) land before the CTA ends
-  if (tid == 0)
-    for (int64_t c = k; c < issued; ++c)
-      if (!mbar_wait(smem_addr(full + (c % nstage)), (uint32_t)((c / nstage) & 1))) atomicOr(status, 4);
-}
+// multiple of 16 entries per block: half the bytes of the full blocks.  The
+// streamed kernel above applies them with PACKED set (one whole block per
+// stage, D folded into the vector gather).
 
 // Lower triangle of S = B D per stored block into the packed layout above.
 template <typename T>
@@ -1281,17 +1161,38 @@ static void launch_prec_plane(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* 
 }
 
 // Packed symmetric blocks: entries per block (the lower triangle padded to a
-// multiple of 16, so every block starts on a 128-byte boundary for c64) and
-// the shared memory of k_block_gemv_packed.
+// multiple of 16, so every block starts on a 128-byte boundary for c64).
 int64_t packed_stride(int n) { return ((int64_t)n * (n + 1) / 2 + 15) / 16 * 16; }
 
+// Streamed-kernel geometry for packed blocks: one whole block per stage,
+// nstage stages (2-8), up to `ctas` CTAs per SM; cq = 0 when two stages do not fit.
 template <typename T>
-size_t packed_smem(int n, int nstage, int rg) {
-  const int G = std::max(1, 256 / n);
-  return 128 + ((size_t)nstage * packed_stride(n) + 2ull * n * 4 * rg + (size_t)G * 4 * rg * n) * sizeof(cplx_t<T>);
+static GemvStream gemv_packed_geometry(int n, int rg, int nstage, int ctas) {
+  const size_t cs = sizeof(cplx_t<T>);
+  GemvStream g{};
+  g.G = std::max(1, std::min(4, 256 / n));
+  g.nc = (g.G * n + 31) / 32 * 32;
+  g.nv = std::max(1, std::min(4, (384 - g.nc - 32) / 32));
+  const size_t vbytes = (size_t)n * 4 * rg * cs;
+  const size_t fixed = 256 + (size_t)2 * vbytes + (size_t)2 * g.G * vbytes;
+  const size_t stage = (size_t)packed_stride(n) * cs;
+  for (int c = std::max(1, std::min(ctas, 4)); c >= 1; --c) {
+    const size_t budget = c == 1 ? 220 * 1024 : (228 * 1024) / c - 1024;
+    int ns = std::min(std::max(nstage, 2), 8);
+    while (ns > 2 && fixed + (size_t)ns * stage > budget) --ns;
+    if (fixed + (size_t)ns * stage > budget) continue;
+    g.cq = n;
+    g.stage_elems = (int)packed_stride(n);
+    g.nstage = ns;
+    g.smem = fixed + (size_t)ns * stage;
+    g.ctas = c;
+    return g;
+  }
+  g.cq = 0;
+  return g;
 }
 
-// Packed copies of the inverse blocks for k_block_gemv_packed, in every
+// Packed copies of the inverse blocks for the streamed kernel, in every
 // precision the preconditioner holds whose two-stage ring fits in shared
 // memory; only for quadrant-symmetric blocks with a uniform scaling (the
 // caller's guarantee that S = B D is symmetric).
@@ -1301,12 +1202,12 @@ void pack_sym_blocks(vs_prec& pr, cudaStream_t st) {
   const int64_t nblk = (int64_t)(pr.L / 2 + 1) * (pr.M / 2 + 1), ps = packed_stride(n);
   pr.pk_stride = ps;
   const int grid = (int)std::min<int64_t>(ceil_div(nblk * ps, 256), 152 * 32);
-  if (pr.inv32.p && packed_smem<float>(n, 2, 1) <= 227 * 1024) {
+  if (pr.inv32.p && gemv_packed_geometry<float>(n, 1, 2, 1).cq > 0) {
     pr.pk32.alloc((size_t)nblk * ps * sizeof(float2));
     k_pack_sym<float><<<grid, 256, 0, st>>>(pr.inv32.as<float2>(), pr.pk32.as<float2>(), n, pr.N, nblk, ps);
     VS_LAUNCH_CHECK();
   }
-  if (pr.inv64.p && packed_smem<double>(n, 2, 1) <= 227 * 1024) {
+  if (pr.inv64.p && gemv_packed_geometry<double>(n, 1, 2, 1).cq > 0) {
     pr.pk64.alloc((size_t)nblk * ps * sizeof(double2));
     k_pack_sym<double><<<grid, 256, 0, st>>>(pr.inv64.as<double2>(), pr.pk64.as<double2>(), n, pr.N, nblk, ps);
     VS_LAUNCH_CHECK();
@@ -1378,31 +1279,22 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
       const int n = 3 * N;
       const int rg_s = nrhs >= 4 ? 4 : 1;
       const C* pk = std::is_same<T, float>::value ? (const C*)pr.pk32.p : (const C*)pr.pk64.p;
-      if (sh.gemv_mode == 2 && pk && pr.gemv_status.p && n * 4 * rg_s <= 256 * 16) {
-        // packed symmetric blocks; gemv_chunk is the ring depth in this mode
-        const int nstage = std::min(std::max(sh.gemv_chunk, 2), 8);
-        const size_t smem = packed_smem<T>(n, nstage, rg_s);
-        if (smem <= 227 * 1024) {
-          // register slots for the gathered vectors: the fewest that cover n * W
-          const int slots = ceil_div(n * 4 * rg_s, 256);
-          auto pick = [&](auto rgc) {
-            constexpr int R = decltype(rgc)::value;
-            return slots <= 2 ? k_block_gemv_packed<T, R, 2>
-                 : slots <= 4 ? k_block_gemv_packed<T, R, 4>
-                 : slots <= 8 ? k_block_gemv_packed<T, R, 8> : k_block_gemv_packed<T, R, 16>;
-          };
-          auto k = rg_s == 4 ? pick(std::integral_constant<int, 4>{}) : pick(std::integral_constant<int, 1>{});
-          set_kernel_smem((const void*)k, smem);
+      if (sh.gemv_mode == 2 && pk && pr.gemv_status.p && n <= 256) {
+        // packed symmetric blocks through the streamed kernel; gemv_chunk is the ring depth here
+        const GemvStream g = gemv_packed_geometry<T>(n, rg_s, sh.gemv_chunk, sh.gemv_ti > 0 ? sh.gemv_ti : 2);
+        if (g.cq > 0) {
+          auto k = rg_s == 4 ? k_block_gemv_stream<T, 4, false, true> : k_block_gemv_stream<T, 1, false, true>;
+          set_kernel_smem((const void*)k, g.smem);
           int fit = 0, dev = 0, nsm = 0;
-          VS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k, 256, smem));
+          const int nthr = g.nc + 32 + 32 * g.nv;
+          VS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k, nthr, g.smem));
           VS_CUDA(cudaGetDevice(&dev));
           VS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-          const int want = sh.gemv_ti > 0 ? std::min(sh.gemv_ti, 4) : 2;
           const int64_t nblk = (int64_t)(L / 2 + 1) * (M / 2 + 1);
-          const dim3 grid((unsigned)std::min<int64_t>(nblk, (int64_t)nsm * std::max(1, std::min(want, fit))),
+          const dim3 grid((unsigned)std::min<int64_t>(nblk, (int64_t)nsm * std::max(1, std::min(g.ctas, fit))),
                           ceil_div(nrhs, rg_s));
-          k<<<grid, 256, smem, st>>>(t, pk, pr.pk_stride, L, M, N, (int64_t)L * M * N * 3, nrhs, skip, skip_stride,
-                                     nstage, pr.gemv_status.as<int>());
+          k<<<grid, nthr, g.smem, st>>>(t, pk, L, M, N, (int64_t)L * M * N * 3, nrhs, skip, skip_stride, g.cq,
+                                        g.nstage, g.stage_elems, g.G, g.nc, g.nv, pr.gemv_status.as<int>());
           VS_LAUNCH_CHECK();
           break;
         }
@@ -1601,7 +1493,8 @@ void autotune_prec(vs_prec& pr, cudaStream_t st) {
       sh.gemv_mode = 2;
       for (int ctas : {1, 2, 3, 4}) {
         for (int ns : {2, 3, 4}) {
-          if (packed_smem<T>(n, ns, 1) > 227 * 1024) continue;
+          const GemvStream pg = gemv_packed_geometry<T>(n, 1, ns, ctas);
+          if (pg.cq == 0 || pg.nstage != ns || pg.ctas != ctas) continue;
           sh.gemv_ti = ctas;
           sh.gemv_chunk = ns;
           const float t = time_ms_prec(st, reps, [&] { prec_apply_pass<T>(pr, x, y, 1, nullptr, st, 2); });
