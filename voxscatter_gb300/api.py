@@ -468,9 +468,10 @@ def pgmresDR(A, b, restart=50, tol=1e-3, maxit=10, ritz=None, L1=None, L2=None, 
     passes it).  GCRO-DR on the device: every cycle of ``restart`` Arnoldi
     steps recycles the ``ritz`` harmonic Ritz vectors of smallest magnitude;
     ``maxit`` counts the cycles after the first, as pgmresDR.m does.  iter =
-    [steps of the last cycle, cycles after the first]; resvec holds the
-    Arnoldi residual estimates relative to ||b||; relres is the true FP64
-    relative residual.  Left preconditioners and a second right factor are
+    [steps of the last cycle, cycles after the first] (with precision "mixed"
+    these count the Arnoldi steps of all refinement solves together); resvec
+    holds the Arnoldi residual estimates relative to ||b||; relres is the
+    true FP64 relative residual.  Left preconditioners and a second right factor are
     not supported."""
     if L1 is not None or L2 is not None or R2 is not None:
         raise NotImplementedError("pgmresDR here takes the preconditioner as R1 only")

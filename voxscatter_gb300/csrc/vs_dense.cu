@@ -39,7 +39,7 @@ std::vector<cd> lu_solve(Mat A, int n, std::vector<cd> b) {
         best = std::abs(A[i + (size_t)k * n]);
         p = i;
       }
-    if (!(best > 0)) throw std::runtime_error("singular matrix in a GCRO-DR least-squares step");
+    if (!(best > 0)) throw Failure("singular matrix in a GCRO-DR least-squares step");
     if (p != k) {
       for (int j = 0; j < n; ++j) std::swap(A[k + (size_t)j * n], A[p + (size_t)j * n]);
       std::swap(b[k], b[p]);
@@ -94,7 +94,7 @@ void sorted_eig(const Mat& A, int n, std::vector<cd>& lam, Mat& X) {
 }  // namespace
 
 void qr_econ(const Mat& A, int r, int c, Mat& Q, Mat& R) {
-  if (r < c) throw std::runtime_error("qr_econ needs rows >= columns");
+  if (r < c) throw Failure("qr_econ needs rows >= columns");
   Mat W = A;
   std::vector<std::vector<cd>> refl(c);
   for (int j = 0; j < c; ++j) {
@@ -144,13 +144,15 @@ std::vector<cd> lstsq(const Mat& A, int r, int c, const std::vector<cd>& rhs) {
   std::vector<cd> y(c);
   for (int j = 0; j < c; ++j) y[j] = dotc(Q.data() + (size_t)j * r, rhs.data(), r);
   for (int i = 0; i < c; ++i)
-    if (!(std::abs(R[i + (size_t)i * c]) > 0)) throw std::runtime_error("rank-deficient GCRO-DR least-squares matrix");
+    if (!(std::abs(R[i + (size_t)i * c]) > 0)) throw Failure("rank-deficient GCRO-DR least-squares matrix");
   Mat Y(y.begin(), y.end());
   Y = left_div_upper(R, c, Y, 1);
   return std::vector<cd>(Y.begin(), Y.end());
 }
 
 Mat right_div_upper(const Mat& B, int r, int c, const Mat& R) {
+  for (int j = 0; j < c; ++j)
+    if (!(std::abs(R[j + (size_t)j * c]) > 0)) throw Failure("singular triangle in a GCRO-DR basis update");
   Mat X((size_t)r * c, 0);
   for (int i = 0; i < r; ++i)
     for (int j = 0; j < c; ++j) {
@@ -168,7 +170,7 @@ void eig(const Mat& A, int n, std::vector<cd>& lam, Mat& X) {
   for (int i = 0; i < n; ++i) z(i, i) = 1;
   double hnorm = 0;
   for (const auto& e : H) hnorm = std::max(hnorm, std::abs(e));
-  if (!std::isfinite(hnorm)) throw std::runtime_error("non-finite matrix in a harmonic Ritz eigenproblem");
+  if (!std::isfinite(hnorm)) throw Failure("non-finite matrix in a harmonic Ritz eigenproblem");
   // Householder reduction to upper Hessenberg form, H = Z^H A Z
   for (int k = 0; k + 2 < n; ++k) {
     const int len = n - k - 1;
@@ -222,7 +224,7 @@ void eig(const Mat& A, int n, std::vector<cd>& lam, Mat& X) {
       iter = 0;
       continue;
     }
-    if (++total > 60 * n) throw std::runtime_error("harmonic Ritz eigenproblem: QR iteration did not converge");
+    if (++total > 60 * n) throw Failure("harmonic Ritz eigenproblem: QR iteration did not converge");
     ++iter;
     cd mu;
     const cd a = h(hi - 1, hi - 1), b = h(hi - 1, hi), c = h(hi, hi - 1), d = h(hi, hi);

@@ -5,6 +5,7 @@
 // hundred), so plain O(n^3) loops are used.
 #pragma once
 #include <complex>
+#include <stdexcept>
 #include <vector>
 
 namespace vs {
@@ -12,6 +13,12 @@ namespace dense {
 
 using cd = std::complex<double>;
 using Mat = std::vector<cd>;
+
+// A numerical failure of one of these routines (singular or rank-deficient
+// matrix, QR iteration without convergence, non-finite input).
+struct Failure : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
 
 // Economy QR of A (r x c, r >= c) by Householder reflections: Q (r x c) with
 // orthonormal columns, R (c x c) upper triangular, A = Q R.

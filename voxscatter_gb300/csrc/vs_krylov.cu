@@ -1464,6 +1464,10 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
     }
     const bool conv = cur.flag == 0;
     const bool more = !conv && steps < maxit;
+    // the small dense problems of the cycle; one that fails (a rank-deficient
+    // least-squares matrix, a harmonic Ritz problem whose QR iteration does not
+    // converge) ends the solve as a breakdown, flag 4, keeping the iterate so far
+    try {
     // B = C^H A M V (kc x kd) and the unrotated Hessenberg ((kd+1) x kd) on the host
     std::vector<double2> bhh((size_t)ld * kd);
     VS_CUDA(cudaMemcpyAsync(bhh.data(), BH, bhh.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
@@ -1542,6 +1546,10 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
         std::swap(U, U2);
         VS_CUDA(cudaMemcpyAsync(Cm, C2, (size_t)kc * n * sizeof(C), cudaMemcpyDeviceToDevice, st));
       }
+    }
+    } catch (const dense::Failure&) {
+      *flag = 4;
+      break;
     }
     if (conv) {
       *flag = 0;
