@@ -31,6 +31,17 @@ METRIC = "solve time to 1e-6 relative residual (BiCGSTAB + 2-level circulant pre
 TOL = 1e-6
 
 
+def _max_over_ranks(value, dist, device):
+    """The largest `value` over all ranks (a replicated job takes as long as
+    its slowest rank); `value` itself without a process group."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _env_int(name, default):
     try:
         return int(os.environ.get(name, default))
@@ -436,11 +447,7 @@ def run_ours(args):
                                           precision=precision))
         ev1.record(stream)
         ev1.synchronize()
-        ms = ev0.elapsed_time(ev1) / steps
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = _max_over_ranks(ev0.elapsed_time(ev1) / steps, dist, "cuda")
         return ms, infos
 
     for _ in range(args.warmup):
