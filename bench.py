@@ -517,7 +517,10 @@ def run_ours(args):
     per_rhs = 8 * (9 * nD + 1.5 * nD + 12 * op.PQR[0] * M * N + 12 * op.PQR[0] * op.PQR[1] * N)
     b16 = pinned + (nb16 - 1) * per_rhs
     del xb, yb
+    # compulsory bytes: read x and write y once, the three diagonals, the spectrum once
+    compulsory = 8 * 7.5 * nD + (pinned - per_rhs)
     matvec = {"ms": mv_total, "pinned_model_bytes": pinned, "GBps_pinned_model": pinned / (mv_total * 1e-3) / 1e9,
+              "compulsory_bytes": compulsory, "GBps_compulsory": compulsory / (mv_total * 1e-3) / 1e9,
               "GBps_own_passes": sum(mv_bytes) / (mv_total * 1e-3) / 1e9, "passes_ms": mv_ms,
               "prec_apply_ms": sum(pc_ms), "prec_passes_ms": pc_ms,
               "prec_GBps": sum(pc_bytes) / (sum(pc_ms) * 1e-3) / 1e9,
