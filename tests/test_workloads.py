@@ -48,3 +48,15 @@ def test_config5_koch_snowflake_grid():
     assert p["refInd"] == 1.78 + 0.005j and np.isclose(p["d"], 0.125)
     nz = np.unique(p["idx"] // (256 * 256))
     assert len(nz) == 16                                      # 2 lambda of thickness at d = lambda/8
+
+
+def test_config5_snowflake_area_matches_koch_formula():
+    """Each filled layer of the level-3 snowflake (circumradius 16 lambda at
+    d = lambda/8) holds as many voxels as the Koch area formula
+    A_n = A_0 (8/5 - 3/5 (4/9)^n), A_0 = 3 sqrt(3)/4 R^2, predicts, to the
+    staircase error of the voxelisation."""
+    p = W.config5()
+    per_layer = len(p["idx"]) / 16
+    R, d, n = 16.0, 0.125, 3
+    area = 3 * np.sqrt(3) / 4 * R ** 2 * (8 / 5 - 3 / 5 * (4 / 9) ** n)
+    assert abs(per_layer - area / d ** 2) < 0.01 * area / d ** 2
