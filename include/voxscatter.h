@@ -141,6 +141,16 @@ int vs_op_apply(vs_op* op, const double* x, double* y, int64_t nrhs, int mode, i
  * double2 for VS_C128), enqueued on the context's stream, no synchronisation. */
 int vs_op_apply_device(vs_op* op, const void* x, void* y, int64_t nrhs, int mode, int precision);
 
+/* vs_op_apply with a Gram of each right-hand side in place of the operator's:
+ * y_r = Gram_r.*Mr.*x_r - Mc.*N(x_r) (and the transposes as in vs_mode), i.e.
+ * MVP.m:1-145 called with that right-hand side's Gram.  The DDA drivers pass
+ * Gram = 1/alpha_LDR (main_DDA.m:75), which getOPERATOR_DDA.m:14-26 computes
+ * from the incident direction and polarisation, so each (kvec, Eo) of a
+ * particle has its own.  gram: nrhs * gram_n complex (host), gram_n = 1 or
+ * L*M*N (column-major grid per right-hand side).  Host buffers as vs_op_apply. */
+int vs_op_apply_gram(vs_op* op, const double* x, double* y, int64_t nrhs, int mode, int precision,
+                     const double* gram, int64_t gram_n);
+
 /* Same as vs_op_apply_device, but allocates nothing: for callers that cannot
  * call cudaMalloc when they apply the operator (while recording a CUDA stream
  * capture, or in services and plug-in hosts that forbid device allocation
@@ -234,6 +244,15 @@ typedef struct vs_solve_opts {
   int transpose;       /* 0: solve A x = b; 1: solve A^T x = b (plain transpose, adjoints)   */
   int restart;         /* VS_GMRES: restart length (Krylov basis size); VS_GMRES_DR: 2..256   */
   int ritz;            /* VS_GMRES_DR: recycled harmonic Ritz vectors, 1..restart-1           */
+  /* Gram of each right-hand side in place of the operator's, as the drivers
+   * pass Gram to every MVP call: NULL = the operator's; else nrhs * gram_n
+   * complex, gram_n = 1 (one value per right-hand side) or L*M*N (a
+   * column-major grid per right-hand side).  DDA: Gram = 1/alpha_LDR of each
+   * incident direction and polarisation (getOPERATOR_DDA.m:14-26 with the
+   * kvec, Eo of main_DDA.m:61-62).  A preconditioner passed with it stays the
+   * one it was built for (it only changes the convergence, not the solution). */
+  const double* gram;
+  int64_t gram_n;
 } vs_solve_opts;
 
 typedef struct vs_solve_info {
@@ -248,7 +267,8 @@ typedef struct vs_solve_info {
 
 /* Fill opts with defaults: BiCGSTAB, MIXED, tol 1e-6, maxit 2000, automatic
  * inner tolerance, 10 refinements, 4 iterations per graph, no resvec, no
- * transpose, GMRES restart 50, 10 recycled vectors for GMRES-DR. */
+ * transpose, GMRES restart 50, 10 recycled vectors for GMRES-DR, the
+ * operator's Gram. */
 void vs_solve_opts_default(vs_solve_opts* opts);
 
 /* Solve A x = b with the (optional, may be NULL) preconditioner, right

@@ -325,3 +325,38 @@ def test_x_lengths_both_x_kernels(api, n):
                     z[prec, x_reg] = pr.apply(x, prec)
             assert rel(z["c128", 1], z["c128", 0]) < 1e-12, L
             assert rel(z["c64", 1], z["c64", 0]) < 2e-6, L
+
+
+@pytest.mark.parametrize("flag", ["notransp", "transp", "plain_transp"])
+@pytest.mark.parametrize("per_voxel", [False, True])
+def test_apply_with_gram_per_rhs(api, flag, per_voxel):
+    """MVP.m called with a different Gram for each right-hand side (the DDA
+    drivers' Gram = 1/alpha_LDR of each incident direction and polarisation):
+    vs_op_apply_gram on three right-hand sides against three oracle MVP calls,
+    with a complex per-voxel Mr so that Gram_r .* Mr (and Gram_r .* conj(Mr) in
+    'transp') is exercised, scalar or per-voxel Gram_r."""
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, chi = _problem(p)
+    fN, Toep, alpha = O.getOPERATOR_DDA(p["r"], p["ko"], p["refInd"], p["kvec"], p["Eo"])
+    dV = p["d"] ** 3
+    rng = np.random.default_rng(31)
+    Mr = 1 + 0.2 * (rng.random((L, M, N)) + 1j * rng.random((L, M, N)))
+    op = api.Operator(L, M, N, idx3, Mr, dV * chi, 1 / alpha, toep=Toep)
+    nrhs = 3
+    X = rng.normal(size=(nrhs, idx3.size)) + 1j * rng.normal(size=(nrhs, idx3.size))
+    if per_voxel:
+        grams = (1 / alpha) * (1 + 0.1 * (rng.normal(size=(nrhs, L, M, N)) + 1j * rng.normal(size=(nrhs, L, M, N))))
+    else:
+        grams = (1 / alpha) * np.array([1.0, 1.013 - 0.004j, 0.987 + 0.02j])
+    for r in range(nrhs):
+        if flag == "plain_transp":
+            y_o = MVP_plain_transpose(X[r], fN, Mr, dV * chi, grams[r], idx3)
+        else:
+            y_o = O.MVP(X[r], fN, Mr, dV * chi, grams[r], flag, idx3)
+        Y128 = op.apply(X.ravel(), flag, "c128", gram=grams).reshape(nrhs, -1)
+        Y64 = op.apply(X.ravel(), flag, "c64", gram=grams).reshape(nrhs, -1)
+        assert rel(Y128[r], y_o) < C128_TOL, r
+        assert rel(Y64[r], y_o) < C64_TOL, r
+    # the operator's own Gram is untouched by a call with per-rhs Grams
+    y0 = O.MVP(X[0], fN, Mr, dV * chi, 1 / alpha, "notransp", idx3)
+    assert rel(op.apply(X[0], "notransp", "c128"), y0) < C128_TOL

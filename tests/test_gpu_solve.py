@@ -151,32 +151,73 @@ def test_config1_gmres_mixed(api):
     assert np.linalg.norm(b - Aor(x)) / np.linalg.norm(b) <= 1e-6 * 1.01
 
 
-@pytest.mark.parametrize("precision,tol", [("mixed", 1e-6), ("fp64", 1e-10)])
-def test_batched_rhs_match_single_solves(api, precision, tol):
-    """8 incident directions x 2 polarisations of one plate solved as one batch:
-    every solution meets tol (FP64 oracle check) and the FP64 batch reproduces
-    the single-rhs iteration counts."""
-    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
-    L, M, N, idx3, Toep, alpha, dV, b0, Aor = _system(p)
-    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
-    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
-    rng = np.random.default_rng(5)
-    B = []
-    for _ in range(8):
+def _directions(p, n, seed):
+    """n random incident directions x 2 polarisations (as the batched
+    configuration draws them): (kvec, pol) pairs."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
         v = rng.normal(size=3); v /= np.linalg.norm(v)
         a = np.cross(v, [0, 0, 1.0]); a /= np.linalg.norm(a)
         for pol in (a, np.cross(v, a)):
-            B.append(O.PlaneWavePointWise(pol, p["ko"] * v, p["r"]).ravel(order="F")[idx3])
-    B = np.array(B)
-    X, infos = api.solve_batch(op, B, pr, tol=tol, precision=precision)
+            out.append((p["ko"] * v, pol))
+    return out
+
+
+@pytest.mark.parametrize("precision,tol", [("mixed", 1e-6), ("fp64", 1e-10)])
+def test_batched_rhs_match_single_solves(api, precision, tol):
+    """8 incident directions x 2 polarisations of one plate solved as one batch,
+    each right-hand side with its own alpha_LDR (getOPERATOR_DDA.m:14-26 takes
+    kvec and Eo, so Gram = 1/alpha differs per direction and polarisation,
+    main_DDA.m:61-62,75).  Every solution meets tol against the oracle
+    operator built with its own alpha, matches a dense direct solve of that
+    operator, and the FP64 batch reproduces the single-rhs solves."""
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, Toep, alpha, dV, b0, Aor = _system(p)
+    fN = O.fft_operator(O.circulant_nop_const(Toep))
+    chi = np.zeros(L * M * N); chi[p["idx"]] = 1
+    chi = chi.reshape((L, M, N), order="F")
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)   # built for the +z, x-pol alpha
+    pairs = _directions(p, 8, 5)
+    B = np.array([O.PlaneWavePointWise(pol, kv, p["r"]).ravel(order="F")[idx3] for kv, pol in pairs])
+    alphas = np.array([O.alpha_ldr(p["refInd"], p["ko"], p["d"], kv, pol) for kv, pol in pairs])
+    # the oblique directions do change the diagonal
+    assert np.max(np.abs(alphas / alpha - 1)) > 1e-3
+    X, infos = api.solve_batch(op, B, pr, tol=tol, precision=precision, gram=1 / alphas)
     for k in range(len(B)):
         assert infos[k]["flag"] == 0, infos[k]
-        assert np.linalg.norm(B[k] - Aor(X[k])) / np.linalg.norm(B[k]) <= tol * 1.01
-    if precision == "fp64":
-        for k in (0, 5, 11):
-            x1, i1, _ = api.solve(op, B[k], pr, tol=tol, precision="fp64")
+        Ak = lambda v: O.MVP(v, fN, np.ones((L, M, N)), dV * chi, 1 / alphas[k], "notransp", idx3)
+        assert np.linalg.norm(B[k] - Ak(X[k])) / np.linalg.norm(B[k]) <= tol * 1.01
+        # against the system with the +z alpha the residual is far larger
+        if abs(alphas[k] / alpha - 1) > 1e-3:
+            assert np.linalg.norm(B[k] - Aor(X[k])) / np.linalg.norm(B[k]) > 10 * tol
+    for k in (0, 5, 11):
+        Ad = O.dense_dda_matrix(p["r"], p["idx"], p["ko"], 1 / alphas[k], dV)
+        xd = np.linalg.solve(Ad, B[k])
+        assert np.linalg.norm(X[k] - xd) / np.linalg.norm(xd) < 100 * tol
+        if precision == "fp64":
+            x1, i1, _ = api.solve(op, B[k], pr, tol=tol, precision="fp64", gram=1 / alphas[k])
             assert i1["iter"] == infos[k]["iter"]
             assert np.linalg.norm(x1 - X[k]) <= 1e-12 * np.linalg.norm(x1)
+
+
+def test_gmres_batch_with_gram_per_rhs(api):
+    """GMRES solves a batch one right-hand side after another, each with its own Gram."""
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.0, nper=4)
+    L, M, N, idx3, Toep, alpha, dV, b0, Aor = _system(p)
+    fN = O.fft_operator(O.circulant_nop_const(Toep))
+    chi = np.zeros(L * M * N); chi[p["idx"]] = 1
+    chi = chi.reshape((L, M, N), order="F")
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pairs = _directions(p, 2, 9)
+    B = np.array([O.PlaneWavePointWise(pol, kv, p["r"]).ravel(order="F")[idx3] for kv, pol in pairs])
+    alphas = np.array([O.alpha_ldr(p["refInd"], p["ko"], p["d"], kv, pol) for kv, pol in pairs])
+    X, infos = api.solve_batch(op, B, None, tol=1e-8, precision="fp64", method="gmres", restart=30, gram=1 / alphas)
+    for k in range(len(B)):
+        assert infos[k]["flag"] == 0
+        Ak = lambda v: O.MVP(v, fN, np.ones((L, M, N)), dV * chi, 1 / alphas[k], "notransp", idx3)
+        assert np.linalg.norm(B[k] - Ak(X[k])) / np.linalg.norm(B[k]) <= 1e-8 * 1.01
 
 
 def _prec_oracle(p, Toep, alpha, dV, idx3):

@@ -44,6 +44,7 @@ SIGNATURES = {
     "vs_op_info": (C.c_int, [_vp, _pi64, _pi64, _pi64]),
     "vs_op_apply": (C.c_int, [_vp, _pd, _pd, _i64, C.c_int, C.c_int]),
     "vs_op_apply_device": (C.c_int, [_vp, _vp, _vp, _i64, C.c_int, C.c_int]),
+    "vs_op_apply_gram": (C.c_int, [_vp, _pd, _pd, _i64, C.c_int, C.c_int, _pd, _i64]),
     "vs_op_apply_device_noalloc": (C.c_int, [_vp, _vp, _vp, _i64, C.c_int, C.c_int]),
     "vs_circ_levels": (C.c_int, [_vp, _i64, _i64, _i64, _pd, _pd, _pd, _pd]),
     "vs_prec_create": (C.c_int, [_vp, _pd, _pd, _i64, C.c_int, C.POINTER(_vp)]),
@@ -62,7 +63,7 @@ class vs_solve_opts(C.Structure):
     _fields_ = [("method", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("maxit", C.c_int),
                 ("inner_tol", C.c_double), ("max_refine", C.c_int), ("iters_per_graph", C.c_int),
                 ("resvec", _pd), ("resvec_cap", _i64), ("transpose", C.c_int), ("restart", C.c_int),
-                ("ritz", C.c_int)]
+                ("ritz", C.c_int), ("gram", _pd), ("gram_n", _i64)]
 
 
 class vs_solve_info(C.Structure):

@@ -168,13 +168,23 @@ class Operator:
         L.check(lib.vs_op_info(h, lmn, pqr, None))
         self.LMN = tuple(lmn); self.PQR = tuple(pqr)
 
-    def apply(self, x, transp_flag="notransp", precision="c64"):
+    def apply(self, x, transp_flag="notransp", precision="c64", gram=None):
+        """y = A x for nrhs = x.size / n3 right-hand sides.  ``gram``: None (the
+        operator's Gram) or one Gram per right-hand side in its place, as an
+        (nrhs,) array of scalars or an (nrhs, L, M, N) array of grids (MVP.m
+        called with each right-hand side's Gram)."""
         x = np.ascontiguousarray(np.asarray(x, dtype=np.complex128))
         nrhs = x.size // self.n3
         assert nrhs * self.n3 == x.size
         y = np.empty_like(x)
-        L.check(self.ctx._lib.vs_op_apply(self.h, L.dptr(x), L.dptr(y), nrhs, _TRANSP[transp_flag],
-                                          L.VS_C64 if precision == "c64" else L.VS_C128), self.ctx.h)
+        prec = L.VS_C64 if precision == "c64" else L.VS_C128
+        if gram is None:
+            L.check(self.ctx._lib.vs_op_apply(self.h, L.dptr(x), L.dptr(y), nrhs, _TRANSP[transp_flag], prec),
+                    self.ctx.h)
+            return y
+        g, gn = _gram_array(gram, nrhs, self.LMN)
+        L.check(self.ctx._lib.vs_op_apply_gram(self.h, L.dptr(x), L.dptr(y), nrhs, _TRANSP[transp_flag], prec,
+                                               L.dptr(g), gn), self.ctx.h)
         return y
 
     def apply_device(self, x, y, transp_flag="notransp"):
@@ -217,6 +227,20 @@ class Operator:
             self.close()
         except Exception:
             pass
+
+
+def _gram_array(gram, nrhs, LMN):
+    """(flat complex array, entries per right-hand side) of a Gram per
+    right-hand side: nrhs scalars, or nrhs column-major (L, M, N) grids."""
+    g = np.asarray(gram, dtype=np.complex128)
+    V = int(np.prod(LMN))
+    if g.size == nrhs:
+        return np.ascontiguousarray(g.ravel()), 1
+    if g.size == nrhs * V:
+        flat = np.ascontiguousarray(g.reshape(nrhs, -1, order="C") if g.ndim == 2 else
+                                    np.stack([gi.ravel(order="F") for gi in g.reshape((nrhs,) + tuple(LMN))]))
+        return flat.ravel(), V
+    raise ValueError(f"gram must hold {nrhs} scalars or {nrhs} grids of {LMN}")
 
 
 def MVP(JIn0, fN, Mr, Mc, Gram, transp_flag, idx, GPU_flag=1, precision="c128", ctx=None):
@@ -377,8 +401,9 @@ def _method(name):
 
 
 def solve(op, b, prec=None, tol=1e-6, maxit=2000, precision="mixed", x0=None, inner_tol=0.0, max_refine=10,
-          iters_per_graph=4, want_resvec=True, transpose=False, method="bicgstab", restart=50, ritz=10):
-    """Device Krylov solve; returns (x, info dict, resvec)."""
+          iters_per_graph=4, want_resvec=True, transpose=False, method="bicgstab", restart=50, ritz=10, gram=None):
+    """Device Krylov solve; returns (x, info dict, resvec).  ``gram``: None or
+    this solve's Gram in place of the operator's (a scalar or an (L, M, N) grid)."""
     lib = op.ctx._lib
     b = np.ascontiguousarray(np.asarray(b, dtype=np.complex128).ravel())
     x = np.zeros_like(b) if x0 is None else np.ascontiguousarray(np.asarray(x0, dtype=np.complex128).ravel()).copy()
@@ -394,6 +419,9 @@ def solve(op, b, prec=None, tol=1e-6, maxit=2000, precision="mixed", x0=None, in
     rv = np.zeros(4 * int(maxit) + 64 if want_resvec else 1)
     if want_resvec:
         o.resvec = L.dptr(rv); o.resvec_cap = rv.size
+    if gram is not None:
+        g, o.gram_n = _gram_array(gram, 1, op.LMN)
+        o.gram = L.dptr(g)
     info = L.vs_solve_info()
     L.check(lib.vs_solve(op.h, prec.h if prec is not None else None, L.dptr(b), L.dptr(x), C.byref(o),
                          C.byref(info)), op.ctx.h)
@@ -598,9 +626,11 @@ def cext_grad(op, prec, Einc, eps, ko, d, kvec, Eo, tol=1e-6, maxit=2000, precis
 
 
 def solve_batch(op, B, prec=None, tol=1e-6, maxit=2000, precision="mixed", method="bicgstab", restart=50,
-                iters_per_graph=4, ritz=10):
-    """Solve A x_r = b_r for every row b_r of B (nrhs x n3) as one batch; returns
-    (X, list of info dicts)."""
+                iters_per_graph=4, ritz=10, gram=None):
+    """Solve A_r x_r = b_r for every row b_r of B (nrhs x n3) as one batch; returns
+    (X, list of info dicts).  ``gram``: None (every A_r is the operator) or the
+    Gram of each right-hand side (nrhs scalars or nrhs (L, M, N) grids), e.g.
+    1/alpha_LDR of each incident direction and polarisation."""
     lib = op.ctx._lib
     B = np.ascontiguousarray(np.asarray(B, dtype=np.complex128))
     nrhs = B.shape[0]
@@ -610,6 +640,9 @@ def solve_batch(op, B, prec=None, tol=1e-6, maxit=2000, precision="mixed", metho
     o.restart = int(restart)
     o.ritz = int(ritz)
     o.iters_per_graph = int(iters_per_graph)
+    if gram is not None:
+        g, o.gram_n = _gram_array(gram, nrhs, op.LMN)
+        o.gram = L.dptr(g)
     infos = (L.vs_solve_info * nrhs)()
     L.check(lib.vs_solve_batch(op.h, prec.h if prec is not None else None, L.dptr(B), L.dptr(X), nrhs, C.byref(o),
                                infos), op.ctx.h)
@@ -645,11 +678,15 @@ def solve_particles_device(ops, precs, b_ptrs, x_ptrs, nrhs, tol=1e-6, maxit=200
 
 
 def solve_batch_device(op, b_ptr, x_ptr, nrhs, prec=None, tol=1e-6, maxit=2000, precision="mixed",
-                       iters_per_graph=4):
-    """vs_solve_batch_device on device buffers (double2, nrhs*n3 each)."""
+                       iters_per_graph=4, gram=None):
+    """vs_solve_batch_device on device buffers (double2, nrhs*n3 each); ``gram``
+    as in solve_batch."""
     lib = op.ctx._lib
     o = _solve_opts(lib, tol, maxit, precision)
     o.iters_per_graph = int(iters_per_graph)
+    if gram is not None:
+        g, o.gram_n = _gram_array(gram, nrhs, op.LMN)
+        o.gram = L.dptr(g)
     infos = (L.vs_solve_info * nrhs)()
     L.check(lib.vs_solve_batch_device(op.h, prec.h if prec is not None else None, C.c_void_p(b_ptr),
                                       C.c_void_p(x_ptr), nrhs, C.byref(o), infos), op.ctx.h)

@@ -108,16 +108,18 @@ void op_common(vs_op* op, const int64_t* idx3, int64_t n3, vs_diag Mr, vs_diag M
   VS_CUDA(cudaMemcpyAsync(op->map3.p, map3.data(), map3.size() * sizeof(int), cudaMemcpyHostToDevice, st));
   VS_CUDA(cudaMemcpyAsync(op->pos2grid.p, p2g.data(), p2g.size() * sizeof(int), cudaMemcpyHostToDevice, st));
   HostDiag mr = check_diag(Mr, V, "Mr"), mc = check_diag(Mc, V, "Mc"), gr = check_diag(Gram, V, "Gram");
-  std::vector<cd> d1(n3), d1c(n3), d2(n3);
+  std::vector<cd> d1(n3), d1c(n3), d2(n3), dmr(n3);
   for (int64_t e = 0; e < n3; ++e) {
     const int64_t vox = idx3[e] % V;
     d1[e] = gr.at(vox) * mr.at(vox);
     d1c[e] = gr.at(vox) * std::conj(mr.at(vox));
     d2[e] = mc.at(vox);
+    dmr[e] = mr.at(vox);
   }
   upload_diag(op->d1, d1, st);
   upload_diag(op->d1c, d1c, st);
   upload_diag(op->d2, d2, st);
+  upload_diag(op->mr, dmr, st);
   VS_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -259,6 +261,10 @@ vs::SolveParams solve_params(vs_op* op, vs_prec* prec, const vs_solve_opts* o) {
   prm.op_mode = o->transpose ? VS_TRANSP : VS_NOTRANSP;
   prm.restart = o->restart;
   prm.ritz = o->ritz;
+  VS_REQUIRE(o->gram == nullptr || o->gram_n == 1 || o->gram_n == op->V,
+             "gram_n must be 1 or L*M*N when a Gram per right-hand side is given");
+  prm.gram_host = reinterpret_cast<const double2*>(o->gram);
+  prm.gram_n = o->gram ? o->gram_n : 0;
   return prm;
 }
 
@@ -295,6 +301,7 @@ void solve_batch_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, in
     for (int64_t r = 0; r < nrhs; ++r) {
       vs::SolveParams p1 = prm;
       p1.resvec_host = prm.resvec_host ? prm.resvec_host + r * prm.resvec_cap : nullptr;
+      p1.gram_host = prm.gram_host ? prm.gram_host + r * prm.gram_n : nullptr;
       vs::SolveResult res;
       if (o->method == VS_GMRES) vs::solve_gmres(*op, prec, b + r * n, x + r * n, p1, res, op->ctx->stream);
       else vs::solve_gmres_dr(*op, prec, b + r * n, x + r * n, p1, res, op->ctx->stream);
@@ -632,6 +639,38 @@ int vs_op_apply(vs_op* op, const double* x, double* y, int64_t nrhs, int mode, i
   });
 }
 
+int vs_op_apply_gram(vs_op* op, const double* x, double* y, int64_t nrhs, int mode, int precision,
+                     const double* gram, int64_t gram_n) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(x && y && gram, "NULL argument");
+    VS_REQUIRE(nrhs >= 1 && nrhs <= 65535, "nrhs must be in [1, 65535]");
+    VS_REQUIRE(precision == VS_C64 || precision == VS_C128, "precision must be VS_C64 or VS_C128");
+    VS_REQUIRE(mode >= VS_NOTRANSP && mode <= VS_CONJTRANSP, "bad mode");
+    cudaStream_t st = op->ctx->stream;
+    vs::DevBuf g64, g32, stage, xd, yd, y64;
+    vs::RhsGram rg;
+    vs::upload_rhs_gram(*op, reinterpret_cast<const double2*>(gram), nrhs, gram_n, g64, g32, rg, st);
+    const int64_t n = op->n3 * nrhs;
+    const bool c64 = precision == VS_C64;
+    upload_as(x, n, c64, stage, xd, st);
+    if (c64) {
+      yd.alloc(n * sizeof(float2));
+      y64.alloc(n * sizeof(double2));
+      vs::ensure_scratch(*op, (int)nrhs, sizeof(float2));
+      vs::matvec<float>(*op, xd.as<float2>(), yd.as<float2>(), (int)nrhs, mode, nullptr, st, 0, &rg);
+      vs::c64_to_c128(yd.as<float2>(), y64.as<double2>(), n, st);
+      VS_CUDA(cudaMemcpyAsync(y, y64.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    } else {
+      yd.alloc(n * sizeof(double2));
+      vs::ensure_scratch(*op, (int)nrhs, sizeof(double2));
+      vs::matvec<double>(*op, xd.as<double2>(), yd.as<double2>(), (int)nrhs, mode, nullptr, st, 0, &rg);
+      VS_CUDA(cudaMemcpyAsync(y, yd.p, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    }
+    VS_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
 // ---- preconditioner ---------------------------------------------------
 
 int vs_circ_levels(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const double* toep, double* circL_out,
@@ -865,6 +904,8 @@ void vs_solve_opts_default(vs_solve_opts* o) {
   o->transpose = 0;
   o->restart = 50;
   o->ritz = 10;
+  o->gram = nullptr;
+  o->gram_n = 0;
 }
 
 
@@ -1230,6 +1271,10 @@ int vs_solve_particles_device(int64_t nparticles, vs_op* const* ops, vs_prec* co
                               void* const* x, const int64_t* nrhs, const vs_solve_opts* opts, vs_solve_info* infos) {
   if (nparticles < 1 || !ops || !b || !x || !nrhs || !opts || !infos) {
     g_last_error = "vs_solve_particles_device: NULL argument or no particles";
+    return VS_ERR_ARG;
+  }
+  if (opts->gram) {
+    g_last_error = "vs_solve_particles_device: opts->gram must be NULL (a Gram per right-hand side belongs to one particle)";
     return VS_ERR_ARG;
   }
   // particles grouped by context: one host thread per context

@@ -60,6 +60,18 @@ struct PassShape {
   int z_df = -1;       // c128 z pass: 1 double-float arithmetic on the FP64 data (two-level kernel only)
 };
 
+// Gram of each right-hand side, in place of the operator's (the reference
+// passes Gram to every MVP call, and the DDA drivers' Gram = 1/alpha_LDR
+// depends on the incident direction and polarisation, getOPERATOR_DDA.m:14-26):
+// nrhs x per complex values at the unknowns, per = 1 (a scalar per
+// right-hand side) or n3.  Empty (g32 == g64 == nullptr): the operator's Gram.
+struct RhsGram {
+  const float2* g32 = nullptr;
+  const double2* g64 = nullptr;
+  int64_t per = 0;
+  bool empty() const { return g32 == nullptr && g64 == nullptr; }
+};
+
 // Work vectors and device scalars of the Krylov solvers (vs_krylov.cu).
 // A captured iteration graph and the buffers/settings it was captured with.
 struct GraphCache {
@@ -87,6 +99,9 @@ struct KrylovWork {
   // the residual, the stacked [C^H A M V; Hessenberg] columns, partial and
   // final Gram products, combination coefficients.
   DevBuf rCV, rU, rU2, rC2, rz, rr, rBH, rgpart, rgram, rcoef;
+  // Gram of each right-hand side of the current solve (empty: the operator's)
+  DevBuf rg32, rg64;
+  RhsGram rg;
   template <typename T> void ensure(int64_t n);
 };
 
@@ -124,6 +139,7 @@ struct vs_op {
   vs::DevBuf pos2grid;  // int32[n3]: grid entry of each unknown
   vs::DevBuf map_all;   // int32[3V]: identity map of whole-domain applies (built on first use)
   VsDiagDev d1, d1c, d2;  // Gram.*Mr, Gram.*conj(Mr), Mc at the unknowns
+  VsDiagDev mr;           // Mr at the unknowns (with a Gram per right-hand side)
   bool gsym = false;    // G holds only the first octant (exact per-axis parity)
   vs::DevBuf G32, G64;  // spectrum of the embedded tensor / (P*Q*R): 6 x P*Q*R, or 6 x octant
   vs::DevBuf toep64;    // first-octant Toeplitz tensor, L*M*N*6 (double2)
@@ -160,9 +176,10 @@ struct vs_prec {
 namespace vs {
 
 // Launchers (vs_matvec.cu)
+// rg: optional Gram of each right-hand side (nullptr or empty: the operator's).
 template <typename T>
 void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
-                 cudaStream_t st, int pass, int skip_stride = 0);
+                 cudaStream_t st, int pass, int skip_stride = 0, const RhsGram* rg = nullptr);
 template <typename T>
 void matvec_scratch(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, cplx_t<T>* t1,
                     cplx_t<T>* t2, cudaStream_t st);
@@ -170,8 +187,13 @@ void matvec_scratch(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs,
 // skip[r * skip_stride] != 0.
 template <typename T>
 void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
-            cudaStream_t st, int skip_stride = 0);
+            cudaStream_t st, int skip_stride = 0, const RhsGram* rg = nullptr);
 void ensure_scratch(vs_op& op, int nrhs, size_t elem_bytes);
+// Uploads a Gram per right-hand side (host, nrhs x gram_n complex with
+// gram_n = 1 or L*M*N, a column-major grid) to g64 / g32 at op's unknowns and
+// describes it in `out`.
+void upload_rhs_gram(const vs_op& op, const double2* gram, int64_t nrhs, int64_t gram_n, DevBuf& g64, DevBuf& g32,
+                     RhsGram& out, cudaStream_t st);
 
 // Generic batched FFT passes (vs_matvec.cu)
 template <typename T, bool INV>

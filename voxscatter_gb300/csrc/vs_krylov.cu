@@ -434,6 +434,20 @@ constexpr int kStagnationWindow = 8;
 
 static int vec_grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), kRedBlocks)); }
 
+// The Gram per right-hand side of the current solve, or nullptr (the operator's).
+static const RhsGram* rgp(const KrylovWork& w) { return w.rg.empty() ? nullptr : &w.rg; }
+
+// Installs the solve's Gram per right-hand side (if any) on the work buffers
+// for the duration of one solve.
+struct RhsGramScope {
+  KrylovWork& w;
+  RhsGramScope(const vs_op& op, KrylovWork& wk, const SolveParams& prm, int nrhs, cudaStream_t st) : w(wk) {
+    w.rg = RhsGram{};
+    if (prm.gram_host) upload_rhs_gram(op, prm.gram_host, nrhs, prm.gram_n, w.rg64, w.rg32, w.rg, st);
+  }
+  ~RhsGramScope() { w.rg = RhsGram{}; }
+};
+
 // ---- host driver ---------------------------------------------------------
 
 template <typename T>
@@ -487,13 +501,13 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
   k_bicg_p<T><<<g, 256, 0, st>>>(p, r, v, n, s);
   if (pr) prec_apply<T>(*pr, p, ph, nrhs, skip, st, ss);
   else k_copy<T><<<dim3(vec_grid(n * nrhs)), 256, 0, st>>>(ph, p, n * nrhs);
-  matvec<T>(op, ph, v, nrhs, mode, skip, st, ss);
+  matvec<T>(op, ph, v, nrhs, mode, skip, st, ss, rgp(w));
   k_bicg_alpha<T><<<g, kRedThreads, 0, st>>>(rt, v, n, s);
   k_bicg_s<T><<<g, kRedThreads, 0, st>>>(sv, r, v, n, s);
   k_bicg_xhalf<T><<<g, kRedThreads, 0, st>>>(x, ph, n, s);
   if (pr) prec_apply<T>(*pr, sv, sh, nrhs, skip, st, ss);
   else k_copy<T><<<dim3(vec_grid(n * nrhs)), 256, 0, st>>>(sh, sv, n * nrhs);
-  matvec<T>(op, sh, t, nrhs, mode, skip, st, ss);
+  matvec<T>(op, sh, t, nrhs, mode, skip, st, ss, rgp(w));
   k_bicg_omega<T><<<g, kRedThreads, 0, st>>>(t, sv, n, s);
   k_bicg_xr<T><<<g, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, rt, n, s);
   VS_LAUNCH_CHECK();
@@ -560,7 +574,7 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
                                   w.state.p, w.partials.p, op.t1.p, op.t2.p,
                                   (const void*)(uintptr_t)(pr ? pr->id : 0), pr ? pr->t.p : nullptr,
                                   (const void*)(uintptr_t)per_graph, (const void*)(uintptr_t)mode,
-                                  (const void*)(uintptr_t)nrhs};
+                                  (const void*)(uintptr_t)nrhs, w.rg.g32, w.rg.g64, (const void*)(uintptr_t)w.rg.per};
   if (gc.exec == nullptr || gc.key != key) {
     gc.reset();
     // One launch sequence with every rhs skipped, outside capture: all
@@ -624,7 +638,7 @@ static std::vector<double> residuals64(const vs_op& op, KrylovWork& w, const dou
   std::vector<KState> h(nrhs);
   upload_states(w, h, st);
   double2* y = w.y64.as<double2>();
-  matvec<double>(op, x, y, nrhs, mode, nullptr, st);
+  matvec<double>(op, x, y, nrhs, mode, nullptr, st, 0, rgp(w));
   k_resid64<<<dim3(vec_grid(n), nrhs), kRedThreads, 0, st>>>(b, y, r, n, w.state.as<KState>(), w.scal.as<double>());
   VS_LAUNCH_CHECK();
   *launches += 6;
@@ -644,6 +658,7 @@ void solve_bicgstab_batch(vs_op& op, vs_prec* pr, const double2* b, double2* x, 
                           std::vector<SolveResult>& out, cudaStream_t st) {
   const int64_t n = op.n3;
   KrylovWork& w = op.kw;
+  RhsGramScope gram_scope(op, w, prm, nrhs, st);
   reduction_buffers(w, nrhs);
   const int cap = prm.resvec_cap;
   w.resvec.alloc((size_t)std::max(1, cap) * nrhs * sizeof(double));
@@ -1050,7 +1065,7 @@ static int gmres_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t
     if (cycle == 0) {
       minv(rin, V);
     } else {
-      matvec<T>(op, d, tmp, 1, op_mode, nullptr, st);
+      matvec<T>(op, d, tmp, 1, op_mode, nullptr, st, 0, rgp(w));
       k_sub<T><<<g, 256, 0, st>>>(rin, tmp, tmp, n);
       minv(tmp, V);
       *launches += 6;
@@ -1091,7 +1106,7 @@ static int gmres_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t
     int issued = 0;
     for (int k = 0; k < kmax; ++k) {
       const C* vk = V + (int64_t)k * n;
-      matvec<T>(op, vk, tmp, 1, op_mode, &gs->skip, st);
+      matvec<T>(op, vk, tmp, 1, op_mode, &gs->skip, st, 0, rgp(w));
       minv(tmp, wv);
       double2* Hcol = H + (int64_t)k * (m + 1);
       for (int pass = 0; pass < 2; ++pass) {
@@ -1427,7 +1442,7 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
     GState cur{};
     for (int k = 0; k < kmax; ++k) {
       rprec(V + (int64_t)k * n, tmp, &gs->skip);
-      matvec<T>(op, tmp, wv, 1, op_mode, &gs->skip, st);
+      matvec<T>(op, tmp, wv, 1, op_mode, &gs->skip, st, 0, rgp(w));
       *launches += 5;
       double2* col = BH + (int64_t)k * ld;
       const int nb = kc + k + 1;  // C_0..C_kc-1, V_0..V_k
@@ -1635,6 +1650,7 @@ static void solve_gmres_impl(vs_op& op, vs_prec* pr, const double2* b, double2* 
                              SolveResult& out, cudaStream_t st) {
   const int64_t n = op.n3;
   KrylovWork& w = op.kw;
+  RhsGramScope gram_scope(op, w, prm, 1, st);
   reduction_buffers(w, 1);
   std::vector<KState> zero(1);
   upload_states(w, zero, st);

@@ -42,6 +42,10 @@ struct SolveParams {
   int op_mode = 0;  // VS_NOTRANSP: solve A x = b; VS_TRANSP: solve A^T x = b
   int restart = 50; // GMRES restart length
   int ritz = 10;     // GCRO-DR: recycled harmonic Ritz vectors
+  // Gram of each right-hand side (host, nrhs x gram_n complex, gram_n = 1 or
+  // L*M*N) in place of the operator's; nullptr: the operator's
+  const double2* gram_host = nullptr;
+  int64_t gram_n = 0;
 };
 
 struct SolveResult {

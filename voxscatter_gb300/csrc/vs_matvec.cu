@@ -126,9 +126,9 @@ __global__ void __launch_bounds__(kThreads) k_xi(PipeArgs<T> a) {
       out = conv;
     } else {
       const C xv = x[pos];
-      if (MODE == VS_NOTRANSP) out = csub(cmul(a.d1.at(pos), xv), cmul(a.d2.at(pos), conv));
-      else if (MODE == VS_TRANSP) out = csub(cmul(a.d1.at(pos), xv), conv);
-      else out = csub(cmul(a.d1c.at(pos), xv), cconj(conv));
+      if (MODE == VS_NOTRANSP) out = csub(cmul(diag_term(a, pos, rhs, false), xv), cmul(a.d2.at(pos), conv));
+      else if (MODE == VS_TRANSP) out = csub(cmul(diag_term(a, pos, rhs, false), xv), conv);
+      else out = csub(cmul(diag_term(a, pos, rhs, true), xv), cconj(conv));
     }
     y[pos] = out;
   }
@@ -345,7 +345,7 @@ static StridedArgs<T> y_pass_args(const vs_op& op, const PipeArgs<T>& a, bool in
 
 template <typename T>
 static PipeArgs<T> pipe_args(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, const int* skip,
-                             int skip_stride = 0) {
+                             int skip_stride = 0, const RhsGram* rg = nullptr) {
   using C = cplx_t<T>;
   PipeArgs<T> a{};
   a.L = op.L; a.M = op.M; a.N = op.N; a.P = op.P; a.Q = op.Q; a.R = op.R;
@@ -355,6 +355,15 @@ static PipeArgs<T> pipe_args(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, 
   a.d1 = {op.d1.ptr<T>(), mk<C>(op.d1.s.x, op.d1.s.y)};
   a.d1c = {op.d1c.ptr<T>(), mk<C>(op.d1c.s.x, op.d1c.s.y)};
   a.d2 = {op.d2.ptr<T>(), mk<C>(op.d2.s.x, op.d2.s.y)};
+  a.mr = {op.mr.ptr<T>(), mk<C>(op.mr.s.x, op.mr.s.y)};
+  a.grhs = nullptr;
+  a.grhs_per = 0;
+  if (rg && !rg->empty()) {
+    const C* g = std::is_same<T, float>::value ? (const C*)rg->g32 : (const C*)rg->g64;
+    VS_REQUIRE(g != nullptr, "Gram per right-hand side missing in this precision");
+    a.grhs = g;
+    a.grhs_per = rg->per;
+  }
   a.t1 = op.t1.as<C>();
   a.t2 = op.t2.as<C>();
   a.G = std::is_same<T, float>::value ? (const C*)op.G32.p : (const C*)op.G64.p;
@@ -401,10 +410,10 @@ static void launch_z(const vs_op& op, const PipeArgs<T>& a, int nrhs, cudaStream
 
 template <typename T>
 void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
-                 cudaStream_t st, int pass, int skip_stride) {
+                 cudaStream_t st, int pass, int skip_stride, const RhsGram* rg) {
   using C = cplx_t<T>;
   VS_REQUIRE(mode >= VS_NOTRANSP && mode <= VS_CONJTRANSP, "mode must be VS_NOTRANSP, VS_TRANSP or VS_CONJTRANSP");
-  const PipeArgs<T> a = pipe_args<T>(op, x, y, skip, skip_stride);
+  const PipeArgs<T> a = pipe_args<T>(op, x, y, skip, skip_stride, rg);
   switch (pass) {
     case 0: launch_x_pass<T>(a, false, mode, nrhs, st); break;
     case 1: launch_strided_pass<T, false>(y_pass_args<T>(op, a, false), op.N * 3, nrhs, st); break;
@@ -416,8 +425,51 @@ void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, in
 
 template <typename T>
 void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
-            cudaStream_t st, int skip_stride) {
-  for (int pass = 0; pass < 5; ++pass) matvec_pass<T>(op, x, y, nrhs, mode, skip, st, pass, skip_stride);
+            cudaStream_t st, int skip_stride, const RhsGram* rg) {
+  for (int pass = 0; pass < 5; ++pass) matvec_pass<T>(op, x, y, nrhs, mode, skip, st, pass, skip_stride, rg);
+}
+
+// Gram per right-hand side at the unknowns: out[r * n3 + e] = grid[r * V + vox(e)]
+// with vox(e) = pos2grid[e] mod V.
+__global__ void k_rhs_gram_gather(const double2* __restrict__ grid, const int* __restrict__ pos2grid, int64_t n3,
+                                  int64_t V, int64_t nrhs, double2* __restrict__ o64, float2* __restrict__ o32) {
+  const int64_t total = n3 * nrhs;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / n3, e = i - r * n3;
+    const double2 v = grid[r * V + pos2grid[e] % V];
+    o64[i] = v;
+    o32[i] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+void upload_rhs_gram(const vs_op& op, const double2* gram, int64_t nrhs, int64_t gram_n, DevBuf& g64, DevBuf& g32,
+                     RhsGram& out, cudaStream_t st) {
+  VS_REQUIRE(gram != nullptr, "Gram per right-hand side is NULL");
+  VS_REQUIRE(gram_n == 1 || gram_n == op.V, "Gram per right-hand side must have 1 or L*M*N entries each");
+  VS_REQUIRE(nrhs >= 1, "nrhs must be >= 1");
+  for (int64_t i = 0; i < nrhs * gram_n; ++i)
+    VS_REQUIRE(std::isfinite(gram[i].x) && std::isfinite(gram[i].y), "Gram per right-hand side is not finite");
+  const int64_t per = gram_n == 1 ? 1 : op.n3;
+  g64.alloc(nrhs * per * sizeof(double2));
+  g32.alloc(nrhs * per * sizeof(float2));
+  if (gram_n == 1) {
+    std::vector<float2> f(nrhs);
+    for (int64_t r = 0; r < nrhs; ++r) f[r] = make_float2((float)gram[r].x, (float)gram[r].y);
+    VS_CUDA(cudaMemcpyAsync(g64.p, gram, nrhs * sizeof(double2), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemcpyAsync(g32.p, f.data(), nrhs * sizeof(float2), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaStreamSynchronize(st));  // f is released on return
+  } else {
+    DevBuf raw;
+    raw.alloc(nrhs * op.V * sizeof(double2));
+    VS_CUDA(cudaMemcpyAsync(raw.p, gram, nrhs * op.V * sizeof(double2), cudaMemcpyHostToDevice, st));
+    k_rhs_gram_gather<<<(int)std::min<int64_t>(ceil_div(nrhs * op.n3, 256), 152 * 16), 256, 0, st>>>(
+        raw.as<double2>(), op.pos2grid.as<int>(), op.n3, op.V, nrhs, g64.as<double2>(), g32.as<float2>());
+    VS_LAUNCH_CHECK();
+    VS_CUDA(cudaStreamSynchronize(st));  // raw is released on return
+  }
+  out.g64 = g64.as<double2>();
+  out.g32 = g32.as<float2>();
+  out.per = per;
 }
 
 template void launch_x_pass<float>(const PipeArgs<float>&, bool, int, int, cudaStream_t);
@@ -471,10 +523,14 @@ template void matvec_scratch<float>(const vs_op&, const float2*, float2*, int, i
 template void matvec_scratch<double>(const vs_op&, const double2*, double2*, int, int, double2*, double2*,
                                      cudaStream_t);
 
-template void matvec_pass<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t, int, int);
-template void matvec_pass<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t, int, int);
-template void matvec<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t, int);
-template void matvec<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t, int);
+template void matvec_pass<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t, int, int,
+                                 const RhsGram*);
+template void matvec_pass<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t, int, int,
+                                  const RhsGram*);
+template void matvec<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t, int,
+                            const RhsGram*);
+template void matvec<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t, int,
+                             const RhsGram*);
 
 // ---- generic batched FFTs (operator setup, preconditioner) --------------
 template <typename T, bool INV>

@@ -36,7 +36,26 @@ struct PipeArgs {
   const int* skip;   // right-hand side r is skipped when skip[r * skip_stride] != 0
   int skip_stride;
   int two_level;     // x passes: 1 two-level register kernel (vs_xpass.cuh) when P has one
+  // Gram of each right-hand side in place of the operator's (the reference
+  // passes Gram to every MVP call; DDA's Gram = 1/alpha_LDR depends on the
+  // incident direction and polarisation): Gram_r(pos) = grhs[r * grhs_per +
+  // (grhs_per > 1 ? pos : 0)], and the diagonal term is Gram_r .* Mr.
+  // nullptr: the operator's own d1 / d1c.
+  const C* grhs;
+  int64_t grhs_per;
+  DiagArg<C> mr;
 };
+
+// Diagonal coefficient of the XI epilogue at unknown `pos` of right-hand side
+// `rhs`: Gram.*Mr, or Gram.*conj(Mr) for VS_CONJTRANSP (MVP.m:72-98 conjugates
+// Mr but not Gram).
+template <typename T>
+__device__ __forceinline__ cplx_t<T> diag_term(const PipeArgs<T>& a, int pos, int rhs, bool conj_mr) {
+  if (a.grhs == nullptr) return conj_mr ? a.d1c.at(pos) : a.d1.at(pos);
+  const cplx_t<T> g = a.grhs[rhs * a.grhs_per + (a.grhs_per > 1 ? pos : 0)];
+  const cplx_t<T> m = a.mr.at(pos);
+  return cmul(g, conj_mr ? cconj(m) : m);
+}
 
 // ---- strided-axis pass (y of the pipeline; y and z of the setup FFTs) ----
 // Lines run along a strided axis; a CTA owns an x-tile of `tx` columns of one

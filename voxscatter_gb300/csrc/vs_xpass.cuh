@@ -145,9 +145,9 @@ __global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
           out = conv;
         } else {
           const C xv = x[pos];
-          if (mode == VS_NOTRANSP) out = csub(cmul(a.d1.at(pos), xv), cmul(a.d2.at(pos), conv));
-          else if (mode == VS_TRANSP) out = csub(cmul(a.d1.at(pos), xv), conv);
-          else out = csub(cmul(a.d1c.at(pos), xv), cconj(conv));
+          if (mode == VS_NOTRANSP) out = csub(cmul(diag_term(a, pos, rhs, false), xv), cmul(a.d2.at(pos), conv));
+          else if (mode == VS_TRANSP) out = csub(cmul(diag_term(a, pos, rhs, false), xv), conv);
+          else out = csub(cmul(diag_term(a, pos, rhs, true), xv), cconj(conv));
         }
         y[pos] = out;
       }
