@@ -55,15 +55,16 @@ def _workload():
     return p
 
 
-def _config_dict(p, PQR=None):
+def _config_dict(p, world=1):
+    """The workload as both arms describe it (the FFT grid each arm embeds the
+    same Toeplitz operator in is reported beside it as ``fft_grid``)."""
     L, M, N = p["L"], p["M"], p["N"]
-    d = {"workload": f"hex plate D=8 lambda, t=2 lambda, m=1.31+0.01i, grid {L}x{M}x{N}, "
-                     f"{len(p['idx'])} dipoles, {3 * len(p['idx'])} unknowns, +z incidence, x-pol",
-         "tol": TOL, "solver": "BiCGSTAB, right 2-level circulant preconditioner",
-         "l2": "inputs larger than L2 (c64 Green spectrum ~103 MB + preconditioner blocks ~465 MB read per iteration)"}
-    if PQR:
-        d["fft_grid"] = "x".join(str(v) for v in PQR)
-    return d
+    return {"workload": f"hex plate D=8 lambda, t=2 lambda, m=1.31+0.01i, grid {L}x{M}x{N}, "
+                        f"{len(p['idx'])} dipoles, {3 * len(p['idx'])} unknowns, +z incidence, x-pol",
+            "tol": TOL, "solver": "BiCGSTAB, right 2-level circulant preconditioner",
+            "l2": "inputs larger than L2: preconditioner blocks (118.7 MB c64), Green spectrum and ~10 "
+                  "solution-sized vectors, ~180 MB read per iteration against a 129 MB L2",
+            "parallelism": f"replicas x{world}"}
 
 
 def _peaks():
@@ -248,13 +249,15 @@ def run_reference(args):
     per = [_cpu_iteration_seconds(A, Pm, b, sample_iters) for _ in range(args.steps)]
     per_it = float(np.median(per))
     value_ms = per_it * it_needed * 1e3
-    sample = (f"{sample_iters} BiCGSTAB iterations per step of the FP64 NumPy/SciPy restatement "
+    sample = (f"one replica's solve on rank 0: {sample_iters} BiCGSTAB iterations per step of the FP64 "
+              f"NumPy/SciPy restatement "
               f"(scipy.fft workers={workers}); solve = median s/iteration x {it_needed} iterations "
               f"(full untimed reference solve: flag {flag}, relres {relres:.2e})")
     line = {"impl": "reference", "metric": METRIC, "value": value_ms, "unit": "ms", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_it * sample_iters * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-            "data": "synthetic (seeded reference-rule geometry)", "config": _config_dict(p),
+            "data": "synthetic (seeded reference-rule geometry)", "config": _config_dict(p, args.gpus),
+            "fft_grid": "x".join(str(2 * v) for v in (p["L"], p["M"], p["N"])),
             "iterations": it_needed,
             "cpu_baseline": {"value": value_ms, "unit": "ms", "cores": workers, "kind": "port", "sample": sample},
             "e2e": {"value": value_ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -536,7 +539,7 @@ def run_ours(args):
             "vs_baseline": None,
             "dtype": "c64 (refinement residual on FP64 data, its z FFTs in double-float when faster; FP64 dots, norms)",
             "data": "synthetic (seeded reference-rule geometry, plane-wave RHS)",
-            "config": dict(_config_dict(p, op.PQR), parallelism=f"replicas x{world}"),
+            "config": _config_dict(p, world), "fft_grid": "x".join(str(v) for v in op.PQR),
             "converged": ok, "relres": last["relres"], "iterations": last["iter"],
             "refinements": last["refinements"],
             "fp64_solve_ms": ms_fp64, "fp64_iterations": infos64[-1]["iter"],

@@ -152,15 +152,18 @@ int vs_op_apply_gram(vs_op* op, const double* x, double* y, int64_t nrhs, int mo
                      const double* gram, int64_t gram_n);
 
 /* Same as vs_op_apply_device, but allocates nothing: for callers that cannot
- * call cudaMalloc when they apply the operator (while recording a CUDA stream
- * capture, or in services and plug-in hosts that forbid device allocation
- * after start-up).  No counterpart in the reference (its MVP.m allocates
- * freely).  The pipeline intermediates (P*M*N*3 + P*Q*N*3 elements per
- * right-hand side, plus 256 bytes of alignment) live in a 64 MiB array the
- * library reserves on every device that loads it, until the process exits;
- * larger requests return VS_ERR_UNSUPPORTED.  The first call on a device looks
- * up the array's address: make it before any stream capture.  All calls share
- * the array: calls whose GPU work overlaps race and must be serialised. */
+ * call cudaMalloc when they apply the operator (services and plug-in hosts
+ * that reserve their device memory at start-up and forbid allocation
+ * afterwards, or that run inside a memory budget owned by another allocator,
+ * such as a MEX function in MATLAB's GPU memory pool).  No counterpart in the
+ * reference (its MVP.m allocates freely).  The pipeline intermediates
+ * (P*M*N*3 + P*Q*N*3 elements per right-hand side, plus 256 bytes of
+ * alignment) live in a 64 MiB array the library reserves on every device that
+ * loads it, until the process exits; larger requests return
+ * VS_ERR_UNSUPPORTED.  The first call on a device looks up the array's address
+ * and caches it for the process (do not reset the device meanwhile): make that
+ * first call before any stream capture.  All calls share the array: calls whose
+ * GPU work overlaps race and must be serialised. */
 int vs_op_apply_device_noalloc(vs_op* op, const void* x, void* y, int64_t nrhs, int mode, int precision);
 
 /* ---- 2-level circulant preconditioner ------------------------------- */

@@ -318,6 +318,11 @@ void solve_batch_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, in
 
 }  // namespace
 
+void record_error(vs_ctx* ctx, const char* msg) {
+  g_last_error = msg;
+  if (ctx) ctx->err = msg;
+}
+
 void ctx_retain(vs_ctx* ctx) {
   if (ctx) ctx->refs.fetch_add(1);
 }

@@ -119,6 +119,9 @@ struct vs_ctx {
 };
 void ctx_retain(vs_ctx* ctx);
 void ctx_release(vs_ctx* ctx);
+// Records a failure message where vs_last_error() reads it: on the context
+// (if any) and as this thread's last error.
+void record_error(vs_ctx* ctx, const char* msg);
 
 // Diagonal coefficients of an operator at the n3 unknown positions.
 struct VsDiagDev {

@@ -1,19 +1,22 @@
 // Allocation-free operator apply.
 //
 // Some callers cannot allocate device memory at the moment they need a matvec:
-// code recording a CUDA stream capture (cudaMalloc is not a stream operation
-// and breaks or invalidates the capture), services that reserve all their
-// device memory at start-up and forbid allocation afterwards, and MEX or
-// plug-in hosts that run the solver inside a memory budget owned by someone
-// else.  vs_op_apply_device allocates its pipeline intermediates on demand;
-// this entry point instead runs the same fused pipeline with its
-// intermediates in one statically sized device array that the library owns.
+// services that reserve all their device memory at start-up and forbid
+// allocation afterwards, and MEX or plug-in hosts that run the solver inside a
+// device-memory budget owned by another allocator (MATLAB's GPU memory pool,
+// a framework's caching allocator), where a cudaMalloc of the library's own
+// either fails or competes with the host.  vs_op_apply_device allocates its
+// pipeline intermediates on demand; this entry point instead runs the same
+// fused pipeline with its intermediates in one statically sized device array
+// that the library owns.
 //
 // The array is kNoAllocScratchBytes (64 MiB) of file-scope __device__ memory:
 // every GPU that loads the library holds it until the process exits.  Its
 // device address is looked up once per device (cudaGetSymbolAddress), by the
-// first call made with that device current; make that first call before any
-// stream capture.  All calls share the array and it keeps the last call's
+// first call made with that device current, and cached for the life of the
+// process: this assumes the device's primary context is not reset
+// (cudaDeviceReset) while the library is in use.  Make that first call before
+// any stream capture.  All calls share the array and it keeps the last call's
 // contents; the pipeline writes every scratch element before reading it, so
 // nothing needs clearing.  Two calls whose work overlaps on the GPU (other
 // streams, other host threads) race on the array: serialise them.
@@ -75,10 +78,10 @@ extern "C" int vs_op_apply_device_noalloc(vs_op* op, const void* x, void* y, int
                                  (double2*)(base + off2), st);
     return VS_OK;
   } catch (const vs::Error& e) {
-    op->ctx->err = e.what();
+    record_error(op->ctx, e.what());
     return e.status;
   } catch (const std::exception& e) {
-    op->ctx->err = e.what();
+    record_error(op->ctx, e.what());
     return VS_ERR_CUDA;
   }
 }
