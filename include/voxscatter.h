@@ -170,8 +170,13 @@ int vs_op_apply_device_noalloc(vs_op* op, const void* x, void* y, int64_t nrhs, 
 
 typedef struct vs_prec vs_prec;
 
-/* Bit mask of the precisions a preconditioner is built for. */
-enum vs_prec_mask { VS_BUILD_C64 = 1, VS_BUILD_C128 = 2 };
+/* Bit mask of the precisions a preconditioner is built for, and how the
+ * FP32 (VS_BUILD_C64) blocks are inverted: by default on the tensor cores
+ * (batched blocked Gauss-Jordan, tcgen05 3xTF32 trailing updates) when
+ * 3N > 168 and 3N <= 256, else one CTA per block in shared memory;
+ * VS_BUILD_LU_TC forces the tensor cores for any 3N <= 256, VS_BUILD_LU_CUDA
+ * the CUDA-core kernels.  FP64 blocks are always inverted on the CUDA cores. */
+enum vs_prec_mask { VS_BUILD_C64 = 1, VS_BUILD_C128 = 2, VS_BUILD_LU_TC = 4, VS_BUILD_LU_CUDA = 8 };
 
 /* circ_1_level (on_off = 'off') followed by circ_2_level on the device, FP64:
  * src/src_preconditioning/circ_1_level.m:1-93 and circ_2_level.m:1-155.

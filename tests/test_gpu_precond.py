@@ -183,6 +183,52 @@ def test_prec_large_blocks(api, N, L, M):
                 pr.set_shape(prec, gemv_mode=2, gemv_chunk=2, gemv_blocks=1, gemv_threads=0)
 
 
+@pytest.mark.parametrize("N,L,M", [(3, 5, 4), (12, 8, 6), (26, 6, 5), (40, 4, 4), (64, 3, 3), (80, 3, 2)])
+def test_prec_tensor_core_inversion(api, N, L, M):
+    """FP32 blocks inverted on the tensor cores (batched blocked Gauss-Jordan,
+    tcgen05 3xTF32 trailing updates; forced for every 3N <= 256) against the
+    oracle's FP64 inverses (inv of main_DDA.m:107-111) at the FP32 tolerance
+    and against the CUDA-core FP32 inverses.  3N = 9 is one partial panel,
+    3N = 36 two panels, 3N = 78 the 105x91x26 plate's block (a partial last
+    panel and row tile), 3N = 120, 192 (the snowflake's block) and 240 several
+    panels and row tiles."""
+    p = W.config5(level=2, L=L, M=M, N=N, layers=max(N - 8, 1))
+    L, M, N, idx3, Toep, alpha, dV = _setup(p)
+    _, c1_o = O.circ_1_level(Toep, L, M, N, 0, "off")
+    _, blk_o = O.circ_2_level(c1_o, L, M, N)
+    inv_o = O.invert_blocks(blk_o, 1 / alpha, dV)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr_tc = api.Preconditioner(op, shift=1 / alpha, d=dV, precisions=("c64",), lu="tc")
+    pr_cu = api.Preconditioner(op, shift=1 / alpha, d=dV, precisions=("c64",), lu="cuda")
+    b_tc, b_cu = pr_tc.blocks(L, M, N, "c64"), pr_cu.blocks(L, M, N, "c64")
+    assert np.all(np.isfinite(b_tc))
+    assert rel(b_tc, inv_o) < 1e-4
+    assert rel(b_tc, b_cu) < 1e-4
+    # every block individually (a wrong panel or tile shows in one block)
+    for i in range(L):
+        for j in range(M):
+            assert rel(b_tc[i, j], inv_o[i, j]) < 1e-4, (i, j)
+    rng = np.random.default_rng(9)
+    x = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
+    assert rel(pr_tc.apply(x, "c64"), O.mvp_circ_2_level(inv_o, x, L, M, N, idx3)) < 1e-4
+
+
+def test_prec_build_options_rejected(api):
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.0, nper=3)
+    L, M, N, idx3, Toep, alpha, dV = _setup(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    from voxscatter_gb300 import _lib
+    import ctypes
+    h = ctypes.c_void_p()
+    sh = np.array([1 / alpha], dtype=np.complex128)
+    dd = np.array([dV], dtype=np.complex128)
+    both = _lib.VS_BUILD_C64 | _lib.VS_BUILD_LU_TC | _lib.VS_BUILD_LU_CUDA
+    st = op.ctx._lib.vs_prec_create(op.h, _lib.dptr(sh), _lib.dptr(dd), 1, both, ctypes.byref(h))
+    assert st == _lib.VS_ERR_ARG
+    st = op.ctx._lib.vs_prec_create(op.h, _lib.dptr(sh), _lib.dptr(dd), 1, _lib.VS_BUILD_LU_TC, ctypes.byref(h))
+    assert st == _lib.VS_ERR_ARG
+
+
 def test_context_outlives_its_objects(api):
     """vs_ctx_destroy before the operator and preconditioner made on the
     context: both keep working (they hold the context) and are released

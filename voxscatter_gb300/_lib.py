@@ -54,7 +54,7 @@ SIGNATURES = {
     "vs_prec_apply_device": (C.c_int, [_vp, _vp, _vp, _i64, C.c_int]),
     "vs_prec_get_blocks": (C.c_int, [_vp, C.c_int, _pd]),
 }
-VS_BUILD_C64, VS_BUILD_C128 = 1, 2
+VS_BUILD_C64, VS_BUILD_C128, VS_BUILD_LU_TC, VS_BUILD_LU_CUDA = 1, 2, 4, 8
 VS_BICGSTAB, VS_GMRES, VS_GMRES_DR = 0, 1, 2
 VS_SOLVE_MIXED, VS_SOLVE_FP64 = 0, 1
 

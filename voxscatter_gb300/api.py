@@ -309,9 +309,11 @@ class Preconditioner:
     """Handle on a device 2-level circulant preconditioner (y = M^-1 x)."""
 
     def __init__(self, op=None, shift=None, d=None, inv_blocks=None, LMN=None, idx3=None,
-                 precisions=("c64", "c128"), ctx=None):
+                 precisions=("c64", "c128"), ctx=None, lu="auto"):
+        """lu: how the FP32 blocks are inverted -- "auto", "tc" (tensor cores,
+        3N <= 256) or "cuda" (CUDA-core kernels)."""
         h = C.c_void_p()
-        mask = _precisions(precisions)
+        mask = _precisions(precisions) | {"auto": 0, "tc": L.VS_BUILD_LU_TC, "cuda": L.VS_BUILD_LU_CUDA}[lu]
         if op is not None:
             self.ctx = op.ctx
             sh = np.array([complex(shift)], dtype=np.complex128)

@@ -181,7 +181,9 @@ __global__ void k_blocks_out(const double2* __restrict__ i64, const float2* __re
 }
 
 void prec_common_impl(vs_prec* pr, int precisions) {
-  VS_REQUIRE(precisions >= 1 && precisions <= 3, "precisions must be VS_BUILD_C64 and/or VS_BUILD_C128");
+  VS_REQUIRE((precisions & 3) != 0 && (precisions & ~15) == 0,
+             "precisions must be VS_BUILD_C64 and/or VS_BUILD_C128 (optionally one of VS_BUILD_LU_TC, VS_BUILD_LU_CUDA)");
+  VS_REQUIRE((precisions & 12) != 12, "VS_BUILD_LU_TC and VS_BUILD_LU_CUDA exclude each other");
   cudaStream_t st = pr->ctx->stream;
   pr->axL.init(pr->L, st);
   pr->axM.init(pr->M, st);
@@ -754,8 +756,10 @@ int vs_prec_create(vs_op* op, const double* shift, const double* d, int64_t nd, 
     const int64_t nblk = pr->sym ? (int64_t)(op->L / 2 + 1) * (op->M / 2 + 1) : LM;
     if (precisions & VS_BUILD_C64) {
       pr->inv32.alloc(nblk * n * n * sizeof(float2) + 64);
+      const int lu = (precisions & VS_BUILD_LU_TC) ? vs::LU_TC : (precisions & VS_BUILD_LU_CUDA) ? vs::LU_CUDA
+                                                                                                  : vs::LU_AUTO;
       vs::assemble_invert<float>(l2.as<double2>(), op->L, op->M, op->N, sh, dptr, ds, true, true, scale,
-                                 pr->inv32.as<float2>(), status.as<int>(), st, pr->sym);
+                                 pr->inv32.as<float2>(), status.as<int>(), st, pr->sym, lu);
     }
     if (precisions & VS_BUILD_C128) {
       pr->inv64.alloc(nblk * n * n * sizeof(double2) + 64);
@@ -765,6 +769,7 @@ int vs_prec_create(vs_op* op, const double* shift, const double* d, int64_t nd, 
     int hs = 0;
     VS_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
+    if (hs & 8) throw vs::Error(VS_ERR_TIMEOUT, "a tensor-core MMA of the block inversion did not complete in time");
     VS_REQUIRE(hs == 0, "a preconditioner block is singular or its inverse is not finite");
     // with a uniform scaling d every block is symmetric up to the x/y sign flips
     if (nd == 1) vs::pack_sym_blocks(*pr, st);

@@ -227,10 +227,21 @@ void nop_assemble_device(int L, int M, int N, double ko, double dx, const double
 
 // Smallest instantiated two-level z length >= min_len (5-smooth beyond 256).
 int z_pass_length(int min_len);
+// lu: how FP32 blocks are inverted: LU_AUTO (tensor cores for blocks too
+// large for the one-CTA shared-memory kernel, up to 256), LU_TC (tensor cores
+// whenever 3N <= 256), LU_CUDA (CUDA-core kernels only).  FP64 blocks always
+// use the CUDA-core kernels.
+enum { LU_AUTO = 0, LU_TC = 1, LU_CUDA = 2 };
 template <typename T>
 void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, const double2* dvec, double2 dscal,
                      bool invert, bool colmajor, double scale, cplx_t<T>* out, int* status, cudaStream_t st,
-                     bool sym = false);
+                     bool sym = false, int lu = LU_AUTO);
+// Batched in-place inversion of nmat row-major n x n FP32 complex matrices
+// (n <= 256) by blocked Gauss-Jordan with tcgen05 trailing updates
+// (vs_lu_tc.cu); results scaled by `scale`; status bits 1 zero pivot,
+// 2 non-finite result, 8 an MMA wait ran out.
+bool tc_invert_supported(int n);
+void invert_blocks_tc(float2* mats, int n, int64_t nmat, double scale, int* status, cudaStream_t st);
 template <typename T>
 void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
                      cudaStream_t st, int pass, int skip_stride = 0);

@@ -423,11 +423,24 @@ size_t gj_blocked_smem(int n, size_t csize) {
 template <typename T>
 void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, const double2* dvec, double2 dscal,
                      bool invert, bool colmajor, double scale, cplx_t<T>* out, int* status, cudaStream_t st,
-                     bool sym) {
+                     bool sym, int lu) {
   const size_t smem = assemble_smem(N, sizeof(cplx_t<T>));
   const int Lb = sym ? L / 2 + 1 : L, Mb = sym ? M / 2 + 1 : M;
   const int n = 3 * N;
   const int64_t nmat = (int64_t)Lb * Mb;
+  const bool fp32 = std::is_same<T, float>::value;
+  const bool use_tc = invert && fp32 && tc_invert_supported(n) &&
+                      (lu == LU_TC || (lu == LU_AUTO && smem > 227 * 1024));
+  if (use_tc) {
+    VS_REQUIRE(colmajor, "tensor-core inversion produces column-major blocks");
+    // the transposes assembled row-major; the inverse of A^T row-major is A^-1 column-major
+    const int64_t total = nmat * n * n;
+    const int blocks = (int)std::min<int64_t>(ceil_div(total, 256), 152 * 64);
+    k_assemble<T><<<blocks, 256, 0, st>>>(lev2, L, M, N, shift, dvec, dscal, 1, 1.0, out, Lb, Mb);
+    VS_LAUNCH_CHECK();
+    if constexpr (std::is_same<T, float>::value) invert_blocks_tc(out, n, nmat, scale, status, st);
+    return;
+  }
   if (!invert || smem > 227 * 1024) {
     // element-wise assembly; the inverse of A^T in row-major order is A^-1 in column-major order
     const int64_t total = nmat * n * n;
@@ -459,9 +472,9 @@ void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, co
   VS_LAUNCH_CHECK();
 }
 template void assemble_invert<float>(const double2*, int, int, int, double2, const double2*, double2, bool, bool,
-                                     double, float2*, int*, cudaStream_t, bool);
+                                     double, float2*, int*, cudaStream_t, bool, int);
 template void assemble_invert<double>(const double2*, int, int, int, double2, const double2*, double2, bool, bool,
-                                      double, double2*, int*, cudaStream_t, bool);
+                                      double, double2*, int*, cudaStream_t, bool, int);
 
 // ---- apply: block GEMV on the (x,y)-frequency planes --------------------
 // Inverse blocks are stored column-major (element (r, q) at q*n + r), so the
