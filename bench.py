@@ -306,17 +306,20 @@ def _batched(api, ctx, stream, p, op, prec, steps):
     import torch
     from voxscatter_gb300 import workloads as W
     out = {}
-    B = np.array([api.plane_wave(op, p["r"], p["ko"] * v, pol) for v, pol in _directions(7, 8)])
+    pairs = _directions(7, 8)
+    B = np.array([api.plane_wave(op, p["r"], p["ko"] * v, pol) for v, pol in pairs])
+    # each direction and polarisation has its own alpha_LDR (getOPERATOR_DDA.m:14-26)
+    gram = np.array([1 / api.alpha_ldr(p["refInd"], p["ko"], p["d"], p["ko"] * v, pol) for v, pol in pairs])
     Bd = torch.from_numpy(B).cuda()
     Xd = torch.zeros_like(Bd)
     torch.cuda.synchronize()
-    api.solve_batch_device(op, Bd.data_ptr(), Xd.data_ptr(), len(B), prec, tol=TOL)  # warm-up / graph capture
+    api.solve_batch_device(op, Bd.data_ptr(), Xd.data_ptr(), len(B), prec, tol=TOL, gram=gram)  # warm-up / capture
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     for _ in range(steps):
         with torch.cuda.stream(stream):
             Xd.zero_()
-        infos = api.solve_batch_device(op, Bd.data_ptr(), Xd.data_ptr(), len(B), prec, tol=TOL)
+        infos = api.solve_batch_device(op, Bd.data_ptr(), Xd.data_ptr(), len(B), prec, tol=TOL, gram=gram)
     ev1.record(stream)
     ev1.synchronize()
     ms = ev0.elapsed_time(ev1) / steps
@@ -341,7 +344,8 @@ def _batched(api, ctx, stream, p, op, prec, steps):
         opq = api.Operator(L, M, N, idx3, 1.0, dV, ainv, toep=Tq, ctx=cq)
         prq = api.Preconditioner(opq, shift=ainv, d=dV, precisions=("c64", "c128"))
         Bq = np.array([api.plane_wave(opq, q["r"], q["ko"] * v, pol) for v, pol in q["rhs"]])
-        parts.append((opq, prq, torch.from_numpy(Bq).cuda(), len(Bq), len(q["idx"])))
+        gq = np.array([1 / api.alpha_ldr(q["refInd"], q["ko"], q["d"], q["ko"] * v, pol) for v, pol in q["rhs"]])
+        parts.append((opq, prq, torch.from_numpy(Bq).cuda(), len(Bq), len(q["idx"]), gq))
     torch.cuda.synchronize()
     setup = (time.perf_counter() - t0) * 1e3
     Xs = [torch.zeros_like(Bq) for (_, _, Bq, _, _) in parts]
@@ -800,6 +804,58 @@ def run_koch(args):
     return 0
 
 
+def run_lu(args):
+    """Batched inversion of the preconditioner blocks (the parfor of inv() at
+    main_DDA.m:107-111 / main_koch.m:114-118) on the tensor cores against the
+    CUDA-core blocked Gauss-Jordan: the 256x256x64 snowflake's 16,641 stored
+    blocks of 192 and the 105x91x26 plate's 2,523 blocks of 78, FP32 complex,
+    seeded well-conditioned matrices of those sizes in HBM (values do not
+    change the work).  --lu-batch limits the batch (small cases for profiling).
+    One JSON line."""
+    import torch
+    from voxscatter_gb300 import api
+    ctx = api.Context(0)
+    ext = torch.cuda.ExternalStream(ctx.stream_ptr())
+    out = {}
+    cases = (("snowflake_192", 192, 16641), ("hexplate_78", 78, 2523))
+    for name, n, nmat in cases:
+        if args.lu_batch:
+            nmat = min(nmat, args.lu_batch)
+        g = torch.Generator(device="cuda").manual_seed(0)
+        A = (torch.randn(nmat, n, n, dtype=torch.complex64, device="cuda", generator=g) * (0.5 / n ** 0.5)
+             + torch.eye(n, dtype=torch.complex64, device="cuda") * (1.0 + 0.3j))
+        W = torch.empty_like(A)
+        res = {"n": n, "blocks": nmat, "flops_per_block": 8 * n ** 3}
+        for method in ("tc", "cuda"):
+            for _ in range(args.warmup):
+                W.copy_(A)
+                torch.cuda.synchronize()
+                api.invert_blocks_device(W.data_ptr(), n, nmat, method, ctx=ctx)
+            times = []
+            for _ in range(args.steps):
+                W.copy_(A)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(ext)
+                api.invert_blocks_device(W.data_ptr(), n, nmat, method, ctx=ctx)
+                e1.record(ext)
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1))
+            ms = float(np.median(times))
+            # accuracy on a sample of blocks against an FP64 inverse
+            idx = np.linspace(0, nmat - 1, 8).astype(int)
+            Ah = A[idx].cpu().numpy().astype(np.complex128)
+            Wh = W[idx].cpu().numpy().astype(np.complex128)
+            err = max(np.linalg.norm(Wh[k] - np.linalg.inv(Ah[k])) / np.linalg.norm(np.linalg.inv(Ah[k]))
+                      for k in range(len(idx)))
+            res[method] = {"ms": ms, "TFLOPs": 8 * n ** 3 * nmat / (ms * 1e-3) / 1e12, "max_rel_err_vs_fp64": err}
+        res["speedup_tc_vs_cuda"] = res["cuda"]["ms"] / res["tc"]["ms"]
+        out[name] = res
+    print(json.dumps({"metric": "batched block inversion (preconditioner build), FP32 complex", "unit": "ms",
+                      "steps": args.steps, "warmup": args.warmup, "results": out}), flush=True)
+    return 0
+
+
 def run_nop(args):
     """Galerkin N-operator Toeplitz assembly (far + medium cells of
     assembly_nop_const.m) on a 128x128x64 grid: device time, against the FP64
@@ -843,7 +899,8 @@ def main():
     ap.add_argument("--shapes", default=None,
                     help='JSON {"op": {...}, "prec": {...}} c64 launch shapes applied after autotuning '
                          '(replays a tuned configuration, e.g. under a profiler)')
-    ap.add_argument("--mode", default="solve", choices=["solve", "passes", "koch", "nop", "adjoint"],
+    ap.add_argument("--lu-batch", type=int, default=0, help="lu mode: at most this many blocks per case")
+    ap.add_argument("--mode", default="solve", choices=["solve", "passes", "koch", "nop", "adjoint", "lu"],
                     help="passes: only build the operator/preconditioner and time each pipeline launch "
                          "(a short command for ncu captures); koch: the 256x256x64 snowflake's pipeline "
                          "times and a bounded GMRES(50) solve")
@@ -856,6 +913,8 @@ def main():
         return run_adjoint(args)
     if args.mode == "nop":
         return run_nop(args)
+    if args.mode == "lu":
+        return run_lu(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

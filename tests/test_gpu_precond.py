@@ -213,6 +213,32 @@ def test_prec_tensor_core_inversion(api, N, L, M):
     assert rel(pr_tc.apply(x, "c64"), O.mvp_circ_2_level(inv_o, x, L, M, N, idx3)) < 1e-4
 
 
+@pytest.mark.parametrize("n", [17, 78, 192, 256, 300])
+def test_invert_blocks_device(api, n):
+    """vs_invert_blocks_device on a batch of complex FP32 matrices, tensor
+    cores (n <= 256) and CUDA cores, against FP64 inverses; a singular matrix
+    in the batch is reported."""
+    import torch
+    rng = np.random.default_rng(n)
+    nmat = 5
+    A = (rng.normal(size=(nmat, n, n)) + 1j * rng.normal(size=(nmat, n, n))) * (0.5 / np.sqrt(n)) + \
+        np.eye(n) * (1.0 + 0.3j)
+    inv = np.linalg.inv(A)
+    for method in (("tc", "cuda", "auto") if n <= 256 else ("auto", "cuda")):
+        W = torch.tensor(A, dtype=torch.complex64, device="cuda")
+        torch.cuda.synchronize()
+        api.invert_blocks_device(W.data_ptr(), n, nmat, method)
+        Wh = W.cpu().numpy()
+        for k in range(nmat):
+            assert rel(Wh[k], inv[k]) < 1e-5, (method, k)
+    S = A.copy()
+    S[2] = 0
+    W = torch.tensor(S, dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    with pytest.raises(VoxScatterError, match="singular"):
+        api.invert_blocks_device(W.data_ptr(), n, nmat, "auto")
+
+
 def test_prec_build_options_rejected(api):
     p = W.small_hex(m=1.31 + 0.05j, diameter=2.0, nper=3)
     L, M, N, idx3, Toep, alpha, dV = _setup(p)

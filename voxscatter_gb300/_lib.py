@@ -50,6 +50,7 @@ SIGNATURES = {
     "vs_prec_create": (C.c_int, [_vp, _pd, _pd, _i64, C.c_int, C.POINTER(_vp)]),
     "vs_prec_create_blocks": (C.c_int, [_vp, _i64, _i64, _i64, _pd, _pi64, _i64, C.c_int, C.POINTER(_vp)]),
     "vs_prec_destroy": (C.c_int, [_vp]),
+    "vs_invert_blocks_device": (C.c_int, [_vp, _vp, _i64, _i64, C.c_int]),
     "vs_prec_apply": (C.c_int, [_vp, _pd, _pd, _i64, C.c_int]),
     "vs_prec_apply_device": (C.c_int, [_vp, _vp, _vp, _i64, C.c_int]),
     "vs_prec_get_blocks": (C.c_int, [_vp, C.c_int, _pd]),

@@ -310,8 +310,8 @@ class Preconditioner:
 
     def __init__(self, op=None, shift=None, d=None, inv_blocks=None, LMN=None, idx3=None,
                  precisions=("c64", "c128"), ctx=None, lu="auto"):
-        """lu: how the FP32 blocks are inverted -- "auto", "tc" (tensor cores,
-        3N <= 256) or "cuda" (CUDA-core kernels)."""
+        """lu: how the FP32 blocks are inverted -- "auto" (= "cuda", the CUDA-core
+        kernels) or "tc" (tcgen05 trailing updates, 3N <= 256)."""
         h = C.c_void_p()
         mask = _precisions(precisions) | {"auto": 0, "tc": L.VS_BUILD_LU_TC, "cuda": L.VS_BUILD_LU_CUDA}[lu]
         if op is not None:
@@ -380,6 +380,15 @@ class Preconditioner:
             self.close()
         except Exception:
             pass
+
+
+def invert_blocks_device(mats_ptr, n, nmat, method="auto", ctx=None):
+    """In-place FP32 inversion of nmat complex n x n matrices at the device
+    address mats_ptr (complex64, either storage order): "auto" / "cuda"
+    (CUDA-core blocked Gauss-Jordan) or "tc" (tensor cores, n <= 256)."""
+    ctx = ctx or default_context()
+    code = {"auto": 0, "tc": L.VS_BUILD_LU_TC, "cuda": L.VS_BUILD_LU_CUDA}[method]
+    L.check(ctx._lib.vs_invert_blocks_device(ctx.h, C.c_void_p(mats_ptr), int(n), int(nmat), code), ctx.h)
 
 
 def mvp_circ_2_level(inv_blocks, JIn, Lx, My, Nz, idx, precision="c128", ctx=None):

@@ -827,6 +827,27 @@ int vs_prec_create_blocks(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const do
   return s;
 }
 
+int vs_invert_blocks_device(vs_ctx* ctx, void* mats, int64_t n, int64_t nmat, int method) {
+  if (!ctx) return VS_ERR_ARG;
+  return guarded(ctx, [&] {
+    VS_REQUIRE(mats, "NULL argument");
+    VS_REQUIRE(n >= 1 && n <= 4096 && nmat >= 0, "n must be in [1, 4096] and nmat >= 0");
+    VS_REQUIRE(method == 0 || method == VS_BUILD_LU_TC || method == VS_BUILD_LU_CUDA, "bad method");
+    VS_REQUIRE(method != VS_BUILD_LU_TC || vs::tc_invert_supported((int)n), "tensor-core inversion takes n <= 256");
+    cudaStream_t st = ctx->stream;
+    vs::DevBuf status;
+    status.alloc(sizeof(int));
+    VS_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), st));
+    vs::invert_blocks_device((float2*)mats, (int)n, nmat, method == VS_BUILD_LU_TC ? vs::LU_TC : vs::LU_CUDA, 1.0,
+                             status.as<int>(), st);
+    int hs = 0;
+    VS_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+    if (hs & 8) throw vs::Error(VS_ERR_TIMEOUT, "a tensor-core MMA of the block inversion did not complete in time");
+    VS_REQUIRE(hs == 0, "a matrix is singular or its inverse is not finite");
+  });
+}
+
 int vs_prec_destroy(vs_prec* prec) {
   if (!prec) return VS_OK;
   int s = guarded(prec->ctx, [&] { VS_CUDA(cudaStreamSynchronize(prec->ctx->stream)); });

@@ -38,9 +38,10 @@ constexpr int kNB = 32;             // panel width (complex columns)
 constexpr int kK = 2 * kNB;         // real reduction length of one panel
 constexpr int kRowsPerTile = 64;    // complex rows per MMA tile (M = 128 real rows)
 constexpr int kPanelThreads = 256;
-constexpr int kUpdThreads = 128;
+constexpr int kUpdThreads = 256;
 constexpr int kTQ = 64;             // column tile of the permutation in k_tc_panel
 constexpr uint32_t kMmaPolls = 1u << 22;
+constexpr int kMaxChunks = 4;       // 16-column chunks per warp of the update epilogue (NT <= 128)
 
 __device__ __forceinline__ float2 crecipf(float2 a) {
   const float d = a.x * a.x + a.y * a.y;
@@ -49,26 +50,33 @@ __device__ __forceinline__ float2 crecipf(float2 a) {
 
 // Shared memory of k_tc_panel for blocks of n.
 size_t panel_smem(int n) {
-  return ((size_t)n * (kNB + 1) + (size_t)n + 2ull * kNB * kTQ) * sizeof(float2) + (3ull * n + kNB) * sizeof(int) +
-         64;
+  return (2ull * kNB * kTQ + 3ull * kNB) * sizeof(float2) + (3ull * n + kNB + 2 * 8) * sizeof(int) + 64;
 }
 
+// The panel lives in registers: lane c holds column c of the panel for the
+// warp's rows (8 warps, row r in warp r % 8 at slot r / 8, RPW >= n / 8 slots),
+// so a row's column kk (the elimination multiplier) is one shuffle away and
+// only the pivot search, the row swap and the scaled pivot row cross warps
+// (three barriers per step).
+template <int kPanelRows>
 __global__ void __launch_bounds__(kPanelThreads) k_tc_panel(float2* __restrict__ mats, int n, int64_t nmat, int k0,
                                                             float2* __restrict__ V, int* __restrict__ perm_all,
                                                             int* __restrict__ status) {
-  constexpr int PS = kNB + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* P = reinterpret_cast<float2*>(smem_raw);  // [n][PS]
-  float2* colk = P + (size_t)n * PS;                // [n]
-  float2* buf = colk + n;                           // [2*NB][TQ]: old K rows, then old rows feeding O rows
-  int* rowsrc = reinterpret_cast<int*>(buf + 2 * kNB * kTQ);  // new row r = old row rowsrc[r]
-  int* oidx = rowsrc + n;                                     // slot of a changed row below the panel, or -1
-  int* olist = oidx + n;                                      // [NB]
-  int* piv = olist + kNB;                                     // [n] pivots of this panel (local copy)
-  __shared__ int s_piv, s_ocnt;
-  __shared__ float s_pmag;
-  const int tid = threadIdx.x;
+  float2* buf = reinterpret_cast<float2*>(smem_raw);  // [2*NB][TQ]: old K rows, then old rows feeding O rows
+  float2* prow = buf + 2 * kNB * kTQ;                  // [NB] scaled pivot row
+  float2* swk = prow + kNB;                            // [NB] row k before the swap
+  float2* swp = swk + kNB;                             // [NB] row p before the swap
+  int* rowsrc = reinterpret_cast<int*>(swp + kNB);     // new row r = old row rowsrc[r]
+  int* oidx = rowsrc + n;                              // slot of a changed row below the panel, or -1
+  int* olist = oidx + n;                               // [NB]
+  int* piv = olist + kNB;                              // [n]
+  float* cand_m = reinterpret_cast<float*>(piv + n);   // [8] best magnitude per warp
+  int* cand_i = reinterpret_cast<int*>(cand_m + 8);    // [8] its row
+  __shared__ int s_ocnt;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nb = min(kNB, n - k0);
+  const float2 z2 = make_float2(0.f, 0.f);
   for (int64_t b = blockIdx.x; b < nmat; b += gridDim.x) {
     float2* B = mats + b * (int64_t)n * n;
     int* perm = perm_all + b * (int64_t)n;
@@ -76,63 +84,98 @@ __global__ void __launch_bounds__(kPanelThreads) k_tc_panel(float2* __restrict__
       rowsrc[r] = r;
       oidx[r] = -1;
     }
-    for (int u = tid; u < n * kNB; u += blockDim.x) {
-      const int r = u / kNB, c = u - r * kNB;
-      P[r * PS + c] = c < nb ? B[(int64_t)r * n + k0 + c] : make_float2(0.f, 0.f);
+    float2 P[kPanelRows];
+#pragma unroll
+    for (int i = 0; i < kPanelRows; ++i) {
+      const int r = warp + 8 * i;
+      P[i] = (r < n && lane < nb) ? B[(int64_t)r * n + k0 + lane] : z2;
     }
     __syncthreads();
     for (int kk = 0; kk < nb; ++kk) {
       const int k = k0 + kk;
-      if (tid < 32) {
-        float best = -1.f;
-        int bi = k;
-        for (int r = k + tid; r < n; r += 32) {
-          const float2 a = P[r * PS + kk];
-          const float m = a.x * a.x + a.y * a.y;
-          if (m > best) { best = m; bi = r; }
-        }
-        for (int off = 16; off; off >>= 1) {
-          const float ob = __shfl_xor_sync(0xffffffffu, best, off);
-          const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-          if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-        }
-        if (tid == 0) {
-          s_piv = bi;
-          s_pmag = best;
-          piv[kk] = bi;
-          const int t = rowsrc[k];
-          rowsrc[k] = rowsrc[bi];
-          rowsrc[bi] = t;
-        }
+      // pivot search in column kk over rows >= k: per warp in lane kk, then
+      // every thread reduces the eight candidates (same order, same result)
+      float best = -1.f;
+      int bi = k;
+#pragma unroll
+      for (int i = 0; i < kPanelRows; ++i) {
+        const int r = warp + 8 * i;
+        const float m = P[i].x * P[i].x + P[i].y * P[i].y;
+        if (r >= k && r < n && m > best) { best = m; bi = r; }
+      }
+      if (lane == kk) {
+        cand_m[warp] = best;
+        cand_i[warp] = bi;
       }
       __syncthreads();
-      const int p = s_piv;
-      if (tid == 0 && !(s_pmag > 0.f)) atomicOr(status, 1);
-      if (p != k && tid < kNB) {
-        const float2 t = P[k * PS + tid];
-        P[k * PS + tid] = P[p * PS + tid];
-        P[p * PS + tid] = t;
+      float pm = cand_m[0];
+      int p = cand_i[0];
+      for (int w = 1; w < 8; ++w) {
+        const float m = cand_m[w];
+        const int ri = cand_i[w];
+        if (m > pm || (m == pm && ri < p)) { pm = m; p = ri; }
+      }
+      if (p < k) p = k;  // no candidate (all below k): keep k, flagged as a zero pivot
+      if (tid == 0) {
+        if (!(pm > 0.f)) atomicOr(status, 1);
+        piv[kk] = p;
+        const int t = rowsrc[k];
+        rowsrc[k] = rowsrc[p];
+        rowsrc[p] = t;
+      }
+      // swap rows k and p through shared memory (selects over every slot,
+      // so the slots stay in registers)
+      const int ks = k >> 3, ps = p >> 3;
+      if (p != k) {
+        float2 tk = z2, tp = z2;
+#pragma unroll
+        for (int i = 0; i < kPanelRows; ++i) {
+          tk = (i == ks) ? P[i] : tk;
+          tp = (i == ps) ? P[i] : tp;
+        }
+        if (warp == (k & 7)) swk[lane] = tk;
+        if (warp == (p & 7)) swp[lane] = tp;
       }
       __syncthreads();
-      for (int r = tid; r < n; r += blockDim.x) colk[r] = P[r * PS + kk];
-      __syncthreads();
-      const float2 rinv = crecipf(colk[k]);
-      if (tid < kNB) P[k * PS + tid] = (tid == kk) ? rinv : cmul(P[k * PS + tid], rinv);
-      __syncthreads();
-      for (int u = tid; u < n * kNB; u += blockDim.x) {
-        const int r = u / kNB, c = u - r * kNB;
-        if (r == k) continue;
-        const float2 base = (c == kk) ? make_float2(0.f, 0.f) : P[r * PS + c];
-        P[r * PS + c] = csub(base, cmul(colk[r], P[k * PS + c]));
+      if (p != k) {
+        const float2 nk = swp[lane], np = swk[lane];
+        const bool wk = warp == (k & 7), wp = warp == (p & 7);
+#pragma unroll
+        for (int i = 0; i < kPanelRows; ++i) {
+          P[i] = (wk && i == ks) ? nk : P[i];
+          P[i] = (wp && i == ps) ? np : P[i];
+        }
+      }
+      // scaled pivot row (row k's warp), broadcast through shared memory
+      {
+        float2 pk = z2;
+#pragma unroll
+        for (int i = 0; i < kPanelRows; ++i) pk = (i == ks) ? P[i] : pk;
+        const float2 pv = make_float2(__shfl_sync(0xffffffffu, pk.x, kk), __shfl_sync(0xffffffffu, pk.y, kk));
+        const float2 rinv = crecipf(pv);
+        const float2 nv = (lane == kk) ? rinv : cmul(pk, rinv);
+        if (warp == (k & 7)) prow[lane] = nv;
       }
       __syncthreads();
+      const float2 pr = prow[lane];
+#pragma unroll
+      for (int i = 0; i < kPanelRows; ++i) {
+        const int r = warp + 8 * i;
+        const float2 ck = make_float2(__shfl_sync(0xffffffffu, P[i].x, kk), __shfl_sync(0xffffffffu, P[i].y, kk));
+        const float2 base0 = (lane == kk) ? z2 : P[i];
+        const float2 el = csub(base0, cmul(ck, pr));
+        P[i] = (r == k) ? pr : (r < n ? el : P[i]);
+      }
+      // the next step's first barrier orders these register updates against
+      // the shared buffers it rewrites
     }
-    // the panel's final columns, and the bookkeeping of the rows below it
-    // that a swap changed (each receives an old row of K)
-    for (int u = tid; u < n * kNB; u += blockDim.x) {
-      const int r = u / kNB, c = u - r * kNB;
-      if (c < nb) B[(int64_t)r * n + k0 + c] = P[r * PS + c];
+    // the panel's final columns
+#pragma unroll
+    for (int i = 0; i < kPanelRows; ++i) {
+      const int r = warp + 8 * i;
+      if (r < n && lane < nb) B[(int64_t)r * n + k0 + lane] = P[i];
     }
+    __syncthreads();
     if (tid < nb) perm[k0 + tid] = piv[tid];
     if (tid == 0) {
       int cnt = 0;
@@ -163,7 +206,7 @@ __global__ void __launch_bounds__(kPanelThreads) k_tc_panel(float2* __restrict__
         if (q >= n) continue;
         const bool inpanel = q >= k0 && q < k0 + nb;
         if (rr < kNB) {
-          Vb[(int64_t)rr * n + q] = (rr < nb && !inpanel) ? buf[rr * kTQ + qi] : make_float2(0.f, 0.f);
+          Vb[(int64_t)rr * n + q] = (rr < nb && !inpanel) ? buf[rr * kTQ + qi] : z2;
         } else if (!inpanel) {
           B[(int64_t)olist[rr - kNB] * n + q] = buf[(nb + rr - kNB) * kTQ + qi];
         }
@@ -173,17 +216,27 @@ __global__ void __launch_bounds__(kPanelThreads) k_tc_panel(float2* __restrict__
   }
 }
 
-// Shared memory of k_tc_update: A_hi, A_lo (128 x K) and B_hi, B_lo (NT x K), FP32.
-size_t update_smem(int NT) { return (2ull * 128 * kK + 2ull * NT * kK) * sizeof(float) + 1024; }
+// Shared memory of k_tc_update: A_hi, A_lo (128 x K) and B_hi, B_lo (NT x K),
+// FP32, plus alignment slack.
+size_t update_smem(int NT) { return (2ull * 128 * kK + 2ull * NT * kK) * sizeof(float) + 128; }
 
-// One CTA per (matrix, 64-row tile); NT = MMA N (columns 0..NT-1 of the
-// matrix, NT a multiple of 16 covering n).
+// Column tiles of the update: at most 128 columns each (two CTAs per SM fit),
+// NT a multiple of 16.
+void update_tiling(int n, int* q_tiles, int* NT) {
+  *q_tiles = (n + 127) / 128;
+  const int w = (n + *q_tiles - 1) / *q_tiles;
+  *NT = (w + 15) / 16 * 16;
+}
+
+// One CTA per (matrix, 64-row tile, NT-column tile).  Operands are staged
+// with 16-byte stores, one row of a core matrix per thread and the rows of a
+// core on consecutive threads, so each quarter-warp fills one 128-byte core
+// without bank conflicts.
 __global__ void __launch_bounds__(kUpdThreads) k_tc_update(float2* __restrict__ mats, int n, int64_t nmat, int k0,
-                                                           const float2* __restrict__ V, int NT, int tiles,
-                                                           int* __restrict__ status) {
+                                                           const float2* __restrict__ V, int NT, int q_tiles,
+                                                           int r_tiles, int* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  // 1024-byte alignment of the operand arrays (the descriptors need 16)
-  unsigned char* base = smem_raw + ((1024u - (tc::smem_addr(smem_raw) & 1023u)) & 1023u);
+  unsigned char* base = smem_raw + ((128u - (tc::smem_addr(smem_raw) & 127u)) & 127u);
   unsigned char* sAh = base;
   unsigned char* sAl = sAh + 128 * kK * 4;
   unsigned char* sBh = sAl + 128 * kK * 4;
@@ -191,39 +244,52 @@ __global__ void __launch_bounds__(kUpdThreads) k_tc_update(float2* __restrict__ 
   __shared__ uint32_t s_tmem;
   __shared__ __align__(8) uint64_t s_bar;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t b = blockIdx.x / tiles;
-  const int tile = (int)(blockIdx.x - b * tiles);
+  const int per_mat = r_tiles * q_tiles;
+  const int64_t b = blockIdx.x / per_mat;
+  const int rem = (int)(blockIdx.x - b * per_mat);
+  const int r0 = (rem / q_tiles) * kRowsPerTile, c0 = (rem % q_tiles) * NT;
   if (b >= nmat) return;
   float2* B = mats + b * (int64_t)n * n;
   const float2* Vb = V + b * (int64_t)kNB * n;
-  const int r0 = tile * kRowsPerTile;
   const int nb = min(kNB, n - k0);
-  // A~ (2x2 real blocks of the panel rows r0..r0+63): thread -> (row, k) with k fastest
-  for (int u = tid; u < kRowsPerTile * kNB; u += kUpdThreads) {
-    const int rl = u / kNB, kk = u - rl * kNB, r = r0 + rl;
-    float2 w = make_float2(0.f, 0.f);
-    if (r < n && kk < nb) w = B[(int64_t)r * n + k0 + kk];
-    const float v[4] = {w.x, -w.y, w.y, w.x};  // (row 2rl: Re, -Im), (row 2rl+1: Im, Re)
-#pragma unroll
-    for (int e = 0; e < 2; ++e)
-#pragma unroll
-      for (int f = 0; f < 2; ++f) {
-        const float x = v[2 * e + f];
-        const float hi = tc::to_tf32(x);
-        const uint32_t off = tc::kmajor_offset(2 * rl + e, 2 * kk + f, kK);
-        *reinterpret_cast<float*>(sAh + off) = hi;
-        *reinterpret_cast<float*>(sAl + off) = x - hi;
-      }
+  const float2 z2 = make_float2(0.f, 0.f);
+  // A~: real row R = 2 rl + e of panel row r0 + rl, K chunk c (panel columns
+  // 2c, 2c+1): (Re, -Im) pairs for e = 0, (Im, Re) pairs for e = 1
+  for (int u = tid; u < 128 * (kK / 4); u += kUpdThreads) {
+    const int R = u & 127, c = u >> 7, rl = R >> 1, r = r0 + rl;
+    float2 w0 = z2, w1 = z2;
+    if (r < n) {
+      const float2* rowp = B + (int64_t)r * n + k0;
+      if (2 * c < nb) w0 = rowp[2 * c];
+      if (2 * c + 1 < nb) w1 = rowp[2 * c + 1];
+    }
+    const float4 v = (R & 1) ? make_float4(w0.y, w0.x, w1.y, w1.x) : make_float4(w0.x, -w0.y, w1.x, -w1.y);
+    const float4 h = make_float4(tc::to_tf32(v.x), tc::to_tf32(v.y), tc::to_tf32(v.z), tc::to_tf32(v.w));
+    const uint32_t off = tc::kmajor_offset(R, 4 * c, kK);
+    *reinterpret_cast<float4*>(sAh + off) = h;
+    *reinterpret_cast<float4*>(sAl + off) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
   }
-  // B~ (columns q of V): thread -> (k, q) with q fastest
-  for (int u = tid; u < kNB * NT; u += kUpdThreads) {
-    const int kk = u / NT, q = u - kk * NT;
-    const float2 w = (q < n && kk < nb) ? Vb[(int64_t)kk * n + q] : make_float2(0.f, 0.f);
-    const float hx = tc::to_tf32(w.x), hy = tc::to_tf32(w.y);
-    const uint32_t off = tc::kmajor_offset(q, 2 * kk, kK);  // (q, 2kk) and (q, 2kk+1) are adjacent
-    *reinterpret_cast<float2*>(sBh + off) = make_float2(hx, hy);
-    *reinterpret_cast<float2*>(sBl + off) = make_float2(w.x - hx, w.y - hy);
+  // B~: row q of the column tile, K chunk c: (Re, Im) of V[2c, q], V[2c+1, q]
+  for (int u = tid; u < NT * (kK / 4); u += kUpdThreads) {
+    const int ql = u % NT, c = u / NT, q = c0 + ql;
+    float2 w0 = z2, w1 = z2;
+    if (q < n) {
+      if (2 * c < nb) w0 = Vb[(int64_t)(2 * c) * n + q];
+      if (2 * c + 1 < nb) w1 = Vb[(int64_t)(2 * c + 1) * n + q];
+    }
+    const float4 v = make_float4(w0.x, w0.y, w1.x, w1.y);
+    const float4 h = make_float4(tc::to_tf32(v.x), tc::to_tf32(v.y), tc::to_tf32(v.z), tc::to_tf32(v.w));
+    const uint32_t off = tc::kmajor_offset(ql, 4 * c, kK);
+    *reinterpret_cast<float4*>(sBh + off) = h;
+    *reinterpret_cast<float4*>(sBl + off) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
   }
+  // epilogue mapping: warp w takes TMEM lanes 32 (w % 4).. (complex row
+  // r0 + 16 (w % 4) + lane/2, real part in even lanes, imaginary part in odd
+  // lanes) and, with warp w + 4, alternate 16-column chunks
+  const int qd = warp & 3, half = warp >> 2;
+  const int r_e = r0 + 16 * qd + (lane >> 1);
+  const bool odd = lane & 1;
+  const bool inK = r_e >= k0 && r_e < k0 + nb;
   const uint32_t ncols = NT <= 32 ? 32u : NT <= 64 ? 64u : NT <= 128 ? 128u : 256u;
   if (warp == 0) tc::tmem_alloc(&s_tmem, ncols);
   if (tid == 0) tc::mbar_init(&s_bar, 1);
@@ -253,14 +319,12 @@ __global__ void __launch_bounds__(kUpdThreads) k_tc_update(float2* __restrict__ 
   }
   tc::fence_after_sync();
   if (ok) {
-    // warp w holds TMEM lanes 32w..32w+31: complex row r0 + 16w + lane/2,
-    // real part in even lanes, imaginary part in odd lanes
-    const int rl = 16 * warp + (lane >> 1), r = r0 + rl;
-    const bool odd = lane & 1;
-    const bool inK = r >= k0 && r < k0 + nb;
-    for (int c = 0; c < NT; c += 16) {
+#pragma unroll
+    for (int j = 0; j < kMaxChunks; ++j) {
+      const int c = 16 * half + 32 * j;
+      if (c >= NT) break;
       float v[16];
-      tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + c, v);
+      tc::tmem_ld16(tmem + ((uint32_t)(32 * qd) << 16) + c, v);
       float2 d[8];
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
@@ -268,14 +332,14 @@ __global__ void __launch_bounds__(kUpdThreads) k_tc_update(float2* __restrict__ 
         const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
         d[i] = odd ? make_float2(recv, v[8 + i]) : make_float2(v[i], recv);
       }
-      if (r < n) {
-        const int q0 = c + (odd ? 8 : 0);
-        float2* row = B + (int64_t)r * n;
+      if (r_e < n) {
+        const int qb = c0 + c + (odd ? 8 : 0);
+        float2* row = B + (int64_t)r_e * n;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-          const int q = q0 + i;
+          const int q = qb + i;
           if (q >= n || (q >= k0 && q < k0 + nb)) continue;
-          const float2 base0 = inK ? make_float2(0.f, 0.f) : row[q];
+          const float2 base0 = inK ? z2 : row[q];
           row[q] = make_float2(base0.x + d[i].x, base0.y + d[i].y);
         }
       }
@@ -290,16 +354,20 @@ __global__ void __launch_bounds__(kUpdThreads) k_tc_update(float2* __restrict__ 
 }
 
 // Undo the column interchanges (composed over all panels), scale, flag
-// non-finite entries.  One CTA per matrix.
+// non-finite entries.  One CTA per matrix; each warp permutes whole rows
+// through its own shared-memory row buffer.
 __global__ void __launch_bounds__(256) k_tc_finish(float2* __restrict__ mats, int n, int64_t nmat,
                                                    const int* __restrict__ perm_all, float scale,
                                                    int* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int* cmap = reinterpret_cast<int*>(smem_raw);
-  float2* row = reinterpret_cast<float2*>(smem_raw + ((n * sizeof(int) + 15) & ~size_t(15)));
+  float2* rows = reinterpret_cast<float2*>(smem_raw + ((n * sizeof(int) + 15) & ~size_t(15)));  // [8][n]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float2* row = rows + (size_t)warp * n;
   for (int64_t b = blockIdx.x; b < nmat; b += gridDim.x) {
     float2* B = mats + b * (int64_t)n * n;
     const int* perm = perm_all + b * (int64_t)n;
+    __syncthreads();  // the previous matrix's cmap is no longer read
     if (threadIdx.x == 0) {
       for (int c = 0; c < n; ++c) cmap[c] = c;
       for (int k = n - 1; k >= 0; --k) {
@@ -312,17 +380,17 @@ __global__ void __launch_bounds__(256) k_tc_finish(float2* __restrict__ mats, in
       }
     }
     __syncthreads();
-    for (int r = 0; r < n; ++r) {
+    for (int r = warp; r < n; r += 8) {
       float2* Br = B + (int64_t)r * n;
-      for (int c = threadIdx.x; c < n; c += blockDim.x) row[c] = Br[c];
-      __syncthreads();
-      for (int c = threadIdx.x; c < n; c += blockDim.x) {
+      for (int c = lane; c < n; c += 32) row[c] = Br[c];
+      __syncwarp();
+      for (int c = lane; c < n; c += 32) {
         const float2 a = row[cmap[c]];
         const float2 o = make_float2(a.x * scale, a.y * scale);
         if (!(isfinite(o.x) && isfinite(o.y))) atomicOr(status, 2);
         Br[c] = o;
       }
-      __syncthreads();
+      __syncwarp();
     }
   }
 }
@@ -334,19 +402,27 @@ bool tc_invert_supported(int n) { return n >= 2 && n <= 256; }
 void invert_blocks_tc(float2* mats, int n, int64_t nmat, double scale, int* status, cudaStream_t st) {
   VS_REQUIRE(tc_invert_supported(n), "tensor-core inversion takes blocks of 2..256");
   if (nmat <= 0) return;
-  const int NT = (n + 15) / 16 * 16;
-  const int tiles = (n + kRowsPerTile - 1) / kRowsPerTile;
+  int q_tiles = 1, NT = 16;
+  update_tiling(n, &q_tiles, &NT);
+  const int r_tiles = (n + kRowsPerTile - 1) / kRowsPerTile;
   int dev = 0, nsm = 0;
   VS_CUDA(cudaGetDevice(&dev));
   VS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const size_t psm = panel_smem(n), usm = update_smem(NT), fsm = n * sizeof(int) + 16 + n * sizeof(float2);
-  set_kernel_smem((const void*)k_tc_panel, psm);
+  const size_t psm = panel_smem(n), usm = update_smem(NT), fsm = n * sizeof(int) + 16 + 8 * n * sizeof(float2);
+  const int rpw = (n + 7) / 8;
+  auto kp = rpw <= 4 ? k_tc_panel<4> : rpw <= 8 ? k_tc_panel<8> : rpw <= 16 ? k_tc_panel<16>
+          : rpw <= 24 ? k_tc_panel<24> : k_tc_panel<32>;
+  set_kernel_smem((const void*)kp, psm);
   set_kernel_smem((const void*)k_tc_update, usm);
   set_kernel_smem((const void*)k_tc_finish, fsm);
   int per_sm = 0;
-  VS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tc_panel, kPanelThreads, psm));
-  // scratch V (32 rows of every matrix) bounded to ~512 MB: matrices in chunks
-  const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nmat, (int64_t(512) << 20) / (kNB * n * 8)));
+  VS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp, kPanelThreads, psm));
+  // Matrices in chunks that stay resident in L2 across all panels of the
+  // chunk (each panel re-reads and rewrites every matrix): one panel-kernel
+  // wave, at most ~80 MB of matrices (the GB300's L2 is 129 MB).
+  const int64_t l2_fit = std::max<int64_t>(1, (int64_t(80) << 20) / ((int64_t)n * n * 8));
+  const int64_t wave = (int64_t)nsm * std::max(per_sm, 1);
+  const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nmat, std::min(wave, l2_fit)));
   DevBuf V, perm;
   V.alloc((size_t)chunk * kNB * n * sizeof(float2));
   perm.alloc((size_t)chunk * n * sizeof(int));
@@ -355,11 +431,12 @@ void invert_blocks_tc(float2* mats, int n, int64_t nmat, double scale, int* stat
     float2* mc = mats + m0 * (int64_t)n * n;
     const int pgrid = (int)std::min<int64_t>(cm, (int64_t)nsm * std::max(per_sm, 1));
     for (int k0 = 0; k0 < n; k0 += kNB) {
-      k_tc_panel<<<pgrid, kPanelThreads, psm, st>>>(mc, n, cm, k0, V.as<float2>(), perm.as<int>(), status);
+      kp<<<pgrid, kPanelThreads, psm, st>>>(mc, n, cm, k0, V.as<float2>(), perm.as<int>(), status);
       VS_LAUNCH_CHECK();
-      const int64_t ublocks = cm * tiles;
+      const int64_t ublocks = cm * r_tiles * q_tiles;
       VS_REQUIRE(ublocks < (int64_t(1) << 31), "too many blocks for one launch");
-      k_tc_update<<<(unsigned)ublocks, kUpdThreads, usm, st>>>(mc, n, cm, k0, V.as<float2>(), NT, tiles, status);
+      k_tc_update<<<(unsigned)ublocks, kUpdThreads, usm, st>>>(mc, n, cm, k0, V.as<float2>(), NT, q_tiles, r_tiles,
+                                                                status);
       VS_LAUNCH_CHECK();
     }
     k_tc_finish<<<(int)std::min<int64_t>(cm, (int64_t)nsm * 8), 256, fsm, st>>>(mc, n, cm, perm.as<int>(),

@@ -429,8 +429,7 @@ void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, co
   const int n = 3 * N;
   const int64_t nmat = (int64_t)Lb * Mb;
   const bool fp32 = std::is_same<T, float>::value;
-  const bool use_tc = invert && fp32 && tc_invert_supported(n) &&
-                      (lu == LU_TC || (lu == LU_AUTO && smem > 227 * 1024));
+  const bool use_tc = invert && fp32 && tc_invert_supported(n) && lu == LU_TC;
   if (use_tc) {
     VS_REQUIRE(colmajor, "tensor-core inversion produces column-major blocks");
     // the transposes assembled row-major; the inverse of A^T row-major is A^-1 column-major
@@ -471,6 +470,30 @@ void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, co
                                      status, Lb);
   VS_LAUNCH_CHECK();
 }
+// In-place inversion of nmat n x n FP32 complex matrices already in device
+// memory (either storage order: the inverse of the transpose is the
+// transpose of the inverse), scaled by `scale`.
+void invert_blocks_device(float2* mats, int n, int64_t nmat, int lu, double scale, int* status, cudaStream_t st) {
+  if (nmat <= 0) return;
+  if (lu == LU_TC && tc_invert_supported(n)) {
+    invert_blocks_tc(mats, n, nmat, scale, status, st);
+    return;
+  }
+  const size_t gsm = gj_blocked_smem(n, sizeof(float2));
+  if (gsm > 227 * 1024)
+    throw Error(VS_ERR_UNSUPPORTED, "block of " + std::to_string(n) + " is too large to invert");
+  auto k = k_gj_blocked<float, 32, gj_cn<float>()>;
+  set_kernel_smem((const void*)k, gsm);
+  int per_sm = 0;
+  VS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, gsm));
+  int dev = 0, nsm = 0;
+  VS_CUDA(cudaGetDevice(&dev));
+  VS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = (int)std::min<int64_t>(nmat, (int64_t)nsm * std::max(per_sm, 1));
+  k<<<grid, 256, gsm, st>>>(mats, n, nmat, scale, status);
+  VS_LAUNCH_CHECK();
+}
+
 template void assemble_invert<float>(const double2*, int, int, int, double2, const double2*, double2, bool, bool,
                                      double, float2*, int*, cudaStream_t, bool, int);
 template void assemble_invert<double>(const double2*, int, int, int, double2, const double2*, double2, bool, bool,
