@@ -326,6 +326,22 @@ int vs_solve_batch_device(vs_op* op, vs_prec* prec, const void* b, void* x, int6
 int vs_solve_particles_device(int64_t nparticles, vs_op* const* ops, vs_prec* const* precs, const void* const* b,
                               void* const* x, const int64_t* nrhs, const vs_solve_opts* opts, vs_solve_info* infos);
 
+/* Several particles solved in lockstep on one context (the loop of bicgstab
+ * calls over particles, incident directions and polarisations of
+ * main_DDA.m:61-82): every inner BiCGSTAB iteration of all particles is one
+ * CUDA graph launch whose branches -- one per particle, with its own operator,
+ * preconditioner and per-rhs Gram -- the GPU runs concurrently; the FP64
+ * refinement steps of all particles run together.  ops: distinct operators,
+ * all on one context; precs: NULL or distinct preconditioners (or NULL
+ * entries); b[i], x[i]: device double2, nrhs[i] * n3 each (x starts from 0);
+ * gram: NULL or per particle NULL / nrhs[i] * gram_n[i] complex (host), the
+ * Gram of each right-hand side as in vs_solve_opts.gram.  opts: BiCGSTAB,
+ * MIXED or FP64; opts->gram and opts->resvec must be NULL.  infos: sum(nrhs)
+ * entries, particle by particle. */
+int vs_solve_particles(int64_t nparticles, vs_op* const* ops, vs_prec* const* precs, const void* const* b,
+                       void* const* x, const int64_t* nrhs, const double* const* gram, const int64_t* gram_n,
+                       const vs_solve_opts* opts, vs_solve_info* infos);
+
 /* ---- excitation, extinction cross section, gradient ------------------- */
 
 /* Plane wave E0 .* exp(1i k.r) at op's unknowns: PlaneWavePointWise.m:7-19
@@ -422,6 +438,12 @@ typedef struct vs_prec_shape {
   int x_reg;       /* x passes: 0 shared-memory Stockham, 1 two-level registers */
   int fuse_xy;     /* 1: both FFTs of each (z, component) plane in one CTA when the
                       plane fits in shared memory; 0 / -1: separate x and y passes */
+  int wait_polls;  /* streamed GEMV (gemv_mode 1, 2): polls before a wait on another
+                      warp role gives up (0 = 2^20; -1 = none, every such wait
+                      gives up at once, for exercising the failure path).  A
+                      wait that runs out ends the CTA's work and the apply fails
+                      with VS_ERR_TIMEOUT; the wait for the CTA's own copies
+                      still in flight always keeps the full bound. */
 } vs_prec_shape;
 int vs_prec_get_shape(const vs_prec* prec, int precision, vs_prec_shape* shape);
 int vs_prec_set_shape(vs_prec* prec, int precision, const vs_prec_shape* shape);

@@ -239,6 +239,33 @@ def test_invert_blocks_device(api, n):
         api.invert_blocks_device(W.data_ptr(), n, nmat, "auto")
 
 
+def test_streamed_gemv_wait_that_runs_out_is_reported_and_recovered(api):
+    """The streamed GEMV's waits on other warp roles are bounded; with the
+    bound set to none every such wait gives up at once: the CTAs stop (the
+    producer still lets its own copies land), the apply reports
+    VS_ERR_TIMEOUT, and with the default bound restored the next apply is
+    correct."""
+    from voxscatter_gb300 import _lib
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, Toep, alpha, dV = _setup(p)
+    _, c1_o = O.circ_1_level(Toep, L, M, N, 0, "off")
+    _, blk_o = O.circ_2_level(c1_o, L, M, N)
+    inv_o = O.invert_blocks(blk_o, 1 / alpha, dV)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
+    x = np.random.default_rng(4).normal(size=idx3.size) + 0j
+    y_o = O.mvp_circ_2_level(inv_o, x, L, M, N, idx3)
+    for prec, tol in (("c64", 1e-4), ("c128", 1e-10)):
+        pr.set_shape(prec, gemv_mode=1, gemv_chunk=0, gemv_blocks=1, gemv_threads=0, fuse_xy=0, wait_polls=-1)
+        with pytest.raises(VoxScatterError) as e:
+            pr.apply(x, prec)
+        assert e.value.status == _lib.VS_ERR_TIMEOUT
+        pr.set_shape(prec, wait_polls=0)
+        assert pr.shape(prec)["wait_polls"] == 0
+        assert rel(pr.apply(x, prec), y_o) < tol
+        assert rel(pr.apply(x, prec), y_o) < tol
+
+
 def test_prec_build_options_rejected(api):
     p = W.small_hex(m=1.31 + 0.05j, diameter=2.0, nper=3)
     L, M, N, idx3, Toep, alpha, dV = _setup(p)

@@ -80,7 +80,7 @@ class vs_shape(C.Structure):
 class vs_prec_shape(C.Structure):
     _fields_ = [("lg_lines_x", C.c_int), ("lg_tile_y", C.c_int), ("gemv_blocks", C.c_int), ("gemv_threads", C.c_int),
                 ("gemv_mode", C.c_int), ("gemv_chunk", C.c_int), ("y_reg", C.c_int), ("x_reg", C.c_int),
-                ("fuse_xy", C.c_int)]
+                ("fuse_xy", C.c_int), ("wait_polls", C.c_int)]
 
 
 SIGNATURES.update({
@@ -93,6 +93,9 @@ SIGNATURES.update({
                                         C.POINTER(vs_solve_info)]),
     "vs_solve_particles_device": (C.c_int, [_i64, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp),
                                             C.POINTER(_i64), C.POINTER(vs_solve_opts), C.POINTER(vs_solve_info)]),
+    "vs_solve_particles": (C.c_int, [_i64, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp),
+                                     C.POINTER(_i64), C.POINTER(_pd), C.POINTER(_i64), C.POINTER(vs_solve_opts),
+                                     C.POINTER(vs_solve_info)]),
     "vs_plane_wave": (C.c_int, [_vp, _pd, _pd, _pd, _pd, _pd, _pd]),
     "vs_cext": (C.c_int, [_vp, _pd, _pd, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double)]),
     "vs_op_apply_domain": (C.c_int, [_vp, _pd, _pd, C.c_int64, _pd, _pd, C.c_int]),

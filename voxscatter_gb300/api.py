@@ -354,7 +354,7 @@ class Preconditioner:
                                                 C.byref(sh)))
         return dict(lg_lines_x=sh.lg_lines_x, lg_tile_y=sh.lg_tile_y, gemv_blocks=sh.gemv_blocks,
                     gemv_threads=sh.gemv_threads, gemv_mode=sh.gemv_mode, gemv_chunk=sh.gemv_chunk, y_reg=sh.y_reg,
-                    x_reg=sh.x_reg, fuse_xy=sh.fuse_xy)
+                    x_reg=sh.x_reg, fuse_xy=sh.fuse_xy, wait_polls=sh.wait_polls)
 
     def set_shape(self, precision="c64", **kw):
         cur = self.shape(precision)
@@ -680,6 +680,45 @@ def solve_particles_device(ops, precs, b_ptrs, x_ptrs, nrhs, tol=1e-6, maxit=200
     nr = (C.c_int64 * k)(*[int(v) for v in nrhs])
     infos = (L.vs_solve_info * int(sum(nrhs)))()
     L.check(lib.vs_solve_particles_device(k, pops, ppr, arr(b_ptrs), arr(x_ptrs), nr, C.byref(o), infos))
+    out, at = [], 0
+    for v in nrhs:
+        out.append([dict(flag=i.flag, relres=i.relres, iter=i.iter, refinements=i.refinements, time_ms=i.time_ms,
+                         launches=i.kernel_launches) for i in infos[at:at + int(v)]])
+        at += int(v)
+    return out
+
+
+def solve_particles(ops, precs, b_ptrs, x_ptrs, nrhs, grams=None, tol=1e-6, maxit=2000, precision="mixed",
+                    iters_per_graph=4):
+    """vs_solve_particles: several particles (distinct operators on one
+    Context) solved in lockstep, one CUDA graph launch per inner iteration of
+    all of them.  b_ptrs / x_ptrs: device buffers (complex128, nrhs[i]*n3
+    each; x starts from zero); grams: None or per particle None / the Gram of
+    each right-hand side (nrhs[i] scalars or grids).  Returns one list of
+    info dicts per particle."""
+    if not ops:
+        return []
+    lib = ops[0].ctx._lib
+    k = len(ops)
+    o = _solve_opts(lib, tol, maxit, precision)
+    o.iters_per_graph = int(iters_per_graph)
+    raw = lambda v: v.value if isinstance(v, C.c_void_p) else v
+    arr = lambda vals: (C.c_void_p * k)(*[C.c_void_p(raw(v)) for v in vals])
+    keep = []
+    gptr = (L._pd * k)()
+    gn = (C.c_int64 * k)()
+    for i in range(k):
+        if grams is not None and grams[i] is not None:
+            g, n_ = _gram_array(grams[i], int(nrhs[i]), ops[i].LMN)
+            keep.append(g)
+            gptr[i] = L.dptr(g)
+            gn[i] = n_
+    nr = (C.c_int64 * k)(*[int(v) for v in nrhs])
+    infos = (L.vs_solve_info * int(sum(nrhs)))()
+    L.check(lib.vs_solve_particles(k, arr([op.h for op in ops]),
+                                   arr([pr.h if pr is not None else None for pr in (precs or [None] * k)]),
+                                   arr(b_ptrs), arr(x_ptrs), nr, gptr if grams is not None else None, gn,
+                                   C.byref(o), infos), ops[0].ctx.h)
     out, at = [], 0
     for v in nrhs:
         out.append([dict(flag=i.flag, relres=i.relres, iter=i.iter, refinements=i.refinements, time_ms=i.time_ms,

@@ -9,6 +9,7 @@
 #include <complex>
 #include <cstring>
 #include <cmath>
+#include <set>
 
 namespace {
 
@@ -199,7 +200,11 @@ void check_prec_status(vs_prec* pr) {
   if (!pr || !pr->gemv_status.p) return;
   int hs = 0;
   VS_CUDA(cudaMemcpy(&hs, pr->gemv_status.p, sizeof(int), cudaMemcpyDeviceToHost));
-  VS_REQUIRE(hs == 0, "a streamed preconditioner copy did not complete in time");
+  if (hs != 0) {
+    // reported once: the next apply starts from a clear status
+    VS_CUDA(cudaMemset(pr->gemv_status.p, 0, sizeof(int)));
+    throw vs::Error(VS_ERR_TIMEOUT, "a streamed preconditioner GEMV wait ran out (its result is not valid)");
+  }
 }
 
 void prec_scratch_impl(vs_prec* pr, int64_t nrhs) {
@@ -332,6 +337,9 @@ void ctx_retain(vs_ctx* ctx) {
 void ctx_release(vs_ctx* ctx) {
   if (!ctx || ctx->refs.fetch_sub(1) != 1) return;
   cudaSetDevice(ctx->device);
+  ctx->pgraph32.reset();
+  ctx->pgraph64.reset();
+  for (cudaStream_t a : ctx->aux) cudaStreamDestroy(a);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -995,6 +1003,7 @@ int vs_prec_get_shape(const vs_prec* prec, int precision, vs_prec_shape* shape) 
   shape->y_reg = s.y_reg;
   shape->x_reg = s.x_reg;
   shape->fuse_xy = s.fuse_xy;
+  shape->wait_polls = s.wait_polls;
   return VS_OK;
 }
 
@@ -1032,6 +1041,8 @@ int vs_prec_set_shape(vs_prec* prec, int precision, const vs_prec_shape* shape) 
     s.y_reg = shape->y_reg;
     s.x_reg = shape->x_reg;
     s.fuse_xy = shape->fuse_xy;
+    VS_REQUIRE(shape->wait_polls >= -1, "wait_polls must be >= -1");
+    s.wait_polls = shape->wait_polls;
   });
 }
 
@@ -1364,6 +1375,61 @@ int vs_solve_particles_device(int64_t nparticles, vs_op* const* ops, vs_prec* co
       return status[g];
     }
   return VS_OK;
+}
+
+int vs_solve_particles(int64_t nparticles, vs_op* const* ops, vs_prec* const* precs, const void* const* b,
+                       void* const* x, const int64_t* nrhs, const double* const* gram, const int64_t* gram_n,
+                       const vs_solve_opts* opts, vs_solve_info* infos) {
+  if (nparticles < 1 || !ops || !ops[0]) {
+    g_last_error = "vs_solve_particles: no particles or NULL operator";
+    return VS_ERR_ARG;
+  }
+  vs_ctx* ctx = ops[0]->ctx;
+  return guarded(ctx, [&] {
+    VS_REQUIRE(b && x && nrhs && opts && infos, "vs_solve_particles: NULL argument");
+    VS_REQUIRE(nparticles <= 65536, "vs_solve_particles: at most 65536 particles");
+    VS_REQUIRE(opts->method == VS_BICGSTAB, "vs_solve_particles runs BiCGSTAB");
+    VS_REQUIRE(opts->gram == nullptr, "vs_solve_particles takes the Gram per right-hand side in `gram`, not opts");
+    VS_REQUIRE(opts->resvec == nullptr, "vs_solve_particles returns no residual history (opts->resvec must be NULL)");
+    std::vector<vs::PartJob> jobs(nparticles);
+    std::set<const void*> seen_op, seen_pr;
+    int64_t total = 0;
+    for (int64_t i = 0; i < nparticles; ++i) {
+      vs_op* op = ops[i];
+      VS_REQUIRE(op != nullptr, "vs_solve_particles: NULL operator for particle " + std::to_string(i));
+      VS_REQUIRE(op->ctx == ctx, "vs_solve_particles: all operators must be on one context");
+      VS_REQUIRE(seen_op.insert(op).second, "vs_solve_particles: an operator appears twice");
+      vs_prec* pr = precs ? precs[i] : nullptr;
+      if (pr) VS_REQUIRE(seen_pr.insert(pr).second, "vs_solve_particles: a preconditioner appears twice");
+      VS_REQUIRE(b[i] && x[i], "vs_solve_particles: NULL b or x for particle " + std::to_string(i));
+      VS_REQUIRE(nrhs[i] >= 1 && nrhs[i] <= 4096, "vs_solve_particles: nrhs must be in [1, 4096]");
+      vs::SolveParams chk = solve_params(op, pr, opts);  // precision, tolerance and preconditioner checks
+      (void)chk;
+      const double* g = gram ? gram[i] : nullptr;
+      if (g) VS_REQUIRE(gram_n && (gram_n[i] == 1 || gram_n[i] == op->V),
+                        "vs_solve_particles: gram_n[i] must be 1 or L*M*N");
+      jobs[i].op = op;
+      jobs[i].pr = pr;
+      jobs[i].b = (const double2*)b[i];
+      jobs[i].x = (double2*)x[i];
+      jobs[i].nrhs = (int)nrhs[i];
+      jobs[i].gram = reinterpret_cast<const double2*>(g);
+      jobs[i].gram_n = g ? gram_n[i] : 0;
+      total += nrhs[i];
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    vs::SolveParams prm = solve_params(ops[0], jobs[0].pr, opts);
+    vs::solve_bicgstab_particles(ctx, jobs, prm, ctx->stream);
+    for (auto& j : jobs) check_prec_status(j.pr);
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    int64_t at = 0;
+    for (auto& j : jobs)
+      for (auto& r : j.out) {
+        fill_info(r, infos + at);
+        infos[at++].time_ms = ms;
+      }
+    (void)total;
+  });
 }
 
 int vs_solve_batch(vs_op* op, vs_prec* prec, const double* b, double* x, int64_t nrhs, const vs_solve_opts* opts,

@@ -58,6 +58,7 @@ struct PassShape {
   int z_reg = -1;      // z pass: 0 shared-memory Stockham, 1 two-level, 2 two-level with register cap, -1 default
   int fuse_xy = -1;    // preconditioner: 1 both x/y FFTs of a plane in one CTA (when it fits), 0/-1 separate passes
   int z_df = -1;       // c128 z pass: 1 double-float arithmetic on the FP64 data (two-level kernel only)
+  int wait_polls = 0;  // streamed GEMV: polls before a wait on another warp role gives up (0: 2^20, -1: none)
 };
 
 // Gram of each right-hand side, in place of the operator's (the reference
@@ -116,6 +117,12 @@ struct vs_ctx {
   std::string err;
   vs::DevBuf stage;  // host<->device staging for the host-buffer entry points
   std::atomic<int> refs{1};
+  // lockstep multi-particle solves: the auxiliary streams their graphs' branches
+  // are captured on, the cached iteration graphs, and the device table of the
+  // particles' states / rhs offsets / gathered skip flags
+  std::vector<cudaStream_t> aux;
+  vs::GraphCache pgraph32, pgraph64;
+  vs::DevBuf pstates, poff, pskip;
 };
 void ctx_retain(vs_ctx* ctx);
 void ctx_release(vs_ctx* ctx);

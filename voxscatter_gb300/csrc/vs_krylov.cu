@@ -21,6 +21,7 @@
 #include <chrono>
 #include <cmath>
 #include <vector>
+#include <memory>
 
 namespace vs {
 
@@ -806,6 +807,421 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
   std::vector<SolveResult> r;
   solve_bicgstab_batch(op, pr, b, x, 1, prm, r, st);
   out = r[0];
+}
+
+// ===========================================================================
+// Lockstep BiCGSTAB over several particles (the reference solves each
+// particle, incident direction and polarisation with its own bicgstab call,
+// main_DDA.m:61-82).  Every particle keeps its own operator, preconditioner,
+// work buffers and per-rhs states; an inner iteration of all particles is one
+// CUDA graph whose branches (one per particle, forked to auxiliary streams
+// during capture) the GPU runs concurrently, so the small particles' launches
+// overlap instead of queueing.  A last node gathers every right-hand side's
+// skip flag, so the host polls all particles with one copy per graph launch.
+// Converged right-hand sides keep costing nothing but empty CTAs (skip flag),
+// and a particle whose right-hand sides all converged skips whole launches.
+// The FP64 refinement steps run in lockstep too (one host synchronisation per
+// phase for all particles).
+// ===========================================================================
+
+// out[off[p] + r] = states_p[r].skip
+__global__ void k_gather_skip(const KState* const* states, const int* off, int nparts, int* out) {
+  for (int p = blockIdx.x; p < nparts; p += gridDim.x)
+    for (int r = threadIdx.x; r < off[p + 1] - off[p]; r += blockDim.x) out[off[p] + r] = states[p][r].skip;
+}
+
+namespace {
+
+constexpr int kMaxAuxStreams = 16;
+
+// Per-particle bookkeeping of a lockstep solve.
+struct PartState {
+  PartJob* job = nullptr;
+  int64_t n = 0;
+  std::unique_ptr<RhsGramScope> gram;
+  std::vector<double> bnorm, bsafe, rn, scal;
+  std::vector<int> inner2, flag, refine;
+  std::vector<double> tolr, rscale;  // inner solve: tolerance factor and resvec scale per rhs
+  std::vector<KState> h, cur;
+};
+
+// Enqueue ||u_r|| (FP64, compensated) of every particle into its w.scal.
+void enqueue_norms(std::vector<PartState>& ps, const std::vector<const double2*>& u, cudaStream_t st) {
+  for (size_t i = 0; i < ps.size(); ++i) {
+    PartState& p = ps[i];
+    KrylovWork& w = p.job->op->kw;
+    p.h.assign(p.job->nrhs, KState{});
+    upload_states(w, p.h, st);
+    k_norm<double><<<dim3(vec_grid(p.n), p.job->nrhs), kRedThreads, 0, st>>>(u[i], p.n, w.state.as<KState>(),
+                                                                             w.scal.as<double>());
+  }
+  VS_LAUNCH_CHECK();
+}
+
+// r64 = b - A x64 for every particle (its Gram per rhs), norms into w.scal.
+void enqueue_residuals(std::vector<PartState>& ps, const std::vector<double2*>& xs, std::vector<double2*>& rs,
+                       int mode, cudaStream_t st) {
+  for (size_t i = 0; i < ps.size(); ++i) {
+    PartState& p = ps[i];
+    vs_op& op = *p.job->op;
+    KrylovWork& w = op.kw;
+    p.h.assign(p.job->nrhs, KState{});
+    upload_states(w, p.h, st);
+    matvec<double>(op, xs[i], w.y64.as<double2>(), p.job->nrhs, mode, nullptr, st, 0, rgp(w));
+    k_resid64<<<dim3(vec_grid(p.n), p.job->nrhs), kRedThreads, 0, st>>>(p.job->b, w.y64.as<double2>(), rs[i], p.n,
+                                                                       w.state.as<KState>(), w.scal.as<double>());
+  }
+  VS_LAUNCH_CHECK();
+}
+
+// Copy every particle's w.scal (nrhs doubles) to p.scal; one synchronisation.
+void read_all_scal(std::vector<PartState>& ps, cudaStream_t st) {
+  for (auto& p : ps) {
+    p.scal.resize(p.job->nrhs);
+    VS_CUDA(cudaMemcpyAsync(p.scal.data(), p.job->op->kw.scal.p, p.job->nrhs * sizeof(double),
+                            cudaMemcpyDeviceToHost, st));
+  }
+  VS_CUDA(cudaStreamSynchronize(st));
+}
+
+// Lockstep inner BiCGSTAB on every particle's w.x / w.r (precision T): rhs r
+// of particle p stops at ||r|| <= tol * p.tolr[r], resvec entries scaled by
+// p.rscale[r].  Returns with p.cur holding the final states.
+template <typename T>
+void bicgstab_lockstep(vs_ctx* ctx, std::vector<PartState>& ps, double tol, int maxit, int per_graph, int stag,
+                       int mode, cudaStream_t st, int64_t* launches) {
+  using C = cplx_t<T>;
+  const int np = (int)ps.size();
+  bool any_active = false;
+  for (auto& p : ps) {
+    const int nrhs = p.job->nrhs;
+    KrylovWork& w = p.job->op->kw;
+    p.h.assign(nrhs, KState{});
+    for (int r = 0; r < nrhs; ++r) {
+      KState& k = p.h[r];
+      k.tol_abs = tol * p.tolr[r];
+      k.maxit = maxit;
+      k.res_scale = p.rscale[r];
+      k.flag = 1;
+      k.stag_window = stag;
+      k.best_res = INFINITY;
+    }
+    upload_states(w, p.h, st);
+    k_copy<T><<<vec_grid(p.n * nrhs), 256, 0, st>>>(w.rt.as<C>(), w.r.as<C>(), p.n * nrhs);
+    k_norm<T><<<dim3(vec_grid(p.n), nrhs), kRedThreads, 0, st>>>(w.r.as<C>(), p.n, w.state.as<KState>(),
+                                                                 w.scal.as<double>());
+    *launches += 2;
+  }
+  VS_LAUNCH_CHECK();
+  read_all_scal(ps, st);
+  for (auto& p : ps) {
+    for (int r = 0; r < p.job->nrhs; ++r) {
+      KState& k = p.h[r];
+      k.res = p.scal[r];
+      k.nres = 1;
+      k.best_res = p.scal[r];
+      if (!(p.scal[r] > k.tol_abs) || maxit <= 0) {
+        k.flag = (p.scal[r] <= k.tol_abs) ? 0 : 1;
+        k.skip = 1;
+      } else {
+        any_active = true;
+      }
+    }
+    p.cur = p.h;
+  }
+  if (!any_active) return;
+  // the graph: every particle's iterations as a branch, then the skip gather
+  GraphCache& gc = std::is_same<T, float>::value ? ctx->pgraph32 : ctx->pgraph64;
+  std::vector<const void*> key = {(const void*)(uintptr_t)per_graph, (const void*)(uintptr_t)mode,
+                                  (const void*)(uintptr_t)np, ctx->pskip.p, ctx->pstates.p, ctx->poff.p};
+  for (auto& p : ps) {
+    const vs_op& op = *p.job->op;
+    const KrylovWork& w = op.kw;
+    const vs_prec* pr = p.job->pr;
+    const void* bufs[] = {w.r.p, w.rt.p, w.p.p, w.v_.p, w.s.p, w.t.p, w.ph.p, w.sh.p, w.x.p, w.state.p,
+                          w.partials.p, op.t1.p, op.t2.p, (const void*)w.rg.g32, (const void*)w.rg.g64};
+    for (const void* v : bufs) key.push_back(v);
+    key.push_back((const void*)(uintptr_t)w.rg.per);
+    key.push_back((const void*)(uintptr_t)p.job->nrhs);
+    key.push_back((const void*)(uintptr_t)(pr ? pr->id : 0));
+    key.push_back(pr ? pr->t.p : nullptr);
+  }
+  if (gc.exec == nullptr || gc.key != key) {
+    gc.reset();
+    // one idle launch sequence per particle outside capture (first-use attribute calls)
+    for (auto& p : ps) {
+      KrylovWork& w = p.job->op->kw;
+      std::vector<KState> idle = p.h;
+      for (auto& k : idle) k.skip = 1;
+      upload_states(w, idle, st);
+      bicg_iteration<T>(*p.job->op, p.job->pr, w, w.state.as<KState>(), p.n, p.job->nrhs, mode, st);
+      *launches += kernels_per_iteration<T>(p.job->pr);
+    }
+    VS_CUDA(cudaStreamSynchronize(st));
+    const int naux = std::min(np, kMaxAuxStreams);
+    while ((int)ctx->aux.size() < naux) {
+      cudaStream_t a;
+      VS_CUDA(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
+      ctx->aux.push_back(a);
+    }
+    std::vector<cudaEvent_t> ev(np + 1, nullptr);
+    auto destroy_events = [&] {
+      for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    };
+    cudaGraph_t graph = nullptr;
+    try {
+      for (auto& e : ev) VS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      VS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      try {
+        VS_CUDA(cudaEventRecord(ev[np], st));
+        for (int i = 0; i < np; ++i) {
+          cudaStream_t si = ctx->aux[i % naux];
+          VS_CUDA(cudaStreamWaitEvent(si, ev[np], 0));
+          PartState& p = ps[i];
+          KrylovWork& w = p.job->op->kw;
+          for (int k = 0; k < per_graph; ++k)
+            bicg_iteration<T>(*p.job->op, p.job->pr, w, w.state.as<KState>(), p.n, p.job->nrhs, mode, si);
+          VS_CUDA(cudaEventRecord(ev[i], si));
+        }
+        for (int i = 0; i < np; ++i) VS_CUDA(cudaStreamWaitEvent(st, ev[i], 0));
+        k_gather_skip<<<std::min(np, 152), 32, 0, st>>>(ctx->pstates.as<const KState*>(), ctx->poff.as<int>(), np,
+                                                          ctx->pskip.as<int>());
+        VS_LAUNCH_CHECK();
+      } catch (...) {
+        cudaStreamEndCapture(st, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        throw;
+      }
+      VS_CUDA(cudaStreamEndCapture(st, &graph));
+      cudaError_t e = cudaGraphInstantiate(&gc.exec, graph, 0);
+      cudaGraphDestroy(graph);
+      VS_CUDA(e);
+      gc.key = key;
+    } catch (...) {
+      destroy_events();
+      throw;
+    }
+    destroy_events();
+  }
+  for (auto& p : ps) {
+    KrylovWork& w = p.job->op->kw;
+    upload_states(w, p.h, st);
+    k_bicg_rho<T><<<dim3(vec_grid(p.n), p.job->nrhs), kRedThreads, 0, st>>>(w.rt.as<C>(), w.r.as<C>(), p.n,
+                                                                           w.state.as<KState>());
+    *launches += 1;
+  }
+  VS_LAUNCH_CHECK();
+  int total = 0;
+  for (auto& p : ps) total += p.job->nrhs;
+  std::vector<int> skip(total);
+  int64_t per_launch = 1;
+  for (auto& p : ps) per_launch += (int64_t)per_graph * kernels_per_iteration<T>(p.job->pr);
+  const int max_launch = (maxit + per_graph - 1) / per_graph + 1;
+  for (int it = 0; it < max_launch; ++it) {
+    VS_CUDA(cudaGraphLaunch(gc.exec, st));
+    *launches += per_launch;
+    VS_CUDA(cudaMemcpyAsync(skip.data(), ctx->pskip.p, total * sizeof(int), cudaMemcpyDeviceToHost, st));
+    VS_CUDA(cudaStreamSynchronize(st));
+    bool all = true;
+    for (int v : skip) all = all && v;
+    if (all) break;
+  }
+  for (auto& p : ps) {
+    p.cur.resize(p.job->nrhs);
+    VS_CUDA(cudaMemcpyAsync(p.cur.data(), p.job->op->kw.state.p, p.job->nrhs * sizeof(KState),
+                            cudaMemcpyDeviceToHost, st));
+  }
+  VS_CUDA(cudaStreamSynchronize(st));
+  for (auto& p : ps)
+    for (auto& k : p.cur)
+      if (!k.skip) k.flag = 1;
+}
+
+}  // namespace
+
+void solve_bicgstab_particles(vs_ctx* ctx, std::vector<PartJob>& jobs, const SolveParams& prm, cudaStream_t st) {
+  const int np = (int)jobs.size();
+  std::vector<PartState> ps(np);
+  std::vector<int> off(np + 1, 0);
+  std::vector<const KState*> sp(np);
+  int64_t launches = 0;
+  for (int i = 0; i < np; ++i) {
+    PartState& p = ps[i];
+    p.job = &jobs[i];
+    vs_op& op = *jobs[i].op;
+    KrylovWork& w = op.kw;
+    const int nrhs = jobs[i].nrhs;
+    p.n = op.n3;
+    SolveParams pi = prm;
+    pi.gram_host = jobs[i].gram;
+    pi.gram_n = jobs[i].gram_n;
+    p.gram.reset(new RhsGramScope(op, w, pi, nrhs, st));
+    reduction_buffers(w, nrhs);
+    ensure_scratch(op, nrhs, sizeof(double2));
+    if (jobs[i].pr) {
+      vs_prec& pr = *jobs[i].pr;
+      const size_t need = (size_t)pr.L * pr.M * pr.N * 3 * sizeof(double2) * nrhs;
+      if (pr.t.bytes < need) pr.t.alloc(need);
+    }
+    if (prm.mode == VS_SOLVE_FP64) w.ensure<double>(p.n * nrhs);
+    else w.ensure<float>(p.n * nrhs);
+    w.y64.alloc(p.n * nrhs * sizeof(double2));
+    w.r64.alloc(p.n * nrhs * sizeof(double2));
+    off[i + 1] = off[i] + nrhs;
+    sp[i] = w.state.as<KState>();
+    jobs[i].out.assign(nrhs, SolveResult{});
+  }
+  ctx->pstates.alloc(np * sizeof(KState*));
+  ctx->poff.alloc((np + 1) * sizeof(int));
+  ctx->pskip.alloc(std::max(1, off[np]) * sizeof(int));
+  VS_CUDA(cudaMemcpyAsync(ctx->pstates.p, sp.data(), np * sizeof(KState*), cudaMemcpyHostToDevice, st));
+  VS_CUDA(cudaMemcpyAsync(ctx->poff.p, off.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+  // ||b||, and a zero initial guess (the particles entry starts from x = 0)
+  std::vector<const double2*> bs(np);
+  for (int i = 0; i < np; ++i) bs[i] = jobs[i].b;
+  enqueue_norms(ps, bs, st);
+  read_all_scal(ps, st);
+  for (int i = 0; i < np; ++i) {
+    PartState& p = ps[i];
+    const int nrhs = jobs[i].nrhs;
+    p.bnorm = p.scal;
+    p.bsafe.resize(nrhs);
+    for (int r = 0; r < nrhs; ++r) {
+      if (!std::isfinite(p.bnorm[r])) throw Error(VS_ERR_NONFINITE, "right-hand side has NaN or Inf entries");
+      p.bsafe[r] = p.bnorm[r] > 0 ? p.bnorm[r] : 1.0;
+    }
+    VS_CUDA(cudaMemsetAsync(jobs[i].x, 0, p.n * nrhs * sizeof(double2), st));
+    p.inner2.assign(nrhs, 0);
+    p.flag.assign(nrhs, 1);
+    p.refine.assign(nrhs, 0);
+  }
+  std::vector<double2*> xs(np), r64s(np), rws(np);
+  for (int i = 0; i < np; ++i) {
+    xs[i] = jobs[i].x;
+    r64s[i] = jobs[i].op->kw.r64.as<double2>();
+  }
+  if (prm.mode == VS_SOLVE_FP64) {
+    for (int i = 0; i < np; ++i) {
+      PartState& p = ps[i];
+      KrylovWork& w = jobs[i].op->kw;
+      const int64_t m = p.n * jobs[i].nrhs;
+      k_zero<double><<<vec_grid(m), 256, 0, st>>>(w.x.as<double2>(), m);
+      k_copy<double><<<vec_grid(m), 256, 0, st>>>(w.r.as<double2>(), jobs[i].b, m);
+      p.tolr = p.bsafe;
+      p.rscale.resize(jobs[i].nrhs);
+      for (int r = 0; r < jobs[i].nrhs; ++r) p.rscale[r] = 1.0 / p.bsafe[r];
+    }
+    bicgstab_lockstep<double>(ctx, ps, prm.tol, prm.maxit, prm.per_graph, 0, prm.op_mode, st, &launches);
+    for (int i = 0; i < np; ++i) {
+      KrylovWork& w = jobs[i].op->kw;
+      const int64_t m = ps[i].n * jobs[i].nrhs;
+      k_copy<double><<<vec_grid(m), 256, 0, st>>>(jobs[i].x, w.x.as<double2>(), m);
+    }
+    enqueue_residuals(ps, xs, r64s, prm.op_mode, st);
+    read_all_scal(ps, st);
+    for (int i = 0; i < np; ++i) {
+      PartState& p = ps[i];
+      for (int r = 0; r < jobs[i].nrhs; ++r) {
+        SolveResult& o = jobs[i].out[r];
+        o.flag = p.cur[r].flag;
+        o.iter = o.inner_iters = p.cur[r].iter2 * 0.5;
+        o.relres = p.bnorm[r] > 0 ? p.scal[r] / p.bnorm[r] : 0.0;
+        if (p.bnorm[r] == 0) o.flag = 0;
+        else if (o.flag == 0 && o.relres > prm.tol) o.flag = 1;
+      }
+    }
+  } else {
+    // mixed: c64 inner solves of all particles in lockstep inside FP64 refinement
+    for (int i = 0; i < np; ++i) {
+      const int64_t m = ps[i].n * jobs[i].nrhs;
+      k_copy<double><<<vec_grid(m), 256, 0, st>>>(r64s[i], jobs[i].b, m);
+      ps[i].rn = ps[i].bnorm;
+    }
+    VS_LAUNCH_CHECK();
+    DevBuf scd;
+    int maxr = 1;
+    for (auto& j : jobs) maxr = std::max(maxr, j.nrhs);
+    std::vector<DevBuf> scales(np);
+    for (int step = 0; step <= prm.max_refine; ++step) {
+      bool all_done = true;
+      int used = 0;
+      for (auto& p : ps)
+        for (int r = 0; r < p.job->nrhs; ++r) {
+          const bool done = p.rn[r] <= prm.tol * p.bnorm[r] || p.flag[r] >= 4;
+          if (p.rn[r] <= prm.tol * p.bnorm[r]) p.flag[r] = 0;
+          all_done = all_done && done;
+          used = std::max(used, p.inner2[r]);
+        }
+      if (all_done || step == prm.max_refine || used >= 2 * prm.maxit) break;
+      // per-rhs inner tolerance relative to the scaled residual; one common
+      // inner tolerance tmin, expressed per rhs through tolr = itol / tmin
+      double tmin = 1.0;
+      std::vector<std::vector<double>> itol(np);
+      for (int i = 0; i < np; ++i) {
+        PartState& p = ps[i];
+        const int nrhs = jobs[i].nrhs;
+        itol[i].resize(nrhs);
+        std::vector<double> scale(nrhs);
+        p.rscale.resize(nrhs);
+        for (int r = 0; r < nrhs; ++r) {
+          const bool done = p.rn[r] <= prm.tol * p.bnorm[r] || p.flag[r] >= 4;
+          scale[r] = p.rn[r] > 0 ? 1.0 / p.rn[r] : 0.0;
+          const double t = prm.inner_tol > 0 ? prm.inner_tol
+                                             : std::max(0.3 * prm.tol * p.bnorm[r] / p.rn[r], prm.inner_floor);
+          itol[i][r] = done ? 2.0 : std::min(t, 0.5);
+          p.rscale[r] = p.bnorm[r] > 0 ? p.rn[r] / p.bnorm[r] : 0.0;
+          p.refine[r] += done ? 0 : 1;
+          tmin = std::min(tmin, itol[i][r]);
+        }
+        KrylovWork& w = jobs[i].op->kw;
+        scales[i].alloc(nrhs * sizeof(double));
+        VS_CUDA(cudaMemcpyAsync(scales[i].p, scale.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, st));
+        k_scale_down<<<dim3(vec_grid(p.n), nrhs), 256, 0, st>>>(r64s[i], w.r.as<float2>(), p.n, scales[i].as<double>());
+        k_zero<float><<<vec_grid(p.n * nrhs), 256, 0, st>>>(w.x.as<float2>(), p.n * nrhs);
+        launches += 2;
+      }
+      for (int i = 0; i < np; ++i) {
+        ps[i].tolr.resize(jobs[i].nrhs);
+        for (int r = 0; r < jobs[i].nrhs; ++r) ps[i].tolr[r] = itol[i][r] / tmin;
+      }
+      bicgstab_lockstep<float>(ctx, ps, tmin, prm.maxit - used / 2, prm.per_graph, kStagnationWindow, prm.op_mode, st,
+                               &launches);
+      bool progressed = false;
+      for (int i = 0; i < np; ++i) {
+        PartState& p = ps[i];
+        const int nrhs = jobs[i].nrhs;
+        for (int r = 0; r < nrhs; ++r) {
+          p.inner2[r] += p.cur[r].iter2;
+          if (p.cur[r].flag >= 4 && p.cur[r].iter2 == 0 && !(p.rn[r] <= prm.tol * p.bnorm[r])) p.flag[r] = p.cur[r].flag;
+          progressed = progressed || p.cur[r].iter2 > 0;
+        }
+        KrylovWork& w = jobs[i].op->kw;
+        VS_CUDA(cudaMemcpyAsync(scales[i].p, p.rn.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, st));
+        k_update64<<<dim3(vec_grid(p.n), nrhs), 256, 0, st>>>(jobs[i].x, w.x.as<float2>(), p.n, scales[i].as<double>());
+        launches += 1;
+      }
+      VS_LAUNCH_CHECK();
+      enqueue_residuals(ps, xs, r64s, prm.op_mode, st);
+      read_all_scal(ps, st);
+      for (auto& p : ps) p.rn = p.scal;
+      if (!progressed) break;
+    }
+    for (int i = 0; i < np; ++i) {
+      PartState& p = ps[i];
+      for (int r = 0; r < jobs[i].nrhs; ++r) {
+        SolveResult& o = jobs[i].out[r];
+        o.flag = (p.rn[r] <= prm.tol * p.bnorm[r]) ? 0 : (p.flag[r] >= 4 ? p.flag[r] : 1);
+        o.relres = p.bnorm[r] > 0 ? p.rn[r] / p.bnorm[r] : 0.0;
+        o.iter = o.inner_iters = p.inner2[r] * 0.5;
+        o.refinements = p.refine[r];
+        if (p.bnorm[r] == 0) o.flag = 0;
+      }
+    }
+  }
+  for (auto& j : jobs)
+    for (auto& o : j.out) o.launches = launches;
+  VS_CUDA(cudaStreamSynchronize(st));
 }
 
 }  // namespace vs

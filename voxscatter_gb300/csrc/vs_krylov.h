@@ -60,6 +60,21 @@ void solve_bicgstab(vs_op& op, vs_prec* pr, const double2* b, double2* x, const 
                     cudaStream_t st);
 void solve_bicgstab_batch(vs_op& op, vs_prec* pr, const double2* b, double2* x, int nrhs, const SolveParams& prm,
                           std::vector<SolveResult>& out, cudaStream_t st);
+// One particle of a lockstep multi-particle BiCGSTAB solve (device b and x,
+// nrhs * n3 each; gram: host Gram per rhs or nullptr).
+struct PartJob {
+  vs_op* op = nullptr;
+  vs_prec* pr = nullptr;
+  const double2* b = nullptr;
+  double2* x = nullptr;
+  int nrhs = 0;
+  const double2* gram = nullptr;
+  int64_t gram_n = 0;
+  std::vector<SolveResult> out;
+};
+// All particles' operators on ctx (one stream), distinct operators and
+// preconditioners; x starts from zero.
+void solve_bicgstab_particles(vs_ctx* ctx, std::vector<PartJob>& jobs, const SolveParams& prm, cudaStream_t st);
 void solve_gmres(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,
                  cudaStream_t st);
 void solve_gmres_dr(vs_op& op, vs_prec* pr, const double2* b, double2* x, const SolveParams& prm, SolveResult& out,

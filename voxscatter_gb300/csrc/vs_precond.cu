@@ -716,8 +716,10 @@ __device__ __forceinline__ uint64_t l2_evict_first_policy() {
   return p;
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (int i = 0; i < (1 << 20); ++i) {
+constexpr int kGemvPolls = 1 << 20;  // default bound of every streamed-GEMV wait
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int polls = kGemvPolls) {
+  for (int i = 0; i < polls; ++i) {
     uint32_t ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
@@ -776,7 +778,7 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
                                                            int L, int M, int N, int64_t rhs_stride, int nrhs,
                                                            const int* skip, int skip_stride, int cq, int nstage,
                                                            int stage_elems, int G, int nc, int nv,
-                                                           int* __restrict__ status) {
+                                                           int* __restrict__ status, int polls) {
   using C = cplx_t<T>;
   constexpr int W = 4 * RG, RW = PAIR ? 2 : 1;
   const int rhs0 = blockIdx.y * RG;
@@ -870,7 +872,7 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
     for (int64_t kb = 0; kb < nmine; ++kb) {
       const int b = (int)(kb & 1);
       bool ok = true;
-      if (lane == 0) ok = !ctl[0] && mbar_wait(smem_addr(done + b), (uint32_t)((kb >> 1) & 1));
+      if (lane == 0) ok = !ctl[0] && mbar_wait(smem_addr(done + b), (uint32_t)((kb >> 1) & 1), polls);
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) {
         if (lane == 0) fail();
@@ -901,7 +903,7 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
       int s = 0, round = 0, cc = 0;
       for (; ch < total; ++ch) {
         if (ctl[0]) break;
-        if (round > 0 && !mbar_wait(smem_addr(empty + s), (uint32_t)((round - 1) & 1))) {
+        if (round > 0 && !mbar_wait(smem_addr(empty + s), (uint32_t)((round - 1) & 1), polls)) {
           fail();
           break;
         }
@@ -941,7 +943,7 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
   uint32_t sph = 0;
   for (int64_t kb = 0; kb < nmine; ++kb) {
     const int b = (int)(kb & 1);
-    bool ok = !ctl[0] && mbar_wait(smem_addr(vfull + b), (uint32_t)((kb >> 1) & 1));
+    bool ok = !ctl[0] && mbar_wait(smem_addr(vfull + b), (uint32_t)((kb >> 1) & 1), polls);
     const C* vt = vt0 + (size_t)b * nW;
     C acc[RW][W];
 #pragma unroll
@@ -950,7 +952,7 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
       for (int c = 0; c < W; ++c) acc[h][c] = czero<C>();
     const C* blk = PACKED ? inv : inv + (blockIdx.x + kb * gridDim.x) * (int64_t)n * n;
     for (int cc = 0; cc < cpb && ok; ++cc) {
-      ok = !ctl[0] && mbar_wait(smem_addr(full + s), sph);
+      ok = !ctl[0] && mbar_wait(smem_addr(full + s), sph, polls);
       if (!ok) break;
       if (PACKED && tid < nact) {
         // the lower triangle of S: column q (rows q..n-1) from q n - q (q - 1) / 2;
@@ -1025,7 +1027,7 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
         sph ^= 1;
       }
     }
-    if (ok && kb >= 2) ok = !ctl[0] && mbar_wait(smem_addr(rfree + b), (uint32_t)(((kb >> 1) - 1) & 1));
+    if (ok && kb >= 2) ok = !ctl[0] && mbar_wait(smem_addr(rfree + b), (uint32_t)(((kb >> 1) - 1) & 1), polls);
     if (!ok) {
       if (lane == 0) fail();
       break;
@@ -1314,6 +1316,7 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
     case 2: {
       const int n = 3 * N;
       const int rg_s = nrhs >= 4 ? 4 : 1;
+      const int polls = sh.wait_polls > 0 ? sh.wait_polls : (sh.wait_polls < 0 ? 0 : kGemvPolls);
       const C* pk = std::is_same<T, float>::value ? (const C*)pr.pk32.p : (const C*)pr.pk64.p;
       if (sh.gemv_mode == 2 && pk && pr.gemv_status.p && n <= 256) {
         // packed symmetric blocks through the streamed kernel; gemv_chunk is the ring depth here
@@ -1330,7 +1333,7 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
           const dim3 grid((unsigned)std::min<int64_t>(nblk, (int64_t)nsm * std::max(1, std::min(g.ctas, fit))),
                           ceil_div(nrhs, rg_s));
           k<<<grid, nthr, g.smem, st>>>(t, pk, L, M, N, (int64_t)L * M * N * 3, nrhs, skip, skip_stride, g.cq,
-                                        g.nstage, g.stage_elems, g.G, g.nc, g.nv, pr.gemv_status.as<int>());
+                                        g.nstage, g.stage_elems, g.G, g.nc, g.nv, pr.gemv_status.as<int>(), polls);
           VS_LAUNCH_CHECK();
           break;
         }
@@ -1355,7 +1358,7 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
                     ceil_div(nrhs, rg));                                                                      \
     k<<<grid, g.nc + 32 + 32 * g.nv, g.smem, st>>>(t, inv, L, M, N, (int64_t)L * M * N * 3, nrhs, skip,        \
                                                    skip_stride, g.cq, g.nstage, g.stage_elems, g.G, g.nc,     \
-                                                   g.nv, status);                                             \
+                                                   g.nv, status, polls);                                      \
   }
         if constexpr (std::is_same<T, float>::value) {
           if (pair) {
