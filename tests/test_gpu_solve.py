@@ -318,3 +318,78 @@ def test_particles_solved_concurrently_match_batch_solves(api):
         api.solve_particles_device([parts[0][0], parts[1][0]], [parts[0][1], parts[0][1]],
                                    [parts[0][2].data_ptr(), parts[1][2].data_ptr()], [Xs[0].data_ptr(), Xs[1].data_ptr()],
                                    [4, 4], tol=1e-10, precision="fp64")
+
+
+@pytest.mark.parametrize("precision,tol", [("mixed", 1e-6), ("fp64", 1e-10)])
+def test_particles_lockstep_per_direction_alpha(api, precision, tol):
+    """vs_solve_particles: three plates of different sizes on one context,
+    4 incident directions / polarisations each with its own alpha_LDR, solved
+    in lockstep (one graph launch per inner iteration of all plates).  Every
+    right-hand side meets tol against the oracle operator with its own alpha;
+    in FP64 every particle reproduces its own vs_solve_batch_device solve
+    (same iteration counts, same solutions)."""
+    import torch
+    parts = []
+    for k, diam in enumerate((2.5, 2.0, 3.0)):
+        p = W.small_hex(m=1.31 + 0.05j, diameter=diam, nper=4)
+        L, M, N, idx3, Toep, alpha, dV, b0, Aor = _system(p)
+        fN = O.fft_operator(O.circulant_nop_const(Toep))
+        chi = np.zeros(L * M * N); chi[p["idx"]] = 1
+        chi = chi.reshape((L, M, N), order="F")
+        op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+        pr = api.Preconditioner(op, shift=1 / alpha, d=dV) if k != 1 else None  # one without
+        pairs = _directions(p, 2, 20 + k)
+        B = np.array([O.PlaneWavePointWise(pol, kv, p["r"]).ravel(order="F")[idx3] for kv, pol in pairs])
+        alphas = np.array([O.alpha_ldr(p["refInd"], p["ko"], p["d"], kv, pol) for kv, pol in pairs])
+        parts.append(dict(op=op, pr=pr, B=B, Bd=torch.from_numpy(B).cuda(), alphas=alphas, fN=fN, chi=chi, dV=dV,
+                          LMN=(L, M, N), idx3=idx3))
+    Xs = [torch.zeros_like(q["Bd"]) for q in parts]
+    torch.cuda.synchronize()
+    out = api.solve_particles([q["op"] for q in parts], [q["pr"] for q in parts], [q["Bd"].data_ptr() for q in parts],
+                              [X.data_ptr() for X in Xs], [len(q["B"]) for q in parts],
+                              grams=[1 / q["alphas"] for q in parts], tol=tol, precision=precision)
+    assert len(out) == 3
+    for q, X, inf in zip(parts, Xs, out):
+        Xh = X.cpu().numpy()
+        L, M, N = q["LMN"]
+        for r in range(len(q["B"])):
+            assert inf[r]["flag"] == 0, inf[r]
+            Ar = O.MVP(Xh[r], q["fN"], np.ones((L, M, N)), q["dV"] * q["chi"], 1 / q["alphas"][r], "notransp", q["idx3"])
+            assert np.linalg.norm(q["B"][r] - Ar) / np.linalg.norm(q["B"][r]) <= tol * 1.01
+        if precision == "fp64":
+            Xr = torch.zeros_like(q["Bd"])
+            torch.cuda.synchronize()
+            ir = api.solve_batch_device(q["op"], q["Bd"].data_ptr(), Xr.data_ptr(), len(q["B"]), q["pr"], tol=tol,
+                                        precision="fp64", gram=1 / q["alphas"])
+            for r in range(len(q["B"])):
+                assert ir[r]["iter"] == inf[r]["iter"]
+            assert np.linalg.norm(Xh - Xr.cpu().numpy()) <= 1e-12 * np.linalg.norm(Xh)
+    # a second call reuses the captured graph and gives the same result
+    Xs2 = [torch.zeros_like(q["Bd"]) for q in parts]
+    torch.cuda.synchronize()
+    out2 = api.solve_particles([q["op"] for q in parts], [q["pr"] for q in parts],
+                               [q["Bd"].data_ptr() for q in parts], [X.data_ptr() for X in Xs2],
+                               [len(q["B"]) for q in parts], grams=[1 / q["alphas"] for q in parts], tol=tol,
+                               precision=precision)
+    for X, X2, i1, i2 in zip(Xs, Xs2, out, out2):
+        assert [a["iter"] for a in i1] == [a["iter"] for a in i2]
+        assert torch.equal(X, X2)
+
+
+def test_particles_rejects_shared_objects(api):
+    import torch
+    from voxscatter_gb300._lib import VoxScatterError
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.0, nper=3)
+    L, M, N, idx3, Toep, alpha, dV, b0, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    op2 = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
+    Bd = torch.from_numpy(np.array([b0])).cuda()
+    X = torch.zeros_like(Bd)
+    with pytest.raises(VoxScatterError, match="appears twice"):
+        api.solve_particles([op, op], None, [Bd.data_ptr()] * 2, [X.data_ptr()] * 2, [1, 1])
+    with pytest.raises(VoxScatterError, match="appears twice"):
+        api.solve_particles([op, op2], [pr, pr], [Bd.data_ptr()] * 2, [X.data_ptr()] * 2, [1, 1])
+    other = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep, ctx=api.Context(0))
+    with pytest.raises(VoxScatterError, match="one context"):
+        api.solve_particles([op, other], None, [Bd.data_ptr()] * 2, [X.data_ptr()] * 2, [1, 1])
