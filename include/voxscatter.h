@@ -397,6 +397,32 @@ int vs_cext_grad(vs_op* op, vs_prec* prec, const double* Einc, const double* eps
                  const double kvec[3], const double E0[3], const vs_solve_opts* opts, double* cext, double* grad_re,
                  double* grad_im, double* P_out, vs_solve_info* info_fwd, vs_solve_info* info_adj);
 
+/* Orientation-averaged extinction cross section (random-orientation averaging,
+ * listed as a to-do at README.md:37).  The particle stays fixed on op's grid
+ * and the incident plane wave takes ndir orientations: a unit direction k
+ * (dirs, ndir x 3) and an angle psi (NULL: 0) turning the polarisation pair
+ * b1 = k x z / |k x z| (k x x when k is along z), b2 = k x b1 about k, giving
+ * e1 = cos(psi) b1 + sin(psi) b2 and e2 = k x e1 -- the three Euler angles of
+ * a particle orientation (rotating the particle is rotating the incident wave
+ * the other way).  Every (orientation, polarisation) is solved with its own
+ * LDR polarisability (Gram = 1/alpha_LDR(m, k, e), getOPERATOR_DDA.m:7-26)
+ * on op's Toeplitz operator, 8 orientations per batched solve; C_ext (vs_cext,
+ * |E0| = 1) is averaged over the two polarisations (unpolarised incidence)
+ * and then over the orientations with the weights (NULL: equal weights;
+ * normalised by their sum).  The LDR polarisability depends on the
+ * polarisation, so the two-polarisation average depends on psi: a random
+ * orientation average samples psi as well as k.
+ *   op: the DDA operator (Mr = 1, Mc = dV; idx3 in the [idx; V+idx; 2V+idx]
+ *   form); m: refractive index, 1 value or n3/3 in idx order; x, y, z: grid
+ *   axes (as vs_plane_wave); ko, d: wavenumber and dipole spacing; opts: the
+ *   solver (opts->gram NULL, no transpose).  Outputs: cext_avg; cext_each
+ *   (optional, ndir x 2: per orientation and polarisation); infos (optional,
+ *   ndir x 2). */
+int vs_orientation_average(vs_op* op, vs_prec* prec, const double* m, int64_t nm, const double* x, const double* y,
+                           const double* z, double ko, double d, const double* dirs, const double* psi,
+                           const double* weights, int64_t ndir, const vs_solve_opts* opts, double* cext_avg,
+                           double* cext_each, vs_solve_info* infos);
+
 /* ---- diagnostics ----------------------------------------------------- */
 
 /* Launch shape of an operator's pipeline in one precision, as chosen by the

@@ -27,6 +27,7 @@ from .mvp import MVP, mv_AN_const, dense_dda_matrix, dense_from_toeplitz
 from .precond import (circ_1_level, circ_2_level, eps_layer_average, invert_blocks,
                       mvp_circ_2_level, chan_mvp_idx, circ_1_level_blocks)
 from .krylov import bicgstab, gmres, pgmres, pgmres_dr, harm_vecs1, harm_vecs2
-from .physics import (PlaneWavePointWise, cext_dda, cext_grad_dda, far_field, field_dda, mie_qext)
+from .physics import (PlaneWavePointWise, cext_dda, cext_grad_dda, far_field, field_dda, mie_qext,
+                      polarisation_basis, orientation_average_cext)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

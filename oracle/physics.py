@@ -99,3 +99,38 @@ def far_field(P, idx3, r, ko, dV, dirs):
         s = Pv @ ph
         out.append(ko ** 2 * dV * (s - n * (n @ s)))
     return np.array(out)
+
+
+def polarisation_basis(k):
+    """Two orthonormal linear polarisations of a unit direction k:
+    e1 = k x z / |k x z| (k x x when k is along z), e2 = k x e1."""
+    k = np.asarray(k, dtype=float)
+    a = np.cross(k, [0.0, 0.0, 1.0])
+    if np.linalg.norm(a) < 1e-6:
+        a = np.cross(k, [1.0, 0.0, 0.0])
+    e1 = a / np.linalg.norm(a)
+    return e1, np.cross(k, e1)
+
+
+def orientation_average_cext(solve, Einc_of, ko, dV, dirs, weights=None, psi=None):
+    """Random-orientation averaging (absent from the reference, README.md:37):
+    the particle stays fixed and the incident wave runs over the orientations
+    (unit direction dirs[j], polarisation pair of polarisation_basis turned by
+    psi[j] about it) with weights; solve(kvec, e) returns the polarisation P
+    of that incidence (the system with that incidence's alpha_LDR) and
+    Einc_of(kvec, e) its incident field at the unknowns.  C_ext (|E0| = 1) is
+    averaged over the two polarisations and then over the orientations.
+    Returns (average, (ndir, 2))."""
+    dirs = np.asarray(dirs, dtype=float).reshape(-1, 3)
+    w = np.ones(len(dirs)) if weights is None else np.asarray(weights, dtype=float)
+    psi = np.zeros(len(dirs)) if psi is None else np.asarray(psi, dtype=float)
+    each = np.zeros((len(dirs), 2))
+    for j, d in enumerate(dirs):
+        k = d / np.linalg.norm(d)
+        b1, b2 = polarisation_basis(k)
+        c, s_ = np.cos(psi[j]), np.sin(psi[j])
+        for pol, e in enumerate((c * b1 + s_ * b2, -s_ * b1 + c * b2)):
+            kvec = ko * k
+            P = solve(kvec, e)
+            each[j, pol] = cext_dda(P, Einc_of(kvec, e), ko, dV, e)
+    return float(np.sum(w * each.mean(axis=1)) / np.sum(w)), each

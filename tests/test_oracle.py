@@ -334,3 +334,42 @@ def test_inverse_blocks_times_component_flips_are_symmetric():
     inv_f = O.invert_blocks(blk, 0.8, face)
     worst_f = max(np.linalg.norm(S - S.T) / np.linalg.norm(S) for S in (inv_f[i, j] * D for i in range(L) for j in range(M)))
     assert worst_f > 1e-3
+
+
+def test_unpolarised_cext_and_the_polarisation_basis():
+    """The two-polarisation average of C_ext used by the orientation averaging:
+    with a polarisation-independent polarisability it is the trace of a
+    quadratic form, the same for any orthonormal pair perpendicular to k; with
+    the LDR polarisability (its S term depends on the polarisation,
+    getOPERATOR_DDA.m:14-26) it is not, which is why an orientation average
+    samples the angle of the pair about k as well (dense solves)."""
+    p = W.small_hex(m=1.31 + 0.05j, diameter=1.5, nper=4)
+    L, M, N = p["L"], p["M"], p["N"]
+    idx = p["idx"]
+    nD = L * M * N
+    idx3 = np.concatenate([idx, nD + idx, 2 * nD + idx])
+    ko, d = p["ko"], p["d"]
+    k = np.array([0.3, -0.5, 0.81]); k /= np.linalg.norm(k)
+    e1, e2 = O.polarisation_basis(k)
+    assert abs(e1 @ k) < 1e-12 and abs(e2 @ k) < 1e-12 and abs(e1 @ e2) < 1e-12
+
+    def cext(e, ldr):
+        # without LDR dependence: alpha of a fixed S (that of e1)
+        ainv = 1 / O.alpha_ldr(p["refInd"], ko, d, ko * k, e if ldr else e1)
+        A = O.dense_dda_matrix(p["r"], idx, ko, ainv, d ** 3)
+        b = O.PlaneWavePointWise(e, ko * k, p["r"]).ravel(order="F")[idx3]
+        return O.cext_dda(np.linalg.solve(A, b), b, ko, d ** 3, e)
+
+    t = 0.7
+    f1, f2 = np.cos(t) * e1 + np.sin(t) * e2, -np.sin(t) * e1 + np.cos(t) * e2
+    base = 0.5 * (cext(e1, False) + cext(e2, False))
+    assert abs(0.5 * (cext(f1, False) + cext(f2, False)) - base) < 1e-9 * abs(base)
+    base_ldr = 0.5 * (cext(e1, True) + cext(e2, True))
+    assert abs(0.5 * (cext(f1, True) + cext(f2, True)) - base_ldr) > 1e-5 * abs(base_ldr)
+    # the oracle's orientation average honours psi
+    solve = lambda kv, e: np.linalg.solve(
+        O.dense_dda_matrix(p["r"], idx, ko, 1 / O.alpha_ldr(p["refInd"], ko, d, kv, e), d ** 3),
+        O.PlaneWavePointWise(e, kv, p["r"]).ravel(order="F")[idx3])
+    einc = lambda kv, e: O.PlaneWavePointWise(e, kv, p["r"]).ravel(order="F")[idx3]
+    avg, each = O.orientation_average_cext(solve, einc, ko, d ** 3, [k], psi=[t])
+    assert abs(avg - 0.5 * (cext(f1, True) + cext(f2, True))) < 1e-12 * abs(avg)

@@ -96,6 +96,9 @@ SIGNATURES.update({
     "vs_solve_particles": (C.c_int, [_i64, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp),
                                      C.POINTER(_i64), C.POINTER(_pd), C.POINTER(_i64), C.POINTER(vs_solve_opts),
                                      C.POINTER(vs_solve_info)]),
+    "vs_orientation_average": (C.c_int, [_vp, _vp, _pd, _i64, _pd, _pd, _pd, C.c_double, C.c_double, _pd, _pd,
+                                         _pd, _i64, C.POINTER(vs_solve_opts), C.POINTER(C.c_double), _pd,
+                                         C.POINTER(vs_solve_info)]),
     "vs_plane_wave": (C.c_int, [_vp, _pd, _pd, _pd, _pd, _pd, _pd]),
     "vs_cext": (C.c_int, [_vp, _pd, _pd, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double)]),
     "vs_op_apply_domain": (C.c_int, [_vp, _pd, _pd, C.c_int64, _pd, _pd, C.c_int]),

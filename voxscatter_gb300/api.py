@@ -617,6 +617,36 @@ def far_field(op, P, r, ko, dV, dirs):
     return F[0] if Pa.ndim == 1 else F
 
 
+def orientation_average(op, prec, m, r, ko, d, dirs, weights=None, psi=None, tol=1e-6, maxit=2000,
+                        precision="mixed", method="bicgstab", restart=50):
+    """Orientation-averaged C_ext over the orientations (unit incident
+    direction dirs[j], polarisation pair turned by psi[j] about it; weights or
+    equal weights), two orthogonal linear polarisations each, every incidence
+    with its own alpha_LDR; m: refractive index (scalar or one per voxel in idx
+    order).  Returns (cext_avg, cext_each (ndir, 2), infos)."""
+    lib = op.ctx._lib
+    mv = np.ascontiguousarray(np.atleast_1d(np.asarray(m, dtype=np.complex128)).ravel())
+    r = np.asarray(r, dtype=float)
+    x = np.ascontiguousarray(r[:, 0, 0, 0]); y = np.ascontiguousarray(r[0, :, 0, 1])
+    z = np.ascontiguousarray(r[0, 0, :, 2])
+    D = np.ascontiguousarray(np.asarray(dirs, dtype=float).reshape(-1, 3))
+    nd = D.shape[0]
+    wv = None if weights is None else np.ascontiguousarray(np.asarray(weights, dtype=float).ravel())
+    pv = None if psi is None else np.ascontiguousarray(np.asarray(psi, dtype=float).ravel())
+    o = _solve_opts(lib, tol, maxit, precision)
+    o.method = _method(method)
+    o.restart = int(restart)
+    avg = C.c_double()
+    each = np.zeros((nd, 2))
+    infos = (L.vs_solve_info * (2 * nd))()
+    L.check(lib.vs_orientation_average(op.h, prec.h if prec is not None else None, L.dptr(mv), mv.size, L.dptr(x),
+                                       L.dptr(y), L.dptr(z), float(ko), float(d), L.dptr(D),
+                                       L.dptr(pv) if pv is not None else None,
+                                       L.dptr(wv) if wv is not None else None, nd, C.byref(o), C.byref(avg),
+                                       L.dptr(each), infos), op.ctx.h)
+    return avg.value, each, [dict(flag=i.flag, relres=i.relres, iter=i.iter) for i in infos]
+
+
 def cext_grad(op, prec, Einc, eps, ko, d, kvec, Eo, tol=1e-6, maxit=2000, precision="mixed"):
     """(C_ext, dC/dRe(eps), dC/dIm(eps), P, info_fwd, info_adj) by the adjoint method."""
     lib = op.ctx._lib

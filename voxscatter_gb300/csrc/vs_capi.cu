@@ -323,6 +323,42 @@ void solve_batch_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, in
   for (int64_t r = 0; r < nrhs; ++r) fill_info(res[r], infos + r);
 }
 
+// S = sum_j (k_hat_j e_hat_j)^2 of the LDR polarisability (getOPERATOR_DDA.m:14-20).
+double ldr_S(const double kvec[3], const double E0[3]) {
+  const double nk = std::sqrt(kvec[0] * kvec[0] + kvec[1] * kvec[1] + kvec[2] * kvec[2]);
+  const double ne = std::sqrt(E0[0] * E0[0] + E0[1] * E0[1] + E0[2] * E0[2]);
+  VS_REQUIRE(nk > 0 && ne > 0, "kvec and E0 must be non-zero");
+  double S = 0;
+  for (int j = 0; j < 3; ++j) {
+    const double t = (kvec[j] / nk) * (E0[j] / ne);
+    S += t * t;
+  }
+  return S;
+}
+
+// Two orthonormal polarisations of a unit incident direction k:
+// e1 = k x z / |k x z| (k x x when k is along z), e2 = k x e1.
+void polarisation_basis(const double k[3], double e1[3], double e2[3]) {
+  double a[3] = {k[1], -k[0], 0.0};  // k x z
+  double na = std::sqrt(a[0] * a[0] + a[1] * a[1]);
+  if (na < 1e-6) {
+    a[0] = 0.0; a[1] = k[2]; a[2] = -k[1];  // k x x
+    na = std::sqrt(a[1] * a[1] + a[2] * a[2]);
+  }
+  for (int j = 0; j < 3; ++j) e1[j] = a[j] / na;
+  e2[0] = k[1] * e1[2] - k[2] * e1[1];
+  e2[1] = k[2] * e1[0] - k[0] * e1[2];
+  e2[2] = k[0] * e1[1] - k[1] * e1[0];
+}
+
+// alpha_LDR of one element (getOPERATOR_DDA.m:7-26), dimensionless.
+cd alpha_ldr_one(cd m, bool is_eps, double kd, double S) {
+  const double b1 = -1.8915316, b2 = 0.1648469, b3 = -1.7700004;
+  const cd msqr = is_eps ? m : m * m;
+  const cd aCM = 3.0 / (4.0 * M_PI) * (msqr - 1.0) / (msqr + 2.0);
+  return aCM / (1.0 + aCM * ((b1 + msqr * b2 + msqr * b3 * S) * kd * kd - cd(0, 2.0 / 3.0) * kd * kd * kd));
+}
+
 }  // namespace
 
 void record_error(vs_ctx* ctx, const char* msg) {
@@ -403,26 +439,13 @@ int vs_ctx_stream(vs_ctx* ctx, void** stream) {
 }
 
 int vs_alpha_ldr(const double* m, int64_t n, int is_eps, double ko, double d, const double kvec[3],
-                 const double E0[3], double* alpha_out) {
+                            const double E0[3], double* alpha_out) {
   return guarded(nullptr, [&] {
     VS_REQUIRE(m && alpha_out && kvec && E0 && n >= 0, "NULL argument");
-    const double b1 = -1.8915316, b2 = 0.1648469, b3 = -1.7700004;
-    const double nk = std::sqrt(kvec[0] * kvec[0] + kvec[1] * kvec[1] + kvec[2] * kvec[2]);
-    const double ne = std::sqrt(E0[0] * E0[0] + E0[1] * E0[1] + E0[2] * E0[2]);
-    VS_REQUIRE(nk > 0 && ne > 0, "kvec and E0 must be non-zero");
-    double S = 0;
-    for (int j = 0; j < 3; ++j) {
-      const double t = (kvec[j] / nk) * (E0[j] / ne);
-      S += t * t;
-    }
+    const double S = ldr_S(kvec, E0);
     const cd* mm = reinterpret_cast<const cd*>(m);
     cd* out = reinterpret_cast<cd*>(alpha_out);
-    const double kd = ko * d;
-    for (int64_t e = 0; e < n; ++e) {
-      const cd msqr = is_eps ? mm[e] : mm[e] * mm[e];
-      const cd aCM = 3.0 / (4.0 * M_PI) * (msqr - 1.0) / (msqr + 2.0);
-      out[e] = aCM / (1.0 + aCM * ((b1 + msqr * b2 + msqr * b3 * S) * kd * kd - cd(0, 2.0 / 3.0) * kd * kd * kd));
-    }
+    for (int64_t e = 0; e < n; ++e) out[e] = alpha_ldr_one(mm[e], is_eps != 0, ko * d, S);
   });
 }
 
@@ -1450,6 +1473,116 @@ int vs_solve_batch(vs_op* op, vs_prec* prec, const double* b, double* x, int64_t
     VS_CUDA(cudaStreamSynchronize(st));
     const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     for (int64_t r = 0; r < nrhs; ++r) infos[r].time_ms = ms;
+  });
+}
+
+int vs_orientation_average(vs_op* op, vs_prec* prec, const double* m, int64_t nm, const double* x, const double* y,
+                           const double* z, double ko, double d, const double* dirs, const double* psi,
+                           const double* weights, int64_t ndir, const vs_solve_opts* opts, double* cext_avg,
+                           double* cext_each, vs_solve_info* infos) {
+  if (!op) return VS_ERR_ARG;
+  return guarded(op->ctx, [&] {
+    VS_REQUIRE(m && x && y && z && dirs && opts && cext_avg, "NULL argument");
+    VS_REQUIRE(ndir >= 1 && ndir <= (int64_t(1) << 20), "ndir must be in [1, 2^20]");
+    VS_REQUIRE(op->std3, "orientation averaging needs idx3 in the [idx; V+idx; 2V+idx] form");
+    VS_REQUIRE(opts->gram == nullptr, "the Gram of every direction is formed here: opts->gram must be NULL");
+    VS_REQUIRE(opts->transpose == 0, "orientation averaging solves A x = b (opts->transpose must be 0)");
+    VS_REQUIRE(ko > 0 && d > 0, "ko and d must be positive");
+    const int64_t n = op->n3, nvox = n / 3, V = op->V;
+    VS_REQUIRE(nm == 1 || nm == nvox, "m must have 1 or n3/3 entries");
+    cudaStream_t st = op->ctx->stream;
+    const cd* mm = reinterpret_cast<const cd*>(m);
+    // grid voxel of each idx entry (the x-component unknowns), for a per-voxel m
+    std::vector<int> vox;
+    if (nm > 1) {
+      vox.resize(nvox);
+      VS_CUDA(cudaMemcpyAsync(vox.data(), op->pos2grid.p, nvox * sizeof(int), cudaMemcpyDeviceToHost, st));
+      VS_CUDA(cudaStreamSynchronize(st));
+    }
+    std::vector<double> w(ndir, 1.0);
+    double wsum = 0;
+    for (int64_t j = 0; j < ndir; ++j) {
+      if (weights) w[j] = weights[j];
+      VS_REQUIRE(std::isfinite(w[j]) && w[j] >= 0, "weights must be finite and non-negative");
+      wsum += w[j];
+    }
+    VS_REQUIRE(wsum > 0, "the weights sum to zero");
+    vs::DevBuf dx, dy, dz;
+    dx.alloc(op->L * sizeof(double)); dy.alloc(op->M * sizeof(double)); dz.alloc(op->N * sizeof(double));
+    VS_CUDA(cudaMemcpyAsync(dx.p, x, op->L * sizeof(double), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemcpyAsync(dy.p, y, op->M * sizeof(double), cudaMemcpyHostToDevice, st));
+    VS_CUDA(cudaMemcpyAsync(dz.p, z, op->N * sizeof(double), cudaMemcpyHostToDevice, st));
+    // directions in batches of 8 (16 right-hand sides: every pipeline launch serves all of them)
+    constexpr int64_t kDirChunk = 8;
+    const int64_t cap = std::min<int64_t>(ndir, kDirChunk) * 2;
+    vs::DevBuf B, X;
+    B.alloc(cap * n * sizeof(double2));
+    X.alloc(cap * n * sizeof(double2));
+    std::vector<cd> gram(nm > 1 ? cap * V : cap);
+    vs::SolveParams prm = solve_params(op, prec, opts);
+    const double kd = ko * d, scale = 4.0 * M_PI * ko * d * d * d;  // |E0| = 1
+    double acc = 0;
+    for (int64_t c0 = 0; c0 < ndir; c0 += kDirChunk) {
+      const int64_t nd = std::min(kDirChunk, ndir - c0), nr = 2 * nd;
+      for (int64_t j = 0; j < nd; ++j) {
+        const double* dj = dirs + 3 * (c0 + j);
+        const double nk = std::sqrt(dj[0] * dj[0] + dj[1] * dj[1] + dj[2] * dj[2]);
+        VS_REQUIRE(nk > 0 && std::isfinite(nk), "a direction is zero or not finite");
+        const double k[3] = {dj[0] / nk, dj[1] / nk, dj[2] / nk};
+        double b1[3], b2[3], e[2][3];
+        polarisation_basis(k, b1, b2);
+        const double ps = psi ? psi[c0 + j] : 0.0;
+        VS_REQUIRE(std::isfinite(ps), "psi must be finite");
+        const double cp = std::cos(ps), sp = std::sin(ps);
+        for (int q = 0; q < 3; ++q) {
+          e[0][q] = cp * b1[q] + sp * b2[q];
+          e[1][q] = -sp * b1[q] + cp * b2[q];
+        }
+        const double kvec[3] = {ko * k[0], ko * k[1], ko * k[2]};
+        for (int pol = 0; pol < 2; ++pol) {
+          const int64_t r = 2 * j + pol;
+          const double2 E0[3] = {make_double2(e[pol][0], 0), make_double2(e[pol][1], 0), make_double2(e[pol][2], 0)};
+          vs::plane_wave_device(*op, dx.as<double>(), dy.as<double>(), dz.as<double>(), kvec, E0,
+                                B.as<double2>() + r * n, st);
+          const double S = ldr_S(kvec, e[pol]);
+          if (nm == 1) {
+            gram[r] = 1.0 / alpha_ldr_one(mm[0], false, kd, S);
+          } else {
+            cd* g = gram.data() + r * V;
+            std::fill(g, g + V, cd(1.0, 0.0));  // entries off the particle are never read
+            for (int64_t v = 0; v < nvox; ++v) g[vox[v]] = 1.0 / alpha_ldr_one(mm[v], false, kd, S);
+          }
+        }
+      }
+      vs::SolveParams pc = prm;
+      pc.gram_host = reinterpret_cast<const double2*>(gram.data());
+      pc.gram_n = nm == 1 ? 1 : V;
+      VS_CUDA(cudaMemsetAsync(X.p, 0, nr * n * sizeof(double2), st));
+      std::vector<vs::SolveResult> res(nr);
+      if (opts->method == VS_BICGSTAB) {
+        vs::solve_bicgstab_batch(*op, prec, B.as<double2>(), X.as<double2>(), (int)nr, pc, res, st);
+      } else {
+        for (int64_t r = 0; r < nr; ++r) {
+          vs::SolveParams p1 = pc;
+          p1.gram_host = pc.gram_host + r * pc.gram_n;
+          p1.resvec_host = nullptr;
+          p1.resvec_cap = 0;
+          if (opts->method == VS_GMRES)
+            vs::solve_gmres(*op, prec, B.as<double2>() + r * n, X.as<double2>() + r * n, p1, res[r], st);
+          else
+            vs::solve_gmres_dr(*op, prec, B.as<double2>() + r * n, X.as<double2>() + r * n, p1, res[r], st);
+        }
+      }
+      check_prec_status(prec);
+      for (int64_t r = 0; r < nr; ++r) {
+        const double c = vs::cext_device(X.as<double2>() + r * n, B.as<double2>() + r * n, n, scale, st);
+        const int64_t j = c0 + r / 2;
+        if (cext_each) cext_each[2 * j + (r & 1)] = c;
+        if (infos) fill_info(res[r], infos + 2 * j + (r & 1));
+        acc += w[j] * 0.5 * c;
+      }
+    }
+    *cext_avg = acc / wsum;
   });
 }
 
