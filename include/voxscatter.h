@@ -171,12 +171,13 @@ int vs_op_apply_device_noalloc(vs_op* op, const void* x, void* y, int64_t nrhs, 
 typedef struct vs_prec vs_prec;
 
 /* Bit mask of the precisions a preconditioner is built for, and how the
- * FP32 (VS_BUILD_C64) blocks are inverted: by default (or VS_BUILD_LU_CUDA)
- * on the CUDA cores -- one CTA per block in shared memory up to 3N = 168,
- * beyond that a persistent blocked Gauss-Jordan whose blocks stay
- * L2-resident; VS_BUILD_LU_TC runs the batched blocked Gauss-Jordan whose
- * rank-32 trailing updates are tcgen05 3xTF32 MMAs (any 3N <= 256).  FP64
- * blocks are always inverted on the CUDA cores. */
+ * FP32 (VS_BUILD_C64) blocks are inverted.  By default: one CTA per block in
+ * shared memory up to 3N = 168; for 168 < 3N <= 256 a persistent blocked
+ * Gauss-Jordan whose rank-32 trailing updates are tcgen05 3xTF32 MMAs (each
+ * block L2-resident in one CTA); beyond that the same on the CUDA cores.
+ * VS_BUILD_LU_TC forces the tensor-core kernel for any 3N <= 256,
+ * VS_BUILD_LU_CUDA the CUDA-core kernels.  FP64 blocks are always inverted
+ * on the CUDA cores. */
 enum vs_prec_mask { VS_BUILD_C64 = 1, VS_BUILD_C128 = 2, VS_BUILD_LU_TC = 4, VS_BUILD_LU_CUDA = 8 };
 
 /* circ_1_level (on_off = 'off') followed by circ_2_level on the device, FP64:
@@ -215,9 +216,10 @@ int vs_prec_create_blocks(vs_ctx* ctx, int64_t L, int64_t M, int64_t N, const do
 /* Batched inversion of nmat complex n x n matrices in device memory, in place,
  * FP32 (float2), column-major or row-major alike: the parfor of inv() over the
  * preconditioner blocks at main_DDA.m:107-111 (main_koch.m:114-118), e.g. for
- * inverse blocks handed to vs_prec_create_blocks.  method: 0 or
- * VS_BUILD_LU_CUDA (persistent blocked Gauss-Jordan on the CUDA cores),
- * VS_BUILD_LU_TC (tensor-core trailing updates, n <= 256).  Enqueued on the
+ * inverse blocks handed to vs_prec_create_blocks.  method: 0 (tensor-core
+ * trailing updates for n <= 256, else the CUDA cores), VS_BUILD_LU_TC
+ * (tensor cores, n <= 256), VS_BUILD_LU_CUDA (persistent blocked
+ * Gauss-Jordan on the CUDA cores).  Enqueued on the
  * context's stream; returns after it completes, VS_ERR_ARG if a matrix is
  * singular or its inverse is not finite. */
 int vs_invert_blocks_device(vs_ctx* ctx, void* mats, int64_t n, int64_t nmat, int method);

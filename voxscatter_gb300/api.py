@@ -310,8 +310,9 @@ class Preconditioner:
 
     def __init__(self, op=None, shift=None, d=None, inv_blocks=None, LMN=None, idx3=None,
                  precisions=("c64", "c128"), ctx=None, lu="auto"):
-        """lu: how the FP32 blocks are inverted -- "auto" (= "cuda", the CUDA-core
-        kernels) or "tc" (tcgen05 trailing updates, 3N <= 256)."""
+        """lu: how the FP32 blocks are inverted -- "auto" (shared-memory kernel up
+        to 3N = 168, tensor cores up to 256, then CUDA cores), "tc" (tcgen05
+        trailing updates, 3N <= 256) or "cuda" (CUDA-core kernels)."""
         h = C.c_void_p()
         mask = _precisions(precisions) | {"auto": 0, "tc": L.VS_BUILD_LU_TC, "cuda": L.VS_BUILD_LU_CUDA}[lu]
         if op is not None:
@@ -384,8 +385,8 @@ class Preconditioner:
 
 def invert_blocks_device(mats_ptr, n, nmat, method="auto", ctx=None):
     """In-place FP32 inversion of nmat complex n x n matrices at the device
-    address mats_ptr (complex64, either storage order): "auto" / "cuda"
-    (CUDA-core blocked Gauss-Jordan) or "tc" (tensor cores, n <= 256)."""
+    address mats_ptr (complex64, either storage order): "auto" (tensor cores
+    for n <= 256, else CUDA cores), "tc" or "cuda"."""
     ctx = ctx or default_context()
     code = {"auto": 0, "tc": L.VS_BUILD_LU_TC, "cuda": L.VS_BUILD_LU_CUDA}[method]
     L.check(ctx._lib.vs_invert_blocks_device(ctx.h, C.c_void_p(mats_ptr), int(n), int(nmat), code), ctx.h)

@@ -869,7 +869,7 @@ int vs_invert_blocks_device(vs_ctx* ctx, void* mats, int64_t n, int64_t nmat, in
     vs::DevBuf status;
     status.alloc(sizeof(int));
     VS_CUDA(cudaMemsetAsync(status.p, 0, sizeof(int), st));
-    vs::invert_blocks_device((float2*)mats, (int)n, nmat, method == VS_BUILD_LU_TC ? vs::LU_TC : vs::LU_CUDA, 1.0,
+    vs::invert_blocks_device((float2*)mats, (int)n, nmat, method == VS_BUILD_LU_CUDA ? vs::LU_CUDA : vs::LU_TC, 1.0,
                              status.as<int>(), st);
     int hs = 0;
     VS_CUDA(cudaMemcpyAsync(&hs, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));

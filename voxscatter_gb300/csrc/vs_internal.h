@@ -234,11 +234,11 @@ void nop_assemble_device(int L, int M, int N, double ko, double dx, const double
 
 // Smallest instantiated two-level z length >= min_len (5-smooth beyond 256).
 int z_pass_length(int min_len);
-// lu: how FP32 blocks are inverted: LU_AUTO and LU_CUDA (CUDA-core kernels:
-// one CTA per block in shared memory, or the persistent blocked kernel whose
-// blocks stay L2-resident; the faster choice at the measured sizes), LU_TC
-// (tensor-core trailing updates whenever 3N <= 256).  FP64 blocks always use
-// the CUDA-core kernels.
+// lu: how FP32 blocks are inverted: LU_AUTO (one CTA per block in shared
+// memory up to 3N = 168, then the tensor-core kernel up to 256, then the
+// persistent CUDA-core blocked kernel: the fastest at each measured size),
+// LU_TC (tensor-core trailing updates whenever 3N <= 256), LU_CUDA (CUDA-core
+// kernels only).  FP64 blocks always use the CUDA-core kernels.
 enum { LU_AUTO = 0, LU_TC = 1, LU_CUDA = 2 };
 template <typename T>
 void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, const double2* dvec, double2 dscal,
@@ -251,7 +251,8 @@ void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, co
 bool tc_invert_supported(int n);
 void invert_blocks_tc(float2* mats, int n, int64_t nmat, double scale, int* status, cudaStream_t st);
 // In-place inversion of nmat n x n FP32 complex matrices on the device: the
-// tensor-core kernels (lu == LU_TC, n <= 256) or the blocked CUDA-core kernel.
+// tensor-core kernel (n <= 256 unless lu == LU_CUDA) or the blocked CUDA-core
+// kernel.
 void invert_blocks_device(float2* mats, int n, int64_t nmat, int lu, double scale, int* status, cudaStream_t st);
 template <typename T>
 void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,

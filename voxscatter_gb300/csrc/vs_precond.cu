@@ -429,7 +429,11 @@ void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, co
   const int n = 3 * N;
   const int64_t nmat = (int64_t)Lb * Mb;
   const bool fp32 = std::is_same<T, float>::value;
-  const bool use_tc = invert && fp32 && tc_invert_supported(n) && lu == LU_TC;
+  // tensor cores when forced, and by default where the alternative is the
+  // persistent CUDA-core kernel (blocks beyond the one-CTA shared-memory
+  // kernel): measured faster there, slower than the shared-memory kernel below
+  const bool use_tc = invert && fp32 && tc_invert_supported(n) &&
+                      (lu == LU_TC || (lu == LU_AUTO && smem > 227 * 1024));
   if (use_tc) {
     VS_REQUIRE(colmajor, "tensor-core inversion produces column-major blocks");
     // the transposes assembled row-major; the inverse of A^T row-major is A^-1 column-major
@@ -475,7 +479,7 @@ void assemble_invert(const double2* lev2, int L, int M, int N, double2 shift, co
 // transpose of the inverse), scaled by `scale`.
 void invert_blocks_device(float2* mats, int n, int64_t nmat, int lu, double scale, int* status, cudaStream_t st) {
   if (nmat <= 0) return;
-  if (lu == LU_TC && tc_invert_supported(n)) {
+  if (lu != LU_CUDA && tc_invert_supported(n)) {
     invert_blocks_tc(mats, n, nmat, scale, status, st);
     return;
   }
