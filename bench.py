@@ -536,6 +536,7 @@ def run_ours(args):
                             "frac_of_measured_hbm": b16 / (sum(mv16) * 1e-3) / 1e9 / peak}}
 
     batched = _batched(api, ctx, stream, p, op, prec, max(1, min(args.steps, 2))) if not args.no_batched else None
+    koch = _koch_summary(api, ctx, max(2, min(args.steps, 5)), maxit=100) if not args.no_koch else None
     variants = _krylov_variants(api, stream, op, prec, b_dev, x_dev, max(1, min(args.steps, 2)))
 
     line = {"metric": METRIC, "value": ms_mixed, "unit": "ms", "n_gpus": world, "steps": args.steps,
@@ -553,6 +554,7 @@ def run_ours(args):
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(b_pin.numel() * 16 * 2),
                     "d2h_bytes_per_step": int(x_pin.numel() * 16)},
             "gpu_launches": launches * args.steps, "clocks": clk.summary(), "batched": batched,
+            "koch_256x256x64": koch,
             "krylov_variants": variants}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # one full FP64 solve of the same plate by the NumPy/SciPy restatement on
@@ -740,14 +742,15 @@ def run_adjoint(args):
     return 0
 
 
-def run_koch(args):
+def _koch_summary(api, ctx, steps, maxit=200, with_lu=True):
     """256x256x64 Koch snowflake (level 3, 16 central layers, m = 1.78+0.005i):
-    setup times, per-launch pipeline times, the matvec's model bandwidth, and a
-    bounded mixed GMRES(50) solve (this system converges slowly; relres after
-    the iteration budget is reported).  One JSON line."""
+    setup times (Green tensor, operator, c64 preconditioner -- its 16,641
+    blocks of 192 inverted on the tensor cores by default), the block inversion
+    on the tensor cores against the CUDA cores, per-launch pipeline times, the
+    matvec's model bandwidth and a bounded mixed GMRES(50) solve (this system
+    converges slowly: relres after the iteration budget is reported)."""
     import torch
-    from voxscatter_gb300 import api, workloads as W
-    ctx = api.Context(0)
+    from voxscatter_gb300 import workloads as W
     p = W.config5()
     L, M, N = p["L"], p["M"], p["N"]
     nD = L * M * N
@@ -771,13 +774,12 @@ def run_koch(args):
     xs = torch.randn(n3, dtype=torch.complex64, device="cuda")
     ys = torch.empty_like(xs)
     torch.cuda.synchronize()
-    mv = op.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", args.steps)
-    pc = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", args.steps)
+    mv = op.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", steps)
+    pc = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", steps)
     mv_bytes, pc_bytes, pinned = _pass_bytes(p, op.PQR, n3)
     b = api.plane_wave(op, p["r"], p["kvec"], p["Eo"])
     bd = torch.from_numpy(np.ascontiguousarray(b)).cuda()
     xd = torch.zeros_like(bd)
-    maxit = 200
     api.solve_device(op, bd.data_ptr(), xd.data_ptr(), prec, tol=1e-6, maxit=50, precision="mixed",
                      method="gmres", restart=50)
     xd.zero_()
@@ -789,20 +791,74 @@ def run_koch(args):
     solve_ms = (time.perf_counter() - t) * 1e3
     peak, peak_kind = _peaks()
     mv_ms = sum(mv)
-    line = {"metric": "koch 256x256x64: pipeline launch times and bounded GMRES(50)", "unit": "ms",
-            "config": {"workload": f"Koch snowflake level 3, grid {L}x{M}x{N}, {len(idx)} dipoles, "
-                                   f"{n3} unknowns, m=1.78+0.005i", "fft_grid": "x".join(map(str, op.PQR))},
-            "setup_s": {"green": green_s, "operator": op_s, "preconditioner_c64": prec_s},
-            "shapes": {"op": op.shape("c64"), "prec": prec.shape("c64")},
-            "matvec_c64_ms": mv, "prec_c64_ms": pc,
-            "matvec_model_bytes": pinned, "matvec_model_GBps": pinned / (mv_ms * 1e-3) / 1e9,
-            "matvec_model_frac": pinned / (mv_ms * 1e-3) / 1e9 / peak, "peak_GBps": peak, "peak_source": peak_kind,
-            "gemv_GBps": pc_bytes[2] / (pc[2] * 1e-3) / 1e9,
-            "gmres50": {"maxit": maxit, "ms": solve_ms, "ms_per_iteration": solve_ms / max(1.0, info["iter"]),
-                        "flag": info["flag"], "relres": info["relres"], "iter": info["iter"]}}
+    out = {"workload": f"Koch snowflake level 3, grid {L}x{M}x{N}, {len(idx)} dipoles, {n3} unknowns, "
+                       f"m=1.78+0.005i", "fft_grid": "x".join(map(str, op.PQR)),
+           "setup_s": {"green": green_s, "operator": op_s, "preconditioner_c64": prec_s},
+           "shapes": {"op": op.shape("c64"), "prec": prec.shape("c64")},
+           "matvec_c64_ms": mv, "prec_c64_ms": pc,
+           "matvec_model_bytes": pinned, "matvec_model_GBps": pinned / (mv_ms * 1e-3) / 1e9,
+           "matvec_model_frac": pinned / (mv_ms * 1e-3) / 1e9 / peak, "peak_GBps": peak, "peak_source": peak_kind,
+           "gemv_GBps": pc_bytes[2] / (pc[2] * 1e-3) / 1e9,
+           "gmres50": {"maxit": maxit, "ms": solve_ms, "ms_per_iteration": solve_ms / max(1.0, info["iter"]),
+                       "flag": info["flag"], "relres": info["relres"], "iter": info["iter"]}}
+    del op, prec, xs, ys, bd, xd
+    if with_lu:
+        out["block_inversion"] = _lu_cases(api, ctx, steps, 2, cases=(("snowflake_192", 192, 16641),))
+    return out
+
+
+def _lu_cases(api, ctx, steps, warmup, cases=(("snowflake_192", 192, 16641), ("hexplate_78", 78, 2523)),
+              batch_cap=0):
+    """The batched block inversion on the tensor cores against the CUDA-core
+    blocked kernel, CUDA events on the context's stream, seeded
+    well-conditioned FP32 blocks of the configurations' sizes."""
+    import torch
+    ext = torch.cuda.ExternalStream(ctx.stream_ptr())
+    out = {}
+    for name, n, nmat in cases:
+        if batch_cap:
+            nmat = min(nmat, batch_cap)
+        g = torch.Generator(device="cuda").manual_seed(0)
+        A = (torch.randn(nmat, n, n, dtype=torch.complex64, device="cuda", generator=g) * (0.5 / n ** 0.5)
+             + torch.eye(n, dtype=torch.complex64, device="cuda") * (1.0 + 0.3j))
+        Wk = torch.empty_like(A)
+        res = {"n": n, "blocks": nmat, "flops_per_block": 8 * n ** 3}
+        for method in ("tc", "cuda"):
+            for _ in range(warmup):
+                Wk.copy_(A)
+                torch.cuda.synchronize()
+                api.invert_blocks_device(Wk.data_ptr(), n, nmat, method, ctx=ctx)
+            times = []
+            for _ in range(steps):
+                Wk.copy_(A)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(ext)
+                api.invert_blocks_device(Wk.data_ptr(), n, nmat, method, ctx=ctx)
+                e1.record(ext)
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1))
+            ms = float(np.median(times))
+            idx = np.linspace(0, nmat - 1, 8).astype(int)
+            Ah = A[idx].cpu().numpy().astype(np.complex128)
+            Wh = Wk[idx].cpu().numpy().astype(np.complex128)
+            err = max(np.linalg.norm(Wh[k] - np.linalg.inv(Ah[k])) / np.linalg.norm(np.linalg.inv(Ah[k]))
+                      for k in range(len(idx)))
+            res[method] = {"ms": ms, "TFLOPs": 8 * n ** 3 * nmat / (ms * 1e-3) / 1e12, "max_rel_err_vs_fp64": err}
+        res["speedup_tc_vs_cuda"] = res["cuda"]["ms"] / res["tc"]["ms"]
+        out[name] = res
+        del A, Wk
+    return out
+
+
+def run_koch(args):
+    """256x256x64 Koch snowflake: one JSON line (see _koch_summary)."""
+    from voxscatter_gb300 import api
+    ctx = api.Context(0)
+    line = {"metric": "koch 256x256x64: setup, pipeline launch times and bounded GMRES(50)", "unit": "ms"}
+    line.update(_koch_summary(api, ctx, args.steps))
     print(json.dumps(line), flush=True)
     return 0
-
 
 def run_lu(args):
     """Batched inversion of the preconditioner blocks (the parfor of inv() at
@@ -812,49 +868,12 @@ def run_lu(args):
     seeded well-conditioned matrices of those sizes in HBM (values do not
     change the work).  --lu-batch limits the batch (small cases for profiling).
     One JSON line."""
-    import torch
     from voxscatter_gb300 import api
     ctx = api.Context(0)
-    ext = torch.cuda.ExternalStream(ctx.stream_ptr())
-    out = {}
-    cases = (("snowflake_192", 192, 16641), ("hexplate_78", 78, 2523))
-    for name, n, nmat in cases:
-        if args.lu_batch:
-            nmat = min(nmat, args.lu_batch)
-        g = torch.Generator(device="cuda").manual_seed(0)
-        A = (torch.randn(nmat, n, n, dtype=torch.complex64, device="cuda", generator=g) * (0.5 / n ** 0.5)
-             + torch.eye(n, dtype=torch.complex64, device="cuda") * (1.0 + 0.3j))
-        W = torch.empty_like(A)
-        res = {"n": n, "blocks": nmat, "flops_per_block": 8 * n ** 3}
-        for method in ("tc", "cuda"):
-            for _ in range(args.warmup):
-                W.copy_(A)
-                torch.cuda.synchronize()
-                api.invert_blocks_device(W.data_ptr(), n, nmat, method, ctx=ctx)
-            times = []
-            for _ in range(args.steps):
-                W.copy_(A)
-                torch.cuda.synchronize()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(ext)
-                api.invert_blocks_device(W.data_ptr(), n, nmat, method, ctx=ctx)
-                e1.record(ext)
-                e1.synchronize()
-                times.append(e0.elapsed_time(e1))
-            ms = float(np.median(times))
-            # accuracy on a sample of blocks against an FP64 inverse
-            idx = np.linspace(0, nmat - 1, 8).astype(int)
-            Ah = A[idx].cpu().numpy().astype(np.complex128)
-            Wh = W[idx].cpu().numpy().astype(np.complex128)
-            err = max(np.linalg.norm(Wh[k] - np.linalg.inv(Ah[k])) / np.linalg.norm(np.linalg.inv(Ah[k]))
-                      for k in range(len(idx)))
-            res[method] = {"ms": ms, "TFLOPs": 8 * n ** 3 * nmat / (ms * 1e-3) / 1e12, "max_rel_err_vs_fp64": err}
-        res["speedup_tc_vs_cuda"] = res["cuda"]["ms"] / res["tc"]["ms"]
-        out[name] = res
+    out = _lu_cases(api, ctx, args.steps, args.warmup, batch_cap=args.lu_batch)
     print(json.dumps({"metric": "batched block inversion (preconditioner build), FP32 complex", "unit": "ms",
                       "steps": args.steps, "warmup": args.warmup, "results": out}), flush=True)
     return 0
-
 
 def run_nop(args):
     """Galerkin N-operator Toeplitz assembly (far + medium cells of
@@ -895,6 +914,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (16- and 512-rhs) measurements")
+    ap.add_argument("--no-koch", action="store_true", help="skip the 256x256x64 snowflake section of the main line")
     ap.add_argument("--sweep", action="store_true", help="passes mode: also time every z-pass and GEMV shape")
     ap.add_argument("--shapes", default=None,
                     help='JSON {"op": {...}, "prec": {...}} c64 launch shapes applied after autotuning '
