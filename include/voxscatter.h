@@ -436,8 +436,10 @@ typedef struct vs_shape {
   int lg_tile_z;   /* z pass (shared-memory kernel): log2 x-tile width             */
   int z_reg;       /* z pass: 0 shared-memory Stockham, 1 two-level registers,
                       2 two-level with a register cap for occupancy          */
-  int y_reg;       /* y passes: 0 shared-memory Stockham, 1 two-level registers */
-  int x_reg;       /* x passes: 0 shared-memory Stockham, 1 two-level registers */
+  int y_reg;       /* y passes: 0 shared-memory Stockham, 1 two-level registers,
+                      2 (VS_C128 only) two-level in double-float arithmetic,
+                      where the length has that kernel (else as 1)        */
+  int x_reg;       /* x passes: as y_reg                                    */
   int z_df;        /* VS_C128 only: 1 runs the two-level z pass in double-float
                       arithmetic (pairs of floats, about 48 bits) on the FP64
                       data; 0 / -1 FP64 arithmetic                            */

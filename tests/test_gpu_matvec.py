@@ -7,6 +7,7 @@ import pytest
 import oracle as O
 from oracle.mvp import MVP_plain_transpose
 from voxscatter_gb300 import workloads as W
+from voxscatter_gb300._lib import VoxScatterError
 
 pytestmark = pytest.mark.gpu
 
@@ -237,9 +238,10 @@ Y_LENGTHS = [8, 9, 10, 12, 15, 16, 18, 20, 24, 25, 27, 30, 32, 36, 40, 45, 48, 5
 def test_y_lengths_both_y_kernels(api, n):
     """Every strided length with a two-level register kernel: the matvec's
     y passes with Q = n forced (M = ceil(n/2)) and the preconditioner's y
-    passes with M = n, in c64 and c128, two-level and shared-memory Stockham,
-    against the oracle on a 3 x M x 2 block of voxels (tolerances in the
-    body)."""
+    passes with M = n, in c64 and c128, two-level and shared-memory Stockham
+    (c128 also two-level in double-float arithmetic, where the length has that
+    kernel), against the oracle on a 3 x M x 2 block of voxels (tolerances in
+    the body)."""
     from voxscatter_gb300.geometry import grid3d
     rng = np.random.default_rng(n)
     d, ko = 0.07, 2 * np.pi
@@ -255,7 +257,7 @@ def test_y_lengths_both_y_kernels(api, n):
         x = rng.normal(size=idx3.size) + 1j * rng.normal(size=idx3.size)
         y_o = O.MVP(x, fN, np.ones((L, M, N)), d ** 3, 3.0, "notransp", idx3)
         for prec, tol in (("c64", C64_TOL), ("c128", C128_TOL)):
-            for y_reg in (0, 1):
+            for y_reg in ((0, 1) if prec == "c64" else (0, 1, 2)):
                 op.set_shape(prec, y_reg=y_reg)
                 assert rel(op.apply(x, "notransp", prec), y_o) < tol, (prec, y_reg, op.PQR)
         if check_prec:
@@ -286,8 +288,9 @@ def test_x_lengths_both_x_kernels(api, n):
     """Every x length with a two-level register kernel: the matvec's x passes
     with P = n forced (L = ceil(n/2), a quarter of the voxels absent, varying
     diagonals, all three modes) and the preconditioner's x passes with L = n,
-    c64 and c128, two-level and shared-memory Stockham, against the oracle
-    (tolerances in the body)."""
+    c64 and c128, two-level and shared-memory Stockham (the matvec's c128 also
+    two-level in double-float arithmetic, where the length has that kernel),
+    against the oracle (tolerances in the body)."""
     from voxscatter_gb300.geometry import grid3d
     rng = np.random.default_rng(1000 + n)
     d, ko = 0.07, 2 * np.pi
@@ -309,11 +312,13 @@ def test_x_lengths_both_x_kernels(api, n):
         for flag in ("notransp", "transp"):
             y_o = O.MVP(x, fN, Mr, Mc, Gram, flag, idx3)
             for prec, tol in (("c64", C64_TOL), ("c128", C128_TOL)):
-                for x_reg in (0, 1):
+                for x_reg in ((0, 1) if prec == "c64" else (0, 1, 2)):
                     op.set_shape(prec, x_reg=x_reg)
                     assert rel(op.apply(x, flag, prec), y_o) < tol, (flag, prec, x_reg, op.PQR)
+        with pytest.raises(VoxScatterError, match="VS_C128 only"):
+            op.set_shape("c64", x_reg=2)
         y_t = MVP_plain_transpose(x, fN, Mr, Mc, Gram, idx3)
-        for x_reg in (0, 1):
+        for x_reg in (0, 1, 2):
             op.set_shape("c128", x_reg=x_reg)
             assert rel(op.apply(x, "plain_transp", "c128"), y_t) < C128_TOL, (x_reg, op.PQR)
         if check_prec:

@@ -1084,15 +1084,17 @@ int vs_op_set_shape(vs_op* op, int precision, const vs_shape* shape) {
                "y tile exceeds shared memory");
     VS_REQUIRE(shape->lg_tile_z < 0 || (2ull * op->R * 3 * (1 << shape->lg_tile_z) + op->R) * cs <= lim,
                "z tile exceeds shared memory");
+    VS_REQUIRE(shape->z_reg >= -1 && shape->z_reg <= 2, "z_reg must be -1, 0, 1 or 2");
+    VS_REQUIRE(shape->y_reg >= -1 && shape->y_reg <= 2, "y_reg must be -1, 0, 1 or 2");
+    VS_REQUIRE(shape->x_reg >= -1 && shape->x_reg <= 2, "x_reg must be -1, 0, 1 or 2");
+    VS_REQUIRE((shape->y_reg != 2 && shape->x_reg != 2) || precision == VS_C128,
+               "x_reg / y_reg 2 (double-float arithmetic) apply to VS_C128 only");
+    VS_REQUIRE(shape->z_df >= -1 && shape->z_df <= 1, "z_df must be -1, 0 or 1");
+    VS_REQUIRE(shape->z_df != 1 || precision == VS_C128, "z_df applies to VS_C128 only");
     vs::PassShape& s = op->shape[precision == VS_C64 ? 0 : 1];
     s.lg_lpb_x = shape->lg_lines_x;
     s.lg_tx_y = shape->lg_tile_y;
     s.lg_tx_z = shape->lg_tile_z;
-    VS_REQUIRE(shape->z_reg >= -1 && shape->z_reg <= 2, "z_reg must be -1, 0, 1 or 2");
-    VS_REQUIRE(shape->y_reg >= -1 && shape->y_reg <= 1, "y_reg must be -1, 0 or 1");
-    VS_REQUIRE(shape->x_reg >= -1 && shape->x_reg <= 1, "x_reg must be -1, 0 or 1");
-    VS_REQUIRE(shape->z_df >= -1 && shape->z_df <= 1, "z_df must be -1, 0 or 1");
-    VS_REQUIRE(shape->z_df != 1 || precision == VS_C128, "z_df applies to VS_C128 only");
     s.z_reg = shape->z_reg;
     s.y_reg = shape->y_reg;
     s.x_reg = shape->x_reg;

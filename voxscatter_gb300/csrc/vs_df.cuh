@@ -48,6 +48,9 @@ __device__ __forceinline__ df operator+(df a, df b) {
 __device__ __forceinline__ df operator-(df a) { return df_make(-a.hi, -a.lo); }
 __device__ __forceinline__ df operator-(df a, df b) { return a + (-b); }
 
+__device__ __forceinline__ df& operator+=(df& a, df b) { return a = a + b; }
+__device__ __forceinline__ df& operator-=(df& a, df b) { return a = a - b; }
+
 __device__ __forceinline__ df operator*(df a, df b) {
   const float p = __fmul_rn(a.hi, b.hi);
   float e = __fmaf_rn(a.hi, b.hi, -p);  // exact error of the leading product
@@ -68,6 +71,7 @@ __device__ __forceinline__ dfc cmul(dfc a, dfc b) { return dfc{a.x * b.x - a.y *
 __device__ __forceinline__ dfc cfma(dfc b, dfc c, dfc a) {
   return dfc{a.x + (b.x * c.x - b.y * c.y), a.y + (b.x * c.y + b.y * c.x)};
 }
+__device__ __forceinline__ dfc cconj(dfc a) { return dfc{a.x, -a.y}; }
 template <> __device__ __forceinline__ dfc czero<dfc>() { return dfc{df(0.0), df(0.0)}; }
 
 // storage (double2) <-> compute (dfc); identity for the native types

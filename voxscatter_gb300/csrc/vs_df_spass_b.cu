@@ -1,0 +1,6 @@
+// Double-float two-level strided (y) passes on FP64 data, lengths of VS_DF_LIST_B.
+#include "vs_df_passes.cuh"
+
+namespace vs {
+VS_DF_S_UNIT(strided_two_level_df_b, VS_DF_LIST_B)
+}  // namespace vs

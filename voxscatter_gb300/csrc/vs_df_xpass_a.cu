@@ -1,0 +1,6 @@
+// Double-float two-level x passes on FP64 data, lengths of VS_DF_LIST_A.
+#include "vs_df_passes.cuh"
+
+namespace vs {
+VS_DF_X_UNIT(x_two_level_df_a, VS_DF_LIST_A)
+}  // namespace vs

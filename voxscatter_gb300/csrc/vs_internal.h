@@ -47,8 +47,9 @@ template <> inline const double2* FftAxis::tw<double>() const { return tw64.as<d
 struct PassShape {
   int lg_lpb_x = -1;   // x passes: lines per CTA
   int lg_tx_y = -1;    // y passes: x-tile width
-  int y_reg = -1;      // y passes: 1 two-level register kernel, 0 shared-memory Stockham, -1 default (Stockham)
-  int x_reg = -1;      // x passes: 1 two-level register kernel, 0 shared-memory Stockham, -1 default (Stockham)
+  int y_reg = -1;      // y passes: 1 two-level register kernel, 0 shared-memory Stockham, -1 default (Stockham),
+                       // 2 (operators' FP64 data) two-level in double-float arithmetic
+  int x_reg = -1;      // x passes: as y_reg
   int lg_tx_z = -1;    // z pass: x-tile width
   int gemv_ti = 0;     // preconditioner GEMV: stored blocks per CTA (direct) or CTAs per SM (streamed); 0 = default
   int gemv_threads = 0;

@@ -265,7 +265,10 @@ void ensure_scratch(vs_op& op, int nrhs, size_t elem_bytes) {
 
 template <typename T>
 void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaStream_t st) {
-  if (a.two_level == 1) {
+  if constexpr (std::is_same<T, double>::value) {
+    if (a.two_level == 2 && x_two_level_df(a, inverse, mode, nrhs, st)) return;
+  }
+  if (a.two_level >= 1) {
     if (!inverse && x_two_level<T, false>(a, mode, nrhs, st)) return;
     if (inverse && x_two_level<T, true>(a, mode, nrhs, st)) return;
   }
@@ -303,7 +306,10 @@ void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaS
 
 template <typename T, bool INV>
 void launch_strided_pass(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st) {
-  if (a.two_level == 1 && strided_two_level<T, INV>(a, nplanes, nrhs, st)) return;
+  if constexpr (std::is_same<T, double>::value) {
+    if (a.two_level == 2 && strided_two_level_df(a, INV, nplanes, nrhs, st)) return;
+  }
+  if (a.two_level >= 1 && strided_two_level<T, INV>(a, nplanes, nrhs, st)) return;
   const int tx = 1 << a.lg_tx;
   dim3 grid(ceil_div(a.xext, tx), nplanes, nrhs);
   const size_t smem = (2ull * a.plan.n * tx + a.plan.n) * sizeof(cplx_t<T>);
@@ -339,7 +345,7 @@ static StridedArgs<T> y_pass_args(const vs_op& op, const PipeArgs<T>& a, bool in
   s.tw = a.twQ;
   s.skip = a.skip;
   s.skip_stride = a.skip_stride;
-  s.two_level = sh.y_reg == 1 ? 1 : 0;
+  s.two_level = sh.y_reg >= 1 ? sh.y_reg : 0;
   return s;
 }
 
@@ -371,7 +377,7 @@ static PipeArgs<T> pipe_args(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, 
   a.pP = op.ax[0].plan; a.pQ = op.ax[1].plan; a.pR = op.ax[2].plan;
   const PassShape& sh = op.shape[std::is_same<T, float>::value ? 0 : 1];
   a.lg_lpb = sh.lg_lpb_x >= 0 ? sh.lg_lpb_x : ilog2(pick_lpb(op.P, sizeof(C)));
-  a.two_level = sh.x_reg == 1 ? 1 : 0;
+  a.two_level = sh.x_reg >= 1 ? sh.x_reg : 0;
   a.lg_tx = sh.lg_tx_z >= 0 ? sh.lg_tx_z : ilog2(pick_tile(op.R, sizeof(C), 3));
   a.skip = skip;
   a.skip_stride = skip_stride;
@@ -645,7 +651,10 @@ void autotune_op(vs_op& op, cudaStream_t st) {
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 0);
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 4);
           });
-  best_of(&sh.x_reg, 0, 1, [&](int) { return true; },
+  // FP64 data: 2 is the two-level kernel in double-float arithmetic (where
+  // the length has it; its results agree with FP64 to a few units of 2^-48)
+  const int reg_hi = std::is_same<T, double>::value ? 2 : 1;
+  best_of(&sh.x_reg, 0, reg_hi, [&](int v) { return v < 2 || x_df_available(op.P); },
           [&] {
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 0);
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 4);
@@ -656,7 +665,7 @@ void autotune_op(vs_op& op, cudaStream_t st) {
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 1);
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 3);
           });
-  best_of(&sh.y_reg, 0, 1, [&](int) { return true; },
+  best_of(&sh.y_reg, 0, reg_hi, [&](int v) { return v < 2 || strided_df_available(op.Q); },
           [&] {
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 1);
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 3);

@@ -35,7 +35,8 @@ struct PipeArgs {
   int lg_tx;   // log2 x-tile width of the z pass
   const int* skip;   // right-hand side r is skipped when skip[r * skip_stride] != 0
   int skip_stride;
-  int two_level;     // x passes: 1 two-level register kernel (vs_xpass.cuh) when P has one
+  int two_level;     // x passes: 1 two-level register kernel (vs_xpass.cuh) when P has one,
+                     // 2 the same in double-float arithmetic (FP64 data only)
   // Gram of each right-hand side in place of the operator's (the reference
   // passes Gram to every MVP call; DDA's Gram = 1/alpha_LDR depends on the
   // incident direction and polarisation): Gram_r(pos) = grhs[r * grhs_per +
@@ -74,7 +75,8 @@ struct StridedArgs {
   const C* tw;
   const int* skip;
   int skip_stride;
-  int two_level;  // 1: two-level register kernel (vs_spass.cuh) when the length has one
+  int two_level;  // 1: two-level register kernel (vs_spass.cuh) when the length has one;
+                  // 2: the same in double-float arithmetic (FP64 data only)
 };
 
 // Two-level x pass (vs_xpass.cuh); false when P has no instantiation.
@@ -90,6 +92,12 @@ template <typename T, typename K = cplx_t<T>>
 bool z_pass_two_level(const PipeArgs<T>& a, bool sym, bool cap, int nrhs, cudaStream_t st);
 // c128 storage, double-float arithmetic (vs_zpass_df.cu)
 bool z_pass_two_level_df(const PipeArgs<double>& a, bool sym, int nrhs, cudaStream_t st);
+// c128 storage, double-float arithmetic of the two-level x and strided passes
+// (vs_df_xpass.cu, vs_df_spass.cu); false when the length has no instantiation.
+bool x_two_level_df(const PipeArgs<double>& a, bool inverse, int mode, int nrhs, cudaStream_t st);
+bool strided_two_level_df(const StridedArgs<double>& a, bool inverse, int nplanes, int nrhs, cudaStream_t st);
+bool x_df_available(int P);
+bool strided_df_available(int n);
 
 template <typename T>
 void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaStream_t st);

@@ -767,9 +767,11 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 //    and leaves its partial sums as [g][W][row].
 // Block boundaries therefore never stop the stream.  Hand-offs use mbarriers:
 // vfull[b] (vector warps -> consumers: buffer b holds the block's vectors),
-// done[b] (consumers -> vector warps: partial sums of buffer b written, the
-// block's vectors no longer needed) and rfree[b] (vector warps -> consumers:
-// partial sums of buffer b consumed).  Ring positions and phases advance by
+// done[b] (consumers -> vector warps: the block's partial sums written, its
+// vectors no longer needed) and rfree (vector warps -> consumers: the partial
+// sums consumed).  The partial sums have one buffer: a block's are written
+// after all of its chunks, by when the previous block's have long been
+// reduced, so a second buffer would only take shared memory from the ring.  Ring positions and phases advance by
 // counters (no divisions on the loops).  Every wait is bounded; a wait that
 // runs out sets status bit 4 and the abort flag, every role leaves its loop,
 // and the producer waits (bounded) for its last copies before the CTA ends.
@@ -797,12 +799,12 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
   uint64_t* empty = full + 8;                               // [8]
   uint64_t* vfull = empty + 8;                              // [2]
   uint64_t* done = vfull + 2;                               // [2]
-  uint64_t* rfree = done + 2;                               // [2]
+  uint64_t* rfree = done + 2;                               // [1]
   volatile int* ctl = reinterpret_cast<volatile int*>(rfree + 2);  // [0] abort
   C* stg = reinterpret_cast<C*>(smem_raw + 256);
   const int n = 3 * N, Lb = L / 2 + 1, Mb = M / 2 + 1;
   C* vt0 = stg + (size_t)nstage * stage_elems;  // 2 x [n][W]
-  C* red0 = vt0 + (size_t)2 * n * W;            // 2 x [G][n][W]
+  C* red0 = vt0 + (size_t)2 * n * W;            // [G][W][n]
   const int64_t nblk = (int64_t)Lb * Mb, LM = (int64_t)L * M;
   const int tid = threadIdx.x, lane = tid & 31;
   const int64_t nmine = blockIdx.x < nblk ? (nblk - 1 - blockIdx.x) / gridDim.x + 1 : 0;
@@ -818,8 +820,8 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
     for (int b = 0; b < 2; ++b) {
       mbar_init(smem_addr(vfull + b), nv);
       mbar_init(smem_addr(done + b), ncw);
-      mbar_init(smem_addr(rfree + b), nv);
     }
+    mbar_init(smem_addr(rfree), nv);
     ctl[0] = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -884,7 +886,7 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
       }
       const int64_t base = base_of(kb);
       if (rg < nr && base >= 0) {
-        const C* red = red0 + (size_t)b * G * nW + (size_t)col * n;
+        const C* red = red0 + (size_t)col * n;
         C* dst = trg + base;
         for (int q = q0; q < n; q += qstep) {
           C sum = red[q];
@@ -894,7 +896,7 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
         }
       }
       __syncwarp();
-      if (lane == 0) mbar_arrive(smem_addr(rfree + b));
+      if (lane == 0) mbar_arrive(smem_addr(rfree));
       if (kb + 2 < nmine) gather(kb + 2);
     }
     return;
@@ -1031,14 +1033,15 @@ __global__ void __launch_bounds__(384) k_block_gemv_stream(cplx_t<T>* __restrict
         sph ^= 1;
       }
     }
-    if (ok && kb >= 2) ok = !ctl[0] && mbar_wait(smem_addr(rfree + b), (uint32_t)(((kb >> 1) - 1) & 1), polls);
+    // the previous block's partial sums have been reduced (phase kb - 1 of rfree)
+    if (ok && kb >= 1) ok = !ctl[0] && mbar_wait(smem_addr(rfree), (uint32_t)((kb - 1) & 1), polls);
     if (!ok) {
       if (lane == 0) fail();
       break;
     }
     if (tid < nact) {
       // partial sums as [g][W][row]: the RW rows of a thread are adjacent
-      C* red = red0 + (size_t)b * G * nW + (size_t)g * W * n + RW * rp;
+      C* red = red0 + (size_t)g * W * n + RW * rp;
 #pragma unroll
       for (int c = 0; c < W; ++c) {
         if constexpr (PAIR) {
@@ -1106,7 +1109,7 @@ static GemvStream gemv_stream_geometry(int n, int rg, int chunk_cols, bool pair,
   g.nc = (g.G * nrow + 31) / 32 * 32;
   g.nv = std::max(1, std::min(4, (384 - g.nc - 32) / 32));
   const size_t vbytes = (size_t)n * 4 * rg * cs;
-  const size_t fixed = 256 + (size_t)2 * vbytes + (size_t)2 * g.G * vbytes;
+  const size_t fixed = 256 + (size_t)2 * vbytes + (size_t)g.G * vbytes;
   const size_t stage_target = 16 * 1024;
   auto stage_bytes = [&](int c) { return (((size_t)n * c + 2) * cs + 15) / 16 * 16; };
   for (int c = std::max(1, std::min(ctas, 4)); c >= 1; --c) {
@@ -1216,7 +1219,7 @@ static GemvStream gemv_packed_geometry(int n, int rg, int nstage, int ctas) {
   g.nc = (g.G * n + 31) / 32 * 32;
   g.nv = std::max(1, std::min(4, (384 - g.nc - 32) / 32));
   const size_t vbytes = (size_t)n * 4 * rg * cs;
-  const size_t fixed = 256 + (size_t)2 * vbytes + (size_t)2 * g.G * vbytes;
+  const size_t fixed = 256 + (size_t)2 * vbytes + (size_t)g.G * vbytes;
   const size_t stage = (size_t)packed_stride(n) * cs;
   for (int c = std::max(1, std::min(ctas, 4)); c >= 1; --c) {
     const size_t budget = c == 1 ? 220 * 1024 : (228 * 1024) / c - 1024;

@@ -17,8 +17,10 @@
 // Each element crosses shared memory once each way (the shared-memory
 // Stockham kernel k_strided of vs_matvec.cu crosses it once per radix stage);
 // the shared layout [n1][k2][x] is conflict-free in both stages.  Lengths
-// outside the instantiated list use k_strided.  Instantiated per precision in
-// vs_spass_c64.cu and vs_spass_c128.cu.
+// outside the instantiated list use k_strided.  K is the arithmetic type: the
+// storage type, or double-float (dfc) on FP64 data.  Instantiated per
+// precision in vs_spass_c64.cu and vs_spass_c128.cu, in double-float in
+// vs_df_passes.cu.
 #pragma once
 #include "vs_zpass.cuh"
 
@@ -34,14 +36,15 @@ constexpr int s2_tx() {
   return tx;
 }
 
-template <typename T, int R1, int R2, bool INV>
+template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>>
 __global__ void __launch_bounds__(z2_threads(R2, s2_tx<T, R2>())) k_s2(StridedArgs<T> a) {
-  using C = cplx_t<T>;
+  using C = cplx_t<T>;  // storage
+  static_assert(sizeof(K) == sizeof(C), "compute and storage elements share the shared-memory layout");
   constexpr int N = R1 * R2, TX = s2_tx<T, R2>(), NT = z2_threads(R2, TX);
   if (a.skip && a.skip[blockIdx.z * a.skip_stride]) return;
-  C* S = shmem<C>();  // [R1][R2][TX]
-  C* tw = S + N * TX;
-  for (int i = threadIdx.x; i < N; i += NT) tw[i] = __ldg(a.tw + i);
+  K* S = shmem<K>();  // [R1][R2][TX]
+  K* tw = S + N * TX;
+  for (int i = threadIdx.x; i < N; i += NT) tw[i] = to_compute<K>(__ldg(a.tw + i));
   const int x0 = blockIdx.x * TX;
   const int pa = blockIdx.y % a.na, pb = blockIdx.y / a.na;
   const C* src = a.src + pa * a.s_a + pb * a.s_b + (int64_t)blockIdx.z * a.s_rhs;
@@ -52,14 +55,14 @@ __global__ void __launch_bounds__(z2_threads(R2, s2_tx<T, R2>())) k_s2(StridedAr
       const int xl = it % TX, n1 = it / TX;
       const int x = x0 + xl;
       const bool xin = x < a.xext;
-      C v[R2];
+      K v[R2];
 #pragma unroll
       for (int n2 = 0; n2 < R2; ++n2) {
         const int row = n1 + R1 * n2;
-        v[n2] = (xin && row < a.n_in) ? src[row * a.s_row + x] : czero<C>();
+        v[n2] = (xin && row < a.n_in) ? to_compute<K>(src[row * a.s_row + x]) : czero<K>();
       }
-      reg_dft<R2, R2, 1, R1, false, C>(v, tw);
-      C* s = S + (n1 * R2) * TX + xl;
+      reg_dft<R2, R2, 1, R1, false, K>(v, tw);
+      K* s = S + (n1 * R2) * TX + xl;
 #pragma unroll
       for (int k2 = 0; k2 < R2; ++k2) s[k2 * TX] = (k2 == 0 || n1 == 0) ? v[k2] : cmul(v[k2], tw[n1 * k2]);
     }
@@ -67,15 +70,15 @@ __global__ void __launch_bounds__(z2_threads(R2, s2_tx<T, R2>())) k_s2(StridedAr
     for (int it = threadIdx.x; it < R2 * TX; it += NT) {
       const int xl = it % TX, k2 = it / TX;
       const int x = x0 + xl;
-      C u[R1];
+      K u[R1];
 #pragma unroll
       for (int n1 = 0; n1 < R1; ++n1) u[n1] = S[(n1 * R2 + k2) * TX + xl];
-      reg_dft<R1, R1, 1, R2, false, C>(u, tw);
+      reg_dft<R1, R1, 1, R2, false, K>(u, tw);
       if (x < a.xext) {
 #pragma unroll
         for (int k1 = 0; k1 < R1; ++k1) {
           const int row = k2 + R2 * k1;
-          if (row < a.n_out) dst[row * a.d_row + x] = u[k1];
+          if (row < a.n_out) dst[row * a.d_row + x] = to_storage(u[k1], C{});
         }
       }
     }
@@ -84,13 +87,13 @@ __global__ void __launch_bounds__(z2_threads(R2, s2_tx<T, R2>())) k_s2(StridedAr
       const int xl = it % TX, k2 = it / TX;
       const int x = x0 + xl;
       const bool xin = x < a.xext;
-      C u[R1];
+      K u[R1];
 #pragma unroll
       for (int k1 = 0; k1 < R1; ++k1) {
         const int row = k2 + R2 * k1;
-        u[k1] = (xin && row < a.n_in) ? src[row * a.s_row + x] : czero<C>();
+        u[k1] = (xin && row < a.n_in) ? to_compute<K>(src[row * a.s_row + x]) : czero<K>();
       }
-      reg_dft<R1, R1, 1, R2, true, C>(u, tw);
+      reg_dft<R1, R1, 1, R2, true, K>(u, tw);
 #pragma unroll
       for (int n1 = 0; n1 < R1; ++n1)
         S[(n1 * R2 + k2) * TX + xl] = (n1 == 0 || k2 == 0) ? u[n1] : cmul(u[n1], twid<true>(tw, n1 * k2));
@@ -100,25 +103,25 @@ __global__ void __launch_bounds__(z2_threads(R2, s2_tx<T, R2>())) k_s2(StridedAr
       const int xl = it % TX, n1 = it / TX;
       const int x = x0 + xl;
       if (x >= a.xext || n1 >= a.n_out) continue;
-      C v[R2];
-      const C* s = S + (n1 * R2) * TX + xl;
+      K v[R2];
+      const K* s = S + (n1 * R2) * TX + xl;
 #pragma unroll
       for (int k2 = 0; k2 < R2; ++k2) v[k2] = s[k2 * TX];
-      reg_dft<R2, R2, 1, R1, true, C>(v, tw);
+      reg_dft<R2, R2, 1, R1, true, K>(v, tw);
 #pragma unroll
       for (int n2 = 0; n2 < R2; ++n2) {
         const int row = n1 + R1 * n2;
-        if (row < a.n_out) dst[row * a.d_row + x] = v[n2];
+        if (row < a.n_out) dst[row * a.d_row + x] = to_storage(v[n2], C{});
       }
     }
   }
 }
 
-template <typename T, int R1, int R2, bool INV>
+template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>>
 static void launch_s2(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st) {
   constexpr int TX = s2_tx<T, R2>(), NT = z2_threads(R2, TX);
   const size_t smem = (size_t)(R1 * R2 * TX + R1 * R2) * sizeof(cplx_t<T>);
-  auto k = k_s2<T, R1, R2, INV>;
+  auto k = k_s2<T, R1, R2, INV, K>;
   set_kernel_smem((const void*)k, smem);
   k<<<dim3(ceil_div(a.xext, TX), nplanes, nrhs), NT, smem, st>>>(a);
   VS_LAUNCH_CHECK();

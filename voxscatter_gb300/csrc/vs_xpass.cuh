@@ -19,8 +19,11 @@
 // threads vary (conflict-free, unlike the strided 1-D table), and the first
 // stage issues its global loads before the tables are filled, so the fill
 // and the barrier overlap their latency.  Every thread holds at most one item
-// of a stage (R1 <= R2).
-// Instantiated per precision in vs_xpass_c64.cu and vs_xpass_c128.cu.
+// of a stage (R1 <= R2).  K is the arithmetic type: the storage type, or
+// double-float (dfc) on FP64 data, whose DFTs then run on the FP32 pipes and
+// whose results are rounded back to FP64 at the global stores.
+// Instantiated per precision in vs_xpass_c64.cu and vs_xpass_c128.cu, in
+// double-float in vs_df_passes.cu.
 #pragma once
 #include "vs_spass.cuh"
 
@@ -38,17 +41,18 @@ __device__ __forceinline__ cplx_t<T> x2_gather(const PipeArgs<T>& a, const cplx_
   return v;
 }
 
-template <typename T, int R1, int R2, bool INV>
+template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>>
 __global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
-  using C = cplx_t<T>;
+  using C = cplx_t<T>;  // storage
+  static_assert(sizeof(K) == sizeof(C), "compute and storage elements share the shared-memory layout");
   constexpr int P = R1 * R2, NL = kX2Threads / R2, RS = R2 | 1;
   static_assert(R1 <= R2, "one stage item per thread");
   if (a.skip && a.skip[blockIdx.y * a.skip_stride]) return;
-  C* S = shmem<C>();  // [NL][R1][RS]
-  C* tw = S + NL * R1 * RS;
+  K* S = shmem<K>();  // [NL][R1][RS]
+  K* tw = S + NL * R1 * RS;
   // w^(n1*k2) laid out with the index the threads of a stage vary fastest:
   // [k2][n1] for XF stage A, [n1][k2] for XI stage B'
-  C* tw2 = tw + P;
+  K* tw2 = tw + P;
   const int rhs = blockIdx.y;
   const C* x = a.x + (int64_t)rhs * a.n3;
   const int64_t t1off = (int64_t)rhs * P * a.M * a.N * 3;
@@ -60,28 +64,28 @@ __global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
     // stage A loads first: the table fill and the barrier overlap their latency
     const int n1 = it % R1, l = it / R1, line = line0 + l;
     const bool act = it < R1 * NL;
-    C v[R2];
+    K v[R2];
     if (act && line < nlines) {
       const int c = line / MN, jk = line - c * MN;
       const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
 #pragma unroll
       for (int n2 = 0; n2 < R2; ++n2) {
         const int i = n1 + R1 * n2;
-        v[n2] = i < a.L ? x2_gather(a, x, __ldg(map + i), mode) : czero<C>();
+        v[n2] = i < a.L ? to_compute<K>(x2_gather(a, x, __ldg(map + i), mode)) : czero<K>();
       }
     } else {
 #pragma unroll
-      for (int n2 = 0; n2 < R2; ++n2) v[n2] = czero<C>();
+      for (int n2 = 0; n2 < R2; ++n2) v[n2] = czero<K>();
     }
     for (int i = it; i < P; i += kX2Threads) {
-      tw[i] = __ldg(a.twP + i);
+      tw[i] = to_compute<K>(__ldg(a.twP + i));
       const int k2 = i / R1, m1 = i - k2 * R1;
-      tw2[i] = __ldg(a.twP + m1 * k2);
+      tw2[i] = to_compute<K>(__ldg(a.twP + m1 * k2));
     }
     __syncthreads();
     if (act) {
-      reg_dft<R2, R2, 1, R1, false, C>(v, tw);
-      C* s = S + (l * R1 + n1) * RS;
+      reg_dft<R2, R2, 1, R1, false, K>(v, tw);
+      K* s = S + (l * R1 + n1) * RS;
 #pragma unroll
       for (int k2 = 0; k2 < R2; ++k2) s[k2] = (k2 == 0 || n1 == 0) ? v[k2] : cmul(v[k2], tw2[k2 * R1 + n1]);
     }
@@ -89,13 +93,13 @@ __global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
     {
       const int k2 = it % R2, lb = it / R2, lineb = line0 + lb;
       if (it < R2 * NL && lineb < nlines) {
-        C u[R1];
+        K u[R1];
 #pragma unroll
         for (int m1 = 0; m1 < R1; ++m1) u[m1] = S[(lb * R1 + m1) * RS + k2];
-        reg_dft<R1, R1, 1, R2, false, C>(u, tw);
+        reg_dft<R1, R1, 1, R2, false, K>(u, tw);
         C* out = t1 + (int64_t)lineb * P;
 #pragma unroll
-        for (int k1 = 0; k1 < R1; ++k1) out[k2 + R2 * k1] = u[k1];
+        for (int k1 = 0; k1 < R1; ++k1) out[k2 + R2 * k1] = to_storage(u[k1], C{});
       }
     }
   } else {
@@ -104,21 +108,21 @@ __global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
     // stage B' loads first
     const int k2 = it % R2, l = it / R2, line = line0 + l;
     const bool act = it < R2 * NL;
-    C u[R1];
+    K u[R1];
     {
       const C* in = t1 + (int64_t)line * P;
       const bool ld = act && line < nlines;
 #pragma unroll
-      for (int k1 = 0; k1 < R1; ++k1) u[k1] = ld ? in[k2 + R2 * k1] : czero<C>();
+      for (int k1 = 0; k1 < R1; ++k1) u[k1] = ld ? to_compute<K>(in[k2 + R2 * k1]) : czero<K>();
     }
     for (int i = it; i < P; i += kX2Threads) {
-      tw[i] = __ldg(a.twP + i);
+      tw[i] = to_compute<K>(__ldg(a.twP + i));
       const int m1 = i / R2, j2 = i - m1 * R2;
-      tw2[i] = __ldg(a.twP + m1 * j2);
+      tw2[i] = to_compute<K>(__ldg(a.twP + m1 * j2));
     }
     __syncthreads();
     if (act) {
-      reg_dft<R1, R1, 1, R2, true, C>(u, tw);
+      reg_dft<R1, R1, 1, R2, true, K>(u, tw);
 #pragma unroll
       for (int n1 = 0; n1 < R1; ++n1)
         S[(l * R1 + n1) * RS + k2] = (n1 == 0 || k2 == 0) ? u[n1] : cmul(u[n1], cconj(tw2[n1 * R2 + k2]));
@@ -126,11 +130,11 @@ __global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
     __syncthreads();
     const int n1 = it % R1, la = it / R1, linea = line0 + la;
     if (it < R1 * NL && linea < nlines && n1 < a.L) {
-      C v[R2];
-      const C* s = S + (la * R1 + n1) * RS;
+      K v[R2];
+      const K* s = S + (la * R1 + n1) * RS;
 #pragma unroll
       for (int j2 = 0; j2 < R2; ++j2) v[j2] = s[j2];
-      reg_dft<R2, R2, 1, R1, true, C>(v, tw);
+      reg_dft<R2, R2, 1, R1, true, K>(v, tw);
       const int c = linea / MN, jk = linea - c * MN;
       const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
 #pragma unroll
@@ -139,7 +143,7 @@ __global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
         if (i >= a.L) continue;
         const int pos = __ldg(map + i);
         if (pos < 0) continue;
-        const C conv = v[n2];
+        const C conv = to_storage(v[n2], C{});
         C out;
         if (mode == MODE_PLAIN) {
           out = conv;
@@ -155,11 +159,11 @@ __global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
   }
 }
 
-template <typename T, int R1, int R2, bool INV>
+template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>>
 static void launch_x2(const PipeArgs<T>& a, int mode, int nrhs, cudaStream_t st) {
   constexpr int NL = kX2Threads / R2, RS = R2 | 1;
   const size_t smem = (size_t)(NL * R1 * RS + 2 * R1 * R2) * sizeof(cplx_t<T>);
-  auto k = k_x2<T, R1, R2, INV>;
+  auto k = k_x2<T, R1, R2, INV, K>;
   set_kernel_smem((const void*)k, smem);
   const int nlines = a.M * a.N * 3;
   k<<<dim3(ceil_div(nlines, NL), nrhs), kX2Threads, smem, st>>>(a, mode);

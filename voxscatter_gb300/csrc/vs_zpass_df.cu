@@ -19,3 +19,26 @@ bool z_pass_two_level_df(const PipeArgs<double>& a, bool sym, int nrhs, cudaStre
   }
 }
 }  // namespace vs
+
+// ---- double-float x and strided passes (lengths in vs_df_passes.cuh) ----
+#include "vs_df_passes.cuh"
+
+namespace vs {
+bool x_df_available(int P) {
+  switch (P) {
+#define VS_DFA(R1, R2) case R1 * R2:
+    VS_DF_LIST(VS_DFA)
+#undef VS_DFA
+    return true;
+    default: return false;
+  }
+}
+bool strided_df_available(int n) { return x_df_available(n); }
+bool x_two_level_df(const PipeArgs<double>& a, bool inverse, int mode, int nrhs, cudaStream_t st) {
+  return x_two_level_df_a(a, inverse, mode, nrhs, st) || x_two_level_df_b(a, inverse, mode, nrhs, st);
+}
+bool strided_two_level_df(const StridedArgs<double>& a, bool inverse, int nplanes, int nrhs, cudaStream_t st) {
+  return strided_two_level_df_a(a, inverse, nplanes, nrhs, st) ||
+         strided_two_level_df_b(a, inverse, nplanes, nrhs, st);
+}
+}  // namespace vs
