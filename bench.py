@@ -496,7 +496,16 @@ def run_ours(args):
     torch.cuda.nvtx.range_pop()
     x_mixed = x_dev.cpu().numpy()
 
-    # per-launch timing of the pipeline passes (c64) for the roofline
+    # one more mixed solve with CUDA events between the launches of its
+    # captured iterations: every pass's duration inside the solve itself
+    # (vs_solve_opts.profile_ms; the event nodes add a little, so it is not timed)
+    with torch.cuda.stream(stream):
+        x_dev.zero_()
+    ctx.synchronize()
+    prof = api.solve_device(op, b_dev.data_ptr(), x_dev.data_ptr(), prec, tol=TOL, precision="mixed",
+                            profile=True)["profile"]
+
+    # per-launch timing of the pipeline passes (c64), each pass alone
     xs = torch.randn(n3, dtype=torch.complex64, device="cuda")
     ys = torch.empty_like(xs)
     torch.cuda.synchronize()
@@ -504,15 +513,32 @@ def run_ours(args):
     pc_ms = prec.time_passes(xs.data_ptr(), ys.data_ptr(), 1, "c64", 50)
     mv_bytes, pc_bytes, pinned = _pass_bytes(p, op.PQR, n3, packed=prec.shape("c64")["gemv_mode"] == 2)
     names_mv, names_pc = _pass_names(op, prec)
-    allk = [(names_mv[i], mv_ms[i], mv_bytes[i]) for i in range(5)] + \
-           [(names_pc[i], pc_ms[i], pc_bytes[i]) for i in range(5)]
+    keys = api.PROFILE_KEYS
+    in_solve = [prof[k] for k in keys]
+    # the dominant HBM-bound launch and its roofline: CUDA events around one
+    # launch of each pass on the library's stream (mean of 50), its duration
+    # inside the solve's graph beside it
+    allk = [(names_pc[i], pc_ms[i], pc_bytes[i], in_solve[i]) for i in range(5)] + \
+           [(names_mv[i], mv_ms[i], mv_bytes[i], in_solve[5 + i]) for i in range(5)]
     dom = max(allk, key=lambda t: t[1])
     peak, peak_kind = _peaks()
     achieved = dom[2] / (dom[1] * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind,
             "bytes_per_launch": dom[2], "ms_per_launch": dom[1],
+            "ms_source": "CUDA events around one launch on the library's stream, mean of 50",
+            "ms_per_launch_in_solve": dom[3],
             "traffic": _traffic_from_profiles(dom[0])}
+    per_iter = 2 * sum(in_solve) + prof["solver_kernels_per_iter"]
+    in_solve_line = {
+        "source": "CUDA event nodes between the launches of one solve's captured iterations "
+                  "(vs_solve_opts.profile_ms); each interval also holds one event node, so the "
+                  "absolutes run a few us high and the shares are the figures to read",
+        "per_iteration_ms": per_iter, "iterations_profiled": prof["iterations"],
+        "passes_ms": dict(zip(keys, in_solve)), "solver_kernels_per_iter_ms": prof["solver_kernels_per_iter"],
+        "share_of_iteration": {**{k: 2 * v / per_iter for k, v in zip(keys, in_solve)},
+                               "solver_kernels": prof["solver_kernels_per_iter"] / per_iter},
+        "fp64_residual_ms": prof["fp64_residual"], "fp64_residual_calls": prof["fp64_residual_calls"]}
     mv_total = sum(mv_ms)
     # the same pipeline on a batch of 16 right-hand sides (8 directions x 2
     # polarisations share one operator): intermediates 16x, spectrum read once
@@ -549,7 +575,7 @@ def run_ours(args):
             "refinements": last["refinements"],
             "fp64_solve_ms": ms_fp64, "fp64_iterations": infos64[-1]["iter"],
             "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed, "setup_ms": setup_ms,
-            "roofline": roof, "matvec": matvec,
+            "roofline": roof, "in_solve": in_solve_line, "matvec": matvec,
             "shapes": {"op": op.shape("c64"), "prec": prec.shape("c64")},
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(b_pin.numel() * 16 * 2),
                     "d2h_bytes_per_step": int(x_pin.numel() * 16)},

@@ -274,6 +274,17 @@ typedef struct vs_solve_opts {
    * one it was built for (it only changes the convergence, not the solution). */
   const double* gram;
   int64_t gram_n;
+  /* Optional, VS_BICGSTAB: 16 floats that receive durations inside this solve
+   * (ms), from CUDA events recorded between the launches of the captured
+   * iterations (graph launches after which every right-hand side was still
+   * iterating): [0..4] the preconditioner's five passes, [5..9] the matvec's
+   * five passes, each averaged over its launches; [10] the solver's own
+   * kernels per iteration; [11] iterations averaged; [12] the FP64 residuals
+   * b - A x, average per call; [13] their calls; [14..15] 0.  The
+   * instrumented iteration graph replaces the plain one (later plain solves
+   * capture it again), and its event nodes add a little time: time solves
+   * without it.  NULL: no profile. */
+  float* profile_ms;
 } vs_solve_opts;
 
 typedef struct vs_solve_info {
@@ -289,7 +300,7 @@ typedef struct vs_solve_info {
 /* Fill opts with defaults: BiCGSTAB, MIXED, tol 1e-6, maxit 2000, automatic
  * inner tolerance, 10 refinements, 4 iterations per graph, no resvec, no
  * transpose, GMRES restart 50, 10 recycled vectors for GMRES-DR, the
- * operator's Gram. */
+ * operator's Gram, no profile. */
 void vs_solve_opts_default(vs_solve_opts* opts);
 
 /* Solve A x = b with the (optional, may be NULL) preconditioner, right

@@ -393,3 +393,38 @@ def test_particles_rejects_shared_objects(api):
     other = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep, ctx=api.Context(0))
     with pytest.raises(VoxScatterError, match="one context"):
         api.solve_particles([op, other], None, [Bd.data_ptr()] * 2, [X.data_ptr()] * 2, [1, 1])
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_solve_profile_inside_the_graph(api, precision):
+    """vs_solve_opts.profile_ms: a BiCGSTAB solve with CUDA events between the
+    launches of its captured iterations gives the same solution bit for bit as
+    the plain solve (the events change no arithmetic), a positive duration for
+    every preconditioner and matvec pass and for the solver kernels, counted
+    over whole graph launches (multiples of iters_per_graph), and the FP64
+    residual per call; a plain solve afterwards captures its own graph again."""
+    import torch
+    p = W.small_hex(m=1.31 + 0.05j, diameter=2.5, nper=4)
+    L, M, N, idx3, Toep, alpha, dV, b, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
+    bd = torch.from_numpy(b.astype(np.complex128)).cuda()
+    xs = []
+    for profile in (False, True, False):
+        xd = torch.zeros_like(bd)
+        torch.cuda.synchronize()
+        info = api.solve_device(op, bd.data_ptr(), xd.data_ptr(), pr, tol=1e-6 if precision == "mixed" else 1e-10,
+                                precision=precision, iters_per_graph=2, profile=profile)
+        op.ctx.synchronize()
+        assert info["flag"] == 0, info
+        xs.append(xd.cpu().numpy())
+        if profile:
+            prof = info["profile"]
+            assert all(prof[k] > 0 for k in api.PROFILE_KEYS), prof
+            assert prof["solver_kernels_per_iter"] > 0
+            assert prof["iterations"] >= 2 and prof["iterations"] % 2 == 0, prof
+            assert prof["iterations"] <= info["iter"] + 1
+            assert prof["fp64_residual"] > 0 and prof["fp64_residual_calls"] >= 1
+            # one pass takes less than the whole solve
+            assert max(prof[k] for k in api.PROFILE_KEYS) < info["time_ms"]
+    assert np.array_equal(xs[0], xs[1]) and np.array_equal(xs[0], xs[2])

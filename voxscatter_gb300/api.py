@@ -442,9 +442,16 @@ def solve(op, b, prec=None, tol=1e-6, maxit=2000, precision="mixed", x0=None, in
     return x, d, rv[:info.n_resvec].copy()
 
 
+PROFILE_KEYS = ("prec_x_fwd", "prec_y_fwd", "prec_gemv", "prec_y_inv", "prec_x_inv",
+                "mv_x_fwd", "mv_y_fwd", "mv_z", "mv_y_inv", "mv_x_inv")
+
+
 def solve_device(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="mixed", inner_tol=0.0,
-                 max_refine=10, iters_per_graph=4, method="bicgstab", restart=50, ritz=10):
-    """vs_solve_device on device buffers (double2, n3 each); returns the info dict."""
+                 max_refine=10, iters_per_graph=4, method="bicgstab", restart=50, ritz=10, profile=False):
+    """vs_solve_device on device buffers (double2, n3 each); returns the info
+    dict.  profile=True (BiCGSTAB) adds "profile": the in-solve durations of
+    vs_solve_opts.profile_ms in ms (each pass, the solver's kernels per
+    iteration, the FP64 residual per call) and the counts they average over."""
     lib = op.ctx._lib
     o = L.vs_solve_opts()
     lib.vs_solve_opts_default(C.byref(o))
@@ -454,11 +461,19 @@ def solve_device(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="m
     o.method = _method(method)
     o.restart = int(restart)
     o.ritz = int(ritz)
+    prof = (C.c_float * 16)() if profile else None
+    if profile:
+        o.profile_ms = C.cast(prof, C.POINTER(C.c_float))
     info = L.vs_solve_info()
     L.check(lib.vs_solve_device(op.h, prec.h if prec is not None else None, C.c_void_p(b_ptr), C.c_void_p(x_ptr),
                                 C.byref(o), C.byref(info)), op.ctx.h)
-    return dict(flag=info.flag, relres=info.relres, iter=info.iter, refinements=info.refinements,
-                time_ms=info.time_ms, launches=info.kernel_launches)
+    out = dict(flag=info.flag, relres=info.relres, iter=info.iter, refinements=info.refinements,
+               time_ms=info.time_ms, launches=info.kernel_launches)
+    if profile:
+        p = list(prof)
+        out["profile"] = dict(zip(PROFILE_KEYS, p[:10]), solver_kernels_per_iter=p[10], iterations=int(p[11]),
+                              fp64_residual=p[12], fp64_residual_calls=int(p[13]))
+    return out
 
 
 def solve_host_ptr(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="mixed", iters_per_graph=4,

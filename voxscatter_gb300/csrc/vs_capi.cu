@@ -284,16 +284,32 @@ void fill_info(const vs::SolveResult& r, vs_solve_info* info) {
   info->kernel_launches = r.launches;
 }
 
+// The 16 floats of vs_solve_opts.profile_ms from a solve's profile.
+void write_profile(const vs::SolveProfile& p, float* out) {
+  for (int i = 0; i < 16; ++i) out[i] = 0.0f;
+  if (p.iters > 0) {
+    // every pass runs twice per iteration
+    for (int i = 0; i < 10; ++i) out[i] = (float)(p.pass_ms[i] / (2.0 * p.iters));
+    out[10] = (float)(p.vec_ms / p.iters);
+  }
+  out[11] = (float)p.iters;
+  if (p.resid_calls > 0) out[12] = (float)(p.resid_ms / p.resid_calls);
+  out[13] = (float)p.resid_calls;
+}
+
 void solve_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, const vs_solve_opts* o,
                 vs_solve_info* info) {
   VS_REQUIRE(info, "NULL argument");
   vs::SolveParams prm = solve_params(op, prec, o);
+  vs::SolveProfile prof;
+  if (o->profile_ms) prm.profile = &prof;
   vs::SolveResult r;
   if (o->method == VS_GMRES) vs::solve_gmres(*op, prec, b, x, prm, r, op->ctx->stream);
   else if (o->method == VS_GMRES_DR) vs::solve_gmres_dr(*op, prec, b, x, prm, r, op->ctx->stream);
   else vs::solve_bicgstab(*op, prec, b, x, prm, r, op->ctx->stream);
   check_prec_status(prec);
   fill_info(r, info);
+  if (o->profile_ms) write_profile(prof, o->profile_ms);
 }
 
 // nrhs right-hand sides: BiCGSTAB runs them as one batch (every launch serves
@@ -317,10 +333,13 @@ void solve_batch_impl(vs_op* op, vs_prec* prec, const double2* b, double2* x, in
     check_prec_status(prec);
     return;
   }
+  vs::SolveProfile prof;
+  if (o->profile_ms) prm.profile = &prof;
   std::vector<vs::SolveResult> res;
   vs::solve_bicgstab_batch(*op, prec, b, x, (int)nrhs, prm, res, op->ctx->stream);
   check_prec_status(prec);
   for (int64_t r = 0; r < nrhs; ++r) fill_info(res[r], infos + r);
+  if (o->profile_ms) write_profile(prof, o->profile_ms);
 }
 
 // S = sum_j (k_hat_j e_hat_j)^2 of the LDR polarisability (getOPERATOR_DDA.m:14-20).
@@ -968,6 +987,7 @@ void vs_solve_opts_default(vs_solve_opts* o) {
   o->ritz = 10;
   o->gram = nullptr;
   o->gram_n = 0;
+  o->profile_ms = nullptr;
 }
 
 

@@ -87,7 +87,27 @@ struct GraphCache {
   ~GraphCache() { reset(); }
 };
 
+// CUDA events of an instrumented iteration graph, destroyed with the work
+// area (after the graphs that record them: declared before them).
+struct EventSet {
+  std::vector<cudaEvent_t> ev;
+  void ensure(size_t n) {
+    while (ev.size() < n) {
+      cudaEvent_t e;
+      VS_CUDA(cudaEventCreate(&e));
+      ev.push_back(e);
+    }
+  }
+  EventSet() = default;
+  EventSet(const EventSet&) = delete;
+  EventSet& operator=(const EventSet&) = delete;
+  ~EventSet() {
+    for (auto e : ev) cudaEventDestroy(e);
+  }
+};
+
 struct KrylovWork {
+  EventSet prof_ev;                      // events of the profiled BiCGSTAB graph
   DevBuf r, rt, p, v_, s, t, ph, sh, x;  // in the inner solver's precision
   DevBuf r64, y64;                       // FP64 residual / matvec output
   DevBuf partials, state, scal, resvec;

@@ -481,11 +481,18 @@ static std::vector<double> read_scal(KrylovWork& w, int nrhs, cudaStream_t st) {
   return v;
 }
 
+// Events recorded by one profiled iteration (kIterMarks per iteration): 0
+// before it, 1 after the direction update, 2..6 after the five passes of the
+// first preconditioner apply, 7..11 after the matvec's five, 12 after the
+// alpha / s / half-step kernels, 13..17 and 18..22 the second apply and
+// matvec, 23 after the omega / x, r kernels.
+constexpr int kIterMarks = 24;
+
 // One BiCGSTAB iteration (two half steps) for all right-hand sides as a fixed
-// launch sequence.
+// launch sequence; mk (kIterMarks events) records the marks above.
 template <typename T>
 static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KState* s, int64_t n, int nrhs,
-                           int mode, cudaStream_t st) {
+                           int mode, cudaStream_t st, cudaEvent_t* mk = nullptr) {
   using C = cplx_t<T>;
   C* r = w.r.as<C>();
   C* rt = w.rt.as<C>();
@@ -499,19 +506,50 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
   const dim3 g(vec_grid(n), nrhs);
   const int* skip = &s->skip;
   const int ss = (int)(sizeof(KState) / sizeof(int));
+  // an external record: a node of the captured graph (a plain record inside
+  // a capture only orders streams)
+  auto mark = [&](int i) {
+    if (mk) VS_CUDA(cudaEventRecordWithFlags(mk[i], st, cudaEventRecordExternal));
+  };
+  // M^-1 u -> o then A o -> y, one event after each pass when profiled
+  auto prec_then_matvec = [&](const C* u, C* o, C* y, int m0) {
+    for (int pass = 0; pass < 5; ++pass) {
+      if (pr) prec_apply_pass<T>(*pr, u, o, nrhs, skip, st, pass, ss);
+      else if (pass == 0) k_copy<T><<<dim3(vec_grid(n * nrhs)), 256, 0, st>>>(o, u, n * nrhs);
+      mark(m0 + pass);
+    }
+    for (int pass = 0; pass < 5; ++pass) {
+      matvec_pass<T>(op, o, y, nrhs, mode, skip, st, pass, ss, rgp(w));
+      mark(m0 + 5 + pass);
+    }
+  };
+  mark(0);
   k_bicg_p<T><<<g, 256, 0, st>>>(p, r, v, n, s);
-  if (pr) prec_apply<T>(*pr, p, ph, nrhs, skip, st, ss);
-  else k_copy<T><<<dim3(vec_grid(n * nrhs)), 256, 0, st>>>(ph, p, n * nrhs);
-  matvec<T>(op, ph, v, nrhs, mode, skip, st, ss, rgp(w));
+  mark(1);
+  prec_then_matvec(p, ph, v, 2);
   k_bicg_alpha<T><<<g, kRedThreads, 0, st>>>(rt, v, n, s);
   k_bicg_s<T><<<g, kRedThreads, 0, st>>>(sv, r, v, n, s);
   k_bicg_xhalf<T><<<g, kRedThreads, 0, st>>>(x, ph, n, s);
-  if (pr) prec_apply<T>(*pr, sv, sh, nrhs, skip, st, ss);
-  else k_copy<T><<<dim3(vec_grid(n * nrhs)), 256, 0, st>>>(sh, sv, n * nrhs);
-  matvec<T>(op, sh, t, nrhs, mode, skip, st, ss, rgp(w));
+  mark(12);
+  prec_then_matvec(sv, sh, t, 13);
   k_bicg_omega<T><<<g, kRedThreads, 0, st>>>(t, sv, n, s);
   k_bicg_xr<T><<<g, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, rt, n, s);
+  mark(23);
   VS_LAUNCH_CHECK();
+}
+
+// Adds the durations between the marks of `iters` profiled iterations.
+static void add_iteration_profile(const cudaEvent_t* ev, int iters, SolveProfile* prof) {
+  auto dt = [&](int it, int a, int b) {
+    float ms = 0;
+    VS_CUDA(cudaEventElapsedTime(&ms, ev[it * kIterMarks + a], ev[it * kIterMarks + b]));
+    return (double)ms;
+  };
+  for (int it = 0; it < iters; ++it) {
+    prof->vec_ms += dt(it, 0, 1) + dt(it, 11, 12) + dt(it, 22, 23);
+    for (int p = 0; p < 10; ++p) prof->pass_ms[p] += dt(it, 1 + p, 2 + p) + dt(it, 12 + p, 13 + p);
+  }
+  prof->iters += iters;
 }
 
 // Kernels in one bicg_iteration: 6 solver kernels, 2 matvecs of 5 passes, and
@@ -528,7 +566,7 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
                                          const std::vector<double>& bnorm, double tol, int maxit,
                                          const std::vector<double>& res_scale, double* resvec_dev, int resvec_cap,
                                          int per_graph, cudaStream_t st, int64_t* launches, int stag_window,
-                                         int mode) {
+                                         int mode, SolveProfile* prof = nullptr) {
   using C = cplx_t<T>;
   std::vector<KState> h(nrhs);
   for (int r = 0; r < nrhs; ++r) {
@@ -575,7 +613,9 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
                                   w.state.p, w.partials.p, op.t1.p, op.t2.p,
                                   (const void*)(uintptr_t)(pr ? pr->id : 0), pr ? pr->t.p : nullptr,
                                   (const void*)(uintptr_t)per_graph, (const void*)(uintptr_t)mode,
-                                  (const void*)(uintptr_t)nrhs, w.rg.g32, w.rg.g64, (const void*)(uintptr_t)w.rg.per};
+                                  (const void*)(uintptr_t)nrhs, w.rg.g32, w.rg.g64, (const void*)(uintptr_t)w.rg.per,
+                                  (const void*)(uintptr_t)(prof ? 1 : 0)};
+  if (prof) w.prof_ev.ensure((size_t)per_graph * kIterMarks);
   if (gc.exec == nullptr || gc.key != key) {
     gc.reset();
     // One launch sequence with every rhs skipped, outside capture: all
@@ -589,7 +629,8 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
     cudaGraph_t graph = nullptr;
     VS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     try {
-      for (int k = 0; k < per_graph; ++k) bicg_iteration<T>(op, pr, w, s, n, nrhs, mode, st);
+      for (int k = 0; k < per_graph; ++k)
+        bicg_iteration<T>(op, pr, w, s, n, nrhs, mode, st, prof ? w.prof_ev.ev.data() + k * kIterMarks : nullptr);
     } catch (...) {
       cudaStreamEndCapture(st, &graph);
       if (graph) cudaGraphDestroy(graph);
@@ -613,8 +654,13 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
     *launches += (int64_t)per_graph * kernels_per_iteration<T>(pr);
     VS_CUDA(cudaMemcpyAsync(cur.data(), s, nrhs * sizeof(KState), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
-    bool all = true;
-    for (int r = 0; r < nrhs; ++r) all = all && cur[r].skip;
+    bool all = true, none = true;
+    for (int r = 0; r < nrhs; ++r) {
+      all = all && cur[r].skip;
+      none = none && !cur[r].skip;
+    }
+    // every iteration of this launch ran for every rhs: a profile sample
+    if (prof && none) add_iteration_profile(w.prof_ev.ev.data(), per_graph, prof);
     if (all) break;
   }
   for (int r = 0; r < nrhs; ++r)
@@ -635,15 +681,28 @@ static std::vector<double> norms64(KrylovWork& w, const double2* u, int64_t n, i
 
 // r64 = b - A x64 (c128 pipeline); returns ||r64|| per rhs.
 static std::vector<double> residuals64(const vs_op& op, KrylovWork& w, const double2* b, const double2* x, double2* r,
-                                       int64_t n, int nrhs, cudaStream_t st, int64_t* launches, int mode) {
+                                       int64_t n, int nrhs, cudaStream_t st, int64_t* launches, int mode,
+                                       SolveProfile* prof = nullptr) {
   std::vector<KState> h(nrhs);
   upload_states(w, h, st);
   double2* y = w.y64.as<double2>();
+  if (prof) {
+    w.prof_ev.ensure(2);
+    VS_CUDA(cudaEventRecord(w.prof_ev.ev[0], st));
+  }
   matvec<double>(op, x, y, nrhs, mode, nullptr, st, 0, rgp(w));
   k_resid64<<<dim3(vec_grid(n), nrhs), kRedThreads, 0, st>>>(b, y, r, n, w.state.as<KState>(), w.scal.as<double>());
   VS_LAUNCH_CHECK();
   *launches += 6;
-  return read_scal(w, nrhs, st);
+  if (prof) VS_CUDA(cudaEventRecord(w.prof_ev.ev[1], st));
+  std::vector<double> out = read_scal(w, nrhs, st);
+  if (prof) {
+    float ms = 0;
+    VS_CUDA(cudaEventElapsedTime(&ms, w.prof_ev.ev[0], w.prof_ev.ev[1]));
+    prof->resid_ms += ms;
+    prof->resid_calls += 1;
+  }
+  return out;
 }
 
 // Single-rhs helpers used by GMRES.
@@ -691,16 +750,16 @@ void solve_bicgstab_batch(vs_op& op, vs_prec* pr, const double2* b, double2* x, 
     w.y64.alloc(n * nrhs * sizeof(double2));
     k_copy<double><<<vec_grid(n * nrhs), 256, 0, st>>>(w.x.as<double2>(), x, n * nrhs);
     if (x0zero) k_copy<double><<<vec_grid(n * nrhs), 256, 0, st>>>(w.r.as<double2>(), b, n * nrhs);
-    else residuals64(op, w, b, x, w.r.as<double2>(), n, nrhs, st, &launches, prm.op_mode);
+    else residuals64(op, w, b, x, w.r.as<double2>(), n, nrhs, st, &launches, prm.op_mode, prm.profile);
     launches += 2;
     std::vector<double> sc(nrhs);
     for (int r = 0; r < nrhs; ++r) sc[r] = 1.0 / bsafe[r];
     std::vector<KState> fs = bicgstab_core<double>(op, pr, w, n, nrhs, bsafe, prm.tol, prm.maxit, sc, rv, cap,
-                                                   prm.per_graph, st, &launches, 0, prm.op_mode);
+                                                   prm.per_graph, st, &launches, 0, prm.op_mode, prm.profile);
     k_copy<double><<<vec_grid(n * nrhs), 256, 0, st>>>(x, w.x.as<double2>(), n * nrhs);
     VS_LAUNCH_CHECK();
     launches += 1;
-    rn = residuals64(op, w, b, x, w.r.as<double2>(), n, nrhs, st, &launches, prm.op_mode);
+    rn = residuals64(op, w, b, x, w.r.as<double2>(), n, nrhs, st, &launches, prm.op_mode, prm.profile);
     for (int r = 0; r < nrhs; ++r) {
       out[r].flag = fs[r].flag;
       out[r].iter = fs[r].iter2 * 0.5;
@@ -722,7 +781,7 @@ void solve_bicgstab_batch(vs_op& op, vs_prec* pr, const double2* b, double2* x, 
       launches += 1;
       rn = bnorm;
     } else {
-      rn = residuals64(op, w, b, x, r64, n, nrhs, st, &launches, prm.op_mode);
+      rn = residuals64(op, w, b, x, r64, n, nrhs, st, &launches, prm.op_mode, prm.profile);
     }
     DevBuf scd;
     scd.alloc(nrhs * sizeof(double));
@@ -767,7 +826,7 @@ void solve_bicgstab_batch(vs_op& op, vs_prec* pr, const double2* b, double2* x, 
       }
       std::vector<KState> fs = bicgstab_core<float>(op, pr, w, n, nrhs, bn, tmin, prm.maxit - used / 2, rscale, rvk,
                                                     capk, prm.per_graph, st, &launches, kStagnationWindow,
-                                                    prm.op_mode);
+                                                    prm.op_mode, prm.profile);
       bool progressed = false;
       for (int r = 0; r < nrhs; ++r) {
         inner2[r] += fs[r].iter2;
@@ -779,7 +838,7 @@ void solve_bicgstab_batch(vs_op& op, vs_prec* pr, const double2* b, double2* x, 
       k_update64<<<dim3(vec_grid(n), nrhs), 256, 0, st>>>(x, w.x.as<float2>(), n, scd.as<double>());
       VS_LAUNCH_CHECK();
       launches += 1;
-      rn = residuals64(op, w, b, x, r64, n, nrhs, st, &launches, prm.op_mode);
+      rn = residuals64(op, w, b, x, r64, n, nrhs, st, &launches, prm.op_mode, prm.profile);
       if (!progressed) break;
     }
     for (int r = 0; r < nrhs; ++r) {

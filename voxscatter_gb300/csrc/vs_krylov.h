@@ -29,7 +29,19 @@ struct GState {
   int skip, flag, nres, resvec_cap;
 };
 
+// Durations inside a BiCGSTAB solve, from CUDA events recorded between the
+// launches of its captured iterations (only graph launches after which every
+// right-hand side was still iterating count), plus the FP64 residuals.
+struct SolveProfile {
+  double pass_ms[10] = {};  // preconditioner passes 0..4, matvec passes 0..4 (sum over iters)
+  double vec_ms = 0;        // the solver's own kernels (sum over iters)
+  int64_t iters = 0;        // iterations summed
+  double resid_ms = 0;      // FP64 residuals b - A x (sum)
+  int64_t resid_calls = 0;
+};
+
 struct SolveParams {
+  SolveProfile* profile = nullptr;  // non-null: record the in-solve durations
   int mode = 0;  // 0 mixed, 1 fp64
   double tol = 1e-6;
   int maxit = 2000;
