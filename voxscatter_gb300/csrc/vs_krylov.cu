@@ -25,6 +25,10 @@
 
 namespace vs {
 
+// The reduction kernels (dots and norms with a grid-wide sum): two CTAs of
+// 256 threads per SM.  Each CTA ends with a fence and one atomic on the
+// right-hand side's counter, and those serialise (eight CTAs per SM made the
+// kernels slower; one CTA of 1024 per SM was no faster).
 constexpr int kRedThreads = 256;
 constexpr int kRedBlocks = 2 * 152;
 
@@ -103,52 +107,86 @@ struct Acc<double> {
   __device__ __forceinline__ double2 value() const { return make_double2(re.hi + re.lo, im.hi + im.lo); }
 };
 
+// ff (float-float) sum of two ff values: TwoSum of the leading parts, the
+// trailing parts and the error added, renormalised (about 48 bits).
+__device__ __forceinline__ void ff_add2(float& hi, float& lo, float bhi, float blo) {
+  const float s = __fadd_rn(hi, bhi);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(bhi, bb));
+  const float t = __fadd_rn(err, __fadd_rn(lo, blo));
+  hi = __fadd_rn(s, t);
+  lo = __fsub_rn(t, __fsub_rn(hi, s));
+}
+
+// Warp sum (xor tree) of one value per lane: float-float on the FP32 pipes
+// (FF, the c64 solver's accumulators, which are float-float already), or
+// double (the FP64 path, which keeps double's exponent range).
+template <bool FF>
+__device__ __forceinline__ double warp_sum(double v) {
+  if constexpr (FF) {
+    float hi = (float)v;
+    float lo = (float)(v - (double)hi);
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, hi, off), ol = __shfl_xor_sync(0xffffffffu, lo, off);
+      ff_add2(hi, lo, oh, ol);
+    }
+    return (double)hi + (double)lo;
+  } else {
+#pragma unroll
+    for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+  }
+}
+
 // Block reduction of NV doubles; returns true in the last CTA to finish, with
-// the grid totals in `tot` (all threads of that CTA).  Partials are summed in
-// CTA order, so the result does not depend on scheduling.
-template <int NV>
+// the grid totals in `tot` (all threads of that CTA).  GB300's FP64 rate is a
+// small fraction of its FP32 rate, and a double tree in which every thread of
+// a large CTA took part cost several microseconds, so: the warp level runs as
+// warp_sum<FF>, warp 0 alone adds the warps' sums and writes the CTA's partial
+// (double), and warp 0 of the last CTA adds the partials in CTA order, so the
+// result does not depend on scheduling.
+template <int NV, bool FF>
 __device__ bool grid_reduce(double (&v)[NV], double* __restrict__ partials, unsigned* __restrict__ counter,
                             double (&tot)[NV]) {
   __shared__ double sm[NV][kRedThreads / 32];
+  __shared__ double stot[NV];
   __shared__ bool s_last;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
-    double x = v[k];
-#pragma unroll
-    for (int off = 16; off; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    const double x = warp_sum<FF>(v[k]);
     if (lane == 0) sm[k][warp] = x;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (warp == 0) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      double x = 0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) x += sm[k][w];
-      partials[blockIdx.x * NV + k] = x;
+      const double x = warp_sum<FF>(lane < nw ? sm[k][lane] : 0.0);
+      if (lane == 0) partials[blockIdx.x * NV + k] = x;
     }
-    __threadfence();
-    const unsigned t = atomicAdd(counter, 1u);
-    s_last = (t == gridDim.x - 1);
+    if (lane == 0) {
+      __threadfence();
+      const unsigned t = atomicAdd(counter, 1u);
+      s_last = (t == gridDim.x - 1);
+    }
   }
   __syncthreads();
   if (!s_last) return false;
   __threadfence();
+  if (warp == 0) {
 #pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    double x = 0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) x += ((volatile double*)partials)[b * NV + k];
+    for (int k = 0; k < NV; ++k) {
+      double x = 0;
+      for (int b = lane; b < (int)gridDim.x; b += 32) x += ((volatile double*)partials)[b * NV + k];
 #pragma unroll
-    for (int off = 16; off; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
-    if (lane == 0) sm[k][warp] = x;
+      for (int off = 16; off; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+      if (lane == 0) stot[k] = x;
+    }
   }
   __syncthreads();
 #pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    double x = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) x += sm[k][w];
-    tot[k] = x;
-  }
+  for (int k = 0; k < NV; ++k) tot[k] = stot[k];
   if (threadIdx.x == 0) *counter = 0;
   return true;
 }
@@ -161,6 +199,10 @@ __device__ __forceinline__ bool cz(double2 a) { return a.x == 0.0 && a.y == 0.0;
 __device__ __forceinline__ bool cfinite(double2 a) { return isfinite(a.x) && isfinite(a.y); }
 
 #define GRID_LOOP(i, n) for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+// The same loop unrolled four ways: with the vectors declared __restrict__,
+// the loads of four elements issue before the first store, so a thread's
+// handful of elements costs about two memory latencies instead of one each.
+#define GRID_LOOP4(i, n) _Pragma("unroll 4") GRID_LOOP(i, n)
 
 // All BiCGSTAB kernels below run on a batch of right-hand sides sharing one
 // operator: blockIdx.y is the right-hand side, its vectors start at
@@ -169,15 +211,16 @@ __device__ __forceinline__ bool cfinite(double2 a) { return isfinite(a.x) && isf
 
 // rho = rt^H r ; beta = (rho/rho_prev)(alpha/omega)
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_bicg_rho(const cplx_t<T>* rt, const cplx_t<T>* r, int64_t n,
+__global__ void __launch_bounds__(kRedThreads) k_bicg_rho(const cplx_t<T>* __restrict__ rt,
+                                                         const cplx_t<T>* __restrict__ r, int64_t n,
                                                          KState* states) {
   KState* s = states + blockIdx.y;
   if (s->skip) return;
   rt += blockIdx.y * n; r += blockIdx.y * n;
   Acc<T> a;
-  GRID_LOOP(i, n) a.dot(rt[i], r[i]);
+  GRID_LOOP4(i, n) a.dot(rt[i], r[i]);
   double v[2] = {a.value().x, a.value().y}, t[2];
-  if (grid_reduce<2>(v, s->partials, &s->counter, t) && threadIdx.x == 0) {
+  if (grid_reduce<2, std::is_same<T, float>::value>(v, s->partials, &s->counter, t) && threadIdx.x == 0) {
     const double2 rho = make_double2(t[0], t[1]);
     if (cz(rho) || !cfinite(rho)) {
       s->flag = cfinite(rho) ? 4 : 5;
@@ -191,30 +234,32 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_rho(const cplx_t<T>* rt, c
 
 // p = r (first iteration) or r + beta (p - omega v)
 template <typename T>
-__global__ void k_bicg_p(cplx_t<T>* p, const cplx_t<T>* r, const cplx_t<T>* v, int64_t n, const KState* states) {
+__global__ void k_bicg_p(cplx_t<T>* __restrict__ p, const cplx_t<T>* __restrict__ r,
+                         const cplx_t<T>* __restrict__ v, int64_t n, const KState* states) {
   using C = cplx_t<T>;
   const KState* s = states + blockIdx.y;
   if (s->skip) return;
   p += blockIdx.y * n; r += blockIdx.y * n; v += blockIdx.y * n;
   if (s->iter2 == 0) {
-    GRID_LOOP(i, n) p[i] = r[i];
+    GRID_LOOP4(i, n) p[i] = r[i];
     return;
   }
   const C beta = ccast<C>(s->beta), om = ccast<C>(s->omega);
-  GRID_LOOP(i, n) p[i] = cfma(beta, csub(p[i], cmul(om, v[i])), r[i]);
+  GRID_LOOP4(i, n) p[i] = cfma(beta, csub(p[i], cmul(om, v[i])), r[i]);
 }
 
 // alpha = rho / (rt^H v)
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_bicg_alpha(const cplx_t<T>* rt, const cplx_t<T>* v, int64_t n,
+__global__ void __launch_bounds__(kRedThreads) k_bicg_alpha(const cplx_t<T>* __restrict__ rt,
+                                                           const cplx_t<T>* __restrict__ v, int64_t n,
                                                            KState* states) {
   KState* s = states + blockIdx.y;
   if (s->skip) return;
   rt += blockIdx.y * n; v += blockIdx.y * n;
   Acc<T> a;
-  GRID_LOOP(i, n) a.dot(rt[i], v[i]);
+  GRID_LOOP4(i, n) a.dot(rt[i], v[i]);
   double w[2] = {a.value().x, a.value().y}, t[2];
-  if (grid_reduce<2>(w, s->partials, &s->counter, t) && threadIdx.x == 0) {
+  if (grid_reduce<2, std::is_same<T, float>::value>(w, s->partials, &s->counter, t) && threadIdx.x == 0) {
     const double2 d = make_double2(t[0], t[1]);
     if (cz(d) || !cfinite(d)) {
       s->flag = cfinite(d) ? 4 : 5;
@@ -227,21 +272,21 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_alpha(const cplx_t<T>* rt,
 
 // s = r - alpha v ; ||s|| ; half-step convergence test
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_bicg_s(cplx_t<T>* sv, const cplx_t<T>* r, const cplx_t<T>* v,
-                                                       int64_t n, KState* states) {
+__global__ void __launch_bounds__(kRedThreads) k_bicg_s(cplx_t<T>* __restrict__ sv, const cplx_t<T>* __restrict__ r,
+                                                       const cplx_t<T>* __restrict__ v, int64_t n, KState* states) {
   using C = cplx_t<T>;
   KState* s = states + blockIdx.y;
   if (s->skip) return;
   sv += blockIdx.y * n; r += blockIdx.y * n; v += blockIdx.y * n;
   const C al = ccast<C>(s->alpha);
   Acc<T> a;
-  GRID_LOOP(i, n) {
+  GRID_LOOP4(i, n) {
     const C x = csub(r[i], cmul(al, v[i]));
     sv[i] = x;
     a.norm2(x);
   }
   double w[1] = {a.value().x}, t[1];
-  if (grid_reduce<1>(w, s->partials, &s->counter, t) && threadIdx.x == 0) {
+  if (grid_reduce<1, std::is_same<T, float>::value>(w, s->partials, &s->counter, t) && threadIdx.x == 0) {
     const double res = sqrt(t[0]);
     const int k = s->iter2 + 1;
     if (k < s->resvec_cap) s->resvec[k] = res * s->res_scale;
@@ -261,7 +306,8 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_s(cplx_t<T>* sv, const cpl
 
 // x += alpha ph when the half step converged (runs regardless of skip).
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_bicg_xhalf(cplx_t<T>* x, const cplx_t<T>* ph, int64_t n,
+__global__ void __launch_bounds__(kRedThreads) k_bicg_xhalf(cplx_t<T>* __restrict__ x,
+                                                           const cplx_t<T>* __restrict__ ph, int64_t n,
                                                            KState* states) {
   using C = cplx_t<T>;
   KState* s = states + blockIdx.y;
@@ -272,7 +318,7 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_xhalf(cplx_t<T>* x, const 
   if (!s_go) return;
   x += blockIdx.y * n; ph += blockIdx.y * n;
   const C al = ccast<C>(s->alpha);
-  GRID_LOOP(i, n) x[i] = cfma(al, ph[i], x[i]);
+  GRID_LOOP4(i, n) x[i] = cfma(al, ph[i], x[i]);
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -287,18 +333,19 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_xhalf(cplx_t<T>* x, const 
 
 // omega = (t^H s)/(t^H t)
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_bicg_omega(const cplx_t<T>* t, const cplx_t<T>* sv, int64_t n,
+__global__ void __launch_bounds__(kRedThreads) k_bicg_omega(const cplx_t<T>* __restrict__ t,
+                                                           const cplx_t<T>* __restrict__ sv, int64_t n,
                                                            KState* states) {
   KState* s = states + blockIdx.y;
   if (s->skip) return;
   t += blockIdx.y * n; sv += blockIdx.y * n;
   Acc<T> a, b;
-  GRID_LOOP(i, n) {
+  GRID_LOOP4(i, n) {
     a.dot(t[i], sv[i]);
     b.norm2(t[i]);
   }
   double w[3] = {a.value().x, a.value().y, b.value().x}, tt[3];
-  if (grid_reduce<3>(w, s->partials, &s->counter, tt) && threadIdx.x == 0) {
+  if (grid_reduce<3, std::is_same<T, float>::value>(w, s->partials, &s->counter, tt) && threadIdx.x == 0) {
     const double2 ts = make_double2(tt[0], tt[1]);
     const double t2 = tt[2];
     if (!(t2 > 0) || !cfinite(ts)) {
@@ -320,9 +367,12 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_omega(const cplx_t<T>* t, 
 // when the iteration continues, the next rho = rt^H r with its breakdown test
 // and beta = (rho_new/rho)(alpha/omega) (the first rho comes from k_bicg_rho)
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* x, cplx_t<T>* r, const cplx_t<T>* ph,
-                                                        const cplx_t<T>* sh, const cplx_t<T>* sv, const cplx_t<T>* t,
-                                                        const cplx_t<T>* rt, int64_t n, KState* states) {
+__global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* __restrict__ x, cplx_t<T>* __restrict__ r,
+                                                        const cplx_t<T>* __restrict__ ph,
+                                                        const cplx_t<T>* __restrict__ sh,
+                                                        const cplx_t<T>* __restrict__ sv,
+                                                        const cplx_t<T>* __restrict__ t,
+                                                        const cplx_t<T>* __restrict__ rt, int64_t n, KState* states) {
   using C = cplx_t<T>;
   KState* s = states + blockIdx.y;
   if (s->skip) return;
@@ -330,7 +380,7 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* x, cplx_t<T>
   x += o; r += o; ph += o; sh += o; sv += o; t += o; rt += o;
   const C al = ccast<C>(s->alpha), om = ccast<C>(s->omega);
   Acc<T> a, d;
-  GRID_LOOP(i, n) {
+  GRID_LOOP4(i, n) {
     x[i] = cfma(om, sh[i], cfma(al, ph[i], x[i]));
     const C ri = csub(sv[i], cmul(om, t[i]));
     r[i] = ri;
@@ -338,7 +388,7 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* x, cplx_t<T>
     d.dot(rt[i], ri);
   }
   double w[3] = {a.value().x, d.value().x, d.value().y}, tt[3];
-  if (grid_reduce<3>(w, s->partials, &s->counter, tt) && threadIdx.x == 0) {
+  if (grid_reduce<3, std::is_same<T, float>::value>(w, s->partials, &s->counter, tt) && threadIdx.x == 0) {
     const double res = sqrt(tt[0]);
     const int k = s->iter2 + 2;
     if (k < s->resvec_cap) s->resvec[k] = res * s->res_scale;
@@ -384,7 +434,7 @@ __global__ void __launch_bounds__(kRedThreads) k_norm(const cplx_t<T>* u, int64_
   Acc<T> a;
   GRID_LOOP(i, n) a.norm2(u[i]);
   double w[1] = {a.value().x}, t[1];
-  if (grid_reduce<1>(w, s->partials, &s->counter, t) && threadIdx.x == 0) out[blockIdx.y] = sqrt(t[0]);
+  if (grid_reduce<1, std::is_same<T, float>::value>(w, s->partials, &s->counter, t) && threadIdx.x == 0) out[blockIdx.y] = sqrt(t[0]);
 }
 
 template <typename T>
@@ -409,7 +459,7 @@ __global__ void __launch_bounds__(kRedThreads) k_resid64(const double2* b, const
     a.norm2(v);
   }
   double w[1] = {a.value().x}, t[1];
-  if (grid_reduce<1>(w, s->partials, &s->counter, t) && threadIdx.x == 0) out[blockIdx.y] = sqrt(t[0]);
+  if (grid_reduce<1, false>(w, s->partials, &s->counter, t) && threadIdx.x == 0) out[blockIdx.y] = sqrt(t[0]);
 }
 
 // r32 = r64 * sc[rhs]
@@ -433,7 +483,12 @@ __global__ void k_update64(double2* x, const float2* d, int64_t n, const double*
 // refinement takes over.
 constexpr int kStagnationWindow = 8;
 
-static int vec_grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), kRedBlocks)); }
+// CTAs of the element-wise kernels (256 threads, no grid-wide sum)
+static int vec_grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), 8 * 152)); }
+// CTAs of the reduction kernels (kRedThreads threads; at most kRedBlocks partials)
+static int red_grid(int64_t n) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, kRedThreads), kRedBlocks));
+}
 
 // The Gram per right-hand side of the current solve, or nullptr (the operator's).
 static const RhsGram* rgp(const KrylovWork& w) { return w.rg.empty() ? nullptr : &w.rg; }
@@ -503,7 +558,7 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
   C* ph = w.ph.as<C>();
   C* sh = w.sh.as<C>();
   C* x = w.x.as<C>();
-  const dim3 g(vec_grid(n), nrhs);
+  const dim3 g(vec_grid(n), nrhs), gr(red_grid(n), nrhs);
   const int* skip = &s->skip;
   const int ss = (int)(sizeof(KState) / sizeof(int));
   // an external record: a node of the captured graph (a plain record inside
@@ -527,13 +582,13 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
   k_bicg_p<T><<<g, 256, 0, st>>>(p, r, v, n, s);
   mark(1);
   prec_then_matvec(p, ph, v, 2);
-  k_bicg_alpha<T><<<g, kRedThreads, 0, st>>>(rt, v, n, s);
-  k_bicg_s<T><<<g, kRedThreads, 0, st>>>(sv, r, v, n, s);
-  k_bicg_xhalf<T><<<g, kRedThreads, 0, st>>>(x, ph, n, s);
+  k_bicg_alpha<T><<<gr, kRedThreads, 0, st>>>(rt, v, n, s);
+  k_bicg_s<T><<<gr, kRedThreads, 0, st>>>(sv, r, v, n, s);
+  k_bicg_xhalf<T><<<gr, kRedThreads, 0, st>>>(x, ph, n, s);
   mark(12);
   prec_then_matvec(sv, sh, t, 13);
-  k_bicg_omega<T><<<g, kRedThreads, 0, st>>>(t, sv, n, s);
-  k_bicg_xr<T><<<g, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, rt, n, s);
+  k_bicg_omega<T><<<gr, kRedThreads, 0, st>>>(t, sv, n, s);
+  k_bicg_xr<T><<<gr, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, rt, n, s);
   mark(23);
   VS_LAUNCH_CHECK();
 }
@@ -585,7 +640,7 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
   upload_states(w, h, st);
   const int gn = vec_grid(n * nrhs);
   k_copy<T><<<gn, 256, 0, st>>>(w.rt.as<C>(), w.r.as<C>(), n * nrhs);
-  k_norm<T><<<dim3(vec_grid(n), nrhs), kRedThreads, 0, st>>>(w.r.as<C>(), n, s, w.scal.as<double>());
+  k_norm<T><<<dim3(red_grid(n), nrhs), kRedThreads, 0, st>>>(w.r.as<C>(), n, s, w.scal.as<double>());
   *launches += 2;
   const std::vector<double> r0 = read_scal(w, nrhs, st);
   bool any_active = false;
@@ -644,7 +699,7 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
   }
   upload_states(w, h, st);
   // rho of the initial residual; later ones come out of k_bicg_xr
-  k_bicg_rho<T><<<dim3(vec_grid(n), nrhs), kRedThreads, 0, st>>>(w.rt.as<C>(), w.r.as<C>(), n, s);
+  k_bicg_rho<T><<<dim3(red_grid(n), nrhs), kRedThreads, 0, st>>>(w.rt.as<C>(), w.r.as<C>(), n, s);
   VS_LAUNCH_CHECK();
   *launches += 1;
   std::vector<KState> cur(nrhs);
@@ -673,7 +728,7 @@ static std::vector<double> norms64(KrylovWork& w, const double2* u, int64_t n, i
                                    int64_t* launches) {
   std::vector<KState> h(nrhs);
   upload_states(w, h, st);
-  k_norm<double><<<dim3(vec_grid(n), nrhs), kRedThreads, 0, st>>>(u, n, w.state.as<KState>(), w.scal.as<double>());
+  k_norm<double><<<dim3(red_grid(n), nrhs), kRedThreads, 0, st>>>(u, n, w.state.as<KState>(), w.scal.as<double>());
   VS_LAUNCH_CHECK();
   *launches += 1;
   return read_scal(w, nrhs, st);
@@ -691,7 +746,7 @@ static std::vector<double> residuals64(const vs_op& op, KrylovWork& w, const dou
     VS_CUDA(cudaEventRecord(w.prof_ev.ev[0], st));
   }
   matvec<double>(op, x, y, nrhs, mode, nullptr, st, 0, rgp(w));
-  k_resid64<<<dim3(vec_grid(n), nrhs), kRedThreads, 0, st>>>(b, y, r, n, w.state.as<KState>(), w.scal.as<double>());
+  k_resid64<<<dim3(red_grid(n), nrhs), kRedThreads, 0, st>>>(b, y, r, n, w.state.as<KState>(), w.scal.as<double>());
   VS_LAUNCH_CHECK();
   *launches += 6;
   if (prof) VS_CUDA(cudaEventRecord(w.prof_ev.ev[1], st));
@@ -911,7 +966,7 @@ void enqueue_norms(std::vector<PartState>& ps, const std::vector<const double2*>
     KrylovWork& w = p.job->op->kw;
     p.h.assign(p.job->nrhs, KState{});
     upload_states(w, p.h, st);
-    k_norm<double><<<dim3(vec_grid(p.n), p.job->nrhs), kRedThreads, 0, st>>>(u[i], p.n, w.state.as<KState>(),
+    k_norm<double><<<dim3(red_grid(p.n), p.job->nrhs), kRedThreads, 0, st>>>(u[i], p.n, w.state.as<KState>(),
                                                                              w.scal.as<double>());
   }
   VS_LAUNCH_CHECK();
@@ -927,7 +982,7 @@ void enqueue_residuals(std::vector<PartState>& ps, const std::vector<double2*>& 
     p.h.assign(p.job->nrhs, KState{});
     upload_states(w, p.h, st);
     matvec<double>(op, xs[i], w.y64.as<double2>(), p.job->nrhs, mode, nullptr, st, 0, rgp(w));
-    k_resid64<<<dim3(vec_grid(p.n), p.job->nrhs), kRedThreads, 0, st>>>(p.job->b, w.y64.as<double2>(), rs[i], p.n,
+    k_resid64<<<dim3(red_grid(p.n), p.job->nrhs), kRedThreads, 0, st>>>(p.job->b, w.y64.as<double2>(), rs[i], p.n,
                                                                        w.state.as<KState>(), w.scal.as<double>());
   }
   VS_LAUNCH_CHECK();
@@ -967,7 +1022,7 @@ void bicgstab_lockstep(vs_ctx* ctx, std::vector<PartState>& ps, double tol, int 
     }
     upload_states(w, p.h, st);
     k_copy<T><<<vec_grid(p.n * nrhs), 256, 0, st>>>(w.rt.as<C>(), w.r.as<C>(), p.n * nrhs);
-    k_norm<T><<<dim3(vec_grid(p.n), nrhs), kRedThreads, 0, st>>>(w.r.as<C>(), p.n, w.state.as<KState>(),
+    k_norm<T><<<dim3(red_grid(p.n), nrhs), kRedThreads, 0, st>>>(w.r.as<C>(), p.n, w.state.as<KState>(),
                                                                  w.scal.as<double>());
     *launches += 2;
   }
@@ -1066,7 +1121,7 @@ void bicgstab_lockstep(vs_ctx* ctx, std::vector<PartState>& ps, double tol, int 
   for (auto& p : ps) {
     KrylovWork& w = p.job->op->kw;
     upload_states(w, p.h, st);
-    k_bicg_rho<T><<<dim3(vec_grid(p.n), p.job->nrhs), kRedThreads, 0, st>>>(w.rt.as<C>(), w.r.as<C>(), p.n,
+    k_bicg_rho<T><<<dim3(red_grid(p.n), p.job->nrhs), kRedThreads, 0, st>>>(w.rt.as<C>(), w.r.as<C>(), p.n,
                                                                            w.state.as<KState>());
     *launches += 1;
   }
@@ -1376,7 +1431,7 @@ __global__ void __launch_bounds__(kRedThreads) k_gm_norm(const cplx_t<T>* w, int
   Acc<T> a;
   GRID_LOOP(i, n) a.norm2(w[i]);
   double v[1] = {a.value().x}, t[1];
-  if (grid_reduce<1>(v, partials, counter, t) && threadIdx.x == 0) *Hk1 = make_double2(sqrt(t[0]), 0.0);
+  if (grid_reduce<1, std::is_same<T, float>::value>(v, partials, counter, t) && threadIdx.x == 0) *Hk1 = make_double2(sqrt(t[0]), 0.0);
 }
 
 // V_{k+1} = w / H(k+1,k)
@@ -1545,7 +1600,7 @@ static int gmres_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t
       minv(tmp, V);
       *launches += 6;
     }
-    k_norm<T><<<g, kRedThreads, 0, st>>>(V, n, ks, w.scal.as<double>());
+    k_norm<T><<<red_grid(n), kRedThreads, 0, st>>>(V, n, ks, w.scal.as<double>());
     double beta = 0;
     VS_CUDA(cudaMemcpyAsync(&beta, w.scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
@@ -1590,7 +1645,7 @@ static int gmres_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t
         k_gm_axpy<T><<<g, 256, (k + 1) * sizeof(C), st>>>(V, wv, n, k + 1, hp, gs);
       }
       // partial sums and counter of the shared reduction state (device addresses)
-      k_gm_norm<T><<<g, kRedThreads, 0, st>>>(wv, n, w.partials.as<double>(), &ks->counter, Hcol + k + 1, gs);
+      k_gm_norm<T><<<red_grid(n), kRedThreads, 0, st>>>(wv, n, w.partials.as<double>(), &ks->counter, Hcol + k + 1, gs);
       k_gm_scale<T><<<g, 256, 0, st>>>(wv, V + (int64_t)(k + 1) * n, n, Hcol + k + 1, gs);
       k_gm_givens<<<1, 32, 0, st>>>(gs, H, w.gcs.as<double>(), w.gsn.as<double2>(), w.gg.as<double2>());
       VS_LAUNCH_CHECK();
@@ -1860,7 +1915,7 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
     *launches += pr ? prec_launches<T>(*pr) : 1;
   };
   auto norm_dev = [&](const C* u) {
-    k_norm<T><<<g, kRedThreads, 0, st>>>(u, n, ks, w.scal.as<double>());
+    k_norm<T><<<red_grid(n), kRedThreads, 0, st>>>(u, n, ks, w.scal.as<double>());
     double v = 0;
     VS_CUDA(cudaMemcpyAsync(&v, w.scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
@@ -1927,7 +1982,7 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
         k_gm_axpy<T><<<g, 256, nb * sizeof(C), st>>>(Cm, wv, n, nb, hp, gs);
       }
       double2* Hcol = col + kc;
-      k_gm_norm<T><<<g, kRedThreads, 0, st>>>(wv, n, w.partials.as<double>(), &ks->counter, Hcol + k + 1, gs);
+      k_gm_norm<T><<<red_grid(n), kRedThreads, 0, st>>>(wv, n, w.partials.as<double>(), &ks->counter, Hcol + k + 1, gs);
       k_gm_scale<T><<<g, 256, 0, st>>>(wv, V + (int64_t)(k + 1) * n, n, Hcol + k + 1, gs);
       k_dr_copycol<<<1, 64, 0, st>>>(gs, Hcol, H + (int64_t)k * (m + 1), k + 2);
       k_gm_givens<<<1, 32, 0, st>>>(gs, H, w.gcs.as<double>(), w.gsn.as<double2>(), w.gg.as<double2>());

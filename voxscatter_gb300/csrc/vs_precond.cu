@@ -721,14 +721,19 @@ __device__ __forceinline__ uint64_t l2_evict_first_policy() {
 }
 
 constexpr int kGemvPolls = 1 << 20;  // default bound of every streamed-GEMV wait
+// Each poll may suspend the waiting thread in hardware for up to this many
+// nanoseconds (it resumes when the phase completes): waiting warps then stop
+// taking issue slots from the warps that compute, and a wait still gives up
+// after at most kGemvPolls polls (about a second).
+constexpr uint32_t kGemvSuspendNs = 1000;
 
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int polls = kGemvPolls) {
   for (int i = 0; i < polls; ++i) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
         : "=r"(ok)
-        : "r"(bar), "r"(parity)
+        : "r"(bar), "r"(parity), "r"(kGemvSuspendNs)
         : "memory");
     if (ok) return true;
   }
