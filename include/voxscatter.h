@@ -285,6 +285,13 @@ typedef struct vs_solve_opts {
    * capture it again), and its event nodes add a little time: time solves
    * without it.  NULL: no profile. */
   float* profile_ms;
+  /* VS_BICGSTAB: 0 (default) folds the vector steps of an iteration into the
+   * x passes (p and s formed in the preconditioner's forward x pass, the
+   * inner products of v and t added in the matvec's inverse x pass, one-warp
+   * kernels for alpha, ||s|| and omega) wherever both x passes run the
+   * two-level kernels; 1 keeps them as separate kernels.  The two agree to
+   * the rounding of the inner products' summation order. */
+  int unfused;
 } vs_solve_opts;
 
 typedef struct vs_solve_info {
@@ -300,7 +307,7 @@ typedef struct vs_solve_info {
 /* Fill opts with defaults: BiCGSTAB, MIXED, tol 1e-6, maxit 2000, automatic
  * inner tolerance, 10 refinements, 4 iterations per graph, no resvec, no
  * transpose, GMRES restart 50, 10 recycled vectors for GMRES-DR, the
- * operator's Gram, no profile. */
+ * operator's Gram, no profile, folded vector steps. */
 void vs_solve_opts_default(vs_solve_opts* opts);
 
 /* Solve A x = b with the (optional, may be NULL) preconditioner, right

@@ -428,3 +428,42 @@ def test_solve_profile_inside_the_graph(api, precision):
             # one pass takes less than the whole solve
             assert max(prof[k] for k in api.PROFILE_KEYS) < info["time_ms"]
     assert np.array_equal(xs[0], xs[1]) and np.array_equal(xs[0], xs[2])
+
+
+@pytest.mark.parametrize("precision,tol", [("mixed", 1e-6), ("fp64", 1e-10)])
+@pytest.mark.parametrize("nrhs", [1, 3])
+def test_folded_vector_steps_match_separate_kernels(api, precision, tol, nrhs):
+    """BiCGSTAB with its vector steps folded into the x passes (p and s formed
+    in the preconditioner's forward x pass, rt^H v and t^H s, t^H t added in the
+    matvec's inverse x pass, one-warp scalar steps) against the separate
+    kernels, on the 27 x 23 x 7 hex plate with both x passes forced to the
+    two-level kernels (the folded form needs them): both converge with the
+    oracle's FP64 MVP confirming ||b - A x|| <= tol ||b||, the solutions agree
+    to the tolerance, the iteration counts to a half step, and the launch
+    counts show which form ran (25 against 26 kernels per iteration)."""
+    p = W.config1()
+    L, M, N, idx3, Toep, alpha, dV, b, Aor = _system(p)
+    op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
+    pr = api.Preconditioner(op, shift=1 / alpha, d=dV)
+    for prec in ("c64", "c128"):
+        op.set_shape(prec, x_reg=1)
+        pr.set_shape(prec, x_reg=1, fuse_xy=0)
+    rng = np.random.default_rng(7)
+    B = np.stack([b] + [b * np.exp(1j * rng.uniform(0, 2 * np.pi)) + 0.3 * (rng.normal(size=b.size) +
+                                                                              1j * rng.normal(size=b.size))
+                        for _ in range(nrhs - 1)])
+    out = {}
+    for fold in (True, False):
+        X, infos = api.solve_batch(op, B, pr, tol=tol, precision=precision, fold=fold)
+        for r in range(nrhs):
+            assert infos[r]["flag"] == 0, (fold, r, infos[r])
+            true_rel = np.linalg.norm(B[r] - Aor(X[r])) / np.linalg.norm(B[r])
+            assert true_rel <= tol * 1.01, (fold, r, true_rel)
+        out[fold] = (X, infos)
+    Xf, inf_f = out[True]
+    Xs, inf_s = out[False]
+    for r in range(nrhs):
+        assert np.linalg.norm(Xf[r] - Xs[r]) / np.linalg.norm(Xs[r]) < 20 * tol, r
+        assert abs(inf_f[r]["iter"] - inf_s[r]["iter"]) <= 0.5, (r, inf_f[r]["iter"], inf_s[r]["iter"])
+    # per graph launch: 25 kernels folded, 26 separate (4 iterations per graph)
+    assert inf_f[0]["launches"] < inf_s[0]["launches"], (inf_f[0]["launches"], inf_s[0]["launches"])

@@ -64,7 +64,8 @@ class vs_solve_opts(C.Structure):
     _fields_ = [("method", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("maxit", C.c_int),
                 ("inner_tol", C.c_double), ("max_refine", C.c_int), ("iters_per_graph", C.c_int),
                 ("resvec", _pd), ("resvec_cap", _i64), ("transpose", C.c_int), ("restart", C.c_int),
-                ("ritz", C.c_int), ("gram", _pd), ("gram_n", _i64), ("profile_ms", C.POINTER(C.c_float))]
+                ("ritz", C.c_int), ("gram", _pd), ("gram_n", _i64), ("profile_ms", C.POINTER(C.c_float)),
+                ("unfused", C.c_int)]
 
 
 class vs_solve_info(C.Structure):

@@ -447,11 +447,14 @@ PROFILE_KEYS = ("prec_x_fwd", "prec_y_fwd", "prec_gemv", "prec_y_inv", "prec_x_i
 
 
 def solve_device(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="mixed", inner_tol=0.0,
-                 max_refine=10, iters_per_graph=4, method="bicgstab", restart=50, ritz=10, profile=False):
+                 max_refine=10, iters_per_graph=4, method="bicgstab", restart=50, ritz=10, profile=False,
+                 fold=True):
     """vs_solve_device on device buffers (double2, n3 each); returns the info
     dict.  profile=True (BiCGSTAB) adds "profile": the in-solve durations of
     vs_solve_opts.profile_ms in ms (each pass, the solver's kernels per
-    iteration, the FP64 residual per call) and the counts they average over."""
+    iteration, the FP64 residual per call) and the counts they average over.
+    fold=False keeps BiCGSTAB's vector steps as separate kernels
+    (vs_solve_opts.unfused)."""
     lib = op.ctx._lib
     o = L.vs_solve_opts()
     lib.vs_solve_opts_default(C.byref(o))
@@ -461,6 +464,7 @@ def solve_device(op, b_ptr, x_ptr, prec=None, tol=1e-6, maxit=2000, precision="m
     o.method = _method(method)
     o.restart = int(restart)
     o.ritz = int(ritz)
+    o.unfused = 0 if fold else 1
     prof = (C.c_float * 16)() if profile else None
     if profile:
         o.profile_ms = C.cast(prof, C.POINTER(C.c_float))
@@ -683,11 +687,12 @@ def cext_grad(op, prec, Einc, eps, ko, d, kvec, Eo, tol=1e-6, maxit=2000, precis
 
 
 def solve_batch(op, B, prec=None, tol=1e-6, maxit=2000, precision="mixed", method="bicgstab", restart=50,
-                iters_per_graph=4, ritz=10, gram=None):
+                iters_per_graph=4, ritz=10, gram=None, fold=True):
     """Solve A_r x_r = b_r for every row b_r of B (nrhs x n3) as one batch; returns
     (X, list of info dicts).  ``gram``: None (every A_r is the operator) or the
     Gram of each right-hand side (nrhs scalars or nrhs (L, M, N) grids), e.g.
-    1/alpha_LDR of each incident direction and polarisation."""
+    1/alpha_LDR of each incident direction and polarisation.  fold=False keeps
+    BiCGSTAB's vector steps as separate kernels (vs_solve_opts.unfused)."""
     lib = op.ctx._lib
     B = np.ascontiguousarray(np.asarray(B, dtype=np.complex128))
     nrhs = B.shape[0]
@@ -697,6 +702,7 @@ def solve_batch(op, B, prec=None, tol=1e-6, maxit=2000, precision="mixed", metho
     o.restart = int(restart)
     o.ritz = int(ritz)
     o.iters_per_graph = int(iters_per_graph)
+    o.unfused = 0 if fold else 1
     if gram is not None:
         g, o.gram_n = _gram_array(gram, nrhs, op.LMN)
         o.gram = L.dptr(g)

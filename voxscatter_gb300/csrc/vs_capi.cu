@@ -272,6 +272,8 @@ vs::SolveParams solve_params(vs_op* op, vs_prec* prec, const vs_solve_opts* o) {
              "gram_n must be 1 or L*M*N when a Gram per right-hand side is given");
   prm.gram_host = reinterpret_cast<const double2*>(o->gram);
   prm.gram_n = o->gram ? o->gram_n : 0;
+  VS_REQUIRE(o->unfused == 0 || o->unfused == 1, "unfused must be 0 or 1");
+  prm.fold_steps = o->unfused == 0;
   return prm;
 }
 
@@ -988,6 +990,7 @@ void vs_solve_opts_default(vs_solve_opts* o) {
   o->gram = nullptr;
   o->gram_n = 0;
   o->profile_ms = nullptr;
+  o->unfused = 0;
 }
 
 

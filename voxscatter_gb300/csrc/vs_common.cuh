@@ -9,6 +9,7 @@
 #include <stdexcept>
 #include <mutex>
 #include <set>
+#include <map>
 #include <utility>
 #include "../../include/voxscatter.h"
 
@@ -88,25 +89,37 @@ inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 // host thread, so it is raised straight to the hardware maximum and never
 // lowered: launches from concurrent threads with different tile sizes all fit.
 inline void set_kernel_smem(const void* kernel, size_t bytes) {
-  constexpr size_t kMax = 227 * 1024;
+  constexpr size_t kMax = 227 * 1024, kDefault = 48 * 1024;
   if (bytes > kMax)
     throw Error(VS_ERR_UNSUPPORTED, "kernel tile needs " + std::to_string(bytes) + " bytes of shared memory (> 227 KB)");
-  if (bytes <= 48 * 1024) return;
   int dev = 0;
   VS_CUDA(cudaGetDevice(&dev));
   static std::mutex mu;
-  static std::set<std::pair<const void*, int>> done;
+  // per kernel and device: its static shared memory, and whether the
+  // dynamic limit has been raised to what the static part leaves
+  static std::map<std::pair<const void*, int>, std::pair<size_t, bool>> seen;
   std::lock_guard<std::mutex> lock(mu);
-  if (done.count({kernel, dev})) return;
-  // the per-CTA limit covers static and dynamic shared memory together
-  cudaFuncAttributes fa;
-  VS_CUDA(cudaFuncGetAttributes(&fa, kernel));
-  const size_t cap = kMax - fa.sharedSizeBytes;
+  auto it = seen.find({kernel, dev});
+  if (it == seen.end()) {
+    cudaFuncAttributes fa;
+    VS_CUDA(cudaFuncGetAttributes(&fa, kernel));
+    it = seen.emplace(std::make_pair(kernel, dev), std::make_pair((size_t)fa.sharedSizeBytes, false)).first;
+  }
+  const size_t stat = it->second.first;
+  // without the attribute, static and dynamic shared memory together must
+  // stay within the default 48 KB
+  if (bytes + stat <= kDefault || it->second.second) {
+    if (bytes + stat > kMax)
+      throw Error(VS_ERR_UNSUPPORTED, "kernel tile needs " + std::to_string(bytes) + " bytes of shared memory (> " +
+                                          std::to_string(kMax - stat) + " available)");
+    return;
+  }
+  const size_t cap = kMax - stat;
   if (bytes > cap)
     throw Error(VS_ERR_UNSUPPORTED, "kernel tile needs " + std::to_string(bytes) + " bytes of shared memory (> " +
                                         std::to_string(cap) + " available)");
   VS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
-  done.insert({kernel, dev});
+  it->second.second = true;
 }
 
 }  // namespace vs

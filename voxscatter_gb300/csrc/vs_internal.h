@@ -111,6 +111,7 @@ struct KrylovWork {
   DevBuf r, rt, p, v_, s, t, ph, sh, x;  // in the inner solver's precision
   DevBuf r64, y64;                       // FP64 residual / matvec output
   DevBuf partials, state, scal, resvec;
+  DevBuf xpart;                          // per-CTA partial sums of the folded BiCGSTAB steps
   GraphCache graph32, graph64;           // BiCGSTAB iteration graphs (c64 / c128)
   // GMRES(m): Krylov basis, Hessenberg (column-major, m+1 rows), rotations,
   // right-hand side g, solution y, pass coefficients, partial dots, state,
@@ -206,11 +207,20 @@ struct vs_prec {
 
 namespace vs {
 
+template <typename T>
+struct XFuse;  // a BiCGSTAB step folded into a two-level x pass (vs_pipeline.cuh)
+
+// CTAs of a two-level x pass of length P over nlines lines (0: P has no
+// two-level kernel); the solver sizes the folded steps' partial sums by it.
+int x2_ctas(int P, int nlines);
+
 // Launchers (vs_matvec.cu)
 // rg: optional Gram of each right-hand side (nullptr or empty: the operator's).
+// fz: optional solver step folded into the inverse x pass (pass 4).
 template <typename T>
 void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
-                 cudaStream_t st, int pass, int skip_stride = 0, const RhsGram* rg = nullptr);
+                 cudaStream_t st, int pass, int skip_stride = 0, const RhsGram* rg = nullptr,
+                 const XFuse<T>* fz = nullptr);
 template <typename T>
 void matvec_scratch(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, cplx_t<T>* t1,
                     cplx_t<T>* t2, cudaStream_t st);
@@ -275,9 +285,10 @@ void invert_blocks_tc(float2* mats, int n, int64_t nmat, double scale, int* stat
 // tensor-core kernel (n <= 256 unless lu == LU_CUDA) or the blocked CUDA-core
 // kernel.
 void invert_blocks_device(float2* mats, int n, int64_t nmat, int lu, double scale, int* status, cudaStream_t st);
+// fz: optional solver step folded into the forward x pass (pass 0).
 template <typename T>
 void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
-                     cudaStream_t st, int pass, int skip_stride = 0);
+                     cudaStream_t st, int pass, int skip_stride = 0, const XFuse<T>* fz = nullptr);
 // kernel launches of one preconditioner apply (3 with fused x/y planes, else 5)
 template <typename T>
 int prec_launches(const vs_prec& pr);

@@ -17,6 +17,8 @@
 // x += ||r|| d in FP64 until ||r||/||b|| <= tol.
 #include "vs_krylov.h"
 #include "vs_dense.h"
+#include "vs_reduce.cuh"
+#include "vs_pipeline.cuh"
 
 #include <chrono>
 #include <cmath>
@@ -31,113 +33,6 @@ namespace vs {
 // kernels slower; one CTA of 1024 per SM was no faster).
 constexpr int kRedThreads = 256;
 constexpr int kRedBlocks = 2 * 152;
-
-// FP64 double-double accumulation (TwoSum / TwoProd by fma) for the c128 path.
-struct DD {
-  double hi, lo;
-};
-__device__ __forceinline__ DD dd_add(DD a, double b) {
-  const double s = a.hi + b;
-  const double bb = s - a.hi;
-  const double err = (a.hi - (s - bb)) + (b - bb);
-  return DD{s, a.lo + err};
-}
-__device__ __forceinline__ DD dd_add(DD a, DD b) {
-  DD r = dd_add(a, b.hi);
-  r.lo += b.lo;
-  return r;
-}
-__device__ __forceinline__ DD dd_fma(DD a, double x, double y) {
-  const double p = x * y;
-  const double e = fma(x, y, -p);
-  DD r = dd_add(a, p);
-  r.lo += e;
-  return r;
-}
-
-// Accumulators.  c64 inputs: every product of two floats is formed exactly as
-// a float pair (p = a*b rounded, e = fma(a, b, -p)) and added into a
-// float-float sum by TwoSum (Knuth), about 48 bits of significand for the
-// few elements a thread visits; the pair is widened to double once, and the
-// grid-wide sums are taken in double.  This keeps compensated inner products
-// without a double-precision FMA per element.
-__device__ __forceinline__ void ff_add(float& hi, float& lo, float b) {
-  const float s = __fadd_rn(hi, b);
-  const float bb = __fsub_rn(s, hi);
-  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-  hi = s;
-  lo = __fadd_rn(lo, err);
-}
-__device__ __forceinline__ void ff_fma(float& hi, float& lo, float a, float b) {
-  const float pr = __fmul_rn(a, b);
-  const float e = __fmaf_rn(a, b, -pr);
-  ff_add(hi, lo, pr);
-  lo = __fadd_rn(lo, e);
-}
-template <typename T>
-struct Acc {
-  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-  __device__ __forceinline__ void dot(cplx_t<T> u, cplx_t<T> v) {  // += conj(u) v
-    ff_fma(rh, rl, u.x, v.x);
-    ff_fma(rh, rl, u.y, v.y);
-    ff_fma(ih, il, u.x, v.y);
-    ff_fma(ih, il, -u.y, v.x);
-  }
-  __device__ __forceinline__ void norm2(cplx_t<T> u) {
-    ff_fma(rh, rl, u.x, u.x);
-    ff_fma(rh, rl, u.y, u.y);
-  }
-  __device__ __forceinline__ double2 value() const {
-    return make_double2((double)rh + (double)rl, (double)ih + (double)il);
-  }
-};
-template <>
-struct Acc<double> {
-  DD re{0, 0}, im{0, 0};
-  __device__ __forceinline__ void dot(double2 u, double2 v) {
-    re = dd_fma(re, u.x, v.x);
-    re = dd_fma(re, u.y, v.y);
-    im = dd_fma(im, u.x, v.y);
-    im = dd_fma(im, -u.y, v.x);
-  }
-  __device__ __forceinline__ void norm2(double2 u) {
-    re = dd_fma(re, u.x, u.x);
-    re = dd_fma(re, u.y, u.y);
-  }
-  __device__ __forceinline__ double2 value() const { return make_double2(re.hi + re.lo, im.hi + im.lo); }
-};
-
-// ff (float-float) sum of two ff values: TwoSum of the leading parts, the
-// trailing parts and the error added, renormalised (about 48 bits).
-__device__ __forceinline__ void ff_add2(float& hi, float& lo, float bhi, float blo) {
-  const float s = __fadd_rn(hi, bhi);
-  const float bb = __fsub_rn(s, hi);
-  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(bhi, bb));
-  const float t = __fadd_rn(err, __fadd_rn(lo, blo));
-  hi = __fadd_rn(s, t);
-  lo = __fsub_rn(t, __fsub_rn(hi, s));
-}
-
-// Warp sum (xor tree) of one value per lane: float-float on the FP32 pipes
-// (FF, the c64 solver's accumulators, which are float-float already), or
-// double (the FP64 path, which keeps double's exponent range).
-template <bool FF>
-__device__ __forceinline__ double warp_sum(double v) {
-  if constexpr (FF) {
-    float hi = (float)v;
-    float lo = (float)(v - (double)hi);
-#pragma unroll
-    for (int off = 16; off; off >>= 1) {
-      const float oh = __shfl_xor_sync(0xffffffffu, hi, off), ol = __shfl_xor_sync(0xffffffffu, lo, off);
-      ff_add2(hi, lo, oh, ol);
-    }
-    return (double)hi + (double)lo;
-  } else {
-#pragma unroll
-    for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    return v;
-  }
-}
 
 // Block reduction of NV doubles; returns true in the last CTA to finish, with
 // the grid totals in `tot` (all threads of that CTA).  GB300's FP64 rate is a
@@ -209,6 +104,87 @@ __device__ __forceinline__ bool cfinite(double2 a) { return isfinite(a.x) && isf
 // rhs * n, and its scalars live in states[rhs] (each state carries its own
 // reduction partials and counter).
 
+// The scalar steps of BiCGSTAB, from the grid totals (one thread):
+// alpha = rho / (rt^H v) with its breakdown test;
+__device__ __forceinline__ void finish_alpha(KState* s, const double (&t)[2]) {
+  const double2 d = make_double2(t[0], t[1]);
+  if (cz(d) || !cfinite(d)) {
+    s->flag = cfinite(d) ? 4 : 5;
+    s->skip = 1;
+    return;
+  }
+  s->alpha = cdiv(s->rho, d);
+}
+// ||s|| (t = ||s||^2) and the half-step convergence test;
+__device__ __forceinline__ void finish_s(KState* s, const double (&t)[1]) {
+  const double res = sqrt(t[0]);
+  const int k = s->iter2 + 1;
+  if (k < s->resvec_cap) s->resvec[k] = res * s->res_scale;
+  s->nres = k + 1;
+  s->res = res;
+  if (!isfinite(res)) {
+    s->flag = 5;
+    s->skip = 1;
+  } else if (res <= s->tol_abs) {
+    s->half_pending = 1;
+    s->flag = 0;
+    s->iter2 = k;
+    s->skip = 1;
+  }
+}
+// omega = (t^H s)/(t^H t) (tt = t^H s, t^H t) with its breakdown tests.
+__device__ __forceinline__ void finish_omega(KState* s, const double (&tt)[3]) {
+  const double2 ts = make_double2(tt[0], tt[1]);
+  const double t2 = tt[2];
+  if (!(t2 > 0) || !cfinite(ts)) {
+    s->flag = (t2 == 0) ? 4 : 5;
+    s->skip = 1;
+    return;
+  }
+  const double2 om = make_double2(ts.x / t2, ts.y / t2);
+  if (cz(om)) {
+    s->flag = 4;
+    s->skip = 1;
+    return;
+  }
+  s->omega = om;
+}
+
+// Folded steps (vs_pipeline.cuh XFuse): a two-level x pass left nb per-CTA
+// partial sums (NV each) of right-hand side blockIdx.x at part + blockIdx.x *
+// pstride; one warp adds them in CTA order and takes the scalar step.
+template <int NV>
+__device__ __forceinline__ void sum_cta_partials(const double* part, int nb, double (&tot)[NV]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = 0;
+    for (int b = lane; b < nb; b += 32) x += part[b * NV + k];
+    tot[k] = warp_sum<false>(x);
+  }
+}
+__global__ void __launch_bounds__(32) k_fin_alpha(KState* states, const double* part, int64_t pstride, int nb) {
+  KState* s = states + blockIdx.x;
+  if (s->skip) return;
+  double t[2];
+  sum_cta_partials<2>(part + blockIdx.x * pstride, nb, t);
+  if (threadIdx.x == 0) finish_alpha(s, t);
+}
+__global__ void __launch_bounds__(32) k_fin_s(KState* states, const double* part, int64_t pstride, int nb) {
+  KState* s = states + blockIdx.x;
+  if (s->skip) return;
+  double t[1];
+  sum_cta_partials<1>(part + blockIdx.x * pstride, nb, t);
+  if (threadIdx.x == 0) finish_s(s, t);
+}
+__global__ void __launch_bounds__(32) k_fin_omega(KState* states, const double* part, int64_t pstride, int nb) {
+  KState* s = states + blockIdx.x;
+  if (s->skip) return;
+  double t[3];
+  sum_cta_partials<3>(part + blockIdx.x * pstride, nb, t);
+  if (threadIdx.x == 0) finish_omega(s, t);
+}
+
 // rho = rt^H r ; beta = (rho/rho_prev)(alpha/omega)
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) k_bicg_rho(const cplx_t<T>* __restrict__ rt,
@@ -259,15 +235,8 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_alpha(const cplx_t<T>* __r
   Acc<T> a;
   GRID_LOOP4(i, n) a.dot(rt[i], v[i]);
   double w[2] = {a.value().x, a.value().y}, t[2];
-  if (grid_reduce<2, std::is_same<T, float>::value>(w, s->partials, &s->counter, t) && threadIdx.x == 0) {
-    const double2 d = make_double2(t[0], t[1]);
-    if (cz(d) || !cfinite(d)) {
-      s->flag = cfinite(d) ? 4 : 5;
-      s->skip = 1;
-      return;
-    }
-    s->alpha = cdiv(s->rho, d);
-  }
+  if (grid_reduce<2, std::is_same<T, float>::value>(w, s->partials, &s->counter, t) && threadIdx.x == 0)
+    finish_alpha(s, t);
 }
 
 // s = r - alpha v ; ||s|| ; half-step convergence test
@@ -286,22 +255,8 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_s(cplx_t<T>* __restrict__ 
     a.norm2(x);
   }
   double w[1] = {a.value().x}, t[1];
-  if (grid_reduce<1, std::is_same<T, float>::value>(w, s->partials, &s->counter, t) && threadIdx.x == 0) {
-    const double res = sqrt(t[0]);
-    const int k = s->iter2 + 1;
-    if (k < s->resvec_cap) s->resvec[k] = res * s->res_scale;
-    s->nres = k + 1;
-    s->res = res;
-    if (!isfinite(res)) {
-      s->flag = 5;
-      s->skip = 1;
-    } else if (res <= s->tol_abs) {
-      s->half_pending = 1;
-      s->flag = 0;
-      s->iter2 = k;
-      s->skip = 1;
-    }
-  }
+  if (grid_reduce<1, std::is_same<T, float>::value>(w, s->partials, &s->counter, t) && threadIdx.x == 0)
+    finish_s(s, t);
 }
 
 // x += alpha ph when the half step converged (runs regardless of skip).
@@ -345,22 +300,8 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_omega(const cplx_t<T>* __r
     b.norm2(t[i]);
   }
   double w[3] = {a.value().x, a.value().y, b.value().x}, tt[3];
-  if (grid_reduce<3, std::is_same<T, float>::value>(w, s->partials, &s->counter, tt) && threadIdx.x == 0) {
-    const double2 ts = make_double2(tt[0], tt[1]);
-    const double t2 = tt[2];
-    if (!(t2 > 0) || !cfinite(ts)) {
-      s->flag = (t2 == 0) ? 4 : 5;
-      s->skip = 1;
-      return;
-    }
-    const double2 om = make_double2(ts.x / t2, ts.y / t2);
-    if (cz(om)) {
-      s->flag = 4;
-      s->skip = 1;
-      return;
-    }
-    s->omega = om;
-  }
+  if (grid_reduce<3, std::is_same<T, float>::value>(w, s->partials, &s->counter, tt) && threadIdx.x == 0)
+    finish_omega(s, tt);
 }
 
 // x += alpha ph + omega sh ; r = s - omega t ; ||r|| ; full-step test ; and,
@@ -540,14 +481,40 @@ static std::vector<double> read_scal(KrylovWork& w, int nrhs, cudaStream_t st) {
 // before it, 1 after the direction update, 2..6 after the five passes of the
 // first preconditioner apply, 7..11 after the matvec's five, 12 after the
 // alpha / s / half-step kernels, 13..17 and 18..22 the second apply and
-// matvec, 23 after the omega / x, r kernels.
-constexpr int kIterMarks = 24;
+// matvec, 23 after the omega / x, r kernels; with folded steps, 24 after the
+// ||s|| step and the half-step update (between 13 and 14).
+constexpr int kIterMarks = 25;
+
+// BiCGSTAB's vector steps folded into the x passes (XFuse): the
+// preconditioner's forward x pass forms p (first apply) and s with ||s||^2
+// (second apply), the matvec's inverse x pass adds rt^H v (first) and t^H s,
+// t^H t (second); the partial sums of nb_mv / nb_pr CTAs per right-hand side
+// go to part (pstride doubles each), and one-warp kernels take the scalar
+// steps.  Four streaming vector kernels of the iteration are gone.
+struct FoldPlan {
+  int nb_mv = 0, nb_pr = 0;
+  int64_t pstride = 0;
+  double* part = nullptr;
+};
+
+// Whether both x passes of this precision run the two-level kernel (the one
+// with the folded steps).
+template <typename T>
+static bool can_fold(const vs_op& op, const vs_prec* pr) {
+  if (!pr) return false;
+  const int pi = std::is_same<T, float>::value ? 0 : 1;
+  const PassShape& sp = pr->shape[pi];
+  const PassShape& so = op.shape[pi];
+  if (sp.x_reg != 1 || sp.fuse_xy == 1 || so.x_reg < 1) return false;
+  const int nl = op.M * op.N * 3;
+  return x2_ctas(pr->L, nl) > 0 && x2_ctas(op.P, nl) > 0 && pr->L == op.L && pr->M == op.M && pr->N == op.N;
+}
 
 // One BiCGSTAB iteration (two half steps) for all right-hand sides as a fixed
 // launch sequence; mk (kIterMarks events) records the marks above.
 template <typename T>
 static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KState* s, int64_t n, int nrhs,
-                           int mode, cudaStream_t st, cudaEvent_t* mk = nullptr) {
+                           int mode, cudaStream_t st, cudaEvent_t* mk = nullptr, const FoldPlan* fold = nullptr) {
   using C = cplx_t<T>;
   C* r = w.r.as<C>();
   C* rt = w.rt.as<C>();
@@ -578,6 +545,61 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
       mark(m0 + 5 + pass);
     }
   };
+  if (fold) {
+    XFuse<T> f{};
+    f.sbase = reinterpret_cast<const char*>(s);
+    f.sstride = (int64_t)sizeof(KState);
+    f.part = fold->part;
+    f.pstride = fold->pstride;
+    XFuse<T> fp = f, fsv = f, fd = f, fo = f;
+    fp.kind = XF_GATHER_P;
+    fp.off_a = (int)offsetof(KState, beta);
+    fp.off_b = (int)offsetof(KState, omega);
+    fp.off_iter = (int)offsetof(KState, iter2);
+    fp.u = r; fp.v = v; fp.w = p;
+    fsv.kind = XF_GATHER_S;
+    fsv.off_a = (int)offsetof(KState, alpha);
+    fsv.u = r; fsv.v = v; fsv.w = sv;
+    fd.kind = XF_SCATTER_DOT;
+    fd.u = rt;
+    fo.kind = XF_SCATTER_OMEGA;
+    fo.u = sv;
+    mark(0);
+    mark(1);
+    // p = r + beta (p - omega v) in the first apply's forward x pass
+    for (int pass = 0; pass < 5; ++pass) {
+      prec_apply_pass<T>(*pr, p, ph, nrhs, skip, st, pass, ss, pass == 0 ? &fp : nullptr);
+      mark(2 + pass);
+    }
+    // rt^H v in the matvec's inverse x pass; alpha
+    for (int pass = 0; pass < 5; ++pass) {
+      matvec_pass<T>(op, ph, v, nrhs, mode, skip, st, pass, ss, rgp(w), pass == 4 ? &fd : nullptr);
+      mark(7 + pass);
+    }
+    k_fin_alpha<<<nrhs, 32, 0, st>>>(s, fold->part, fold->pstride, fold->nb_mv);
+    mark(12);
+    // s = r - alpha v and ||s||^2 in the second apply's forward x pass; the
+    // half-step test, then the rest of the apply
+    prec_apply_pass<T>(*pr, sv, sh, nrhs, skip, st, 0, ss, &fsv);
+    mark(13);
+    k_fin_s<<<nrhs, 32, 0, st>>>(s, fold->part, fold->pstride, fold->nb_pr);
+    k_bicg_xhalf<T><<<gr, kRedThreads, 0, st>>>(x, ph, n, s);
+    mark(24);
+    for (int pass = 1; pass < 5; ++pass) {
+      prec_apply_pass<T>(*pr, sv, sh, nrhs, skip, st, pass, ss);
+      mark(13 + pass);
+    }
+    // t^H s, t^H t in the matvec's inverse x pass; omega
+    for (int pass = 0; pass < 5; ++pass) {
+      matvec_pass<T>(op, sh, t, nrhs, mode, skip, st, pass, ss, rgp(w), pass == 4 ? &fo : nullptr);
+      mark(18 + pass);
+    }
+    k_fin_omega<<<nrhs, 32, 0, st>>>(s, fold->part, fold->pstride, fold->nb_mv);
+    k_bicg_xr<T><<<gr, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, rt, n, s);
+    mark(23);
+    VS_LAUNCH_CHECK();
+    return;
+  }
   mark(0);
   k_bicg_p<T><<<g, 256, 0, st>>>(p, r, v, n, s);
   mark(1);
@@ -594,23 +616,28 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
 }
 
 // Adds the durations between the marks of `iters` profiled iterations.
-static void add_iteration_profile(const cudaEvent_t* ev, int iters, SolveProfile* prof) {
+static void add_iteration_profile(const cudaEvent_t* ev, int iters, SolveProfile* prof, bool folded) {
   auto dt = [&](int it, int a, int b) {
     float ms = 0;
     VS_CUDA(cudaEventElapsedTime(&ms, ev[it * kIterMarks + a], ev[it * kIterMarks + b]));
     return (double)ms;
   };
   for (int it = 0; it < iters; ++it) {
-    prof->vec_ms += dt(it, 0, 1) + dt(it, 11, 12) + dt(it, 22, 23);
-    for (int p = 0; p < 10; ++p) prof->pass_ms[p] += dt(it, 1 + p, 2 + p) + dt(it, 12 + p, 13 + p);
+    prof->vec_ms += dt(it, 0, 1) + dt(it, 11, 12) + dt(it, 22, 23) + (folded ? dt(it, 13, 24) : 0.0);
+    for (int p = 0; p < 10; ++p)
+      prof->pass_ms[p] += dt(it, 1 + p, 2 + p) + ((folded && p == 1) ? dt(it, 24, 14) : dt(it, 12 + p, 13 + p));
   }
   prof->iters += iters;
 }
 
 // Kernels in one bicg_iteration: 6 solver kernels, 2 matvecs of 5 passes, and
-// 2 preconditioner applies (or 2 copies without preconditioner).
+// 2 preconditioner applies (or 2 copies without preconditioner); with folded
+// steps 5 solver kernels (the three one-warp scalar steps, x after a
+// converged half step, x and r) and 20 passes.
 template <typename T>
-static int kernels_per_iteration(const vs_prec* pr) { return 6 + 10 + (pr ? 2 * prec_launches<T>(*pr) : 2); }
+static int kernels_per_iteration(const vs_prec* pr, bool folded = false) {
+  return folded ? 25 : 6 + 10 + (pr ? 2 * prec_launches<T>(*pr) : 2);
+}
 
 // BiCGSTAB on w.x (initial guesses already there) with initial residuals in
 // w.r, for nrhs right-hand sides.  The absolute tolerance of rhs r is
@@ -621,7 +648,7 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
                                          const std::vector<double>& bnorm, double tol, int maxit,
                                          const std::vector<double>& res_scale, double* resvec_dev, int resvec_cap,
                                          int per_graph, cudaStream_t st, int64_t* launches, int stag_window,
-                                         int mode, SolveProfile* prof = nullptr) {
+                                         int mode, SolveProfile* prof = nullptr, bool fold_steps = false) {
   using C = cplx_t<T>;
   std::vector<KState> h(nrhs);
   for (int r = 0; r < nrhs; ++r) {
@@ -664,12 +691,25 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
   // batch size and the graph length (scalars live in the device states), so
   // it is captured once and reused by later solves on this operator.
   GraphCache& gc = std::is_same<T, float>::value ? w.graph32 : w.graph64;
+  FoldPlan plan;
+  const FoldPlan* fold = nullptr;
+  if (fold_steps && can_fold<T>(op, pr)) {
+    const int nl = op.M * op.N * 3;
+    plan.nb_mv = x2_ctas(op.P, nl);
+    plan.nb_pr = x2_ctas(pr->L, nl);
+    plan.pstride = 3 * (int64_t)std::max(plan.nb_mv, plan.nb_pr);
+    const size_t need = (size_t)nrhs * plan.pstride * sizeof(double);
+    if (w.xpart.bytes < need) w.xpart.alloc(need);
+    plan.part = w.xpart.as<double>();
+    fold = &plan;
+  }
   std::vector<const void*> key = {w.r.p, w.rt.p, w.p.p, w.v_.p, w.s.p, w.t.p, w.ph.p, w.sh.p, w.x.p,
                                   w.state.p, w.partials.p, op.t1.p, op.t2.p,
                                   (const void*)(uintptr_t)(pr ? pr->id : 0), pr ? pr->t.p : nullptr,
                                   (const void*)(uintptr_t)per_graph, (const void*)(uintptr_t)mode,
                                   (const void*)(uintptr_t)nrhs, w.rg.g32, w.rg.g64, (const void*)(uintptr_t)w.rg.per,
-                                  (const void*)(uintptr_t)(prof ? 1 : 0)};
+                                  (const void*)(uintptr_t)(prof ? 1 : 0), (const void*)(uintptr_t)(fold ? 1 : 0),
+                                  fold ? w.xpart.p : nullptr};
   if (prof) w.prof_ev.ensure((size_t)per_graph * kIterMarks);
   if (gc.exec == nullptr || gc.key != key) {
     gc.reset();
@@ -679,13 +719,14 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
     std::vector<KState> idle = h;
     for (auto& k : idle) k.skip = 1;
     upload_states(w, idle, st);
-    bicg_iteration<T>(op, pr, w, s, n, nrhs, mode, st);
-    *launches += kernels_per_iteration<T>(pr);
+    bicg_iteration<T>(op, pr, w, s, n, nrhs, mode, st, nullptr, fold);
+    *launches += kernels_per_iteration<T>(pr, fold != nullptr);
     cudaGraph_t graph = nullptr;
     VS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     try {
       for (int k = 0; k < per_graph; ++k)
-        bicg_iteration<T>(op, pr, w, s, n, nrhs, mode, st, prof ? w.prof_ev.ev.data() + k * kIterMarks : nullptr);
+        bicg_iteration<T>(op, pr, w, s, n, nrhs, mode, st, prof ? w.prof_ev.ev.data() + k * kIterMarks : nullptr,
+                          fold);
     } catch (...) {
       cudaStreamEndCapture(st, &graph);
       if (graph) cudaGraphDestroy(graph);
@@ -706,7 +747,7 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
   const int max_launch = (maxit + per_graph - 1) / per_graph + 1;
   for (int it = 0; it < max_launch; ++it) {
     VS_CUDA(cudaGraphLaunch(gc.exec, st));
-    *launches += (int64_t)per_graph * kernels_per_iteration<T>(pr);
+    *launches += (int64_t)per_graph * kernels_per_iteration<T>(pr, fold != nullptr);
     VS_CUDA(cudaMemcpyAsync(cur.data(), s, nrhs * sizeof(KState), cudaMemcpyDeviceToHost, st));
     VS_CUDA(cudaStreamSynchronize(st));
     bool all = true, none = true;
@@ -715,7 +756,7 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
       none = none && !cur[r].skip;
     }
     // every iteration of this launch ran for every rhs: a profile sample
-    if (prof && none) add_iteration_profile(w.prof_ev.ev.data(), per_graph, prof);
+    if (prof && none) add_iteration_profile(w.prof_ev.ev.data(), per_graph, prof, fold != nullptr);
     if (all) break;
   }
   for (int r = 0; r < nrhs; ++r)
@@ -810,7 +851,8 @@ void solve_bicgstab_batch(vs_op& op, vs_prec* pr, const double2* b, double2* x, 
     std::vector<double> sc(nrhs);
     for (int r = 0; r < nrhs; ++r) sc[r] = 1.0 / bsafe[r];
     std::vector<KState> fs = bicgstab_core<double>(op, pr, w, n, nrhs, bsafe, prm.tol, prm.maxit, sc, rv, cap,
-                                                   prm.per_graph, st, &launches, 0, prm.op_mode, prm.profile);
+                                                   prm.per_graph, st, &launches, 0, prm.op_mode, prm.profile,
+                                                   prm.fold_steps);
     k_copy<double><<<vec_grid(n * nrhs), 256, 0, st>>>(x, w.x.as<double2>(), n * nrhs);
     VS_LAUNCH_CHECK();
     launches += 1;
@@ -881,7 +923,7 @@ void solve_bicgstab_batch(vs_op& op, vs_prec* pr, const double2* b, double2* x, 
       }
       std::vector<KState> fs = bicgstab_core<float>(op, pr, w, n, nrhs, bn, tmin, prm.maxit - used / 2, rscale, rvk,
                                                     capk, prm.per_graph, st, &launches, kStagnationWindow,
-                                                    prm.op_mode, prm.profile);
+                                                    prm.op_mode, prm.profile, prm.fold_steps);
       bool progressed = false;
       for (int r = 0; r < nrhs; ++r) {
         inner2[r] += fs[r].iter2;

@@ -42,6 +42,7 @@ struct SolveProfile {
 
 struct SolveParams {
   SolveProfile* profile = nullptr;  // non-null: record the in-solve durations
+  bool fold_steps = true;           // BiCGSTAB: fold the vector steps into the x passes where possible
   int mode = 0;  // 0 mixed, 1 fp64
   double tol = 1e-6;
   int maxit = 2000;

@@ -416,10 +416,14 @@ static void launch_z(const vs_op& op, const PipeArgs<T>& a, int nrhs, cudaStream
 
 template <typename T>
 void matvec_pass(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
-                 cudaStream_t st, int pass, int skip_stride, const RhsGram* rg) {
+                 cudaStream_t st, int pass, int skip_stride, const RhsGram* rg, const XFuse<T>* fz) {
   using C = cplx_t<T>;
   VS_REQUIRE(mode >= VS_NOTRANSP && mode <= VS_CONJTRANSP, "mode must be VS_NOTRANSP, VS_TRANSP or VS_CONJTRANSP");
-  const PipeArgs<T> a = pipe_args<T>(op, x, y, skip, skip_stride, rg);
+  PipeArgs<T> a = pipe_args<T>(op, x, y, skip, skip_stride, rg);
+  if (fz && pass == 4) {
+    VS_REQUIRE(a.two_level >= 1 && x2_ctas(op.P, op.M * op.N * 3) > 0, "folded solver step needs the two-level x pass");
+    a.fz = *fz;
+  }
   switch (pass) {
     case 0: launch_x_pass<T>(a, false, mode, nrhs, st); break;
     case 1: launch_strided_pass<T, false>(y_pass_args<T>(op, a, false), op.N * 3, nrhs, st); break;
@@ -530,9 +534,9 @@ template void matvec_scratch<double>(const vs_op&, const double2*, double2*, int
                                      cudaStream_t);
 
 template void matvec_pass<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t, int, int,
-                                 const RhsGram*);
+                                 const RhsGram*, const XFuse<float>*);
 template void matvec_pass<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t, int, int,
-                                  const RhsGram*);
+                                  const RhsGram*, const XFuse<double>*);
 template void matvec<float>(const vs_op&, const float2*, float2*, int, int, const int*, cudaStream_t, int,
                             const RhsGram*);
 template void matvec<double>(const vs_op&, const double2*, double2*, int, int, const int*, cudaStream_t, int,

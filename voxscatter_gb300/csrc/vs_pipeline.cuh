@@ -15,6 +15,38 @@ struct DiagArg {
   __device__ __forceinline__ C at(int pos) const { return v ? v[pos] : s; }
 };
 
+// BiCGSTAB vector steps folded into an x pass (kind XF_NONE: none): the
+// gather of the preconditioner's forward x pass forms the vector it
+// transforms (XF_GATHER_P: p = r + beta (p - omega v), or p = r on the first
+// iteration; XF_GATHER_S: s = r - alpha v, with ||s||^2) and writes it back,
+// and the scatter of the matvec's inverse x pass adds the inner products of
+// the vector it writes (XF_SCATTER_DOT: rt^H v; XF_SCATTER_OMEGA: t^H s and
+// t^H t).  Scalars of right-hand side r are read at sbase + r * sstride +
+// offset (bytes); each CTA writes its NV partial sums to part + r * pstride +
+// blockIdx.x * NV, which the solver adds up afterwards.
+enum XFuseKind { XF_NONE = 0, XF_GATHER_P = 1, XF_GATHER_S = 2, XF_SCATTER_DOT = 3, XF_SCATTER_OMEGA = 4 };
+
+template <typename T>
+struct XFuse {
+  using C = cplx_t<T>;
+  int kind;
+  const char* sbase;
+  int64_t sstride;
+  int off_a, off_b, off_iter;  // XF_GATHER_P: beta, omega, iteration counter; XF_GATHER_S: alpha
+  const C* u;                  // r (gathers), rt (XF_SCATTER_DOT), s (XF_SCATTER_OMEGA)
+  const C* v;                  // v (gathers)
+  C* w;                        // p (XF_GATHER_P, read and written), s (XF_GATHER_S, written)
+  double* part;
+  int64_t pstride;
+  __device__ __forceinline__ C scalar(int rhs, int off) const {
+    const double2 d = *reinterpret_cast<const double2*>(sbase + rhs * sstride + off);
+    C c;
+    c.x = (decltype(c.x))d.x;
+    c.y = (decltype(c.y))d.y;
+    return c;
+  }
+};
+
 template <typename T>
 struct PipeArgs {
   using C = cplx_t<T>;
@@ -45,6 +77,7 @@ struct PipeArgs {
   const C* grhs;
   int64_t grhs_per;
   DiagArg<C> mr;
+  XFuse<T> fz;  // folded solver step of the two-level x passes (kind XF_NONE: none)
 };
 
 // Diagonal coefficient of the XI epilogue at unknown `pos` of right-hand side

@@ -1266,7 +1266,7 @@ void pack_sym_blocks(vs_prec& pr, cudaStream_t st) {
 
 template <typename T>
 void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
-                     cudaStream_t st, int pass, int skip_stride) {
+                     cudaStream_t st, int pass, int skip_stride, const XFuse<T>* fz) {
   using C = cplx_t<T>;
   const int L = pr.L, M = pr.M, N = pr.N;
   const C* inv = std::is_same<T, float>::value ? (const C*)pr.inv32.p : (const C*)pr.inv64.p;
@@ -1293,6 +1293,11 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
   a.skip = skip;
   a.skip_stride = skip_stride;
   a.two_level = sh.x_reg == 1 ? 1 : 0;
+  if (fz && pass == 0) {
+    VS_REQUIRE(a.two_level == 1 && sh.fuse_xy != 1 && x2_ctas(L, M * N * 3) > 0,
+               "folded solver step needs the two-level x pass");
+    a.fz = *fz;
+  }
   StridedArgs<T> s{};
   s.src = t; s.dst = t;
   s.xext = L; s.n_in = M; s.n_out = M;
@@ -1563,8 +1568,10 @@ void autotune_prec(vs_prec& pr, cudaStream_t st) {
 template void autotune_prec<float>(vs_prec&, cudaStream_t);
 template void autotune_prec<double>(vs_prec&, cudaStream_t);
 
-template void prec_apply_pass<float>(const vs_prec&, const float2*, float2*, int, const int*, cudaStream_t, int, int);
-template void prec_apply_pass<double>(const vs_prec&, const double2*, double2*, int, const int*, cudaStream_t, int, int);
+template void prec_apply_pass<float>(const vs_prec&, const float2*, float2*, int, const int*, cudaStream_t, int, int,
+                                     const XFuse<float>*);
+template void prec_apply_pass<double>(const vs_prec&, const double2*, double2*, int, const int*, cudaStream_t, int,
+                                      int, const XFuse<double>*);
 template void prec_apply<float>(const vs_prec&, const float2*, float2*, int, const int*, cudaStream_t, int);
 template void prec_apply<double>(const vs_prec&, const double2*, double2*, int, const int*, cudaStream_t, int);
 

@@ -1,0 +1,141 @@
+// Compensated accumulation and warp / CTA sums shared by the Krylov kernels
+// and the pipeline passes that fold BiCGSTAB's vector steps in: float-float
+// accumulators for c64 data (every product of two floats formed exactly by an
+// FMA and added by TwoSum), double-double for c128, and deterministic warp and
+// CTA sums (fixed xor trees, warp 0 adding the warps in order).
+#pragma once
+#include "vs_common.cuh"
+
+namespace vs {
+
+// FP64 double-double accumulation (TwoSum / TwoProd by fma) for the c128 path.
+struct DD {
+  double hi, lo;
+};
+__device__ __forceinline__ DD dd_add(DD a, double b) {
+  const double s = a.hi + b;
+  const double bb = s - a.hi;
+  const double err = (a.hi - (s - bb)) + (b - bb);
+  return DD{s, a.lo + err};
+}
+__device__ __forceinline__ DD dd_add(DD a, DD b) {
+  DD r = dd_add(a, b.hi);
+  r.lo += b.lo;
+  return r;
+}
+__device__ __forceinline__ DD dd_fma(DD a, double x, double y) {
+  const double p = x * y;
+  const double e = fma(x, y, -p);
+  DD r = dd_add(a, p);
+  r.lo += e;
+  return r;
+}
+
+// Accumulators.  c64 inputs: every product of two floats is formed exactly as
+// a float pair (p = a*b rounded, e = fma(a, b, -p)) and added into a
+// float-float sum by TwoSum (Knuth), about 48 bits of significand for the
+// few elements a thread visits; the pair is widened to double once, and the
+// grid-wide sums are taken in double.  This keeps compensated inner products
+// without a double-precision FMA per element.
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float b) {
+  const float s = __fadd_rn(hi, b);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  hi = s;
+  lo = __fadd_rn(lo, err);
+}
+__device__ __forceinline__ void ff_fma(float& hi, float& lo, float a, float b) {
+  const float pr = __fmul_rn(a, b);
+  const float e = __fmaf_rn(a, b, -pr);
+  ff_add(hi, lo, pr);
+  lo = __fadd_rn(lo, e);
+}
+template <typename T>
+struct Acc {
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+  __device__ __forceinline__ void dot(cplx_t<T> u, cplx_t<T> v) {  // += conj(u) v
+    ff_fma(rh, rl, u.x, v.x);
+    ff_fma(rh, rl, u.y, v.y);
+    ff_fma(ih, il, u.x, v.y);
+    ff_fma(ih, il, -u.y, v.x);
+  }
+  __device__ __forceinline__ void norm2(cplx_t<T> u) {
+    ff_fma(rh, rl, u.x, u.x);
+    ff_fma(rh, rl, u.y, u.y);
+  }
+  __device__ __forceinline__ double2 value() const {
+    return make_double2((double)rh + (double)rl, (double)ih + (double)il);
+  }
+};
+template <>
+struct Acc<double> {
+  DD re{0, 0}, im{0, 0};
+  __device__ __forceinline__ void dot(double2 u, double2 v) {
+    re = dd_fma(re, u.x, v.x);
+    re = dd_fma(re, u.y, v.y);
+    im = dd_fma(im, u.x, v.y);
+    im = dd_fma(im, -u.y, v.x);
+  }
+  __device__ __forceinline__ void norm2(double2 u) {
+    re = dd_fma(re, u.x, u.x);
+    re = dd_fma(re, u.y, u.y);
+  }
+  __device__ __forceinline__ double2 value() const { return make_double2(re.hi + re.lo, im.hi + im.lo); }
+};
+
+// ff (float-float) sum of two ff values: TwoSum of the leading parts, the
+// trailing parts and the error added, renormalised (about 48 bits).
+__device__ __forceinline__ void ff_add2(float& hi, float& lo, float bhi, float blo) {
+  const float s = __fadd_rn(hi, bhi);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(bhi, bb));
+  const float t = __fadd_rn(err, __fadd_rn(lo, blo));
+  hi = __fadd_rn(s, t);
+  lo = __fsub_rn(t, __fsub_rn(hi, s));
+}
+
+// Warp sum (xor tree) of one value per lane: float-float on the FP32 pipes
+// (FF, the c64 solver's accumulators, which are float-float already), or
+// double (the FP64 path, which keeps double's exponent range).
+template <bool FF>
+__device__ __forceinline__ double warp_sum(double v) {
+  if constexpr (FF) {
+    float hi = (float)v;
+    float lo = (float)(v - (double)hi);
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, hi, off), ol = __shfl_xor_sync(0xffffffffu, lo, off);
+      ff_add2(hi, lo, oh, ol);
+    }
+    return (double)hi + (double)lo;
+  } else {
+#pragma unroll
+    for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+  }
+}
+
+
+// Sums NV per-thread values over the CTA (all threads must call it) and
+// writes them to out[0..NV-1] (thread 0; blockDim.x a multiple of 32, at most
+// 1024 threads).  FF selects the float-float warp tree (c64 accumulators).
+template <int NV, bool FF>
+__device__ __forceinline__ void cta_partials(const double (&v)[NV], double* __restrict__ out) {
+  __shared__ double sm[NV][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const double x = warp_sum<FF>(v[k]);
+    if (lane == 0) sm[k][warp] = x;
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const double x = warp_sum<FF>(lane < nw ? sm[k][lane] : 0.0);
+      if (lane == 0) out[k] = x;
+    }
+  }
+}
+
+}  // namespace vs

@@ -26,10 +26,12 @@
 // double-float in vs_df_passes.cu.
 #pragma once
 #include "vs_spass.cuh"
+#include "vs_reduce.cuh"
 
 namespace vs {
 
 constexpr int kX2Threads = 256;
+constexpr int X2C = 4;  // elements per chunk of the folded gather
 
 template <typename T>
 __device__ __forceinline__ cplx_t<T> x2_gather(const PipeArgs<T>& a, const cplx_t<T>* x, int pos, int mode) {
@@ -42,7 +44,7 @@ __device__ __forceinline__ cplx_t<T> x2_gather(const PipeArgs<T>& a, const cplx_
 }
 
 template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>>
-__global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
+__global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && R2 <= 18) ? 4 : 1) k_x2(PipeArgs<T> a, int mode) {
   using C = cplx_t<T>;  // storage
   static_assert(sizeof(K) == sizeof(C), "compute and storage elements share the shared-memory layout");
   constexpr int P = R1 * R2, NL = kX2Threads / R2, RS = R2 | 1;
@@ -65,13 +67,56 @@ __global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
     const int n1 = it % R1, l = it / R1, line = line0 + l;
     const bool act = it < R1 * NL;
     K v[R2];
+    const bool fused = a.fz.kind == XF_GATHER_P || a.fz.kind == XF_GATHER_S;
+    Acc<T> acc;
     if (act && line < nlines) {
       const int c = line / MN, jk = line - c * MN;
       const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
+      if (fused) {
+        // in chunks of X2C elements: indices, then the solver's vectors, then
+        // the formed elements written back, so a chunk's loads are in flight
+        // together (a store before the next element's loads would order them)
+        const int64_t off = (int64_t)rhs * a.n3;
+        const bool pk = a.fz.kind == XF_GATHER_P;
+        const C sa = a.fz.scalar(rhs, a.fz.off_a);
+        const C sb = pk ? a.fz.scalar(rhs, a.fz.off_b) : czero<C>();
+        const bool first = pk && *reinterpret_cast<const int*>(a.fz.sbase + rhs * a.fz.sstride + a.fz.off_iter) == 0;
+        const C* __restrict__ fu = a.fz.u + off;
+        const C* __restrict__ fv = a.fz.v + off;
+        C* __restrict__ fw = a.fz.w + off;
 #pragma unroll
-      for (int n2 = 0; n2 < R2; ++n2) {
-        const int i = n1 + R1 * n2;
-        v[n2] = i < a.L ? to_compute<K>(x2_gather(a, x, __ldg(map + i), mode)) : czero<K>();
+        for (int c0 = 0; c0 < R2; c0 += X2C) {
+          int pos[X2C];
+          C val[X2C];
+#pragma unroll
+          for (int j = 0; j < X2C; ++j) {
+            const int i = n1 + R1 * (c0 + j);
+            pos[j] = (c0 + j < R2 && i < a.L) ? __ldg(map + i) : -1;
+          }
+#pragma unroll
+          for (int j = 0; j < X2C; ++j) {
+            val[j] = czero<C>();
+            if (pos[j] >= 0) {
+              const C r = fu[pos[j]], vv = fv[pos[j]];
+              if (pk) val[j] = first ? r : cfma(sa, csub(fw[pos[j]], cmul(sb, vv)), r);
+              else val[j] = csub(r, cmul(sa, vv));
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < X2C; ++j) {
+            if (c0 + j < R2) v[c0 + j] = to_compute<K>(val[j]);
+            if (pos[j] >= 0) {
+              fw[pos[j]] = val[j];
+              if (!pk) acc.norm2(val[j]);
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2) {
+          const int i = n1 + R1 * n2;
+          v[n2] = i < a.L ? to_compute<K>(x2_gather(a, x, __ldg(map + i), mode)) : czero<K>();
+        }
       }
     } else {
 #pragma unroll
@@ -102,6 +147,10 @@ __global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
         for (int k1 = 0; k1 < R1; ++k1) out[k2 + R2 * k1] = to_storage(u[k1], C{});
       }
     }
+    if (a.fz.kind == XF_GATHER_S) {  // the CTA's ||s||^2 (every thread takes part)
+      const double w[1] = {acc.value().x};
+      cta_partials<1, std::is_same<T, float>::value>(w, a.fz.part + rhs * a.fz.pstride + blockIdx.x);
+    }
   } else {
     const C* t1 = a.t1 + t1off;
     C* y = a.y + (int64_t)rhs * a.n3;
@@ -129,6 +178,8 @@ __global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
     }
     __syncthreads();
     const int n1 = it % R1, la = it / R1, linea = line0 + la;
+    Acc<T> acc, acc2;
+    const int fk = a.fz.kind;
     if (it < R1 * NL && linea < nlines && n1 < a.L) {
       K v[R2];
       const K* s = S + (la * R1 + n1) * RS;
@@ -137,24 +188,45 @@ __global__ void __launch_bounds__(kX2Threads) k_x2(PipeArgs<T> a, int mode) {
       reg_dft<R2, R2, 1, R1, true, K>(v, tw);
       const int c = linea / MN, jk = linea - c * MN;
       const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
+      // the output never aliases the input or the solver's vectors: with the
+      // pointers restrict-qualified the next element's loads need not wait
+      // for this element's store
+      const C* __restrict__ xr = x;
+      C* __restrict__ yr = y;
+      const C* __restrict__ fu = fk != XF_NONE ? a.fz.u + (int64_t)rhs * a.n3 : nullptr;
 #pragma unroll
       for (int n2 = 0; n2 < R2; ++n2) {
         const int i = n1 + R1 * n2;
         if (i >= a.L) continue;
-        const int pos = __ldg(map + i);
-        if (pos < 0) continue;
+        const int p = __ldg(map + i);
+        if (p < 0) continue;
         const C conv = to_storage(v[n2], C{});
         C out;
         if (mode == MODE_PLAIN) {
           out = conv;
         } else {
-          const C xv = x[pos];
-          if (mode == VS_NOTRANSP) out = csub(cmul(diag_term(a, pos, rhs, false), xv), cmul(a.d2.at(pos), conv));
-          else if (mode == VS_TRANSP) out = csub(cmul(diag_term(a, pos, rhs, false), xv), conv);
-          else out = csub(cmul(diag_term(a, pos, rhs, true), xv), cconj(conv));
+          const C xv = xr[p];
+          if (mode == VS_NOTRANSP) out = csub(cmul(diag_term(a, p, rhs, false), xv), cmul(a.d2.at(p), conv));
+          else if (mode == VS_TRANSP) out = csub(cmul(diag_term(a, p, rhs, false), xv), conv);
+          else out = csub(cmul(diag_term(a, p, rhs, true), xv), cconj(conv));
         }
-        y[pos] = out;
+        yr[p] = out;
+        if (fk == XF_SCATTER_DOT) {
+          acc.dot(fu[p], out);  // rt^H v
+        } else if (fk == XF_SCATTER_OMEGA) {
+          acc.dot(out, fu[p]);  // t^H s
+          acc2.norm2(out);      // t^H t
+        }
       }
+    }
+    // the CTA's inner products (every thread takes part)
+    constexpr bool FF = std::is_same<T, float>::value;
+    if (fk == XF_SCATTER_DOT) {
+      const double w[2] = {acc.value().x, acc.value().y};
+      cta_partials<2, FF>(w, a.fz.part + rhs * a.fz.pstride + (int64_t)blockIdx.x * 2);
+    } else if (fk == XF_SCATTER_OMEGA) {
+      const double w[3] = {acc.value().x, acc.value().y, acc2.value().x};
+      cta_partials<3, FF>(w, a.fz.part + rhs * a.fz.pstride + (int64_t)blockIdx.x * 3);
     }
   }
 }
