@@ -568,7 +568,8 @@ def run_ours(args):
     line = {"metric": METRIC, "value": ms_mixed, "unit": "ms", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "c64 (refinement residual on FP64 data, its z FFTs in double-float when faster; FP64 dots, norms)",
+            "dtype": "c64 (inner products: exact float products summed in float-float; refinement residual on "
+                     "FP64 data, its FFTs in double-float where faster; FP64 norms)",
             "data": "synthetic (seeded reference-rule geometry, plane-wave RHS)",
             "config": _config_dict(p, world), "fft_grid": "x".join(str(v) for v in op.PQR),
             "converged": ok, "relres": last["relres"], "iterations": last["iter"],

@@ -287,7 +287,7 @@ typedef struct vs_solve_opts {
   float* profile_ms;
   /* VS_BICGSTAB: 0 (default) folds the vector steps of an iteration into the
    * x passes (p and s formed in the preconditioner's forward x pass, the
-   * inner products of v and t added in the matvec's inverse x pass, one-warp
+   * inner products of v and t added in the matvec's inverse x pass, one-CTA
    * kernels for alpha, ||s|| and omega) wherever both x passes run the
    * two-level kernels; 1 keeps them as separate kernels.  The two agree to
    * the rounding of the inner products' summation order. */

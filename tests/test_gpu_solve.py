@@ -435,7 +435,7 @@ def test_solve_profile_inside_the_graph(api, precision):
 def test_folded_vector_steps_match_separate_kernels(api, precision, tol, nrhs):
     """BiCGSTAB with its vector steps folded into the x passes (p and s formed
     in the preconditioner's forward x pass, rt^H v and t^H s, t^H t added in the
-    matvec's inverse x pass, one-warp scalar steps) against the separate
+    matvec's inverse x pass, one-CTA scalar steps) against the separate
     kernels, on the 27 x 23 x 7 hex plate with both x passes forced to the
     two-level kernels (the folded form needs them): both converge with the
     oracle's FP64 MVP confirming ||b - A x|| <= tol ||b||, the solutions agree

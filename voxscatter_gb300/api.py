@@ -780,12 +780,13 @@ def solve_particles(ops, precs, b_ptrs, x_ptrs, nrhs, grams=None, tol=1e-6, maxi
 
 
 def solve_batch_device(op, b_ptr, x_ptr, nrhs, prec=None, tol=1e-6, maxit=2000, precision="mixed",
-                       iters_per_graph=4, gram=None):
+                       iters_per_graph=4, gram=None, fold=True):
     """vs_solve_batch_device on device buffers (double2, nrhs*n3 each); ``gram``
-    as in solve_batch."""
+    and ``fold`` as in solve_batch."""
     lib = op.ctx._lib
     o = _solve_opts(lib, tol, maxit, precision)
     o.iters_per_graph = int(iters_per_graph)
+    o.unfused = 0 if fold else 1
     if gram is not None:
         g, o.gram_n = _gram_array(gram, nrhs, op.LMN)
         o.gram = L.dptr(g)

@@ -152,32 +152,53 @@ __device__ __forceinline__ void finish_omega(KState* s, const double (&tt)[3]) {
 
 // Folded steps (vs_pipeline.cuh XFuse): a two-level x pass left nb per-CTA
 // partial sums (NV each) of right-hand side blockIdx.x at part + blockIdx.x *
-// pstride; one warp adds them in CTA order and takes the scalar step.
+// pstride; one CTA of kFinThreads adds them in a fixed order (each thread a
+// few partials, loaded together, then the warp and CTA trees) and takes the
+// scalar step.  (One warp walking all partials waited on one L2 load per
+// partial: 5-8 us per step.)
+constexpr int kFinThreads = 256;
 template <int NV>
-__device__ __forceinline__ void sum_cta_partials(const double* part, int nb, double (&tot)[NV]) {
-  const int lane = threadIdx.x & 31;
+__device__ __forceinline__ void sum_cta_partials(const double* __restrict__ part, int nb, double (&tot)[NV]) {
+  __shared__ double sm[NV][kFinThreads / 32];
+  __shared__ double st[NV];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
     double x = 0;
-    for (int b = lane; b < nb; b += 32) x += part[b * NV + k];
-    tot[k] = warp_sum<false>(x);
+#pragma unroll 4
+    for (int b = threadIdx.x; b < nb; b += kFinThreads) x += part[b * NV + k];
+    x = warp_sum<false>(x);
+    if (lane == 0) sm[k][warp] = x;
   }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const double y = warp_sum<false>(lane < kFinThreads / 32 ? sm[k][lane] : 0.0);
+      if (lane == 0) st[k] = y;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) tot[k] = st[k];
 }
-__global__ void __launch_bounds__(32) k_fin_alpha(KState* states, const double* part, int64_t pstride, int nb) {
+__global__ void __launch_bounds__(kFinThreads) k_fin_alpha(KState* states, const double* part, int64_t pstride,
+                                                           int nb) {
   KState* s = states + blockIdx.x;
   if (s->skip) return;
   double t[2];
   sum_cta_partials<2>(part + blockIdx.x * pstride, nb, t);
   if (threadIdx.x == 0) finish_alpha(s, t);
 }
-__global__ void __launch_bounds__(32) k_fin_s(KState* states, const double* part, int64_t pstride, int nb) {
+__global__ void __launch_bounds__(kFinThreads) k_fin_s(KState* states, const double* part, int64_t pstride, int nb) {
   KState* s = states + blockIdx.x;
   if (s->skip) return;
   double t[1];
   sum_cta_partials<1>(part + blockIdx.x * pstride, nb, t);
   if (threadIdx.x == 0) finish_s(s, t);
 }
-__global__ void __launch_bounds__(32) k_fin_omega(KState* states, const double* part, int64_t pstride, int nb) {
+__global__ void __launch_bounds__(kFinThreads) k_fin_omega(KState* states, const double* part, int64_t pstride,
+                                                           int nb) {
   KState* s = states + blockIdx.x;
   if (s->skip) return;
   double t[3];
@@ -489,7 +510,7 @@ constexpr int kIterMarks = 25;
 // preconditioner's forward x pass forms p (first apply) and s with ||s||^2
 // (second apply), the matvec's inverse x pass adds rt^H v (first) and t^H s,
 // t^H t (second); the partial sums of nb_mv / nb_pr CTAs per right-hand side
-// go to part (pstride doubles each), and one-warp kernels take the scalar
+// go to part (pstride doubles each), and one-CTA kernels take the scalar
 // steps.  Four streaming vector kernels of the iteration are gone.
 struct FoldPlan {
   int nb_mv = 0, nb_pr = 0;
@@ -576,13 +597,13 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
       matvec_pass<T>(op, ph, v, nrhs, mode, skip, st, pass, ss, rgp(w), pass == 4 ? &fd : nullptr);
       mark(7 + pass);
     }
-    k_fin_alpha<<<nrhs, 32, 0, st>>>(s, fold->part, fold->pstride, fold->nb_mv);
+    k_fin_alpha<<<nrhs, kFinThreads, 0, st>>>(s, fold->part, fold->pstride, fold->nb_mv);
     mark(12);
     // s = r - alpha v and ||s||^2 in the second apply's forward x pass; the
     // half-step test, then the rest of the apply
     prec_apply_pass<T>(*pr, sv, sh, nrhs, skip, st, 0, ss, &fsv);
     mark(13);
-    k_fin_s<<<nrhs, 32, 0, st>>>(s, fold->part, fold->pstride, fold->nb_pr);
+    k_fin_s<<<nrhs, kFinThreads, 0, st>>>(s, fold->part, fold->pstride, fold->nb_pr);
     k_bicg_xhalf<T><<<gr, kRedThreads, 0, st>>>(x, ph, n, s);
     mark(24);
     for (int pass = 1; pass < 5; ++pass) {
@@ -594,7 +615,7 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
       matvec_pass<T>(op, sh, t, nrhs, mode, skip, st, pass, ss, rgp(w), pass == 4 ? &fo : nullptr);
       mark(18 + pass);
     }
-    k_fin_omega<<<nrhs, 32, 0, st>>>(s, fold->part, fold->pstride, fold->nb_mv);
+    k_fin_omega<<<nrhs, kFinThreads, 0, st>>>(s, fold->part, fold->pstride, fold->nb_mv);
     k_bicg_xr<T><<<gr, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, rt, n, s);
     mark(23);
     VS_LAUNCH_CHECK();
@@ -632,7 +653,7 @@ static void add_iteration_profile(const cudaEvent_t* ev, int iters, SolveProfile
 
 // Kernels in one bicg_iteration: 6 solver kernels, 2 matvecs of 5 passes, and
 // 2 preconditioner applies (or 2 copies without preconditioner); with folded
-// steps 5 solver kernels (the three one-warp scalar steps, x after a
+// steps 5 solver kernels (the three one-CTA scalar steps, x after a
 // converged half step, x and r) and 20 passes.
 template <typename T>
 static int kernels_per_iteration(const vs_prec* pr, bool folded = false) {

@@ -164,6 +164,29 @@ __global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && 
 #pragma unroll
       for (int k1 = 0; k1 < R1; ++k1) u[k1] = ld ? to_compute<K>(in[k2 + R2 * k1]) : czero<K>();
     }
+    // With a folded inner product, the solver vector read at the scatter (rt
+    // or s) was last touched an iteration or a preconditioner apply ago and is
+    // mostly out of L2: each thread prefetches it (and the input) into L2 at
+    // the unknowns its stage-A' item will write, so the latency overlaps the
+    // first DFT stage instead of the scatter.
+    if (a.fz.kind == XF_SCATTER_DOT || a.fz.kind == XF_SCATTER_OMEGA) {
+      const int pn1 = it % R1, pla = it / R1, pline = line0 + pla;
+      if (it < R1 * NL && pline < nlines && pn1 < a.L) {
+        const int c = pline / MN, jk = pline - c * MN;
+        const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
+        const C* fu = a.fz.u + (int64_t)rhs * a.n3;
+        const C* xin = a.x + (int64_t)rhs * a.n3;
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2) {
+          const int i = pn1 + R1 * n2;
+          if (i >= a.L) continue;
+          const int p = __ldg(map + i);
+          if (p < 0) continue;
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(fu + p));
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(xin + p));
+        }
+      }
+    }
     for (int i = it; i < P; i += kX2Threads) {
       tw[i] = to_compute<K>(__ldg(a.twP + i));
       const int m1 = i / R2, j2 = i - m1 * R2;
