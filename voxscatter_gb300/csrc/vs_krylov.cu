@@ -531,6 +531,21 @@ static bool can_fold(const vs_op& op, const vs_prec* pr) {
   return x2_ctas(pr->L, nl) > 0 && x2_ctas(op.P, nl) > 0 && pr->L == op.L && pr->M == op.M && pr->N == op.N;
 }
 
+// The fold plan of an operator / preconditioner pair and nrhs right-hand
+// sides, its partial sums in w.xpart; false when the steps cannot be folded.
+template <typename T>
+static bool make_fold_plan(const vs_op& op, const vs_prec* pr, KrylovWork& w, int nrhs, FoldPlan& plan) {
+  if (!can_fold<T>(op, pr)) return false;
+  const int nl = op.M * op.N * 3;
+  plan.nb_mv = x2_ctas(op.P, nl);
+  plan.nb_pr = x2_ctas(pr->L, nl);
+  plan.pstride = 3 * (int64_t)std::max(plan.nb_mv, plan.nb_pr);
+  const size_t need = (size_t)nrhs * plan.pstride * sizeof(double);
+  if (w.xpart.bytes < need) w.xpart.alloc(need);
+  plan.part = w.xpart.as<double>();
+  return true;
+}
+
 // One BiCGSTAB iteration (two half steps) for all right-hand sides as a fixed
 // launch sequence; mk (kIterMarks events) records the marks above.
 template <typename T>
@@ -713,17 +728,7 @@ static std::vector<KState> bicgstab_core(const vs_op& op, const vs_prec* pr, Kry
   // it is captured once and reused by later solves on this operator.
   GraphCache& gc = std::is_same<T, float>::value ? w.graph32 : w.graph64;
   FoldPlan plan;
-  const FoldPlan* fold = nullptr;
-  if (fold_steps && can_fold<T>(op, pr)) {
-    const int nl = op.M * op.N * 3;
-    plan.nb_mv = x2_ctas(op.P, nl);
-    plan.nb_pr = x2_ctas(pr->L, nl);
-    plan.pstride = 3 * (int64_t)std::max(plan.nb_mv, plan.nb_pr);
-    const size_t need = (size_t)nrhs * plan.pstride * sizeof(double);
-    if (w.xpart.bytes < need) w.xpart.alloc(need);
-    plan.part = w.xpart.as<double>();
-    fold = &plan;
-  }
+  const FoldPlan* fold = fold_steps && make_fold_plan<T>(op, pr, w, nrhs, plan) ? &plan : nullptr;
   std::vector<const void*> key = {w.r.p, w.rt.p, w.p.p, w.v_.p, w.s.p, w.t.p, w.ph.p, w.sh.p, w.x.p,
                                   w.state.p, w.partials.p, op.t1.p, op.t2.p,
                                   (const void*)(uintptr_t)(pr ? pr->id : 0), pr ? pr->t.p : nullptr,
@@ -1066,7 +1071,7 @@ void read_all_scal(std::vector<PartState>& ps, cudaStream_t st) {
 // p.rscale[r].  Returns with p.cur holding the final states.
 template <typename T>
 void bicgstab_lockstep(vs_ctx* ctx, std::vector<PartState>& ps, double tol, int maxit, int per_graph, int stag,
-                       int mode, cudaStream_t st, int64_t* launches) {
+                       int mode, cudaStream_t st, int64_t* launches, bool fold_steps) {
   using C = cplx_t<T>;
   const int np = (int)ps.size();
   bool any_active = false;
@@ -1107,10 +1112,17 @@ void bicgstab_lockstep(vs_ctx* ctx, std::vector<PartState>& ps, double tol, int 
     p.cur = p.h;
   }
   if (!any_active) return;
-  // the graph: every particle's iterations as a branch, then the skip gather
+  // the graph: every particle's iterations as a branch, then the skip gather;
+  // each particle folds its vector steps into its x passes where it can
   GraphCache& gc = std::is_same<T, float>::value ? ctx->pgraph32 : ctx->pgraph64;
+  std::vector<FoldPlan> plans(np);
+  std::vector<const FoldPlan*> folds(np, nullptr);
+  for (int i = 0; i < np; ++i)
+    if (fold_steps && make_fold_plan<T>(*ps[i].job->op, ps[i].job->pr, ps[i].job->op->kw, ps[i].job->nrhs, plans[i]))
+      folds[i] = &plans[i];
   std::vector<const void*> key = {(const void*)(uintptr_t)per_graph, (const void*)(uintptr_t)mode,
                                   (const void*)(uintptr_t)np, ctx->pskip.p, ctx->pstates.p, ctx->poff.p};
+  for (int i = 0; i < np; ++i) key.push_back(folds[i] ? folds[i]->part : nullptr);
   for (auto& p : ps) {
     const vs_op& op = *p.job->op;
     const KrylovWork& w = op.kw;
@@ -1126,13 +1138,15 @@ void bicgstab_lockstep(vs_ctx* ctx, std::vector<PartState>& ps, double tol, int 
   if (gc.exec == nullptr || gc.key != key) {
     gc.reset();
     // one idle launch sequence per particle outside capture (first-use attribute calls)
-    for (auto& p : ps) {
+    for (int i = 0; i < np; ++i) {
+      PartState& p = ps[i];
       KrylovWork& w = p.job->op->kw;
       std::vector<KState> idle = p.h;
       for (auto& k : idle) k.skip = 1;
       upload_states(w, idle, st);
-      bicg_iteration<T>(*p.job->op, p.job->pr, w, w.state.as<KState>(), p.n, p.job->nrhs, mode, st);
-      *launches += kernels_per_iteration<T>(p.job->pr);
+      bicg_iteration<T>(*p.job->op, p.job->pr, w, w.state.as<KState>(), p.n, p.job->nrhs, mode, st, nullptr,
+                        folds[i]);
+      *launches += kernels_per_iteration<T>(p.job->pr, folds[i] != nullptr);
     }
     VS_CUDA(cudaStreamSynchronize(st));
     const int naux = std::min(np, kMaxAuxStreams);
@@ -1158,7 +1172,8 @@ void bicgstab_lockstep(vs_ctx* ctx, std::vector<PartState>& ps, double tol, int 
           PartState& p = ps[i];
           KrylovWork& w = p.job->op->kw;
           for (int k = 0; k < per_graph; ++k)
-            bicg_iteration<T>(*p.job->op, p.job->pr, w, w.state.as<KState>(), p.n, p.job->nrhs, mode, si);
+            bicg_iteration<T>(*p.job->op, p.job->pr, w, w.state.as<KState>(), p.n, p.job->nrhs, mode, si, nullptr,
+                              folds[i]);
           VS_CUDA(cudaEventRecord(ev[i], si));
         }
         for (int i = 0; i < np; ++i) VS_CUDA(cudaStreamWaitEvent(st, ev[i], 0));
@@ -1193,7 +1208,8 @@ void bicgstab_lockstep(vs_ctx* ctx, std::vector<PartState>& ps, double tol, int 
   for (auto& p : ps) total += p.job->nrhs;
   std::vector<int> skip(total);
   int64_t per_launch = 1;
-  for (auto& p : ps) per_launch += (int64_t)per_graph * kernels_per_iteration<T>(p.job->pr);
+  for (int i = 0; i < np; ++i)
+    per_launch += (int64_t)per_graph * kernels_per_iteration<T>(ps[i].job->pr, folds[i] != nullptr);
   const int max_launch = (maxit + per_graph - 1) / per_graph + 1;
   for (int it = 0; it < max_launch; ++it) {
     VS_CUDA(cudaGraphLaunch(gc.exec, st));
@@ -1289,7 +1305,8 @@ void solve_bicgstab_particles(vs_ctx* ctx, std::vector<PartJob>& jobs, const Sol
       p.rscale.resize(jobs[i].nrhs);
       for (int r = 0; r < jobs[i].nrhs; ++r) p.rscale[r] = 1.0 / p.bsafe[r];
     }
-    bicgstab_lockstep<double>(ctx, ps, prm.tol, prm.maxit, prm.per_graph, 0, prm.op_mode, st, &launches);
+    bicgstab_lockstep<double>(ctx, ps, prm.tol, prm.maxit, prm.per_graph, 0, prm.op_mode, st, &launches,
+                              prm.fold_steps);
     for (int i = 0; i < np; ++i) {
       KrylovWork& w = jobs[i].op->kw;
       const int64_t m = ps[i].n * jobs[i].nrhs;
@@ -1363,7 +1380,7 @@ void solve_bicgstab_particles(vs_ctx* ctx, std::vector<PartJob>& jobs, const Sol
         for (int r = 0; r < jobs[i].nrhs; ++r) ps[i].tolr[r] = itol[i][r] / tmin;
       }
       bicgstab_lockstep<float>(ctx, ps, tmin, prm.maxit - used / 2, prm.per_graph, kStagnationWindow, prm.op_mode, st,
-                               &launches);
+                               &launches, prm.fold_steps);
       bool progressed = false;
       for (int i = 0; i < np; ++i) {
         PartState& p = ps[i];
