@@ -87,6 +87,12 @@ constexpr int z2_min_blocks(int R1, int R2) {
   return nb < 1 ? 1 : (nb > 8 ? 8 : nb);
 }
 
+// Entries n2 of a length-R1*R2 z line (z = n1 + R1 n2) that can be below N
+// when R >= 2N - 1: n2 < ((R - 1) / 2) / R1 + 1.
+constexpr int z2_nzo(int R1, int R2) {
+  return ((R1 * R2 - 1) / 2) / R1 + 1 < R2 ? ((R1 * R2 - 1) / 2) / R1 + 1 : R2;
+}
+
 template <typename T, int R1, int R2, bool CAP, typename K = cplx_t<T>>
 __global__ void __launch_bounds__(z2_threads(R2, z2_tx<T>(R2)), CAP ? z2_min_blocks<T>(R1, R2) : 1)
     k_z2(PipeArgs<T> a, int sym) {
@@ -114,7 +120,7 @@ __global__ void __launch_bounds__(z2_threads(R2, z2_tx<T>(R2)), CAP ? z2_min_blo
 #pragma unroll
     for (int n2 = 0; n2 < R2; ++n2) {
       const int z = n1 + R1 * n2;
-      v[n2] = (xin && z < N) ? to_compute<K>(t2[x + z * zs + c * cs]) : czero<K>();
+      v[n2] = (n2 < z2_nzo(R1, R2) && xin && z < N) ? to_compute<K>(t2[x + z * zs + c * cs]) : czero<K>();
     }
     reg_dft<R2, R2, 1, R1, false, K>(v, tw);
     K* s = S + ((c * R1 + n1) * R2) * TX + xl;
@@ -185,7 +191,10 @@ __global__ void __launch_bounds__(z2_threads(R2, z2_tx<T>(R2)), CAP ? z2_min_blo
   }
   __syncthreads();
 
-  // A': inverse over k2, store the first N z entries
+  // A': inverse over k2, store the first N z entries.  The embedding has
+  // R >= 2N - 1 (checked at operator creation), so only n2 < NZO can hold a
+  // stored z = n1 + R1 n2 < N: the outputs above are never formed (the
+  // compiler drops their share of the last butterfly stage).
   for (int it = threadIdx.x; it < 3 * R1 * TX; it += NT) {
     const int xl = it % TX, rest = it / TX;
     const int n1 = rest % R1, c = rest / R1;
@@ -197,7 +206,7 @@ __global__ void __launch_bounds__(z2_threads(R2, z2_tx<T>(R2)), CAP ? z2_min_blo
     for (int k2 = 0; k2 < R2; ++k2) v[k2] = s[k2 * TX];
     reg_dft<R2, R2, 1, R1, true, K>(v, tw);
 #pragma unroll
-    for (int n2 = 0; n2 < R2; ++n2) {
+    for (int n2 = 0; n2 < z2_nzo(R1, R2); ++n2) {
       const int z = n1 + R1 * n2;
       if (z < N) t2[x + z * zs + c * cs] = to_storage(v[n2], C{});
     }
