@@ -36,7 +36,9 @@ constexpr int s2_tx() {
   return tx;
 }
 
-template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>>
+// HO (inverse only): n_out <= (R1 R2 + 1) / 2, so the outputs n2 >=
+// lower_half_n2 are never stored and never formed.
+template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>, bool HO = false>
 __global__ void __launch_bounds__(z2_threads(R2, s2_tx<T, R2>())) k_s2(StridedArgs<T> a) {
   using C = cplx_t<T>;  // storage
   static_assert(sizeof(K) == sizeof(C), "compute and storage elements share the shared-memory layout");
@@ -109,7 +111,7 @@ __global__ void __launch_bounds__(z2_threads(R2, s2_tx<T, R2>())) k_s2(StridedAr
       for (int k2 = 0; k2 < R2; ++k2) v[k2] = s[k2 * TX];
       reg_dft<R2, R2, 1, R1, true, K>(v, tw);
 #pragma unroll
-      for (int n2 = 0; n2 < R2; ++n2) {
+      for (int n2 = 0; n2 < (HO ? lower_half_n2(R1, R2) : R2); ++n2) {
         const int row = n1 + R1 * n2;
         if (row < a.n_out) dst[row * a.d_row + x] = to_storage(v[n2], C{});
       }
@@ -121,7 +123,11 @@ template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>>
 static void launch_s2(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st) {
   constexpr int TX = s2_tx<T, R2>(), NT = z2_threads(R2, TX);
   const size_t smem = (size_t)(R1 * R2 * TX + R1 * R2) * sizeof(cplx_t<T>);
+  // the matvec's inverse y pass keeps at most half the line (Q >= 2M - 1)
   auto k = k_s2<T, R1, R2, INV, K>;
+  if constexpr (INV) {
+    if (2 * a.n_out - 1 <= R1 * R2) k = k_s2<T, R1, R2, INV, K, true>;
+  }
   set_kernel_smem((const void*)k, smem);
   k<<<dim3(ceil_div(a.xext, TX), nplanes, nrhs), NT, smem, st>>>(a);
   VS_LAUNCH_CHECK();

@@ -43,7 +43,9 @@ __device__ __forceinline__ cplx_t<T> x2_gather(const PipeArgs<T>& a, const cplx_
   return v;
 }
 
-template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>>
+// HO (inverse only): L <= (R1 R2 + 1) / 2, so the outputs n2 >=
+// lower_half_n2 are never scattered and never formed.
+template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>, bool HO = false>
 __global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && R2 <= 18) ? 4 : 1) k_x2(PipeArgs<T> a, int mode) {
   using C = cplx_t<T>;  // storage
   static_assert(sizeof(K) == sizeof(C), "compute and storage elements share the shared-memory layout");
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && 
       C* __restrict__ yr = y;
       const C* __restrict__ fu = fk != XF_NONE ? a.fz.u + (int64_t)rhs * a.n3 : nullptr;
 #pragma unroll
-      for (int n2 = 0; n2 < R2; ++n2) {
+      for (int n2 = 0; n2 < (HO ? lower_half_n2(R1, R2) : R2); ++n2) {
         const int i = n1 + R1 * n2;
         if (i >= a.L) continue;
         const int p = __ldg(map + i);
@@ -258,7 +260,11 @@ template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>>
 static void launch_x2(const PipeArgs<T>& a, int mode, int nrhs, cudaStream_t st) {
   constexpr int NL = kX2Threads / R2, RS = R2 | 1;
   const size_t smem = (size_t)(NL * R1 * RS + 2 * R1 * R2) * sizeof(cplx_t<T>);
+  // the matvec's inverse x pass keeps at most half the line (P >= 2L - 1)
   auto k = k_x2<T, R1, R2, INV, K>;
+  if constexpr (INV) {
+    if (2 * a.L - 1 <= R1 * R2) k = k_x2<T, R1, R2, INV, K, true>;
+  }
   set_kernel_smem((const void*)k, smem);
   const int nlines = a.M * a.N * 3;
   k<<<dim3(ceil_div(nlines, NL), nrhs), kX2Threads, smem, st>>>(a, mode);

@@ -87,9 +87,10 @@ constexpr int z2_min_blocks(int R1, int R2) {
   return nb < 1 ? 1 : (nb > 8 ? 8 : nb);
 }
 
-// Entries n2 of a length-R1*R2 z line (z = n1 + R1 n2) that can be below N
-// when R >= 2N - 1: n2 < ((R - 1) / 2) / R1 + 1.
-constexpr int z2_nzo(int R1, int R2) {
+// Entries n2 of a length-R1*R2 line (index n1 + R1 n2) that can be below an
+// extent E when the length is at least 2E - 1 (the circulant embedding's
+// bound): n2 < ((R1 R2 - 1) / 2) / R1 + 1.
+constexpr int lower_half_n2(int R1, int R2) {
   return ((R1 * R2 - 1) / 2) / R1 + 1 < R2 ? ((R1 * R2 - 1) / 2) / R1 + 1 : R2;
 }
 
@@ -120,7 +121,7 @@ __global__ void __launch_bounds__(z2_threads(R2, z2_tx<T>(R2)), CAP ? z2_min_blo
 #pragma unroll
     for (int n2 = 0; n2 < R2; ++n2) {
       const int z = n1 + R1 * n2;
-      v[n2] = (n2 < z2_nzo(R1, R2) && xin && z < N) ? to_compute<K>(t2[x + z * zs + c * cs]) : czero<K>();
+      v[n2] = (n2 < lower_half_n2(R1, R2) && xin && z < N) ? to_compute<K>(t2[x + z * zs + c * cs]) : czero<K>();
     }
     reg_dft<R2, R2, 1, R1, false, K>(v, tw);
     K* s = S + ((c * R1 + n1) * R2) * TX + xl;
@@ -206,7 +207,7 @@ __global__ void __launch_bounds__(z2_threads(R2, z2_tx<T>(R2)), CAP ? z2_min_blo
     for (int k2 = 0; k2 < R2; ++k2) v[k2] = s[k2 * TX];
     reg_dft<R2, R2, 1, R1, true, K>(v, tw);
 #pragma unroll
-    for (int n2 = 0; n2 < z2_nzo(R1, R2); ++n2) {
+    for (int n2 = 0; n2 < lower_half_n2(R1, R2); ++n2) {
       const int z = n1 + R1 * n2;
       if (z < N) t2[x + z * zs + c * cs] = to_storage(v[n2], C{});
     }
