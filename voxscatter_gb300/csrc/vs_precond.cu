@@ -1293,7 +1293,7 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
   a.skip = skip;
   a.skip_stride = skip_stride;
   a.two_level = sh.x_reg == 1 ? 1 : 0;
-  if (fz && pass == 0) {
+  if (fz && pass == 0) {  // the forward x pass, whose gather is plain (MODE_PLAIN)
     VS_REQUIRE(a.two_level == 1 && sh.fuse_xy != 1 && x2_ctas(L, M * N * 3) > 0,
                "folded solver step needs the two-level x pass");
     a.fz = *fz;

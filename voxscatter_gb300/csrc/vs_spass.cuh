@@ -20,7 +20,7 @@
 // outside the instantiated list use k_strided.  K is the arithmetic type: the
 // storage type, or double-float (dfc) on FP64 data.  Instantiated per
 // precision in vs_spass_c64.cu and vs_spass_c128.cu, in double-float in
-// vs_df_passes.cu.
+// vs_df_spass_a.cu / vs_df_spass_b.cu (vs_df_passes.cuh).
 #pragma once
 #include "vs_zpass.cuh"
 

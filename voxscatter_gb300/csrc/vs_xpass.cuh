@@ -23,7 +23,7 @@
 // double-float (dfc) on FP64 data, whose DFTs then run on the FP32 pipes and
 // whose results are rounded back to FP64 at the global stores.
 // Instantiated per precision in vs_xpass_c64.cu and vs_xpass_c128.cu, in
-// double-float in vs_df_passes.cu.
+// double-float in vs_df_xpass_a.cu / vs_df_xpass_b.cu (vs_df_passes.cuh).
 #pragma once
 #include "vs_spass.cuh"
 #include "vs_reduce.cuh"
@@ -75,6 +75,8 @@ __global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && 
       const int c = line / MN, jk = line - c * MN;
       const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
       if (fused) {
+        // (only the preconditioner's forward pass folds a step, and its gather
+        // is plain: no diagonal or conjugation applies to the formed element)
         // in chunks of X2C elements: indices, then the solver's vectors, then
         // the formed elements written back, so a chunk's loads are in flight
         // together (a store before the next element's loads would order them)
