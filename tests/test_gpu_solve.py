@@ -435,12 +435,13 @@ def test_solve_profile_inside_the_graph(api, precision):
 def test_folded_vector_steps_match_separate_kernels(api, precision, tol, nrhs):
     """BiCGSTAB with its vector steps folded into the x passes (p and s formed
     in the preconditioner's forward x pass, rt^H v and t^H s, t^H t added in the
-    matvec's inverse x pass, one-CTA scalar steps) against the separate
-    kernels, on the 27 x 23 x 7 hex plate with both x passes forced to the
-    two-level kernels (the folded form needs them): both converge with the
-    oracle's FP64 MVP confirming ||b - A x|| <= tol ||b||, the solutions agree
-    to the tolerance, the iteration counts to a half step, and the launch
-    counts show which form ran (25 against 26 kernels per iteration)."""
+    matvec's inverse x pass, the scalar steps taken from the passes' partial
+    sums) against the separate kernels, on the 27 x 23 x 7 hex plate with
+    both x passes forced to the two-level kernels (the folded form needs
+    them): both converge with the oracle's FP64 MVP confirming
+    ||b - A x|| <= tol ||b||, the solutions agree to the tolerance, the
+    iteration counts to a half step, and the launch counts show which form
+    ran (23 against 26 kernels per iteration)."""
     p = W.config1()
     L, M, N, idx3, Toep, alpha, dV, b, Aor = _system(p)
     op = api.Operator(L, M, N, idx3, 1.0, dV, 1 / alpha, toep=Toep)
@@ -465,5 +466,5 @@ def test_folded_vector_steps_match_separate_kernels(api, precision, tol, nrhs):
     for r in range(nrhs):
         assert np.linalg.norm(Xf[r] - Xs[r]) / np.linalg.norm(Xs[r]) < 20 * tol, r
         assert abs(inf_f[r]["iter"] - inf_s[r]["iter"]) <= 0.5, (r, inf_f[r]["iter"], inf_s[r]["iter"])
-    # per graph launch: 25 kernels folded, 26 separate (4 iterations per graph)
+    # per graph launch: 23 kernels per iteration folded, 26 separate
     assert inf_f[0]["launches"] < inf_s[0]["launches"], (inf_f[0]["launches"], inf_s[0]["launches"])

@@ -34,49 +34,36 @@ namespace vs {
 constexpr int kRedThreads = 256;
 constexpr int kRedBlocks = 2 * 152;
 
-// Block reduction of NV doubles; returns true in the last CTA to finish, with
-// the grid totals in `tot` (all threads of that CTA).  GB300's FP64 rate is a
-// small fraction of its FP32 rate, and a double tree in which every thread of
-// a large CTA took part cost several microseconds, so: the warp level runs as
-// warp_sum<FF>, warp 0 alone adds the warps' sums and writes the CTA's partial
-// (double), and warp 0 of the last CTA adds the partials in CTA order, so the
-// result does not depend on scheduling.
-template <int NV, bool FF>
-__device__ bool grid_reduce(double (&v)[NV], double* __restrict__ partials, unsigned* __restrict__ counter,
+// Grid sum of NV per-thread values (FF2 for the c64 kernels, double for
+// c128); returns true in the last CTA to finish, with the grid totals in
+// `tot` (all threads of that CTA).  Each CTA adds its threads' values
+// (cta_partials: warp trees, then warp 0 over the warps) into one slot per
+// value, and warp 0 of the last CTA adds the slots in CTA order, so the
+// result does not depend on scheduling.  GB300 runs FP64 at a small fraction
+// of its FP32 rate (an FP64 instruction that every thread of a 300-CTA grid
+// executed cost about 0.1 us), so the c64 sums stay float-float on the FP32
+// pipes and one lane widens each total to double.
+template <int NV, typename V>
+__device__ bool grid_reduce(const V (&v)[NV], double* __restrict__ partials, unsigned* __restrict__ counter,
                             double (&tot)[NV]) {
-  __shared__ double sm[NV][kRedThreads / 32];
   __shared__ double stot[NV];
   __shared__ bool s_last;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    const double x = warp_sum<FF>(v[k]);
-    if (lane == 0) sm[k][warp] = x;
-  }
-  __syncthreads();
-  if (warp == 0) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      const double x = warp_sum<FF>(lane < nw ? sm[k][lane] : 0.0);
-      if (lane == 0) partials[blockIdx.x * NV + k] = x;
-    }
-    if (lane == 0) {
-      __threadfence();
-      const unsigned t = atomicAdd(counter, 1u);
-      s_last = (t == gridDim.x - 1);
-    }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  cta_partials<NV>(v, partials + (int64_t)blockIdx.x * NV);  // written by thread 0
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
   }
   __syncthreads();
   if (!s_last) return false;
   __threadfence();
   if (warp == 0) {
+    V x[NV];
+    slot_sums<NV, (kRedBlocks + 31) / 32, true>(partials, (int)gridDim.x, lane, 32, x);
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      double x = 0;
-      for (int b = lane; b < (int)gridDim.x; b += 32) x += ((volatile double*)partials)[b * NV + k];
-#pragma unroll
-      for (int off = 16; off; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
-      if (lane == 0) stot[k] = x;
+      const V y = warp_sum_v(x[k]);
+      if (lane == 0) stot[k] = widen(y);
     }
   }
   __syncthreads();
@@ -94,15 +81,49 @@ __device__ __forceinline__ bool cz(double2 a) { return a.x == 0.0 && a.y == 0.0;
 __device__ __forceinline__ bool cfinite(double2 a) { return isfinite(a.x) && isfinite(a.y); }
 
 #define GRID_LOOP(i, n) for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
-// The same loop unrolled four ways: with the vectors declared __restrict__,
-// the loads of four elements issue before the first store, so a thread's
-// handful of elements costs about two memory latencies instead of one each.
-#define GRID_LOOP4(i, n) _Pragma("unroll 4") GRID_LOOP(i, n)
+
+// Grid-stride walk over [0, n) in chunks of kChunk elements per thread: the
+// loads of a chunk (ld(i), each predicated on i < n) are all issued before
+// its first use (use(i, loaded)), so a thread waits about one memory latency
+// per chunk rather than one per element.  Elements are used in increasing i,
+// as in a plain grid-stride loop, so per-thread sums keep their order.
+constexpr int kChunk = 4;
+template <typename Ld, typename Use>
+__device__ __forceinline__ void grid_chunks(int64_t n, Ld ld, Use use) {
+  const int64_t st = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < n; b += kChunk * st) {
+    decltype(ld(b)) v[kChunk];
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u)
+      if (b + u * st < n) v[u] = ld(b + u * st);
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u)
+      if (b + u * st < n) use(b + u * st, v[u]);
+  }
+}
+template <typename C, int K>
+struct Loaded {
+  C e[K];
+};
 
 // All BiCGSTAB kernels below run on a batch of right-hand sides sharing one
 // operator: blockIdx.y is the right-hand side, its vectors start at
 // rhs * n, and its scalars live in states[rhs] (each state carries its own
-// reduction partials and counter).
+// reduction partials and counter).  A kernel of more than one CTA writes a
+// state only from the last CTA to count in on that counter, after every
+// thread of every CTA has read the skip flag, so a CTA never splits over it.
+
+// The scalars in the kernels' precision: the float copies for c64.
+template <typename C>
+__device__ __forceinline__ C scal(const double2& d, const float2& f);
+template <>
+__device__ __forceinline__ float2 scal<float2>(const double2&, const float2& f) { return f; }
+template <>
+__device__ __forceinline__ double2 scal<double2>(const double2& d, const float2&) { return d; }
+__device__ __forceinline__ float2 to_f2(double2 v) { return make_float2((float)v.x, (float)v.y); }
+__device__ __forceinline__ void set_alpha(KState* s, double2 v) { s->alpha = v; s->alpha32 = to_f2(v); }
+__device__ __forceinline__ void set_omega(KState* s, double2 v) { s->omega = v; s->omega32 = to_f2(v); }
+__device__ __forceinline__ void set_beta(KState* s, double2 v) { s->beta = v; s->beta32 = to_f2(v); }
 
 // The scalar steps of BiCGSTAB, from the grid totals (one thread):
 // alpha = rho / (rt^H v) with its breakdown test;
@@ -113,7 +134,7 @@ __device__ __forceinline__ void finish_alpha(KState* s, const double (&t)[2]) {
     s->skip = 1;
     return;
   }
-  s->alpha = cdiv(s->rho, d);
+  set_alpha(s, cdiv(s->rho, d));
 }
 // ||s|| (t = ||s||^2) and the half-step convergence test;
 __device__ __forceinline__ void finish_s(KState* s, const double (&t)[1]) {
@@ -132,78 +153,62 @@ __device__ __forceinline__ void finish_s(KState* s, const double (&t)[1]) {
     s->skip = 1;
   }
 }
-// omega = (t^H s)/(t^H t) (tt = t^H s, t^H t) with its breakdown tests.
-__device__ __forceinline__ void finish_omega(KState* s, const double (&tt)[3]) {
+// omega = (t^H s)/(t^H t) (tt = t^H s, t^H t) with its breakdown tests:
+// the flag that ends the iteration (4 breakdown, 5 not finite), or -1 and
+// omega in om.
+__device__ __forceinline__ int omega_step(const double (&tt)[3], double2& om) {
   const double2 ts = make_double2(tt[0], tt[1]);
   const double t2 = tt[2];
-  if (!(t2 > 0) || !cfinite(ts)) {
-    s->flag = (t2 == 0) ? 4 : 5;
+  if (!(t2 > 0) || !cfinite(ts)) return (t2 == 0) ? 4 : 5;
+  om = make_double2(ts.x / t2, ts.y / t2);
+  return cz(om) ? 4 : -1;
+}
+__device__ __forceinline__ void finish_omega(KState* s, const double (&tt)[3]) {
+  double2 om;
+  const int f = omega_step(tt, om);
+  if (f >= 0) {
+    s->flag = f;
     s->skip = 1;
     return;
   }
-  const double2 om = make_double2(ts.x / t2, ts.y / t2);
-  if (cz(om)) {
-    s->flag = 4;
-    s->skip = 1;
-    return;
-  }
-  s->omega = om;
+  set_omega(s, om);
 }
 
 // Folded steps (vs_pipeline.cuh XFuse): a two-level x pass left nb per-CTA
-// partial sums (NV each) of right-hand side blockIdx.x at part + blockIdx.x *
-// pstride; one CTA of kFinThreads adds them in a fixed order (each thread a
-// few partials, loaded together, then the warp and CTA trees) and takes the
-// scalar step.  (One warp walking all partials waited on one L2 load per
-// partial: 5-8 us per step.)
+// partial sums (NV slots each, slot form V) of a right-hand side at part; a
+// CTA of kFinThreads adds them in a fixed order (each thread a few slots, all
+// loaded before the first add, then the warp and CTA trees; float-float for
+// c64), so every CTA that adds the same slots gets the same bits; thread 0
+// widens the totals to double, and every thread gets them in tot.  (One warp
+// walking all partials waited on one L2 load per partial: 5-8 us per step.)
 constexpr int kFinThreads = 256;
-template <int NV>
+static_assert(kFinThreads == kRedThreads, "the merged kernels add partials with their own CTAs");
+template <int NV, typename V>
 __device__ __forceinline__ void sum_cta_partials(const double* __restrict__ part, int nb, double (&tot)[NV]) {
-  __shared__ double sm[NV][kFinThreads / 32];
-  __shared__ double st[NV];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    double x = 0;
-#pragma unroll 4
-    for (int b = threadIdx.x; b < nb; b += kFinThreads) x += part[b * NV + k];
-    x = warp_sum<false>(x);
-    if (lane == 0) sm[k][warp] = x;
-  }
-  __syncthreads();
-  if (warp == 0) {
+  __shared__ double slot[NV];
+  V x[NV];
+  slot_sums<NV, 4, false>(part, nb, (int)threadIdx.x, kFinThreads, x);
+  cta_partials<NV>(x, slot);  // thread 0 writes the CTA's sums in slot form
+  if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      const double y = warp_sum<false>(lane < kFinThreads / 32 ? sm[k][lane] : 0.0);
-      if (lane == 0) st[k] = y;
+      V y;
+      get_slot<false>(slot + k, y);
+      slot[k] = widen(y);
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int k = 0; k < NV; ++k) tot[k] = st[k];
+  for (int k = 0; k < NV; ++k) tot[k] = slot[k];
 }
+template <typename T>
 __global__ void __launch_bounds__(kFinThreads) k_fin_alpha(KState* states, const double* part, int64_t pstride,
                                                            int nb) {
   KState* s = states + blockIdx.x;
   if (s->skip) return;
   double t[2];
-  sum_cta_partials<2>(part + blockIdx.x * pstride, nb, t);
+  sum_cta_partials<2, SlotV<T>>(part + blockIdx.x * pstride, nb, t);
   if (threadIdx.x == 0) finish_alpha(s, t);
-}
-__global__ void __launch_bounds__(kFinThreads) k_fin_s(KState* states, const double* part, int64_t pstride, int nb) {
-  KState* s = states + blockIdx.x;
-  if (s->skip) return;
-  double t[1];
-  sum_cta_partials<1>(part + blockIdx.x * pstride, nb, t);
-  if (threadIdx.x == 0) finish_s(s, t);
-}
-__global__ void __launch_bounds__(kFinThreads) k_fin_omega(KState* states, const double* part, int64_t pstride,
-                                                           int nb) {
-  KState* s = states + blockIdx.x;
-  if (s->skip) return;
-  double t[3];
-  sum_cta_partials<3>(part + blockIdx.x * pstride, nb, t);
-  if (threadIdx.x == 0) finish_omega(s, t);
 }
 
 // rho = rt^H r ; beta = (rho/rho_prev)(alpha/omega)
@@ -211,20 +216,23 @@ template <typename T>
 __global__ void __launch_bounds__(kRedThreads) k_bicg_rho(const cplx_t<T>* __restrict__ rt,
                                                          const cplx_t<T>* __restrict__ r, int64_t n,
                                                          KState* states) {
+  using C = cplx_t<T>;
   KState* s = states + blockIdx.y;
   if (s->skip) return;
   rt += blockIdx.y * n; r += blockIdx.y * n;
   Acc<T> a;
-  GRID_LOOP4(i, n) a.dot(rt[i], r[i]);
-  double v[2] = {a.value().x, a.value().y}, t[2];
-  if (grid_reduce<2, std::is_same<T, float>::value>(v, s->partials, &s->counter, t) && threadIdx.x == 0) {
+  grid_chunks(n, [&](int64_t i) { return Loaded<C, 2>{{rt[i], r[i]}}; },
+              [&](int64_t, const Loaded<C, 2>& l) { a.dot(l.e[0], l.e[1]); });
+  const SlotV<T> v[2] = {a.vre(), a.vim()};
+  double t[2];
+  if (grid_reduce<2>(v, s->partials, &s->counter, t) && threadIdx.x == 0) {
     const double2 rho = make_double2(t[0], t[1]);
     if (cz(rho) || !cfinite(rho)) {
       s->flag = cfinite(rho) ? 4 : 5;
       s->skip = 1;
       return;
     }
-    if (s->iter2 > 0) s->beta = cmul(cdiv(rho, s->rho_prev), cdiv(s->alpha, s->omega));
+    if (s->iter2 > 0) set_beta(s, cmul(cdiv(rho, s->rho_prev), cdiv(s->alpha, s->omega)));
     s->rho = rho;
   }
 }
@@ -238,11 +246,12 @@ __global__ void k_bicg_p(cplx_t<T>* __restrict__ p, const cplx_t<T>* __restrict_
   if (s->skip) return;
   p += blockIdx.y * n; r += blockIdx.y * n; v += blockIdx.y * n;
   if (s->iter2 == 0) {
-    GRID_LOOP4(i, n) p[i] = r[i];
+    grid_chunks(n, [&](int64_t i) { return r[i]; }, [&](int64_t i, C x) { p[i] = x; });
     return;
   }
-  const C beta = ccast<C>(s->beta), om = ccast<C>(s->omega);
-  GRID_LOOP4(i, n) p[i] = cfma(beta, csub(p[i], cmul(om, v[i])), r[i]);
+  const C beta = scal<C>(s->beta, s->beta32), om = scal<C>(s->omega, s->omega32);
+  grid_chunks(n, [&](int64_t i) { return Loaded<C, 3>{{p[i], v[i], r[i]}}; },
+              [&](int64_t i, const Loaded<C, 3>& l) { p[i] = cfma(beta, csub(l.e[0], cmul(om, l.e[1])), l.e[2]); });
 }
 
 // alpha = rho / (rt^H v)
@@ -250,14 +259,16 @@ template <typename T>
 __global__ void __launch_bounds__(kRedThreads) k_bicg_alpha(const cplx_t<T>* __restrict__ rt,
                                                            const cplx_t<T>* __restrict__ v, int64_t n,
                                                            KState* states) {
+  using C = cplx_t<T>;
   KState* s = states + blockIdx.y;
   if (s->skip) return;
   rt += blockIdx.y * n; v += blockIdx.y * n;
   Acc<T> a;
-  GRID_LOOP4(i, n) a.dot(rt[i], v[i]);
-  double w[2] = {a.value().x, a.value().y}, t[2];
-  if (grid_reduce<2, std::is_same<T, float>::value>(w, s->partials, &s->counter, t) && threadIdx.x == 0)
-    finish_alpha(s, t);
+  grid_chunks(n, [&](int64_t i) { return Loaded<C, 2>{{rt[i], v[i]}}; },
+              [&](int64_t, const Loaded<C, 2>& l) { a.dot(l.e[0], l.e[1]); });
+  const SlotV<T> w[2] = {a.vre(), a.vim()};
+  double t[2];
+  if (grid_reduce<2>(w, s->partials, &s->counter, t) && threadIdx.x == 0) finish_alpha(s, t);
 }
 
 // s = r - alpha v ; ||s|| ; half-step convergence test
@@ -268,16 +279,17 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_s(cplx_t<T>* __restrict__ 
   KState* s = states + blockIdx.y;
   if (s->skip) return;
   sv += blockIdx.y * n; r += blockIdx.y * n; v += blockIdx.y * n;
-  const C al = ccast<C>(s->alpha);
+  const C al = scal<C>(s->alpha, s->alpha32);
   Acc<T> a;
-  GRID_LOOP4(i, n) {
-    const C x = csub(r[i], cmul(al, v[i]));
-    sv[i] = x;
-    a.norm2(x);
-  }
-  double w[1] = {a.value().x}, t[1];
-  if (grid_reduce<1, std::is_same<T, float>::value>(w, s->partials, &s->counter, t) && threadIdx.x == 0)
-    finish_s(s, t);
+  grid_chunks(n, [&](int64_t i) { return Loaded<C, 2>{{r[i], v[i]}}; },
+              [&](int64_t i, const Loaded<C, 2>& l) {
+                const C x = csub(l.e[0], cmul(al, l.e[1]));
+                sv[i] = x;
+                a.norm2(x);
+              });
+  const SlotV<T> w[1] = {a.vre()};
+  double t[1];
+  if (grid_reduce<1>(w, s->partials, &s->counter, t) && threadIdx.x == 0) finish_s(s, t);
 }
 
 // x += alpha ph when the half step converged (runs regardless of skip).
@@ -288,19 +300,56 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_xhalf(cplx_t<T>* __restric
   using C = cplx_t<T>;
   KState* s = states + blockIdx.y;
   __shared__ int s_go;
-  __shared__ bool s_last;
   if (threadIdx.x == 0) s_go = s->half_pending;
   __syncthreads();
   if (!s_go) return;
   x += blockIdx.y * n; ph += blockIdx.y * n;
-  const C al = ccast<C>(s->alpha);
-  GRID_LOOP4(i, n) x[i] = cfma(al, ph[i], x[i]);
+  const C al = scal<C>(s->alpha, s->alpha32);
+  grid_chunks(n, [&](int64_t i) { return Loaded<C, 2>{{x[i], ph[i]}}; },
+              [&](int64_t i, const Loaded<C, 2>& l) { x[i] = cfma(al, l.e[1], l.e[0]); });
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
-    const unsigned t = atomicAdd(&s->counter, 1u);
-    s_last = (t == gridDim.x - 1);
-    if (s_last) {
+    if (atomicAdd(&s->counter, 1u) == gridDim.x - 1) {
+      s->half_pending = 0;
+      s->counter = 0;
+    }
+  }
+}
+
+// Folded steps, after the second preconditioner apply's forward x pass left
+// the partial sums of ||s||^2 at part (nb per right-hand side): every CTA
+// adds them (same order, same bits) and its thread 0 takes the half-step
+// test; every CTA adds its share of alpha ph to x when the half step
+// converged, and the last CTA to finish -- after every CTA has read the skip
+// flag -- writes the half-step state (finish_s).
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_bicg_shalf(cplx_t<T>* __restrict__ x,
+                                                           const cplx_t<T>* __restrict__ ph, int64_t n,
+                                                           KState* states, const double* __restrict__ part,
+                                                           int64_t pstride, int nb) {
+  using C = cplx_t<T>;
+  KState* s = states + blockIdx.y;
+  __shared__ int s_conv;
+  if (s->skip) return;
+  double t[1];
+  sum_cta_partials<1, SlotV<T>>(part + blockIdx.y * pstride, nb, t);
+  if (threadIdx.x == 0) {
+    const double res = sqrt(t[0]);
+    s_conv = isfinite(res) && res <= s->tol_abs;
+  }
+  __syncthreads();
+  if (s_conv) {
+    x += blockIdx.y * n; ph += blockIdx.y * n;
+    const C al = scal<C>(s->alpha, s->alpha32);
+    grid_chunks(n, [&](int64_t i) { return Loaded<C, 2>{{x[i], ph[i]}}; },
+                [&](int64_t i, const Loaded<C, 2>& l) { x[i] = cfma(al, l.e[1], l.e[0]); });
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&s->counter, 1u) == gridDim.x - 1) {
+      finish_s(s, t);
       s->half_pending = 0;
       s->counter = 0;
     }
@@ -312,45 +361,89 @@ template <typename T>
 __global__ void __launch_bounds__(kRedThreads) k_bicg_omega(const cplx_t<T>* __restrict__ t,
                                                            const cplx_t<T>* __restrict__ sv, int64_t n,
                                                            KState* states) {
+  using C = cplx_t<T>;
   KState* s = states + blockIdx.y;
   if (s->skip) return;
   t += blockIdx.y * n; sv += blockIdx.y * n;
   Acc<T> a, b;
-  GRID_LOOP4(i, n) {
-    a.dot(t[i], sv[i]);
-    b.norm2(t[i]);
-  }
-  double w[3] = {a.value().x, a.value().y, b.value().x}, tt[3];
-  if (grid_reduce<3, std::is_same<T, float>::value>(w, s->partials, &s->counter, tt) && threadIdx.x == 0)
-    finish_omega(s, tt);
+  grid_chunks(n, [&](int64_t i) { return Loaded<C, 2>{{t[i], sv[i]}}; },
+              [&](int64_t, const Loaded<C, 2>& l) {
+                a.dot(l.e[0], l.e[1]);
+                b.norm2(l.e[0]);
+              });
+  const SlotV<T> w[3] = {a.vre(), a.vim(), b.vre()};
+  double tt[3];
+  if (grid_reduce<3>(w, s->partials, &s->counter, tt) && threadIdx.x == 0) finish_omega(s, tt);
 }
 
 // x += alpha ph + omega sh ; r = s - omega t ; ||r|| ; full-step test ; and,
 // when the iteration continues, the next rho = rt^H r with its breakdown test
-// and beta = (rho_new/rho)(alpha/omega) (the first rho comes from k_bicg_rho)
+// and beta = (rho_new/rho)(alpha/omega) (the first rho comes from k_bicg_rho).
+// omega: from the state (k_bicg_omega), or, with folded steps (opart
+// non-null), from the partial sums of t^H s and t^H t that the matvec's
+// inverse x pass left at opart (nb per right-hand side), added by every CTA
+// in the same order and divided by its thread 0; a breakdown there ends the
+// iteration (every CTA returns, the last to finish writes the flag), else the
+// last CTA stores omega with the rest.
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* __restrict__ x, cplx_t<T>* __restrict__ r,
                                                         const cplx_t<T>* __restrict__ ph,
                                                         const cplx_t<T>* __restrict__ sh,
                                                         const cplx_t<T>* __restrict__ sv,
                                                         const cplx_t<T>* __restrict__ t,
-                                                        const cplx_t<T>* __restrict__ rt, int64_t n, KState* states) {
+                                                        const cplx_t<T>* __restrict__ rt, int64_t n, KState* states,
+                                                        const double* __restrict__ opart, int64_t pstride, int nb) {
   using C = cplx_t<T>;
   KState* s = states + blockIdx.y;
+  __shared__ double2 s_om;
+  __shared__ float2 s_om32;
+  __shared__ int s_flag;
   if (s->skip) return;
+  if (opart) {
+    double tt[3];
+    sum_cta_partials<3, SlotV<T>>(opart + blockIdx.y * pstride, nb, tt);
+    if (threadIdx.x == 0) {
+      double2 om = make_double2(0, 0);
+      s_flag = omega_step(tt, om);
+      s_om = om;
+      s_om32 = to_f2(om);
+    }
+    __syncthreads();
+    if (s_flag >= 0) {
+      // every CTA sees the breakdown; the last one to count in writes it
+      // (no state is written while a CTA may still read the skip flag)
+      if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&s->counter, 1u) == gridDim.x - 1) {
+          s->flag = s_flag;
+          s->skip = 1;
+          s->counter = 0;
+        }
+      }
+      return;
+    }
+  } else if (threadIdx.x == 0) {
+    s_om = s->omega;
+    s_om32 = s->omega32;
+  }
+  __syncthreads();
   const int64_t o = blockIdx.y * n;
   x += o; r += o; ph += o; sh += o; sv += o; t += o; rt += o;
-  const C al = ccast<C>(s->alpha), om = ccast<C>(s->omega);
+  const C al = scal<C>(s->alpha, s->alpha32), om = scal<C>(s_om, s_om32);
   Acc<T> a, d;
-  GRID_LOOP4(i, n) {
-    x[i] = cfma(om, sh[i], cfma(al, ph[i], x[i]));
-    const C ri = csub(sv[i], cmul(om, t[i]));
-    r[i] = ri;
-    a.norm2(ri);
-    d.dot(rt[i], ri);
-  }
-  double w[3] = {a.value().x, d.value().x, d.value().y}, tt[3];
-  if (grid_reduce<3, std::is_same<T, float>::value>(w, s->partials, &s->counter, tt) && threadIdx.x == 0) {
+  grid_chunks(n, [&](int64_t i) { return Loaded<C, 6>{{x[i], ph[i], sh[i], sv[i], t[i], rt[i]}}; },
+              [&](int64_t i, const Loaded<C, 6>& l) {
+                x[i] = cfma(om, l.e[2], cfma(al, l.e[1], l.e[0]));
+                const C ri = csub(l.e[3], cmul(om, l.e[4]));
+                r[i] = ri;
+                a.norm2(ri);
+                d.dot(l.e[5], ri);
+              });
+  const SlotV<T> w[3] = {a.vre(), d.vre(), d.vim()};
+  double tt[3];
+  if (grid_reduce<3>(w, s->partials, &s->counter, tt) && threadIdx.x == 0) {
+    const double2 omd = s_om;
+    set_omega(s, omd);
     const double res = sqrt(tt[0]);
     const int k = s->iter2 + 2;
     if (k < s->resvec_cap) s->resvec[k] = res * s->res_scale;
@@ -381,7 +474,7 @@ __global__ void __launch_bounds__(kRedThreads) k_bicg_xr(cplx_t<T>* __restrict__
         s->flag = cfinite(rho) ? 4 : 5;
         s->skip = 1;
       } else {
-        s->beta = cmul(cdiv(rho, s->rho), cdiv(s->alpha, s->omega));
+        set_beta(s, cmul(cdiv(rho, s->rho), cdiv(s->alpha, omd)));
         s->rho = rho;
       }
     }
@@ -394,9 +487,10 @@ __global__ void __launch_bounds__(kRedThreads) k_norm(const cplx_t<T>* u, int64_
   KState* s = states + blockIdx.y;
   u += blockIdx.y * n;
   Acc<T> a;
-  GRID_LOOP(i, n) a.norm2(u[i]);
-  double w[1] = {a.value().x}, t[1];
-  if (grid_reduce<1, std::is_same<T, float>::value>(w, s->partials, &s->counter, t) && threadIdx.x == 0) out[blockIdx.y] = sqrt(t[0]);
+  grid_chunks(n, [&](int64_t i) { return u[i]; }, [&](int64_t, cplx_t<T> x) { a.norm2(x); });
+  const SlotV<T> w[1] = {a.vre()};
+  double t[1];
+  if (grid_reduce<1>(w, s->partials, &s->counter, t) && threadIdx.x == 0) out[blockIdx.y] = sqrt(t[0]);
 }
 
 template <typename T>
@@ -420,8 +514,9 @@ __global__ void __launch_bounds__(kRedThreads) k_resid64(const double2* b, const
     r[i] = v;
     a.norm2(v);
   }
-  double w[1] = {a.value().x}, t[1];
-  if (grid_reduce<1, false>(w, s->partials, &s->counter, t) && threadIdx.x == 0) out[blockIdx.y] = sqrt(t[0]);
+  const double w[1] = {a.vre()};
+  double t[1];
+  if (grid_reduce<1>(w, s->partials, &s->counter, t) && threadIdx.x == 0) out[blockIdx.y] = sqrt(t[0]);
 }
 
 // r32 = r64 * sc[rhs]
@@ -503,15 +598,17 @@ static std::vector<double> read_scal(KrylovWork& w, int nrhs, cudaStream_t st) {
 // first preconditioner apply, 7..11 after the matvec's five, 12 after the
 // alpha / s / half-step kernels, 13..17 and 18..22 the second apply and
 // matvec, 23 after the omega / x, r kernels; with folded steps, 24 after the
-// ||s|| step and the half-step update (between 13 and 14).
+// half-step kernel (between 13 and 14).
 constexpr int kIterMarks = 25;
 
 // BiCGSTAB's vector steps folded into the x passes (XFuse): the
 // preconditioner's forward x pass forms p (first apply) and s with ||s||^2
 // (second apply), the matvec's inverse x pass adds rt^H v (first) and t^H s,
 // t^H t (second); the partial sums of nb_mv / nb_pr CTAs per right-hand side
-// go to part (pstride doubles each), and one-CTA kernels take the scalar
-// steps.  Four streaming vector kernels of the iteration are gone.
+// go to part (pstride doubles each).  A one-CTA kernel takes alpha; the
+// half-step test and omega are taken by every CTA of the kernels that use
+// them (k_bicg_shalf, k_bicg_xr).  Four streaming vector kernels and two
+// scalar kernels of the iteration are gone.
 struct FoldPlan {
   int nb_mv = 0, nb_pr = 0;
   int64_t pstride = 0;
@@ -588,13 +685,15 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
     f.part = fold->part;
     f.pstride = fold->pstride;
     XFuse<T> fp = f, fsv = f, fd = f, fo = f;
+    // the passes read the scalars in their own precision (float copies for c64)
+    constexpr bool c64 = std::is_same<T, float>::value;
     fp.kind = XF_GATHER_P;
-    fp.off_a = (int)offsetof(KState, beta);
-    fp.off_b = (int)offsetof(KState, omega);
+    fp.off_a = c64 ? (int)offsetof(KState, beta32) : (int)offsetof(KState, beta);
+    fp.off_b = c64 ? (int)offsetof(KState, omega32) : (int)offsetof(KState, omega);
     fp.off_iter = (int)offsetof(KState, iter2);
     fp.u = r; fp.v = v; fp.w = p;
     fsv.kind = XF_GATHER_S;
-    fsv.off_a = (int)offsetof(KState, alpha);
+    fsv.off_a = c64 ? (int)offsetof(KState, alpha32) : (int)offsetof(KState, alpha);
     fsv.u = r; fsv.v = v; fsv.w = sv;
     fd.kind = XF_SCATTER_DOT;
     fd.u = rt;
@@ -612,26 +711,25 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
       matvec_pass<T>(op, ph, v, nrhs, mode, skip, st, pass, ss, rgp(w), pass == 4 ? &fd : nullptr);
       mark(7 + pass);
     }
-    k_fin_alpha<<<nrhs, kFinThreads, 0, st>>>(s, fold->part, fold->pstride, fold->nb_mv);
+    k_fin_alpha<T><<<nrhs, kFinThreads, 0, st>>>(s, fold->part, fold->pstride, fold->nb_mv);
     mark(12);
     // s = r - alpha v and ||s||^2 in the second apply's forward x pass; the
-    // half-step test, then the rest of the apply
+    // half-step test (and x += alpha ph if it converged), then the rest of
+    // the apply
     prec_apply_pass<T>(*pr, sv, sh, nrhs, skip, st, 0, ss, &fsv);
     mark(13);
-    k_fin_s<<<nrhs, kFinThreads, 0, st>>>(s, fold->part, fold->pstride, fold->nb_pr);
-    k_bicg_xhalf<T><<<gr, kRedThreads, 0, st>>>(x, ph, n, s);
+    k_bicg_shalf<T><<<gr, kRedThreads, 0, st>>>(x, ph, n, s, fold->part, fold->pstride, fold->nb_pr);
     mark(24);
     for (int pass = 1; pass < 5; ++pass) {
       prec_apply_pass<T>(*pr, sv, sh, nrhs, skip, st, pass, ss);
       mark(13 + pass);
     }
-    // t^H s, t^H t in the matvec's inverse x pass; omega
+    // t^H s, t^H t in the matvec's inverse x pass; omega, x and r
     for (int pass = 0; pass < 5; ++pass) {
       matvec_pass<T>(op, sh, t, nrhs, mode, skip, st, pass, ss, rgp(w), pass == 4 ? &fo : nullptr);
       mark(18 + pass);
     }
-    k_fin_omega<<<nrhs, kFinThreads, 0, st>>>(s, fold->part, fold->pstride, fold->nb_mv);
-    k_bicg_xr<T><<<gr, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, rt, n, s);
+    k_bicg_xr<T><<<gr, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, rt, n, s, fold->part, fold->pstride, fold->nb_mv);
     mark(23);
     VS_LAUNCH_CHECK();
     return;
@@ -646,7 +744,7 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
   mark(12);
   prec_then_matvec(sv, sh, t, 13);
   k_bicg_omega<T><<<gr, kRedThreads, 0, st>>>(t, sv, n, s);
-  k_bicg_xr<T><<<gr, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, rt, n, s);
+  k_bicg_xr<T><<<gr, kRedThreads, 0, st>>>(x, r, ph, sh, sv, t, rt, n, s, nullptr, 0, 0);
   mark(23);
   VS_LAUNCH_CHECK();
 }
@@ -668,11 +766,11 @@ static void add_iteration_profile(const cudaEvent_t* ev, int iters, SolveProfile
 
 // Kernels in one bicg_iteration: 6 solver kernels, 2 matvecs of 5 passes, and
 // 2 preconditioner applies (or 2 copies without preconditioner); with folded
-// steps 5 solver kernels (the three one-CTA scalar steps, x after a
-// converged half step, x and r) and 20 passes.
+// steps 3 solver kernels (alpha; the half-step test with x after a converged
+// half step; omega with x and r) and 20 passes.
 template <typename T>
 static int kernels_per_iteration(const vs_prec* pr, bool folded = false) {
-  return folded ? 25 : 6 + 10 + (pr ? 2 * prec_launches<T>(*pr) : 2);
+  return folded ? 23 : 6 + 10 + (pr ? 2 * prec_launches<T>(*pr) : 2);
 }
 
 // BiCGSTAB on w.x (initial guesses already there) with initial residuals in
@@ -1510,8 +1608,9 @@ __global__ void __launch_bounds__(kRedThreads) k_gm_norm(const cplx_t<T>* w, int
   if (st->skip) return;
   Acc<T> a;
   GRID_LOOP(i, n) a.norm2(w[i]);
-  double v[1] = {a.value().x}, t[1];
-  if (grid_reduce<1, std::is_same<T, float>::value>(v, partials, counter, t) && threadIdx.x == 0) *Hk1 = make_double2(sqrt(t[0]), 0.0);
+  const SlotV<T> v[1] = {a.vre()};
+  double t[1];
+  if (grid_reduce<1>(v, partials, counter, t) && threadIdx.x == 0) *Hk1 = make_double2(sqrt(t[0]), 0.0);
 }
 
 // V_{k+1} = w / H(k+1,k)

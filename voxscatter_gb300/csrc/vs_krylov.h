@@ -8,6 +8,7 @@ namespace vs {
 // Scalars of one Krylov iteration, resident in device memory.
 struct KState {
   double2 rho, rho_prev, alpha, omega, beta;
+  float2 alpha32, omega32, beta32;  // float copies for the c64 kernels (written with the doubles)
   double tol_abs, res, res_scale;
   double best_res;  // smallest full-step residual so far (stagnation guard)
   double* partials;

@@ -22,8 +22,10 @@ struct DiagArg {
 // and the scatter of the matvec's inverse x pass adds the inner products of
 // the vector it writes (XF_SCATTER_DOT: rt^H v; XF_SCATTER_OMEGA: t^H s and
 // t^H t).  Scalars of right-hand side r are read at sbase + r * sstride +
-// offset (bytes); each CTA writes its NV partial sums to part + r * pstride +
-// blockIdx.x * NV, which the solver adds up afterwards.
+// offset (bytes), in the storage precision (the solver keeps a float copy of
+// each scalar for c64); each CTA writes its NV partial sums to part + r *
+// pstride + blockIdx.x * NV (float-float pairs for c64, doubles for c128),
+// which the solver adds up afterwards.
 enum XFuseKind { XF_NONE = 0, XF_GATHER_P = 1, XF_GATHER_S = 2, XF_SCATTER_DOT = 3, XF_SCATTER_OMEGA = 4 };
 
 template <typename T>
@@ -39,11 +41,7 @@ struct XFuse {
   double* part;
   int64_t pstride;
   __device__ __forceinline__ C scalar(int rhs, int off) const {
-    const double2 d = *reinterpret_cast<const double2*>(sbase + rhs * sstride + off);
-    C c;
-    c.x = (decltype(c.x))d.x;
-    c.y = (decltype(c.y))d.y;
-    return c;
+    return *reinterpret_cast<const C*>(sbase + rhs * sstride + off);
   }
 };
 

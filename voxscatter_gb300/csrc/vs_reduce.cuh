@@ -6,6 +6,8 @@
 #pragma once
 #include "vs_common.cuh"
 
+#include <type_traits>
+
 namespace vs {
 
 // FP64 double-double accumulation (TwoSum / TwoProd by fma) for the c128 path.
@@ -34,9 +36,10 @@ __device__ __forceinline__ DD dd_fma(DD a, double x, double y) {
 // Accumulators.  c64 inputs: every product of two floats is formed exactly as
 // a float pair (p = a*b rounded, e = fma(a, b, -p)) and added into a
 // float-float sum by TwoSum (Knuth), about 48 bits of significand for the
-// few elements a thread visits; the pair is widened to double once, and the
-// grid-wide sums are taken in double.  This keeps compensated inner products
-// without a double-precision FMA per element.
+// few elements a thread visits; the CTA and grid sums add the pairs
+// float-float as well, and one thread widens the total to double for the
+// scalar step.  This keeps compensated inner products without FP64 work per
+// element or per thread.
 __device__ __forceinline__ void ff_add(float& hi, float& lo, float b) {
   const float s = __fadd_rn(hi, b);
   const float bb = __fsub_rn(s, hi);
@@ -50,9 +53,18 @@ __device__ __forceinline__ void ff_fma(float& hi, float& lo, float a, float b) {
   ff_add(hi, lo, pr);
   lo = __fadd_rn(lo, e);
 }
+// A float-float value (hi + lo, not necessarily renormalised).
+struct FF2 {
+  float hi, lo;
+};
+
 template <typename T>
 struct Acc {
   float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+  // the sums in their own form (float-float here, double for c128), for the
+  // CTA and grid sums below
+  __device__ __forceinline__ FF2 vre() const { return FF2{rh, rl}; }
+  __device__ __forceinline__ FF2 vim() const { return FF2{ih, il}; }
   __device__ __forceinline__ void dot(cplx_t<T> u, cplx_t<T> v) {  // += conj(u) v
     ff_fma(rh, rl, u.x, v.x);
     ff_fma(rh, rl, u.y, v.y);
@@ -81,6 +93,8 @@ struct Acc<double> {
     re = dd_fma(re, u.y, u.y);
   }
   __device__ __forceinline__ double2 value() const { return make_double2(re.hi + re.lo, im.hi + im.lo); }
+  __device__ __forceinline__ double vre() const { return re.hi + re.lo; }
+  __device__ __forceinline__ double vim() const { return im.hi + im.lo; }
 };
 
 // ff (float-float) sum of two ff values: TwoSum of the leading parts, the
@@ -116,23 +130,102 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 
+// Warp sum (xor tree) of float-float values, on the FP32 pipes only.
+__device__ __forceinline__ FF2 warp_sum(FF2 v) {
+#pragma unroll
+  for (int off = 16; off; off >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, v.hi, off), ol = __shfl_xor_sync(0xffffffffu, v.lo, off);
+    ff_add2(v.hi, v.lo, oh, ol);
+  }
+  return v;
+}
+
+__device__ __forceinline__ FF2 warp_sum_v(FF2 v) { return warp_sum(v); }
+__device__ __forceinline__ double warp_sum_v(double v) { return warp_sum<false>(v); }
+
+// A partial sum slot (8 bytes): float-float sums (the c64 solver's) are
+// stored there as float2 (hi, lo), doubles as doubles.  GB300 runs FP64 at a
+// small fraction of its FP32 rate, so c64 sums stay float-float from the
+// per-thread accumulators to the last slot, and only the one thread that
+// takes a scalar step widens them to double.
+__device__ __forceinline__ void put_slot(double* p, FF2 v) { *reinterpret_cast<float2*>(p) = make_float2(v.hi, v.lo); }
+__device__ __forceinline__ void put_slot(double* p, double v) { *p = v; }
+// CG: through L2 only (slots written by other CTAs of the same kernel)
+template <bool CG>
+__device__ __forceinline__ void get_slot(const double* p, FF2& v) {
+  const float2 f = CG ? __ldcg(reinterpret_cast<const float2*>(p)) : *reinterpret_cast<const float2*>(p);
+  v = FF2{f.x, f.y};
+}
+template <bool CG>
+__device__ __forceinline__ void get_slot(const double* p, double& v) {
+  v = CG ? __ldcg(p) : *p;
+}
+__device__ __forceinline__ void add_slot(FF2& a, FF2 b) { ff_add2(a.hi, a.lo, b.hi, b.lo); }
+__device__ __forceinline__ void add_slot(double& a, double b) { a += b; }
+__device__ __forceinline__ double widen(FF2 v) { return (double)v.hi + (double)v.lo; }
+__device__ __forceinline__ double widen(double v) { return v; }
+// The slot form of a precision's sums.
+template <typename T>
+using SlotV = typename std::conditional<std::is_same<T, float>::value, FF2, double>::type;
+
+// Per-thread sums x[k] of slots b * NV + k for b = t0, t0 + nt, ... < nb, in
+// that order; U slots' loads are issued before their adds.
+template <int NV, int U, bool CG, typename V>
+__device__ __forceinline__ void slot_sums(const double* __restrict__ part, int nb, int t0, int nt, V (&x)[NV]) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) x[k] = V{};
+  for (int b0 = t0; b0 < nb; b0 += U * nt) {
+    V v[U][NV];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int k = 0; k < NV; ++k)
+        if (b0 + u * nt < nb) get_slot<CG>(part + (int64_t)(b0 + u * nt) * NV + k, v[u][k]);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int k = 0; k < NV; ++k)
+        if (b0 + u * nt < nb) add_slot(x[k], v[u][k]);
+  }
+}
+
 // Sums NV per-thread values over the CTA (all threads must call it) and
 // writes them to out[0..NV-1] (thread 0; blockDim.x a multiple of 32, at most
-// 1024 threads).  FF selects the float-float warp tree (c64 accumulators).
-template <int NV, bool FF>
-__device__ __forceinline__ void cta_partials(const double (&v)[NV], double* __restrict__ out) {
+// 1024 threads): float-float values by float-float warp trees into float2
+// slots, doubles by double trees.
+template <int NV>
+__device__ __forceinline__ void cta_partials(const FF2 (&v)[NV], double* out) {
+  __shared__ float2 sm[NV][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const FF2 x = warp_sum(v[k]);
+    if (lane == 0) sm[k][warp] = make_float2(x.hi, x.lo);
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const float2 y = lane < nw ? sm[k][lane] : make_float2(0.f, 0.f);
+      const FF2 x = warp_sum(FF2{y.x, y.y});
+      if (lane == 0) put_slot(out + k, x);
+    }
+  }
+}
+template <int NV>
+__device__ __forceinline__ void cta_partials(const double (&v)[NV], double* out) {
   __shared__ double sm[NV][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
-    const double x = warp_sum<FF>(v[k]);
+    const double x = warp_sum<false>(v[k]);
     if (lane == 0) sm[k][warp] = x;
   }
   __syncthreads();
   if (warp == 0) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      const double x = warp_sum<FF>(lane < nw ? sm[k][lane] : 0.0);
+      const double x = warp_sum<false>(lane < nw ? sm[k][lane] : 0.0);
       if (lane == 0) out[k] = x;
     }
   }

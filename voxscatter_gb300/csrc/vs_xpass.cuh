@@ -152,8 +152,8 @@ __global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && 
       }
     }
     if (a.fz.kind == XF_GATHER_S) {  // the CTA's ||s||^2 (every thread takes part)
-      const double w[1] = {acc.value().x};
-      cta_partials<1, std::is_same<T, float>::value>(w, a.fz.part + rhs * a.fz.pstride + blockIdx.x);
+      const decltype(acc.vre()) w[1] = {acc.vre()};
+      cta_partials<1>(w, a.fz.part + rhs * a.fz.pstride + blockIdx.x);
     }
   } else {
     const C* t1 = a.t1 + t1off;
@@ -247,13 +247,13 @@ __global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && 
       }
     }
     // the CTA's inner products (every thread takes part)
-    constexpr bool FF = std::is_same<T, float>::value;
+    using V = decltype(acc.vre());
     if (fk == XF_SCATTER_DOT) {
-      const double w[2] = {acc.value().x, acc.value().y};
-      cta_partials<2, FF>(w, a.fz.part + rhs * a.fz.pstride + (int64_t)blockIdx.x * 2);
+      const V w[2] = {acc.vre(), acc.vim()};
+      cta_partials<2>(w, a.fz.part + rhs * a.fz.pstride + (int64_t)blockIdx.x * 2);
     } else if (fk == XF_SCATTER_OMEGA) {
-      const double w[3] = {acc.value().x, acc.value().y, acc2.value().x};
-      cta_partials<3, FF>(w, a.fz.part + rhs * a.fz.pstride + (int64_t)blockIdx.x * 3);
+      const V w[3] = {acc.vre(), acc.vim(), acc2.vre()};
+      cta_partials<3>(w, a.fz.part + rhs * a.fz.pstride + (int64_t)blockIdx.x * 3);
     }
   }
 }
