@@ -30,8 +30,6 @@ __device__ __forceinline__ df df_make(float hi, float lo) {
   return r;
 }
 
-__device__ __forceinline__ double df_to_double(df a) { return (double)a.hi + (double)a.lo; }
-
 // hi + lo with |lo| <= ulp(hi)/2 from s + e (|e| small against s)
 __device__ __forceinline__ df df_renorm(float s, float e) {
   const float h = __fadd_rn(s, e);
@@ -74,16 +72,63 @@ __device__ __forceinline__ dfc cfma(dfc b, dfc c, dfc a) {
 __device__ __forceinline__ dfc cconj(dfc a) { return dfc{a.x, -a.y}; }
 template <> __device__ __forceinline__ dfc czero<dfc>() { return dfc{df(0.0), df(0.0)}; }
 
+// Conversions between FP64 storage and double-float from the bits, on the
+// integer and FP32 pipes: the FP64 conversions (and the FP64 subtraction
+// that forms lo) run on GB300's FP64 pipe, at a small fraction of its FP32
+// rate, and bound the double-float passes at loads and stores.
+//
+// The double-float nearest a double: hi = RN(d), lo = RN(d - hi), the same
+// bits as the FP64 conversions (round to nearest, ties to even).  Fast path
+// for d = 0 and for 2^-74 <= |d| < 2^126 (biased exponent 949..1149, where
+// hi and lo are normal floats); other values take the FP64 conversions.
+// From the 53-bit significand S of |d|: hi keeps its top 24 bits, rounded on
+// the other 29 (a carry out of the mantissa moves into the exponent field);
+// the rounding residual r = S mod 2^29 (less 2^29 if rounded up) is exact,
+// |r| <= 2^28, and lo = RN(r) 2^(e-52): r's two halves convert exactly
+// through the 1.5 * 2^23 mantissa trick and one FMA rounds their sum.
+__device__ __forceinline__ df df_from_double(double d) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(d);
+  const unsigned h = (unsigned)(bits >> 32), l = (unsigned)bits;
+  const unsigned eb = (h >> 20) & 0x7FFu;
+  if (eb - 949u <= 1149u - 949u) {
+    const unsigned sign = h & 0x80000000u;
+    const unsigned m23 = ((h & 0xFFFFFu) << 3) | (l >> 29);
+    const unsigned rem = l & 0x1FFFFFFFu;
+    const unsigned up = (rem > 0x10000000u ? 1u : 0u) | ((rem == 0x10000000u ? 1u : 0u) & m23);
+    const float hi = __uint_as_float(sign | (((eb - 896u) << 23) + m23 + up));
+    int r = (int)rem - (int)(up << 29);
+    if (sign) r = -r;
+    const float ra = __fsub_rn(__int_as_float(0x4B400000 + (r >> 14)), 12582912.0f);
+    const float rb = __fsub_rn(__int_as_float(0x4B400000 + (r & 0x3FFF)), 12582912.0f);
+    const float lo = __fmul_rn(__fmaf_rn(ra, 16384.0f, rb), __uint_as_float((eb - 948u) << 23));
+    return df_make(hi, lo);
+  }
+  if ((h & 0x7FFFFFFFu) == 0u && l == 0u) return df_make(__uint_as_float(h), 0.0f);  // +-0
+  return df(d);
+}
+// A float widened to double from its bits (exact; normal floats and zeros,
+// others by the FP64 conversion).
+__device__ __forceinline__ double double_from_float(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xFFu;
+  if (e - 1u < 254u)
+    return __hiloint2double((int)((b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3)), (int)(b << 29));
+  if ((b & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)b, 0);
+  return (double)f;
+}
+// hi + lo rounded to double: one FP64 addition
+__device__ __forceinline__ double df_store(df a) { return double_from_float(a.hi) + double_from_float(a.lo); }
+
 // storage (double2) <-> compute (dfc); identity for the native types
 template <typename K> __device__ __forceinline__ K to_compute(double2 v);
 template <> __device__ __forceinline__ double2 to_compute<double2>(double2 v) { return v; }
-template <> __device__ __forceinline__ dfc to_compute<dfc>(double2 v) { return dfc{df(v.x), df(v.y)}; }
+template <> __device__ __forceinline__ dfc to_compute<dfc>(double2 v) {
+  return dfc{df_from_double(v.x), df_from_double(v.y)};
+}
 template <typename K> __device__ __forceinline__ K to_compute(float2 v) { return v; }
 
 __device__ __forceinline__ double2 to_storage(double2 v, double2) { return v; }
-__device__ __forceinline__ double2 to_storage(dfc v, double2) {
-  return make_double2(df_to_double(v.x), df_to_double(v.y));
-}
+__device__ __forceinline__ double2 to_storage(dfc v, double2) { return make_double2(df_store(v.x), df_store(v.y)); }
 __device__ __forceinline__ float2 to_storage(float2 v, float2) { return v; }
 
 }  // namespace vs

@@ -230,6 +230,10 @@ template <typename T>
 void matvec(const vs_op& op, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, int mode, const int* skip,
             cudaStream_t st, int skip_stride = 0, const RhsGram* rg = nullptr);
 void ensure_scratch(vs_op& op, int nrhs, size_t elem_bytes);
+// Fills n complex values (c128 when dbl, else c64) with seeded values in
+// [-0.5, 0.5): the autotuners time the passes on data like a solve's (the
+// double-float kernels take a shorter path for zeros).
+void fill_tuning_data(void* x, int64_t n, bool dbl, cudaStream_t st);
 // Uploads a Gram per right-hand side (host, nrhs x gram_n complex with
 // gram_n = 1 or L*M*N, a column-major grid) to g64 / g32 at op's unknowns and
 // describes it in `out`.

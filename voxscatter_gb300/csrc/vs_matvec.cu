@@ -145,8 +145,8 @@ __global__ void __launch_bounds__(kThreads) k_strided(StridedArgs<T> a) {
   const int b1 = n * tx, tw = 2 * n * tx;
   load_twiddles(a.tw, n, tw);
   const int x0 = blockIdx.x * tx;
-  const int pa = blockIdx.y % a.na;
-  const int pb = blockIdx.y / a.na;
+  int pa, pb;
+  a.plane(pa, pb);
   const C* src = a.src + pa * a.s_a + pb * a.s_b + (int64_t)blockIdx.z * a.s_rhs;
   C* dst = a.dst + pa * a.d_a + pb * a.d_b + (int64_t)blockIdx.z * a.d_rhs;
   const int xl = threadIdx.x & (tx - 1), r0 = threadIdx.x >> lg_nl;
@@ -305,7 +305,10 @@ void launch_x_pass(const PipeArgs<T>& a, bool inverse, int mode, int nrhs, cudaS
 }
 
 template <typename T, bool INV>
-void launch_strided_pass(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st) {
+void launch_strided_pass(const StridedArgs<T>& args, int nplanes, int nrhs, cudaStream_t st) {
+  if (args.na < 1 || args.na > 65536 || nplanes > 65535) throw Error(VS_ERR_UNSUPPORTED, "strided pass: plane grid out of range");
+  StridedArgs<T> a = args;
+  a.na_mul = a.na >= 2 ? (unsigned)(((1ull << 32) + (uint64_t)a.na - 1) / (uint64_t)a.na) : 0u;
   if constexpr (std::is_same<T, double>::value) {
     if (a.two_level == 2 && strided_two_level_df(a, INV, nplanes, nrhs, st)) return;
   }
@@ -603,6 +606,24 @@ template void fft_strided<float, false>(float2*, int, int, int64_t, int, int64_t
 template void fft_strided<float, true>(float2*, int, int, int64_t, int, int64_t, int, int64_t, const FftAxis&, cudaStream_t);
 
 // ---- autotuning of the pass shapes -------------------------------------
+template <typename C>
+__global__ void k_fill_tuning(C* x, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    // a 32-bit integer hash (multiply-xorshift) of the index, per component
+    uint32_t h = (uint32_t)i * 0x9E3779B1u + 0x7F4A7C15u;
+    h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12;
+    uint32_t g = h * 0x297A2D39u; g ^= g >> 15;
+    x[i].x = (decltype(x[i].x))((int32_t)(h >> 8) - (1 << 23)) * (decltype(x[i].x))(1.0 / (1 << 24));
+    x[i].y = (decltype(x[i].y))((int32_t)(g >> 8) - (1 << 23)) * (decltype(x[i].y))(1.0 / (1 << 24));
+  }
+}
+void fill_tuning_data(void* x, int64_t n, bool dbl, cudaStream_t st) {
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), 8 * 152));
+  if (dbl) k_fill_tuning<double2><<<g, 256, 0, st>>>(static_cast<double2*>(x), n);
+  else k_fill_tuning<float2><<<g, 256, 0, st>>>(static_cast<float2*>(x), n);
+  VS_LAUNCH_CHECK();
+}
+
 // Times pass pairs (x forward+inverse, y forward+inverse, z) for each
 // candidate shape on scratch vectors and keeps the fastest; candidates whose
 // tiles exceed the shared-memory limit are skipped.
@@ -631,22 +652,28 @@ void autotune_op(vs_op& op, cudaStream_t st) {
   DevBuf xb, yb;
   xb.alloc(op.n3 * sizeof(C));
   yb.alloc(op.n3 * sizeof(C));
-  VS_CUDA(cudaMemsetAsync(xb.p, 0, op.n3 * sizeof(C), st));
+  fill_tuning_data(xb.p, op.n3, std::is_same<T, double>::value, st);
   const C* x = xb.as<C>();
   C* y = yb.as<C>();
   const size_t cs = sizeof(C);
   const size_t lim = 227 * 1024;
   PassShape& sh = op.shape[pi];
-  const int reps = std::is_same<T, float>::value ? 3 : 1;
+  const int reps = 3;
+  // two rounds over the candidates, each candidate's best time kept: the
+  // clocks may still be ramping up while the first candidates are timed
   auto best_of = [&](int* field, int lo, int hi, auto fits, auto run) {
-    float best = 1e30f;
+    float t[8];
+    for (int v = lo; v <= hi; ++v) t[v - lo] = 1e30f;
+    for (int round = 0; round < 2; ++round)
+      for (int v = lo; v <= hi; ++v) {
+        if (!fits(v)) continue;
+        *field = v;
+        t[v - lo] = std::min(t[v - lo], time_ms(st, reps, run));
+      }
     int arg = -1;
-    for (int v = lo; v <= hi; ++v) {
-      if (!fits(v)) continue;
-      *field = v;
-      const float t = time_ms(st, reps, run);
-      if (t < best) { best = t; arg = v; }
-    }
+    float best = 1e30f;
+    for (int v = lo; v <= hi; ++v)
+      if (fits(v) && t[v - lo] < best) { best = t[v - lo]; arg = v; }
     *field = arg;
   };
   sh.x_reg = 0;
@@ -656,12 +683,19 @@ void autotune_op(vs_op& op, cudaStream_t st) {
             matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 4);
           });
   // FP64 data: 2 is the two-level kernel in double-float arithmetic (where
-  // the length has it; its results agree with FP64 to a few units of 2^-48)
+  // the length has it; its results agree with FP64 to a few units of 2^-48).
+  // FP64 data times the whole matvec: the double-float x passes timed as a
+  // forward + inverse pair ranked differently from the same passes inside
+  // the pipeline.
   const int reg_hi = std::is_same<T, double>::value ? 2 : 1;
   best_of(&sh.x_reg, 0, reg_hi, [&](int v) { return v < 2 || x_df_available(op.P); },
           [&] {
-            matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 0);
-            matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 4);
+            if (std::is_same<T, double>::value) {
+              matvec<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st);
+            } else {
+              matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 0);
+              matvec_pass<T>(op, x, y, 1, VS_NOTRANSP, nullptr, st, 4);
+            }
           });
   sh.y_reg = 0;
   best_of(&sh.lg_tx_y, 1, 5, [&](int v) { return (2ull * op.Q * (1 << v) + op.Q) * cs <= lim; },

@@ -108,6 +108,18 @@ struct StridedArgs {
   int skip_stride;
   int two_level;  // 1: two-level register kernel (vs_spass.cuh) when the length has one;
                   // 2: the same in double-float arithmetic (FP64 data only)
+  unsigned na_mul;  // ceil(2^32 / na) for na >= 2, else 0 (set by launch_strided_pass)
+  // plane (pa, pb) of blockIdx.y = pa + na * pb.  A division by a runtime
+  // value goes through integer <-> float conversions, which GB300 runs on its
+  // narrow FP64 pipe; the multiply-high by ceil(2^32 / na) is exact for
+  // blockIdx.y < 2^16 and na <= 2^16 (the error of the reciprocal times
+  // blockIdx.y stays below 1/na).
+  __device__ __forceinline__ void plane(int& pa, int& pb) const {
+    const unsigned y = blockIdx.y;
+    const unsigned q = na_mul ? __umulhi(y, na_mul) : y;
+    pb = (int)q;
+    pa = (int)(y - q * (unsigned)na);
+  }
 };
 
 // Two-level x pass (vs_xpass.cuh); false when P has no instantiation.

@@ -48,7 +48,8 @@ __global__ void __launch_bounds__(z2_threads(R2, s2_tx<T, R2>())) k_s2(StridedAr
   K* tw = S + N * TX;
   for (int i = threadIdx.x; i < N; i += NT) tw[i] = to_compute<K>(__ldg(a.tw + i));
   const int x0 = blockIdx.x * TX;
-  const int pa = blockIdx.y % a.na, pb = blockIdx.y / a.na;
+  int pa, pb;
+  a.plane(pa, pb);
   const C* src = a.src + pa * a.s_a + pb * a.s_b + (int64_t)blockIdx.z * a.s_rhs;
   C* dst = a.dst + pa * a.d_a + pb * a.d_b + (int64_t)blockIdx.z * a.d_rhs;
   __syncthreads();

@@ -43,6 +43,11 @@ __device__ __forceinline__ cplx_t<T> x2_gather(const PipeArgs<T>& a, const cplx_
   return v;
 }
 
+// Component of x line `line` (< 3 MN) by two compares: a division by the
+// runtime MN goes through integer <-> float conversions, which GB300 runs on
+// its narrow FP64 pipe.
+__device__ __forceinline__ int comp_of(int line, int MN) { return (line >= MN) + (line >= 2 * MN); }
+
 // HO (inverse only): L <= (R1 R2 + 1) / 2, so the outputs n2 >=
 // lower_half_n2 are never scattered and never formed.
 template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>, bool HO = false>
@@ -72,7 +77,7 @@ __global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && 
     const bool fused = a.fz.kind == XF_GATHER_P || a.fz.kind == XF_GATHER_S;
     Acc<T> acc;
     if (act && line < nlines) {
-      const int c = line / MN, jk = line - c * MN;
+      const int c = comp_of(line, MN), jk = line - c * MN;
       const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
       if (fused) {
         // (only the preconditioner's forward pass folds a step, and its gather
@@ -176,7 +181,7 @@ __global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && 
     if (a.fz.kind == XF_SCATTER_DOT || a.fz.kind == XF_SCATTER_OMEGA) {
       const int pn1 = it % R1, pla = it / R1, pline = line0 + pla;
       if (it < R1 * NL && pline < nlines && pn1 < a.L) {
-        const int c = pline / MN, jk = pline - c * MN;
+        const int c = comp_of(pline, MN), jk = pline - c * MN;
         const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
         const C* fu = a.fz.u + (int64_t)rhs * a.n3;
         const C* xin = a.x + (int64_t)rhs * a.n3;
@@ -213,7 +218,7 @@ __global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && 
 #pragma unroll
       for (int j2 = 0; j2 < R2; ++j2) v[j2] = s[j2];
       reg_dft<R2, R2, 1, R1, true, K>(v, tw);
-      const int c = linea / MN, jk = linea - c * MN;
+      const int c = comp_of(linea, MN), jk = linea - c * MN;
       const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
       // the output never aliases the input or the solver's vectors: with the
       // pointers restrict-qualified the next element's loads need not wait
