@@ -76,67 +76,88 @@ __global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && 
     K v[R2];
     const bool fused = a.fz.kind == XF_GATHER_P || a.fz.kind == XF_GATHER_S;
     Acc<T> acc;
-    if (act && line < nlines) {
-      const int c = comp_of(line, MN), jk = line - c * MN;
-      const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
-      if (fused) {
-        // (only the preconditioner's forward pass folds a step, and its gather
-        // is plain: no diagonal or conjugation applies to the formed element)
-        // in chunks of X2C elements: indices, then the solver's vectors, then
-        // the formed elements written back, so a chunk's loads are in flight
-        // together (a store before the next element's loads would order them)
-        const int64_t off = (int64_t)rhs * a.n3;
-        const bool pk = a.fz.kind == XF_GATHER_P;
-        const C sa = a.fz.scalar(rhs, a.fz.off_a);
-        const C sb = pk ? a.fz.scalar(rhs, a.fz.off_b) : czero<C>();
-        const bool first = pk && *reinterpret_cast<const int*>(a.fz.sbase + rhs * a.fz.sstride + a.fz.off_iter) == 0;
-        const C* __restrict__ fu = a.fz.u + off;
-        const C* __restrict__ fv = a.fz.v + off;
-        C* __restrict__ fw = a.fz.w + off;
+    auto fill_tables = [&] {
+      for (int i = it; i < P; i += kX2Threads) {
+        tw[i] = to_compute<K>(__ldg(a.twP + i));
+        const int k2 = i / R1, m1 = i - k2 * R1;
+        tw2[i] = to_compute<K>(__ldg(a.twP + m1 * k2));
+      }
+    };
+    if (fused) {
+      // (only the preconditioner's forward pass folds a step, and its gather
+      // is plain: no diagonal or conjugation applies to the formed element)
+      // Every thread of the CTA forms elements of its NL lines (element e =
+      // l P + i, i < L; zeros up to P) into S in stage A's input layout
+      // [l][n1][n2] (i = n1 + R1 n2), in chunks of X2C: indices, then the
+      // solver's vectors, then the formed elements written back, so a chunk's
+      // loads are in flight together.  (Stage A's R1 NL threads alone, R2
+      // elements each, waited on twice as many rounds of dependent loads.)
+      const int64_t off = (int64_t)rhs * a.n3;
+      const bool pk = a.fz.kind == XF_GATHER_P;
+      const C sa = a.fz.scalar(rhs, a.fz.off_a);
+      const C sb = pk ? a.fz.scalar(rhs, a.fz.off_b) : czero<C>();
+      const bool first = pk && *reinterpret_cast<const int*>(a.fz.sbase + rhs * a.fz.sstride + a.fz.off_iter) == 0;
+      const C* __restrict__ fu = a.fz.u + off;
+      const C* __restrict__ fv = a.fz.v + off;
+      C* __restrict__ fw = a.fz.w + off;
+      constexpr int NE = NL * P, NCH = (NE + kX2Threads - 1) / kX2Threads;
 #pragma unroll
-        for (int c0 = 0; c0 < R2; c0 += X2C) {
-          int pos[X2C];
-          C val[X2C];
+      for (int c0 = 0; c0 < NCH; c0 += X2C) {
+        int pos[X2C], sidx[X2C];
+        C val[X2C];
 #pragma unroll
-          for (int j = 0; j < X2C; ++j) {
-            const int i = n1 + R1 * (c0 + j);
-            pos[j] = (c0 + j < R2 && i < a.L) ? __ldg(map + i) : -1;
-          }
-#pragma unroll
-          for (int j = 0; j < X2C; ++j) {
-            val[j] = czero<C>();
-            if (pos[j] >= 0) {
-              const C r = fu[pos[j]], vv = fv[pos[j]];
-              if (pk) val[j] = first ? r : cfma(sa, csub(fw[pos[j]], cmul(sb, vv)), r);
-              else val[j] = csub(r, cmul(sa, vv));
-            }
-          }
-#pragma unroll
-          for (int j = 0; j < X2C; ++j) {
-            if (c0 + j < R2) v[c0 + j] = to_compute<K>(val[j]);
-            if (pos[j] >= 0) {
-              fw[pos[j]] = val[j];
-              if (!pk) acc.norm2(val[j]);
-            }
+        for (int j = 0; j < X2C; ++j) {
+          const int e = it + kX2Threads * (c0 + j);
+          const int le = e / P, i = e - le * P, linee = line0 + le;
+          sidx[j] = (c0 + j < NCH && e < NE) ? (le * R1 + i % R1) * RS + i / R1 : -1;
+          pos[j] = -1;
+          if (sidx[j] >= 0 && i < a.L && linee < nlines) {
+            const int ce = comp_of(linee, MN), jke = linee - ce * MN;
+            pos[j] = __ldg(a.map3 + (int64_t)ce * a.V + (int64_t)jke * a.L + i);
           }
         }
-      } else {
+#pragma unroll
+        for (int j = 0; j < X2C; ++j) {
+          val[j] = czero<C>();
+          if (pos[j] >= 0) {
+            const C r = fu[pos[j]], vv = fv[pos[j]];
+            if (pk) val[j] = first ? r : cfma(sa, csub(fw[pos[j]], cmul(sb, vv)), r);
+            else val[j] = csub(r, cmul(sa, vv));
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < X2C; ++j) {
+          if (sidx[j] >= 0) S[sidx[j]] = to_compute<K>(val[j]);
+          if (pos[j] >= 0) {
+            fw[pos[j]] = val[j];
+            if (!pk) acc.norm2(val[j]);
+          }
+        }
+      }
+      fill_tables();
+      __syncthreads();
+      // each stage-A thread reads its own row, which it alone rewrites below
+      if (act) {
+        const K* s = S + (l * R1 + n1) * RS;
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2) v[n2] = s[n2];
+      }
+    } else {
+      if (act && line < nlines) {
+        const int c = comp_of(line, MN), jk = line - c * MN;
+        const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
 #pragma unroll
         for (int n2 = 0; n2 < R2; ++n2) {
           const int i = n1 + R1 * n2;
           v[n2] = i < a.L ? to_compute<K>(x2_gather(a, x, __ldg(map + i), mode)) : czero<K>();
         }
-      }
-    } else {
+      } else {
 #pragma unroll
-      for (int n2 = 0; n2 < R2; ++n2) v[n2] = czero<K>();
+        for (int n2 = 0; n2 < R2; ++n2) v[n2] = czero<K>();
+      }
+      fill_tables();
+      __syncthreads();
     }
-    for (int i = it; i < P; i += kX2Threads) {
-      tw[i] = to_compute<K>(__ldg(a.twP + i));
-      const int k2 = i / R1, m1 = i - k2 * R1;
-      tw2[i] = to_compute<K>(__ldg(a.twP + m1 * k2));
-    }
-    __syncthreads();
     if (act) {
       reg_dft<R2, R2, 1, R1, false, K>(v, tw);
       K* s = S + (l * R1 + n1) * RS;
@@ -175,8 +196,8 @@ __global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && 
     }
     // With a folded inner product, the solver vector read at the scatter (rt
     // or s) was last touched an iteration or a preconditioner apply ago and is
-    // mostly out of L2: each thread prefetches it (and the input) into L2 at
-    // the unknowns its stage-A' item will write, so the latency overlaps the
+    // mostly out of L2: the stage-A' threads prefetch it (and the input) into
+    // L2 at the unknowns of the CTA's lines, so the latency overlaps the
     // first DFT stage instead of the scatter.
     if (a.fz.kind == XF_SCATTER_DOT || a.fz.kind == XF_SCATTER_OMEGA) {
       const int pn1 = it % R1, pla = it / R1, pline = line0 + pla;
@@ -210,43 +231,74 @@ __global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && 
     }
     __syncthreads();
     const int n1 = it % R1, la = it / R1, linea = line0 + la;
-    Acc<T> acc, acc2;
-    const int fk = a.fz.kind;
+    constexpr int NO = HO ? lower_half_n2(R1, R2) : R2;  // outputs formed per row
+    // stage A' by R1 NL threads: the row's outputs i = n1 + R1 n2 back into
+    // its own row of S
     if (it < R1 * NL && linea < nlines && n1 < a.L) {
       K v[R2];
-      const K* s = S + (la * R1 + n1) * RS;
+      K* s = S + (la * R1 + n1) * RS;
 #pragma unroll
       for (int j2 = 0; j2 < R2; ++j2) v[j2] = s[j2];
       reg_dft<R2, R2, 1, R1, true, K>(v, tw);
-      const int c = comp_of(linea, MN), jk = linea - c * MN;
-      const int* map = a.map3 + (int64_t)c * a.V + (int64_t)jk * a.L;
-      // the output never aliases the input or the solver's vectors: with the
-      // pointers restrict-qualified the next element's loads need not wait
-      // for this element's store
-      const C* __restrict__ xr = x;
-      C* __restrict__ yr = y;
-      const C* __restrict__ fu = fk != XF_NONE ? a.fz.u + (int64_t)rhs * a.n3 : nullptr;
 #pragma unroll
-      for (int n2 = 0; n2 < (HO ? lower_half_n2(R1, R2) : R2); ++n2) {
-        const int i = n1 + R1 * n2;
-        if (i >= a.L) continue;
-        const int p = __ldg(map + i);
+      for (int n2 = 0; n2 < NO; ++n2) s[n2] = v[n2];
+    }
+    __syncthreads();
+    // The scatter, by every thread of the CTA: element e = l IH + i of its NL
+    // lines (outputs i < L; IH bounds the formed outputs), in chunks of X2C
+    // (indices, then the inputs, then the outputs).  (Stage A''s R1 NL
+    // threads alone, R2 outputs each, waited on more rounds of dependent
+    // loads.)
+    constexpr int IH = (R1 * NO < P) ? R1 * NO : P;
+    constexpr int NE = NL * IH, NCH = (NE + kX2Threads - 1) / kX2Threads;
+    Acc<T> acc, acc2;
+    const int fk = a.fz.kind;
+    // the output never aliases the input or the solver's vectors: with the
+    // pointers restrict-qualified a chunk's loads need not wait for the
+    // previous chunk's stores
+    const C* __restrict__ xr = x;
+    C* __restrict__ yr = y;
+    const C* __restrict__ fu = fk != XF_NONE ? a.fz.u + (int64_t)rhs * a.n3 : nullptr;
+#pragma unroll
+    for (int c0 = 0; c0 < NCH; c0 += X2C) {
+      int pos[X2C], sidx[X2C];
+#pragma unroll
+      for (int j = 0; j < X2C; ++j) {
+        const int e = it + kX2Threads * (c0 + j);
+        const int le = e / IH, i = e - le * IH, linee = line0 + le;
+        pos[j] = -1;
+        sidx[j] = (le * R1 + i % R1) * RS + i / R1;
+        if (c0 + j < NCH && e < NE && i < a.L && linee < nlines) {
+          const int ce = comp_of(linee, MN), jke = linee - ce * MN;
+          pos[j] = __ldg(a.map3 + (int64_t)ce * a.V + (int64_t)jke * a.L + i);
+        }
+      }
+      C xv[X2C], fv[X2C];
+#pragma unroll
+      for (int j = 0; j < X2C; ++j) {
+        if (pos[j] >= 0) {
+          if (mode != MODE_PLAIN) xv[j] = xr[pos[j]];
+          if (fk != XF_NONE) fv[j] = fu[pos[j]];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < X2C; ++j) {
+        const int p = pos[j];
         if (p < 0) continue;
-        const C conv = to_storage(v[n2], C{});
+        const C conv = to_storage(S[sidx[j]], C{});
         C out;
         if (mode == MODE_PLAIN) {
           out = conv;
         } else {
-          const C xv = xr[p];
-          if (mode == VS_NOTRANSP) out = csub(cmul(diag_term(a, p, rhs, false), xv), cmul(a.d2.at(p), conv));
-          else if (mode == VS_TRANSP) out = csub(cmul(diag_term(a, p, rhs, false), xv), conv);
-          else out = csub(cmul(diag_term(a, p, rhs, true), xv), cconj(conv));
+          if (mode == VS_NOTRANSP) out = csub(cmul(diag_term(a, p, rhs, false), xv[j]), cmul(a.d2.at(p), conv));
+          else if (mode == VS_TRANSP) out = csub(cmul(diag_term(a, p, rhs, false), xv[j]), conv);
+          else out = csub(cmul(diag_term(a, p, rhs, true), xv[j]), cconj(conv));
         }
         yr[p] = out;
         if (fk == XF_SCATTER_DOT) {
-          acc.dot(fu[p], out);  // rt^H v
+          acc.dot(fv[j], out);  // rt^H v
         } else if (fk == XF_SCATTER_OMEGA) {
-          acc.dot(out, fu[p]);  // t^H s
+          acc.dot(out, fv[j]);  // t^H s
           acc2.norm2(out);      // t^H t
         }
       }
