@@ -31,7 +31,7 @@
 namespace vs {
 
 constexpr int kX2Threads = 256;
-constexpr int X2C = 4;  // elements per chunk of the folded gather
+constexpr int X2C = 4;  // elements per chunk of the cooperative gather and scatter
 
 template <typename T>
 __device__ __forceinline__ cplx_t<T> x2_gather(const PipeArgs<T>& a, const cplx_t<T>* x, int pos, int mode) {
