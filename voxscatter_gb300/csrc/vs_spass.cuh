@@ -36,8 +36,10 @@ constexpr int s2_tx() {
   return tx;
 }
 
-// HO (inverse only): n_out <= (R1 R2 + 1) / 2, so the outputs n2 >=
-// lower_half_n2 are never stored and never formed.
+// HO, inverse: n_out <= (R1 R2 + 1) / 2, so the outputs n2 >= lower_half_n2
+// are never stored and never formed; forward (c64): n_in <= (R1 R2 + 1) / 2,
+// so the inputs n2 >= lower_half_n2 are zeros the compiler folds out of the
+// first DFT stage (the matvec's y pass has Q >= 2M - 1).
 template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>, bool HO = false>
 __global__ void __launch_bounds__(z2_threads(R2, s2_tx<T, R2>())) k_s2(StridedArgs<T> a) {
   using C = cplx_t<T>;  // storage
@@ -62,7 +64,8 @@ __global__ void __launch_bounds__(z2_threads(R2, s2_tx<T, R2>())) k_s2(StridedAr
 #pragma unroll
       for (int n2 = 0; n2 < R2; ++n2) {
         const int row = n1 + R1 * n2;
-        v[n2] = (xin && row < a.n_in) ? to_compute<K>(src[row * a.s_row + x]) : czero<K>();
+        v[n2] = ((!HO || n2 < lower_half_n2(R1, R2)) && xin && row < a.n_in) ? to_compute<K>(src[row * a.s_row + x])
+                                                                              : czero<K>();
       }
       reg_dft<R2, R2, 1, R1, false, K>(v, tw);
       K* s = S + (n1 * R2) * TX + xl;
@@ -124,10 +127,13 @@ template <typename T, int R1, int R2, bool INV, typename K = cplx_t<T>>
 static void launch_s2(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream_t st) {
   constexpr int TX = s2_tx<T, R2>(), NT = z2_threads(R2, TX);
   const size_t smem = (size_t)(R1 * R2 * TX + R1 * R2) * sizeof(cplx_t<T>);
-  // the matvec's inverse y pass keeps at most half the line (Q >= 2M - 1)
+  // the matvec's y passes read (forward) and keep (inverse) at most half the
+  // line (Q >= 2M - 1)
   auto k = k_s2<T, R1, R2, INV, K>;
   if constexpr (INV) {
     if (2 * a.n_out - 1 <= R1 * R2) k = k_s2<T, R1, R2, INV, K, true>;
+  } else if constexpr (std::is_same<T, float>::value) {
+    if (2 * a.n_in - 1 <= R1 * R2) k = k_s2<T, R1, R2, INV, K, true>;
   }
   set_kernel_smem((const void*)k, smem);
   k<<<dim3(ceil_div(a.xext, TX), nplanes, nrhs), NT, smem, st>>>(a);
