@@ -1532,6 +1532,66 @@ namespace vs {
 
 constexpr int kDotChunk = 4096;  // elements per CTA of the batched dots
 
+// A complex chunk partial in its 16-byte slot: the float-float real and
+// imaginary parts as float4 (hi, lo, hi, lo) for c64, a double2 for c128.
+// The c64 sums stay on the FP32 pipes until one thread widens the total
+// (GB300 runs FP64 at a small fraction of its FP32 rate).
+__device__ __forceinline__ void put_cslot(double2* p, FF2 re, FF2 im) {
+  *reinterpret_cast<float4*>(p) = make_float4(re.hi, re.lo, im.hi, im.lo);
+}
+__device__ __forceinline__ void put_cslot(double2* p, double re, double im) { *p = make_double2(re, im); }
+__device__ __forceinline__ void get_cslot(const double2* p, FF2& re, FF2& im) {
+  const float4 f = *reinterpret_cast<const float4*>(p);
+  re = FF2{f.x, f.y};
+  im = FF2{f.z, f.w};
+}
+__device__ __forceinline__ void get_cslot(const double2* p, double& re, double& im) {
+  const double2 d = *p;
+  re = d.x;
+  im = d.y;
+}
+// CTA sum of one complex value per thread (blockDim.x <= 256): warp trees,
+// then thread 0 adds the warps in order; the total in thread 0.
+template <typename V>
+__device__ __forceinline__ void cta_csum(V& re, V& im) {
+  __shared__ V sre[8], sim[8];
+  re = warp_sum_v(re);
+  im = warp_sum_v(im);
+  if ((threadIdx.x & 31) == 0) {
+    sre[threadIdx.x >> 5] = re;
+    sim[threadIdx.x >> 5] = im;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    re = sre[0];
+    im = sim[0];
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+      add_slot(re, sre[k]);
+      add_slot(im, sim[k]);
+    }
+  }
+}
+// Per-thread x^H y over [i0, i1) with stride blockDim.x, four elements'
+// loads issued together.
+template <typename T>
+__device__ __forceinline__ void chunk_dot(const cplx_t<T>* __restrict__ x, const cplx_t<T>* __restrict__ y,
+                                          int64_t i0, int64_t i1, Acc<T>& a) {
+  using C = cplx_t<T>;
+  const int64_t st = blockDim.x;
+  for (int64_t b = i0 + threadIdx.x; b < i1; b += 4 * st) {
+    C u[4], v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (b + k * st < i1) {
+        u[k] = x[b + k * st];
+        v[k] = y[b + k * st];
+      }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (b + k * st < i1) a.dot(u[k], v[k]);
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_gm_dots(const cplx_t<T>* __restrict__ V, const cplx_t<T>* __restrict__ w,
                                                  int64_t n, double2* __restrict__ part, int nchunk,
@@ -1542,42 +1602,38 @@ __global__ void __launch_bounds__(256) k_gm_dots(const cplx_t<T>* __restrict__ V
   const int64_t i0 = (int64_t)blockIdx.x * kDotChunk;
   const int64_t i1 = (n < i0 + kDotChunk) ? n : i0 + kDotChunk;
   Acc<T> a;
-  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) a.dot(v[i], w[i]);
-  __shared__ double sre[8], sim[8];
-  double re = a.value().x, im = a.value().y;
-  for (int off = 16; off; off >>= 1) {
-    re += __shfl_xor_sync(0xffffffffu, re, off);
-    im += __shfl_xor_sync(0xffffffffu, im, off);
+  chunk_dot<T>(v, w, i0, i1, a);
+  SlotV<T> re = a.vre(), im = a.vim();
+  cta_csum(re, im);
+  if (threadIdx.x == 0) put_cslot(part + (int64_t)j * nchunk + blockIdx.x, re, im);
+}
+
+// Sum of the nchunk complex slots at part (one CTA), widened to double in thread 0.
+template <typename T>
+__device__ __forceinline__ double2 sum_cslots(const double2* __restrict__ part, int nchunk) {
+  using V = SlotV<T>;
+  V r{}, q{};
+  for (int c = threadIdx.x; c < nchunk; c += blockDim.x) {
+    V a, b;
+    get_cslot(part + c, a, b);
+    add_slot(r, a);
+    add_slot(q, b);
   }
-  if ((threadIdx.x & 31) == 0) { sre[threadIdx.x >> 5] = re; sim[threadIdx.x >> 5] = im; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double r = 0, q = 0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { r += sre[k]; q += sim[k]; }
-    part[(int64_t)j * nchunk + blockIdx.x] = make_double2(r, q);
-  }
+  cta_csum(r, q);
+  return threadIdx.x == 0 ? make_double2(widen(r), widen(q)) : make_double2(0, 0);
 }
 
 // hp[j] = sum of the partials of vector j; H(:,k) += hp (column k of the Hessenberg)
+template <typename T>
 __global__ void k_gm_dots_final(const double2* __restrict__ part, int nchunk, double2* __restrict__ hp,
                                 double2* __restrict__ Hcol, GState* st) {
   if (st->skip) return;
   const int j = blockIdx.x;
-  double r = 0, q = 0;
-  for (int c = threadIdx.x; c < nchunk; c += blockDim.x) { r += part[(int64_t)j * nchunk + c].x; q += part[(int64_t)j * nchunk + c].y; }
-  for (int off = 16; off; off >>= 1) {
-    r += __shfl_xor_sync(0xffffffffu, r, off);
-    q += __shfl_xor_sync(0xffffffffu, q, off);
-  }
-  __shared__ double sr[8], sq[8];
-  if ((threadIdx.x & 31) == 0) { sr[threadIdx.x >> 5] = r; sq[threadIdx.x >> 5] = q; }
-  __syncthreads();
+  const double2 t = sum_cslots<T>(part + (int64_t)j * nchunk, nchunk);
   if (threadIdx.x == 0) {
-    double a = 0, b = 0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { a += sr[k]; b += sq[k]; }
-    hp[j] = make_double2(a, b);
-    Hcol[j].x += a;
-    Hcol[j].y += b;
+    hp[j] = t;
+    Hcol[j].x += t.x;
+    Hcol[j].y += t.y;
   }
 }
 
@@ -1613,13 +1669,18 @@ __global__ void __launch_bounds__(kRedThreads) k_gm_norm(const cplx_t<T>* w, int
   if (grid_reduce<1>(v, partials, counter, t) && threadIdx.x == 0) *Hk1 = make_double2(sqrt(t[0]), 0.0);
 }
 
-// V_{k+1} = w / H(k+1,k)
+// V_{k+1} = w / H(k+1,k) (the reciprocal taken once per CTA)
 template <typename T>
 __global__ void k_gm_scale(const cplx_t<T>* __restrict__ w, cplx_t<T>* __restrict__ vnext, int64_t n,
                            const double2* Hk1, const GState* st) {
   if (st->skip) return;
-  const double h = Hk1->x;
-  const T s = (T)(h > 0 ? 1.0 / h : 0.0);
+  __shared__ T s_s;
+  if (threadIdx.x == 0) {
+    const double h = Hk1->x;
+    s_s = (T)(h > 0 ? 1.0 / h : 0.0);
+  }
+  __syncthreads();
+  const T s = s_s;
   GRID_LOOP(i, n) vnext[i] = cscale(w[i], s);
 }
 
@@ -1711,8 +1772,13 @@ __global__ void k_sub(const cplx_t<T>* __restrict__ a, const cplx_t<T>* __restri
 
 template <typename T>
 __global__ void k_scale_by(const cplx_t<T>* __restrict__ a, cplx_t<T>* __restrict__ o, int64_t n, const double* nrm) {
-  const double h = *nrm;
-  const T s = (T)(h > 0 ? 1.0 / h : 0.0);
+  __shared__ T s_s;
+  if (threadIdx.x == 0) {
+    const double h = *nrm;
+    s_s = (T)(h > 0 ? 1.0 / h : 0.0);
+  }
+  __syncthreads();
+  const T s = s_s;
   GRID_LOOP(i, n) o[i] = cscale(a[i], s);
 }
 
@@ -1820,7 +1886,7 @@ static int gmres_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_t
       double2* Hcol = H + (int64_t)k * (m + 1);
       for (int pass = 0; pass < 2; ++pass) {
         k_gm_dots<T><<<dim3(nchunk, k + 1), 256, 0, st>>>(V, wv, n, part, nchunk, gs);
-        k_gm_dots_final<<<k + 1, 256, 0, st>>>(part, nchunk, hp, Hcol, gs);
+        k_gm_dots_final<T><<<k + 1, 256, 0, st>>>(part, nchunk, hp, Hcol, gs);
         k_gm_axpy<T><<<g, 256, (k + 1) * sizeof(C), st>>>(V, wv, n, k + 1, hp, gs);
       }
       // partial sums and counter of the shared reduction state (device addresses)
@@ -1909,55 +1975,19 @@ __global__ void __launch_bounds__(256) k_dr_gram(const cplx_t<T>* __restrict__ X
   const int64_t i0 = (int64_t)blockIdx.x * kDotChunk;
   const int64_t i1 = (n < i0 + kDotChunk) ? n : i0 + kDotChunk;
   Acc<T> a;
-  for (int64_t e = i0 + threadIdx.x; e < i1; e += blockDim.x) a.dot(x[e], y[e]);
-  __shared__ double sre[8], sim[8];
-  double re = a.value().x, im = a.value().y;
-  for (int off = 16; off; off >>= 1) {
-    re += __shfl_xor_sync(0xffffffffu, re, off);
-    im += __shfl_xor_sync(0xffffffffu, im, off);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    sre[threadIdx.x >> 5] = re;
-    sim[threadIdx.x >> 5] = im;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double r = 0, q = 0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-      r += sre[k];
-      q += sim[k];
-    }
-    part[((int64_t)i * gridDim.z + j) * nchunk + blockIdx.x] = make_double2(r, q);
-  }
+  chunk_dot<T>(x, y, i0, i1, a);
+  SlotV<T> re = a.vre(), im = a.vim();
+  cta_csum(re, im);
+  if (threadIdx.x == 0) put_cslot(part + ((int64_t)i * gridDim.z + j) * nchunk + blockIdx.x, re, im);
 }
 
 // G(i, j) (column-major, nx rows) = sum of the chunk partials of pair (i, j);
 // one CTA per pair, block b = i * ny + j.
+template <typename T>
 __global__ void k_dr_gram_final(const double2* __restrict__ part, int nchunk, int nx, int ny, double2* __restrict__ G) {
   const int b = blockIdx.x, i = b / ny, j = b - i * ny;
-  double r = 0, q = 0;
-  for (int c = threadIdx.x; c < nchunk; c += blockDim.x) {
-    r += part[(int64_t)b * nchunk + c].x;
-    q += part[(int64_t)b * nchunk + c].y;
-  }
-  for (int off = 16; off; off >>= 1) {
-    r += __shfl_xor_sync(0xffffffffu, r, off);
-    q += __shfl_xor_sync(0xffffffffu, q, off);
-  }
-  __shared__ double sr[8], sq[8];
-  if ((threadIdx.x & 31) == 0) {
-    sr[threadIdx.x >> 5] = r;
-    sq[threadIdx.x >> 5] = q;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double a = 0, c2 = 0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-      a += sr[k];
-      c2 += sq[k];
-    }
-    G[i + (int64_t)j * nx] = make_double2(a, c2);
-  }
+  const double2 t = sum_cslots<T>(part + (int64_t)b * nchunk, nchunk);
+  if (threadIdx.x == 0) G[i + (int64_t)j * nx] = t;
 }
 
 // out_c = (accumulate ? out_c : 0) + sum_j X_j coef(j, c) for c < ncol, with
@@ -2014,7 +2044,7 @@ static std::vector<cd> dr_gram(KrylovWork& w, const cplx_t<T>* Xa, int na, const
   w.rgpart.alloc((size_t)nx * ny * nchunk * sizeof(double2));
   w.rgram.alloc((size_t)nx * ny * sizeof(double2));
   k_dr_gram<T><<<dim3(nchunk, nx, ny), 256, 0, st>>>(Xa, na, nb ? Xb : Xa, Y, n, w.rgpart.as<double2>(), nchunk);
-  k_dr_gram_final<<<nx * ny, 256, 0, st>>>(w.rgpart.as<double2>(), nchunk, nx, ny, w.rgram.as<double2>());
+  k_dr_gram_final<T><<<nx * ny, 256, 0, st>>>(w.rgpart.as<double2>(), nchunk, nx, ny, w.rgram.as<double2>());
   VS_LAUNCH_CHECK();
   *launches += 2;
   std::vector<double2> h((size_t)nx * ny);
@@ -2157,7 +2187,7 @@ static int gcrodr_core(const vs_op& op, const vs_prec* pr, KrylovWork& w, int64_
       const int nb = kc + k + 1;  // C_0..C_kc-1, V_0..V_k
       for (int pass = 0; pass < 2; ++pass) {
         k_gm_dots<T><<<dim3(nchunk, nb), 256, 0, st>>>(Cm, wv, n, part, nchunk, gs);
-        k_gm_dots_final<<<nb, 256, 0, st>>>(part, nchunk, hp, col, gs);
+        k_gm_dots_final<T><<<nb, 256, 0, st>>>(part, nchunk, hp, col, gs);
         k_gm_axpy<T><<<g, 256, nb * sizeof(C), st>>>(Cm, wv, n, nb, hp, gs);
       }
       double2* Hcol = col + kc;
