@@ -149,6 +149,7 @@ __global__ void __launch_bounds__(kThreads) k_strided(StridedArgs<T> a) {
   a.plane(pa, pb);
   const C* src = a.src + pa * a.s_a + pb * a.s_b + (int64_t)blockIdx.z * a.s_rhs;
   C* dst = a.dst + pa * a.d_a + pb * a.d_b + (int64_t)blockIdx.z * a.d_rhs;
+  a.prefetch_l2();
   const int xl = threadIdx.x & (tx - 1), r0 = threadIdx.x >> lg_nl;
   const int x = x0 + xl;
   const bool xin = x < a.xext;
@@ -315,6 +316,7 @@ void launch_strided_pass(const StridedArgs<T>& args, int nplanes, int nrhs, cuda
   if (a.two_level >= 1 && strided_two_level<T, INV>(a, nplanes, nrhs, st)) return;
   const int tx = 1 << a.lg_tx;
   dim3 grid(ceil_div(a.xext, tx), nplanes, nrhs);
+  if (a.pf) a.pf_per_cta = prefetch_share(a.pf_bytes, (uint64_t)grid.x * grid.y * grid.z);
   const size_t smem = (2ull * a.plan.n * tx + a.plan.n) * sizeof(cplx_t<T>);
   if (plan_is_small_radix(a.plan)) {
     auto k = k_strided<T, INV, true>;
@@ -330,7 +332,7 @@ void launch_strided_pass(const StridedArgs<T>& args, int nplanes, int nrhs, cuda
 
 template <typename T>
 static StridedArgs<T> y_pass_args(const vs_op& op, const PipeArgs<T>& a, bool inverse) {
-  StridedArgs<T> s;
+  StridedArgs<T> s{};
   const int64_t pm = (int64_t)op.P * op.M, pq = (int64_t)op.P * op.Q;
   s.src = inverse ? a.t2 : a.t1;
   s.dst = inverse ? a.t1 : a.t2;
@@ -579,7 +581,7 @@ void fft_axis0(cplx_t<T>* data, int n, int64_t nlines, const FftAxis& ax, cudaSt
 template <typename T, bool INV>
 void fft_strided(cplx_t<T>* data, int xext, int n, int64_t row_stride, int na, int64_t stride_a, int nb,
                  int64_t stride_b, const FftAxis& ax, cudaStream_t st) {
-  StridedArgs<T> s;
+  StridedArgs<T> s{};
   s.src = data; s.dst = data;
   s.xext = xext; s.n_in = n; s.n_out = n;
   s.lg_tx = ilog2(pick_tile(n, sizeof(cplx_t<T>), 1));

@@ -94,6 +94,11 @@ __device__ __forceinline__ cplx_t<T> diag_term(const PipeArgs<T>& a, int pos, in
 // plane.  Element (x, row) of plane (pa, pb) of the source is at
 //   src + pa*s_a + pb*s_b + row*s_row + x      (same form for the destination).
 // Rows [0, n_in) are loaded (zero pad up to n), rows [0, n_out) are stored.
+// Bytes per CTA of an L2 prefetch of `bytes` over `nctas` CTAs (a multiple of 16).
+inline uint64_t prefetch_share(uint64_t bytes, uint64_t nctas) {
+  return ((bytes + nctas - 1) / nctas + 15) & ~uint64_t(15);
+}
+
 template <typename T>
 struct StridedArgs {
   using C = cplx_t<T>;
@@ -109,6 +114,22 @@ struct StridedArgs {
   int two_level;  // 1: two-level register kernel (vs_spass.cuh) when the length has one;
                   // 2: the same in double-float arithmetic (FP64 data only)
   unsigned na_mul;  // ceil(2^32 / na) for na >= 2, else 0 (set by launch_strided_pass)
+  // L2 prefetch issued at the start (pf null: none): pf_bytes from pf, split
+  // over the CTAs, pf_per_cta bytes each (multiples of 16; the launcher sets
+  // pf_per_cta).  The preconditioner's forward y pass uses it for the blocks
+  // the streamed GEMV that follows reads first.
+  const void* pf;
+  uint64_t pf_bytes, pf_per_cta;
+  __device__ __forceinline__ void prefetch_l2() const {
+    if (pf == nullptr || threadIdx.x != 0) return;
+    const uint64_t id = blockIdx.x + (uint64_t)gridDim.x * (blockIdx.y + (uint64_t)gridDim.y * blockIdx.z);
+    const uint64_t off = id * pf_per_cta;
+    if (off >= pf_bytes) return;
+    const uint64_t len = pf_bytes - off < pf_per_cta ? pf_bytes - off : pf_per_cta;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(static_cast<const char*>(pf) + off),
+                 "r"((unsigned)len)
+                 : "memory");
+  }
   // plane (pa, pb) of blockIdx.y = pa + na * pb.  A division by a runtime
   // value goes through integer <-> float conversions, which GB300 runs on its
   // narrow FP64 pipe; the multiply-high by ceil(2^32 / na) is exact for

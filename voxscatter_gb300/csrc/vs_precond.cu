@@ -721,6 +721,9 @@ __device__ __forceinline__ uint64_t l2_evict_first_policy() {
 }
 
 constexpr int kGemvPolls = 1 << 20;  // default bound of every streamed-GEMV wait
+// Stored blocks per CTA of the streamed GEMV that the forward y pass before it
+// prefetches into L2 (gemv_first_bytes).
+constexpr int kGemvPrefetchBlocks = 1;
 // Each poll may suspend the waiting thread in hardware for up to this many
 // nanoseconds (it resumes when the phase completes): waiting warps then stop
 // taking issue slots from the warps that compute, and a wait still gives up
@@ -1264,6 +1267,31 @@ void pack_sym_blocks(vs_prec& pr, cudaStream_t st) {
   }
 }
 
+// Blocks of the full-block streamed GEMV that its CTAs read first (CTA c
+// starts on stored block c, and the blocks lie in order), in bytes from the
+// start of the block array; 0 when another GEMV form runs.  The forward y
+// pass that precedes the GEMV prefetches them into L2 with bulk prefetches,
+// which the y pass's idle DRAM cycles absorb: the GEMV's CTAs then start on
+// L2 hits instead of all asking HBM for their first chunk at once.
+template <typename T>
+static uint64_t gemv_first_bytes(const vs_prec& pr, const PassShape& sh, int nrhs) {
+  using C = cplx_t<T>;
+  const int n = 3 * pr.N;
+  const int rg_s = nrhs >= 4 ? 4 : 1;
+  const C* pk = std::is_same<T, float>::value ? (const C*)pr.pk32.p : (const C*)pr.pk64.p;
+  if (sh.gemv_mode == 2 && pk && pr.gemv_status.p && n <= 256) return 0;  // packed blocks
+  const bool pair = std::is_same<T, float>::value && n % 2 == 0;
+  const int want = sh.gemv_ti > 0 ? std::min(sh.gemv_ti, 4) : 2;
+  const GemvStream g = gemv_stream_geometry<T>(n, rg_s, sh.gemv_chunk, pair, want);
+  if (!(pr.sym && sh.gemv_mode != 0 && pr.gemv_status.p && n <= 192 && g.cq > 0)) return 0;
+  int dev = 0, nsm = 0;
+  VS_CUDA(cudaGetDevice(&dev));
+  VS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t nblk = (int64_t)(pr.L / 2 + 1) * (pr.M / 2 + 1);
+  const int64_t first = std::min<int64_t>(nblk, (int64_t)nsm * std::max(1, g.ctas)) * kGemvPrefetchBlocks;
+  return (uint64_t)(std::min(first, nblk) * n * n * (int64_t)sizeof(C)) & ~uint64_t(15);
+}
+
 template <typename T>
 void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nrhs, const int* skip,
                      cudaStream_t st, int pass, int skip_stride, const XFuse<T>* fz) {
@@ -1322,6 +1350,7 @@ void prec_apply_pass(const vs_prec& pr, const cplx_t<T>* x, cplx_t<T>* y, int nr
   s.two_level = sh.y_reg == 1 ? 1 : 0;
   // fused x/y planes: pass 0 does both forward FFTs, pass 4 both inverse ones
   const bool fuse = sh.fuse_xy == 1 && prec_plane_fits<T>(L, M);
+  if (pass == 1 && !fuse) s.pf_bytes = gemv_first_bytes<T>(pr, sh, nrhs), s.pf = s.pf_bytes ? inv : nullptr;
   switch (pass) {
     case 0:
       if (fuse) launch_prec_plane<T, false>(pr, x, y, nrhs, skip, skip_stride, st);

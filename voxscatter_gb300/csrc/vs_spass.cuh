@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(z2_threads(R2, s2_tx<T, R2>())) k_s2(StridedAr
   static_assert(sizeof(K) == sizeof(C), "compute and storage elements share the shared-memory layout");
   constexpr int N = R1 * R2, TX = s2_tx<T, R2>(), NT = z2_threads(R2, TX);
   if (a.skip && a.skip[blockIdx.z * a.skip_stride]) return;
+  a.prefetch_l2();
   K* S = shmem<K>();  // [R1][R2][TX]
   K* tw = S + N * TX;
   for (int i = threadIdx.x; i < N; i += NT) tw[i] = to_compute<K>(__ldg(a.tw + i));
@@ -136,7 +137,10 @@ static void launch_s2(const StridedArgs<T>& a, int nplanes, int nrhs, cudaStream
     if (2 * a.n_in - 1 <= R1 * R2) k = k_s2<T, R1, R2, INV, K, true>;
   }
   set_kernel_smem((const void*)k, smem);
-  k<<<dim3(ceil_div(a.xext, TX), nplanes, nrhs), NT, smem, st>>>(a);
+  const dim3 grid(ceil_div(a.xext, TX), nplanes, nrhs);
+  StridedArgs<T> b = a;
+  if (b.pf) b.pf_per_cta = prefetch_share(b.pf_bytes, (uint64_t)grid.x * grid.y * grid.z);
+  k<<<grid, NT, smem, st>>>(b);
   VS_LAUNCH_CHECK();
 }
 
