@@ -159,6 +159,11 @@ def _pass_bytes(p, PQR, n3, e=8, sym=True, packed=False):
     return mv, pc, pinned
 
 
+def _num_sms():
+    import torch
+    return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+
+
 def _apply_shapes(args, op, prec):
     if args.shapes:
         j = json.loads(args.shapes)
@@ -529,6 +534,17 @@ def run_ours(args):
             "ms_source": "CUDA events around one launch on the library's stream, mean of 50",
             "ms_per_launch_in_solve": dom[3],
             "traffic": _traffic_from_profiles(dom[0])}
+    if dom[0].startswith("k_block_gemv_stream"):
+        # the forward y pass before the GEMV prefetches the block every GEMV CTA
+        # starts on into L2, so those bytes reach this launch from L2: the
+        # HBM-served share of the algorithmic bytes over the same time beside it
+        sh = prec.shape("c64")
+        n = 3 * p["N"]
+        nblk = (p["L"] // 2 + 1) * (p["M"] // 2 + 1)
+        ctas = min(sh.get("gemv_blocks") or 2, 4)
+        pf = min(nblk, _num_sms() * ctas) * n * n * 8 // 16 * 16 if sh.get("gemv_mode") == 1 else 0
+        roof["l2_prefetched_bytes"] = pf
+        roof["frac_hbm_served"] = (dom[2] - pf) / (dom[1] * 1e-3) / 1e9 / peak
     per_iter = 2 * sum(in_solve) + prof["solver_kernels_per_iter"]
     in_solve_line = {
         "source": "CUDA event nodes between the launches of one solve's captured iterations "
