@@ -351,6 +351,13 @@ static StridedArgs<T> y_pass_args(const vs_op& op, const PipeArgs<T>& a, bool in
   s.skip = a.skip;
   s.skip_stride = a.skip_stride;
   s.two_level = sh.y_reg >= 1 ? sh.y_reg : 0;
+  if (!inverse) {
+    // the Green spectrum the z pass reads next, prefetched into L2 while this
+    // pass keeps DRAM mostly idle (its data sit in L2)
+    const DevBuf& g = std::is_same<T, float>::value ? op.G32 : op.G64;
+    s.pf = g.p;
+    s.pf_bytes = (uint64_t)g.bytes & ~uint64_t(15);
+  }
   return s;
 }
 
