@@ -137,7 +137,7 @@ struct StridedArgs {
   // blockIdx.y stays below 1/na).
   __device__ __forceinline__ void plane(int& pa, int& pb) const {
     const unsigned y = blockIdx.y;
-    const unsigned q = na_mul ? __umulhi(y, na_mul) : y;
+    const unsigned q = na_mul ? __umulhi(y, na_mul) : (na == 1 ? y : y / (unsigned)na);
     pb = (int)q;
     pa = (int)(y - q * (unsigned)na);
   }
