@@ -73,12 +73,6 @@ __device__ bool grid_reduce(const V (&v)[NV], double* __restrict__ partials, uns
   return true;
 }
 
-__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
-  const double d = b.x * b.x + b.y * b.y;
-  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
-}
-__device__ __forceinline__ bool cz(double2 a) { return a.x == 0.0 && a.y == 0.0; }
-__device__ __forceinline__ bool cfinite(double2 a) { return isfinite(a.x) && isfinite(a.y); }
 
 #define GRID_LOOP(i, n) for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
 
@@ -126,15 +120,16 @@ __device__ __forceinline__ void set_omega(KState* s, double2 v) { s->omega = v; 
 __device__ __forceinline__ void set_beta(KState* s, double2 v) { s->beta = v; s->beta32 = to_f2(v); }
 
 // The scalar steps of BiCGSTAB, from the grid totals (one thread):
-// alpha = rho / (rt^H v) with its breakdown test;
+// alpha = rho / (rt^H v) with its breakdown test (alpha_step);
 __device__ __forceinline__ void finish_alpha(KState* s, const double (&t)[2]) {
-  const double2 d = make_double2(t[0], t[1]);
-  if (cz(d) || !cfinite(d)) {
-    s->flag = cfinite(d) ? 4 : 5;
+  double2 al;
+  const int f = alpha_step(s->rho, t, al);
+  if (f >= 0) {
+    s->flag = f;
     s->skip = 1;
     return;
   }
-  set_alpha(s, cdiv(s->rho, d));
+  set_alpha(s, al);
 }
 // ||s|| (t = ||s||^2) and the half-step convergence test;
 __device__ __forceinline__ void finish_s(KState* s, const double (&t)[1]) {
@@ -201,16 +196,6 @@ __device__ __forceinline__ void sum_cta_partials(const double* __restrict__ part
 #pragma unroll
   for (int k = 0; k < NV; ++k) tot[k] = slot[k];
 }
-template <typename T>
-__global__ void __launch_bounds__(kFinThreads) k_fin_alpha(KState* states, const double* part, int64_t pstride,
-                                                           int nb) {
-  KState* s = states + blockIdx.x;
-  if (s->skip) return;
-  double t[2];
-  sum_cta_partials<2, SlotV<T>>(part + blockIdx.x * pstride, nb, t);
-  if (threadIdx.x == 0) finish_alpha(s, t);
-}
-
 // rho = rt^H r ; beta = (rho/rho_prev)(alpha/omega)
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) k_bicg_rho(const cplx_t<T>* __restrict__ rt,
@@ -596,19 +581,20 @@ static std::vector<double> read_scal(KrylovWork& w, int nrhs, cudaStream_t st) {
 // Events recorded by one profiled iteration (kIterMarks per iteration): 0
 // before it, 1 after the direction update, 2..6 after the five passes of the
 // first preconditioner apply, 7..11 after the matvec's five, 12 after the
-// alpha / s / half-step kernels, 13..17 and 18..22 the second apply and
-// matvec, 23 after the omega / x, r kernels; with folded steps, 24 after the
-// half-step kernel (between 13 and 14).
+// alpha / s / half-step kernels (with folded steps none: 12 follows 11),
+// 13..17 and 18..22 the second apply and matvec, 23 after the omega / x, r
+// kernels; with folded steps, 24 after the half-step kernel (between 13 and
+// 14).
 constexpr int kIterMarks = 25;
 
 // BiCGSTAB's vector steps folded into the x passes (XFuse): the
 // preconditioner's forward x pass forms p (first apply) and s with ||s||^2
 // (second apply), the matvec's inverse x pass adds rt^H v (first) and t^H s,
 // t^H t (second); the partial sums of nb_mv / nb_pr CTAs per right-hand side
-// go to part (pstride doubles each).  A one-CTA kernel takes alpha; the
-// half-step test and omega are taken by every CTA of the kernels that use
-// them (k_bicg_shalf, k_bicg_xr).  Four streaming vector kernels and two
-// scalar kernels of the iteration are gone.
+// go to part (pstride doubles each).  alpha, the half-step test and omega
+// are taken by every CTA of the kernels that use them (the second apply's
+// forward x pass, k_bicg_shalf, k_bicg_xr).  Four streaming vector kernels
+// and three scalar kernels of the iteration are gone.
 struct FoldPlan {
   int nb_mv = 0, nb_pr = 0;
   int64_t pstride = 0;
@@ -695,6 +681,14 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
     fsv.kind = XF_GATHER_S;
     fsv.off_a = c64 ? (int)offsetof(KState, alpha32) : (int)offsetof(KState, alpha);
     fsv.u = r; fsv.v = v; fsv.w = sv;
+    // alpha from the first matvec's partial sums, taken by the gather itself
+    fsv.apart = fold->part;
+    fsv.anb = fold->nb_mv;
+    fsv.off_rho = (int)offsetof(KState, rho);
+    fsv.off_alpha = (int)offsetof(KState, alpha);
+    fsv.off_flag = (int)offsetof(KState, flag);
+    fsv.off_skip = (int)offsetof(KState, skip);
+    fsv.off_counter = (int)offsetof(KState, counter);
     fd.kind = XF_SCATTER_DOT;
     fd.u = rt;
     fo.kind = XF_SCATTER_OMEGA;
@@ -706,16 +700,15 @@ static void bicg_iteration(const vs_op& op, const vs_prec* pr, KrylovWork& w, KS
       prec_apply_pass<T>(*pr, p, ph, nrhs, skip, st, pass, ss, pass == 0 ? &fp : nullptr);
       mark(2 + pass);
     }
-    // rt^H v in the matvec's inverse x pass; alpha
+    // rt^H v in the matvec's inverse x pass
     for (int pass = 0; pass < 5; ++pass) {
       matvec_pass<T>(op, ph, v, nrhs, mode, skip, st, pass, ss, rgp(w), pass == 4 ? &fd : nullptr);
       mark(7 + pass);
     }
-    k_fin_alpha<T><<<nrhs, kFinThreads, 0, st>>>(s, fold->part, fold->pstride, fold->nb_mv);
     mark(12);
-    // s = r - alpha v and ||s||^2 in the second apply's forward x pass; the
-    // half-step test (and x += alpha ph if it converged), then the rest of
-    // the apply
+    // alpha, then s = r - alpha v and ||s||^2, in the second apply's forward
+    // x pass; the half-step test (and x += alpha ph if it converged), then
+    // the rest of the apply
     prec_apply_pass<T>(*pr, sv, sh, nrhs, skip, st, 0, ss, &fsv);
     mark(13);
     k_bicg_shalf<T><<<gr, kRedThreads, 0, st>>>(x, ph, n, s, fold->part, fold->pstride, fold->nb_pr);
@@ -766,11 +759,11 @@ static void add_iteration_profile(const cudaEvent_t* ev, int iters, SolveProfile
 
 // Kernels in one bicg_iteration: 6 solver kernels, 2 matvecs of 5 passes, and
 // 2 preconditioner applies (or 2 copies without preconditioner); with folded
-// steps 3 solver kernels (alpha; the half-step test with x after a converged
-// half step; omega with x and r) and 20 passes.
+// steps 2 solver kernels (the half-step test with x after a converged half
+// step; omega with x and r) and 20 passes.
 template <typename T>
 static int kernels_per_iteration(const vs_prec* pr, bool folded = false) {
-  return folded ? 23 : 6 + 10 + (pr ? 2 * prec_launches<T>(*pr) : 2);
+  return folded ? 22 : 6 + 10 + (pr ? 2 * prec_launches<T>(*pr) : 2);
 }
 
 // BiCGSTAB on w.x (initial guesses already there) with initial residuals in

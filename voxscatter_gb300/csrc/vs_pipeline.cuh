@@ -40,6 +40,16 @@ struct XFuse {
   C* w;                        // p (XF_GATHER_P, read and written), s (XF_GATHER_S, written)
   double* part;
   int64_t pstride;
+  // XF_GATHER_S with apart set: alpha = rho / (rt^H v) is taken by the pass
+  // itself from the matvec's partial sums at apart + r * pstride (anb CTAs, 2
+  // slots each), every CTA adding them in the same order (the same bits) and
+  // its thread 0 dividing; CTA 0 stores alpha (FP64 at off_alpha, storage
+  // precision at off_a) for the later steps.  A breakdown ends the iteration:
+  // every CTA returns before touching a vector, and the last to count in on
+  // the counter at off_counter writes the flag and the skip flag.
+  const double* apart;
+  int anb;
+  int off_rho, off_alpha, off_flag, off_skip, off_counter;
   __device__ __forceinline__ C scalar(int rhs, int off) const {
     return *reinterpret_cast<const C*>(sbase + rhs * sstride + off);
   }

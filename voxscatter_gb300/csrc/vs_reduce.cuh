@@ -231,4 +231,21 @@ __device__ __forceinline__ void cta_partials(const double (&v)[NV], double* out)
   }
 }
 
+// Complex FP64 scalars of the solver steps (one thread).
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  const double d = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+__device__ __forceinline__ bool cz(double2 a) { return a.x == 0.0 && a.y == 0.0; }
+__device__ __forceinline__ bool cfinite(double2 a) { return isfinite(a.x) && isfinite(a.y); }
+// BiCGSTAB's alpha = rho / (rt^H v) (t = rt^H v as re, im) with its breakdown
+// test: the flag that ends the iteration (4 breakdown, 5 not finite), or -1
+// and alpha in al.
+__device__ __forceinline__ int alpha_step(double2 rho, const double (&t)[2], double2& al) {
+  const double2 d = make_double2(t[0], t[1]);
+  if (cz(d) || !cfinite(d)) return cfinite(d) ? 4 : 5;
+  al = cdiv(rho, d);
+  return -1;
+}
+
 }  // namespace vs

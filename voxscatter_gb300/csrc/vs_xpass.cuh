@@ -43,6 +43,56 @@ __device__ __forceinline__ cplx_t<T> x2_gather(const PipeArgs<T>& a, const cplx_
   return v;
 }
 
+// The folded gather's alpha step (XFuse::apart): every CTA adds the
+// matvec's partial sums of rt^H v in the same order and its thread 0 forms
+// alpha = rho / (rt^H v) and the breakdown test; false (every thread) on a
+// breakdown, after the last CTA to count in has written the flags.
+template <typename T>
+__device__ __noinline__ bool x2_alpha_step(const XFuse<T>& f, int rhs, cplx_t<T>& sa) {
+  using C = cplx_t<T>;
+  __shared__ double tot[2];
+  __shared__ C s_al;
+  __shared__ int s_flag;
+  SlotV<T> x[2];
+  slot_sums<2, 4, false>(f.apart + rhs * f.pstride, f.anb, (int)threadIdx.x, (int)blockDim.x, x);
+  cta_partials<2>(x, tot);  // thread 0 writes the CTA's sums in slot form
+  char* st = const_cast<char*>(f.sbase) + rhs * f.sstride;
+  if (threadIdx.x == 0) {
+    double t[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      SlotV<T> y;
+      get_slot<false>(tot + k, y);
+      t[k] = widen(y);
+    }
+    double2 al = make_double2(0.0, 0.0);
+    s_flag = alpha_step(*reinterpret_cast<const double2*>(st + f.off_rho), t, al);
+    C c;
+    c.x = (decltype(c.x))al.x;
+    c.y = (decltype(c.y))al.y;
+    s_al = c;
+    if (s_flag < 0 && blockIdx.x == 0) {
+      *reinterpret_cast<double2*>(st + f.off_alpha) = al;
+      *reinterpret_cast<C*>(st + f.off_a) = c;
+    }
+  }
+  __syncthreads();
+  if (s_flag >= 0) {
+    if (threadIdx.x == 0) {
+      __threadfence();
+      unsigned* counter = reinterpret_cast<unsigned*>(st + f.off_counter);
+      if (atomicAdd(counter, 1u) == gridDim.x - 1) {
+        *reinterpret_cast<int*>(st + f.off_flag) = s_flag;
+        *reinterpret_cast<int*>(st + f.off_skip) = 1;
+        *counter = 0;
+      }
+    }
+    return false;
+  }
+  sa = s_al;
+  return true;
+}
+
 // Component of x line `line` (< 3 MN) by two compares: a division by the
 // runtime MN goes through integer <-> float conversions, which GB300 runs on
 // its narrow FP64 pipe.
@@ -94,7 +144,12 @@ __global__ void __launch_bounds__(kX2Threads, (std::is_same<T, float>::value && 
       // elements each, waited on twice as many rounds of dependent loads.)
       const int64_t off = (int64_t)rhs * a.n3;
       const bool pk = a.fz.kind == XF_GATHER_P;
-      const C sa = a.fz.scalar(rhs, a.fz.off_a);
+      C sa;
+      if (!pk && a.fz.apart) {
+        if (!x2_alpha_step(a.fz, rhs, sa)) return;  // breakdown: no vector is touched
+      } else {
+        sa = a.fz.scalar(rhs, a.fz.off_a);
+      }
       const C sb = pk ? a.fz.scalar(rhs, a.fz.off_b) : czero<C>();
       const bool first = pk && *reinterpret_cast<const int*>(a.fz.sbase + rhs * a.fz.sstride + a.fz.off_iter) == 0;
       const C* __restrict__ fu = a.fz.u + off;
